@@ -1,0 +1,162 @@
+/*
+ * sfb_gpu.h - C ABI of the GB300 catalogue -> spherical Fourier-Bessel path.
+ *
+ * Drop-in for SuperFaB's Cat2Anlm functions.  Every array argument is a
+ * plain pointer with Julia's memory layout (column-major, 1-based indices in
+ * the reference become 0-based offsets here); no PyTorch or CUDA types appear
+ * in the signatures.  Complex outputs are interleaved (re, im) doubles, which
+ * is the memory layout of Julia's Vector{ComplexF64}.
+ *
+ * Every entry point returns an sfb_status; sfb_last_error() gives the text of
+ * the last failure on the calling thread.  Nothing is printed.  There is no
+ * CPU fallback: without a usable CUDA device every compute call fails with
+ * SFB_ECUDA.
+ */
+#ifndef SFB_GPU_H
+#define SFB_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    SFB_OK = 0,
+    SFB_EINVAL = 1,      /* bad argument (reference: ArgumentError / @assert) */
+    SFB_ENOMEM = 2,      /* device allocation failed */
+    SFB_ENONFINITE = 3,  /* non-finite input or result (reference src/cat2anlm.jl:308) */
+    SFB_ERANGE = 4,      /* theta outside [0, pi] or lmax > 4*nside (reference src/healpix_helpers.jl:51-54) */
+    SFB_ETIMEOUT = 5,    /* a bounded device wait gave up */
+    SFB_ECUDA = 6,       /* CUDA runtime error (no device, launch failure) */
+    SFB_ENOTSUP = 7      /* combination of options not implemented */
+} sfb_status;
+
+typedef enum {
+    SFB_FP64 = 0,        /* every stage in FP64 */
+    SFB_MIXED = 1        /* FP64 binning/tables/window term, FP32 ring FFT, tensor-core contractions */
+} sfb_precision;
+
+typedef enum {
+    /* Galaxy radii enter through a piecewise-Legendre expansion of every
+     * g_nl spline (projection error below radial_tol); the spherical-harmonic
+     * transforms run once per radial basis function. */
+    SFB_RADIAL_POLY = 0,
+    /* Every galaxy evaluates every g_nl spline, one map per (n,l) as in the
+     * reference loop (src/cat2anlm.jl:278-306).  Cost grows as N * #(n,l). */
+    SFB_RADIAL_SPLINE = 1
+} sfb_radial_mode;
+
+/* Plan description: the contents of an AnlmModes (reference src/modes.jl:92-105)
+ * plus the transform options.  All host pointers; copied at plan creation. */
+typedef struct {
+    int64_t nside;             /* HEALPix resolution of the transform */
+    int64_t lmax;              /* AnlmModes.lmax */
+    int64_t nmax;              /* AnlmModes.nmax */
+    const int64_t *lmax_n;     /* [nmax] AnlmModes.lmax_n */
+    double rmin, rmax;         /* AnlmModes.rmin / rmax */
+    /* Cubic splines of amodes.basisfunctions.gnl[n,l+1] (Splines.jl Spline1D{3}:
+     * fields x, y, ypp) for every pair (n,l), l <= lmax_n[n], in the a_nlm block
+     * order (n slowest, then l).  Spline p occupies [spl_offset[p], spl_offset[p+1]). */
+    const int64_t *spl_offset; /* [npairs + 1] */
+    const double *spl_x;
+    const double *spl_y;
+    const double *spl_ypp;
+    int32_t niter;             /* map2alm refinement iterations (3 in mymap2alm!) */
+    int32_t precision;         /* sfb_precision */
+    int32_t radial_mode;       /* sfb_radial_mode */
+    int32_t radial_pieces;     /* SFB_RADIAL_POLY: number of pieces, 0 = automatic */
+    int32_t radial_degree;     /* SFB_RADIAL_POLY: Legendre degree per piece, 0 = automatic */
+    double radial_tol;         /* SFB_RADIAL_POLY: max |g - expansion| / max|g|, 0 = 1e-11 */
+} sfb_plan_desc;
+
+/* win_rhat_ln argument of cat2amln (reference src/windows.jl:244-270). */
+typedef enum {
+    SFB_WINDOW_ZERO = 0,       /* all-zero window term */
+    SFB_WINDOW_SEPARABLE = 1,  /* SeparableArray(mask[npix], W_ln[lmax+1, nmax]) */
+    SFB_WINDOW_DENSE = 2       /* Array W[npix, lmax+1, nmax] (column-major) */
+} sfb_window_kind;
+
+typedef struct {
+    int32_t kind;              /* sfb_window_kind */
+    const double *mask;        /* [npix] RING order (separable) */
+    const double *w_ln;        /* [(lmax+1) * nmax], element (l,n) at l + (lmax+1)*(n-1) */
+    const double *dense;       /* [npix * (lmax+1) * nmax], element (p,l,n) at p + npix*(l + (lmax+1)*(n-1)) */
+} sfb_window;
+
+typedef struct sfb_plan sfb_plan;
+
+typedef struct {
+    int64_t npix;
+    int64_t nlmsize;           /* getnlmsize(amodes), reference src/modes.jl:183-189 */
+    int64_t npairs;            /* number of (n,l) pairs */
+    int64_t nbasis;            /* radial basis functions (maps per catalogue SHT) */
+    int32_t radial_pieces;
+    int32_t radial_degree;
+    double radial_error;       /* measured max projection error / max|g| (poly mode) */
+    int64_t device_bytes;      /* device memory held by the plan */
+} sfb_plan_info;
+
+/* Create a plan on the current CUDA device.
+ * Replaces the per-call setup of cat2amln (src/cat2anlm.jl:257-276). */
+int sfb_plan_create(const sfb_plan_desc *desc, sfb_plan **plan);
+void sfb_plan_destroy(sfb_plan *plan);
+int sfb_plan_get_info(const sfb_plan *plan, sfb_plan_info *info);
+int sfb_set_precision(sfb_plan *plan, int32_t precision);
+
+/* cat2amln(rθϕ, amodes, nbar, win_rhat_ln, weight) -> a_nlm
+ * (reference src/cat2anlm.jl:257-310; alias cat2nlm :312).
+ * rtp: [3*ngal] host array, galaxy i at (r, theta, phi) = rtp[3i..3i+2]
+ * (a Julia 3xN Matrix{Float64}).  weight: [ngal] or NULL for ones.
+ * ngal may be 0 (empty catalogue).  anlm_out: [2*nlmsize] interleaved complex.
+ * Inputs are not modified. */
+int sfb_cat2amln(sfb_plan *plan, const double *rtp, const double *weight, int64_t ngal,
+                 double nbar, const sfb_window *window, double *anlm_out);
+
+/* Same as sfb_cat2amln with every pointer (rtp, weight, window arrays and
+ * anlm_out) in device memory, launched on `stream` (cudaStream_t or NULL for
+ * the legacy default stream).  Returns after the result is complete. */
+int sfb_cat2amln_device(sfb_plan *plan, const double *rtp, const double *weight, int64_t ngal,
+                        double nbar, const sfb_window *window, double *anlm_out, void *stream);
+
+/* field2anlm(f_xyz, wmodes, amodes) (reference field2anlm_v2, src/cat2anlm.jl:323-357).
+ * f: [nr * npix] host array, element (ir, p) at ir + nr*p (Julia nr x npix matrix).
+ * ConfigurationSpaceModes(rmin, rmax, nr, nside) shells (src/windows.jl:98-103). */
+int sfb_field2anlm(sfb_plan *plan, const double *f, int64_t nr, double rmin, double rmax,
+                   double *anlm_out);
+
+/* anlm2field(f_nlm, wmodes, amodes) (reference src/cat2anlm.jl:383-422).
+ * anlm: [2*nlmsize] interleaved complex; f_out: [nr * npix], element (ir,p) at ir + nr*p. */
+int sfb_anlm2field(sfb_plan *plan, const double *anlm, int64_t nr, double rmin, double rmax,
+                   double *f_out);
+
+/* win_rhat_ln for a separable window (reference src/windows.jl:260-270):
+ * W_ln[l,n] = dr * sum_r r^2 g_nl(r) phi(r).  phi: [nr]; w_ln_out: [(lmax+1)*nmax],
+ * NaN where l > lmax_n[n]. */
+int sfb_win_rhat_ln_separable(sfb_plan *plan, const double *phi, int64_t nr, double rmin,
+                              double rmax, double *w_ln_out);
+
+/* win_rhat_ln for a dense window (reference src/windows.jl:244-257).
+ * win: [nr * npix], element (ir, p) at ir + nr*p; w_out: [npix*(lmax+1)*nmax]. */
+int sfb_win_rhat_ln_dense(sfb_plan *plan, const double *win, int64_t nr, double rmin,
+                          double rmax, double *w_out);
+
+/* Batched map2alm with the plan's niter (the transform behind mymap2alm!,
+ * src/healpix_helpers.jl:50-56).  maps: [nmaps * npix], map b at b*npix.
+ * alm_out: [nmaps * 2 * lmsize], lmsize = (lmax+1)(lmax+2)/2, index l(l+1)/2+m. */
+int sfb_map2alm(sfb_plan *plan, const double *maps, int64_t nmaps, double *alm_out);
+
+/* HEALPix RING pixel (0-based; Healpix.jl ang2pixRing returns this + 1) of
+ * n directions, computed on the device with the binning kernel's arithmetic. */
+int sfb_ang2pix_ring(int64_t nside, const double *theta, const double *phi, int64_t n,
+                     int64_t *pix_out);
+
+/* Text of the last error on this thread (NUL-terminated, truncated to len). */
+int sfb_last_error(char *buf, size_t len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SFB_GPU_H */

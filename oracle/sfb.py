@@ -1,0 +1,163 @@
+"""Reference algorithms of the catalogue -> a_nlm path (TEST INFRASTRUCTURE).
+
+Every function takes plain arrays (the same tables the GPU plan receives)
+and follows one reference function:
+
+* ``spline_eval``    Spline1D{3} evaluation, src/Splines.jl:64-101,327-364
+* ``cat2amln``       src/cat2anlm.jl:257-310 (sortout :50-71, scatter :95-103)
+* ``field2anlm``     field2anlm_v2, src/cat2anlm.jl:323-357
+* ``anlm2field``     src/cat2anlm.jl:383-422
+* ``win_rhat_ln``    src/windows.jl:244-257 (dense), :260-270 (separable)
+* ``integrate_window`` src/windows.jl:219-228
+
+``modes`` arguments are dicts with ``nmax``, ``lmax``, ``lmax_n`` (list over n),
+``nside``, ``splines`` {(n, l): (x, y, ypp)} and ``noff`` (offset of each n
+block in the a_nlm vector), built by the tests from the host-side mode tables.
+"""
+
+import numpy as np
+
+from .healpix import ang2pix_ring, nside2npix
+from .sht import SHT
+
+
+def spline_eval(x, y, ypp, r):
+    """Cubic spline with boundary extrapolation (Splines.jl:64-101,327-364)."""
+    N = len(x)
+    r = np.asarray(r, float)
+    i = np.searchsorted(x, r, side="right") - 1
+    i = np.clip(i, 0, N - 2)
+    x0 = x[i]
+    h = x[i + 1] - x0
+    t = (r - x0) / h
+    h2 = h * h
+    b = h2 * ypp[i] / 2
+    a = h2 * (ypp[i + 1] - ypp[i]) / 6
+    d = y[i]
+    c = y[i + 1] - a - b - d
+    val = d + t * (c + t * (b + t * a))
+    val = np.where(r < x[0], y[0], val)
+    return np.where(r > x[-1], y[-1], val)
+
+
+def _idx0(modes, n, l, m):
+    return int(modes["noff"][n - 1]) + l * (l + 1) // 2 + m
+
+
+def nlmsize(modes):
+    return int(modes["noff"][modes["nmax"]])
+
+
+def pairs(modes):
+    return [(n, l) for n in range(1, modes["nmax"] + 1) for l in range(modes["lmax_n"][n - 1] + 1)]
+
+
+def cat2amln(rtp, modes, nbar, window, weight=None, niter=3, sht=None, pair_subset=None):
+    """a_nlm of a catalogue, reference algorithm (src/cat2anlm.jl:257-310).
+
+    rtp: (3, N) array of r, theta, phi.  window: ("dense", W[npix, lmax+1, nmax])
+    or ("separable", mask[npix], W_ln[lmax+1, nmax]).  Returns complex nlmsize.
+    ``pair_subset`` restricts the (n, l) loop (used to time a bounded sample).
+    """
+    rtp = np.asarray(rtp, float)
+    N = rtp.shape[1]
+    weight = np.ones(N) if weight is None else np.asarray(weight, float)
+    # sortout: sort by r, stable (src/cat2anlm.jl:50-71)
+    p = np.argsort(rtp[0], kind="stable")
+    r, th, ph, w = rtp[0, p], rtp[1, p], rtp[2, p], weight[p]
+    nside = modes["nside"]
+    lmax = modes["lmax"]
+    npix = nside2npix(nside)
+    dOmega = 4 * np.pi / npix
+    pix = ang2pix_ring(nside, th, ph)
+    if sht is None:
+        sht = SHT(nside, lmax)
+    if lmax > 4 * nside:
+        raise ValueError("alm.lmax > 4*nside is a poor choice")
+    anlm = np.full(nlmsize(modes), np.nan + 1j * np.nan)
+    todo = pairs(modes) if pair_subset is None else list(pair_subset)
+    chunk = 64
+    for c0 in range(0, len(todo), chunk):
+        batch = todo[c0:c0 + chunk]
+        maps = np.empty((len(batch), npix))
+        for b, (n, l) in enumerate(batch):
+            x, y, ypp = modes["splines"][(n, l)]
+            vals = w * spline_eval(x, y, ypp, r)
+            m = np.bincount(pix, weights=vals, minlength=npix).astype(float)
+            m *= 1 / (nbar * dOmega)
+            if window[0] == "dense":
+                m = m - window[1][:, l, n - 1]
+            else:
+                m = m - window[1] * window[2][l, n - 1]
+            maps[b] = m
+        alm = sht.map2alm(maps, niter=niter)
+        for b, (n, l) in enumerate(batch):
+            i0 = _idx0(modes, n, l, 0)
+            anlm[i0:i0 + l + 1] = alm[b, l, :l + 1]
+    if pair_subset is None:
+        assert np.all(np.isfinite(anlm))
+    return anlm
+
+
+def field2anlm(f, rmin, rmax, nr, modes, niter=3, sht=None):
+    """field2anlm_v2 (src/cat2anlm.jl:323-357): per-shell map2alm, radial sum."""
+    f = np.asarray(f, float)
+    dr = (rmax - rmin) / nr
+    rs = np.linspace(rmin + dr / 2, rmax - dr / 2, nr)
+    if sht is None:
+        sht = SHT(modes["nside"], modes["lmax"])
+    alm = sht.map2alm(f, niter=niter)                  # [nr, l, m]
+    out = np.zeros(nlmsize(modes), complex)
+    for (n, l) in pairs(modes):
+        x, y, ypp = modes["splines"][(n, l)]
+        g = spline_eval(x, y, ypp, rs) * rs ** 2 * dr
+        i0 = _idx0(modes, n, l, 0)
+        out[i0:i0 + l + 1] += g @ alm[:, l, :l + 1]
+    return out
+
+
+def anlm2field(fnlm, rmin, rmax, nr, modes, sht=None):
+    """anlm2field (src/cat2anlm.jl:383-422): radial sum per shell, alm2map."""
+    dr = (rmax - rmin) / nr
+    rs = np.linspace(rmin + dr / 2, rmax - dr / 2, nr)
+    L = modes["lmax"]
+    if sht is None:
+        sht = SHT(modes["nside"], L)
+    alm = np.zeros((nr, L + 1, L + 1), complex)
+    for (n, l) in pairs(modes):
+        x, y, ypp = modes["splines"][(n, l)]
+        g = spline_eval(x, y, ypp, rs)
+        i0 = _idx0(modes, n, l, 0)
+        alm[:, l, :l + 1] += g[:, None] * fnlm[None, i0:i0 + l + 1]
+    return sht.synthesis(alm)
+
+
+def win_rhat_ln_dense(win, rmin, rmax, nr, modes):
+    """W[p, l, n] = dr sum_r win[r, p] r^2 g_nl(r) (src/windows.jl:244-257); NaN off-mode."""
+    dr = (rmax - rmin) / nr
+    rs = np.linspace(rmin + dr / 2, rmax - dr / 2, nr)
+    npix = win.shape[1]
+    W = np.full((npix, modes["lmax"] + 1, modes["nmax"]), np.nan)
+    for (n, l) in pairs(modes):
+        x, y, ypp = modes["splines"][(n, l)]
+        W[:, l, n - 1] = win.T @ (rs ** 2 * spline_eval(x, y, ypp, rs))
+    return W * dr
+
+
+def win_rhat_ln_separable(phi, mask, rmin, rmax, nr, modes):
+    """W_ln[l, n] = dr sum_r r^2 g_nl(r) phi(r) (src/windows.jl:260-270)."""
+    dr = (rmax - rmin) / nr
+    rs = np.linspace(rmin + dr / 2, rmax - dr / 2, nr)
+    W = np.full((modes["lmax"] + 1, modes["nmax"]), np.nan)
+    for (n, l) in pairs(modes):
+        x, y, ypp = modes["splines"][(n, l)]
+        W[l, n - 1] = dr * np.sum(rs ** 2 * spline_eval(x, y, ypp, rs) * phi)
+    return mask, W
+
+
+def integrate_window(win, rmin, rmax, nr):
+    """V_eff = dr dOmega sum_r r^2 sum_p W[r, p] (src/windows.jl:219-228)."""
+    dr = (rmax - rmin) / nr
+    rs = np.linspace(rmin + dr / 2, rmax - dr / 2, nr)
+    npix = win.shape[1]
+    return dr * (4 * np.pi / npix) * np.sum(win.sum(axis=1) * rs ** 2)

@@ -1,0 +1,207 @@
+// Legendre contractions (FP64) and the refinement residual.
+//
+// Analysis, per m and parity p of l - m:
+//   A[l(l+1)/2 + m][c] (+)= sum_r lambda[m][p][li][r] * F[p][m][r][c],  l = m + p + 2 li
+// where F[0] = F_north + F_south and F[1] = F_north - F_south (north/south
+// symmetry lambda_lm(pi - theta) = (-1)^{l+m} lambda_lm(theta)), so the ring
+// sum runs over the 2*nside north rings only.
+// Synthesis is the transpose: G[p][m][r][c] = sum_li lambda[m][p][li][r] A[l(li)][c].
+// The refinement of map2alm (niter Jacobi steps, reference
+// src/healpix_helpers.jl:50-56) is done in ring-Fourier space:
+//   R = F - w * nph * cfold * Fold(G)
+// where Fold sums the synthesised coefficients that alias onto each m on a
+// ring of nph pixels (exactly what the ring FFT of the synthesised map sees).
+#include "sfb_internal.h"
+
+namespace sfb {
+
+namespace {
+constexpr int BM = 64, BN = 64, BK = 16;
+
+__device__ __forceinline__ int nrows_of(int m, int par, int lmax) {
+    return (m + par <= lmax) ? (lmax - m - par) / 2 + 1 : 0;
+}
+}  // namespace
+
+__global__ void __launch_bounds__(256) k_leg_analysis(const double *__restrict__ lam, const int64_t *lam_off,
+                                                      int lmax, int nrn, const double *__restrict__ F,
+                                                      int64_t ncol, double *__restrict__ A, int accumulate) {
+    const int z = blockIdx.z;
+    const int m = z >> 1, par = z & 1;
+    const int nrows = nrows_of(m, par, lmax);
+    const int row0 = blockIdx.y * BM;
+    if (row0 >= nrows) return;
+    const int64_t col0 = (int64_t)blockIdx.x * BN;
+    const double *L = lam + lam_off[z];
+    const double *B = F + ((int64_t)(par * (lmax + 1) + m) * nrn) * ncol;
+    __shared__ double As[BK][BM + 1];
+    __shared__ double Bs[BK][BN];
+    const int tid = threadIdx.x;
+    const int tx = tid & 15, ty = tid >> 4;
+    double acc[4][4] = {};
+    for (int k0 = 0; k0 < nrn; k0 += BK) {
+        for (int i = tid; i < BM * BK; i += 256) {
+            const int rr = i / BK, kk = i % BK;
+            const int row = row0 + rr, k = k0 + kk;
+            As[kk][rr] = (row < nrows && k < nrn) ? L[(int64_t)row * nrn + k] : 0.0;
+        }
+        for (int i = tid; i < BK * BN; i += 256) {
+            const int kk = i / BN, cc = i % BN;
+            const int k = k0 + kk;
+            const int64_t col = col0 + cc;
+            Bs[kk][cc] = (k < nrn && col < ncol) ? B[(int64_t)k * ncol + col] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < BK; ++kk) {
+            double a[4], b[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) a[i] = As[kk][ty * 4 + i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int row = row0 + ty * 4 + i;
+        if (row >= nrows) continue;
+        const int l = m + par + 2 * row;
+        const int64_t lm = (int64_t)l * (l + 1) / 2 + m;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int64_t col = col0 + tx + 16 * j;
+            if (col >= ncol) continue;
+            double *d = A + lm * ncol + col;
+            *d = accumulate ? *d + acc[i][j] : acc[i][j];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_leg_synthesis(const double *__restrict__ lam, const int64_t *lam_off,
+                                                       int lmax, int nrn, const double *__restrict__ A,
+                                                       int64_t ncol, double *__restrict__ G) {
+    const int z = blockIdx.z;
+    const int m = z >> 1, par = z & 1;
+    const int nrows = nrows_of(m, par, lmax);   // K dimension
+    const int r0 = blockIdx.y * BM;
+    if (r0 >= nrn) return;
+    const int64_t col0 = (int64_t)blockIdx.x * BN;
+    const double *L = lam + lam_off[z];
+    __shared__ double As[BK][BM + 1];
+    __shared__ double Bs[BK][BN];
+    const int tid = threadIdx.x;
+    const int tx = tid & 15, ty = tid >> 4;
+    double acc[4][4] = {};
+    for (int k0 = 0; k0 < nrows; k0 += BK) {
+        for (int i = tid; i < BM * BK; i += 256) {
+            const int kk = i / BM, rr = i % BM;
+            const int k = k0 + kk, r = r0 + rr;
+            As[kk][rr] = (k < nrows && r < nrn) ? L[(int64_t)k * nrn + r] : 0.0;
+        }
+        for (int i = tid; i < BK * BN; i += 256) {
+            const int kk = i / BN, cc = i % BN;
+            const int k = k0 + kk;
+            const int64_t col = col0 + cc;
+            double v = 0.0;
+            if (k < nrows && col < ncol) {
+                const int l = m + par + 2 * k;
+                v = A[((int64_t)l * (l + 1) / 2 + m) * ncol + col];
+            }
+            Bs[kk][cc] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < BK; ++kk) {
+            double a[4], b[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) a[i] = As[kk][ty * 4 + i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+    double *Gb = G + ((int64_t)(par * (lmax + 1) + m) * nrn) * ncol;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int r = r0 + ty * 4 + i;
+        if (r >= nrn) continue;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int64_t col = col0 + tx + 16 * j;
+            if (col < ncol) Gb[(int64_t)r * ncol + col] = acc[i][j];
+        }
+    }
+}
+
+// R[p][m'][r][c] = F[p][m'][r][c] - w * nph * cfold * Fold(G[p][.][r][c])[m']
+// Fold(G)_{m'} = sum_{m = m' mod n + t n <= L} G_m e^{i(m-m')phi0}
+//              + sum_{m >= 1, m = -m' mod n + t n <= L} conj(G_m) e^{-i(m+m')phi0},
+// and (m -/+ m') is a multiple of n, phi0 = pi/den with den in {0, n}, so
+// every phase is +1 or (-1)^t.  G_0 enters through its real part.
+__global__ void k_fold_residual(const RingGeom *rings, int nrn, int lmax, double w, const double *__restrict__ F,
+                                const double *__restrict__ G, int64_t ncplx, double *__restrict__ R) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int mp = blockIdx.y;
+    const int r = blockIdx.z % nrn;
+    const int par = blockIdx.z / nrn;
+    if (c >= ncplx) return;
+    const RingGeom g = rings[r];
+    const int n = g.nph;
+    const int L1 = lmax + 1;
+    const int64_t ld = 2 * ncplx;
+    const bool odd_phase = g.phi0_den != 0;   // e^{i t n phi0} = (-1)^t when phi0 = pi/n
+    double sx = 0.0, sy = 0.0;
+    const int k = mp % n;
+    int t = 0;
+    for (int m = k; m <= lmax; m += n, ++t) {
+        const double *gp = G + ((int64_t)(par * L1 + m) * nrn + r) * ld + 2 * c;
+        // (m - m') = (t - t0) n with t0 = m' / n
+        const int dt = t - mp / n;
+        const double sgn = (odd_phase && (dt & 1)) ? -1.0 : 1.0;
+        sx += sgn * gp[0];
+        sy += (m == 0) ? 0.0 : sgn * gp[1];
+    }
+    const int kk = (n - k) % n;
+    for (int m = (kk == 0 ? n : kk); m <= lmax; m += n) {
+        const double *gp = G + ((int64_t)(par * L1 + m) * nrn + r) * ld + 2 * c;
+        const int q = (m + mp) / n;   // (m + m') = q n exactly
+        const double sgn = (odd_phase && (q & 1)) ? -1.0 : 1.0;
+        sx += sgn * gp[0];
+        sy -= sgn * gp[1];
+    }
+    const double f = w * (double)n * g.cfold;
+    const int64_t off = ((int64_t)(par * L1 + mp) * nrn + r) * ld + 2 * c;
+    R[off] = F[off] - f * sx;
+    R[off + 1] = F[off + 1] - f * sy;
+}
+
+void launch_leg_analysis(const Plan &p, const double *F, int64_t ncol, double *A, bool accumulate,
+                         cudaStream_t st) {
+    const int maxrows = p.lmax / 2 + 1;
+    dim3 grid((unsigned)((ncol + BN - 1) / BN), (unsigned)((maxrows + BM - 1) / BM), (unsigned)(2 * (p.lmax + 1)));
+    k_leg_analysis<<<grid, 256, 0, st>>>(p.d_lam, p.d_lam_off, p.lmax, (int)p.nrn, F, ncol, A, accumulate ? 1 : 0);
+}
+
+void launch_leg_synthesis(const Plan &p, const double *A, int64_t ncol, double *G, cudaStream_t st) {
+    dim3 grid((unsigned)((ncol + BN - 1) / BN), (unsigned)((p.nrn + BM - 1) / BM), (unsigned)(2 * (p.lmax + 1)));
+    k_leg_synthesis<<<grid, 256, 0, st>>>(p.d_lam, p.d_lam_off, p.lmax, (int)p.nrn, A, ncol, G);
+}
+
+void launch_fold_residual(const Plan &p, const double *F, const double *G, int64_t ncol, double *R,
+                          cudaStream_t st) {
+    const int64_t ncplx = ncol / 2;
+    dim3 grid((unsigned)((ncplx + 63) / 64), (unsigned)(p.lmax + 1), (unsigned)(2 * p.nrn));
+    const double w = 4.0 * M_PI / (double)p.npix;
+    k_fold_residual<<<grid, 64, 0, st>>>(p.d_rings, (int)p.nrn, p.lmax, w, F, G, ncplx, R);
+}
+
+}  // namespace sfb

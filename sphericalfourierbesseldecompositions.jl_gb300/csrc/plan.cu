@@ -1,0 +1,726 @@
+// Plan management, orchestration and the C ABI (include/sfb_gpu.h).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "sfb_internal.h"
+
+namespace sfb {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+int fail(int code, const std::string &msg) {
+    set_error(msg);
+    return code;
+}
+
+int grow(Plan &p, DevBuf<double> &b, size_t n) {
+    if (b.n >= n) return SFB_OK;
+    if (b.ptr) {
+        cudaFree(b.ptr);
+        p.device_bytes -= (int64_t)(b.n * sizeof(double));
+        b.ptr = nullptr;
+        b.n = 0;
+    }
+    if (n == 0) return SFB_OK;
+    cudaError_t e = cudaMalloc(&b.ptr, n * sizeof(double));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        b.ptr = nullptr;
+        return fail(SFB_ENOMEM, "device allocation of " + std::to_string(n * sizeof(double)) + " bytes failed");
+    }
+    b.n = n;
+    p.device_bytes += (int64_t)(n * sizeof(double));
+    return SFB_OK;
+}
+
+template <typename T>
+static int upload(Plan &p, T **dst, const T *src, size_t n) {
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc(dst, n * sizeof(T));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(SFB_ENOMEM, "device allocation failed");
+    }
+    p.device_bytes += (int64_t)(n * sizeof(T));
+    if (src) SFB_CUDA_TRY(cudaMemcpy(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice));
+    return SFB_OK;
+}
+
+// launch wrappers implemented in radial.cu
+void launch_deposit_spline_chunk(const Plan &p, const double *rtp, const double *w, int64_t ngal, int64_t pair0,
+                                 int64_t npc, double scale, double *maps, cudaStream_t st);
+void launch_subtract_dense_chunk(const Plan &p, double *maps, const double *dense, int64_t pair0, int64_t npc,
+                                 cudaStream_t st);
+void launch_gather_dense_chunk(const Plan &p, double *maps, const double *dense, int64_t pair0, int64_t npc,
+                               cudaStream_t st);
+void launch_radial_error_impl(const Plan &p, const double *coef, const double *ymax, unsigned long long *err_bits,
+                              cudaStream_t st);
+void launch_sub_window_chunk(const Plan &p, const double *Awin, int64_t ldW, int64_t pair0, int64_t npc, double *out,
+                             cudaStream_t st);
+void launch_extract_spline_chunk(const Plan &p, const double *A, int64_t ldA, int64_t pair0, int64_t npc, double *out,
+                                 cudaStream_t st);
+void launch_gtab(const Plan &p, int64_t nr, double rmin, double dr, int with_r2dr, double *gtab, cudaStream_t st);
+void launch_project_shells_g(const Plan &p, const double *gtab, int64_t nr, const double *A, int64_t ldA, double *out,
+                             cudaStream_t st);
+void launch_shell_alm_g(const Plan &p, const int32_t *pair_index, const int64_t *noff, const double *gtab, int64_t nr,
+                        const double *anlm, double *A, int64_t ldA, cudaStream_t st);
+void launch_win_sep_g(const Plan &p, const double *gtab, int64_t nr, const double *phi, double *out, cudaStream_t st);
+void launch_win_dense_g(const Plan &p, const double *gtab, int64_t nr, const double *win, double *out, cudaStream_t st);
+void launch_fill(double *x, int64_t n, double v, cudaStream_t st);
+void launch_subtract_sep_chunk(const Plan &p, double *maps, const double *mask, const double *w_ln, int64_t pair0,
+                               int64_t npc, cudaStream_t st);
+void launch_transpose_ld(const double *in, int64_t ldi, int64_t rows, int64_t cols, double *out, int64_t ldo,
+                         cudaStream_t st);
+void launch_axpy(double *y, const double *x, int64_t n, cudaStream_t st);
+
+}  // namespace sfb
+
+struct sfb_plan {
+    sfb::Plan p;
+    cudaStream_t stream = nullptr;
+    int32_t *d_pair_index = nullptr;
+    int64_t *d_noff = nullptr;
+};
+
+using namespace sfb;
+
+namespace {
+
+// Gauss-Legendre nodes/weights on [-1, 1] (Newton iteration on P_Q).
+void gauss_legendre(int Q, std::vector<double> &x, std::vector<double> &w) {
+    x.resize(Q);
+    w.resize(Q);
+    for (int i = 0; i < Q; ++i) {
+        double z = std::cos(M_PI * (i + 0.75) / (Q + 0.5));
+        double dp = 1.0;
+        for (int it = 0; it < 100; ++it) {
+            double p0 = 1.0, p1 = z;
+            for (int k = 2; k <= Q; ++k) {
+                const double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+                p0 = p1;
+                p1 = p2;
+            }
+            dp = Q * (z * p1 - p0) / (z * z - 1.0);
+            const double dz = p1 / dp;
+            z -= dz;
+            if (std::fabs(dz) < 1e-16) break;
+        }
+        double p0 = 1.0, p1 = z;
+        for (int k = 2; k <= Q; ++k) {
+            const double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+            p0 = p1;
+            p1 = p2;
+        }
+        dp = Q * (z * p1 - p0) / (z * z - 1.0);
+        x[i] = z;
+        w[i] = 2.0 / ((1.0 - z * z) * dp * dp);
+    }
+}
+
+int64_t lmsize_of(int64_t l) { return l < 0 ? 0 : (l + 1) * (l + 2) / 2; }
+
+// Compute coefficients for (pieces, degree) and return the measured error.
+int radial_fit(sfb_plan *h, const double *d_ymax, double *err_out) {
+    Plan &p = h->p;
+    p.nbasis = (int64_t)p.pieces * (p.degree + 1) + 2;
+    const int Q = std::min(2 * (p.degree + 1) + 24, 4096);
+    std::vector<double> gx, gw;
+    gauss_legendre(Q, gx, gw);
+    std::vector<double> pq((size_t)Q * (p.degree + 1));
+    for (int q = 0; q < Q; ++q) {
+        double p0 = 1.0, p1 = gx[q];
+        for (int k = 0; k <= p.degree; ++k) {
+            double pk;
+            if (k == 0) pk = 1.0;
+            else if (k == 1) pk = gx[q];
+            else {
+                pk = ((2.0 * (k - 1) + 1.0) * gx[q] * p1 - (k - 1.0) * p0) / k;
+                p0 = p1;
+                p1 = pk;
+            }
+            pq[(size_t)q * (p.degree + 1) + k] = gw[q] * (2.0 * k + 1.0) / 2.0 * pk;
+        }
+    }
+    double *d_gx = nullptr, *d_pq = nullptr;
+    unsigned long long *d_eb = nullptr;
+    SFB_CUDA_TRY(cudaMalloc(&d_gx, Q * sizeof(double)));
+    SFB_CUDA_TRY(cudaMalloc(&d_pq, pq.size() * sizeof(double)));
+    SFB_CUDA_TRY(cudaMalloc(&d_eb, sizeof(unsigned long long)));
+    SFB_CUDA_TRY(cudaMemcpy(d_gx, gx.data(), Q * sizeof(double), cudaMemcpyHostToDevice));
+    SFB_CUDA_TRY(cudaMemcpy(d_pq, pq.data(), pq.size() * sizeof(double), cudaMemcpyHostToDevice));
+    SFB_CUDA_TRY(cudaMemset(d_eb, 0, sizeof(unsigned long long)));
+    if (p.d_coef) {
+        cudaFree(p.d_coef);
+        p.device_bytes -= p.npairs * 8;  // approximate bookkeeping; recomputed below
+    }
+    p.d_coef = nullptr;
+    SFB_CUDA_TRY(cudaMalloc(&p.d_coef, (size_t)p.npairs * p.nbasis * sizeof(double)));
+    launch_radial_coeffs(p, d_gx, d_pq, Q, p.d_coef, h->stream);
+    launch_radial_error_impl(p, p.d_coef, d_ymax, d_eb, h->stream);
+    unsigned long long eb = 0;
+    SFB_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    SFB_CUDA_TRY(cudaGetLastError());
+    SFB_CUDA_TRY(cudaMemcpy(&eb, d_eb, sizeof(eb), cudaMemcpyDeviceToHost));
+    double e;
+    std::memcpy(&e, &eb, sizeof(e));
+    *err_out = e;
+    cudaFree(d_gx);
+    cudaFree(d_pq);
+    cudaFree(d_eb);
+    return SFB_OK;
+}
+
+int choose_radial_basis(sfb_plan *h, const sfb_plan_desc *d) {
+    Plan &p = h->p;
+    const double L = p.rmax - p.rmin;
+    // knot counts encode k: nr = 3 + 12*ceil(2 k L) (src/SphericalBesselGNLs.jl:571)
+    double kest = 0.0;
+    std::vector<double> ymax(p.npairs);
+    for (int64_t i = 0; i < p.npairs; ++i) {
+        const int64_t N = p.h_spl_off[i + 1] - p.h_spl_off[i];
+        kest = std::max(kest, (double)(N - 4) / (24.0 * L));
+        double ym = 0;
+        for (int64_t k = p.h_spl_off[i]; k < p.h_spl_off[i + 1]; ++k) ym = std::max(ym, std::fabs(d->spl_y[k]));
+        ymax[i] = ym;
+    }
+    double *d_ymax = nullptr;
+    SFB_TRY(upload(p, &d_ymax, ymax.data(), ymax.size()));
+    const double tol = d->radial_tol > 0 ? d->radial_tol : 1e-9;
+    p.pieces = d->radial_pieces > 0 ? d->radial_pieces : std::max(1, (int)std::ceil(kest * L / 16.0));
+    const double omega = kest * L / (2.0 * p.pieces);
+    const bool fixed_deg = d->radial_degree > 0;
+    p.degree = fixed_deg ? d->radial_degree : (int)std::ceil(omega + 12.0);
+    double err = 0;
+    SFB_TRY(radial_fit(h, d_ymax, &err));
+    if (!fixed_deg) {
+        // raise the degree while the projection error still improves markedly
+        for (int it = 0; it < 12 && err > tol; ++it) {
+            const int prev_deg = p.degree;
+            const double prev_err = err;
+            p.degree += 4;
+            SFB_TRY(radial_fit(h, d_ymax, &err));
+            if (err > 0.5 * prev_err) {  // floor reached (spline interpolation error)
+                if (err > prev_err) {
+                    p.degree = prev_deg;
+                    SFB_TRY(radial_fit(h, d_ymax, &err));
+                }
+                break;
+            }
+        }
+    }
+    p.radial_error = err;
+    cudaFree(d_ymax);
+    return SFB_OK;
+}
+
+// map2alm with niter refinement on nm maps already in p.maps; result in p.alm [lmsize][2*nm].
+int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st) {
+    Plan &p = h->p;
+    const int64_t ncol = 2 * nm;
+    const size_t fsz = (size_t)2 * (p.lmax + 1) * p.nrn * ncol;
+    SFB_TRY(grow(p, p.fbuf, fsz));
+    SFB_TRY(grow(p, p.alm, (size_t)p.lmsize * ncol));
+    if (p.niter > 0) {
+        SFB_TRY(grow(p, p.gbuf, fsz));
+        SFB_TRY(grow(p, p.rbuf, fsz));
+    }
+    launch_ring_analysis(p, maps, nm, p.fbuf.ptr, st);
+    launch_leg_analysis(p, p.fbuf.ptr, ncol, p.alm.ptr, false, st);
+    for (int it = 0; it < p.niter; ++it) {
+        launch_leg_synthesis(p, p.alm.ptr, ncol, p.gbuf.ptr, st);
+        launch_fold_residual(p, p.fbuf.ptr, p.gbuf.ptr, ncol, p.rbuf.ptr, st);
+        launch_leg_analysis(p, p.rbuf.ptr, ncol, p.alm.ptr, true, st);
+    }
+    SFB_CUDA_TRY(cudaGetLastError());
+    return SFB_OK;
+}
+
+int finish(sfb_plan *h, const double *out_dev, cudaStream_t st) {
+    Plan &p = h->p;
+    launch_check_finite(out_dev, 2 * p.nlmsize, p.d_err, st);
+    int err = 0;
+    SFB_CUDA_TRY(cudaMemcpyAsync(&err, p.d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    SFB_CUDA_TRY(cudaStreamSynchronize(st));
+    SFB_CUDA_TRY(cudaGetLastError());
+    if (err & ERR_NONFINITE_INPUT) return fail(SFB_ENONFINITE, "non-finite galaxy coordinate or weight");
+    if (err & ERR_THETA_RANGE) return fail(SFB_ERANGE, "galaxy theta outside [0, pi]");
+    if (err & ERR_NONFINITE_OUTPUT) return fail(SFB_ENONFINITE, "non-finite a_nlm (all(isfinite.(anlm)) failed)");
+    return SFB_OK;
+}
+
+int64_t chunk_pairs(const Plan &p) {
+    // keep the per-chunk SHT workspace near 2 GB
+    const double per_map = 8.0 * (p.npix + 3.0 * 2 * (p.lmax + 1) * p.nrn * 2 + 2.0 * p.lmsize);
+    int64_t c = (int64_t)(2.0e9 / per_map);
+    c = std::max<int64_t>(1, std::min<int64_t>(c, p.npairs));
+    return c;
+}
+
+int cat2amln_dev(sfb_plan *h, const double *rtp, const double *w, int64_t ngal, double nbar, const sfb_window *win,
+                 double *out, cudaStream_t st) {
+    Plan &p = h->p;
+    if (ngal < 0) return fail(SFB_EINVAL, "ngal < 0");
+    if (!win) return fail(SFB_EINVAL, "window descriptor is NULL");
+    if (ngal > 0 && !rtp) return fail(SFB_EINVAL, "rtp is NULL");
+    if (!(std::isfinite(nbar) && nbar != 0.0)) return fail(SFB_ENONFINITE, "nbar must be finite and non-zero");
+    const int wk = win->kind;
+    if (wk != SFB_WINDOW_ZERO && wk != SFB_WINDOW_SEPARABLE && wk != SFB_WINDOW_DENSE)
+        return fail(SFB_EINVAL, "unknown window kind");
+    if (wk == SFB_WINDOW_SEPARABLE && !(win->mask && win->w_ln)) return fail(SFB_EINVAL, "separable window needs mask and w_ln");
+    if (wk == SFB_WINDOW_DENSE && !win->dense) return fail(SFB_EINVAL, "dense window pointer is NULL");
+    const double dOmega = 4.0 * M_PI / (double)p.npix;
+    const double scale = 1.0 / (nbar * dOmega);
+    SFB_CUDA_TRY(cudaMemsetAsync(p.d_err, 0, sizeof(int), st));
+    if (p.radial_mode == SFB_RADIAL_POLY) {
+        const int64_t nm = p.nbasis + (wk == SFB_WINDOW_SEPARABLE ? 1 : 0);
+        SFB_TRY(grow(p, p.maps, (size_t)nm * p.npix));
+        SFB_CUDA_TRY(cudaMemsetAsync(p.maps.ptr, 0, (size_t)p.nbasis * p.npix * sizeof(double), st));
+        launch_deposit_poly(p, rtp, w, ngal, p.maps.ptr, st);
+        if (wk == SFB_WINDOW_SEPARABLE)
+            SFB_CUDA_TRY(cudaMemcpyAsync(p.maps.ptr + p.nbasis * p.npix, win->mask, p.npix * sizeof(double),
+                                         cudaMemcpyDeviceToDevice, st));
+        SFB_TRY(sht_analysis(h, p.maps.ptr, nm, st));
+        launch_project_poly(p, p.alm.ptr, 2 * nm, scale, wk, win->w_ln, p.nbasis, nullptr, 0, out, st);
+        if (wk == SFB_WINDOW_DENSE) {
+            const int64_t cp = chunk_pairs(p);
+            SFB_TRY(grow(p, p.maps, (size_t)cp * p.npix));
+            for (int64_t p0 = 0; p0 < p.npairs; p0 += cp) {
+                const int64_t npc = std::min(cp, p.npairs - p0);
+                launch_gather_dense_chunk(p, p.maps.ptr, win->dense, p0, npc, st);
+                SFB_TRY(sht_analysis(h, p.maps.ptr, npc, st));
+                launch_sub_window_chunk(p, p.alm.ptr, 2 * npc, p0, npc, out, st);
+            }
+        }
+    } else {
+        // reference order: map = sum w g / (nbar dOmega) - W[:, l, n], then map2alm, keep row l
+        const int64_t cp = chunk_pairs(p);
+        SFB_TRY(grow(p, p.maps, (size_t)cp * p.npix));
+        for (int64_t p0 = 0; p0 < p.npairs; p0 += cp) {
+            const int64_t npc = std::min(cp, p.npairs - p0);
+            SFB_CUDA_TRY(cudaMemsetAsync(p.maps.ptr, 0, (size_t)npc * p.npix * sizeof(double), st));
+            launch_deposit_spline_chunk(p, rtp, w, ngal, p0, npc, scale, p.maps.ptr, st);
+            if (wk == SFB_WINDOW_DENSE) launch_subtract_dense_chunk(p, p.maps.ptr, win->dense, p0, npc, st);
+            if (wk == SFB_WINDOW_SEPARABLE) launch_subtract_sep_chunk(p, p.maps.ptr, win->mask, win->w_ln, p0, npc, st);
+            SFB_TRY(sht_analysis(h, p.maps.ptr, npc, st));
+            launch_extract_spline_chunk(p, p.alm.ptr, 2 * npc, p0, npc, out, st);
+        }
+    }
+    SFB_CUDA_TRY(cudaGetLastError());
+    return finish(h, out, st);
+}
+
+int check_plan(const sfb_plan *h) {
+    if (!h) return fail(SFB_EINVAL, "plan is NULL");
+    return SFB_OK;
+}
+
+int set_device_of(const sfb_plan *h) {
+    SFB_CUDA_TRY(cudaSetDevice(h->p.device));
+    return SFB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sfb_last_error(char *buf, size_t len) {
+    if (!buf || len == 0) return SFB_EINVAL;
+    std::strncpy(buf, g_last_error.c_str(), len - 1);
+    buf[len - 1] = 0;
+    return SFB_OK;
+}
+
+int sfb_plan_create(const sfb_plan_desc *d, sfb_plan **out) {
+    if (!out) return fail(SFB_EINVAL, "output pointer is NULL");
+    *out = nullptr;
+    if (!d) return fail(SFB_EINVAL, "plan description is NULL");
+    if (d->nside < 1) return fail(SFB_EINVAL, "nside must be >= 1");
+    if (d->nside > 1024) return fail(SFB_ENOTSUP, "nside > 1024 is not supported");
+    if (d->lmax < 0 || d->nmax < 1 || !d->lmax_n) return fail(SFB_EINVAL, "bad lmax/nmax/lmax_n");
+    if (d->lmax > 4 * d->nside) return fail(SFB_ERANGE, "alm.lmax > 4*nside is a poor choice");
+    if (!(d->rmin < d->rmax)) return fail(SFB_EINVAL, "rmin >= rmax");
+    if (!d->spl_offset || !d->spl_x || !d->spl_y || !d->spl_ypp) return fail(SFB_EINVAL, "spline tables missing");
+    if (d->niter < 0 || d->niter > 64) return fail(SFB_EINVAL, "niter out of range");
+    if (d->precision != SFB_FP64 && d->precision != SFB_MIXED) return fail(SFB_EINVAL, "unknown precision");
+    if (d->radial_mode != SFB_RADIAL_POLY && d->radial_mode != SFB_RADIAL_SPLINE)
+        return fail(SFB_EINVAL, "unknown radial mode");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(SFB_ECUDA, "no CUDA device available");
+    }
+    sfb_plan *h = new sfb_plan();
+    Plan &p = h->p;
+    cudaGetDevice(&p.device);
+    p.nside = d->nside;
+    p.npix = 12 * p.nside * p.nside;
+    p.nrn = 2 * p.nside;
+    p.lmax = (int)d->lmax;
+    p.nmax = (int)d->nmax;
+    p.lmax_n.assign(d->lmax_n, d->lmax_n + d->nmax);
+    p.rmin = d->rmin;
+    p.rmax = d->rmax;
+    p.niter = d->niter;
+    p.precision = d->precision;
+    p.radial_mode = d->radial_mode;
+    p.lmsize = lmsize_of(p.lmax);
+    // pairs and output tables
+    std::vector<int32_t> pair_n, pair_l, out_pair, out_lm, pair_index((size_t)p.nmax * (p.lmax + 1), -1);
+    std::vector<int64_t> noff(p.nmax + 1, 0);
+    for (int n = 1; n <= p.nmax; ++n) {
+        const int64_t ln = p.lmax_n[n - 1];
+        if (ln < 0 || ln > p.lmax) {
+            delete h;
+            return fail(SFB_EINVAL, "lmax_n out of range");
+        }
+        noff[n] = noff[n - 1] + lmsize_of(ln);
+        for (int l = 0; l <= ln; ++l) {
+            pair_index[(size_t)(n - 1) * (p.lmax + 1) + l] = (int32_t)pair_n.size();
+            for (int m = 0; m <= l; ++m) {
+                out_pair.push_back((int32_t)pair_n.size());
+                out_lm.push_back((int32_t)((int64_t)l * (l + 1) / 2 + m));
+            }
+            pair_n.push_back(n);
+            pair_l.push_back(l);
+        }
+    }
+    p.npairs = (int64_t)pair_n.size();
+    p.nlmsize = noff[p.nmax];
+    p.h_spl_off.assign(d->spl_offset, d->spl_offset + p.npairs + 1);
+    if (p.h_spl_off[0] != 0) {
+        delete h;
+        return fail(SFB_EINVAL, "spl_offset[0] must be 0");
+    }
+    for (int64_t i = 0; i < p.npairs; ++i) {
+        const int64_t a = p.h_spl_off[i], b = p.h_spl_off[i + 1];
+        if (b - a < 4 || !(d->spl_x[a] < d->spl_x[b - 1])) {
+            delete h;
+            return fail(SFB_EINVAL, "spline " + std::to_string(i) + " needs >= 4 increasing knots");
+        }
+    }
+    const int64_t nknots = p.h_spl_off[p.npairs];
+    // ring geometry of the north half
+    p.h_rings.resize(p.nrn);
+    const int64_t ns = p.nside;
+    const double fact2 = 4.0 / (double)p.npix, fact1 = (double)(2 * ns) * fact2;
+    for (int64_t r = 0; r < p.nrn; ++r) {
+        const int64_t i = r + 1;
+        RingGeom g;
+        if (i < ns) {
+            g.nph = (int32_t)(4 * i);
+            g.start_n = 2 * i * (i - 1);
+            g.start_s = p.npix - 2 * i * (i + 1);
+            const double omz = (double)(i * i) * fact2;
+            g.z = 1.0 - omz;
+            g.sth = std::sqrt(omz * (2.0 - omz));
+            g.phi0_den = (int32_t)(4 * i);
+        } else {
+            g.nph = (int32_t)(4 * ns);
+            g.start_n = 2 * ns * (ns - 1) + (i - ns) * 4 * ns;
+            const int64_t is = 4 * ns - i;  // mirrored ring
+            g.start_s = 2 * ns * (ns - 1) + (is - ns) * 4 * ns;
+            g.z = (double)(2 * ns - i) * fact1;
+            g.sth = std::sqrt((1.0 - g.z) * (1.0 + g.z));
+            g.phi0_den = ((i + ns) & 1) ? 0 : (int32_t)(4 * ns);
+        }
+        g.cfold = (g.start_s == g.start_n) ? 1.0 : 2.0;
+        p.h_rings[r] = g;
+    }
+    int st = SFB_OK;
+    do {
+        if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            cudaGetLastError();
+            st = fail(SFB_ECUDA, "stream creation failed");
+            break;
+        }
+        if ((st = upload(p, &p.d_rings, p.h_rings.data(), p.h_rings.size())) != SFB_OK) break;
+        std::vector<int64_t> lam_off(2 * (p.lmax + 1));
+        int64_t off = 0;
+        for (int m = 0; m <= p.lmax; ++m)
+            for (int par = 0; par < 2; ++par) {
+                lam_off[2 * m + par] = off;
+                const int64_t nr = (m + par <= p.lmax) ? (p.lmax - m - par) / 2 + 1 : 0;
+                off += nr * p.nrn;
+            }
+        p.lam_elems = off;
+        if ((st = upload(p, &p.d_lam_off, lam_off.data(), lam_off.size())) != SFB_OK) break;
+        if ((st = upload<double>(p, &p.d_lam, nullptr, (size_t)off)) != SFB_OK) break;
+        if ((st = upload(p, &p.d_spl_off, p.h_spl_off.data(), p.h_spl_off.size())) != SFB_OK) break;
+        if ((st = upload(p, &p.d_spl_x, d->spl_x, (size_t)nknots)) != SFB_OK) break;
+        if ((st = upload(p, &p.d_spl_y, d->spl_y, (size_t)nknots)) != SFB_OK) break;
+        if ((st = upload(p, &p.d_spl_ypp, d->spl_ypp, (size_t)nknots)) != SFB_OK) break;
+        if ((st = upload(p, &p.d_pair_n, pair_n.data(), pair_n.size())) != SFB_OK) break;
+        if ((st = upload(p, &p.d_pair_l, pair_l.data(), pair_l.size())) != SFB_OK) break;
+        if ((st = upload(p, &p.d_out_pair, out_pair.data(), out_pair.size())) != SFB_OK) break;
+        if ((st = upload(p, &p.d_out_lm, out_lm.data(), out_lm.size())) != SFB_OK) break;
+        if ((st = upload(p, &h->d_pair_index, pair_index.data(), pair_index.size())) != SFB_OK) break;
+        if ((st = upload(p, &h->d_noff, noff.data(), noff.size())) != SFB_OK) break;
+        if ((st = upload<int>(p, &p.d_err, nullptr, 1)) != SFB_OK) break;
+        launch_legendre_table(p, h->stream);
+        if (cudaGetLastError() != cudaSuccess) {
+            st = fail(SFB_ECUDA, "Legendre table kernel failed to launch");
+            break;
+        }
+        if (p.radial_mode == SFB_RADIAL_POLY) {
+            if ((st = choose_radial_basis(h, d)) != SFB_OK) break;
+        } else {
+            p.nbasis = p.npairs;
+        }
+        if (cudaStreamSynchronize(h->stream) != cudaSuccess) {
+            st = fail(SFB_ECUDA, std::string("plan setup failed: ") + cudaGetErrorString(cudaGetLastError()));
+            break;
+        }
+    } while (0);
+    if (st != SFB_OK) {
+        sfb_plan_destroy(h);
+        return st;
+    }
+    *out = h;
+    return SFB_OK;
+}
+
+void sfb_plan_destroy(sfb_plan *h) {
+    if (!h) return;
+    Plan &p = h->p;
+    cudaSetDevice(p.device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    void *ptrs[] = {p.d_rings, p.d_lam, p.d_lam_off, p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp,
+                    p.d_pair_l, p.d_pair_n, p.d_out_pair, p.d_out_lm, p.d_coef, p.d_err,
+                    p.maps.ptr, p.fbuf.ptr, p.gbuf.ptr, p.rbuf.ptr, p.alm.ptr, p.scratch.ptr, p.scratch2.ptr,
+                    h->d_pair_index, h->d_noff};
+    for (void *q : ptrs)
+        if (q) cudaFree(q);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+int sfb_plan_get_info(const sfb_plan *h, sfb_plan_info *info) {
+    SFB_TRY(check_plan(h));
+    if (!info) return fail(SFB_EINVAL, "info is NULL");
+    const Plan &p = h->p;
+    info->npix = p.npix;
+    info->nlmsize = p.nlmsize;
+    info->npairs = p.npairs;
+    info->nbasis = p.nbasis;
+    info->radial_pieces = p.radial_mode == SFB_RADIAL_POLY ? p.pieces : 0;
+    info->radial_degree = p.radial_mode == SFB_RADIAL_POLY ? p.degree : 0;
+    info->radial_error = p.radial_mode == SFB_RADIAL_POLY ? p.radial_error : 0.0;
+    info->device_bytes = p.device_bytes;
+    return SFB_OK;
+}
+
+int sfb_set_precision(sfb_plan *h, int32_t precision) {
+    SFB_TRY(check_plan(h));
+    if (precision != SFB_FP64 && precision != SFB_MIXED) return fail(SFB_EINVAL, "unknown precision");
+    h->p.precision = precision;
+    return SFB_OK;
+}
+
+int sfb_cat2amln_device(sfb_plan *h, const double *rtp, const double *weight, int64_t ngal, double nbar,
+                        const sfb_window *window, double *anlm_out, void *stream) {
+    SFB_TRY(check_plan(h));
+    SFB_TRY(set_device_of(h));
+    if (!anlm_out) return fail(SFB_EINVAL, "output is NULL");
+    return cat2amln_dev(h, rtp, weight, ngal, nbar, window, anlm_out, (cudaStream_t)stream);
+}
+
+int sfb_cat2amln(sfb_plan *h, const double *rtp, const double *weight, int64_t ngal, double nbar,
+                 const sfb_window *window, double *anlm_out) {
+    SFB_TRY(check_plan(h));
+    SFB_TRY(set_device_of(h));
+    if (!anlm_out || !window) return fail(SFB_EINVAL, "output or window is NULL");
+    if (ngal < 0) return fail(SFB_EINVAL, "ngal < 0");
+    if (ngal > 0 && !rtp) return fail(SFB_EINVAL, "rtp is NULL");
+    Plan &p = h->p;
+    cudaStream_t st = h->stream;
+    // device staging: [rtp 3N][w N][out 2*nlmsize][window]
+    const int64_t wlen = window->kind == SFB_WINDOW_SEPARABLE ? p.npix + (int64_t)(p.lmax + 1) * p.nmax
+                       : window->kind == SFB_WINDOW_DENSE ? p.npix * (int64_t)(p.lmax + 1) * p.nmax : 0;
+    const size_t need = (size_t)(3 * ngal + (weight ? ngal : 0) + 2 * p.nlmsize + wlen);
+    SFB_TRY(grow(p, p.scratch, need));
+    double *d_rtp = p.scratch.ptr;
+    double *d_w = weight ? d_rtp + 3 * ngal : nullptr;
+    double *d_out = d_rtp + 3 * ngal + (weight ? ngal : 0);
+    double *d_win = d_out + 2 * p.nlmsize;
+    if (ngal > 0) {
+        SFB_CUDA_TRY(cudaMemcpyAsync(d_rtp, rtp, 3 * ngal * sizeof(double), cudaMemcpyHostToDevice, st));
+        if (weight) SFB_CUDA_TRY(cudaMemcpyAsync(d_w, weight, ngal * sizeof(double), cudaMemcpyHostToDevice, st));
+    }
+    sfb_window dw = *window;
+    if (window->kind == SFB_WINDOW_SEPARABLE) {
+        if (!window->mask || !window->w_ln) return fail(SFB_EINVAL, "separable window needs mask and w_ln");
+        SFB_CUDA_TRY(cudaMemcpyAsync(d_win, window->mask, p.npix * sizeof(double), cudaMemcpyHostToDevice, st));
+        SFB_CUDA_TRY(cudaMemcpyAsync(d_win + p.npix, window->w_ln, (size_t)(p.lmax + 1) * p.nmax * sizeof(double),
+                                     cudaMemcpyHostToDevice, st));
+        dw.mask = d_win;
+        dw.w_ln = d_win + p.npix;
+    } else if (window->kind == SFB_WINDOW_DENSE) {
+        if (!window->dense) return fail(SFB_EINVAL, "dense window pointer is NULL");
+        SFB_CUDA_TRY(cudaMemcpyAsync(d_win, window->dense, (size_t)wlen * sizeof(double), cudaMemcpyHostToDevice, st));
+        dw.dense = d_win;
+    }
+    SFB_TRY(cat2amln_dev(h, ngal > 0 ? d_rtp : nullptr, d_w, ngal, nbar, &dw, d_out, st));
+    SFB_CUDA_TRY(cudaMemcpyAsync(anlm_out, d_out, 2 * p.nlmsize * sizeof(double), cudaMemcpyDeviceToHost, st));
+    SFB_CUDA_TRY(cudaStreamSynchronize(st));
+    return SFB_OK;
+}
+
+int sfb_map2alm(sfb_plan *h, const double *maps, int64_t nmaps, double *alm_out) {
+    SFB_TRY(check_plan(h));
+    SFB_TRY(set_device_of(h));
+    if (nmaps <= 0 || !maps || !alm_out) return fail(SFB_EINVAL, "bad map2alm arguments");
+    Plan &p = h->p;
+    cudaStream_t st = h->stream;
+    SFB_TRY(grow(p, p.maps, (size_t)nmaps * p.npix));
+    SFB_CUDA_TRY(cudaMemcpyAsync(p.maps.ptr, maps, (size_t)nmaps * p.npix * sizeof(double), cudaMemcpyHostToDevice, st));
+    SFB_TRY(sht_analysis(h, p.maps.ptr, nmaps, st));
+    std::vector<double> A((size_t)p.lmsize * 2 * nmaps);
+    SFB_CUDA_TRY(cudaMemcpyAsync(A.data(), p.alm.ptr, A.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    SFB_CUDA_TRY(cudaStreamSynchronize(st));
+    for (int64_t b = 0; b < nmaps; ++b)
+        for (int64_t lm = 0; lm < p.lmsize; ++lm) {
+            alm_out[(b * p.lmsize + lm) * 2] = A[(size_t)lm * 2 * nmaps + 2 * b];
+            alm_out[(b * p.lmsize + lm) * 2 + 1] = A[(size_t)lm * 2 * nmaps + 2 * b + 1];
+        }
+    return SFB_OK;
+}
+
+int sfb_field2anlm(sfb_plan *h, const double *f, int64_t nr, double rmin, double rmax, double *anlm_out) {
+    SFB_TRY(check_plan(h));
+    SFB_TRY(set_device_of(h));
+    if (!f || !anlm_out || nr < 1 || !(rmin < rmax)) return fail(SFB_EINVAL, "bad field2anlm arguments");
+    Plan &p = h->p;
+    cudaStream_t st = h->stream;
+    const double dr = (rmax - rmin) / (double)nr;
+    // [field nr*npix][gtab npairs*nr][out 2*nlmsize][acc 2*nlmsize]
+    SFB_TRY(grow(p, p.scratch, (size_t)(nr * p.npix + p.npairs * nr + 4 * p.nlmsize)));
+    double *d_f = p.scratch.ptr;
+    double *d_g = d_f + nr * p.npix;
+    double *d_out = d_g + p.npairs * nr;
+    double *d_acc = d_out + 2 * p.nlmsize;
+    SFB_CUDA_TRY(cudaMemcpyAsync(d_f, f, (size_t)nr * p.npix * sizeof(double), cudaMemcpyHostToDevice, st));
+    launch_gtab(p, nr, rmin, dr, 1, d_g, st);
+    SFB_CUDA_TRY(cudaMemsetAsync(d_acc, 0, 2 * p.nlmsize * sizeof(double), st));
+    const int64_t cs = std::max<int64_t>(1, std::min<int64_t>(nr, chunk_pairs(p)));
+    SFB_TRY(grow(p, p.scratch2, (size_t)cs * p.npairs));
+    for (int64_t s0 = 0; s0 < nr; s0 += cs) {
+        const int64_t nsc = std::min(cs, nr - s0);
+        SFB_TRY(grow(p, p.maps, (size_t)nsc * p.npix));
+        // maps[s][p] = f[s0+s + nr p]
+        launch_transpose_ld(d_f + s0, nr, p.npix, nsc, p.maps.ptr, p.npix, st);
+        SFB_TRY(sht_analysis(h, p.maps.ptr, nsc, st));
+        // gtab for this chunk: rows pair, cols nsc (copy sub-block)
+        SFB_CUDA_TRY(cudaMemcpy2DAsync(p.scratch2.ptr, nsc * sizeof(double), d_g + s0, nr * sizeof(double),
+                                       nsc * sizeof(double), p.npairs, cudaMemcpyDeviceToDevice, st));
+        launch_project_shells_g(p, p.scratch2.ptr, nsc, p.alm.ptr, 2 * nsc, d_out, st);
+        launch_axpy(d_acc, d_out, 2 * p.nlmsize, st);  // d_acc += d_out
+    }
+    SFB_CUDA_TRY(cudaMemsetAsync(p.d_err, 0, sizeof(int), st));
+    SFB_TRY(finish(h, d_acc, st));
+    SFB_CUDA_TRY(cudaMemcpyAsync(anlm_out, d_acc, 2 * p.nlmsize * sizeof(double), cudaMemcpyDeviceToHost, st));
+    SFB_CUDA_TRY(cudaStreamSynchronize(st));
+    return SFB_OK;
+}
+
+int sfb_anlm2field(sfb_plan *h, const double *anlm, int64_t nr, double rmin, double rmax, double *f_out) {
+    SFB_TRY(check_plan(h));
+    SFB_TRY(set_device_of(h));
+    if (!anlm || !f_out || nr < 1 || !(rmin < rmax)) return fail(SFB_EINVAL, "bad anlm2field arguments");
+    Plan &p = h->p;
+    cudaStream_t st = h->stream;
+    const double dr = (rmax - rmin) / (double)nr;
+    // [anlm 2*nlmsize][gtab npairs*nr][field nr*npix]
+    SFB_TRY(grow(p, p.scratch, (size_t)(2 * p.nlmsize + p.npairs * nr + nr * p.npix)));
+    double *d_a = p.scratch.ptr;
+    double *d_g = d_a + 2 * p.nlmsize;
+    double *d_f = d_g + p.npairs * nr;
+    SFB_CUDA_TRY(cudaMemcpyAsync(d_a, anlm, 2 * p.nlmsize * sizeof(double), cudaMemcpyHostToDevice, st));
+    launch_gtab(p, nr, rmin, dr, 0, d_g, st);
+    const int64_t cs = std::max<int64_t>(1, std::min<int64_t>(nr, chunk_pairs(p)));
+    SFB_TRY(grow(p, p.scratch2, (size_t)cs * p.npairs));
+    const size_t fsz = (size_t)2 * (p.lmax + 1) * p.nrn * 2 * cs;
+    SFB_TRY(grow(p, p.gbuf, fsz));
+    SFB_TRY(grow(p, p.alm, (size_t)p.lmsize * 2 * cs));
+    SFB_TRY(grow(p, p.maps, (size_t)cs * p.npix));
+    for (int64_t s0 = 0; s0 < nr; s0 += cs) {
+        const int64_t nsc = std::min(cs, nr - s0);
+        SFB_CUDA_TRY(cudaMemcpy2DAsync(p.scratch2.ptr, nsc * sizeof(double), d_g + s0, nr * sizeof(double),
+                                       nsc * sizeof(double), p.npairs, cudaMemcpyDeviceToDevice, st));
+        launch_shell_alm_g(p, h->d_pair_index, h->d_noff, p.scratch2.ptr, nsc, d_a, p.alm.ptr, 2 * nsc, st);
+        launch_leg_synthesis(p, p.alm.ptr, 2 * nsc, p.gbuf.ptr, st);
+        launch_ring_synthesis(p, p.gbuf.ptr, nsc, p.maps.ptr, st);
+        // f[s0+s + nr p] = maps[s][p]
+        launch_transpose_ld(p.maps.ptr, p.npix, nsc, p.npix, d_f + s0, nr, st);
+    }
+    SFB_CUDA_TRY(cudaGetLastError());
+    SFB_CUDA_TRY(cudaMemcpyAsync(f_out, d_f, (size_t)nr * p.npix * sizeof(double), cudaMemcpyDeviceToHost, st));
+    SFB_CUDA_TRY(cudaStreamSynchronize(st));
+    return SFB_OK;
+}
+
+int sfb_win_rhat_ln_separable(sfb_plan *h, const double *phi, int64_t nr, double rmin, double rmax, double *w_ln_out) {
+    SFB_TRY(check_plan(h));
+    SFB_TRY(set_device_of(h));
+    if (!phi || !w_ln_out || nr < 1 || !(rmin < rmax)) return fail(SFB_EINVAL, "bad win_rhat_ln arguments");
+    Plan &p = h->p;
+    cudaStream_t st = h->stream;
+    const double dr = (rmax - rmin) / (double)nr;
+    const int64_t nout = (int64_t)(p.lmax + 1) * p.nmax;
+    SFB_TRY(grow(p, p.scratch, (size_t)(nr + p.npairs * nr + nout)));
+    double *d_phi = p.scratch.ptr, *d_g = d_phi + nr, *d_o = d_g + p.npairs * nr;
+    SFB_CUDA_TRY(cudaMemcpyAsync(d_phi, phi, nr * sizeof(double), cudaMemcpyHostToDevice, st));
+    launch_gtab(p, nr, rmin, dr, 1, d_g, st);
+    launch_fill(d_o, nout, NAN, st);
+    launch_win_sep_g(p, d_g, nr, d_phi, d_o, st);
+    SFB_CUDA_TRY(cudaGetLastError());
+    SFB_CUDA_TRY(cudaMemcpyAsync(w_ln_out, d_o, nout * sizeof(double), cudaMemcpyDeviceToHost, st));
+    SFB_CUDA_TRY(cudaStreamSynchronize(st));
+    return SFB_OK;
+}
+
+int sfb_win_rhat_ln_dense(sfb_plan *h, const double *win, int64_t nr, double rmin, double rmax, double *w_out) {
+    SFB_TRY(check_plan(h));
+    SFB_TRY(set_device_of(h));
+    if (!win || !w_out || nr < 1 || !(rmin < rmax)) return fail(SFB_EINVAL, "bad win_rhat_ln arguments");
+    Plan &p = h->p;
+    cudaStream_t st = h->stream;
+    const double dr = (rmax - rmin) / (double)nr;
+    const int64_t nout = p.npix * (int64_t)(p.lmax + 1) * p.nmax;
+    SFB_TRY(grow(p, p.scratch, (size_t)(nr * p.npix + p.npairs * nr + nout)));
+    double *d_win = p.scratch.ptr, *d_g = d_win + nr * p.npix, *d_o = d_g + p.npairs * nr;
+    SFB_CUDA_TRY(cudaMemcpyAsync(d_win, win, (size_t)nr * p.npix * sizeof(double), cudaMemcpyHostToDevice, st));
+    launch_gtab(p, nr, rmin, dr, 1, d_g, st);
+    launch_fill(d_o, nout, NAN, st);
+    launch_win_dense_g(p, d_g, nr, d_win, d_o, st);
+    SFB_CUDA_TRY(cudaGetLastError());
+    SFB_CUDA_TRY(cudaMemcpyAsync(w_out, d_o, (size_t)nout * sizeof(double), cudaMemcpyDeviceToHost, st));
+    SFB_CUDA_TRY(cudaStreamSynchronize(st));
+    return SFB_OK;
+}
+
+int sfb_ang2pix_ring(int64_t nside, const double *theta, const double *phi, int64_t n, int64_t *pix_out) {
+    if (nside < 1 || n < 0 || (n > 0 && (!theta || !phi || !pix_out))) return fail(SFB_EINVAL, "bad ang2pix arguments");
+    if (n == 0) return SFB_OK;
+    double *d = nullptr;
+    int64_t *dp = nullptr;
+    SFB_CUDA_TRY(cudaMalloc(&d, 2 * n * sizeof(double)));
+    if (cudaMalloc(&dp, n * sizeof(int64_t)) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(d);
+        return fail(SFB_ENOMEM, "allocation failed");
+    }
+    cudaMemcpy(d, theta, n * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(d + n, phi, n * sizeof(double), cudaMemcpyHostToDevice);
+    launch_ang2pix(nside, d, d + n, n, dp, 0);
+    cudaError_t e = cudaMemcpy(pix_out, dp, n * sizeof(int64_t), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    cudaFree(dp);
+    if (e != cudaSuccess) return fail(SFB_ECUDA, cudaGetErrorString(e));
+    return SFB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,434 @@
+// Galaxy deposit, radial basis and radial projection kernels.
+//
+// cat2amln (reference src/cat2anlm.jl:257-310) forms, for every (n,l),
+//   map_nl[p] = sum_{i in p} w_i g_nl(r_i) / (nbar dOmega) - W[p,l,n]
+// and keeps row l of map2alm(map_nl).  map2alm is linear, so with
+//   g_nl(r) ~= sum_b C[nl][b] phi_b(r)      (piecewise Legendre basis phi_b)
+// the galaxy term becomes sum_b C[nl][b] map2alm(D_b) / (nbar dOmega) with
+// D_b[p] = sum_{i in p} w_i phi_b(r_i): one transform per basis function
+// instead of one per (n,l).  Galaxies below rmin / above rmax use the
+// spline's boundary extrapolation (src/Splines.jl:72-77) through two
+// constant basis maps.
+#include "sfb_internal.h"
+
+namespace sfb {
+
+__device__ __forceinline__ bool galaxy_ok(double r, double th, double ph, double w, int *err) {
+    if (!(isfinite(r) && isfinite(th) && isfinite(ph) && isfinite(w))) {
+        atomicOr(err, ERR_NONFINITE_INPUT);
+        return false;
+    }
+    if (th < 0.0 || th > M_PI) {
+        atomicOr(err, ERR_THETA_RANGE);
+        return false;
+    }
+    return true;
+}
+
+// One thread per galaxy: HEALPix pixel, piece, Legendre values P_0..P_deg of
+// the local coordinate, scatter-add w*P_k into map (piece*(deg+1)+k).
+__global__ void k_deposit_poly(const double *__restrict__ rtp, const double *__restrict__ wgt, int64_t ngal,
+                               int64_t nside, int64_t npix, double rmin, double rmax, int pieces, int deg,
+                               int64_t nbasis, double *__restrict__ maps, int *err) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ngal) return;
+    const double r = rtp[3 * i], th = rtp[3 * i + 1], ph = rtp[3 * i + 2];
+    const double w = wgt ? wgt[i] : 1.0;
+    if (!galaxy_ok(r, th, ph, w, err)) return;
+    const int64_t pix = ang2pix_ring_z(nside, cos(th), ph);
+    if (r < rmin) {
+        atomicAdd(maps + (nbasis - 2) * npix + pix, w);
+        return;
+    }
+    if (r > rmax) {
+        atomicAdd(maps + (nbasis - 1) * npix + pix, w);
+        return;
+    }
+    const double width = (rmax - rmin) / pieces;
+    int j = (int)((r - rmin) / width);
+    if (j >= pieces) j = pieces - 1;
+    double x = 2.0 * (r - (rmin + j * width)) / width - 1.0;
+    x = fmin(1.0, fmax(-1.0, x));
+    double *base = maps + (int64_t)j * (deg + 1) * npix + pix;
+    double p0 = 1.0, p1 = x;
+    atomicAdd(base, w);
+    if (deg >= 1) atomicAdd(base + npix, w * x);
+    for (int k = 1; k < deg; ++k) {
+        const double p2 = ((2 * k + 1) * x * p1 - k * p0) / (k + 1);
+        atomicAdd(base + (int64_t)(k + 1) * npix, w * p2);
+        p0 = p1;
+        p1 = p2;
+    }
+}
+
+void launch_deposit_poly(const Plan &p, const double *rtp, const double *w, int64_t ngal, double *maps,
+                         cudaStream_t st) {
+    if (ngal <= 0) return;
+    k_deposit_poly<<<(unsigned)((ngal + 255) / 256), 256, 0, st>>>(rtp, w, ngal, p.nside, p.npix, p.rmin, p.rmax,
+                                                                   p.pieces, p.degree, p.nbasis, maps, p.d_err);
+}
+
+// Spline mode: maps[q][pix] += w * g_{pair0+q}(r) / (nbar dOmega) for a chunk of pairs.
+__global__ void k_deposit_spline(const double *__restrict__ rtp, const double *__restrict__ wgt, int64_t ngal,
+                                 int64_t nside, int64_t npix, const int64_t *spl_off, const double *sx,
+                                 const double *sy, const double *sypp, int64_t pair0, int64_t npair_chunk,
+                                 double scale, double *__restrict__ maps, int *err) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ngal) return;
+    const double r = rtp[3 * i], th = rtp[3 * i + 1], ph = rtp[3 * i + 2];
+    const double w = wgt ? wgt[i] : 1.0;
+    if (!galaxy_ok(r, th, ph, w, err)) return;
+    const int64_t pix = ang2pix_ring_z(nside, cos(th), ph);
+    for (int64_t q = blockIdx.y; q < npair_chunk; q += gridDim.y) {
+        const int64_t pr = pair0 + q;
+        const int64_t o = spl_off[pr], N = spl_off[pr + 1] - o;
+        const double g = spline_eval_dev(sx + o, sy + o, sypp + o, N, r);
+        atomicAdd(maps + q * npix + pix, w * g * scale);
+    }
+}
+
+void launch_deposit_spline_chunk(const Plan &p, const double *rtp, const double *w, int64_t ngal,
+                                 int64_t pair0, int64_t npc, double scale, double *maps, cudaStream_t st) {
+    if (ngal <= 0 || npc <= 0) return;
+    unsigned gy = (unsigned)(npc < 64 ? npc : 64);
+    dim3 grid((unsigned)((ngal + 255) / 256), gy);
+    k_deposit_spline<<<grid, 256, 0, st>>>(rtp, w, ngal, p.nside, p.npix, p.d_spl_off, p.d_spl_x, p.d_spl_y,
+                                           p.d_spl_ypp, pair0, npc, scale, maps, p.d_err);
+}
+
+// maps[q][p] -= dense[p + npix*(l + (lmax+1)*(n-1))] for the chunk's pairs.
+__global__ void k_subtract_dense(double *maps, const double *dense, int64_t npix, int lmax, const int32_t *pair_n,
+                                 const int32_t *pair_l, int64_t pair0, int64_t npc) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t q = blockIdx.y;
+    if (p >= npix || q >= npc) return;
+    const int64_t pr = pair0 + q;
+    const int64_t off = npix * ((int64_t)pair_l[pr] + (int64_t)(lmax + 1) * (pair_n[pr] - 1));
+    maps[q * npix + p] -= dense[off + p];
+}
+
+void launch_subtract_dense_chunk(const Plan &p, double *maps, const double *dense, int64_t pair0, int64_t npc,
+                                 cudaStream_t st) {
+    if (npc <= 0) return;
+    dim3 grid((unsigned)((p.npix + 255) / 256), (unsigned)npc);
+    k_subtract_dense<<<grid, 256, 0, st>>>(maps, dense, p.npix, p.lmax, p.d_pair_n, p.d_pair_l, pair0, npc);
+}
+
+// maps[q][p] -= mask[p] * W_ln[l + (lmax+1)(n-1)] for the chunk's pairs (separable window).
+__global__ void k_subtract_sep(double *maps, const double *mask, const double *w_ln, int64_t npix, int lmax,
+                               const int32_t *pair_n, const int32_t *pair_l, int64_t pair0, int64_t npc) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t q = blockIdx.y;
+    if (p >= npix || q >= npc) return;
+    const int64_t pr = pair0 + q;
+    const double wl = w_ln[pair_l[pr] + (int64_t)(lmax + 1) * (pair_n[pr] - 1)];
+    maps[q * npix + p] -= mask[p] * wl;
+}
+
+void launch_subtract_sep_chunk(const Plan &p, double *maps, const double *mask, const double *w_ln, int64_t pair0,
+                               int64_t npc, cudaStream_t st) {
+    if (npc <= 0) return;
+    dim3 grid((unsigned)((p.npix + 255) / 256), (unsigned)npc);
+    k_subtract_sep<<<grid, 256, 0, st>>>(maps, mask, w_ln, p.npix, p.lmax, p.d_pair_n, p.d_pair_l, pair0, npc);
+}
+
+__global__ void k_axpy(double *y, const double *x, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] += x[i];
+}
+
+void launch_axpy(double *y, const double *x, int64_t n, cudaStream_t st) {
+    if (n <= 0) return;
+    int64_t blocks = (n + 255) / 256;
+    if (blocks > 8192) blocks = 8192;
+    k_axpy<<<(unsigned)blocks, 256, 0, st>>>(y, x, n);
+}
+
+// Gather dense window maps of a chunk of pairs: maps[q] = W[:, l, n].
+__global__ void k_gather_dense(double *maps, const double *dense, int64_t npix, int lmax, const int32_t *pair_n,
+                               const int32_t *pair_l, int64_t pair0, int64_t npc) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t q = blockIdx.y;
+    if (p >= npix || q >= npc) return;
+    const int64_t pr = pair0 + q;
+    const int64_t off = npix * ((int64_t)pair_l[pr] + (int64_t)(lmax + 1) * (pair_n[pr] - 1));
+    maps[q * npix + p] = dense[off + p];
+}
+
+void launch_gather_dense_chunk(const Plan &p, double *maps, const double *dense, int64_t pair0, int64_t npc,
+                               cudaStream_t st) {
+    if (npc <= 0) return;
+    dim3 grid((unsigned)((p.npix + 255) / 256), (unsigned)npc);
+    k_gather_dense<<<grid, 256, 0, st>>>(maps, dense, p.npix, p.lmax, p.d_pair_n, p.d_pair_l, pair0, npc);
+}
+
+// Radial coefficients: C[pair][j*(deg+1)+k] = sum_q PQ[q][k] * g(r_q), with
+// r_q the Gauss-Legendre nodes of piece j and PQ[q][k] = w_q (2k+1)/2 P_k(x_q)
+// (L2 projection of the spline onto Legendre polynomials on each piece);
+// C[pair][nbasis-2] / [nbasis-1] = first / last knot value (extrapolation).
+__global__ void k_radial_coeffs(const int64_t *spl_off, const double *sx, const double *sy, const double *sypp,
+                                double rmin, double rmax, int pieces, int deg, int64_t nbasis, const double *glx,
+                                const double *pq, int Q, double *coef) {
+    extern __shared__ double gq[];
+    const int64_t pr = blockIdx.x;
+    const int j = blockIdx.y;
+    const int64_t o = spl_off[pr], N = spl_off[pr + 1] - o;
+    const double width = (rmax - rmin) / pieces;
+    const double a = rmin + j * width;
+    for (int q = threadIdx.x; q < Q; q += blockDim.x) {
+        const double r = a + (glx[q] + 1.0) * 0.5 * width;
+        gq[q] = spline_eval_dev(sx + o, sy + o, sypp + o, N, r);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k <= deg; k += blockDim.x) {
+        double acc = 0.0;
+        for (int q = 0; q < Q; ++q) acc = fma(pq[(int64_t)q * (deg + 1) + k], gq[q], acc);
+        coef[pr * nbasis + (int64_t)j * (deg + 1) + k] = acc;
+    }
+    if (j == 0 && threadIdx.x == 0) {
+        coef[pr * nbasis + nbasis - 2] = sy[o];
+        coef[pr * nbasis + nbasis - 1] = sy[o + N - 1];
+    }
+}
+
+void launch_radial_coeffs(const Plan &p, const double *gl_x, const double *pq, int Q, double *coef,
+                          cudaStream_t st) {
+    dim3 grid((unsigned)p.npairs, (unsigned)p.pieces);
+    k_radial_coeffs<<<grid, 128, Q * sizeof(double), st>>>(p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp, p.rmin,
+                                                          p.rmax, p.pieces, p.degree, p.nbasis, gl_x, pq, Q, coef);
+}
+
+// max over knots of |expansion - y| / max|y| per pair; atomicMax on the bit
+// pattern (non-negative doubles order like their bits).
+__global__ void k_radial_error(const int64_t *spl_off, const double *sx, const double *sy, const double *ymax,
+                               double rmin, double rmax, int pieces, int deg, int64_t nbasis, const double *coef,
+                               unsigned long long *err_bits) {
+    const int64_t pr = blockIdx.x;
+    const int64_t o = spl_off[pr], N = spl_off[pr + 1] - o;
+    const double width = (rmax - rmin) / pieces;
+    const double *C = coef + pr * nbasis;
+    double worst = 0.0;
+    // interior knots only: within a few knots of rmin/rmax the reference
+    // spline carries its parabolic end-slope error, which no smooth expansion
+    // (and no radial resolution below the knot spacing) can follow
+    for (int64_t i = 8 + threadIdx.x; i < N - 8; i += blockDim.x) {
+        const double r = sx[o + i];
+        if (r < rmin || r > rmax) continue;
+        int j = (int)((r - rmin) / width);
+        if (j >= pieces) j = pieces - 1;
+        double x = 2.0 * (r - (rmin + j * width)) / width - 1.0;
+        x = fmin(1.0, fmax(-1.0, x));
+        const double *Cj = C + (int64_t)j * (deg + 1);
+        double p0 = 1.0, p1 = x, v = Cj[0] + (deg >= 1 ? Cj[1] * x : 0.0);
+        for (int k = 1; k < deg; ++k) {
+            const double p2 = ((2 * k + 1) * x * p1 - k * p0) / (k + 1);
+            v = fma(Cj[k + 1], p2, v);
+            p0 = p1;
+            p1 = p2;
+        }
+        worst = fmax(worst, fabs(v - sy[o + i]));
+    }
+    worst /= ymax[pr] > 0 ? ymax[pr] : 1.0;
+    atomicMax(err_bits, (unsigned long long)__double_as_longlong(worst));
+}
+
+void launch_radial_error_impl(const Plan &p, const double *coef, const double *ymax, unsigned long long *err_bits,
+                              cudaStream_t st) {
+    k_radial_error<<<(unsigned)p.npairs, 128, 0, st>>>(p.d_spl_off, p.d_spl_x, p.d_spl_y, ymax, p.rmin, p.rmax,
+                                                       p.pieces, p.degree, p.nbasis, coef, err_bits);
+}
+
+// a_nlm = scale * sum_b C[pair][b] A[lm][b] - window term.
+__global__ void k_project_poly(const int32_t *out_pair, const int32_t *out_lm, const int32_t *pair_n,
+                               const int32_t *pair_l, int64_t nlmsize, int64_t nbasis, const double *coef,
+                               const double *__restrict__ A, int64_t ldA, double scale, int window_kind,
+                               const double *w_ln, int lmax, int64_t mask_col, double *out) {
+    const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= nlmsize) return;
+    const int pr = out_pair[o];
+    const int64_t lm = out_lm[o];
+    const double *C = coef + (int64_t)pr * nbasis;
+    const double *Ar = A + lm * ldA;
+    double re = 0.0, im = 0.0;
+    for (int64_t b = 0; b < nbasis; ++b) {
+        const double c = C[b];
+        re = fma(c, Ar[2 * b], re);
+        im = fma(c, Ar[2 * b + 1], im);
+    }
+    re *= scale;
+    im *= scale;
+    if (window_kind == SFB_WINDOW_SEPARABLE) {
+        const double wl = w_ln[pair_l[pr] + (int64_t)(lmax + 1) * (pair_n[pr] - 1)];
+        re -= wl * Ar[2 * mask_col];
+        im -= wl * Ar[2 * mask_col + 1];
+    }
+    out[2 * o] = re;
+    out[2 * o + 1] = im;
+}
+
+void launch_project_poly(const Plan &p, const double *A, int64_t ldA, double scale, int window_kind,
+                         const double *w_ln, int64_t mask_col, const double *Awin, int64_t ldW, double *out,
+                         cudaStream_t st) {
+    (void)Awin; (void)ldW;
+    if (p.nlmsize <= 0) return;
+    k_project_poly<<<(unsigned)((p.nlmsize + 127) / 128), 128, 0, st>>>(
+        p.d_out_pair, p.d_out_lm, p.d_pair_n, p.d_pair_l, p.nlmsize, p.nbasis, p.d_coef, A, ldA, scale, window_kind,
+        w_ln, p.lmax, mask_col, out);
+}
+
+// out[o] -= Awin[lm][pair - pair0] for outputs whose pair lies in the chunk.
+__global__ void k_sub_window_chunk(const int32_t *out_pair, const int32_t *out_lm, int64_t nlmsize,
+                                   const double *Awin, int64_t ldW, int64_t pair0, int64_t npc, double *out) {
+    const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= nlmsize) return;
+    const int64_t q = (int64_t)out_pair[o] - pair0;
+    if (q < 0 || q >= npc) return;
+    const double *a = Awin + (int64_t)out_lm[o] * ldW + 2 * q;
+    out[2 * o] -= a[0];
+    out[2 * o + 1] -= a[1];
+}
+
+void launch_sub_window_chunk(const Plan &p, const double *Awin, int64_t ldW, int64_t pair0, int64_t npc, double *out,
+                             cudaStream_t st) {
+    if (p.nlmsize <= 0) return;
+    k_sub_window_chunk<<<(unsigned)((p.nlmsize + 127) / 128), 128, 0, st>>>(p.d_out_pair, p.d_out_lm, p.nlmsize, Awin,
+                                                                           ldW, pair0, npc, out);
+}
+
+// Spline mode: out[o] = A[lm][pair - pair0] (map already scaled and window-subtracted).
+__global__ void k_extract_spline(const int32_t *out_pair, const int32_t *out_lm, int64_t nlmsize, const double *A,
+                                 int64_t ldA, int64_t pair0, int64_t npc, double *out) {
+    const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= nlmsize) return;
+    const int64_t q = (int64_t)out_pair[o] - pair0;
+    if (q < 0 || q >= npc) return;
+    const double *a = A + (int64_t)out_lm[o] * ldA + 2 * q;
+    out[2 * o] = a[0];
+    out[2 * o + 1] = a[1];
+}
+
+void launch_extract_spline_chunk(const Plan &p, const double *A, int64_t ldA, int64_t pair0, int64_t npc, double *out,
+                                 cudaStream_t st) {
+    if (p.nlmsize <= 0) return;
+    k_extract_spline<<<(unsigned)((p.nlmsize + 127) / 128), 128, 0, st>>>(p.d_out_pair, p.d_out_lm, p.nlmsize, A, ldA,
+                                                                         pair0, npc, out);
+}
+
+// gtab[pair][s] = g_pair(r_s) * (with_r2dr ? r_s^2 dr : 1), r_s = rmin + (s+1/2) dr.
+__global__ void k_gtab(const int64_t *spl_off, const double *sx, const double *sy, const double *sypp,
+                       int64_t npairs, int64_t nr, double rmin, double dr, int with_r2dr, double *gtab) {
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t pr = blockIdx.y;
+    if (s >= nr || pr >= npairs) return;
+    const double r = rmin + dr / 2 + s * dr;
+    const int64_t o = spl_off[pr], N = spl_off[pr + 1] - o;
+    double g = spline_eval_dev(sx + o, sy + o, sypp + o, N, r);
+    if (with_r2dr) g *= r * r * dr;
+    gtab[pr * nr + s] = g;
+}
+
+void launch_gtab(const Plan &p, int64_t nr, double rmin, double dr, int with_r2dr, double *gtab, cudaStream_t st) {
+    dim3 grid((unsigned)((nr + 127) / 128), (unsigned)p.npairs);
+    k_gtab<<<grid, 128, 0, st>>>(p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp, p.npairs, nr, rmin, dr, with_r2dr,
+                                 gtab);
+}
+
+// field2anlm radial sum: out[o] = sum_s gtab[pair][s] A[lm][s]  (src/cat2anlm.jl:347-353)
+__global__ void k_project_shells(const int32_t *out_pair, const int32_t *out_lm, int64_t nlmsize, const double *gtab,
+                                 int64_t nr, const double *__restrict__ A, int64_t ldA, double *out) {
+    const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= nlmsize) return;
+    const double *g = gtab + (int64_t)out_pair[o] * nr;
+    const double *Ar = A + (int64_t)out_lm[o] * ldA;
+    double re = 0.0, im = 0.0;
+    for (int64_t s = 0; s < nr; ++s) {
+        re = fma(g[s], Ar[2 * s], re);
+        im = fma(g[s], Ar[2 * s + 1], im);
+    }
+    out[2 * o] = re;
+    out[2 * o + 1] = im;
+}
+
+void launch_project_shells_g(const Plan &p, const double *gtab, int64_t nr, const double *A, int64_t ldA, double *out,
+                             cudaStream_t st) {
+    if (p.nlmsize <= 0) return;
+    k_project_shells<<<(unsigned)((p.nlmsize + 127) / 128), 128, 0, st>>>(p.d_out_pair, p.d_out_lm, p.nlmsize, gtab, nr,
+                                                                         A, ldA, out);
+}
+
+// anlm2field radial sum: A[lm][s] = sum_n gtab[pair(n,l)][s] a[idx(n,l,m)] (src/cat2anlm.jl:403-414)
+__global__ void k_shell_alm(const int32_t *pair_index, const int64_t *noff, int nmax, int lmax, const double *gtab,
+                            int64_t nr, const double *anlm, double *A, int64_t ldA) {
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t lm = blockIdx.y;
+    if (s >= nr) return;
+    // recover (l, m) from lm = l(l+1)/2 + m
+    int l = (int)((sqrt(8.0 * (double)lm + 1.0) - 1.0) / 2.0);
+    while ((int64_t)(l + 1) * (l + 2) / 2 <= lm) ++l;
+    while ((int64_t)l * (l + 1) / 2 > lm) --l;
+    const int m = (int)(lm - (int64_t)l * (l + 1) / 2);
+    double re = 0.0, im = 0.0;
+    for (int n = 1; n <= nmax; ++n) {
+        const int pr = pair_index[(int64_t)(n - 1) * (lmax + 1) + l];
+        if (pr < 0) continue;
+        const int64_t idx = noff[n - 1] + (int64_t)l * (l + 1) / 2 + m;
+        const double g = gtab[(int64_t)pr * nr + s];
+        re = fma(g, anlm[2 * idx], re);
+        im = fma(g, anlm[2 * idx + 1], im);
+    }
+    A[lm * ldA + 2 * s] = re;
+    A[lm * ldA + 2 * s + 1] = (m == 0) ? 0.0 : im;
+}
+
+void launch_shell_alm_g(const Plan &p, const int32_t *pair_index, const int64_t *noff, const double *gtab, int64_t nr,
+                        const double *anlm, double *A, int64_t ldA, cudaStream_t st) {
+    dim3 grid((unsigned)((nr + 127) / 128), (unsigned)p.lmsize);
+    k_shell_alm<<<grid, 128, 0, st>>>(pair_index, noff, p.nmax, p.lmax, gtab, nr, anlm, A, ldA);
+}
+
+// W_ln[l + (lmax+1)(n-1)] = sum_s gtab[pair][s] phi[s]  (gtab includes r^2 dr); NaN off-mode.
+__global__ void k_win_sep(const int32_t *pair_n, const int32_t *pair_l, int64_t npairs, const double *gtab, int64_t nr,
+                          const double *phi, int lmax, double *out) {
+    const int64_t pr = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (pr >= npairs) return;
+    double acc = 0.0;
+    for (int64_t s = 0; s < nr; ++s) acc += gtab[pr * nr + s] * phi[s];
+    out[pair_l[pr] + (int64_t)(lmax + 1) * (pair_n[pr] - 1)] = acc;
+}
+
+void launch_win_sep_g(const Plan &p, const double *gtab, int64_t nr, const double *phi, double *out, cudaStream_t st) {
+    k_win_sep<<<(unsigned)((p.npairs + 127) / 128), 128, 0, st>>>(p.d_pair_n, p.d_pair_l, p.npairs, gtab, nr, phi,
+                                                                  p.lmax, out);
+}
+
+// Dense: W[p + npix(l + (lmax+1)(n-1))] = sum_s win[s + nr p] gtab[pair][s]
+__global__ void k_win_dense(const int32_t *pair_n, const int32_t *pair_l, int64_t npairs, const double *gtab, int64_t nr,
+                            const double *win, int64_t npix, int lmax, double *out) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t pr = blockIdx.y;
+    if (p >= npix || pr >= npairs) return;
+    const double *wc = win + p * nr;
+    const double *g = gtab + pr * nr;
+    double acc = 0.0;
+    for (int64_t s = 0; s < nr; ++s) acc += wc[s] * g[s];
+    out[p + npix * ((int64_t)pair_l[pr] + (int64_t)(lmax + 1) * (pair_n[pr] - 1))] = acc;
+}
+
+void launch_win_dense_g(const Plan &p, const double *gtab, int64_t nr, const double *win, double *out, cudaStream_t st) {
+    dim3 grid((unsigned)((p.npix + 127) / 128), (unsigned)p.npairs);
+    k_win_dense<<<grid, 128, 0, st>>>(p.d_pair_n, p.d_pair_l, p.npairs, gtab, nr, win, p.npix, p.lmax, out);
+}
+
+__global__ void k_fill(double *x, int64_t n, double v) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] = v;
+}
+
+void launch_fill(double *x, int64_t n, double v, cudaStream_t st) {
+    if (n <= 0) return;
+    int64_t blocks = (n + 255) / 256;
+    if (blocks > 8192) blocks = 8192;
+    k_fill<<<(unsigned)blocks, 256, 0, st>>>(x, n, v);
+}
+
+}  // namespace sfb

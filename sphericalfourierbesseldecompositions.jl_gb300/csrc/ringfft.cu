@@ -1,0 +1,254 @@
+// Ring Fourier transforms on HEALPix rings (analysis and synthesis direction).
+//
+// A CTA owns one north ring r and its mirrored south ring (same nph and phi0)
+// for a tile of MT maps.  The two real rings are packed as one complex
+// sequence z_j = f_N[j] + i f_S[j], so one complex DFT of length n = nph
+// yields both spectra.  n = 4i (polar) or 4*nside (equatorial) is factored as
+// n = o * 2^s with o odd; the transform is the four-step split
+//   X[k1 + o*k2] = sum_{j2} W_P^{j2 k2} W_n^{j2 k1} sum_{j1} W_o^{j1 k1} x[P*j1 + j2]
+// (P = 2^s): a direct length-o DFT, a twiddle, then an in-place radix-2 FFT of
+// length P in shared memory.  Outputs are the coefficients m = 0..lmax with
+// aliasing (bin m mod n) and the ring phase e^{-i m phi0}, which is the exact
+// ring sum that libsharp's map2alm performs (reference call site
+// src/healpix_helpers.jl:55).
+#include "sfb_internal.h"
+
+namespace sfb {
+
+template <typename T>
+struct cx {
+    T x, y;
+};
+
+template <typename T>
+__device__ __forceinline__ cx<T> cmul(cx<T> a, cx<T> b) {
+    return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+
+__device__ __forceinline__ int bitrev(int v, int s) { return s == 0 ? 0 : (int)(__brev((unsigned)v) >> (32 - s)); }
+
+// Four-step DFT of MT packed sequences held in `src` (natural order, only used
+// when o > 1) / `buf`; result in `buf`, element k at (k % o) * P + k / o.
+// dir = -1 forward (W = e^{-2 pi i/n}), +1 inverse.  `tw` holds W_n^t.
+template <typename T>
+__device__ void four_step(cx<T> *buf, cx<T> *src, const cx<T> *tw, int n, int o, int s, int MT) {
+    const int P = n / o;
+    if (o > 1) {
+        for (int idx = threadIdx.x; idx < MT * n; idx += blockDim.x) {
+            const int b = idx / n;
+            const int rem = idx - b * n;
+            const int k1 = rem / P;
+            const int j2 = rem - k1 * P;
+            const cx<T> *x = src + (int64_t)b * n;
+            cx<T> acc = {0, 0};
+            int e = 0;                    // (P*j1*k1) mod n, advanced incrementally
+            const int step = (int)(((int64_t)P * k1) % n);
+            for (int j1 = 0; j1 < o; ++j1) {
+                const cx<T> v = x[P * j1 + j2];
+                const cx<T> w = tw[e];
+                acc.x += v.x * w.x - v.y * w.y;
+                acc.y += v.x * w.y + v.y * w.x;
+                e += step;
+                if (e >= n) e -= n;
+            }
+            acc = cmul(acc, tw[j2 * k1]);   // j2*k1 < n
+            buf[(int64_t)b * n + k1 * P + bitrev(j2, s)] = acc;
+        }
+        __syncthreads();
+    }
+    // radix-2 DIT stages over the o sequences of length P in each map
+    const int halfP = P >> 1;
+    for (int len = 2; len <= P; len <<= 1) {
+        const int half = len >> 1;
+        const int twstride = n / len;
+        for (int idx = threadIdx.x; idx < MT * o * halfP; idx += blockDim.x) {
+            const int seq = idx / halfP;      // b * o + k1
+            const int u = idx - seq * halfP;
+            const int grp = u / half;
+            const int pos = u - grp * half;
+            const int64_t i0 = (int64_t)seq * P + grp * len + pos;
+            const int64_t i1 = i0 + half;
+            const cx<T> w = tw[twstride * pos];
+            const cx<T> a = buf[i0];
+            const cx<T> bb = cmul(buf[i1], w);
+            buf[i0] = {a.x + bb.x, a.y + bb.y};
+            buf[i1] = {a.x - bb.x, a.y - bb.y};
+        }
+        __syncthreads();
+    }
+}
+
+template <typename T>
+__device__ void fill_twiddles(cx<T> *tw, int n, int dir) {
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        double sn, cs;
+        sincospi(dir * 2.0 * (double)t / (double)n, &sn, &cs);
+        tw[t] = {(T)cs, (T)sn};
+    }
+}
+
+// maps: FP64 [nmaps][npix]; F: [2][lmax+1][nrn][ldF] real view of complex,
+// column 2b / 2b+1 = re / im of map b.
+template <typename T>
+__global__ void __launch_bounds__(256) k_ring_analysis(const RingGeom *rings, int nrn, int lmax, double w,
+                                                       int64_t npix, const double *maps, int64_t nmaps,
+                                                       int MT, T *F, int64_t ldF) {
+    extern __shared__ unsigned char smem_raw[];
+    const int r = blockIdx.x;
+    const int64_t b0 = (int64_t)blockIdx.y * MT;
+    const RingGeom g = rings[r];
+    const int n = g.nph;
+    const int s = __ffs(n) - 1;
+    const int o = n >> s;
+    const int P = 1 << s;
+    const bool paired = g.start_s != g.start_n;
+    cx<T> *tw = reinterpret_cast<cx<T> *>(smem_raw);
+    cx<T> *buf = tw + n;
+    cx<T> *src = buf + (int64_t)MT * n;
+    fill_twiddles(tw, n, -1);
+    for (int idx = threadIdx.x; idx < MT * n; idx += blockDim.x) {
+        const int b = idx / n;
+        const int j = idx - b * n;
+        const int64_t mb = b0 + b;
+        cx<T> v = {0, 0};
+        if (mb < nmaps) {
+            v.x = (T)maps[mb * npix + g.start_n + j];
+            if (paired) v.y = (T)maps[mb * npix + g.start_s + j];
+        }
+        if (o > 1) src[(int64_t)b * n + j] = v;
+        else buf[(int64_t)b * n + bitrev(j, s)] = v;
+    }
+    __syncthreads();
+    four_step<T>(buf, src, tw, n, o, s, MT);
+    // unpack, phase, weight; write F+ and F-
+    const int L1 = lmax + 1;
+    for (int idx = threadIdx.x; idx < MT * L1; idx += blockDim.x) {
+        const int m = idx / MT;
+        const int b = idx - m * MT;
+        const int64_t mb = b0 + b;
+        if (mb >= nmaps) continue;
+        const int k = m % n;
+        const int nk = (n - k) % n;
+        const cx<T> Z = buf[(int64_t)b * n + (k % o) * P + k / o];
+        const cx<T> Zn = buf[(int64_t)b * n + (nk % o) * P + nk / o];
+        const T fnx = (Z.x + Zn.x) * (T)0.5, fny = (Z.y - Zn.y) * (T)0.5;
+        const T fsx = (Z.y + Zn.y) * (T)0.5, fsy = -(Z.x - Zn.x) * (T)0.5;
+        double sn = 0.0, cs = 1.0;
+        if (g.phi0_den != 0) sincospi((double)m / (double)g.phi0_den, &sn, &cs);
+        const T pc = (T)(w * cs), ps = (T)(-w * sn);   // w * e^{-i m phi0}
+        const T px = fnx + fsx, py = fny + fsy;
+        const T qx = fnx - fsx, qy = fny - fsy;
+        T *dp = F + ((int64_t)(0 * L1 + m) * nrn + r) * ldF + 2 * mb;
+        T *dq = F + ((int64_t)(1 * L1 + m) * nrn + r) * ldF + 2 * mb;
+        dp[0] = px * pc - py * ps;
+        dp[1] = px * ps + py * pc;
+        dq[0] = qx * pc - qy * ps;
+        dq[1] = qx * ps + qy * pc;
+    }
+}
+
+// G: [2][lmax+1][nrn][ldG] parity parts of sum_l lambda_lm a_lm.  Writes the
+// real ring values of both rings of the pair into maps (FP64 [nmaps][npix]).
+template <typename T>
+__global__ void __launch_bounds__(256) k_ring_synthesis(const RingGeom *rings, int nrn, int lmax,
+                                                        const T *G, int64_t ldG, int64_t nmaps, int MT,
+                                                        int64_t npix, double *maps) {
+    extern __shared__ unsigned char smem_raw[];
+    const int r = blockIdx.x;
+    const int64_t b0 = (int64_t)blockIdx.y * MT;
+    const RingGeom g = rings[r];
+    const int n = g.nph;
+    const int s = __ffs(n) - 1;
+    const int o = n >> s;
+    const int P = 1 << s;
+    const bool paired = g.start_s != g.start_n;
+    cx<T> *tw = reinterpret_cast<cx<T> *>(smem_raw);
+    cx<T> *buf = tw + n;
+    cx<T> *src = buf + (int64_t)MT * n;
+    fill_twiddles(tw, n, +1);
+    const int L1 = lmax + 1;
+    // spectrum of the packed sequence: c_k = CN_k + i CS_k
+    for (int idx = threadIdx.x; idx < MT * n; idx += blockDim.x) {
+        const int b = idx / n;
+        const int k = idx - b * n;
+        const int64_t mb = b0 + b;
+        double cnx = 0, cny = 0, csx = 0, csy = 0;
+        if (mb < nmaps) {
+            // m = k + t n
+            for (int m = k; m <= lmax; m += n) {
+                const T *gp = G + ((int64_t)(0 * L1 + m) * nrn + r) * ldG + 2 * mb;
+                const T *gq = G + ((int64_t)(1 * L1 + m) * nrn + r) * ldG + 2 * mb;
+                double gnx = (double)gp[0] + (double)gq[0], gny = (double)gp[1] + (double)gq[1];
+                double gsx = (double)gp[0] - (double)gq[0], gsy = (double)gp[1] - (double)gq[1];
+                if (m == 0) { gny = 0; gsy = 0; }
+                double sn = 0.0, cs = 1.0;
+                if (g.phi0_den != 0) sincospi((double)m / (double)g.phi0_den, &sn, &cs);
+                cnx += gnx * cs - gny * sn; cny += gnx * sn + gny * cs;
+                csx += gsx * cs - gsy * sn; csy += gsx * sn + gsy * cs;
+            }
+            // m = -k + t n, m >= 1: conj(G_m) e^{-i m phi0}
+            const int kk = (n - k) % n;
+            for (int m = (kk == 0 ? n : kk); m <= lmax; m += n) {
+                const T *gp = G + ((int64_t)(0 * L1 + m) * nrn + r) * ldG + 2 * mb;
+                const T *gq = G + ((int64_t)(1 * L1 + m) * nrn + r) * ldG + 2 * mb;
+                const double gnx = (double)gp[0] + (double)gq[0], gny = -((double)gp[1] + (double)gq[1]);
+                const double gsx = (double)gp[0] - (double)gq[0], gsy = -((double)gp[1] - (double)gq[1]);
+                double sn = 0.0, cs = 1.0;
+                if (g.phi0_den != 0) sincospi(-(double)m / (double)g.phi0_den, &sn, &cs);
+                cnx += gnx * cs - gny * sn; cny += gnx * sn + gny * cs;
+                csx += gsx * cs - gsy * sn; csy += gsx * sn + gsy * cs;
+            }
+        }
+        // c = CN + i CS
+        const cx<T> v = {(T)(cnx - csy), (T)(cny + csx)};
+        if (o > 1) src[(int64_t)b * n + k] = v;
+        else buf[(int64_t)b * n + bitrev(k, s)] = v;
+    }
+    __syncthreads();
+    four_step<T>(buf, src, tw, n, o, s, MT);
+    for (int idx = threadIdx.x; idx < MT * n; idx += blockDim.x) {
+        const int b = idx / n;
+        const int j = idx - b * n;
+        const int64_t mb = b0 + b;
+        if (mb >= nmaps) continue;
+        const cx<T> z = buf[(int64_t)b * n + (j % o) * P + j / o];
+        maps[mb * npix + g.start_n + j] = (double)z.x;
+        if (paired) maps[mb * npix + g.start_s + j] = (double)z.y;
+    }
+}
+
+static int ring_mt(const Plan &p, size_t elem) {
+    const size_t n = (size_t)(4 * p.nside);
+    for (int mt = 4; mt >= 1; mt >>= 1)
+        if (n * elem * (1 + 2 * (size_t)mt) <= 200 * 1024) return mt;
+    return 0;
+}
+
+void launch_ring_analysis(const Plan &p, const double *maps, int64_t nmaps, double *F, cudaStream_t st) {
+    const int MT = ring_mt(p, sizeof(cx<double>));
+    const size_t smem = (size_t)(4 * p.nside) * sizeof(cx<double>) * (1 + 2 * MT);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_ring_analysis<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        attr_set = true;
+    }
+    dim3 grid((unsigned)p.nrn, (unsigned)((nmaps + MT - 1) / MT));
+    const double w = 4.0 * M_PI / (double)p.npix;
+    k_ring_analysis<double><<<grid, 256, smem, st>>>(p.d_rings, (int)p.nrn, p.lmax, w, p.npix, maps, nmaps,
+                                                     MT, F, 2 * nmaps);
+}
+
+void launch_ring_synthesis(const Plan &p, const double *G, int64_t nmaps, double *maps, cudaStream_t st) {
+    const int MT = ring_mt(p, sizeof(cx<double>));
+    const size_t smem = (size_t)(4 * p.nside) * sizeof(cx<double>) * (1 + 2 * MT);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_ring_synthesis<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        attr_set = true;
+    }
+    dim3 grid((unsigned)p.nrn, (unsigned)((nmaps + MT - 1) / MT));
+    k_ring_synthesis<double><<<grid, 256, smem, st>>>(p.d_rings, (int)p.nrn, p.lmax, G, 2 * nmaps, nmaps, MT,
+                                                      p.npix, maps);
+}
+
+}  // namespace sfb

@@ -1,0 +1,194 @@
+// Internal declarations of the GB300 SFB library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/sfb_gpu.h"
+
+namespace sfb {
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+void set_error(const std::string &msg);
+int fail(int code, const std::string &msg);
+
+#define SFB_CUDA_TRY(expr)                                                        \
+    do {                                                                          \
+        cudaError_t e_ = (expr);                                                  \
+        if (e_ != cudaSuccess)                                                    \
+            return ::sfb::fail(SFB_ECUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+#define SFB_TRY(expr)                  \
+    do {                               \
+        int s_ = (expr);               \
+        if (s_ != SFB_OK) return s_;   \
+    } while (0)
+
+// Device error word bits (set by kernels with atomicOr, read by the host).
+enum : int {
+    ERR_NONFINITE_INPUT = 1,
+    ERR_THETA_RANGE = 2,
+    ERR_NONFINITE_OUTPUT = 4,
+};
+
+// ---------------------------------------------------------------------------
+// HEALPix ring geometry of the north half (rings i = 1..2*nside, equator last)
+// ---------------------------------------------------------------------------
+struct RingGeom {
+    int32_t nph;        // pixels on the ring
+    int32_t phi0_den;   // phi of first pixel = pi / phi0_den  (0 -> phi0 = 0)
+    int64_t start_n;    // first pixel of the north ring
+    int64_t start_s;    // first pixel of the mirrored south ring (== start_n on the equator)
+    double z;           // cos(theta) of the north ring
+    double sth;         // sin(theta)
+    double cfold;       // 2 for a north/south pair, 1 for the equator
+};
+
+// ---------------------------------------------------------------------------
+// Device buffers owned by the plan
+// ---------------------------------------------------------------------------
+template <typename T>
+struct DevBuf {
+    T *ptr = nullptr;
+    size_t n = 0;  // elements
+};
+
+struct Plan {
+    int device = 0;
+    // modes
+    int64_t nside = 0, npix = 0, nrn = 0;  // nrn = 2*nside north rings incl. equator
+    int lmax = 0, nmax = 0;
+    std::vector<int64_t> lmax_n;
+    int64_t npairs = 0, nlmsize = 0, lmsize = 0;
+    double rmin = 0, rmax = 0;
+    int niter = 3;
+    int precision = SFB_FP64;
+    int radial_mode = SFB_RADIAL_POLY;
+    // radial basis (poly mode)
+    int pieces = 1, degree = 0;
+    int64_t nbasis = 0;             // pieces*(degree+1) + 2
+    double radial_error = 0;
+    // host copies
+    std::vector<int64_t> h_spl_off;
+    std::vector<RingGeom> h_rings;
+    // device tables
+    RingGeom *d_rings = nullptr;
+    double *d_lam = nullptr;        // Legendre table, FP64
+    int64_t *d_lam_off = nullptr;   // [2*(lmax+1)] offset of block (m, parity)
+    int64_t lam_elems = 0;
+    int64_t *d_spl_off = nullptr;
+    double *d_spl_x = nullptr, *d_spl_y = nullptr, *d_spl_ypp = nullptr;
+    int32_t *d_pair_l = nullptr;    // [npairs]
+    int32_t *d_pair_n = nullptr;    // [npairs] 1-based n
+    int64_t *d_pair_lmoff = nullptr;// unused placeholder
+    int32_t *d_out_pair = nullptr;  // [nlmsize] pair index of each a_nlm
+    int32_t *d_out_lm = nullptr;    // [nlmsize] l(l+1)/2+m of each a_nlm
+    double *d_coef = nullptr;       // [npairs * nbasis] radial coefficients (poly mode)
+    int *d_err = nullptr;           // device error word
+    // workspaces (grow on demand)
+    DevBuf<double> maps;            // [nmaps_alloc * npix]
+    DevBuf<double> fbuf, gbuf, rbuf;// ring Fourier buffers [2][lmax+1][nrn][2*nmaps]
+    DevBuf<double> alm;             // [lmsize][2*nmaps]
+    DevBuf<double> scratch;         // galaxy/window/output staging
+    DevBuf<double> scratch2;
+    int64_t device_bytes = 0;
+};
+
+int grow(Plan &p, DevBuf<double> &b, size_t n);
+
+// ---------------------------------------------------------------------------
+// kernels (launch wrappers; all enqueue on `st`)
+// ---------------------------------------------------------------------------
+void launch_legendre_table(const Plan &p, cudaStream_t st);
+void launch_deposit_poly(const Plan &p, const double *rtp, const double *w, int64_t ngal, double *maps,
+                         cudaStream_t st);
+void launch_ring_analysis(const Plan &p, const double *maps, int64_t nmaps, double *F, cudaStream_t st);
+void launch_ring_synthesis(const Plan &p, const double *G, int64_t nmaps, double *maps, cudaStream_t st);
+void launch_leg_analysis(const Plan &p, const double *F, int64_t ncol, double *A, bool accumulate,
+                         cudaStream_t st);
+void launch_leg_synthesis(const Plan &p, const double *A, int64_t ncol, double *G, cudaStream_t st);
+void launch_fold_residual(const Plan &p, const double *F, const double *G, int64_t ncol, double *R,
+                          cudaStream_t st);
+void launch_radial_coeffs(const Plan &p, const double *gl_x, const double *pq, int Q, double *coef,
+                          cudaStream_t st);
+void launch_project_poly(const Plan &p, const double *A, int64_t ldA, double scale, int window_kind,
+                         const double *w_ln, int64_t mask_col, const double *Awin, int64_t ldW,
+                         double *out, cudaStream_t st);
+void launch_transpose(const double *in, int64_t rows, int64_t cols, double *out, cudaStream_t st);
+void launch_check_finite(const double *x, int64_t n, int *err, cudaStream_t st);
+void launch_ang2pix(int64_t nside, const double *theta, const double *phi, int64_t n, int64_t *pix,
+                    cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// shared device helpers
+// ---------------------------------------------------------------------------
+#ifdef __CUDACC__
+// 0-based HEALPix RING pixel of (z = cos theta, phi); the HEALPix paper
+// algorithm (Gorski et al. 2005).  Every operation is an explicitly rounded
+// IEEE op (no FMA contraction) so the integer result matches a plain FP64
+// evaluation of the same expressions, operation by operation.
+__device__ __forceinline__ int64_t ang2pix_ring_z(int64_t nside, double z, double phi) {
+    const double inv_halfpi = 0.63661977236758134308;  // 2/pi
+    const double za = fabs(z);
+    double tt = fmod(__dmul_rn(phi, inv_halfpi), 4.0);
+    if (tt < 0) tt = __dadd_rn(tt, 4.0);
+    if (tt >= 4.0) tt = 0.0;
+    const int64_t ns = nside;
+    const double dns = (double)ns;
+    if (za <= 2.0 / 3.0) {
+        const double temp1 = __dmul_rn(dns, __dadd_rn(0.5, tt));
+        const double temp2 = __dmul_rn(__dmul_rn(dns, z), 0.75);
+        const int64_t jp = (int64_t)floor(__dsub_rn(temp1, temp2));
+        const int64_t jm = (int64_t)floor(__dadd_rn(temp1, temp2));
+        const int64_t ir = ns + 1 + jp - jm;
+        const int64_t kshift = 1 - (ir & 1);
+        const int64_t t1 = jp + jm - ns + kshift + 1 + 8 * ns;
+        const int64_t ip = (t1 >> 1) % (4 * ns);
+        const int64_t pix = 2 * ns * (ns - 1) + (ir - 1) * 4 * ns + ip;
+        // rounding at |z| = 2/3 could put ir one ring outside the belt; keep
+        // the index inside the map (the oracle applies the same guard)
+        return pix < 0 ? 0 : (pix >= 12 * ns * ns ? 12 * ns * ns - 1 : pix);
+    }
+    const double tp = __dsub_rn(tt, floor(tt));
+    const double tmp = __dmul_rn(dns, __dsqrt_rn(__dmul_rn(3.0, __dsub_rn(1.0, za))));
+    const int64_t jp = (int64_t)floor(__dmul_rn(tp, tmp));
+    const int64_t jm = (int64_t)floor(__dmul_rn(__dsub_rn(1.0, tp), tmp));
+    const int64_t ir = jp + jm + 1;
+    int64_t ip = (int64_t)floor(__dmul_rn(tt, (double)ir));
+    ip = ip % (4 * ir);
+    if (z > 0) return 2 * ir * (ir - 1) + ip;
+    return 12 * ns * ns - 2 * ir * (ir + 1) + ip;
+}
+
+// Cubic spline with boundary extrapolation on knots x[0..N-1]
+// (reference src/Splines.jl:64-101,327-357).
+__device__ __forceinline__ double spline_eval_dev(const double *x, const double *y, const double *ypp,
+                                                  int64_t N, double r) {
+    if (r < x[0]) return y[0];
+    if (r > x[N - 1]) return y[N - 1];
+    // largest i with x[i] <= r, clamped to the last piece
+    int64_t lo = 0, hi = N - 1;
+    while (hi - lo > 1) {
+        int64_t mid = (lo + hi) >> 1;
+        if (r >= x[mid]) lo = mid; else hi = mid;
+    }
+    const int64_t i = lo;
+    const double x0 = x[i];
+    const double h = x[i + 1] - x0;
+    const double t = (r - x0) / h;
+    const double h2 = h * h;
+    const double b = h2 * ypp[i] / 2;
+    const double a = h2 * (ypp[i + 1] - ypp[i]) / 6;
+    const double d = y[i];
+    const double c = y[i + 1] - a - b - d;
+    return d + t * (c + t * (b + t * a));
+}
+#endif
+
+}  // namespace sfb

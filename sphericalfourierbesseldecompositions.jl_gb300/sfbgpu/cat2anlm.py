@@ -1,0 +1,216 @@
+"""Catalogue / field -> SFB coefficients on the GPU (host API).
+
+Mirrors the reference's ``Cat2Anlm`` module (``src/cat2anlm.jl:33-34``):
+``cat2amln`` (alias ``cat2nlm``), ``field2anlm``, ``anlm2field``,
+``win_rhat_ln`` and ``winweights2galweights``, with the same argument meaning.
+Every transform runs through the C ABI of ``libsfbgpu.so``; there is no CPU
+path, and a missing library or device raises.
+
+Array conventions follow Julia's memory layout: ``rθϕ`` is (3, N), a field is
+(nr, npix), a dense window transform is (npix, lmax+1, nmax); coefficient
+vectors are complex128 of length ``getnlmsize(amodes)`` in the reference
+order.
+"""
+
+import numpy as np
+
+from . import _capi as capi
+from .healpix import nside2npix
+from .modes import getnlmsize
+from .windows import SeparableArray
+
+__all__ = ["GPUPlan", "get_plan", "cat2amln", "cat2nlm", "field2anlm", "anlm2field", "win_rhat_ln",
+           "map2alm", "ang2pix_ring"]
+
+_PRECISION = {"fp64": capi.SFB_FP64, "mixed": capi.SFB_MIXED}
+_RADIAL = {"poly": capi.SFB_RADIAL_POLY, "spline": capi.SFB_RADIAL_SPLINE}
+
+
+class GPUPlan:
+    """A device plan for one AnlmModes (tables uploaded once)."""
+
+    def __init__(self, amodes, niter=3, precision="fp64", radial="poly", pieces=0, degree=0, tol=0.0,
+                 nside=None):
+        self.amodes = amodes
+        pairs = amodes.pairs()
+        spl = amodes.basisfunctions.spline
+        xs = [spl[pr][0] for pr in pairs]
+        off = np.zeros(len(pairs) + 1, np.int64)
+        off[1:] = np.cumsum([len(x) for x in xs])
+        self._x = np.ascontiguousarray(np.concatenate(xs))
+        self._y = np.ascontiguousarray(np.concatenate([spl[pr][1] for pr in pairs]))
+        self._ypp = np.ascontiguousarray(np.concatenate([spl[pr][2] for pr in pairs]))
+        self._off = off
+        self._lmax_n = np.ascontiguousarray(amodes.lmax_n, np.int64)
+        d = capi.PlanDesc()
+        d.nside = int(amodes.nside if nside is None else nside)
+        d.lmax = amodes.lmax
+        d.nmax = amodes.nmax
+        d.lmax_n = self._lmax_n.ctypes.data_as(capi._i64p)
+        d.rmin = amodes.rmin
+        d.rmax = amodes.rmax
+        d.spl_offset = self._off.ctypes.data_as(capi._i64p)
+        d.spl_x = self._x.ctypes.data_as(capi._dp)
+        d.spl_y = self._y.ctypes.data_as(capi._dp)
+        d.spl_ypp = self._ypp.ctypes.data_as(capi._dp)
+        d.niter = niter
+        d.precision = _PRECISION[precision]
+        d.radial_mode = _RADIAL[radial]
+        d.radial_pieces = pieces
+        d.radial_degree = degree
+        d.radial_tol = tol
+        h = capi.C.c_void_p()
+        capi.check(capi.lib.sfb_plan_create(capi.C.byref(d), capi.C.byref(h)))
+        self.handle = h
+        self.nside = d.nside
+        self.npix = nside2npix(d.nside)
+        self.nlmsize = getnlmsize(amodes)
+
+    def info(self):
+        i = capi.PlanInfo()
+        capi.check(capi.lib.sfb_plan_get_info(self.handle, capi.C.byref(i)))
+        return {f: getattr(i, f) for f, _ in capi.PlanInfo._fields_}
+
+    def set_precision(self, precision):
+        capi.check(capi.lib.sfb_set_precision(self.handle, _PRECISION[precision]))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            capi.lib.sfb_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def get_plan(amodes, **opts):
+    """Plan cached on the AnlmModes object per option set."""
+    cache = amodes.__dict__.setdefault("_gpu_plans", {})
+    key = tuple(sorted(opts.items()))
+    if key not in cache:
+        cache[key] = GPUPlan(amodes, **opts)
+    return cache[key]
+
+
+def _window_struct(win_rhat_ln, amodes, npix, keep):
+    w = capi.Window()
+    if win_rhat_ln is None:
+        w.kind = capi.SFB_WINDOW_ZERO
+        return w
+    if isinstance(win_rhat_ln, SeparableArray):
+        mask = np.ascontiguousarray(win_rhat_ln.arr1, float)
+        wln = np.asfortranarray(win_rhat_ln.arr2, float)
+        if mask.shape != (npix,) or wln.shape != (amodes.lmax + 1, amodes.nmax):
+            raise ValueError("separable win_rhat_ln must be (mask[npix], w_ln[lmax+1, nmax])")
+        keep += [mask, wln]
+        w.kind = capi.SFB_WINDOW_SEPARABLE
+        w.mask = mask.ctypes.data_as(capi._dp)
+        w.w_ln = wln.ctypes.data_as(capi._dp)
+        return w
+    W = np.asfortranarray(win_rhat_ln, float)
+    if W.shape != (npix, amodes.lmax + 1, amodes.nmax):
+        raise ValueError(f"dense win_rhat_ln must have shape {(npix, amodes.lmax + 1, amodes.nmax)}")
+    keep.append(W)
+    w.kind = capi.SFB_WINDOW_DENSE
+    w.dense = W.ctypes.data_as(capi._dp)
+    return w
+
+
+def cat2amln(rtp, amodes, nbar, win_rhat_ln, weight=None, **plan_opts):
+    """a_nlm of a catalogue (reference cat2amln, src/cat2anlm.jl:257-310).
+
+    rtp: (3, N) array of r, theta, phi.  win_rhat_ln: dense (npix, lmax+1, nmax)
+    array, ``SeparableArray(mask, w_ln)``, or None for a zero window term.
+    weight: (N,) or None (ones).  Extra keyword arguments select the plan
+    (precision="fp64"|"mixed", radial="poly"|"spline", niter=3, ...).
+    """
+    plan = get_plan(amodes, **plan_opts)
+    rtp = np.asarray(rtp, float)
+    if rtp.ndim != 2 or rtp.shape[0] != 3:
+        raise ValueError("rθϕ must be a 3 x N array")
+    N = rtp.shape[1]
+    gal = np.ascontiguousarray(rtp.T)            # (N, 3): r, theta, phi per galaxy
+    w = None
+    if weight is not None and len(weight) > 0:
+        w = np.ascontiguousarray(weight, float)
+        if w.shape != (N,):
+            raise ValueError("weight must have one entry per galaxy")
+    keep = []
+    win = _window_struct(win_rhat_ln, amodes, plan.npix, keep)
+    out = np.empty(plan.nlmsize, np.complex128)
+    capi.check(capi.lib.sfb_cat2amln(plan.handle, capi.ptr(gal) if N else None, capi.ptr(w), N, float(nbar),
+                                     capi.C.byref(win), capi.ptr(out)))
+    return out
+
+
+cat2nlm = cat2amln
+
+
+def field2anlm(f_xyz, wmodes, amodes, **plan_opts):
+    """SFB coefficients of an (nr, npix) field (reference field2anlm_v2, src/cat2anlm.jl:323-357)."""
+    plan = get_plan(amodes, **plan_opts)
+    f = np.asfortranarray(f_xyz, float)
+    if f.shape != (wmodes.nr, plan.npix):
+        raise ValueError("field must be nr x npix")
+    out = np.empty(plan.nlmsize, np.complex128)
+    capi.check(capi.lib.sfb_field2anlm(plan.handle, capi.ptr(f), wmodes.nr, wmodes.rmin, wmodes.rmax, capi.ptr(out)))
+    return out
+
+
+def anlm2field(f_nlm, wmodes, amodes, **plan_opts):
+    """(nr, npix) field of SFB coefficients (reference src/cat2anlm.jl:383-422)."""
+    plan = get_plan(amodes, **plan_opts)
+    a = np.ascontiguousarray(f_nlm, np.complex128)
+    if a.shape != (plan.nlmsize,):
+        raise ValueError("f_nlm must have getnlmsize(amodes) entries")
+    out = np.empty((wmodes.nr, plan.npix), order="F")
+    capi.check(capi.lib.sfb_anlm2field(plan.handle, capi.ptr(a), wmodes.nr, wmodes.rmin, wmodes.rmax, capi.ptr(out)))
+    return out
+
+
+def win_rhat_ln(win, wmodes, amodes, **plan_opts):
+    """Radial transform of a window (reference src/windows.jl:244-270).
+
+    Dense (nr, npix) -> (npix, lmax+1, nmax); SeparableArray(phi, mask) ->
+    SeparableArray(mask, w_ln[lmax+1, nmax]).  Entries with l > lmax_n[n] are NaN.
+    """
+    plan = get_plan(amodes, **plan_opts)
+    if isinstance(win, SeparableArray):
+        phi = np.ascontiguousarray(win.arr1, float)
+        mask = np.array(win.arr2, float)
+        if phi.shape != (wmodes.nr,):
+            raise ValueError("separable window must be SeparableArray(phi[nr], mask[npix])")
+        out = np.empty((amodes.lmax + 1, amodes.nmax), order="F")
+        capi.check(capi.lib.sfb_win_rhat_ln_separable(plan.handle, capi.ptr(phi), wmodes.nr, wmodes.rmin,
+                                                       wmodes.rmax, capi.ptr(out)))
+        return SeparableArray(mask, out, name1="mask", name2="w_ln")
+    W = np.asfortranarray(win, float)
+    if W.shape != (wmodes.nr, plan.npix):
+        raise ValueError("window must be nr x npix")
+    out = np.empty((plan.npix, amodes.lmax + 1, amodes.nmax), order="F")
+    capi.check(capi.lib.sfb_win_rhat_ln_dense(plan.handle, capi.ptr(W), wmodes.nr, wmodes.rmin, wmodes.rmax,
+                                              capi.ptr(out)))
+    return out
+
+
+def map2alm(maps, amodes, **plan_opts):
+    """Batched map2alm with niter refinement: (nmaps, npix) -> (nmaps, lmsize) complex,
+    index l(l+1)/2 + m (the transform behind mymap2alm!, src/healpix_helpers.jl:50-56)."""
+    plan = get_plan(amodes, **plan_opts)
+    m = np.ascontiguousarray(np.atleast_2d(maps), float)
+    L = amodes.lmax
+    out = np.empty((m.shape[0], (L + 1) * (L + 2) // 2), np.complex128)
+    capi.check(capi.lib.sfb_map2alm(plan.handle, capi.ptr(m), m.shape[0], capi.ptr(out)))
+    return out
+
+
+def ang2pix_ring(nside, theta, phi):
+    """0-based RING pixels computed on the GPU (Healpix.jl ang2pixRing minus one)."""
+    th = np.ascontiguousarray(theta, float).ravel()
+    ph = np.ascontiguousarray(phi, float).ravel()
+    out = np.empty(th.shape, np.int64)
+    capi.check(capi.lib.sfb_ang2pix_ring(int(nside), capi.ptr(th), capi.ptr(ph), len(th), capi.ptr(out)))
+    return out

@@ -1,0 +1,236 @@
+"""GPU parity tests: libsfbgpu.so (through the C ABI) against the CPU oracle.
+
+Tolerances (global relative error max|gpu - oracle| / max|oracle|):
+* FP64 transforms and the spline radial mode: 1e-11 (same algorithm, FP64,
+  only summation order differs);
+* the piecewise-Legendre radial mode: 2e-7 against the reference algorithm
+  (the expansion replaces the per-galaxy cubic spline; its projection error
+  is reported by the plan and stays near the spline's own interpolation
+  error).
+"""
+
+import numpy as np
+import pytest
+
+import sfbgpu
+from sfbgpu import _capi as capi
+from sfbgpu.cat2anlm import GPUPlan
+from helpers import catalogue, modes_dict, rel_err, round_sig, ylm
+from oracle import healpix as ohp, sfb as osfb, sht as osht
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def small():
+    a = sfbgpu.AnlmModes(0.03, 500.0, 1000.0, nside=16)
+    return a
+
+
+# ---------------------------------------------------------------- HEALPix ----
+@pytest.mark.parametrize("nside", [1, 2, 7, 32, 256, 1024])
+def test_ang2pix_bit_exact(nside):
+    rng = np.random.default_rng(nside)
+    n = 200_000
+    th = np.arccos(rng.uniform(-1, 1, n))
+    ph = rng.uniform(-2 * np.pi, 4 * np.pi, n)
+    # pixel centres, poles, equator, phi edges (inputs whose cosine is exact in
+    # every libm, so the pixel is determined by the ang2pix arithmetic alone)
+    cth, cph = ohp.pix2ang_ring(nside, np.arange(min(12 * nside * nside, 50_000)))
+    edge_th = np.array([0.0, np.pi, np.pi / 2, 1e-12, np.pi - 1e-12, 0.0, np.pi / 2])
+    edge_ph = np.array([0.0, 2 * np.pi, -1e-15, np.pi / 2, 2 * np.pi - 1e-15, 1e300, -7.0])
+    th = np.concatenate([th, cth, edge_th])
+    ph = np.concatenate([ph, cph, edge_ph])
+    gpu = sfbgpu.ang2pix_ring(nside, th, ph)
+    ref = ohp.ang2pix_ring(nside, th, ph)
+    assert np.all((gpu >= 0) & (gpu < 12 * nside * nside))
+    assert np.array_equal(gpu, ref), f"{np.sum(gpu != ref)} mismatches"
+
+
+# ---------------------------------------------------------------- SHT --------
+@pytest.mark.parametrize("nside,lmax,niter", [(8, 23, 0), (8, 23, 3), (16, 31, 3), (16, 47, 3), (5, 14, 2)])
+def test_map2alm_vs_oracle(nside, lmax, niter):
+    a = sfbgpu.AnlmModes.from_nmax_lmax(1, lmax, 500.0, 1000.0, nside=nside, cache=True)
+    plan = GPUPlan(a, niter=niter, radial="spline")
+    rng = np.random.default_rng(lmax)
+    maps = rng.normal(size=(3, 12 * nside * nside)) + 2.0
+    out = sfbgpu.cat2anlm.map2alm(maps, a, niter=niter, radial="spline")
+    S = osht.SHT(nside, lmax)
+    ref = S.map2alm(maps, niter=niter)
+    L = lmax
+    tri = np.array([ref[b, l, m] for b in range(3) for l in range(L + 1) for m in range(l + 1)]).reshape(3, -1)
+    assert rel_err(out, tri) < 1e-12
+    plan.close()
+
+
+# ---------------------------------------------------------------- cat2amln ---
+def _sep_window(a, nside, nr=50):
+    wm = sfbgpu.ConfigurationSpaceModes(a.rmin, a.rmax, nr, nside)
+    phi = np.exp(-((wm.r - 750.0) / 200.0) ** 2)
+    mask = sfbgpu.gen_mask(nside, 0.6)
+    md = modes_dict(a, nside)
+    m, wln = osfb.win_rhat_ln_separable(phi, mask, a.rmin, a.rmax, nr, md)
+    return wm, phi, mask, wln
+
+
+def test_cat2amln_spline_mode_vs_oracle(small):
+    a = small
+    md = modes_dict(a)
+    rtp, w = catalogue(30_000, a.rmin, a.rmax, seed=3, weights=True, rpad=20.0)
+    wm, phi, mask, wln = _sep_window(a, a.nside)
+    nbar = rtp.shape[1] / (4 / 3 * np.pi * (a.rmax ** 3 - a.rmin ** 3))
+    win = sfbgpu.SeparableArray(mask, wln, "mask", "w_ln")
+    gpu = sfbgpu.cat2amln(rtp, a, nbar, win, w, radial="spline")
+    ref = osfb.cat2amln(rtp, md, nbar, ("separable", mask, wln), w)
+    assert rel_err(gpu, ref) < 1e-11
+
+
+def test_cat2amln_poly_mode_vs_oracle(small):
+    a = small
+    md = modes_dict(a)
+    rtp, w = catalogue(30_000, a.rmin, a.rmax, seed=4, weights=True, rpad=20.0)
+    wm, phi, mask, wln = _sep_window(a, a.nside)
+    nbar = rtp.shape[1] / (4 / 3 * np.pi * (a.rmax ** 3 - a.rmin ** 3))
+    win = sfbgpu.SeparableArray(mask, wln, "mask", "w_ln")
+    gpu = sfbgpu.cat2amln(rtp, a, nbar, win, w, radial="poly")
+    ref = osfb.cat2amln(rtp, md, nbar, ("separable", mask, wln), w)
+    info = sfbgpu.get_plan(a, radial="poly").info()
+    assert info["radial_error"] < 1e-8
+    assert rel_err(gpu, ref) < 2e-7
+
+
+@pytest.mark.parametrize("radial", ["spline", "poly"])
+def test_cat2amln_dense_window_vs_oracle(small, radial):
+    a = small
+    md = modes_dict(a)
+    nr = 40
+    wm = sfbgpu.ConfigurationSpaceModes(a.rmin, a.rmax, nr, a.nside)
+    rng = np.random.default_rng(5)
+    win = rng.random((nr, wm.npix))
+    W = osfb.win_rhat_ln_dense(win, a.rmin, a.rmax, nr, md)
+    rtp, _ = catalogue(10_000, a.rmin, a.rmax, seed=6)
+    gpu = sfbgpu.cat2amln(rtp, a, 2e-4, W, None, radial=radial)
+    ref = osfb.cat2amln(rtp, md, 2e-4, ("dense", W), None)
+    assert rel_err(gpu, ref) < (1e-11 if radial == "spline" else 2e-7)
+
+
+def test_cat2amln_empty_catalogue_zero_window(small):
+    out = sfbgpu.cat2amln(np.zeros((3, 0)), small, 1.0, None)
+    assert np.all(out == 0)
+
+
+def test_cat2amln_errors(small):
+    a = small
+    rtp, _ = catalogue(100, a.rmin, a.rmax, seed=7)
+    bad = rtp.copy()
+    bad[0, 5] = np.nan
+    with pytest.raises(capi.SFBError) as e:
+        sfbgpu.cat2amln(bad, a, 1.0, None)
+    assert e.value.status == capi.SFB_ENONFINITE
+    bad = rtp.copy()
+    bad[1, 3] = 4.0
+    with pytest.raises(capi.SFBError) as e:
+        sfbgpu.cat2amln(bad, a, 1.0, None)
+    assert e.value.status == capi.SFB_ERANGE
+    with pytest.raises(capi.SFBError) as e:
+        sfbgpu.cat2amln(rtp, a, 0.0, None)
+    assert e.value.status == capi.SFB_ENONFINITE
+    # the plan stays usable after errors
+    out = sfbgpu.cat2amln(rtp, a, 1.0, None)
+    assert np.all(np.isfinite(out))
+
+
+# ---------------------------------------------------------------- fields -----
+def test_field2anlm_anlm2field_winrhat_vs_oracle(small):
+    a = small
+    md = modes_dict(a)
+    nr = 60
+    wm = sfbgpu.ConfigurationSpaceModes(a.rmin, a.rmax, nr, a.nside)
+    rng = np.random.default_rng(8)
+    f = rng.normal(size=(nr, wm.npix))
+    gpu = sfbgpu.field2anlm(f, wm, a)
+    ref = osfb.field2anlm(f, a.rmin, a.rmax, nr, md)
+    assert rel_err(gpu, ref) < 1e-11
+    fb = sfbgpu.anlm2field(ref, wm, a)
+    fr = osfb.anlm2field(ref, a.rmin, a.rmax, nr, md)
+    assert rel_err(fb, fr) < 1e-11
+    Wd = sfbgpu.win_rhat_ln(np.abs(f), wm, a)
+    Wr = osfb.win_rhat_ln_dense(np.abs(f), a.rmin, a.rmax, nr, md)
+    fin = np.isfinite(Wr)
+    assert np.array_equal(fin, np.isfinite(Wd))
+    assert rel_err(Wd[fin], Wr[fin]) < 1e-12
+    phi = np.abs(f[:, 0])
+    mask = np.ones(wm.npix)
+    Ws = sfbgpu.win_rhat_ln(sfbgpu.SeparableArray(phi, mask, "phi", "mask"), wm, a)
+    _, Wsr = osfb.win_rhat_ln_separable(phi, mask, a.rmin, a.rmax, nr, md)
+    fin = np.isfinite(Wsr)
+    assert rel_err(Ws.w_ln[fin], Wsr[fin]) < 1e-12
+
+
+# ------------------------------------------- reference known-answer tests ----
+def test_point_source_kat_nside256():
+    """reference test/test_cat2anlm.jl:153-196 (nside 256, nmax 2, lmax 3, nr 100)."""
+    a = sfbgpu.AnlmModes.from_nmax_lmax(2, 3, 500.0, 1000.0, nside=256)
+    nr, ns = 100, 256
+    wm = sfbgpu.ConfigurationSpaceModes(a.rmin, a.rmax, nr, ns)
+    f = np.zeros((nr, wm.npix))
+    Op = 4 * np.pi / wm.npix
+    for j in range(0, wm.npix, 3 * ns * ns + 7):
+        for i in range(0, nr, 41):
+            f[i, j] = 1
+            an1 = round_sig(sfbgpu.field2anlm(f, wm, a), 6)
+            th, ph = ohp.pix2ang_ring(ns, j)
+            an0 = np.empty_like(an1)
+            for k in range(1, sfbgpu.getnlmsize(a) + 1):
+                n, l, m = sfbgpu.getnlm(a, k)
+                g = a.basisfunctions(n, l, wm.r[i])
+                an0[k - 1] = round_sig(wm.dr * wm.r[i] ** 2 * g * np.conj(ylm(l, m, th, ph)) * Op, 6)
+            assert np.linalg.norm(an0 - an1) <= 1e-5 * max(np.linalg.norm(an0), np.linalg.norm(an1))
+            f[i, j] = 0
+
+
+@pytest.mark.parametrize("radial", ["spline", "poly"])
+def test_basis_function_kat(radial):
+    """reference test/test_cat2anlm.jl:32-67: window = g_nl Y^real_lm, -cat2amln(empty) = unit vector."""
+    a = sfbgpu.AnlmModes(0.02, 0.0, 1000.0, nside=32)
+    nr = 200
+    wm = sfbgpu.ConfigurationSpaceModes(a.rmin, a.rmax, nr, a.nside)
+    th, ph = ohp.pix2ang_ring(32, np.arange(wm.npix))
+    rng = np.random.default_rng(9)
+    for idx in rng.integers(1, sfbgpu.getnlmsize(a) + 1, 6):
+        n, l, m = sfbgpu.getnlm(a, int(idx))
+        g = a.basisfunctions(n, l, wm.r)
+        y = ylm(l, m, th, ph)
+        yr = y.real if m == 0 else np.sqrt(2) * (-1) ** m * y.real
+        W = sfbgpu.win_rhat_ln(np.outer(g, yr), wm, a, radial=radial)
+        an = -sfbgpu.cat2amln(np.zeros((3, 0)), a, 3e-4, W, None, radial=radial)
+        exp = 1 if m == 0 else (-1) ** m / np.sqrt(2)
+        k = int(idx) - 1
+        assert abs(an[k] - exp) < 1e-3
+        assert np.max(np.abs(np.delete(an, k))) <= 2e-3
+
+
+@pytest.mark.parametrize("radial", ["spline", "poly"])
+def test_field2anlm_v1_equals_v2(radial):
+    """reference test/test_cat2anlm.jl:235-258: -cat2amln(empty, win_rhat_ln(f)) == field2anlm(f)."""
+    a = sfbgpu.AnlmModes.from_nmax_lmax(10, 10, 500.0, 1000.0, nside=32)
+    wm = sfbgpu.ConfigurationSpaceModes.from_amodes(a, 100)
+    f = np.random.default_rng(10).random((wm.nr, wm.npix))
+    v1 = -sfbgpu.cat2amln(np.zeros((3, 0)), a, 1.0, sfbgpu.win_rhat_ln(f, wm, a), None, radial=radial)
+    v2 = sfbgpu.field2anlm(f, wm, a)
+    assert np.allclose(v1, v2, rtol=np.sqrt(np.finfo(float).eps), atol=0)
+
+
+def test_anlm2field_round_trip():
+    """reference test/test_cat2anlm.jl:261-289 (rtol 1e-4 after the first projection)."""
+    a = sfbgpu.AnlmModes.from_nmax_lmax(10, 10, 500.0, 1000.0, nside=32)
+    wm = sfbgpu.ConfigurationSpaceModes.from_amodes(a, 100)
+    f1 = np.random.default_rng(11).random((wm.nr, wm.npix))
+    a1 = sfbgpu.field2anlm(f1, wm, a)
+    f2 = sfbgpu.anlm2field(a1, wm, a)
+    a2 = sfbgpu.field2anlm(f2, wm, a)
+    f3 = sfbgpu.anlm2field(a2, wm, a)
+    a3 = sfbgpu.field2anlm(f3, wm, a)
+    assert np.linalg.norm(f2 - f3) <= 1e-4 * np.linalg.norm(f2)
+    assert np.linalg.norm(a1 - a2) <= 1e-4 * np.linalg.norm(a1)
+    assert np.linalg.norm(a2 - a3) <= 1e-4 * np.linalg.norm(a2)
