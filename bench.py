@@ -1,0 +1,452 @@
+#!/usr/bin/env python3
+"""cat2amln throughput on one GB300: galaxies/s at nside 256, kmax 0.1.
+
+Workload (the reference's nside-256 configuration, seeded synthetic data):
+AnlmModes(kmax=0.1, rmin=500, rmax=2500; nside=256), potential boundary
+(lmax 238, 7,520 (n,l) pairs, nlmsize 551,664); window = polar cap
+theta < 60 deg x Gaussian radial selection (mean 1500, sigma 400) on nr=1000
+shells, passed as a separable win_rhat_ln; catalogue = Poisson draw of
+nbar*W with E[N] = 1e7, FP64 weights U[0.5, 1.5].
+
+One step = one cat2amln call.  `value` uses device-resident inputs
+(sfb_cat2amln_device on the current torch stream, CUDA events around the K
+timed steps); `e2e` uses the host-pointer C-ABI call from pinned memory
+(H2D + D2H inside the timed region, host wall clock).  Inputs (320 MB) are
+larger than the 129 MB L2, so no explicit flush is needed between steps.
+
+--impl reference times the reference algorithm (per-(n,l) spline scatter +
+niter=3 map2alm, CPU restatement in oracle/) on the host cores: each step is
+a sample of (n,l) pairs run in parallel, extrapolated to all pairs.
+"""
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "sphericalfourierbesseldecompositions.jl_gb300")
+for _p in (PKG, ROOT):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "cat2amln galaxies/s at nside256 kmax0.1: mixed vs FP64 GPU, ≤1e-7 rel err"
+KMAX, RMIN, RMAX, NSIDE, NR = 0.1, 500.0, 2500.0, 256, 1000
+NGAL_MEAN = 10_000_000
+CAP_DEG, RMEAN, RSIG = 60.0, 1500.0, 400.0
+WORKLOAD = "cat2amln kmax=0.1 rmin=500 rmax=2500 nside=256 nr=1000 N~Poisson(1e7) cap60 x gauss(1500,400) w~U[0.5,1.5]"
+
+
+def make_catalogue(seed=2):
+    """Seeded Poisson draw of nbar*W(r, theta) (rejection sampling in r, uniform in the cap)."""
+    rng = np.random.default_rng(seed)
+    n = int(rng.poisson(NGAL_MEAN))
+    f = lambda r: r * r * np.exp(-(r - RMEAN) ** 2 / (2 * RSIG ** 2))
+    rpk = (RMEAN + np.sqrt(RMEAN ** 2 + 8 * RSIG ** 2)) / 2
+    fmax = f(rpk)
+    rs = []
+    have = 0
+    while have < n:
+        r = rng.uniform(RMIN, RMAX, 2 * (n - have) + 1000)
+        r = r[rng.random(r.size) * fmax <= f(r)]
+        rs.append(r)
+        have += r.size
+    r = np.concatenate(rs)[:n]
+    mu = rng.uniform(np.cos(np.radians(CAP_DEG)), 1.0, n)
+    th = np.arccos(mu)
+    ph = rng.uniform(0.0, 2 * np.pi, n)
+    w = rng.uniform(0.5, 1.5, n)
+    return np.ascontiguousarray(np.stack([r, th, ph], axis=1)), w    # (N, 3) = Julia 3xN memory
+
+
+def window_arrays(sfbgpu, amodes):
+    wm = sfbgpu.ConfigurationSpaceModes(RMIN, RMAX, NR, NSIDE)
+    phi = np.exp(-(wm.r - RMEAN) ** 2 / (2 * RSIG ** 2))
+    th, _ = sfbgpu.pix2ang_ring(NSIDE, np.arange(wm.npix))
+    mask = (th < np.radians(CAP_DEG)).astype(float)
+    return wm, phi, mask
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples while the timed region runs."""
+
+    FIELDS = ["clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.active",
+              "clocks_event_reasons.hw_slowdown", "clocks_event_reasons.hw_thermal_slowdown",
+              "clocks_event_reasons.sw_thermal_slowdown", "clocks_event_reasons.sw_power_cap"]
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + ",".join(self.FIELDS),
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------- reference arm
+_W = {}
+
+
+def _ref_worker_init(shm_names, n, lmax, nside):
+    from multiprocessing import shared_memory
+    from oracle import sht as osht
+    blocks = {}
+    for key, name in shm_names.items():
+        s = shared_memory.SharedMemory(name=name)
+        blocks[key] = s
+    _W["shm"] = blocks
+    dt = {"r": np.float64, "w": np.float64, "pix": np.int64}
+    for key, s in blocks.items():
+        _W[key] = np.ndarray((n,), dtype=dt[key], buffer=s.buf)
+    _W["sht"] = osht.SHT(nside, lmax)
+    _W["nside"] = nside
+
+
+def _ref_worker_pair(args):
+    """One (n,l) iteration of the reference loop (src/cat2anlm.jl:281-306)."""
+    (n, l), (x, y, ypp), nbar, mask, wln = args
+    from oracle import sfb as osfb
+    npix = 12 * _W["nside"] ** 2
+    vals = _W["w"] * osfb.spline_eval(x, y, ypp, _W["r"])
+    m = np.bincount(_W["pix"], weights=vals, minlength=npix).astype(float)
+    m *= 1 / (nbar * 4 * np.pi / npix)
+    m = m - mask * wln
+    alm = _W["sht"].map2alm(m[None, :], niter=3)
+    return alm[0, l, :l + 1]
+
+
+def run_reference_sample(amodes, gal, w, nbar, mask, wln_arr, steps, warmup, workers, pairs_per_step,
+                         emit=True, config=None):
+    """Time the CPU reference algorithm on a sample of (n,l) pairs; returns galaxies/s per step."""
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+    from multiprocessing import shared_memory
+    from oracle import healpix as ohp
+    N = gal.shape[0]
+    # sortout + ang2pix: once per cat2amln call in the reference (src/cat2anlm.jl:259-264)
+    t0 = time.perf_counter()
+    p = np.argsort(gal[:, 0], kind="stable")
+    r = np.ascontiguousarray(gal[p, 0])
+    pix = ohp.ang2pix_ring(NSIDE, gal[p, 1], gal[p, 2])
+    ws = np.ascontiguousarray(w[p])
+    t_setup = time.perf_counter() - t0
+    shms = {}
+    for key, arr in (("r", r), ("w", ws), ("pix", pix)):
+        s = shared_memory.SharedMemory(create=True, size=arr.nbytes)
+        np.ndarray(arr.shape, dtype=arr.dtype, buffer=s.buf)[:] = arr
+        shms[key] = s
+    pairs = amodes.pairs()
+    spl = amodes.basisfunctions.spline
+    ctx = mp.get_context("spawn")
+    vals = []
+    try:
+        with ProcessPoolExecutor(workers, mp_context=ctx, initializer=_ref_worker_init,
+                                 initargs=({k: s.name for k, s in shms.items()}, N, amodes.lmax, NSIDE)) as ex:
+            list(ex.map(_ref_worker_pair, [(pairs[0], spl[pairs[0]], nbar, mask, wln_arr[0, 0])] * workers))
+            for step in range(warmup + steps):
+                idx = np.linspace(0, len(pairs) - 1, pairs_per_step).astype(int)
+                idx = (idx + step * 37) % len(pairs)
+                args = [(pairs[i], spl[pairs[i]], nbar, mask, wln_arr[pairs[i][1], pairs[i][0] - 1]) for i in idx]
+                t0 = time.perf_counter()
+                list(ex.map(_ref_worker_pair, args))
+                dt = time.perf_counter() - t0
+                total = t_setup + dt * len(pairs) / len(idx)
+                if step >= warmup:
+                    vals.append(N / total)
+    finally:
+        for s in shms.values():
+            s.close()
+            s.unlink()
+    return vals, t_setup
+
+
+# ----------------------------------------------------------------------------- GPU arm
+def roofline_for(stage, ms_per_launch, launches, plan_info, peaks, nm):
+    """Algorithmic work of one launch of the dominant stage and its fraction of the measured peak."""
+    L = 238
+    lmsize = (L + 1) * (L + 2) // 2
+    nrn = 2 * NSIDE
+    npix = 12 * NSIDE ** 2
+    ncol = 2 * nm
+    if stage in ("leg_analysis", "leg_synthesis"):
+        flops = 2.0 * lmsize * nrn * ncol                 # one contraction over all m (N/S symmetry counted once)
+        achieved = flops / (ms_per_launch * 1e-3) / 1e12
+        return {"bound": "fp64", "achieved": achieved, "unit": "TFLOP/s", "flops_per_launch": flops}
+    if stage == "ring_fft":
+        byts = 8.0 * nm * npix + 8.0 * 2 * 2 * (L + 1) * nrn * nm
+        achieved = byts / (ms_per_launch * 1e-3) / 1e9
+        return {"bound": "hbm", "achieved": achieved, "unit": "GB/s", "bytes_per_launch": byts}
+    if stage == "deposit":
+        return {"bound": "hbm", "achieved": None, "unit": "GB/s"}
+    return {"bound": "hbm", "achieved": None, "unit": "GB/s"}
+
+
+def fp64_gemm_peak(torch):
+    """Measured FP64 GEMM throughput (cuBLAS DGEMM 8192^3, best of 5) in TFLOP/s."""
+    a = torch.randn(8192, 8192, dtype=torch.float64, device="cuda")
+    b = torch.randn(8192, 8192, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e9
+    for _ in range(5):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b
+    return 2 * 8192 ** 3 / (best * 1e-3) / 1e12
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--ngal", type=int, default=0, help="override the catalogue size (testing)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-workers", type=int, default=0)
+    ap.add_argument("--cpu-pairs", type=int, default=0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    global NGAL_MEAN
+    if args.ngal:
+        NGAL_MEAN = args.ngal
+
+    import sfbgpu
+    cores = os.cpu_count() or 1
+    workers = args.cpu_workers or max(1, min(16, cores))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        amodes = sfbgpu.AnlmModes(KMAX, RMIN, RMAX, nside=NSIDE)
+        gal, w = make_catalogue()
+        wm, phi, mask = window_arrays(sfbgpu, amodes)
+        from oracle import sfb as osfb
+        md = dict(nmax=amodes.nmax, lmax=amodes.lmax, lmax_n=[int(v) for v in amodes.lmax_n], nside=NSIDE,
+                  splines=amodes.basisfunctions.spline, noff=amodes._noff)
+        _, wln = osfb.win_rhat_ln_separable(phi, mask, RMIN, RMAX, NR, md)
+        veff = sfbgpu.integrate_window(sfbgpu.SeparableArray(phi, mask), wm)
+        nbar = gal.shape[0] / veff
+        ppst = args.cpu_pairs or workers
+        vals, t_setup = run_reference_sample(amodes, gal, w, nbar, mask, wln, args.steps, args.warmup, workers, ppst)
+        v = float(np.median(vals))
+        line = {"metric": METRIC, "value": v, "unit": "galaxies/s", "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": gal.shape[0] / v * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "impl": "reference",
+                "config": {"workload": WORKLOAD, "ngal": int(gal.shape[0]), "npairs": len(amodes.pairs()),
+                           "l2": "inputs larger than L2 (CPU run)"},
+                "cpu_baseline": {"value": v, "unit": "galaxies/s", "cores": workers, "kind": "port",
+                                 "sample": f"{ppst} of {len(amodes.pairs())} (n,l) pairs per step (spline scatter "
+                                           f"+ niter=3 map2alm each) on {workers} processes, extrapolated by pair "
+                                           f"count, plus the once-per-call sort/ang2pix ({t_setup:.2f} s)"},
+                "e2e": {"value": v, "unit": "galaxies/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import torch
+    import torch.distributed as dist
+    from sfbgpu import _capi as capi
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+
+    amodes = sfbgpu.AnlmModes(KMAX, RMIN, RMAX, nside=NSIDE)
+    plan = sfbgpu.get_plan(amodes, precision=args.precision, radial="poly")
+    info = plan.info()
+    gal, w = make_catalogue(seed=2 + rank)
+    N = gal.shape[0]
+    wm, phi, mask = window_arrays(sfbgpu, amodes)
+    winsep = sfbgpu.win_rhat_ln(sfbgpu.SeparableArray(phi, mask, "phi", "mask"), wm, amodes,
+                                precision=args.precision, radial="poly")
+    wln = np.asfortranarray(winsep.w_ln)
+    veff = sfbgpu.integrate_window(sfbgpu.SeparableArray(phi, mask), wm)
+    nbar = N / veff
+    nlmsize = plan.nlmsize
+
+    dev = torch.device("cuda", local)
+    d_gal = torch.from_numpy(gal).to(dev)
+    d_w = torch.from_numpy(w).to(dev)
+    d_mask = torch.from_numpy(mask).to(dev)
+    d_wln = torch.from_numpy(np.ascontiguousarray(wln.T)).to(dev)    # element (l, n) at l + (lmax+1)(n-1)
+    d_out = torch.empty(2 * nlmsize, dtype=torch.float64, device=dev)
+    win = capi.Window()
+    win.kind = capi.SFB_WINDOW_SEPARABLE
+    win.mask = capi.C.cast(d_mask.data_ptr(), capi._dp)
+    win.w_ln = capi.C.cast(d_wln.data_ptr(), capi._dp)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        capi.check(capi.lib.sfb_cat2amln_device(plan.handle, capi.C.c_void_p(d_gal.data_ptr()),
+                                                capi.C.c_void_p(d_w.data_ptr()), N, float(nbar),
+                                                capi.C.byref(win), capi.C.c_void_p(d_out.data_ptr()),
+                                                capi.C.c_void_p(stream.cuda_stream)))
+
+    for _ in range(args.warmup):
+        step()
+    capi.check(capi.lib.sfb_set_profiling(plan.handle, 1))
+    clocks = ClockSampler(local)
+    clocks.start()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    l0 = capi.lib.sfb_launch_count()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clk = clocks.stop()
+    launches = capi.lib.sfb_launch_count() - l0
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    stage_ms = (capi.C.c_double * 7)()
+    stage_n = (capi.C.c_int64 * 7)()
+    capi.check(capi.lib.sfb_get_stage_times(plan.handle, stage_ms, stage_n))
+    capi.check(capi.lib.sfb_set_profiling(plan.handle, 0))
+    stages = {nm: {"ms_per_step": stage_ms[i] / args.steps, "launches_per_step": stage_n[i] / args.steps}
+              for i, nm in enumerate(capi.STAGES)}
+    value = N * world / (ms * 1e-3)
+
+    # end to end: host-pointer C-ABI call from pinned memory
+    h_gal = torch.from_numpy(gal).pin_memory()
+    h_w = torch.from_numpy(w).pin_memory()
+    h_mask = torch.from_numpy(mask).pin_memory()
+    h_wln = torch.from_numpy(np.ascontiguousarray(wln.T)).pin_memory()
+    h_out = torch.empty(2 * nlmsize, dtype=torch.float64).pin_memory()
+    hwin = capi.Window()
+    hwin.kind = capi.SFB_WINDOW_SEPARABLE
+    hwin.mask = capi.C.cast(h_mask.data_ptr(), capi._dp)
+    hwin.w_ln = capi.C.cast(h_wln.data_ptr(), capi._dp)
+
+    def host_step():
+        capi.check(capi.lib.sfb_cat2amln(plan.handle, capi.C.c_void_p(h_gal.data_ptr()),
+                                         capi.C.c_void_p(h_w.data_ptr()), N, float(nbar), capi.C.byref(hwin),
+                                         capi.C.c_void_p(h_out.data_ptr())))
+
+    host_step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        host_step()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    h2d = 8 * (3 * N + N + mask.size + wln.size)
+    d2h = 16 * nlmsize
+    res_dev = d_out.cpu().numpy()
+    same = float(np.max(np.abs(h_out.numpy() - res_dev)) / max(np.max(np.abs(res_dev)), 1e-300))
+
+    # roofline of the dominant stage
+    dom = max(stages, key=lambda k: stages[k]["ms_per_step"])
+    nlaunch = max(stages[dom]["launches_per_step"], 1)
+    ms_launch = stages[dom]["ms_per_step"] / nlaunch
+    nm = info["nbasis"] + 1
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    roof = roofline_for(dom, ms_launch, nlaunch, info, peaks, nm)
+    if roof["bound"] == "fp64":
+        peak = fp64_gemm_peak(torch)
+        roof.update({"peak": peak, "peak_source": "cuBLAS DGEMM 8192^3 measured in this run"})
+    elif roof["bound"] == "hbm":
+        peak = peaks.get("hbm_gbs", 6800.0)
+        roof.update({"peak": peak, "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback"})
+    roof["frac"] = (roof["achieved"] / roof["peak"]) if roof.get("achieved") else None
+    roof["kernel_stage"] = dom
+    roof["ms_per_launch"] = ms_launch
+    roof["traffic"] = None
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import sfb as osfb
+        md = dict(nmax=amodes.nmax, lmax=amodes.lmax, lmax_n=[int(v) for v in amodes.lmax_n], nside=NSIDE,
+                  splines=amodes.basisfunctions.spline, noff=amodes._noff)
+        ppst = args.cpu_pairs or workers
+        vals, t_setup = run_reference_sample(amodes, gal, w, nbar, mask, wln, 1, 0, workers, ppst)
+        cpu = {"value": float(vals[0]), "unit": "galaxies/s", "cores": workers, "kind": "port",
+               "sample": f"{ppst} of {len(amodes.pairs())} (n,l) pairs (spline scatter + niter=3 map2alm each) on "
+                         f"{workers} processes, extrapolated by pair count, plus the once-per-call sort/ang2pix "
+                         f"({t_setup:.2f} s)"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "galaxies/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "mixed",
+                "data": "synthetic",
+                "config": {"workload": WORKLOAD, "ngal": N, "precision": args.precision, "radial": "poly",
+                           "radial_pieces": info["radial_pieces"], "radial_degree": info["radial_degree"],
+                           "radial_error": info["radial_error"], "nbasis": info["nbasis"],
+                           "l2": "inputs (320 MB) and maps larger than L2; no flush",
+                           "parallelism": "replicas" if world > 1 else "single"},
+                "roofline": roof, "cpu_baseline": cpu,
+                "e2e": {"value": N / e2e_s, "unit": "galaxies/s", "h2d_bytes_per_step": int(h2d),
+                        "d2h_bytes_per_step": int(d2h), "host_vs_device_result_rel_diff": same},
+                "stages": stages, "clocks": clk, "gpu_launches": int(launches)}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -152,6 +152,28 @@ int sfb_map2alm(sfb_plan *plan, const double *maps, int64_t nmaps, double *alm_o
 int sfb_ang2pix_ring(int64_t nside, const double *theta, const double *phi, int64_t n,
                      int64_t *pix_out);
 
+/* Stages of one transform call, for sfb_get_stage_times. */
+typedef enum {
+    SFB_STAGE_DEPOSIT = 0,       /* galaxy binning into the radial-basis x pixel maps */
+    SFB_STAGE_RING_FFT = 1,      /* ring Fourier transforms (analysis and synthesis) */
+    SFB_STAGE_LEG_ANALYSIS = 2,  /* Legendre contraction, rings -> a_lm */
+    SFB_STAGE_LEG_SYNTHESIS = 3, /* Legendre contraction, a_lm -> rings (refinement) */
+    SFB_STAGE_FOLD = 4,          /* refinement residual in ring-Fourier space */
+    SFB_STAGE_PROJECT = 5,       /* radial projection and window subtraction */
+    SFB_STAGE_OTHER = 6,         /* clears, copies, checks */
+    SFB_NSTAGES = 7
+} sfb_stage;
+
+/* Stage timing with CUDA events recorded on the call's stream (no extra
+ * synchronisation).  Enabling resets the accumulators.  Not part of the
+ * reference interface: measurement support for this library. */
+int sfb_set_profiling(sfb_plan *plan, int32_t enable);
+/* Accumulated device milliseconds and kernel launches per stage since
+ * profiling was enabled; ms and launches are arrays of SFB_NSTAGES (either may be NULL). */
+int sfb_get_stage_times(const sfb_plan *plan, double *ms, int64_t *launches);
+/* Number of kernels this library has launched in this process. */
+int64_t sfb_launch_count(void);
+
 /* Text of the last error on this thread (NUL-terminated, truncated to len). */
 int sfb_last_error(char *buf, size_t len);
 

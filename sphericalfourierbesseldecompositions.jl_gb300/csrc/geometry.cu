@@ -54,6 +54,7 @@ __global__ void k_legendre_table(const RingGeom *rings, int nrn, int lmax, const
 void launch_legendre_table(const Plan &p, cudaStream_t st) {
     dim3 grid((unsigned)((p.nrn + 127) / 128), (unsigned)(p.lmax + 1));
     k_legendre_table<<<grid, 128, 0, st>>>(p.d_rings, (int)p.nrn, p.lmax, p.d_lam_off, p.d_lam);
+    note_launch();
 }
 
 __global__ void k_ang2pix(int64_t nside, const double *theta, const double *phi, int64_t n, int64_t *pix) {
@@ -66,6 +67,7 @@ void launch_ang2pix(int64_t nside, const double *theta, const double *phi, int64
                     cudaStream_t st) {
     if (n <= 0) return;
     k_ang2pix<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(nside, theta, phi, n, pix);
+    note_launch();
 }
 
 // out[c][r] = in[r][c]; in is rows x cols row-major.
@@ -87,6 +89,7 @@ void launch_transpose(const double *in, int64_t rows, int64_t cols, double *out,
     if (rows <= 0 || cols <= 0) return;
     dim3 grid((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32));
     k_transpose<<<grid, dim3(32, 8), 0, st>>>(in, rows, cols, out);
+    note_launch();
 }
 
 // out[c * ldo + r] = in[r * ldi + c] for r < rows, c < cols.
@@ -109,6 +112,7 @@ void launch_transpose_ld(const double *in, int64_t ldi, int64_t rows, int64_t co
     if (rows <= 0 || cols <= 0) return;
     dim3 grid((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32));
     k_transpose_ld<<<grid, dim3(32, 8), 0, st>>>(in, ldi, rows, cols, out, ldo);
+    note_launch();
 }
 
 __global__ void k_check_finite(const double *x, int64_t n, int *err) {
@@ -123,6 +127,7 @@ void launch_check_finite(const double *x, int64_t n, int *err, cudaStream_t st) 
     int64_t blocks = (n + 255) / 256;
     if (blocks > 4096) blocks = 4096;
     k_check_finite<<<(unsigned)blocks, 256, 0, st>>>(x, n, err);
+    note_launch();
 }
 
 }  // namespace sfb

@@ -23,38 +23,39 @@ __device__ __forceinline__ int nrows_of(int m, int par, int lmax) {
 }
 }  // namespace
 
-__global__ void __launch_bounds__(256) k_leg_analysis(const double *__restrict__ lam, const int64_t *lam_off,
-                                                      int lmax, int nrn, const double *__restrict__ F,
-                                                      int64_t ncol, double *__restrict__ A, int accumulate) {
+template <typename T>
+__global__ void __launch_bounds__(256) k_leg_analysis(const T *__restrict__ lam, const int64_t *lam_off,
+                                                      int lmax, int nrn, const T *__restrict__ F,
+                                                      int64_t ncol, T *__restrict__ A, int accumulate) {
     const int z = blockIdx.z;
     const int m = z >> 1, par = z & 1;
     const int nrows = nrows_of(m, par, lmax);
     const int row0 = blockIdx.y * BM;
     if (row0 >= nrows) return;
     const int64_t col0 = (int64_t)blockIdx.x * BN;
-    const double *L = lam + lam_off[z];
-    const double *B = F + ((int64_t)(par * (lmax + 1) + m) * nrn) * ncol;
-    __shared__ double As[BK][BM + 1];
-    __shared__ double Bs[BK][BN];
+    const T *L = lam + lam_off[z];
+    const T *B = F + ((int64_t)(par * (lmax + 1) + m) * nrn) * ncol;
+    __shared__ T As[BK][BM + 1];
+    __shared__ T Bs[BK][BN];
     const int tid = threadIdx.x;
     const int tx = tid & 15, ty = tid >> 4;
-    double acc[4][4] = {};
+    T acc[4][4] = {};
     for (int k0 = 0; k0 < nrn; k0 += BK) {
         for (int i = tid; i < BM * BK; i += 256) {
             const int rr = i / BK, kk = i % BK;
             const int row = row0 + rr, k = k0 + kk;
-            As[kk][rr] = (row < nrows && k < nrn) ? L[(int64_t)row * nrn + k] : 0.0;
+            As[kk][rr] = (row < nrows && k < nrn) ? L[(int64_t)row * nrn + k] : T(0);
         }
         for (int i = tid; i < BK * BN; i += 256) {
             const int kk = i / BN, cc = i % BN;
             const int k = k0 + kk;
             const int64_t col = col0 + cc;
-            Bs[kk][cc] = (k < nrn && col < ncol) ? B[(int64_t)k * ncol + col] : 0.0;
+            Bs[kk][cc] = (k < nrn && col < ncol) ? B[(int64_t)k * ncol + col] : T(0);
         }
         __syncthreads();
 #pragma unroll
         for (int kk = 0; kk < BK; ++kk) {
-            double a[4], b[4];
+            T a[4], b[4];
 #pragma unroll
             for (int i = 0; i < 4; ++i) a[i] = As[kk][ty * 4 + i];
 #pragma unroll
@@ -76,38 +77,39 @@ __global__ void __launch_bounds__(256) k_leg_analysis(const double *__restrict__
         for (int j = 0; j < 4; ++j) {
             const int64_t col = col0 + tx + 16 * j;
             if (col >= ncol) continue;
-            double *d = A + lm * ncol + col;
+            T *d = A + lm * ncol + col;
             *d = accumulate ? *d + acc[i][j] : acc[i][j];
         }
     }
 }
 
-__global__ void __launch_bounds__(256) k_leg_synthesis(const double *__restrict__ lam, const int64_t *lam_off,
-                                                       int lmax, int nrn, const double *__restrict__ A,
-                                                       int64_t ncol, double *__restrict__ G) {
+template <typename T>
+__global__ void __launch_bounds__(256) k_leg_synthesis(const T *__restrict__ lam, const int64_t *lam_off,
+                                                       int lmax, int nrn, const T *__restrict__ A,
+                                                       int64_t ncol, T *__restrict__ G) {
     const int z = blockIdx.z;
     const int m = z >> 1, par = z & 1;
     const int nrows = nrows_of(m, par, lmax);   // K dimension
     const int r0 = blockIdx.y * BM;
     if (r0 >= nrn) return;
     const int64_t col0 = (int64_t)blockIdx.x * BN;
-    const double *L = lam + lam_off[z];
-    __shared__ double As[BK][BM + 1];
-    __shared__ double Bs[BK][BN];
+    const T *L = lam + lam_off[z];
+    __shared__ T As[BK][BM + 1];
+    __shared__ T Bs[BK][BN];
     const int tid = threadIdx.x;
     const int tx = tid & 15, ty = tid >> 4;
-    double acc[4][4] = {};
+    T acc[4][4] = {};
     for (int k0 = 0; k0 < nrows; k0 += BK) {
         for (int i = tid; i < BM * BK; i += 256) {
             const int kk = i / BM, rr = i % BM;
             const int k = k0 + kk, r = r0 + rr;
-            As[kk][rr] = (k < nrows && r < nrn) ? L[(int64_t)k * nrn + r] : 0.0;
+            As[kk][rr] = (k < nrows && r < nrn) ? L[(int64_t)k * nrn + r] : T(0);
         }
         for (int i = tid; i < BK * BN; i += 256) {
             const int kk = i / BN, cc = i % BN;
             const int k = k0 + kk;
             const int64_t col = col0 + cc;
-            double v = 0.0;
+            T v = T(0);
             if (k < nrows && col < ncol) {
                 const int l = m + par + 2 * k;
                 v = A[((int64_t)l * (l + 1) / 2 + m) * ncol + col];
@@ -117,7 +119,7 @@ __global__ void __launch_bounds__(256) k_leg_synthesis(const double *__restrict_
         __syncthreads();
 #pragma unroll
         for (int kk = 0; kk < BK; ++kk) {
-            double a[4], b[4];
+            T a[4], b[4];
 #pragma unroll
             for (int i = 0; i < 4; ++i) a[i] = As[kk][ty * 4 + i];
 #pragma unroll
@@ -129,7 +131,7 @@ __global__ void __launch_bounds__(256) k_leg_synthesis(const double *__restrict_
         }
         __syncthreads();
     }
-    double *Gb = G + ((int64_t)(par * (lmax + 1) + m) * nrn) * ncol;
+    T *Gb = G + ((int64_t)(par * (lmax + 1) + m) * nrn) * ncol;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         const int r = r0 + ty * 4 + i;
@@ -147,8 +149,9 @@ __global__ void __launch_bounds__(256) k_leg_synthesis(const double *__restrict_
 //              + sum_{m >= 1, m = -m' mod n + t n <= L} conj(G_m) e^{-i(m+m')phi0},
 // and (m -/+ m') is a multiple of n, phi0 = pi/den with den in {0, n}, so
 // every phase is +1 or (-1)^t.  G_0 enters through its real part.
-__global__ void k_fold_residual(const RingGeom *rings, int nrn, int lmax, double w, const double *__restrict__ F,
-                                const double *__restrict__ G, int64_t ncplx, double *__restrict__ R) {
+template <typename T>
+__global__ void k_fold_residual(const RingGeom *rings, int nrn, int lmax, double w, const T *__restrict__ F,
+                                const T *__restrict__ G, int64_t ncplx, T *__restrict__ R) {
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int mp = blockIdx.y;
     const int r = blockIdx.z % nrn;
@@ -163,7 +166,7 @@ __global__ void k_fold_residual(const RingGeom *rings, int nrn, int lmax, double
     const int k = mp % n;
     int t = 0;
     for (int m = k; m <= lmax; m += n, ++t) {
-        const double *gp = G + ((int64_t)(par * L1 + m) * nrn + r) * ld + 2 * c;
+        const T *gp = G + ((int64_t)(par * L1 + m) * nrn + r) * ld + 2 * c;
         // (m - m') = (t - t0) n with t0 = m' / n
         const int dt = t - mp / n;
         const double sgn = (odd_phase && (dt & 1)) ? -1.0 : 1.0;
@@ -172,7 +175,7 @@ __global__ void k_fold_residual(const RingGeom *rings, int nrn, int lmax, double
     }
     const int kk = (n - k) % n;
     for (int m = (kk == 0 ? n : kk); m <= lmax; m += n) {
-        const double *gp = G + ((int64_t)(par * L1 + m) * nrn + r) * ld + 2 * c;
+        const T *gp = G + ((int64_t)(par * L1 + m) * nrn + r) * ld + 2 * c;
         const int q = (m + mp) / n;   // (m + m') = q n exactly
         const double sgn = (odd_phase && (q & 1)) ? -1.0 : 1.0;
         sx += sgn * gp[0];
@@ -180,20 +183,31 @@ __global__ void k_fold_residual(const RingGeom *rings, int nrn, int lmax, double
     }
     const double f = w * (double)n * g.cfold;
     const int64_t off = ((int64_t)(par * L1 + mp) * nrn + r) * ld + 2 * c;
-    R[off] = F[off] - f * sx;
-    R[off + 1] = F[off + 1] - f * sy;
+    R[off] = (T)((double)F[off] - f * sx);
+    R[off + 1] = (T)((double)F[off + 1] - f * sy);
 }
 
 void launch_leg_analysis(const Plan &p, const double *F, int64_t ncol, double *A, bool accumulate,
                          cudaStream_t st) {
     const int maxrows = p.lmax / 2 + 1;
     dim3 grid((unsigned)((ncol + BN - 1) / BN), (unsigned)((maxrows + BM - 1) / BM), (unsigned)(2 * (p.lmax + 1)));
-    k_leg_analysis<<<grid, 256, 0, st>>>(p.d_lam, p.d_lam_off, p.lmax, (int)p.nrn, F, ncol, A, accumulate ? 1 : 0);
+    if (p.precision == SFB_MIXED)
+        k_leg_analysis<float><<<grid, 256, 0, st>>>(p.d_lam32, p.d_lam_off, p.lmax, (int)p.nrn, (const float *)F,
+                                                    ncol, (float *)A, accumulate ? 1 : 0);
+    else
+        k_leg_analysis<double><<<grid, 256, 0, st>>>(p.d_lam, p.d_lam_off, p.lmax, (int)p.nrn, F, ncol, A,
+                                                     accumulate ? 1 : 0);
+    note_launch();
 }
 
 void launch_leg_synthesis(const Plan &p, const double *A, int64_t ncol, double *G, cudaStream_t st) {
     dim3 grid((unsigned)((ncol + BN - 1) / BN), (unsigned)((p.nrn + BM - 1) / BM), (unsigned)(2 * (p.lmax + 1)));
-    k_leg_synthesis<<<grid, 256, 0, st>>>(p.d_lam, p.d_lam_off, p.lmax, (int)p.nrn, A, ncol, G);
+    if (p.precision == SFB_MIXED)
+        k_leg_synthesis<float><<<grid, 256, 0, st>>>(p.d_lam32, p.d_lam_off, p.lmax, (int)p.nrn, (const float *)A,
+                                                     ncol, (float *)G);
+    else
+        k_leg_synthesis<double><<<grid, 256, 0, st>>>(p.d_lam, p.d_lam_off, p.lmax, (int)p.nrn, A, ncol, G);
+    note_launch();
 }
 
 void launch_fold_residual(const Plan &p, const double *F, const double *G, int64_t ncol, double *R,
@@ -201,7 +215,25 @@ void launch_fold_residual(const Plan &p, const double *F, const double *G, int64
     const int64_t ncplx = ncol / 2;
     dim3 grid((unsigned)((ncplx + 63) / 64), (unsigned)(p.lmax + 1), (unsigned)(2 * p.nrn));
     const double w = 4.0 * M_PI / (double)p.npix;
-    k_fold_residual<<<grid, 64, 0, st>>>(p.d_rings, (int)p.nrn, p.lmax, w, F, G, ncplx, R);
+    if (p.precision == SFB_MIXED)
+        k_fold_residual<float><<<grid, 64, 0, st>>>(p.d_rings, (int)p.nrn, p.lmax, w, (const float *)F,
+                                                    (const float *)G, ncplx, (float *)R);
+    else
+        k_fold_residual<double><<<grid, 64, 0, st>>>(p.d_rings, (int)p.nrn, p.lmax, w, F, G, ncplx, R);
+    note_launch();
+}
+
+__global__ void k_to_float(const double *in, int64_t n, float *out) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (float)in[i];
+}
+
+void launch_to_float(const double *in, int64_t n, float *out, cudaStream_t st) {
+    if (n <= 0) return;
+    int64_t blocks = (n + 255) / 256;
+    if (blocks > 8192) blocks = 8192;
+    k_to_float<<<(unsigned)blocks, 256, 0, st>>>(in, n, out);
+    note_launch();
 }
 
 }  // namespace sfb

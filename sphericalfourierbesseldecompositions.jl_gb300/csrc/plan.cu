@@ -1,5 +1,6 @@
 // Plan management, orchestration and the C ABI (include/sfb_gpu.h).
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -10,6 +11,9 @@
 namespace sfb {
 
 static thread_local std::string g_last_error;
+static std::atomic<int64_t> g_launches{0};
+
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 void set_error(const std::string &msg) { g_last_error = msg; }
 int fail(int code, const std::string &msg) {
@@ -84,7 +88,72 @@ struct sfb_plan {
     cudaStream_t stream = nullptr;
     int32_t *d_pair_index = nullptr;
     int64_t *d_noff = nullptr;
+    // stage profiling (events on the call's stream)
+    bool profile = false;
+    struct Rec {
+        int stage;
+        cudaEvent_t a, b;
+        int64_t launches;
+    };
+    std::vector<cudaEvent_t> pool;
+    std::vector<Rec> recs;
+    double stage_ms[SFB_NSTAGES] = {};
+    int64_t stage_launches[SFB_NSTAGES] = {};
 };
+
+namespace {
+
+cudaEvent_t take_event(sfb_plan *h) {
+    if (!h->pool.empty()) {
+        cudaEvent_t e = h->pool.back();
+        h->pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return e;
+}
+
+// RAII scope: records a start event on construction and an end event on
+// destruction when profiling is on; launches counted from the global counter.
+struct Stage {
+    sfb_plan *h;
+    int id;
+    cudaStream_t st;
+    cudaEvent_t a = nullptr;
+    int64_t l0 = 0;
+    Stage(sfb_plan *h_, int id_, cudaStream_t st_) : h(h_), id(id_), st(st_) {
+        if (!h->profile) return;
+        a = take_event(h);
+        l0 = sfb::g_launches.load();
+        if (a) cudaEventRecord(a, st);
+    }
+    ~Stage() {
+        if (!h->profile || !a) return;
+        cudaEvent_t b = take_event(h);
+        if (!b) return;
+        cudaEventRecord(b, st);
+        h->recs.push_back({id, a, b, sfb::g_launches.load() - l0});
+    }
+};
+
+// After the stream is synchronised: fold recorded events into the totals.
+void collect_stages(sfb_plan *h) {
+    for (auto &r : h->recs) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) h->stage_ms[r.stage] += ms;
+        else cudaGetLastError();
+        h->stage_launches[r.stage] += r.launches;
+        h->pool.push_back(r.a);
+        h->pool.push_back(r.b);
+    }
+    h->recs.clear();
+}
+
+}  // namespace
 
 using namespace sfb;
 
@@ -228,12 +297,22 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st) {
         SFB_TRY(grow(p, p.gbuf, fsz));
         SFB_TRY(grow(p, p.rbuf, fsz));
     }
-    launch_ring_analysis(p, maps, nm, p.fbuf.ptr, st);
-    launch_leg_analysis(p, p.fbuf.ptr, ncol, p.alm.ptr, false, st);
+    { Stage s(h, SFB_STAGE_RING_FFT, st); launch_ring_analysis(p, maps, nm, p.fbuf.ptr, st); }
+    const bool tc = p.precision == SFB_MIXED;
+    auto analysis = [&](const double *src, bool acc) {
+        Stage s(h, SFB_STAGE_LEG_ANALYSIS, st);
+        if (tc) launch_leg_analysis_tc(p, (const float *)src, ncol, (float *)p.alm.ptr, acc, st);
+        else launch_leg_analysis(p, src, ncol, p.alm.ptr, acc, st);
+    };
+    analysis(p.fbuf.ptr, false);
     for (int it = 0; it < p.niter; ++it) {
-        launch_leg_synthesis(p, p.alm.ptr, ncol, p.gbuf.ptr, st);
-        launch_fold_residual(p, p.fbuf.ptr, p.gbuf.ptr, ncol, p.rbuf.ptr, st);
-        launch_leg_analysis(p, p.rbuf.ptr, ncol, p.alm.ptr, true, st);
+        {
+            Stage s(h, SFB_STAGE_LEG_SYNTHESIS, st);
+            if (tc) launch_leg_synthesis_tc(p, (const float *)p.alm.ptr, ncol, (float *)p.gbuf.ptr, st);
+            else launch_leg_synthesis(p, p.alm.ptr, ncol, p.gbuf.ptr, st);
+        }
+        { Stage s(h, SFB_STAGE_FOLD, st); launch_fold_residual(p, p.fbuf.ptr, p.gbuf.ptr, ncol, p.rbuf.ptr, st); }
+        analysis(p.rbuf.ptr, true);
     }
     SFB_CUDA_TRY(cudaGetLastError());
     return SFB_OK;
@@ -241,13 +320,18 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st) {
 
 int finish(sfb_plan *h, const double *out_dev, cudaStream_t st) {
     Plan &p = h->p;
-    launch_check_finite(out_dev, 2 * p.nlmsize, p.d_err, st);
+    {
+        Stage s(h, SFB_STAGE_OTHER, st);
+        launch_check_finite(out_dev, 2 * p.nlmsize, p.d_err, st);
+    }
     int err = 0;
     SFB_CUDA_TRY(cudaMemcpyAsync(&err, p.d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
     SFB_CUDA_TRY(cudaStreamSynchronize(st));
     SFB_CUDA_TRY(cudaGetLastError());
+    collect_stages(h);
     if (err & ERR_NONFINITE_INPUT) return fail(SFB_ENONFINITE, "non-finite galaxy coordinate or weight");
     if (err & ERR_THETA_RANGE) return fail(SFB_ERANGE, "galaxy theta outside [0, pi]");
+    if (err & ERR_TC_TIMEOUT) return fail(SFB_ETIMEOUT, "tensor-core kernel: bounded mbarrier wait expired");
     if (err & ERR_NONFINITE_OUTPUT) return fail(SFB_ENONFINITE, "non-finite a_nlm (all(isfinite.(anlm)) failed)");
     return SFB_OK;
 }
@@ -278,13 +362,19 @@ int cat2amln_dev(sfb_plan *h, const double *rtp, const double *w, int64_t ngal, 
     if (p.radial_mode == SFB_RADIAL_POLY) {
         const int64_t nm = p.nbasis + (wk == SFB_WINDOW_SEPARABLE ? 1 : 0);
         SFB_TRY(grow(p, p.maps, (size_t)nm * p.npix));
-        SFB_CUDA_TRY(cudaMemsetAsync(p.maps.ptr, 0, (size_t)p.nbasis * p.npix * sizeof(double), st));
-        launch_deposit_poly(p, rtp, w, ngal, p.maps.ptr, st);
-        if (wk == SFB_WINDOW_SEPARABLE)
-            SFB_CUDA_TRY(cudaMemcpyAsync(p.maps.ptr + p.nbasis * p.npix, win->mask, p.npix * sizeof(double),
-                                         cudaMemcpyDeviceToDevice, st));
+        {
+            Stage s(h, SFB_STAGE_OTHER, st);
+            SFB_CUDA_TRY(cudaMemsetAsync(p.maps.ptr, 0, (size_t)p.nbasis * p.npix * sizeof(double), st));
+            if (wk == SFB_WINDOW_SEPARABLE)
+                SFB_CUDA_TRY(cudaMemcpyAsync(p.maps.ptr + p.nbasis * p.npix, win->mask, p.npix * sizeof(double),
+                                             cudaMemcpyDeviceToDevice, st));
+        }
+        { Stage s(h, SFB_STAGE_DEPOSIT, st); launch_deposit_poly(p, rtp, w, ngal, p.maps.ptr, st); }
         SFB_TRY(sht_analysis(h, p.maps.ptr, nm, st));
-        launch_project_poly(p, p.alm.ptr, 2 * nm, scale, wk, win->w_ln, p.nbasis, nullptr, 0, out, st);
+        {
+            Stage s(h, SFB_STAGE_PROJECT, st);
+            launch_project_poly(p, p.alm.ptr, 2 * nm, scale, wk, win->w_ln, p.nbasis, nullptr, 0, out, st);
+        }
         if (wk == SFB_WINDOW_DENSE) {
             const int64_t cp = chunk_pairs(p);
             SFB_TRY(grow(p, p.maps, (size_t)cp * p.npix));
@@ -302,7 +392,7 @@ int cat2amln_dev(sfb_plan *h, const double *rtp, const double *w, int64_t ngal, 
         for (int64_t p0 = 0; p0 < p.npairs; p0 += cp) {
             const int64_t npc = std::min(cp, p.npairs - p0);
             SFB_CUDA_TRY(cudaMemsetAsync(p.maps.ptr, 0, (size_t)npc * p.npix * sizeof(double), st));
-            launch_deposit_spline_chunk(p, rtp, w, ngal, p0, npc, scale, p.maps.ptr, st);
+            { Stage s(h, SFB_STAGE_DEPOSIT, st); launch_deposit_spline_chunk(p, rtp, w, ngal, p0, npc, scale, p.maps.ptr, st); }
             if (wk == SFB_WINDOW_DENSE) launch_subtract_dense_chunk(p, p.maps.ptr, win->dense, p0, npc, st);
             if (wk == SFB_WINDOW_SEPARABLE) launch_subtract_sep_chunk(p, p.maps.ptr, win->mask, win->w_ln, p0, npc, st);
             SFB_TRY(sht_analysis(h, p.maps.ptr, npc, st));
@@ -461,6 +551,24 @@ int sfb_plan_create(const sfb_plan_desc *d, sfb_plan **out) {
         if ((st = upload(p, &h->d_noff, noff.data(), noff.size())) != SFB_OK) break;
         if ((st = upload<int>(p, &p.d_err, nullptr, 1)) != SFB_OK) break;
         launch_legendre_table(p, h->stream);
+        if ((st = upload<float>(p, &p.d_lam32, nullptr, (size_t)off)) != SFB_OK) break;
+        launch_to_float(p.d_lam, off, p.d_lam32, h->stream);
+        {
+            std::vector<int64_t> toff;
+            const int64_t tsz = tc_table_offsets(p, toff);
+            if ((st = upload(p, &p.d_lamtc_off, toff.data(), toff.size())) != SFB_OK) break;
+            if ((st = upload<uint16_t>(p, (uint16_t **)&p.d_lamtc, nullptr, (size_t)tsz)) != SFB_OK) break;
+            if (cudaMemsetAsync(p.d_lamtc, 0, (size_t)tsz * 2, h->stream) != cudaSuccess) {
+                st = fail(SFB_ECUDA, "table clear failed");
+                break;
+            }
+            launch_build_lamtc(p, h->stream);
+            std::vector<int64_t> soff;
+            const int64_t ssz = tc_synth_table_offsets(p, soff);
+            if ((st = upload(p, &p.d_lamts_off, soff.data(), soff.size())) != SFB_OK) break;
+            if ((st = upload<uint16_t>(p, (uint16_t **)&p.d_lamts, nullptr, (size_t)ssz)) != SFB_OK) break;
+            launch_build_lamts(p, h->stream);
+        }
         if (cudaGetLastError() != cudaSuccess) {
             st = fail(SFB_ECUDA, "Legendre table kernel failed to launch");
             break;
@@ -488,12 +596,14 @@ void sfb_plan_destroy(sfb_plan *h) {
     Plan &p = h->p;
     cudaSetDevice(p.device);
     if (h->stream) cudaStreamSynchronize(h->stream);
-    void *ptrs[] = {p.d_rings, p.d_lam, p.d_lam_off, p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp,
+    void *ptrs[] = {p.d_rings, p.d_lam, p.d_lam32, p.d_lamtc, p.d_lamtc_off, p.d_lamts, p.d_lamts_off, p.d_lam_off, p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp,
                     p.d_pair_l, p.d_pair_n, p.d_out_pair, p.d_out_lm, p.d_coef, p.d_err,
                     p.maps.ptr, p.fbuf.ptr, p.gbuf.ptr, p.rbuf.ptr, p.alm.ptr, p.scratch.ptr, p.scratch2.ptr,
                     h->d_pair_index, h->d_noff};
     for (void *q : ptrs)
         if (q) cudaFree(q);
+    collect_stages(h);
+    for (cudaEvent_t e : h->pool) cudaEventDestroy(e);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }
@@ -519,6 +629,29 @@ int sfb_set_precision(sfb_plan *h, int32_t precision) {
     h->p.precision = precision;
     return SFB_OK;
 }
+
+int sfb_set_profiling(sfb_plan *h, int32_t enable) {
+    SFB_TRY(check_plan(h));
+    cudaStreamSynchronize(h->stream);
+    collect_stages(h);
+    h->profile = enable != 0;
+    for (int i = 0; i < SFB_NSTAGES; ++i) {
+        h->stage_ms[i] = 0;
+        h->stage_launches[i] = 0;
+    }
+    return SFB_OK;
+}
+
+int sfb_get_stage_times(const sfb_plan *h, double *ms, int64_t *launches) {
+    SFB_TRY(check_plan(h));
+    for (int i = 0; i < SFB_NSTAGES; ++i) {
+        if (ms) ms[i] = h->stage_ms[i];
+        if (launches) launches[i] = h->stage_launches[i];
+    }
+    return SFB_OK;
+}
+
+int64_t sfb_launch_count(void) { return sfb::g_launches.load(); }
 
 int sfb_cat2amln_device(sfb_plan *h, const double *rtp, const double *weight, int64_t ngal, double nbar,
                         const sfb_window *window, double *anlm_out, void *stream) {
@@ -569,7 +702,7 @@ int sfb_cat2amln(sfb_plan *h, const double *rtp, const double *weight, int64_t n
     return SFB_OK;
 }
 
-int sfb_map2alm(sfb_plan *h, const double *maps, int64_t nmaps, double *alm_out) {
+static int sfb_map2alm_impl(sfb_plan *h, const double *maps, int64_t nmaps, double *alm_out) {
     SFB_TRY(check_plan(h));
     SFB_TRY(set_device_of(h));
     if (nmaps <= 0 || !maps || !alm_out) return fail(SFB_EINVAL, "bad map2alm arguments");
@@ -589,7 +722,7 @@ int sfb_map2alm(sfb_plan *h, const double *maps, int64_t nmaps, double *alm_out)
     return SFB_OK;
 }
 
-int sfb_field2anlm(sfb_plan *h, const double *f, int64_t nr, double rmin, double rmax, double *anlm_out) {
+static int sfb_field2anlm_impl(sfb_plan *h, const double *f, int64_t nr, double rmin, double rmax, double *anlm_out) {
     SFB_TRY(check_plan(h));
     SFB_TRY(set_device_of(h));
     if (!f || !anlm_out || nr < 1 || !(rmin < rmax)) return fail(SFB_EINVAL, "bad field2anlm arguments");
@@ -626,7 +759,7 @@ int sfb_field2anlm(sfb_plan *h, const double *f, int64_t nr, double rmin, double
     return SFB_OK;
 }
 
-int sfb_anlm2field(sfb_plan *h, const double *anlm, int64_t nr, double rmin, double rmax, double *f_out) {
+static int sfb_anlm2field_impl(sfb_plan *h, const double *anlm, int64_t nr, double rmin, double rmax, double *f_out) {
     SFB_TRY(check_plan(h));
     SFB_TRY(set_device_of(h));
     if (!anlm || !f_out || nr < 1 || !(rmin < rmax)) return fail(SFB_EINVAL, "bad anlm2field arguments");
@@ -721,6 +854,36 @@ int sfb_ang2pix_ring(int64_t nside, const double *theta, const double *phi, int6
     cudaFree(dp);
     if (e != cudaSuccess) return fail(SFB_ECUDA, cudaGetErrorString(e));
     return SFB_OK;
+}
+
+int sfb_map2alm(sfb_plan *h, const double *maps, int64_t nmaps, double *alm_out) {
+    SFB_TRY(check_plan(h));
+    // these transforms run in FP64 whatever the plan's cat2amln precision
+    const int saved = h->p.precision;
+    h->p.precision = SFB_FP64;
+    const int rc = sfb_map2alm_impl(h, maps, nmaps, alm_out);
+    h->p.precision = saved;
+    return rc;
+}
+
+int sfb_field2anlm(sfb_plan *h, const double *f, int64_t nr, double rmin, double rmax, double *anlm_out) {
+    SFB_TRY(check_plan(h));
+    // these transforms run in FP64 whatever the plan's cat2amln precision
+    const int saved = h->p.precision;
+    h->p.precision = SFB_FP64;
+    const int rc = sfb_field2anlm_impl(h, f, nr, rmin, rmax, anlm_out);
+    h->p.precision = saved;
+    return rc;
+}
+
+int sfb_anlm2field(sfb_plan *h, const double *anlm, int64_t nr, double rmin, double rmax, double *f_out) {
+    SFB_TRY(check_plan(h));
+    // these transforms run in FP64 whatever the plan's cat2amln precision
+    const int saved = h->p.precision;
+    h->p.precision = SFB_FP64;
+    const int rc = sfb_anlm2field_impl(h, anlm, nr, rmin, rmax, f_out);
+    h->p.precision = saved;
+    return rc;
 }
 
 }  // extern "C"

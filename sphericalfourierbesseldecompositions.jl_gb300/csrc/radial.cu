@@ -66,6 +66,7 @@ void launch_deposit_poly(const Plan &p, const double *rtp, const double *w, int6
     if (ngal <= 0) return;
     k_deposit_poly<<<(unsigned)((ngal + 255) / 256), 256, 0, st>>>(rtp, w, ngal, p.nside, p.npix, p.rmin, p.rmax,
                                                                    p.pieces, p.degree, p.nbasis, maps, p.d_err);
+                                                                   note_launch();
 }
 
 // Spline mode: maps[q][pix] += w * g_{pair0+q}(r) / (nbar dOmega) for a chunk of pairs.
@@ -94,6 +95,7 @@ void launch_deposit_spline_chunk(const Plan &p, const double *rtp, const double 
     dim3 grid((unsigned)((ngal + 255) / 256), gy);
     k_deposit_spline<<<grid, 256, 0, st>>>(rtp, w, ngal, p.nside, p.npix, p.d_spl_off, p.d_spl_x, p.d_spl_y,
                                            p.d_spl_ypp, pair0, npc, scale, maps, p.d_err);
+                                           note_launch();
 }
 
 // maps[q][p] -= dense[p + npix*(l + (lmax+1)*(n-1))] for the chunk's pairs.
@@ -112,6 +114,7 @@ void launch_subtract_dense_chunk(const Plan &p, double *maps, const double *dens
     if (npc <= 0) return;
     dim3 grid((unsigned)((p.npix + 255) / 256), (unsigned)npc);
     k_subtract_dense<<<grid, 256, 0, st>>>(maps, dense, p.npix, p.lmax, p.d_pair_n, p.d_pair_l, pair0, npc);
+    note_launch();
 }
 
 // maps[q][p] -= mask[p] * W_ln[l + (lmax+1)(n-1)] for the chunk's pairs (separable window).
@@ -130,6 +133,7 @@ void launch_subtract_sep_chunk(const Plan &p, double *maps, const double *mask, 
     if (npc <= 0) return;
     dim3 grid((unsigned)((p.npix + 255) / 256), (unsigned)npc);
     k_subtract_sep<<<grid, 256, 0, st>>>(maps, mask, w_ln, p.npix, p.lmax, p.d_pair_n, p.d_pair_l, pair0, npc);
+    note_launch();
 }
 
 __global__ void k_axpy(double *y, const double *x, int64_t n) {
@@ -142,6 +146,7 @@ void launch_axpy(double *y, const double *x, int64_t n, cudaStream_t st) {
     int64_t blocks = (n + 255) / 256;
     if (blocks > 8192) blocks = 8192;
     k_axpy<<<(unsigned)blocks, 256, 0, st>>>(y, x, n);
+    note_launch();
 }
 
 // Gather dense window maps of a chunk of pairs: maps[q] = W[:, l, n].
@@ -160,6 +165,7 @@ void launch_gather_dense_chunk(const Plan &p, double *maps, const double *dense,
     if (npc <= 0) return;
     dim3 grid((unsigned)((p.npix + 255) / 256), (unsigned)npc);
     k_gather_dense<<<grid, 256, 0, st>>>(maps, dense, p.npix, p.lmax, p.d_pair_n, p.d_pair_l, pair0, npc);
+    note_launch();
 }
 
 // Radial coefficients: C[pair][j*(deg+1)+k] = sum_q PQ[q][k] * g(r_q), with
@@ -196,6 +202,7 @@ void launch_radial_coeffs(const Plan &p, const double *gl_x, const double *pq, i
     dim3 grid((unsigned)p.npairs, (unsigned)p.pieces);
     k_radial_coeffs<<<grid, 128, Q * sizeof(double), st>>>(p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp, p.rmin,
                                                           p.rmax, p.pieces, p.degree, p.nbasis, gl_x, pq, Q, coef);
+                                                          note_launch();
 }
 
 // max over knots of |expansion - y| / max|y| per pair; atomicMax on the bit
@@ -236,31 +243,33 @@ void launch_radial_error_impl(const Plan &p, const double *coef, const double *y
                               cudaStream_t st) {
     k_radial_error<<<(unsigned)p.npairs, 128, 0, st>>>(p.d_spl_off, p.d_spl_x, p.d_spl_y, ymax, p.rmin, p.rmax,
                                                        p.pieces, p.degree, p.nbasis, coef, err_bits);
+                                                       note_launch();
 }
 
 // a_nlm = scale * sum_b C[pair][b] A[lm][b] - window term.
+template <typename TA>
 __global__ void k_project_poly(const int32_t *out_pair, const int32_t *out_lm, const int32_t *pair_n,
                                const int32_t *pair_l, int64_t nlmsize, int64_t nbasis, const double *coef,
-                               const double *__restrict__ A, int64_t ldA, double scale, int window_kind,
+                               const TA *__restrict__ A, int64_t ldA, double scale, int window_kind,
                                const double *w_ln, int lmax, int64_t mask_col, double *out) {
     const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= nlmsize) return;
     const int pr = out_pair[o];
     const int64_t lm = out_lm[o];
     const double *C = coef + (int64_t)pr * nbasis;
-    const double *Ar = A + lm * ldA;
+    const TA *Ar = A + lm * ldA;
     double re = 0.0, im = 0.0;
     for (int64_t b = 0; b < nbasis; ++b) {
         const double c = C[b];
-        re = fma(c, Ar[2 * b], re);
-        im = fma(c, Ar[2 * b + 1], im);
+        re = fma(c, (double)Ar[2 * b], re);
+        im = fma(c, (double)Ar[2 * b + 1], im);
     }
     re *= scale;
     im *= scale;
     if (window_kind == SFB_WINDOW_SEPARABLE) {
         const double wl = w_ln[pair_l[pr] + (int64_t)(lmax + 1) * (pair_n[pr] - 1)];
-        re -= wl * Ar[2 * mask_col];
-        im -= wl * Ar[2 * mask_col + 1];
+        re -= wl * (double)Ar[2 * mask_col];
+        im -= wl * (double)Ar[2 * mask_col + 1];
     }
     out[2 * o] = re;
     out[2 * o + 1] = im;
@@ -271,9 +280,15 @@ void launch_project_poly(const Plan &p, const double *A, int64_t ldA, double sca
                          cudaStream_t st) {
     (void)Awin; (void)ldW;
     if (p.nlmsize <= 0) return;
-    k_project_poly<<<(unsigned)((p.nlmsize + 127) / 128), 128, 0, st>>>(
-        p.d_out_pair, p.d_out_lm, p.d_pair_n, p.d_pair_l, p.nlmsize, p.nbasis, p.d_coef, A, ldA, scale, window_kind,
-        w_ln, p.lmax, mask_col, out);
+    if (p.precision == SFB_MIXED)
+        k_project_poly<float><<<(unsigned)((p.nlmsize + 127) / 128), 128, 0, st>>>(
+            p.d_out_pair, p.d_out_lm, p.d_pair_n, p.d_pair_l, p.nlmsize, p.nbasis, p.d_coef, (const float *)A, ldA,
+            scale, window_kind, w_ln, p.lmax, mask_col, out);
+    else
+        k_project_poly<double><<<(unsigned)((p.nlmsize + 127) / 128), 128, 0, st>>>(
+            p.d_out_pair, p.d_out_lm, p.d_pair_n, p.d_pair_l, p.nlmsize, p.nbasis, p.d_coef, A, ldA, scale,
+            window_kind, w_ln, p.lmax, mask_col, out);
+        note_launch();
 }
 
 // out[o] -= Awin[lm][pair - pair0] for outputs whose pair lies in the chunk.
@@ -293,6 +308,7 @@ void launch_sub_window_chunk(const Plan &p, const double *Awin, int64_t ldW, int
     if (p.nlmsize <= 0) return;
     k_sub_window_chunk<<<(unsigned)((p.nlmsize + 127) / 128), 128, 0, st>>>(p.d_out_pair, p.d_out_lm, p.nlmsize, Awin,
                                                                            ldW, pair0, npc, out);
+                                                                           note_launch();
 }
 
 // Spline mode: out[o] = A[lm][pair - pair0] (map already scaled and window-subtracted).
@@ -312,6 +328,7 @@ void launch_extract_spline_chunk(const Plan &p, const double *A, int64_t ldA, in
     if (p.nlmsize <= 0) return;
     k_extract_spline<<<(unsigned)((p.nlmsize + 127) / 128), 128, 0, st>>>(p.d_out_pair, p.d_out_lm, p.nlmsize, A, ldA,
                                                                          pair0, npc, out);
+                                                                         note_launch();
 }
 
 // gtab[pair][s] = g_pair(r_s) * (with_r2dr ? r_s^2 dr : 1), r_s = rmin + (s+1/2) dr.
@@ -331,6 +348,7 @@ void launch_gtab(const Plan &p, int64_t nr, double rmin, double dr, int with_r2d
     dim3 grid((unsigned)((nr + 127) / 128), (unsigned)p.npairs);
     k_gtab<<<grid, 128, 0, st>>>(p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp, p.npairs, nr, rmin, dr, with_r2dr,
                                  gtab);
+                                 note_launch();
 }
 
 // field2anlm radial sum: out[o] = sum_s gtab[pair][s] A[lm][s]  (src/cat2anlm.jl:347-353)
@@ -354,6 +372,7 @@ void launch_project_shells_g(const Plan &p, const double *gtab, int64_t nr, cons
     if (p.nlmsize <= 0) return;
     k_project_shells<<<(unsigned)((p.nlmsize + 127) / 128), 128, 0, st>>>(p.d_out_pair, p.d_out_lm, p.nlmsize, gtab, nr,
                                                                          A, ldA, out);
+                                                                         note_launch();
 }
 
 // anlm2field radial sum: A[lm][s] = sum_n gtab[pair(n,l)][s] a[idx(n,l,m)] (src/cat2anlm.jl:403-414)
@@ -384,6 +403,7 @@ void launch_shell_alm_g(const Plan &p, const int32_t *pair_index, const int64_t 
                         const double *anlm, double *A, int64_t ldA, cudaStream_t st) {
     dim3 grid((unsigned)((nr + 127) / 128), (unsigned)p.lmsize);
     k_shell_alm<<<grid, 128, 0, st>>>(pair_index, noff, p.nmax, p.lmax, gtab, nr, anlm, A, ldA);
+    note_launch();
 }
 
 // W_ln[l + (lmax+1)(n-1)] = sum_s gtab[pair][s] phi[s]  (gtab includes r^2 dr); NaN off-mode.
@@ -399,6 +419,7 @@ __global__ void k_win_sep(const int32_t *pair_n, const int32_t *pair_l, int64_t 
 void launch_win_sep_g(const Plan &p, const double *gtab, int64_t nr, const double *phi, double *out, cudaStream_t st) {
     k_win_sep<<<(unsigned)((p.npairs + 127) / 128), 128, 0, st>>>(p.d_pair_n, p.d_pair_l, p.npairs, gtab, nr, phi,
                                                                   p.lmax, out);
+                                                                  note_launch();
 }
 
 // Dense: W[p + npix(l + (lmax+1)(n-1))] = sum_s win[s + nr p] gtab[pair][s]
@@ -417,6 +438,7 @@ __global__ void k_win_dense(const int32_t *pair_n, const int32_t *pair_l, int64_
 void launch_win_dense_g(const Plan &p, const double *gtab, int64_t nr, const double *win, double *out, cudaStream_t st) {
     dim3 grid((unsigned)((p.npix + 127) / 128), (unsigned)p.npairs);
     k_win_dense<<<grid, 128, 0, st>>>(p.d_pair_n, p.d_pair_l, p.npairs, gtab, nr, win, p.npix, p.lmax, out);
+    note_launch();
 }
 
 __global__ void k_fill(double *x, int64_t n, double v) {
@@ -429,6 +451,7 @@ void launch_fill(double *x, int64_t n, double v, cudaStream_t st) {
     int64_t blocks = (n + 255) / 256;
     if (blocks > 8192) blocks = 8192;
     k_fill<<<(unsigned)blocks, 256, 0, st>>>(x, n, v);
+    note_launch();
 }
 
 }  // namespace sfb

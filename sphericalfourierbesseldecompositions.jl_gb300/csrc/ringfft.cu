@@ -106,14 +106,43 @@ __global__ void __launch_bounds__(256) k_ring_analysis(const RingGeom *rings, in
     cx<T> *buf = tw + n;
     cx<T> *src = buf + (int64_t)MT * n;
     fill_twiddles(tw, n, -1);
+    // Reduced precision: the ring sums (bin 0) are taken in FP64 and the DFT
+    // runs on the mean-subtracted values, so the FP32 arithmetic only carries
+    // the fluctuations about the ring mean (bins k != 0 are unchanged by it).
+    __shared__ double ring_sum[2 * 8];
+    constexpr bool reduced = sizeof(T) < sizeof(double);
+    if (reduced) {
+        if (threadIdx.x < 2 * MT) ring_sum[threadIdx.x] = 0.0;
+        __syncthreads();
+        for (int b = 0; b < MT; ++b) {
+            const int64_t mb = b0 + b;
+            double sn = 0.0, ss = 0.0;
+            if (mb < nmaps)
+                for (int j = threadIdx.x; j < n; j += blockDim.x) {
+                    sn += maps[mb * npix + g.start_n + j];
+                    if (paired) ss += maps[mb * npix + g.start_s + j];
+                }
+            for (int off = 16; off > 0; off >>= 1) {
+                sn += __shfl_xor_sync(0xffffffffu, sn, off);
+                ss += __shfl_xor_sync(0xffffffffu, ss, off);
+            }
+            if ((threadIdx.x & 31) == 0) {
+                atomicAdd(&ring_sum[2 * b], sn);
+                atomicAdd(&ring_sum[2 * b + 1], ss);
+            }
+        }
+        __syncthreads();
+    }
     for (int idx = threadIdx.x; idx < MT * n; idx += blockDim.x) {
         const int b = idx / n;
         const int j = idx - b * n;
         const int64_t mb = b0 + b;
         cx<T> v = {0, 0};
         if (mb < nmaps) {
-            v.x = (T)maps[mb * npix + g.start_n + j];
-            if (paired) v.y = (T)maps[mb * npix + g.start_s + j];
+            const double mn = reduced ? ring_sum[2 * b] / n : 0.0;
+            const double ms = reduced ? ring_sum[2 * b + 1] / n : 0.0;
+            v.x = (T)(maps[mb * npix + g.start_n + j] - mn);
+            if (paired) v.y = (T)(maps[mb * npix + g.start_s + j] - ms);
         }
         if (o > 1) src[(int64_t)b * n + j] = v;
         else buf[(int64_t)b * n + bitrev(j, s)] = v;
@@ -131,8 +160,13 @@ __global__ void __launch_bounds__(256) k_ring_analysis(const RingGeom *rings, in
         const int nk = (n - k) % n;
         const cx<T> Z = buf[(int64_t)b * n + (k % o) * P + k / o];
         const cx<T> Zn = buf[(int64_t)b * n + (nk % o) * P + nk / o];
-        const T fnx = (Z.x + Zn.x) * (T)0.5, fny = (Z.y - Zn.y) * (T)0.5;
-        const T fsx = (Z.y + Zn.y) * (T)0.5, fsy = -(Z.x - Zn.x) * (T)0.5;
+        T fnx = (Z.x + Zn.x) * (T)0.5, fny = (Z.y - Zn.y) * (T)0.5;
+        T fsx = (Z.y + Zn.y) * (T)0.5, fsy = -(Z.x - Zn.x) * (T)0.5;
+        if (reduced && k == 0) {   // bin 0 = ring sums, exact in FP64
+            fnx = (T)ring_sum[2 * b];
+            fsx = (T)ring_sum[2 * b + 1];
+            fny = fsy = (T)0;
+        }
         double sn = 0.0, cs = 1.0;
         if (g.phi0_den != 0) sincospi((double)m / (double)g.phi0_den, &sn, &cs);
         const T pc = (T)(w * cs), ps = (T)(-w * sn);   // w * e^{-i m phi0}
@@ -219,23 +253,34 @@ __global__ void __launch_bounds__(256) k_ring_synthesis(const RingGeom *rings, i
 
 static int ring_mt(const Plan &p, size_t elem) {
     const size_t n = (size_t)(4 * p.nside);
-    for (int mt = 4; mt >= 1; mt >>= 1)
+    for (int mt = 8; mt >= 1; mt >>= 1)
         if (n * elem * (1 + 2 * (size_t)mt) <= 200 * 1024) return mt;
     return 0;
 }
 
 void launch_ring_analysis(const Plan &p, const double *maps, int64_t nmaps, double *F, cudaStream_t st) {
-    const int MT = ring_mt(p, sizeof(cx<double>));
-    const size_t smem = (size_t)(4 * p.nside) * sizeof(cx<double>) * (1 + 2 * MT);
     static bool attr_set = false;
     if (!attr_set) {
         cudaFuncSetAttribute(k_ring_analysis<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        cudaFuncSetAttribute(k_ring_analysis<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
         attr_set = true;
     }
-    dim3 grid((unsigned)p.nrn, (unsigned)((nmaps + MT - 1) / MT));
     const double w = 4.0 * M_PI / (double)p.npix;
+    if (p.precision == SFB_MIXED) {
+        const int MT = ring_mt(p, sizeof(cx<float>));
+        const size_t smem = (size_t)(4 * p.nside) * sizeof(cx<float>) * (1 + 2 * MT);
+        dim3 grid((unsigned)p.nrn, (unsigned)((nmaps + MT - 1) / MT));
+        k_ring_analysis<float><<<grid, 256, smem, st>>>(p.d_rings, (int)p.nrn, p.lmax, w, p.npix, maps, nmaps,
+                                                        MT, (float *)F, 2 * nmaps);
+        note_launch();
+        return;
+    }
+    const int MT = ring_mt(p, sizeof(cx<double>));
+    const size_t smem = (size_t)(4 * p.nside) * sizeof(cx<double>) * (1 + 2 * MT);
+    dim3 grid((unsigned)p.nrn, (unsigned)((nmaps + MT - 1) / MT));
     k_ring_analysis<double><<<grid, 256, smem, st>>>(p.d_rings, (int)p.nrn, p.lmax, w, p.npix, maps, nmaps,
                                                      MT, F, 2 * nmaps);
+                                                     note_launch();
 }
 
 void launch_ring_synthesis(const Plan &p, const double *G, int64_t nmaps, double *maps, cudaStream_t st) {
@@ -249,6 +294,7 @@ void launch_ring_synthesis(const Plan &p, const double *G, int64_t nmaps, double
     dim3 grid((unsigned)p.nrn, (unsigned)((nmaps + MT - 1) / MT));
     k_ring_synthesis<double><<<grid, 256, smem, st>>>(p.d_rings, (int)p.nrn, p.lmax, G, 2 * nmaps, nmaps, MT,
                                                       p.npix, maps);
+                                                      note_launch();
 }
 
 }  // namespace sfb

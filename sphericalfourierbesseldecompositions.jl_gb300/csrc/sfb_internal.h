@@ -35,6 +35,7 @@ enum : int {
     ERR_NONFINITE_INPUT = 1,
     ERR_THETA_RANGE = 2,
     ERR_NONFINITE_OUTPUT = 4,
+    ERR_TC_TIMEOUT = 8,        // a bounded mbarrier wait in a tensor-core kernel gave up
 };
 
 // ---------------------------------------------------------------------------
@@ -80,6 +81,11 @@ struct Plan {
     // device tables
     RingGeom *d_rings = nullptr;
     double *d_lam = nullptr;        // Legendre table, FP64
+    float *d_lam32 = nullptr;       // the same table rounded to FP32 (mixed precision)
+    void *d_lamtc = nullptr;        // split-BF16 table in tensor-core operand layout (analysis)
+    int64_t *d_lamtc_off = nullptr; // [2*(lmax+1)+1] block offsets (bf16 elements)
+    void *d_lamts = nullptr;        // split-BF16 table in tensor-core operand layout (synthesis)
+    int64_t *d_lamts_off = nullptr;
     int64_t *d_lam_off = nullptr;   // [2*(lmax+1)] offset of block (m, parity)
     int64_t lam_elems = 0;
     int64_t *d_spl_off = nullptr;
@@ -102,6 +108,9 @@ struct Plan {
 
 int grow(Plan &p, DevBuf<double> &b, size_t n);
 
+// Count of kernels this library has launched (process-wide).
+void note_launch();
+
 // ---------------------------------------------------------------------------
 // kernels (launch wrappers; all enqueue on `st`)
 // ---------------------------------------------------------------------------
@@ -120,6 +129,14 @@ void launch_radial_coeffs(const Plan &p, const double *gl_x, const double *pq, i
 void launch_project_poly(const Plan &p, const double *A, int64_t ldA, double scale, int window_kind,
                          const double *w_ln, int64_t mask_col, const double *Awin, int64_t ldW,
                          double *out, cudaStream_t st);
+void launch_to_float(const double *in, int64_t n, float *out, cudaStream_t st);
+// tensor-core (tcgen05) Legendre analysis, mixed precision
+int64_t tc_table_offsets(const Plan &p, std::vector<int64_t> &off);
+void launch_build_lamtc(const Plan &p, cudaStream_t st);
+void launch_leg_analysis_tc(const Plan &p, const float *F, int64_t ncol, float *A, bool accumulate, cudaStream_t st);
+int64_t tc_synth_table_offsets(const Plan &p, std::vector<int64_t> &off);
+void launch_build_lamts(const Plan &p, cudaStream_t st);
+void launch_leg_synthesis_tc(const Plan &p, const float *A, int64_t ncol, float *G, cudaStream_t st);
 void launch_transpose(const double *in, int64_t rows, int64_t cols, double *out, cudaStream_t st);
 void launch_check_finite(const double *x, int64_t n, int *err, cudaStream_t st);
 void launch_ang2pix(int64_t nside, const double *theta, const double *phi, int64_t n, int64_t *pix,

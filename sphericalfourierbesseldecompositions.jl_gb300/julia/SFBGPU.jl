@@ -1,0 +1,170 @@
+# SFBGPU.jl - Julia binding of libsfbgpu.so (include/sfb_gpu.h) for
+# SphericalFourierBesselDecompositions.jl.
+#
+# Drop-in replacements for SFB.cat2amln / SFB.cat2nlm, SFB.field2anlm,
+# SFB.anlm2field and SFB.win_rhat_ln (reference src/cat2anlm.jl:257-422,
+# src/windows.jl:244-270) with the same argument meaning.  The device plan is
+# built once per AnlmModes (its k_nl, spline tables and ordering) and freed by
+# a finalizer.  Errors map to the exceptions the reference raises.
+module SFBGPU
+
+using SphericalFourierBesselDecompositions
+const SFB = SphericalFourierBesselDecompositions
+
+const libsfb = get(ENV, "SFBGPU_LIB", joinpath(@__DIR__, "..", "libsfbgpu.so"))
+
+const SFB_OK, SFB_EINVAL, SFB_ENOMEM, SFB_ENONFINITE, SFB_ERANGE, SFB_ETIMEOUT, SFB_ECUDA, SFB_ENOTSUP = 0:7
+const PRECISION = Dict(:fp64 => Int32(0), :mixed => Int32(1))
+const RADIAL = Dict(:poly => Int32(0), :spline => Int32(1))
+
+# Field order and types follow sfb_plan_desc / sfb_window exactly.
+struct PlanDesc
+    nside::Int64
+    lmax::Int64
+    nmax::Int64
+    lmax_n::Ptr{Int64}
+    rmin::Float64
+    rmax::Float64
+    spl_offset::Ptr{Int64}
+    spl_x::Ptr{Float64}
+    spl_y::Ptr{Float64}
+    spl_ypp::Ptr{Float64}
+    niter::Int32
+    precision::Int32
+    radial_mode::Int32
+    radial_pieces::Int32
+    radial_degree::Int32
+    radial_tol::Float64
+end
+
+struct Window
+    kind::Int32
+    mask::Ptr{Float64}
+    w_ln::Ptr{Float64}
+    dense::Ptr{Float64}
+end
+
+function lasterror()
+    buf = Vector{UInt8}(undef, 1024)
+    ccall((:sfb_last_error, libsfb), Cint, (Ptr{UInt8}, Csize_t), buf, length(buf))
+    return unsafe_string(pointer(buf))
+end
+
+function check(st::Integer)
+    st == SFB_OK && return nothing
+    msg = lasterror()
+    st == SFB_ENONFINITE && throw(AssertionError(msg))      # @assert all(isfinite.(anlm))
+    st == SFB_EINVAL && throw(ArgumentError(msg))
+    st == SFB_ERANGE && error(msg)                           # mymap2alm!'s lmax > 4*nside error
+    error("libsfbgpu status $st: $msg")
+end
+
+mutable struct Plan
+    handle::Ptr{Cvoid}
+    nlmsize::Int
+    npix::Int
+end
+
+function Plan(amodes::SFB.AnlmModes; niter=3, precision=:mixed, radial=:poly,
+              pieces=0, degree=0, tol=0.0)
+    pairs = [(n, l) for n in 1:amodes.nmax for l in 0:amodes.lmax_n[n]]
+    gnl = amodes.basisfunctions.gnl          # Spline1D{3} per (n, l+1)
+    xs = [gnl[n, l+1].x for (n, l) in pairs]
+    off = Int64[0; cumsum(length.(xs))]
+    x = reduce(vcat, xs)
+    y = reduce(vcat, [gnl[n, l+1].y for (n, l) in pairs])
+    ypp = reduce(vcat, [gnl[n, l+1].ypp for (n, l) in pairs])
+    lmax_n = Int64.(amodes.lmax_n)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    GC.@preserve x y ypp off lmax_n begin
+        d = PlanDesc(amodes.nside, amodes.lmax, amodes.nmax, pointer(lmax_n), amodes.rmin, amodes.rmax,
+                     pointer(off), pointer(x), pointer(y), pointer(ypp), niter, PRECISION[precision],
+                     RADIAL[radial], pieces, degree, tol)
+        check(ccall((:sfb_plan_create, libsfb), Cint, (Ref{PlanDesc}, Ref{Ptr{Cvoid}}), d, h))
+    end
+    p = Plan(h[], SFB.getnlmsize(amodes), 12 * amodes.nside^2)
+    finalizer(q -> ccall((:sfb_plan_destroy, libsfb), Cvoid, (Ptr{Cvoid},), q.handle), p)
+    return p
+end
+
+const PLANS = IdDict{Any,Plan}()
+getplan(amodes; kw...) = get!(() -> Plan(amodes; kw...), PLANS, (amodes, kw...))
+
+function window(w, amodes)
+    if w isa SFB.SeparableArrays.SeparableArray
+        return Window(1, pointer(w.mask), pointer(w.w_ln), C_NULL), (w.mask, w.w_ln)
+    end
+    W = Array{Float64,3}(w)                  # npix x (lmax+1) x nmax, column-major
+    return Window(2, C_NULL, C_NULL, pointer(W)), (W,)
+end
+
+"""
+    cat2amln(rθϕ, amodes, nbar, win_rhat_ln, weight=ones(N); kw...)
+
+Same contract as `SFB.cat2amln` (src/cat2anlm.jl:257-310); runs on the GPU.
+"""
+function cat2amln(rθϕ, amodes, nbar, win_rhat_ln, weight=ones(size(rθϕ, 2)); kw...)
+    p = getplan(amodes; kw...)
+    r = Matrix{Float64}(rθϕ)
+    N = size(r, 2)
+    w = isempty(weight) ? C_NULL : Vector{Float64}(weight)
+    anlm = Vector{ComplexF64}(undef, p.nlmsize)
+    win, keep = window(win_rhat_ln, amodes)
+    GC.@preserve r w keep anlm begin
+        check(ccall((:sfb_cat2amln, libsfb), Cint,
+                    (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Int64, Float64, Ref{Window}, Ptr{ComplexF64}),
+                    p.handle, N == 0 ? C_NULL : r, w, N, nbar, win, anlm))
+    end
+    return anlm
+end
+
+const cat2nlm = cat2amln
+
+"""
+    field2anlm(f_xyz, wmodes, amodes)    (src/cat2anlm.jl:323-357)
+"""
+function field2anlm(f_xyz, wmodes, amodes; kw...)
+    p = getplan(amodes; kw...)
+    f = Matrix{Float64}(f_xyz)
+    out = Vector{ComplexF64}(undef, p.nlmsize)
+    GC.@preserve f out check(ccall((:sfb_field2anlm, libsfb), Cint,
+                                   (Ptr{Cvoid}, Ptr{Float64}, Int64, Float64, Float64, Ptr{ComplexF64}),
+                                   p.handle, f, wmodes.nr, wmodes.rmin, wmodes.rmax, out))
+    return out
+end
+
+"""
+    anlm2field(f_nlm, wmodes, amodes)    (src/cat2anlm.jl:383-422)
+"""
+function anlm2field(f_nlm, wmodes, amodes; kw...)
+    p = getplan(amodes; kw...)
+    a = Vector{ComplexF64}(f_nlm)
+    f = Matrix{Float64}(undef, wmodes.nr, p.npix)
+    GC.@preserve a f check(ccall((:sfb_anlm2field, libsfb), Cint,
+                                 (Ptr{Cvoid}, Ptr{ComplexF64}, Int64, Float64, Float64, Ptr{Float64}),
+                                 p.handle, a, wmodes.nr, wmodes.rmin, wmodes.rmax, f))
+    return f
+end
+
+"""
+    win_rhat_ln(win, wmodes, amodes)    (src/windows.jl:244-270)
+"""
+function win_rhat_ln(win, wmodes, amodes; kw...)
+    p = getplan(amodes; kw...)
+    if win isa SFB.SeparableArrays.SeparableArray
+        phi = Vector{Float64}(win.phi)
+        W = Matrix{Float64}(undef, amodes.lmax + 1, amodes.nmax)
+        GC.@preserve phi W check(ccall((:sfb_win_rhat_ln_separable, libsfb), Cint,
+                                       (Ptr{Cvoid}, Ptr{Float64}, Int64, Float64, Float64, Ptr{Float64}),
+                                       p.handle, phi, wmodes.nr, wmodes.rmin, wmodes.rmax, W))
+        return SFB.SeparableArrays.SeparableArray(win.mask, W, name1=:mask, name2=:w_ln)
+    end
+    w = Matrix{Float64}(win)
+    W = Array{Float64,3}(undef, p.npix, amodes.lmax + 1, amodes.nmax)
+    GC.@preserve w W check(ccall((:sfb_win_rhat_ln_dense, libsfb), Cint,
+                                 (Ptr{Cvoid}, Ptr{Float64}, Int64, Float64, Float64, Ptr{Float64}),
+                                 p.handle, w, wmodes.nr, wmodes.rmin, wmodes.rmax, W))
+    return W
+end
+
+end # module

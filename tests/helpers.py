@@ -1,5 +1,8 @@
 """Shared test helpers: oracle mode dicts, seeded catalogues, error measures."""
 
+import json
+import os
+
 import numpy as np
 
 
@@ -49,3 +52,12 @@ def round_sig(z, digits=6):
         return out
     z = np.asarray(z)
     return r(z.real) + 1j * r(z.imag)
+
+
+def record(name, value, **extra):
+    """Append a measured parity figure to $SFB_PARITY_REPORT (JSON lines), if set."""
+    path = os.environ.get("SFB_PARITY_REPORT")
+    if not path:
+        return
+    with open(path, "a") as f:
+        f.write(json.dumps({"case": name, "rel_err": float(value), **extra}) + "\n")
