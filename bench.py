@@ -203,24 +203,56 @@ def run_reference_sample(amodes, gal, w, nbar, mask, wln_arr, steps, warmup, wor
 
 
 # ----------------------------------------------------------------------------- GPU arm
-def roofline_for(stage, ms_per_launch, launches, plan_info, peaks, nm):
-    """Algorithmic work of one launch of the dominant stage and its fraction of the measured peak."""
-    L = 238
-    lmsize = (L + 1) * (L + 2) // 2
+def stage_work(stage, precision, nm, ngal, nbasis, lmax=238):
+    """Algorithmic work of ONE launch of a stage: (kind, amount).
+
+    leg_*: 2 flop per (l, m, north ring, real column) -- the ring sum over the
+    2*nside north rings (the N/S symmetry is part of the algorithm here);
+    ring_fft: FP64 maps read + ring spectra written; fold: F, G read + R
+    written; deposit: galaxy records read + basis maps written."""
+    lmsize = (lmax + 1) * (lmax + 2) // 2
     nrn = 2 * NSIDE
     npix = 12 * NSIDE ** 2
     ncol = 2 * nm
+    t = 4 if precision == "mixed" else 8
+    fsz = 2 * (lmax + 1) * nrn * ncol * t
     if stage in ("leg_analysis", "leg_synthesis"):
-        flops = 2.0 * lmsize * nrn * ncol                 # one contraction over all m (N/S symmetry counted once)
-        achieved = flops / (ms_per_launch * 1e-3) / 1e12
-        return {"bound": "fp64", "achieved": achieved, "unit": "TFLOP/s", "flops_per_launch": flops}
+        return ("flop", 2.0 * lmsize * nrn * ncol)
     if stage == "ring_fft":
-        byts = 8.0 * nm * npix + 8.0 * 2 * 2 * (L + 1) * nrn * nm
-        achieved = byts / (ms_per_launch * 1e-3) / 1e9
-        return {"bound": "hbm", "achieved": achieved, "unit": "GB/s", "bytes_per_launch": byts}
+        return ("byte", float(t) * nm * npix + fsz)     # maps are FP32 in mixed precision
+    if stage == "fold":
+        return ("byte", 3.0 * fsz)
     if stage == "deposit":
-        return {"bound": "hbm", "achieved": None, "unit": "GB/s"}
-    return {"bound": "hbm", "achieved": None, "unit": "GB/s"}
+        return ("byte", 32.0 * ngal + float(t) * nbasis * npix)
+    return ("byte", None)
+
+
+def roofline_table(stages, precision, nm, ngal, nbasis, peaks, fp64_peak):
+    out = {}
+    for st, v in stages.items():
+        n = max(v["launches_per_step"], 1)
+        ms = v["ms_per_step"] / n
+        kind, amount = stage_work(st, precision, nm, ngal, nbasis)
+        if amount is None or ms <= 0:
+            continue
+        if st == "deposit":
+            # the deposit is several kernels (sort + moments); count its work once per step
+            ms = v["ms_per_step"]
+        if kind == "flop":
+            ach = amount / (ms * 1e-3) / 1e12
+            if precision == "mixed":
+                peak, bound, src = peaks.get("bf16_tflops", 1900.0), "tensor", "MEASURED_PEAKS.json bf16_tflops (burst)"
+            else:
+                peak, bound, src = fp64_peak, "fp64", "cuBLAS DGEMM 8192^3 measured in this run"
+            out[st] = {"bound": bound, "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+                       "per_launch": amount, "ms_per_launch": ms, "peak_source": src}
+        else:
+            ach = amount / (ms * 1e-3) / 1e9
+            peak = peaks.get("hbm_gbs", 6800.0)
+            out[st] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                       "per_launch": amount, "ms_per_launch": ms,
+                       "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback"}
+    return out
 
 
 def fp64_gemm_peak(torch):
@@ -253,9 +285,17 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-workers", type=int, default=0)
     ap.add_argument("--cpu-pairs", type=int, default=0)
+    ap.add_argument("--profile-case", action="store_true",
+                    help="small case for ncu captures: same geometry, 2 radial pieces x degree 15 (34 maps), "
+                         "1e6 galaxies, no e2e / CPU baseline")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    plan_extra = {}
+    if args.profile_case:
+        args.ngal = args.ngal or 1_000_000
+        args.no_cpu_baseline = True
+        plan_extra = {"pieces": 2, "degree": 15}
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -305,13 +345,13 @@ def main():
         dist.init_process_group("nccl")
 
     amodes = sfbgpu.AnlmModes(KMAX, RMIN, RMAX, nside=NSIDE)
-    plan = sfbgpu.get_plan(amodes, precision=args.precision, radial="poly")
+    plan = sfbgpu.get_plan(amodes, precision=args.precision, radial="poly", **plan_extra)
     info = plan.info()
     gal, w = make_catalogue(seed=2 + rank)
     N = gal.shape[0]
     wm, phi, mask = window_arrays(sfbgpu, amodes)
     winsep = sfbgpu.win_rhat_ln(sfbgpu.SeparableArray(phi, mask, "phi", "mask"), wm, amodes,
-                                precision=args.precision, radial="poly")
+                                precision=args.precision, radial="poly", **plan_extra)
     wln = np.asfortranarray(winsep.w_ln)
     veff = sfbgpu.integrate_window(sfbgpu.SeparableArray(phi, mask), wm)
     nbar = N / veff
@@ -368,6 +408,10 @@ def main():
               for i, nm in enumerate(capi.STAGES)}
     value = N * world / (ms * 1e-3)
 
+    if args.profile_case:
+        if rank == 0:
+            print(json.dumps({"profile_case": True, "ms_per_step": ms, "stages": stages}), flush=True)
+        return
     # end to end: host-pointer C-ABI call from pinned memory
     h_gal = torch.from_numpy(gal).pin_memory()
     h_w = torch.from_numpy(w).pin_memory()
@@ -395,26 +439,18 @@ def main():
     res_dev = d_out.cpu().numpy()
     same = float(np.max(np.abs(h_out.numpy() - res_dev)) / max(np.max(np.abs(res_dev)), 1e-300))
 
-    # roofline of the dominant stage
-    dom = max(stages, key=lambda k: stages[k]["ms_per_step"])
-    nlaunch = max(stages[dom]["launches_per_step"], 1)
-    ms_launch = stages[dom]["ms_per_step"] / nlaunch
+    # roofline of every stage; the headline is the dominant one
     nm = info["nbasis"] + 1
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except OSError:
         pass
-    roof = roofline_for(dom, ms_launch, nlaunch, info, peaks, nm)
-    if roof["bound"] == "fp64":
-        peak = fp64_gemm_peak(torch)
-        roof.update({"peak": peak, "peak_source": "cuBLAS DGEMM 8192^3 measured in this run"})
-    elif roof["bound"] == "hbm":
-        peak = peaks.get("hbm_gbs", 6800.0)
-        roof.update({"peak": peak, "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback"})
-    roof["frac"] = (roof["achieved"] / roof["peak"]) if roof.get("achieved") else None
+    fp64_peak = fp64_gemm_peak(torch) if args.precision == "fp64" else None
+    table = roofline_table(stages, args.precision, nm, N, info["nbasis"], peaks, fp64_peak)
+    dom = max(table, key=lambda k: stages[k]["ms_per_step"])
+    roof = dict(table[dom])
     roof["kernel_stage"] = dom
-    roof["ms_per_launch"] = ms_launch
     roof["traffic"] = None
 
     cpu = None
@@ -442,7 +478,7 @@ def main():
                 "roofline": roof, "cpu_baseline": cpu,
                 "e2e": {"value": N / e2e_s, "unit": "galaxies/s", "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(d2h), "host_vs_device_result_rel_diff": same},
-                "stages": stages, "clocks": clk, "gpu_launches": int(launches)}
+                "stages": stages, "stage_roofline": table, "clocks": clk, "gpu_launches": int(launches)}
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

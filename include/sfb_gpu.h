@@ -147,6 +147,24 @@ int sfb_win_rhat_ln_dense(sfb_plan *plan, const double *win, int64_t nr, double 
  * alm_out: [nmaps * 2 * lmsize], lmsize = (lmax+1)(lmax+2)/2, index l(l+1)/2+m. */
 int sfb_map2alm(sfb_plan *plan, const double *maps, int64_t nmaps, double *alm_out);
 
+/* amln2clnn(anlm1, anlm2, cmodes) (reference src/SphericalFourierBesselDecompositions.jl:114-150):
+ * C[i] = [Re(a1_{n1 l 0} a2_{n2 l 0}) + 2 sum_{m>=1} Re(a1_{n1 l m} conj(a2_{n2 l m}))] / (2l+1)
+ * for every column i of lnn (ClnnModes.lnn, 3 x nlnn column-major: l, n1, n2 with
+ * 1-based n), for nbatch coefficient vectors stored one after another
+ * (anlm: [nbatch * 2 * nlmsize]; anlm2 may be NULL or equal to anlm1 for the
+ * auto spectrum).  clnn_out: [nbatch * nlnn], vector b at b * nlnn. */
+int sfb_amln2clnn(sfb_plan *plan, const double *anlm1, const double *anlm2, int64_t nbatch,
+                  const int64_t *lnn, int64_t nlnn, double *clnn_out);
+
+/* winweights2galweights(weights, wmodes, rθϕ) (reference src/cat2anlm.jl:218-238):
+ * w_out[i] = weights[bin, pix] with pix the RING pixel of (theta_i, phi_i) and
+ * bin = nr if r_i == rbounds[nr], else the largest j with rbounds[j-1] <= r_i
+ * (Julia's searchsortedlast over get_rbounds(wmodes), passed as rbounds[nr+1]).
+ * weights: [nr * npix], element (bin, pix) at (bin-1) + nr*pix.  A radius
+ * outside the shells returns SFB_ERANGE (the reference's "r out of bounds"). */
+int sfb_winweights2galweights(int64_t nside, const double *weights, int64_t nr, const double *rbounds,
+                              const double *rtp, int64_t ngal, double *w_out);
+
 /* HEALPix RING pixel (0-based; Healpix.jl ang2pixRing returns this + 1) of
  * n directions, computed on the device with the binning kernel's arithmetic. */
 int sfb_ang2pix_ring(int64_t nside, const double *theta, const double *phi, int64_t n,
@@ -173,6 +191,12 @@ int sfb_set_profiling(sfb_plan *plan, int32_t enable);
 int sfb_get_stage_times(const sfb_plan *plan, double *ms, int64_t *launches);
 /* Number of kernels this library has launched in this process. */
 int64_t sfb_launch_count(void);
+
+/* Failure-detection self-test (no counterpart in the reference): launches one
+ * CTA whose bounded mbarrier wait has no arrival, so the wait expires after
+ * about a second and the kernel records the timeout in its error word.
+ * Returns SFB_ETIMEOUT when the bound works; the CUDA context stays usable. */
+int sfb_selftest_wait_timeout(void);
 
 /* Text of the last error on this thread (NUL-terminated, truncated to len). */
 int sfb_last_error(char *buf, size_t len);

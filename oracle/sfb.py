@@ -9,6 +9,8 @@ and follows one reference function:
 * ``anlm2field``     src/cat2anlm.jl:383-422
 * ``win_rhat_ln``    src/windows.jl:244-257 (dense), :260-270 (separable)
 * ``integrate_window`` src/windows.jl:219-228
+* ``amln2clnn``      src/SphericalFourierBesselDecompositions.jl:114-150
+* ``winweights2galweights`` src/cat2anlm.jl:218-238
 
 ``modes`` arguments are dicts with ``nmax``, ``lmax``, ``lmax_n`` (list over n),
 ``nside``, ``splines`` {(n, l): (x, y, ypp)} and ``noff`` (offset of each n
@@ -161,3 +163,38 @@ def integrate_window(win, rmin, rmax, nr):
     rs = np.linspace(rmin + dr / 2, rmax - dr / 2, nr)
     npix = win.shape[1]
     return dr * (4 * np.pi / npix) * np.sum(win.sum(axis=1) * rs ** 2)
+
+
+def alm2cl(a1, a2, l):
+    """One l of alm2cl (src/SphericalFourierBesselDecompositions.jl:114-129): m = 0
+    enters as Re(a1 a2) (no conjugate), m > 0 as 2 Re(a1 conj(a2))."""
+    c = (a1[0] * a2[0]).real
+    for m in range(1, l + 1):
+        c += 2 * (a1[m] * np.conj(a2[m])).real
+    return c / (2 * l + 1)
+
+
+def amln2clnn(anlm1, anlm2, lnn, modesA, modesB=None):
+    """C_l(n1, n2) for the columns (l, n1, n2) of lnn (src/...:136-148)."""
+    modesB = modesA if modesB is None else modesB
+    out = np.full(lnn.shape[1], np.nan)
+    for i in range(lnn.shape[1]):
+        l, n1, n2 = (int(v) for v in lnn[:, i])
+        a = anlm1[_idx0(modesA, n1, l, 0):_idx0(modesA, n1, l, 0) + l + 1]
+        b = anlm2[_idx0(modesB, n2, l, 0):_idx0(modesB, n2, l, 0) + l + 1]
+        out[i] = alm2cl(a, b, l)
+    return out
+
+
+def winweights2galweights(weights, rbounds, nside, rtp):
+    """w_i = weights[bin, pix] (src/cat2anlm.jl:218-238); bin = searchsortedlast(rbounds, r),
+    or nr when r == rmax; raises for r out of bounds."""
+    rtp = np.asarray(rtp, float)
+    nr = weights.shape[0]
+    r = rtp[0]
+    pix = ang2pix_ring(nside, rtp[1], rtp[2])
+    b = np.searchsorted(rbounds, r, side="right")      # 1-based searchsortedlast
+    b = np.where(r == rbounds[-1], nr, b)
+    if np.any((b < 1) | (b > nr)):
+        raise ValueError("r out of bounds")
+    return weights[b - 1, pix]

@@ -1,0 +1,243 @@
+// Galaxy deposit without floating-point atomics.
+//
+// The deposit D_b[p] = sum_{i in p} w_i phi_b(r_i) is organised as a counting
+// sort of the galaxies by key = slot * npix + pixel, where slot is the radial
+// piece (0..pieces-1) or one of the two out-of-range slots (r < rmin,
+// r > rmax):
+//   1. keys:    per galaxy, pixel (bit-exact HEALPix), slot and local
+//               coordinate x in [-1, 1]; an int atomic on the key's counter
+//               gives the galaxy its rank inside the bin;
+//   2. scan:    exclusive prefix sum of the (pieces + 2) * npix counters;
+//   3. scatter: (x, w) to its sorted position;
+//   4. moments: one thread per (slot, pixel) sums w P_k(x) over its galaxies
+//               in registers and writes every basis map element exactly once
+//               (coalesced over consecutive pixels; empty bins write zeros,
+//               so the maps need no clearing).
+// Summation order inside a bin follows the int-atomic ranks, so repeated
+// calls agree to rounding, not bit for bit.
+#include "sfb_internal.h"
+
+namespace sfb {
+
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 16;                    // per thread
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+__global__ void k_deposit_keys(const double *__restrict__ rtp, const double *__restrict__ wgt, int64_t ngal,
+                               int64_t nside, int64_t npix, double rmin, double rmax, int pieces,
+                               int32_t *__restrict__ counts, int32_t *__restrict__ key, int32_t *__restrict__ rank,
+                               double *__restrict__ xloc, int *err) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ngal) return;
+    const double r = rtp[3 * i], th = rtp[3 * i + 1], ph = rtp[3 * i + 2];
+    const double w = wgt ? wgt[i] : 1.0;
+    int32_t k = -1;
+    double x = 0.0;
+    if (!(isfinite(r) && isfinite(th) && isfinite(ph) && isfinite(w))) {
+        atomicOr(err, ERR_NONFINITE_INPUT);
+    } else if (th < 0.0 || th > M_PI) {
+        atomicOr(err, ERR_THETA_RANGE);
+    } else {
+        const int64_t pix = ang2pix_ring_z(nside, cos(th), ph);
+        int slot;
+        if (r < rmin) {
+            slot = pieces;
+        } else if (r > rmax) {
+            slot = pieces + 1;
+        } else {
+            const double width = (rmax - rmin) / pieces;
+            slot = (int)((r - rmin) / width);
+            if (slot >= pieces) slot = pieces - 1;
+            x = 2.0 * (r - (rmin + slot * width)) / width - 1.0;
+            x = fmin(1.0, fmax(-1.0, x));
+        }
+        k = (int32_t)(slot * npix + pix);
+        rank[i] = atomicAdd(counts + k, 1);
+    }
+    key[i] = k;
+    xloc[i] = x;
+}
+
+// Exclusive scan, tile pass: each block scans SCAN_TILE counters in place and
+// writes its total.
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tiles(int32_t *__restrict__ data, int64_t n,
+                                                             int32_t *__restrict__ tile_sums) {
+    __shared__ int32_t warp_tot[SCAN_THREADS / 32];
+    const int64_t base = (int64_t)blockIdx.x * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
+    int32_t v[SCAN_ITEMS];
+    int32_t s = 0;
+#pragma unroll
+    for (int j = 0; j < SCAN_ITEMS; ++j) {
+        const int64_t idx = base + j;
+        v[j] = idx < n ? data[idx] : 0;
+        s += v[j];
+    }
+    // exclusive scan of thread sums across the block
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int32_t inc = s;
+    for (int off = 1; off < 32; off <<= 1) {
+        const int32_t t = __shfl_up_sync(0xffffffffu, inc, off);
+        if (lane >= off) inc += t;
+    }
+    if (lane == 31) warp_tot[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        int32_t wv = lane < SCAN_THREADS / 32 ? warp_tot[lane] : 0;
+        for (int off = 1; off < 32; off <<= 1) {
+            const int32_t t = __shfl_up_sync(0xffffffffu, wv, off);
+            if (lane >= off) wv += t;
+        }
+        if (lane < SCAN_THREADS / 32) warp_tot[lane] = wv;   // inclusive warp prefix
+    }
+    __syncthreads();
+    int32_t run = inc - s + (wid > 0 ? warp_tot[wid - 1] : 0);
+#pragma unroll
+    for (int j = 0; j < SCAN_ITEMS; ++j) {
+        const int64_t idx = base + j;
+        if (idx < n) data[idx] = run;
+        run += v[j];
+    }
+    if (threadIdx.x == SCAN_THREADS - 1) tile_sums[blockIdx.x] = run;
+}
+
+// Scan of the tile totals by one block (serial over chunks of 1024).
+__global__ void k_scan_sums(int32_t *__restrict__ sums, int64_t n) {
+    __shared__ int32_t buf[1024];
+    __shared__ int32_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int64_t c0 = 0; c0 < n; c0 += 1024) {
+        const int64_t idx = c0 + threadIdx.x;
+        const int32_t v = idx < n ? sums[idx] : 0;
+        buf[threadIdx.x] = v;
+        __syncthreads();
+        for (int off = 1; off < 1024; off <<= 1) {
+            const int32_t t = threadIdx.x >= off ? buf[threadIdx.x - off] : 0;
+            __syncthreads();
+            buf[threadIdx.x] += t;
+            __syncthreads();
+        }
+        const int32_t excl = buf[threadIdx.x] - v + carry;
+        if (idx < n) sums[idx] = excl;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry = excl + v;
+        __syncthreads();
+    }
+}
+
+__global__ void k_scan_add(int32_t *__restrict__ data, int64_t n, const int32_t *__restrict__ tile_sums) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx < n) data[idx] += tile_sums[idx / SCAN_TILE];
+}
+
+__global__ void k_deposit_scatter(const double *__restrict__ wgt, int64_t ngal, const int32_t *__restrict__ key,
+                                  const int32_t *__restrict__ rank, const double *__restrict__ xloc,
+                                  const int32_t *__restrict__ offset, double2 *__restrict__ sorted) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ngal) return;
+    const int32_t k = key[i];
+    if (k < 0) return;
+    const int64_t pos = (int64_t)offset[k] + rank[i];
+    sorted[pos] = make_double2(xloc[i], wgt ? wgt[i] : 1.0);
+}
+
+// One thread per (slot, pixel): Legendre moments of its galaxies.
+template <int MAXDEG, typename TM>
+__global__ void k_deposit_moments(const int32_t *__restrict__ offset, const double2 *__restrict__ sorted,
+                                  int64_t npix, int pieces, int deg, int64_t nbasis, TM *__restrict__ maps) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nkeys = (int64_t)(pieces + 2) * npix;
+    if (idx >= nkeys) return;
+    const int slot = (int)(idx / npix);
+    const int64_t pix = idx - (int64_t)slot * npix;
+    const int64_t g0 = offset[idx];
+    const int64_t g1 = offset[idx + 1];         // offset[nkeys] = number of keyed galaxies
+    if (slot >= pieces) {       // constant extrapolation maps (r < rmin, r > rmax)
+        double s = 0.0;
+        for (int64_t g = g0; g < g1; ++g) s += sorted[g].y;
+        maps[(nbasis - 2 + (slot - pieces)) * npix + pix] = (TM)s;
+        return;
+    }
+    double acc[MAXDEG + 1];
+#pragma unroll
+    for (int k = 0; k <= MAXDEG; ++k) acc[k] = 0.0;
+    for (int64_t g = g0; g < g1; ++g) {
+        const double2 xw = sorted[g];
+        const double x = xw.x, w = xw.y;
+        double p0 = 1.0, p1 = x;
+        acc[0] += w;
+        if (MAXDEG >= 1) acc[1] += w * x;
+#pragma unroll
+        for (int k = 1; k < MAXDEG; ++k) {
+            if (k >= deg) break;
+            // (k+1) P_{k+1} = (2k+1) x P_k - k P_{k-1}; coefficients fold to constants
+            const double p2 = ((double)(2 * k + 1) / (k + 1)) * x * p1 - ((double)k / (k + 1)) * p0;
+            acc[k + 1] += w * p2;
+            p0 = p1;
+            p1 = p2;
+        }
+    }
+    TM *base = maps + (int64_t)slot * (deg + 1) * npix + pix;
+#pragma unroll
+    for (int k = 0; k <= MAXDEG; ++k)
+        if (k <= deg) base[(int64_t)k * npix] = (TM)acc[k];
+}
+
+int deposit_sorted(Plan &p, const double *rtp, const double *w, int64_t ngal, double *maps, cudaStream_t st) {
+    const int64_t nkeys = (int64_t)(p.pieces + 2) * p.npix;
+    const int64_t nscan = nkeys + 1;            // one extra counter: its exclusive prefix is the total
+    const int64_t ntiles = (nscan + SCAN_TILE - 1) / SCAN_TILE;
+    // workspace: counters/offsets [nscan] int32, tile sums [ntiles] int32, key and rank [ngal] int32,
+    // local coordinate [ngal] double, sorted (x, w) [ngal] double2
+    const int64_t ints = nscan + ntiles + 2 * ngal;
+    const int64_t off_x = (ints + 1) / 2;
+    int64_t off_sorted = off_x + ngal;
+    off_sorted += off_sorted & 1;
+    SFB_TRY(grow(p, p.dep, (size_t)(off_sorted + 2 * ngal + 2)));
+    int32_t *counts = reinterpret_cast<int32_t *>(p.dep.ptr);
+    int32_t *tsum = counts + nscan;
+    int32_t *key = tsum + ntiles;
+    int32_t *rank = key + ngal;
+    double *xloc = p.dep.ptr + off_x;
+    double2 *sorted = reinterpret_cast<double2 *>(p.dep.ptr + off_sorted);
+    SFB_CUDA_TRY(cudaMemsetAsync(counts, 0, (size_t)nscan * sizeof(int32_t), st));
+    if (ngal > 0) {
+        k_deposit_keys<<<(unsigned)((ngal + 255) / 256), 256, 0, st>>>(rtp, w, ngal, p.nside, p.npix, p.rmin, p.rmax,
+                                                                       p.pieces, counts, key, rank, xloc, p.d_err);
+        note_launch();
+    }
+    k_scan_tiles<<<(unsigned)ntiles, SCAN_THREADS, 0, st>>>(counts, nscan, tsum);
+    note_launch();
+    k_scan_sums<<<1, 1024, 0, st>>>(tsum, ntiles);
+    note_launch();
+    k_scan_add<<<(unsigned)((nscan + 255) / 256), 256, 0, st>>>(counts, nscan, tsum);
+    note_launch();
+    if (ngal > 0) {
+        k_deposit_scatter<<<(unsigned)((ngal + 255) / 256), 256, 0, st>>>(w, ngal, key, rank, xloc, counts, sorted);
+        note_launch();
+    }
+    const unsigned blocks = (unsigned)((nkeys + 127) / 128);
+    if (p.degree > 63) return fail(SFB_ENOTSUP, "radial degree above 63 is not supported by the sorted deposit");
+    // moments in FP64; the maps are stored in the transform's precision
+    if (p.precision == SFB_MIXED) {
+        float *m32 = reinterpret_cast<float *>(maps);
+        if (p.degree <= 15)
+            k_deposit_moments<15, float><<<blocks, 128, 0, st>>>(counts, sorted, p.npix, p.pieces, p.degree, p.nbasis, m32);
+        else if (p.degree <= 31)
+            k_deposit_moments<31, float><<<blocks, 128, 0, st>>>(counts, sorted, p.npix, p.pieces, p.degree, p.nbasis, m32);
+        else
+            k_deposit_moments<63, float><<<blocks, 128, 0, st>>>(counts, sorted, p.npix, p.pieces, p.degree, p.nbasis, m32);
+    } else {
+        if (p.degree <= 15)
+            k_deposit_moments<15, double><<<blocks, 128, 0, st>>>(counts, sorted, p.npix, p.pieces, p.degree, p.nbasis, maps);
+        else if (p.degree <= 31)
+            k_deposit_moments<31, double><<<blocks, 128, 0, st>>>(counts, sorted, p.npix, p.pieces, p.degree, p.nbasis, maps);
+        else
+            k_deposit_moments<63, double><<<blocks, 128, 0, st>>>(counts, sorted, p.npix, p.pieces, p.degree, p.nbasis, maps);
+    }
+    note_launch();
+    SFB_CUDA_TRY(cudaGetLastError());
+    return SFB_OK;
+}
+
+}  // namespace sfb

@@ -150,41 +150,50 @@ __global__ void __launch_bounds__(256) k_leg_synthesis(const T *__restrict__ lam
 // and (m -/+ m') is a multiple of n, phi0 = pi/den with den in {0, n}, so
 // every phase is +1 or (-1)^t.  G_0 enters through its real part.
 template <typename T>
-__global__ void k_fold_residual(const RingGeom *rings, int nrn, int lmax, double w, const T *__restrict__ F,
-                                const T *__restrict__ G, int64_t ncplx, T *__restrict__ R) {
-    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int mp = blockIdx.y;
-    const int r = blockIdx.z % nrn;
-    const int par = blockIdx.z / nrn;
-    if (c >= ncplx) return;
+__global__ void __launch_bounds__(128) k_fold_residual(const RingGeom *rings, int nrn, int lmax, double w,
+                                                      const T *__restrict__ F, const T *__restrict__ G, int64_t ncplx,
+                                                      T *__restrict__ R) {
+    // one block per (parity, m', ring); threads stride over the complex columns
+    const int mp = blockIdx.x;
+    const int r = blockIdx.y;
+    const int par = blockIdx.z;
     const RingGeom g = rings[r];
     const int n = g.nph;
     const int L1 = lmax + 1;
     const int64_t ld = 2 * ncplx;
     const bool odd_phase = g.phi0_den != 0;   // e^{i t n phi0} = (-1)^t when phi0 = pi/n
-    double sx = 0.0, sy = 0.0;
+    const T f = (T)(w * (double)n * g.cfold);
+    const int64_t off = ((int64_t)(par * L1 + mp) * nrn + r) * ld;
     const int k = mp % n;
-    int t = 0;
-    for (int m = k; m <= lmax; m += n, ++t) {
-        const T *gp = G + ((int64_t)(par * L1 + m) * nrn + r) * ld + 2 * c;
-        // (m - m') = (t - t0) n with t0 = m' / n
-        const int dt = t - mp / n;
-        const double sgn = (odd_phase && (dt & 1)) ? -1.0 : 1.0;
-        sx += sgn * gp[0];
-        sy += (m == 0) ? 0.0 : sgn * gp[1];
-    }
     const int kk = (n - k) % n;
-    for (int m = (kk == 0 ? n : kk); m <= lmax; m += n) {
-        const T *gp = G + ((int64_t)(par * L1 + m) * nrn + r) * ld + 2 * c;
-        const int q = (m + mp) / n;   // (m + m') = q n exactly
-        const double sgn = (odd_phase && (q & 1)) ? -1.0 : 1.0;
-        sx += sgn * gp[0];
-        sy -= sgn * gp[1];
+    if (n > 2 * lmax) {   // no aliasing on this ring: Fold(G)_{m'} = G_{m'} (real part for m' = 0)
+        for (int64_t c = threadIdx.x; c < ncplx; c += blockDim.x) {
+            const T gx = G[off + 2 * c], gy = mp == 0 ? T(0) : G[off + 2 * c + 1];
+            R[off + 2 * c] = F[off + 2 * c] - f * gx;
+            R[off + 2 * c + 1] = F[off + 2 * c + 1] - f * gy;
+        }
+        return;
     }
-    const double f = w * (double)n * g.cfold;
-    const int64_t off = ((int64_t)(par * L1 + mp) * nrn + r) * ld + 2 * c;
-    R[off] = (T)((double)F[off] - f * sx);
-    R[off + 1] = (T)((double)F[off + 1] - f * sy);
+    for (int64_t c = threadIdx.x; c < ncplx; c += blockDim.x) {
+        T sx = 0, sy = 0;
+        int t = 0;
+        for (int m = k; m <= lmax; m += n, ++t) {
+            const T *gp = G + ((int64_t)(par * L1 + m) * nrn + r) * ld + 2 * c;
+            const int dt = t - mp / n;                       // (m - m') = dt * n
+            const T sgn = (odd_phase && (dt & 1)) ? T(-1) : T(1);
+            sx += sgn * gp[0];
+            if (m != 0) sy += sgn * gp[1];
+        }
+        for (int m = (kk == 0 ? n : kk); m <= lmax; m += n) {
+            const T *gp = G + ((int64_t)(par * L1 + m) * nrn + r) * ld + 2 * c;
+            const int q = (m + mp) / n;                      // (m + m') = q * n
+            const T sgn = (odd_phase && (q & 1)) ? T(-1) : T(1);
+            sx += sgn * gp[0];
+            sy -= sgn * gp[1];
+        }
+        R[off + 2 * c] = F[off + 2 * c] - f * sx;
+        R[off + 2 * c + 1] = F[off + 2 * c + 1] - f * sy;
+    }
 }
 
 void launch_leg_analysis(const Plan &p, const double *F, int64_t ncol, double *A, bool accumulate,
@@ -213,13 +222,13 @@ void launch_leg_synthesis(const Plan &p, const double *A, int64_t ncol, double *
 void launch_fold_residual(const Plan &p, const double *F, const double *G, int64_t ncol, double *R,
                           cudaStream_t st) {
     const int64_t ncplx = ncol / 2;
-    dim3 grid((unsigned)((ncplx + 63) / 64), (unsigned)(p.lmax + 1), (unsigned)(2 * p.nrn));
+    dim3 grid((unsigned)(p.lmax + 1), (unsigned)p.nrn, 2u);
     const double w = 4.0 * M_PI / (double)p.npix;
     if (p.precision == SFB_MIXED)
-        k_fold_residual<float><<<grid, 64, 0, st>>>(p.d_rings, (int)p.nrn, p.lmax, w, (const float *)F,
-                                                    (const float *)G, ncplx, (float *)R);
+        k_fold_residual<float><<<grid, 128, 0, st>>>(p.d_rings, (int)p.nrn, p.lmax, w, (const float *)F,
+                                                     (const float *)G, ncplx, (float *)R);
     else
-        k_fold_residual<double><<<grid, 64, 0, st>>>(p.d_rings, (int)p.nrn, p.lmax, w, F, G, ncplx, R);
+        k_fold_residual<double><<<grid, 128, 0, st>>>(p.d_rings, (int)p.nrn, p.lmax, w, F, G, ncplx, R);
     note_launch();
 }
 

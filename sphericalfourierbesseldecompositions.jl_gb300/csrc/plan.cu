@@ -80,6 +80,10 @@ void launch_subtract_sep_chunk(const Plan &p, double *maps, const double *mask, 
 void launch_transpose_ld(const double *in, int64_t ldi, int64_t rows, int64_t cols, double *out, int64_t ldo,
                          cudaStream_t st);
 void launch_axpy(double *y, const double *x, int64_t n, cudaStream_t st);
+void launch_winweights(const double *weights, int64_t nr, int64_t nside, const double *rbounds, double rmax,
+                       const double *rtp, int64_t ngal, double *w, int *err, cudaStream_t st);
+void launch_amln2clnn(const double *a1, const double *a2, int64_t nlmsize, const int64_t *lnn, int64_t nlnn,
+                      int64_t nbatch, const int64_t *noff, double *out, cudaStream_t st);
 
 }  // namespace sfb
 
@@ -286,9 +290,19 @@ int choose_radial_basis(sfb_plan *h, const sfb_plan_desc *d) {
     return SFB_OK;
 }
 
-// map2alm with niter refinement on nm maps already in p.maps; result in p.alm [lmsize][2*nm].
-int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st) {
+// map2alm with niter refinement on nm maps; result in p.alm [lmsize][2*nm] (FP64).
+// In mixed precision the maps are FP32 ([nm][npix] floats); maps_are_fp64 marks
+// FP64 maps that are converted first.
+int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, bool maps_are_fp64 = false) {
     Plan &p = h->p;
+    if (p.precision == SFB_MIXED && maps_are_fp64) {
+        SFB_TRY(grow(p, p.maps32, (size_t)(nm * p.npix + 1) / 2));
+        {
+            Stage s(h, SFB_STAGE_OTHER, st);
+            launch_to_float(maps, nm * p.npix, reinterpret_cast<float *>(p.maps32.ptr), st);
+        }
+        maps = p.maps32.ptr;
+    }
     const int64_t ncol = 2 * nm;
     const size_t fsz = (size_t)2 * (p.lmax + 1) * p.nrn * ncol;
     SFB_TRY(grow(p, p.fbuf, fsz));
@@ -301,14 +315,14 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st) {
     const bool tc = p.precision == SFB_MIXED;
     auto analysis = [&](const double *src, bool acc) {
         Stage s(h, SFB_STAGE_LEG_ANALYSIS, st);
-        if (tc) launch_leg_analysis_tc(p, (const float *)src, ncol, (float *)p.alm.ptr, acc, st);
+        if (tc) launch_leg_analysis_tc(p, (const float *)src, ncol, p.alm.ptr, acc, st);
         else launch_leg_analysis(p, src, ncol, p.alm.ptr, acc, st);
     };
     analysis(p.fbuf.ptr, false);
     for (int it = 0; it < p.niter; ++it) {
         {
             Stage s(h, SFB_STAGE_LEG_SYNTHESIS, st);
-            if (tc) launch_leg_synthesis_tc(p, (const float *)p.alm.ptr, ncol, (float *)p.gbuf.ptr, st);
+            if (tc) launch_leg_synthesis_tc(p, p.alm.ptr, ncol, (float *)p.gbuf.ptr, st);
             else launch_leg_synthesis(p, p.alm.ptr, ncol, p.gbuf.ptr, st);
         }
         { Stage s(h, SFB_STAGE_FOLD, st); launch_fold_residual(p, p.fbuf.ptr, p.gbuf.ptr, ncol, p.rbuf.ptr, st); }
@@ -362,14 +376,18 @@ int cat2amln_dev(sfb_plan *h, const double *rtp, const double *w, int64_t ngal, 
     if (p.radial_mode == SFB_RADIAL_POLY) {
         const int64_t nm = p.nbasis + (wk == SFB_WINDOW_SEPARABLE ? 1 : 0);
         SFB_TRY(grow(p, p.maps, (size_t)nm * p.npix));
-        {
+        if (wk == SFB_WINDOW_SEPARABLE) {
             Stage s(h, SFB_STAGE_OTHER, st);
-            SFB_CUDA_TRY(cudaMemsetAsync(p.maps.ptr, 0, (size_t)p.nbasis * p.npix * sizeof(double), st));
-            if (wk == SFB_WINDOW_SEPARABLE)
+            if (p.precision == SFB_MIXED)
+                launch_to_float(win->mask, p.npix, reinterpret_cast<float *>(p.maps.ptr) + p.nbasis * p.npix, st);
+            else
                 SFB_CUDA_TRY(cudaMemcpyAsync(p.maps.ptr + p.nbasis * p.npix, win->mask, p.npix * sizeof(double),
                                              cudaMemcpyDeviceToDevice, st));
         }
-        { Stage s(h, SFB_STAGE_DEPOSIT, st); launch_deposit_poly(p, rtp, w, ngal, p.maps.ptr, st); }
+        {
+            Stage s(h, SFB_STAGE_DEPOSIT, st);
+            SFB_TRY(deposit_sorted(p, rtp, w, ngal, p.maps.ptr, st));
+        }
         SFB_TRY(sht_analysis(h, p.maps.ptr, nm, st));
         {
             Stage s(h, SFB_STAGE_PROJECT, st);
@@ -381,7 +399,7 @@ int cat2amln_dev(sfb_plan *h, const double *rtp, const double *w, int64_t ngal, 
             for (int64_t p0 = 0; p0 < p.npairs; p0 += cp) {
                 const int64_t npc = std::min(cp, p.npairs - p0);
                 launch_gather_dense_chunk(p, p.maps.ptr, win->dense, p0, npc, st);
-                SFB_TRY(sht_analysis(h, p.maps.ptr, npc, st));
+                SFB_TRY(sht_analysis(h, p.maps.ptr, npc, st, true));
                 launch_sub_window_chunk(p, p.alm.ptr, 2 * npc, p0, npc, out, st);
             }
         }
@@ -395,7 +413,7 @@ int cat2amln_dev(sfb_plan *h, const double *rtp, const double *w, int64_t ngal, 
             { Stage s(h, SFB_STAGE_DEPOSIT, st); launch_deposit_spline_chunk(p, rtp, w, ngal, p0, npc, scale, p.maps.ptr, st); }
             if (wk == SFB_WINDOW_DENSE) launch_subtract_dense_chunk(p, p.maps.ptr, win->dense, p0, npc, st);
             if (wk == SFB_WINDOW_SEPARABLE) launch_subtract_sep_chunk(p, p.maps.ptr, win->mask, win->w_ln, p0, npc, st);
-            SFB_TRY(sht_analysis(h, p.maps.ptr, npc, st));
+            SFB_TRY(sht_analysis(h, p.maps.ptr, npc, st, true));
             launch_extract_spline_chunk(p, p.alm.ptr, 2 * npc, p0, npc, out, st);
         }
     }
@@ -528,6 +546,43 @@ int sfb_plan_create(const sfb_plan_desc *d, sfb_plan **out) {
             break;
         }
         if ((st = upload(p, &p.d_rings, p.h_rings.data(), p.h_rings.size())) != SFB_OK) break;
+        {
+            // twiddle and ring-phase tables (FP64; rounded to the kernel precision on load)
+            std::vector<int64_t> twoff(p.nrn);
+            std::vector<double2> tw;
+            for (int64_t r = 0; r < p.nrn; ++r) {
+                const int n = p.h_rings[r].nph;
+                twoff[r] = (int64_t)tw.size();
+                for (int t = 0; t < n; ++t) {
+                    // e^{-2 pi i t/n}: reduce t/n to [0, 1) then use the symmetric range for accuracy
+                    const double a = 2.0 * M_PI * (double)t / (double)n;
+                    tw.push_back(make_double2(std::cos(a), -std::sin(a)));
+                }
+            }
+            std::vector<double2> ph((size_t)p.nrn * (p.lmax + 1));
+            for (int64_t r = 0; r < p.nrn; ++r) {
+                const int den = p.h_rings[r].phi0_den;
+                for (int m = 0; m <= p.lmax; ++m) {
+                    // phi0 = pi/den: reduce m mod 2*den exactly before the trig call
+                    const double a = den ? M_PI * (double)(m % (2 * den)) / (double)den : 0.0;
+                    ph[(size_t)r * (p.lmax + 1) + m] = make_double2(std::cos(a), -std::sin(a));
+                }
+            }
+            const double wq = 4.0 * M_PI / (double)p.npix;
+            std::vector<double2> wph(ph.size());
+            std::vector<float2> tw32(tw.size()), wph32(ph.size());
+            for (size_t i = 0; i < ph.size(); ++i) {
+                wph[i] = make_double2(wq * ph[i].x, wq * ph[i].y);
+                wph32[i] = make_float2((float)wph[i].x, (float)wph[i].y);
+            }
+            for (size_t i = 0; i < tw.size(); ++i) tw32[i] = make_float2((float)tw[i].x, (float)tw[i].y);
+            if ((st = upload(p, &p.d_twoff, twoff.data(), twoff.size())) != SFB_OK) break;
+            if ((st = upload(p, &p.d_twtab, tw.data(), tw.size())) != SFB_OK) break;
+            if ((st = upload(p, &p.d_phase, ph.data(), ph.size())) != SFB_OK) break;
+            if ((st = upload(p, &p.d_wphase, wph.data(), wph.size())) != SFB_OK) break;
+            if ((st = upload(p, &p.d_twtab32, tw32.data(), tw32.size())) != SFB_OK) break;
+            if ((st = upload(p, &p.d_wphase32, wph32.data(), wph32.size())) != SFB_OK) break;
+        }
         std::vector<int64_t> lam_off(2 * (p.lmax + 1));
         int64_t off = 0;
         for (int m = 0; m <= p.lmax; ++m)
@@ -596,9 +651,9 @@ void sfb_plan_destroy(sfb_plan *h) {
     Plan &p = h->p;
     cudaSetDevice(p.device);
     if (h->stream) cudaStreamSynchronize(h->stream);
-    void *ptrs[] = {p.d_rings, p.d_lam, p.d_lam32, p.d_lamtc, p.d_lamtc_off, p.d_lamts, p.d_lamts_off, p.d_lam_off, p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp,
+    void *ptrs[] = {p.d_rings, p.d_twtab, p.d_twoff, p.d_phase, p.d_wphase, p.d_twtab32, p.d_wphase32, p.d_lam, p.d_lam32, p.d_lamtc, p.d_lamtc_off, p.d_lamts, p.d_lamts_off, p.d_lam_off, p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp,
                     p.d_pair_l, p.d_pair_n, p.d_out_pair, p.d_out_lm, p.d_coef, p.d_err,
-                    p.maps.ptr, p.fbuf.ptr, p.gbuf.ptr, p.rbuf.ptr, p.alm.ptr, p.scratch.ptr, p.scratch2.ptr,
+                    p.maps.ptr, p.fbuf.ptr, p.gbuf.ptr, p.rbuf.ptr, p.alm.ptr, p.scratch.ptr, p.scratch2.ptr, p.dep.ptr, p.maps32.ptr,
                     h->d_pair_index, h->d_noff};
     for (void *q : ptrs)
         if (q) cudaFree(q);
@@ -833,6 +888,78 @@ int sfb_win_rhat_ln_dense(sfb_plan *h, const double *win, int64_t nr, double rmi
     SFB_CUDA_TRY(cudaMemcpyAsync(w_out, d_o, (size_t)nout * sizeof(double), cudaMemcpyDeviceToHost, st));
     SFB_CUDA_TRY(cudaStreamSynchronize(st));
     return SFB_OK;
+}
+
+int sfb_amln2clnn(sfb_plan *h, const double *anlm1, const double *anlm2, int64_t nbatch, const int64_t *lnn,
+                  int64_t nlnn, double *clnn_out) {
+    SFB_TRY(check_plan(h));
+    SFB_TRY(set_device_of(h));
+    if (!anlm1 || !lnn || !clnn_out || nbatch < 1 || nlnn < 0) return fail(SFB_EINVAL, "bad amln2clnn arguments");
+    Plan &p = h->p;
+    for (int64_t i = 0; i < nlnn; ++i) {
+        const int64_t l = lnn[3 * i], n1 = lnn[3 * i + 1], n2 = lnn[3 * i + 2];
+        if (n1 < 1 || n2 < 1 || n1 > p.nmax || n2 > p.nmax || l < 0 || l > p.lmax_n[n1 - 1] || l > p.lmax_n[n2 - 1])
+            return fail(SFB_EINVAL, "lnn entry " + std::to_string(i) + " is not a mode of the plan");
+    }
+    if (nlnn == 0) return SFB_OK;
+    cudaStream_t st = h->stream;
+    const int64_t na = 2 * p.nlmsize * nbatch;
+    const bool same = anlm2 == nullptr || anlm2 == anlm1;
+    // [a1][a2][lnn (as doubles' storage)][out]
+    const size_t need = (size_t)(na * (same ? 1 : 2) + 3 * nlnn + nlnn * nbatch);
+    SFB_TRY(grow(p, p.scratch, need));
+    double *d1 = p.scratch.ptr;
+    double *d2 = same ? d1 : d1 + na;
+    int64_t *dl = reinterpret_cast<int64_t *>(d2 + na);
+    double *dout = reinterpret_cast<double *>(dl + 3 * nlnn);
+    SFB_CUDA_TRY(cudaMemcpyAsync(d1, anlm1, na * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (!same) SFB_CUDA_TRY(cudaMemcpyAsync(d2, anlm2, na * sizeof(double), cudaMemcpyHostToDevice, st));
+    SFB_CUDA_TRY(cudaMemcpyAsync(dl, lnn, 3 * nlnn * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    launch_amln2clnn(d1, d2, p.nlmsize, dl, nlnn, nbatch, h->d_noff, dout, st);
+    SFB_CUDA_TRY(cudaGetLastError());
+    SFB_CUDA_TRY(cudaMemcpyAsync(clnn_out, dout, nlnn * nbatch * sizeof(double), cudaMemcpyDeviceToHost, st));
+    SFB_CUDA_TRY(cudaStreamSynchronize(st));
+    return SFB_OK;
+}
+
+int sfb_winweights2galweights(int64_t nside, const double *weights, int64_t nr, const double *rbounds,
+                              const double *rtp, int64_t ngal, double *w_out) {
+    if (nside < 1 || nr < 1 || !weights || !rbounds || ngal < 0 || (ngal > 0 && (!rtp || !w_out)))
+        return fail(SFB_EINVAL, "bad winweights2galweights arguments");
+    if (ngal == 0) return SFB_OK;
+    const int64_t npix = 12 * nside * nside;
+    const size_t bytes = sizeof(double) * (size_t)(nr * npix + nr + 1 + 3 * ngal + ngal) + sizeof(int);
+    char *d = nullptr;
+    if (cudaMalloc(&d, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(SFB_ENOMEM, "device allocation failed");
+    }
+    double *dw = reinterpret_cast<double *>(d);
+    double *db = dw + nr * npix;
+    double *dr = db + nr + 1;
+    double *dout = dr + 3 * ngal;
+    int *derr = reinterpret_cast<int *>(dout + ngal);
+    int st = SFB_OK;
+    int herr = 0;
+    do {
+        if (cudaMemcpy(dw, weights, sizeof(double) * nr * npix, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(db, rbounds, sizeof(double) * (nr + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(dr, rtp, sizeof(double) * 3 * ngal, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemset(derr, 0, sizeof(int)) != cudaSuccess) {
+            st = fail(SFB_ECUDA, cudaGetErrorString(cudaGetLastError()));
+            break;
+        }
+        launch_winweights(dw, nr, nside, db, rbounds[nr], dr, ngal, dout, derr, 0);
+        if (cudaMemcpy(w_out, dout, sizeof(double) * ngal, cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) {
+            st = fail(SFB_ECUDA, cudaGetErrorString(cudaGetLastError()));
+            break;
+        }
+        if (herr & ERR_NONFINITE_INPUT) st = fail(SFB_ENONFINITE, "non-finite galaxy coordinate");
+        else if (herr & ERR_RANGE_R) st = fail(SFB_ERANGE, "r out of bounds");
+    } while (0);
+    cudaFree(d);
+    return st;
 }
 
 int sfb_ang2pix_ring(int64_t nside, const double *theta, const double *phi, int64_t n, int64_t *pix_out) {

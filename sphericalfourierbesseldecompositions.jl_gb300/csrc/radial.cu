@@ -25,50 +25,6 @@ __device__ __forceinline__ bool galaxy_ok(double r, double th, double ph, double
     return true;
 }
 
-// One thread per galaxy: HEALPix pixel, piece, Legendre values P_0..P_deg of
-// the local coordinate, scatter-add w*P_k into map (piece*(deg+1)+k).
-__global__ void k_deposit_poly(const double *__restrict__ rtp, const double *__restrict__ wgt, int64_t ngal,
-                               int64_t nside, int64_t npix, double rmin, double rmax, int pieces, int deg,
-                               int64_t nbasis, double *__restrict__ maps, int *err) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= ngal) return;
-    const double r = rtp[3 * i], th = rtp[3 * i + 1], ph = rtp[3 * i + 2];
-    const double w = wgt ? wgt[i] : 1.0;
-    if (!galaxy_ok(r, th, ph, w, err)) return;
-    const int64_t pix = ang2pix_ring_z(nside, cos(th), ph);
-    if (r < rmin) {
-        atomicAdd(maps + (nbasis - 2) * npix + pix, w);
-        return;
-    }
-    if (r > rmax) {
-        atomicAdd(maps + (nbasis - 1) * npix + pix, w);
-        return;
-    }
-    const double width = (rmax - rmin) / pieces;
-    int j = (int)((r - rmin) / width);
-    if (j >= pieces) j = pieces - 1;
-    double x = 2.0 * (r - (rmin + j * width)) / width - 1.0;
-    x = fmin(1.0, fmax(-1.0, x));
-    double *base = maps + (int64_t)j * (deg + 1) * npix + pix;
-    double p0 = 1.0, p1 = x;
-    atomicAdd(base, w);
-    if (deg >= 1) atomicAdd(base + npix, w * x);
-    for (int k = 1; k < deg; ++k) {
-        const double p2 = ((2 * k + 1) * x * p1 - k * p0) / (k + 1);
-        atomicAdd(base + (int64_t)(k + 1) * npix, w * p2);
-        p0 = p1;
-        p1 = p2;
-    }
-}
-
-void launch_deposit_poly(const Plan &p, const double *rtp, const double *w, int64_t ngal, double *maps,
-                         cudaStream_t st) {
-    if (ngal <= 0) return;
-    k_deposit_poly<<<(unsigned)((ngal + 255) / 256), 256, 0, st>>>(rtp, w, ngal, p.nside, p.npix, p.rmin, p.rmax,
-                                                                   p.pieces, p.degree, p.nbasis, maps, p.d_err);
-                                                                   note_launch();
-}
-
 // Spline mode: maps[q][pix] += w * g_{pair0+q}(r) / (nbar dOmega) for a chunk of pairs.
 __global__ void k_deposit_spline(const double *__restrict__ rtp, const double *__restrict__ wgt, int64_t ngal,
                                  int64_t nside, int64_t npix, const int64_t *spl_off, const double *sx,
@@ -280,12 +236,8 @@ void launch_project_poly(const Plan &p, const double *A, int64_t ldA, double sca
                          cudaStream_t st) {
     (void)Awin; (void)ldW;
     if (p.nlmsize <= 0) return;
-    if (p.precision == SFB_MIXED)
-        k_project_poly<float><<<(unsigned)((p.nlmsize + 127) / 128), 128, 0, st>>>(
-            p.d_out_pair, p.d_out_lm, p.d_pair_n, p.d_pair_l, p.nlmsize, p.nbasis, p.d_coef, (const float *)A, ldA,
-            scale, window_kind, w_ln, p.lmax, mask_col, out);
-    else
-        k_project_poly<double><<<(unsigned)((p.nlmsize + 127) / 128), 128, 0, st>>>(
+    // a_lm are held in FP64 in both precision modes
+    k_project_poly<double><<<(unsigned)((p.nlmsize + 127) / 128), 128, 0, st>>>(
             p.d_out_pair, p.d_out_lm, p.d_pair_n, p.d_pair_l, p.nlmsize, p.nbasis, p.d_coef, A, ldA, scale,
             window_kind, w_ln, p.lmax, mask_col, out);
         note_launch();
@@ -438,6 +390,79 @@ __global__ void k_win_dense(const int32_t *pair_n, const int32_t *pair_l, int64_
 void launch_win_dense_g(const Plan &p, const double *gtab, int64_t nr, const double *win, double *out, cudaStream_t st) {
     dim3 grid((unsigned)((p.npix + 127) / 128), (unsigned)p.npairs);
     k_win_dense<<<grid, 128, 0, st>>>(p.d_pair_n, p.d_pair_l, p.npairs, gtab, nr, win, p.npix, p.lmax, out);
+    note_launch();
+}
+
+// amln2clnn (src/SphericalFourierBesselDecompositions.jl:114-150): one warp per
+// (l, n1, n2) column of lnn (3 x nlnn, 1-based n), over nbatch coefficient vectors:
+// C = [Re(a1_0 a2_0) + 2 sum_{m>=1} Re(a1_m conj(a2_m))] / (2l + 1).
+__global__ void k_amln2clnn(const double *__restrict__ a1, const double *__restrict__ a2, int64_t nlmsize,
+                            const int64_t *__restrict__ lnn, int64_t nlnn, int64_t nbatch, const int64_t *noff,
+                            double *__restrict__ out) {
+    const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (wid >= nlnn * nbatch) return;
+    const int64_t b = wid / nlnn, i = wid - b * nlnn;
+    const int64_t l = lnn[3 * i], n1 = lnn[3 * i + 1], n2 = lnn[3 * i + 2];
+    const double *x = a1 + 2 * (b * nlmsize + noff[n1 - 1] + l * (l + 1) / 2);
+    const double *y = a2 + 2 * (b * nlmsize + noff[n2 - 1] + l * (l + 1) / 2);
+    double c = 0.0;
+    for (int64_t m = lane; m <= l; m += 32) {
+        const double xr = x[2 * m], xi = x[2 * m + 1], yr = y[2 * m], yi = y[2 * m + 1];
+        c += (m == 0) ? (xr * yr - xi * yi) : 2.0 * (xr * yr + xi * yi);
+    }
+    for (int off = 16; off > 0; off >>= 1) c += __shfl_xor_sync(0xffffffffu, c, off);
+    if (lane == 0) out[b * nlnn + i] = c / (double)(2 * l + 1);
+}
+
+void launch_amln2clnn(const double *a1, const double *a2, int64_t nlmsize, const int64_t *lnn, int64_t nlnn,
+                      int64_t nbatch, const int64_t *noff, double *out, cudaStream_t st) {
+    const int64_t threads = nlnn * nbatch * 32;
+    if (threads <= 0) return;
+    k_amln2clnn<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(a1, a2, nlmsize, lnn, nlnn, nbatch, noff, out);
+    note_launch();
+}
+
+// winweights2galweights (src/cat2anlm.jl:218-238): w_i = weights[bin(r_i), pix(theta_i, phi_i)]
+// with bin = nr if r == rmax, else searchsortedlast(rbounds, r) (1-based), over
+// the caller's rbounds[0..nr].  Out-of-range bins set ERR_RANGE_R and give NaN.
+__global__ void k_winweights(const double *__restrict__ weights, int64_t nr, int64_t npix, int64_t nside,
+                             const double *__restrict__ rbounds, double rmax, const double *__restrict__ rtp,
+                             int64_t ngal, double *__restrict__ w, int *err) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ngal) return;
+    const double r = rtp[3 * i], th = rtp[3 * i + 1], ph = rtp[3 * i + 2];
+    if (!(isfinite(r) && isfinite(th) && isfinite(ph))) {
+        atomicOr(err, ERR_NONFINITE_INPUT);
+        w[i] = NAN;
+        return;
+    }
+    const int64_t pix = ang2pix_ring_z(nside, cos(th), ph);
+    int64_t bin;
+    if (r == rmax) {
+        bin = nr;
+    } else {
+        // largest 1-based j with rbounds[j] <= r (0 if none)
+        int64_t lo = 0, hi = nr + 1;
+        while (lo < hi) {
+            const int64_t mid = (lo + hi) >> 1;
+            if (rbounds[mid] <= r) lo = mid + 1; else hi = mid;
+        }
+        bin = lo;
+    }
+    if (bin < 1 || bin > nr) {
+        atomicOr(err, ERR_RANGE_R);
+        w[i] = NAN;
+        return;
+    }
+    w[i] = weights[(bin - 1) + nr * pix];
+}
+
+void launch_winweights(const double *weights, int64_t nr, int64_t nside, const double *rbounds, double rmax,
+                       const double *rtp, int64_t ngal, double *w, int *err, cudaStream_t st) {
+    if (ngal <= 0) return;
+    k_winweights<<<(unsigned)((ngal + 255) / 256), 256, 0, st>>>(weights, nr, 12 * nside * nside, nside, rbounds, rmax,
+                                                                 rtp, ngal, w, err);
     note_launch();
 }
 

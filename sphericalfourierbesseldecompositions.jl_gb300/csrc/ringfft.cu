@@ -78,23 +78,29 @@ __device__ void four_step(cx<T> *buf, cx<T> *src, const cx<T> *tw, int n, int o,
     }
 }
 
+// Twiddles W_n^t = e^{dir 2 pi i t / n} from the plan's FP64 table of
+// e^{-2 pi i t / n} (one block of n entries per ring, offset twoff).
 template <typename T>
-__device__ void fill_twiddles(cx<T> *tw, int n, int dir) {
+__device__ void fill_twiddles(cx<T> *tw, const double2 *__restrict__ tab, int n, int dir) {
     for (int t = threadIdx.x; t < n; t += blockDim.x) {
-        double sn, cs;
-        sincospi(dir * 2.0 * (double)t / (double)n, &sn, &cs);
-        tw[t] = {(T)cs, (T)sn};
+        const double2 v = tab[t];
+        tw[t] = {(T)v.x, (T)(dir < 0 ? v.y : -v.y)};
     }
 }
 
 // maps: FP64 [nmaps][npix]; F: [2][lmax+1][nrn][ldF] real view of complex,
 // column 2b / 2b+1 = re / im of map b.
-template <typename T>
-__global__ void __launch_bounds__(256) k_ring_analysis(const RingGeom *rings, int nrn, int lmax, double w,
-                                                       int64_t npix, const double *maps, int64_t nmaps,
-                                                       int MT, T *F, int64_t ldF) {
+// TI: element type of the input maps; TW: element type of the twiddle / phase
+// tables (double2 or float2).  The weighted-phase table holds w e^{-i m phi0}.
+template <typename T, typename TI, typename TW>
+__global__ void __launch_bounds__(256) k_ring_analysis(const RingGeom *rings, int nrn, int lmax,
+                                                       int64_t npix, const TI *maps, int64_t nmaps,
+                                                       int MT, T *F, int64_t ldF, int r0,
+                                                       const TW *__restrict__ twtab,
+                                                       const int64_t *__restrict__ twoff,
+                                                       const TW *__restrict__ wphase) {
     extern __shared__ unsigned char smem_raw[];
-    const int r = blockIdx.x;
+    const int r = r0 + blockIdx.x;
     const int64_t b0 = (int64_t)blockIdx.y * MT;
     const RingGeom g = rings[r];
     const int n = g.nph;
@@ -105,49 +111,56 @@ __global__ void __launch_bounds__(256) k_ring_analysis(const RingGeom *rings, in
     cx<T> *tw = reinterpret_cast<cx<T> *>(smem_raw);
     cx<T> *buf = tw + n;
     cx<T> *src = buf + (int64_t)MT * n;
-    fill_twiddles(tw, n, -1);
-    // Reduced precision: the ring sums (bin 0) are taken in FP64 and the DFT
-    // runs on the mean-subtracted values, so the FP32 arithmetic only carries
-    // the fluctuations about the ring mean (bins k != 0 are unchanged by it).
-    __shared__ double ring_sum[2 * 8];
-    constexpr bool reduced = sizeof(T) < sizeof(double);
-    if (reduced) {
-        if (threadIdx.x < 2 * MT) ring_sum[threadIdx.x] = 0.0;
-        __syncthreads();
-        for (int b = 0; b < MT; ++b) {
-            const int64_t mb = b0 + b;
-            double sn = 0.0, ss = 0.0;
-            if (mb < nmaps)
-                for (int j = threadIdx.x; j < n; j += blockDim.x) {
-                    sn += maps[mb * npix + g.start_n + j];
-                    if (paired) ss += maps[mb * npix + g.start_s + j];
-                }
-            for (int off = 16; off > 0; off >>= 1) {
-                sn += __shfl_xor_sync(0xffffffffu, sn, off);
-                ss += __shfl_xor_sync(0xffffffffu, ss, off);
-            }
-            if ((threadIdx.x & 31) == 0) {
-                atomicAdd(&ring_sum[2 * b], sn);
-                atomicAdd(&ring_sum[2 * b + 1], ss);
-            }
-        }
-        __syncthreads();
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        const TW v = twtab[twoff[r] + t];
+        tw[t] = {(T)v.x, (T)v.y};
     }
+    // Reduced precision: the ring sums (bin 0) are accumulated exactly enough
+    // in double-float (FP32 TwoSum) and replace the FFT's bin 0.
+    constexpr bool reduced = sizeof(T) < sizeof(double);
+    __shared__ float ring_hi[2 * 8], ring_lo[2 * 8];
     for (int idx = threadIdx.x; idx < MT * n; idx += blockDim.x) {
         const int b = idx / n;
         const int j = idx - b * n;
         const int64_t mb = b0 + b;
         cx<T> v = {0, 0};
         if (mb < nmaps) {
-            const double mn = reduced ? ring_sum[2 * b] / n : 0.0;
-            const double ms = reduced ? ring_sum[2 * b + 1] / n : 0.0;
-            v.x = (T)(maps[mb * npix + g.start_n + j] - mn);
-            if (paired) v.y = (T)(maps[mb * npix + g.start_s + j] - ms);
+            v.x = (T)maps[mb * npix + g.start_n + j];
+            if (paired) v.y = (T)maps[mb * npix + g.start_s + j];
         }
         if (o > 1) src[(int64_t)b * n + j] = v;
         else buf[(int64_t)b * n + bitrev(j, s)] = v;
     }
     __syncthreads();
+    if (reduced) {
+        // one warp per (map, ring of the pair): double-float sum of the staged values
+        const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        for (int q = wid; q < 2 * MT; q += blockDim.x >> 5) {
+            const int b = q >> 1, side = q & 1;
+            float hi = 0.f, lo = 0.f;
+            for (int j = lane; j < n; j += 32) {
+                const cx<T> v = (o > 1) ? src[(int64_t)b * n + j] : buf[(int64_t)b * n + bitrev(j, s)];
+                const float x = (float)(side ? v.y : v.x);
+                const float t = hi + x;
+                const float bb = t - hi;
+                lo += (hi - (t - bb)) + (x - bb);
+                hi = t;
+            }
+            for (int off = 16; off > 0; off >>= 1) {
+                const float oh = __shfl_xor_sync(0xffffffffu, hi, off);
+                const float ol = __shfl_xor_sync(0xffffffffu, lo, off);
+                const float t = hi + oh;
+                const float bb = t - hi;
+                lo += ol + (hi - (t - bb)) + (oh - bb);
+                hi = t;
+            }
+            if (lane == 0) {
+                ring_hi[q] = hi;
+                ring_lo[q] = lo;
+            }
+        }
+        __syncthreads();
+    }
     four_step<T>(buf, src, tw, n, o, s, MT);
     // unpack, phase, weight; write F+ and F-
     const int L1 = lmax + 1;
@@ -162,14 +175,13 @@ __global__ void __launch_bounds__(256) k_ring_analysis(const RingGeom *rings, in
         const cx<T> Zn = buf[(int64_t)b * n + (nk % o) * P + nk / o];
         T fnx = (Z.x + Zn.x) * (T)0.5, fny = (Z.y - Zn.y) * (T)0.5;
         T fsx = (Z.y + Zn.y) * (T)0.5, fsy = -(Z.x - Zn.x) * (T)0.5;
-        if (reduced && k == 0) {   // bin 0 = ring sums, exact in FP64
-            fnx = (T)ring_sum[2 * b];
-            fsx = (T)ring_sum[2 * b + 1];
+        if (reduced && k == 0) {   // bin 0 = ring sums (double-float)
+            fnx = (T)(ring_hi[2 * b] + ring_lo[2 * b]);
+            fsx = (T)(ring_hi[2 * b + 1] + ring_lo[2 * b + 1]);
             fny = fsy = (T)0;
         }
-        double sn = 0.0, cs = 1.0;
-        if (g.phi0_den != 0) sincospi((double)m / (double)g.phi0_den, &sn, &cs);
-        const T pc = (T)(w * cs), ps = (T)(-w * sn);   // w * e^{-i m phi0}
+        const TW ph = wphase[(int64_t)r * L1 + m];           // w e^{-i m phi0}
+        const T pc = (T)ph.x, ps = (T)ph.y;
         const T px = fnx + fsx, py = fny + fsy;
         const T qx = fnx - fsx, qy = fny - fsy;
         T *dp = F + ((int64_t)(0 * L1 + m) * nrn + r) * ldF + 2 * mb;
@@ -186,9 +198,12 @@ __global__ void __launch_bounds__(256) k_ring_analysis(const RingGeom *rings, in
 template <typename T>
 __global__ void __launch_bounds__(256) k_ring_synthesis(const RingGeom *rings, int nrn, int lmax,
                                                         const T *G, int64_t ldG, int64_t nmaps, int MT,
-                                                        int64_t npix, double *maps) {
+                                                        int64_t npix, double *maps, int r0,
+                                                        const double2 *__restrict__ twtab,
+                                                        const int64_t *__restrict__ twoff,
+                                                        const double2 *__restrict__ phase) {
     extern __shared__ unsigned char smem_raw[];
-    const int r = blockIdx.x;
+    const int r = r0 + blockIdx.x;
     const int64_t b0 = (int64_t)blockIdx.y * MT;
     const RingGeom g = rings[r];
     const int n = g.nph;
@@ -199,7 +214,7 @@ __global__ void __launch_bounds__(256) k_ring_synthesis(const RingGeom *rings, i
     cx<T> *tw = reinterpret_cast<cx<T> *>(smem_raw);
     cx<T> *buf = tw + n;
     cx<T> *src = buf + (int64_t)MT * n;
-    fill_twiddles(tw, n, +1);
+    fill_twiddles(tw, twtab + twoff[r], n, +1);
     const int L1 = lmax + 1;
     // spectrum of the packed sequence: c_k = CN_k + i CS_k
     for (int idx = threadIdx.x; idx < MT * n; idx += blockDim.x) {
@@ -215,8 +230,8 @@ __global__ void __launch_bounds__(256) k_ring_synthesis(const RingGeom *rings, i
                 double gnx = (double)gp[0] + (double)gq[0], gny = (double)gp[1] + (double)gq[1];
                 double gsx = (double)gp[0] - (double)gq[0], gsy = (double)gp[1] - (double)gq[1];
                 if (m == 0) { gny = 0; gsy = 0; }
-                double sn = 0.0, cs = 1.0;
-                if (g.phi0_den != 0) sincospi((double)m / (double)g.phi0_den, &sn, &cs);
+                const double2 ph = phase[(int64_t)r * L1 + m];     // e^{-i m phi0}
+                const double cs = ph.x, sn = -ph.y;                 // e^{+i m phi0}
                 cnx += gnx * cs - gny * sn; cny += gnx * sn + gny * cs;
                 csx += gsx * cs - gsy * sn; csy += gsx * sn + gsy * cs;
             }
@@ -227,8 +242,8 @@ __global__ void __launch_bounds__(256) k_ring_synthesis(const RingGeom *rings, i
                 const T *gq = G + ((int64_t)(1 * L1 + m) * nrn + r) * ldG + 2 * mb;
                 const double gnx = (double)gp[0] + (double)gq[0], gny = -((double)gp[1] + (double)gq[1]);
                 const double gsx = (double)gp[0] - (double)gq[0], gsy = -((double)gp[1] - (double)gq[1]);
-                double sn = 0.0, cs = 1.0;
-                if (g.phi0_den != 0) sincospi(-(double)m / (double)g.phi0_den, &sn, &cs);
+                const double2 ph = phase[(int64_t)r * L1 + m];     // e^{-i m phi0}
+                const double cs = ph.x, sn = ph.y;
                 cnx += gnx * cs - gny * sn; cny += gnx * sn + gny * cs;
                 csx += gsx * cs - gsy * sn; csy += gsx * sn + gsy * cs;
             }
@@ -251,50 +266,58 @@ __global__ void __launch_bounds__(256) k_ring_synthesis(const RingGeom *rings, i
     }
 }
 
-static int ring_mt(const Plan &p, size_t elem) {
-    const size_t n = (size_t)(4 * p.nside);
+static int ring_mt(size_t n, size_t elem, bool two_buffers) {
     for (int mt = 8; mt >= 1; mt >>= 1)
-        if (n * elem * (1 + 2 * (size_t)mt) <= 200 * 1024) return mt;
-    return 0;
+        if (n * elem * (1 + (two_buffers ? 2 : 1) * (size_t)mt) <= 96 * 1024) return mt;   // <= 2 CTAs per SM
+    return 1;
+}
+
+// Rings [0, nside-1) are polar (nph = 4i, odd factors possible), rings
+// [nside-1, 2*nside) equatorial (nph = 4*nside, one buffer when nside is a
+// power of two).  Each group is one launch with its own shared-memory size.
+template <typename T, typename TI, typename TW>
+static void ring_analysis_t(const Plan &p, const TI *maps, int64_t nmaps, T *F, const TW *tw, const TW *wph,
+                            cudaStream_t st) {
+    const int ns = (int)p.nside;
+    const bool pow2 = (ns & (ns - 1)) == 0;
+    struct Group { int r0, nr; size_t n; bool two; } groups[2] = {
+        {0, ns - 1, (size_t)(4 * (ns - 1)), true},
+        {ns - 1, ns + 1, (size_t)(4 * ns), !pow2}};
+    for (const Group &gr : groups) {
+        if (gr.nr <= 0) continue;
+        const int MT = ring_mt(gr.n, sizeof(cx<T>), gr.two);
+        const size_t smem = gr.n * sizeof(cx<T>) * (1 + (gr.two ? 2 : 1) * (size_t)MT);
+        set_smem(k_ring_analysis<T, TI, TW>, smem);
+        dim3 grid((unsigned)gr.nr, (unsigned)((nmaps + MT - 1) / MT));
+        k_ring_analysis<T, TI, TW><<<grid, 256, smem, st>>>(p.d_rings, (int)p.nrn, p.lmax, p.npix, maps, nmaps, MT,
+                                                            F, 2 * nmaps, gr.r0, tw, p.d_twoff, wph);
+        note_launch();
+    }
 }
 
 void launch_ring_analysis(const Plan &p, const double *maps, int64_t nmaps, double *F, cudaStream_t st) {
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_ring_analysis<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        cudaFuncSetAttribute(k_ring_analysis<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        attr_set = true;
-    }
-    const double w = 4.0 * M_PI / (double)p.npix;
-    if (p.precision == SFB_MIXED) {
-        const int MT = ring_mt(p, sizeof(cx<float>));
-        const size_t smem = (size_t)(4 * p.nside) * sizeof(cx<float>) * (1 + 2 * MT);
-        dim3 grid((unsigned)p.nrn, (unsigned)((nmaps + MT - 1) / MT));
-        k_ring_analysis<float><<<grid, 256, smem, st>>>(p.d_rings, (int)p.nrn, p.lmax, w, p.npix, maps, nmaps,
-                                                        MT, (float *)F, 2 * nmaps);
-        note_launch();
-        return;
-    }
-    const int MT = ring_mt(p, sizeof(cx<double>));
-    const size_t smem = (size_t)(4 * p.nside) * sizeof(cx<double>) * (1 + 2 * MT);
-    dim3 grid((unsigned)p.nrn, (unsigned)((nmaps + MT - 1) / MT));
-    k_ring_analysis<double><<<grid, 256, smem, st>>>(p.d_rings, (int)p.nrn, p.lmax, w, p.npix, maps, nmaps,
-                                                     MT, F, 2 * nmaps);
-                                                     note_launch();
+    if (p.precision == SFB_MIXED)
+        ring_analysis_t<float, float, float2>(p, (const float *)maps, nmaps, (float *)F, p.d_twtab32, p.d_wphase32, st);
+    else
+        ring_analysis_t<double, double, double2>(p, maps, nmaps, F, p.d_twtab, p.d_wphase, st);
 }
 
 void launch_ring_synthesis(const Plan &p, const double *G, int64_t nmaps, double *maps, cudaStream_t st) {
-    const int MT = ring_mt(p, sizeof(cx<double>));
-    const size_t smem = (size_t)(4 * p.nside) * sizeof(cx<double>) * (1 + 2 * MT);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_ring_synthesis<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        attr_set = true;
+    const int ns = (int)p.nside;
+    const bool pow2 = (ns & (ns - 1)) == 0;
+    struct Group { int r0, nr; size_t n; bool two; } groups[2] = {
+        {0, ns - 1, (size_t)(4 * (ns - 1)), true},
+        {ns - 1, ns + 1, (size_t)(4 * ns), !pow2}};
+    for (const Group &gr : groups) {
+        if (gr.nr <= 0) continue;
+        const int MT = ring_mt(gr.n, sizeof(cx<double>), gr.two);
+        const size_t smem = gr.n * sizeof(cx<double>) * (1 + (gr.two ? 2 : 1) * (size_t)MT);
+        set_smem(k_ring_synthesis<double>, smem);
+        dim3 grid((unsigned)gr.nr, (unsigned)((nmaps + MT - 1) / MT));
+        k_ring_synthesis<double><<<grid, 256, smem, st>>>(p.d_rings, (int)p.nrn, p.lmax, G, 2 * nmaps, nmaps, MT,
+                                                          p.npix, maps, gr.r0, p.d_twtab, p.d_twoff, p.d_phase);
+        note_launch();
     }
-    dim3 grid((unsigned)p.nrn, (unsigned)((nmaps + MT - 1) / MT));
-    k_ring_synthesis<double><<<grid, 256, smem, st>>>(p.d_rings, (int)p.nrn, p.lmax, G, 2 * nmaps, nmaps, MT,
-                                                      p.npix, maps);
-                                                      note_launch();
 }
 
 }  // namespace sfb

@@ -36,6 +36,7 @@ enum : int {
     ERR_THETA_RANGE = 2,
     ERR_NONFINITE_OUTPUT = 4,
     ERR_TC_TIMEOUT = 8,        // a bounded mbarrier wait in a tensor-core kernel gave up
+    ERR_RANGE_R = 16,          // a radius outside the shells of winweights2galweights
 };
 
 // ---------------------------------------------------------------------------
@@ -80,6 +81,12 @@ struct Plan {
     std::vector<RingGeom> h_rings;
     // device tables
     RingGeom *d_rings = nullptr;
+    double2 *d_twtab = nullptr;     // e^{-2 pi i t / nph} for every north ring (concatenated)
+    int64_t *d_twoff = nullptr;     // [nrn] offset of ring r's block in d_twtab
+    double2 *d_phase = nullptr;     // [nrn][lmax+1] e^{-i m phi0(r)}
+    double2 *d_wphase = nullptr;    // [nrn][lmax+1] (4 pi / npix) e^{-i m phi0(r)}
+    float2 *d_twtab32 = nullptr;    // FP32 copies for the mixed-precision ring transform
+    float2 *d_wphase32 = nullptr;
     double *d_lam = nullptr;        // Legendre table, FP64
     float *d_lam32 = nullptr;       // the same table rounded to FP32 (mixed precision)
     void *d_lamtc = nullptr;        // split-BF16 table in tensor-core operand layout (analysis)
@@ -103,6 +110,8 @@ struct Plan {
     DevBuf<double> alm;             // [lmsize][2*nmaps]
     DevBuf<double> scratch;         // galaxy/window/output staging
     DevBuf<double> scratch2;
+    DevBuf<double> dep;             // sorted-deposit workspace
+    DevBuf<double> maps32;          // FP32 copy of FP64 maps (mixed precision, spline / dense-window paths)
     int64_t device_bytes = 0;
 };
 
@@ -111,12 +120,19 @@ int grow(Plan &p, DevBuf<double> &b, size_t n);
 // Count of kernels this library has launched (process-wide).
 void note_launch();
 
+// Opt a kernel into `bytes` of dynamic shared memory (only above the 48 KB
+// default).  A failure is left for the caller's cudaGetLastError check.
+template <typename K>
+inline void set_smem(K kernel, size_t bytes) {
+    if (bytes > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
 // ---------------------------------------------------------------------------
 // kernels (launch wrappers; all enqueue on `st`)
 // ---------------------------------------------------------------------------
 void launch_legendre_table(const Plan &p, cudaStream_t st);
-void launch_deposit_poly(const Plan &p, const double *rtp, const double *w, int64_t ngal, double *maps,
-                         cudaStream_t st);
+// galaxies -> radial-basis x pixel maps (counting sort + register moments); writes every map element
+int deposit_sorted(Plan &p, const double *rtp, const double *w, int64_t ngal, double *maps, cudaStream_t st);
 void launch_ring_analysis(const Plan &p, const double *maps, int64_t nmaps, double *F, cudaStream_t st);
 void launch_ring_synthesis(const Plan &p, const double *G, int64_t nmaps, double *maps, cudaStream_t st);
 void launch_leg_analysis(const Plan &p, const double *F, int64_t ncol, double *A, bool accumulate,
@@ -133,10 +149,10 @@ void launch_to_float(const double *in, int64_t n, float *out, cudaStream_t st);
 // tensor-core (tcgen05) Legendre analysis, mixed precision
 int64_t tc_table_offsets(const Plan &p, std::vector<int64_t> &off);
 void launch_build_lamtc(const Plan &p, cudaStream_t st);
-void launch_leg_analysis_tc(const Plan &p, const float *F, int64_t ncol, float *A, bool accumulate, cudaStream_t st);
+void launch_leg_analysis_tc(const Plan &p, const float *F, int64_t ncol, double *A, bool accumulate, cudaStream_t st);
 int64_t tc_synth_table_offsets(const Plan &p, std::vector<int64_t> &off);
 void launch_build_lamts(const Plan &p, cudaStream_t st);
-void launch_leg_synthesis_tc(const Plan &p, const float *A, int64_t ncol, float *G, cudaStream_t st);
+void launch_leg_synthesis_tc(const Plan &p, const double *A, int64_t ncol, float *G, cudaStream_t st);
 void launch_transpose(const double *in, int64_t rows, int64_t cols, double *out, cudaStream_t st);
 void launch_check_finite(const double *x, int64_t n, int *err, cudaStream_t st);
 void launch_ang2pix(int64_t nside, const double *theta, const double *phi, int64_t n, int64_t *pix,

@@ -7,7 +7,8 @@ CUDA for sm_103a) behind the C ABI declared in ``include/sfb_gpu.h``.
 Mode setup (k_nl roots, splines) is host code, as it is on the Julia side.
 """
 
-from .modes import AnlmModes, estimate_nside, getidx, getidx0, getlmsize, getnlm, getnlmsize, isvalidnlm
+from .modes import (AnlmModes, ClnnModes, estimate_nside, getidx, getidx0, getidx_lnn, getlmsize, getlnn,
+                    getlnnsize, getnlm, getnlmsize, isvalidnlm)
 from .windows import (ConfigurationSpaceModes, SeparableArray, gen_mask, get_rbounds, integrate_window, make_window,
                       window_r)
 from .healpix import nside2npix, npix2nside, pix2ang_ring

@@ -58,10 +58,15 @@ _PROTOS = [
                                             C.c_void_p]),
     ("sfb_win_rhat_ln_dense", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_double, C.c_double, C.c_void_p]),
     ("sfb_map2alm", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
+    ("sfb_amln2clnn", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
+                                C.c_void_p]),
+    ("sfb_winweights2galweights", C.c_int, [C.c_int64, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_int64,
+                                            C.c_void_p]),
     ("sfb_ang2pix_ring", C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
     ("sfb_set_profiling", C.c_int, [C.c_void_p, C.c_int32]),
     ("sfb_get_stage_times", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     ("sfb_launch_count", C.c_int64, []),
+    ("sfb_selftest_wait_timeout", C.c_int, []),
     ("sfb_last_error", C.c_int, [C.c_char_p, C.c_size_t]),
 ]
 

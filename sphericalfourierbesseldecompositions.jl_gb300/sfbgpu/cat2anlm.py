@@ -20,7 +20,7 @@ from .modes import getnlmsize
 from .windows import SeparableArray
 
 __all__ = ["GPUPlan", "get_plan", "cat2amln", "cat2nlm", "field2anlm", "anlm2field", "win_rhat_ln",
-           "map2alm", "ang2pix_ring"]
+           "map2alm", "ang2pix_ring", "amln2clnn", "anlm2clnn", "winweights2galweights"]
 
 _PRECISION = {"fp64": capi.SFB_FP64, "mixed": capi.SFB_MIXED}
 _RADIAL = {"poly": capi.SFB_RADIAL_POLY, "spline": capi.SFB_RADIAL_SPLINE}
@@ -213,4 +213,39 @@ def ang2pix_ring(nside, theta, phi):
     ph = np.ascontiguousarray(phi, float).ravel()
     out = np.empty(th.shape, np.int64)
     capi.check(capi.lib.sfb_ang2pix_ring(int(nside), capi.ptr(th), capi.ptr(ph), len(th), capi.ptr(out)))
+    return out
+
+
+def amln2clnn(anlm1, anlm2, cmodes=None, **plan_opts):
+    """Pseudo-SFB power spectrum C_l(n1, n2) on the GPU
+    (reference src/SphericalFourierBesselDecompositions.jl:133-150).
+
+    ``amln2clnn(anlm, cmodes)`` or ``amln2clnn(anlm1, anlm2, cmodes)``; a 2-d
+    (nbatch, nlmsize) input gives one spectrum per row (mock batches)."""
+    if cmodes is None:
+        cmodes, anlm2 = anlm2, None
+    plan = get_plan(cmodes.amodesA, **plan_opts)
+    a1 = np.ascontiguousarray(np.atleast_2d(anlm1), np.complex128)
+    a2 = None if anlm2 is None else np.ascontiguousarray(np.atleast_2d(anlm2), np.complex128)
+    if a1.shape[1] != plan.nlmsize or (a2 is not None and a2.shape != a1.shape):
+        raise ValueError("coefficient vectors must have getnlmsize(amodes) entries")
+    lnn = np.ascontiguousarray(cmodes.lnn.T, np.int64)     # column i at lnn[3i..3i+2]
+    out = np.empty((a1.shape[0], lnn.shape[0]))
+    capi.check(capi.lib.sfb_amln2clnn(plan.handle, capi.ptr(a1), capi.ptr(a2), a1.shape[0], capi.ptr(lnn),
+                                      lnn.shape[0], capi.ptr(out)))
+    return out[0] if np.ndim(anlm1) == 1 else out
+
+
+anlm2clnn = amln2clnn
+
+
+def winweights2galweights(weights, wmodes, rtp):
+    """Per-galaxy weights from a (nr, npix) weight field (reference src/cat2anlm.jl:218-238)."""
+    from .windows import get_rbounds
+    W = np.asfortranarray(weights, float)
+    rb = np.ascontiguousarray(get_rbounds(wmodes), float)
+    gal = np.ascontiguousarray(np.asarray(rtp, float).T)
+    out = np.empty(gal.shape[0])
+    capi.check(capi.lib.sfb_winweights2galweights(wmodes.nside, capi.ptr(W), W.shape[0], capi.ptr(rb),
+                                                  capi.ptr(gal), gal.shape[0], capi.ptr(out)))
     return out

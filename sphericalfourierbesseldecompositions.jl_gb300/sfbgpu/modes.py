@@ -13,8 +13,8 @@ import numpy as np
 
 from .gnl import SphericalBesselGNL, calc_cnl_dnl, calc_knl_kmax, calc_knl_nmax
 
-__all__ = ["AnlmModes", "estimate_nside", "getlmsize", "getnlmsize", "getidx",
-           "getidx0", "getnlm", "isvalidnlm"]
+__all__ = ["AnlmModes", "ClnnModes", "estimate_nside", "getlmsize", "getnlmsize", "getidx",
+           "getidx0", "getnlm", "isvalidnlm", "getlnnsize", "getlnn", "getidx_lnn"]
 
 
 def estimate_nside(lmax):
@@ -138,3 +138,53 @@ def getnlm(amodes, idx):
         l += 1
         nmodes = l + 1
     return n, l, idx - 1
+
+
+class ClnnModes:
+    """(l, n1, n2) ordering of the pseudo-SFB power spectrum
+    (reference ``src/modes.jl:281-401``): entries with |k_n2 - k_n1| <= dkmax
+    and |n2 - n1| <= dnmax, sorted by l, then n2 - n1, then n1; for one
+    AnlmModes (auto-correlation) n2 >= n1."""
+
+    def __init__(self, amodesA, amodesB=None, dkmax=np.inf, dnmax=2 ** 62):
+        self.symmetric = amodesB is None
+        self.amodesA = amodesA
+        self.amodesB = amodesA if amodesB is None else amodesB
+        A, B = self.amodesA, self.amodesB
+        lmax = min(A.lmax, B.lmax)
+        rows = []
+        dk_out, dn_out = -np.inf, 0
+        for l in range(lmax + 1):
+            for nA in range(1, int(A.nmax_l[l]) + 1):
+                for nB in range((nA if self.symmetric else 1), int(B.nmax_l[l]) + 1):
+                    dk = B.knl[nB - 1, l] - A.knl[nA - 1, l]
+                    if abs(dk) <= dkmax and abs(nB - nA) <= dnmax:
+                        rows.append((l, nA, nB))
+                        dk_out = max(abs(dk), dk_out)
+                        dn_out = max(abs(nB - nA), dn_out)
+        rows.sort(key=lambda t: (t[0], t[2] - t[1], t[1]))
+        self.lnn = np.array(rows, dtype=np.int64).reshape(-1, 3).T.copy()     # 3 x nlnn, like Julia's lnn
+        self.dkmax = dk_out
+        self.dnmax = dn_out
+        self._index = {tuple(c): i for i, c in enumerate(self.lnn.T.tolist())}
+
+    @property
+    def amodes(self):
+        return self.amodesA
+
+
+def getlnnsize(cmodes):
+    return cmodes.lnn.shape[1]
+
+
+def getlnn(cmodes, idx):
+    """(l, n1, n2) of a 1-based index (reference src/modes.jl:388-393)."""
+    l, n1, n2 = cmodes.lnn[:, idx - 1]
+    return int(l), int(n1), int(n2)
+
+
+def getidx_lnn(cmodes, l, n1, n2):
+    """1-based index of (l, n1, n2) (reference src/modes.jl:398-...)."""
+    if cmodes.symmetric and n1 > n2:
+        n1, n2 = n2, n1
+    return cmodes._index[(l, n1, n2)] + 1

@@ -86,3 +86,16 @@ def test_spline_matches_clamped_spline_with_parabola_slopes():
 
 def test_spherical_bessel_small_x_rule():
     assert sphericalbesselj(0, 1e-20) == 1.0 and sphericalbesselj(3, 1e-20) == 0.0
+
+
+def test_clnnmodes_order_and_index():
+    """reference src/modes.jl:333-401: sorted by l, then n2-n1, then n1; index round trip."""
+    a = sfbgpu.AnlmModes(0.03, 500.0, 1000.0, cache=False)
+    cm = sfbgpu.ClnnModes(a, dnmax=3)
+    lnn = cm.lnn
+    keys = [(l, n2 - n1, n1) for l, n1, n2 in lnn.T]
+    assert keys == sorted(keys)
+    assert np.all(lnn[2] >= lnn[1]) and np.all(lnn[2] - lnn[1] <= 3)
+    for i in range(1, sfbgpu.getlnnsize(cm) + 1):
+        l, n1, n2 = sfbgpu.getlnn(cm, i)
+        assert sfbgpu.getidx_lnn(cm, l, n1, n2) == i == sfbgpu.getidx_lnn(cm, l, n2, n1)
