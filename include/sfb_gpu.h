@@ -165,6 +165,18 @@ int sfb_amln2clnn(sfb_plan *plan, const double *anlm1, const double *anlm2, int6
 int sfb_winweights2galweights(int64_t nside, const double *weights, int64_t nr, const double *rbounds,
                               const double *rtp, int64_t ngal, double *w_out);
 
+/* No counterpart in the reference.  Same arguments, result and errors as
+ * sfb_winweights2galweights, but the call allocates no device memory: inputs
+ * and outputs are staged through a fixed 16 MiB device array per device, for
+ * callers whose device memory belongs to another allocator or that may not
+ * allocate mid-pipeline.  Limit: nr*npix + nr + 1 <= 2080736 doubles
+ * (e.g. nside 64 with nr <= 42), else SFB_EINVAL.  The first call on a
+ * device does its set-up (device address lookup) and should come before any
+ * stream capture.  Calls on one device are serialised inside the library. */
+int sfb_winweights2galweights_noalloc(int64_t nside, const double *weights, int64_t nr,
+                                      const double *rbounds, const double *rtp, int64_t ngal,
+                                      double *w_out);
+
 /* HEALPix RING pixel (0-based; Healpix.jl ang2pixRing returns this + 1) of
  * n directions, computed on the device with the binning kernel's arithmetic. */
 int sfb_ang2pix_ring(int64_t nside, const double *theta, const double *phi, int64_t n,

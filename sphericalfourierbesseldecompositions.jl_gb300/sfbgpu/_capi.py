@@ -62,6 +62,8 @@ _PROTOS = [
                                 C.c_void_p]),
     ("sfb_winweights2galweights", C.c_int, [C.c_int64, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_int64,
                                             C.c_void_p]),
+    ("sfb_winweights2galweights_noalloc", C.c_int, [C.c_int64, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
+                                                    C.c_int64, C.c_void_p]),
     ("sfb_ang2pix_ring", C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
     ("sfb_set_profiling", C.c_int, [C.c_void_p, C.c_int32]),
     ("sfb_get_stage_times", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
