@@ -280,7 +280,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--no-fp64-leg", action="store_true", help="skip timing the FP64 path beside the mixed one")
     ap.add_argument("--ngal", type=int, default=0, help="override the catalogue size (testing)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-workers", type=int, default=0)
@@ -439,6 +440,42 @@ def main():
     res_dev = d_out.cpu().numpy()
     same = float(np.max(np.abs(h_out.numpy() - res_dev)) / max(np.max(np.abs(res_dev)), 1e-300))
 
+    # the metric compares the mixed path with the FP64 GPU path on the same catalogue
+    vs64 = None
+    if args.precision == "mixed" and not args.no_fp64_leg:
+        plan64 = sfbgpu.get_plan(amodes, precision="fp64", radial="poly", **plan_extra)
+        wln64 = np.asfortranarray(sfbgpu.win_rhat_ln(sfbgpu.SeparableArray(phi, mask, "phi", "mask"), wm, amodes,
+                                                     precision="fp64", radial="poly", **plan_extra).w_ln)
+        d_wln64 = torch.from_numpy(np.ascontiguousarray(wln64.T)).to(dev)
+        d_out64 = torch.empty_like(d_out)
+        win64 = capi.Window()
+        win64.kind = capi.SFB_WINDOW_SEPARABLE
+        win64.mask = capi.C.cast(d_mask.data_ptr(), capi._dp)
+        win64.w_ln = capi.C.cast(d_wln64.data_ptr(), capi._dp)
+
+        def step64():
+            capi.check(capi.lib.sfb_cat2amln_device(plan64.handle, capi.C.c_void_p(d_gal.data_ptr()),
+                                                    capi.C.c_void_p(d_w.data_ptr()), N, float(nbar),
+                                                    capi.C.byref(win64), capi.C.c_void_p(d_out64.data_ptr()),
+                                                    capi.C.c_void_p(stream.cuda_stream)))
+        for _ in range(args.warmup):
+            step64()
+        torch.cuda.synchronize()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(args.steps):
+            step64()
+        f1.record(stream)
+        torch.cuda.synchronize()
+        ms64 = f0.elapsed_time(f1) / args.steps
+        step()
+        torch.cuda.synchronize()
+        a_mix, a_64 = d_out.cpu().numpy(), d_out64.cpu().numpy()
+        vs64 = {"fp64_value": N * world / (ms64 * 1e-3), "fp64_ms_per_step": ms64, "speedup": ms64 / ms,
+                "rel_err": float(np.linalg.norm(a_mix - a_64) / np.linalg.norm(a_64)),
+                "rel_err_definition": "||a_mixed - a_fp64||_2 / ||a_fp64||_2 over the a_nlm vector"}
+
     # roofline of every stage; the headline is the dominant one
     nm = info["nbasis"] + 1
     peaks = {}
@@ -478,6 +515,7 @@ def main():
                 "roofline": roof, "cpu_baseline": cpu,
                 "e2e": {"value": N / e2e_s, "unit": "galaxies/s", "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(d2h), "host_vs_device_result_rel_diff": same},
+                "mixed_vs_fp64": vs64,
                 "stages": stages, "stage_roofline": table, "clocks": clk, "gpu_launches": int(launches)}
         print(json.dumps(line), flush=True)
     if world > 1:
