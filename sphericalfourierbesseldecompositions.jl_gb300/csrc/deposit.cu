@@ -15,6 +15,16 @@
 //               so the maps need no clearing).
 // Summation order inside a bin follows the int-atomic ranks, so repeated
 // calls agree to rounding, not bit for bit.
+//
+// Mixed precision stores the maps in FP32.  With a reference angular map C,
+// each map is written as the fluctuation D_b - mu_b C, with
+// mu_b = <D_b, C> / <C, C> estimated in FP64 on every STATS_STRIDE-th group
+// of 32 bins; the caller adds mu_b C_lm back in FP64 after the transform.
+// C is the weighted galaxy count map of all radial slots, so it carries the
+// mean density and the survey boundary exactly as the galaxies sample them
+// (a pixelised mask misses the partly covered boundary pixels).  The FP32
+// rounding then scales with the fluctuation, not with the mean density that
+// the window term later cancels.
 #include "sfb_internal.h"
 
 namespace sfb {
@@ -141,24 +151,10 @@ __global__ void k_deposit_scatter(const double *__restrict__ wgt, int64_t ngal, 
     sorted[pos] = make_double2(xloc[i], wgt ? wgt[i] : 1.0);
 }
 
-// One thread per (slot, pixel): Legendre moments of its galaxies.
-template <int MAXDEG, typename TM>
-__global__ void k_deposit_moments(const int32_t *__restrict__ offset, const double2 *__restrict__ sorted,
-                                  int64_t npix, int pieces, int deg, int64_t nbasis, TM *__restrict__ maps) {
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t nkeys = (int64_t)(pieces + 2) * npix;
-    if (idx >= nkeys) return;
-    const int slot = (int)(idx / npix);
-    const int64_t pix = idx - (int64_t)slot * npix;
-    const int64_t g0 = offset[idx];
-    const int64_t g1 = offset[idx + 1];         // offset[nkeys] = number of keyed galaxies
-    if (slot >= pieces) {       // constant extrapolation maps (r < rmin, r > rmax)
-        double s = 0.0;
-        for (int64_t g = g0; g < g1; ++g) s += sorted[g].y;
-        maps[(nbasis - 2 + (slot - pieces)) * npix + pix] = (TM)s;
-        return;
-    }
-    double acc[MAXDEG + 1];
+// Legendre moments sum_i w_i P_k(x_i), k <= deg, of the galaxies g0..g1-1 of one bin.
+template <int MAXDEG>
+__device__ __forceinline__ void bin_moments(const double2 *__restrict__ sorted, int64_t g0, int64_t g1, int deg,
+                                            double (&acc)[MAXDEG + 1]) {
 #pragma unroll
     for (int k = 0; k <= MAXDEG; ++k) acc[k] = 0.0;
     for (int64_t g = g0; g < g1; ++g) {
@@ -177,13 +173,145 @@ __global__ void k_deposit_moments(const int32_t *__restrict__ offset, const doub
             p1 = p2;
         }
     }
-    TM *base = maps + (int64_t)slot * (deg + 1) * npix + pix;
-#pragma unroll
-    for (int k = 0; k <= MAXDEG; ++k)
-        if (k <= deg) base[(int64_t)k * npix] = (TM)acc[k];
 }
 
-int deposit_sorted(Plan &p, const double *rtp, const double *w, int64_t ngal, double *maps, cudaStream_t st) {
+__device__ __forceinline__ int64_t basis_of(int slot, int k, int pieces, int deg, int64_t nbasis) {
+    return slot < pieces ? (int64_t)slot * (deg + 1) + k : nbasis - 2 + (slot - pieces);
+}
+
+// One thread per (slot, pixel): Legendre moments of its galaxies, minus
+// mu_b ref[pix] when ref is given.
+template <int MAXDEG, typename TM>
+__global__ void k_deposit_moments(const int32_t *__restrict__ offset, const double2 *__restrict__ sorted,
+                                  int64_t npix, int pieces, int deg, int64_t nbasis, const double *__restrict__ ref,
+                                  const double *__restrict__ mu, TM *__restrict__ maps) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nkeys = (int64_t)(pieces + 2) * npix;
+    if (idx >= nkeys) return;
+    const int slot = (int)(idx / npix);
+    const int64_t pix = idx - (int64_t)slot * npix;
+    const int64_t g0 = offset[idx];
+    const int64_t g1 = offset[idx + 1];         // offset[nkeys] = number of keyed galaxies
+    const double rv = ref ? ref[pix] : 0.0;
+    if (slot >= pieces) {       // constant extrapolation maps (r < rmin, r > rmax)
+        double s = 0.0;
+        for (int64_t g = g0; g < g1; ++g) s += sorted[g].y;
+        const int64_t b = nbasis - 2 + (slot - pieces);
+        if (ref) s -= mu[b] * rv;
+        maps[b * npix + pix] = (TM)s;
+        return;
+    }
+    double acc[MAXDEG + 1];
+    bin_moments<MAXDEG>(sorted, g0, g1, deg, acc);
+    const int64_t b0 = (int64_t)slot * (deg + 1);
+    TM *base = maps + b0 * npix + pix;
+#pragma unroll
+    for (int k = 0; k <= MAXDEG; ++k) {
+        if (k <= deg) {
+            const double v = ref ? acc[k] - mu[b0 + k] * rv : acc[k];
+            base[(int64_t)k * npix] = (TM)v;
+        }
+    }
+}
+
+constexpr int STATS_STRIDE = 32;
+
+// Sampled projections onto ref over the bins of every STATS_STRIDE-th group of
+// 32 bins (one warp per block): S[b] += <D_b, ref>, Q[slot] += <ref, ref>.
+// A slot-uniform warp reduces through shared memory (lane k sums column k);
+// a warp that straddles two slots adds per thread.
+template <int MAXDEG>
+__global__ void __launch_bounds__(32) k_deposit_stats(const int32_t *__restrict__ offset,
+                                                      const double2 *__restrict__ sorted, int64_t npix, int pieces,
+                                                      int deg, int64_t nbasis, const double *__restrict__ ref,
+                                                      double *__restrict__ S, double *__restrict__ Q) {
+    __shared__ double red[32][MAXDEG + 3];
+    const int lane = threadIdx.x;
+    const int64_t idx = (int64_t)blockIdx.x * STATS_STRIDE * 32 + lane;
+    const int64_t nkeys = (int64_t)(pieces + 2) * npix;
+    const bool valid = idx < nkeys;
+    const int slot = valid ? (int)(idx / npix) : -1;
+    const int64_t pix = valid ? idx - (int64_t)slot * npix : 0;
+    const double rv = valid ? ref[pix] : 0.0;
+    double acc[MAXDEG + 1];
+    if (valid) {
+        bin_moments<MAXDEG>(sorted, offset[idx], offset[idx + 1], slot < pieces ? deg : 0, acc);
+    } else {
+#pragma unroll
+        for (int k = 0; k <= MAXDEG; ++k) acc[k] = 0.0;
+    }
+    const int nk = slot < 0 ? 0 : (slot < pieces ? deg + 1 : 1);
+    const unsigned full = 0xffffffffu;
+    const int slot0 = __shfl_sync(full, slot, 0);
+    if (__all_sync(full, slot == slot0)) {
+        if (slot0 < 0) return;
+#pragma unroll
+        for (int k = 0; k <= MAXDEG; ++k)
+            if (k < nk) red[lane][k] = acc[k] * rv;
+        red[lane][nk] = rv * rv;
+        __syncwarp();
+        for (int k = lane; k <= nk; k += 32) {
+            double v = 0.0;
+            for (int j = 0; j < 32; ++j) v += red[j][k];
+            if (k < nk) atomicAdd(S + basis_of(slot0, k, pieces, deg, nbasis), v);
+            else atomicAdd(Q + slot0, v);
+        }
+    } else if (valid) {
+#pragma unroll
+        for (int k = 0; k <= MAXDEG; ++k)
+            if (k < nk) atomicAdd(S + basis_of(slot, k, pieces, deg, nbasis), acc[k] * rv);
+        atomicAdd(Q + slot, rv * rv);
+    }
+}
+
+// mu[b] = S[b] / Q[slot(b)] (0 where the sampled reference map is zero).
+__global__ void k_mean_finalize(const double *S, const double *Q, int pieces, int deg, int64_t nbasis, double *mu) {
+    const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nbasis) return;
+    const int64_t npoly = (int64_t)pieces * (deg + 1);
+    const int slot = b < npoly ? (int)(b / (deg + 1)) : pieces + (int)(b - npoly);
+    mu[b] = Q[slot] > 0.0 ? S[b] / Q[slot] : 0.0;
+}
+
+// Weighted galaxy count per pixel over all radial slots (FP64).
+__global__ void k_weight_map(const int32_t *__restrict__ offset, const double2 *__restrict__ sorted, int64_t npix,
+                             int nslots, double *__restrict__ C) {
+    const int64_t pix = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= npix) return;
+    double s = 0.0;
+    for (int sl = 0; sl < nslots; ++sl) {
+        const int64_t k = (int64_t)sl * npix + pix;
+        for (int64_t g = offset[k]; g < offset[k + 1]; ++g) s += sorted[g].y;
+    }
+    C[pix] = s;
+}
+
+template <int MAXDEG>
+static void launch_moments(const Plan &p, const int32_t *counts, const double2 *sorted, const double *ref,
+                           const double *mu, double *maps, cudaStream_t st) {
+    const int64_t nkeys = (int64_t)(p.pieces + 2) * p.npix;
+    const unsigned blocks = (unsigned)((nkeys + 127) / 128);
+    if (p.precision == SFB_MIXED)
+        k_deposit_moments<MAXDEG, float><<<blocks, 128, 0, st>>>(counts, sorted, p.npix, p.pieces, p.degree,
+                                                                 p.nbasis, ref, mu, reinterpret_cast<float *>(maps));
+    else
+        k_deposit_moments<MAXDEG, double><<<blocks, 128, 0, st>>>(counts, sorted, p.npix, p.pieces, p.degree,
+                                                                  p.nbasis, ref, mu, maps);
+    note_launch();
+}
+
+template <int MAXDEG>
+static void launch_stats(const Plan &p, const int32_t *counts, const double2 *sorted, const double *ref, double *S,
+                         double *Q, cudaStream_t st) {
+    const int64_t nkeys = (int64_t)(p.pieces + 2) * p.npix;
+    const int64_t blocks = (nkeys + 32 * STATS_STRIDE - 1) / (32 * STATS_STRIDE);
+    k_deposit_stats<MAXDEG><<<(unsigned)blocks, 32, 0, st>>>(counts, sorted, p.npix, p.pieces, p.degree, p.nbasis,
+                                                              ref, S, Q);
+    note_launch();
+}
+
+int deposit_sorted(Plan &p, const double *rtp, const double *w, int64_t ngal, double *maps, double *ref,
+                   double *mu, cudaStream_t st) {
     const int64_t nkeys = (int64_t)(p.pieces + 2) * p.npix;
     const int64_t nscan = nkeys + 1;            // one extra counter: its exclusive prefix is the total
     const int64_t ntiles = (nscan + SCAN_TILE - 1) / SCAN_TILE;
@@ -193,7 +321,8 @@ int deposit_sorted(Plan &p, const double *rtp, const double *w, int64_t ngal, do
     const int64_t off_x = (ints + 1) / 2;
     int64_t off_sorted = off_x + ngal;
     off_sorted += off_sorted & 1;
-    SFB_TRY(grow(p, p.dep, (size_t)(off_sorted + 2 * ngal + 2)));
+    const int64_t off_stats = off_sorted + 2 * ngal + 2;       // S [nbasis], Q [pieces + 2]
+    SFB_TRY(grow(p, p.dep, (size_t)(off_stats + p.nbasis + p.pieces + 2)));
     int32_t *counts = reinterpret_cast<int32_t *>(p.dep.ptr);
     int32_t *tsum = counts + nscan;
     int32_t *key = tsum + ntiles;
@@ -216,26 +345,25 @@ int deposit_sorted(Plan &p, const double *rtp, const double *w, int64_t ngal, do
         k_deposit_scatter<<<(unsigned)((ngal + 255) / 256), 256, 0, st>>>(w, ngal, key, rank, xloc, counts, sorted);
         note_launch();
     }
-    const unsigned blocks = (unsigned)((nkeys + 127) / 128);
     if (p.degree > 63) return fail(SFB_ENOTSUP, "radial degree above 63 is not supported by the sorted deposit");
-    // moments in FP64; the maps are stored in the transform's precision
-    if (p.precision == SFB_MIXED) {
-        float *m32 = reinterpret_cast<float *>(maps);
-        if (p.degree <= 15)
-            k_deposit_moments<15, float><<<blocks, 128, 0, st>>>(counts, sorted, p.npix, p.pieces, p.degree, p.nbasis, m32);
-        else if (p.degree <= 31)
-            k_deposit_moments<31, float><<<blocks, 128, 0, st>>>(counts, sorted, p.npix, p.pieces, p.degree, p.nbasis, m32);
-        else
-            k_deposit_moments<63, float><<<blocks, 128, 0, st>>>(counts, sorted, p.npix, p.pieces, p.degree, p.nbasis, m32);
-    } else {
-        if (p.degree <= 15)
-            k_deposit_moments<15, double><<<blocks, 128, 0, st>>>(counts, sorted, p.npix, p.pieces, p.degree, p.nbasis, maps);
-        else if (p.degree <= 31)
-            k_deposit_moments<31, double><<<blocks, 128, 0, st>>>(counts, sorted, p.npix, p.pieces, p.degree, p.nbasis, maps);
-        else
-            k_deposit_moments<63, double><<<blocks, 128, 0, st>>>(counts, sorted, p.npix, p.pieces, p.degree, p.nbasis, maps);
+    const bool split = ref != nullptr && p.precision == SFB_MIXED;
+    if (split) {
+        k_weight_map<<<(unsigned)((p.npix + 255) / 256), 256, 0, st>>>(counts, sorted, p.npix, p.pieces + 2, ref);
+        note_launch();
+        double *S = p.dep.ptr + off_stats;
+        double *Q = S + p.nbasis;
+        SFB_CUDA_TRY(cudaMemsetAsync(S, 0, (size_t)(p.nbasis + p.pieces + 2) * sizeof(double), st));
+        if (p.degree <= 15) launch_stats<15>(p, counts, sorted, ref, S, Q, st);
+        else if (p.degree <= 31) launch_stats<31>(p, counts, sorted, ref, S, Q, st);
+        else launch_stats<63>(p, counts, sorted, ref, S, Q, st);
+        k_mean_finalize<<<(unsigned)((p.nbasis + 127) / 128), 128, 0, st>>>(S, Q, p.pieces, p.degree, p.nbasis, mu);
+        note_launch();
     }
-    note_launch();
+    // moments in FP64; the maps are stored in the transform's precision
+    const double *r = split ? ref : nullptr;
+    if (p.degree <= 15) launch_moments<15>(p, counts, sorted, r, mu, maps, st);
+    else if (p.degree <= 31) launch_moments<31>(p, counts, sorted, r, mu, maps, st);
+    else launch_moments<63>(p, counts, sorted, r, mu, maps, st);
     SFB_CUDA_TRY(cudaGetLastError());
     return SFB_OK;
 }

@@ -196,8 +196,110 @@ __global__ void __launch_bounds__(128) k_fold_residual(const RingGeom *rings, in
     }
 }
 
+// Few columns (ncol <= 8, e.g. one reference map): matrix-vector shape.
+// Analysis: one warp per (block z, row li), lanes stride over the rings
+// (coalesced lambda rows), warp-reduced.
+template <typename T, int NC>
+__global__ void __launch_bounds__(256) k_leg_analysis_narrow(const T *__restrict__ lam, const int64_t *lam_off,
+                                                             int lmax, int nrn, const T *__restrict__ F,
+                                                             T *__restrict__ A, int accumulate) {
+    const int z = blockIdx.y;
+    const int m = z >> 1, par = z & 1;
+    const int nrows = nrows_of(m, par, lmax);
+    const int row = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (row >= nrows) return;
+    const int lane = threadIdx.x & 31;
+    const T *L = lam + lam_off[z] + (int64_t)row * nrn;
+    const T *B = F + ((int64_t)(par * (lmax + 1) + m) * nrn) * NC;
+    T acc[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) acc[c] = T(0);
+    for (int r = lane; r < nrn; r += 32) {
+        const T l = L[r];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) acc[c] = fma(l, B[(int64_t)r * NC + c], acc[c]);
+    }
+#pragma unroll
+    for (int c = 0; c < NC; ++c)
+        for (int off = 16; off > 0; off >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], off);
+    if (lane < NC) {
+        T v = acc[0];
+#pragma unroll
+        for (int c = 1; c < NC; ++c)
+            if (lane == c) v = acc[c];
+        const int l = m + par + 2 * row;
+        T *d = A + ((int64_t)l * (l + 1) / 2 + m) * NC + lane;
+        *d = accumulate ? *d + v : v;
+    }
+}
+
+// Synthesis: one thread per (block z, ring r), looping over the rows li
+// (lambda reads coalesced over r, a_lm broadcast).
+template <typename T, int NC>
+__global__ void __launch_bounds__(128) k_leg_synthesis_narrow(const T *__restrict__ lam, const int64_t *lam_off,
+                                                              int lmax, int nrn, const T *__restrict__ A,
+                                                              T *__restrict__ G) {
+    const int z = blockIdx.y;
+    const int m = z >> 1, par = z & 1;
+    const int nrows = nrows_of(m, par, lmax);
+    const int r = blockIdx.x * 128 + threadIdx.x;
+    if (r >= nrn) return;
+    const T *L = lam + lam_off[z] + r;
+    T acc[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) acc[c] = T(0);
+    for (int li = 0; li < nrows; ++li) {
+        const T l = L[(int64_t)li * nrn];
+        const int ll = m + par + 2 * li;
+        const T *a = A + ((int64_t)ll * (ll + 1) / 2 + m) * NC;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) acc[c] = fma(l, a[c], acc[c]);
+    }
+    T *g = G + (((int64_t)(par * (lmax + 1) + m) * nrn) + r) * NC;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) g[c] = acc[c];
+}
+
+template <typename T, int NC>
+static void narrow_analysis(const Plan &p, const T *lam, const T *F, T *A, bool accumulate, cudaStream_t st) {
+    const int maxrows = p.lmax / 2 + 1;
+    dim3 grid((unsigned)((maxrows + 7) / 8), (unsigned)(2 * (p.lmax + 1)));
+    k_leg_analysis_narrow<T, NC><<<grid, 256, 0, st>>>(lam, p.d_lam_off, p.lmax, (int)p.nrn, F, A, accumulate ? 1 : 0);
+}
+
+template <typename T, int NC>
+static void narrow_synthesis(const Plan &p, const T *lam, const T *A, T *G, cudaStream_t st) {
+    dim3 grid((unsigned)((p.nrn + 127) / 128), (unsigned)(2 * (p.lmax + 1)));
+    k_leg_synthesis_narrow<T, NC><<<grid, 128, 0, st>>>(lam, p.d_lam_off, p.lmax, (int)p.nrn, A, G);
+}
+
+template <typename T>
+static bool narrow_dispatch(const Plan &p, const T *lam, const T *in, int64_t ncol, T *out, bool analysis,
+                            bool accumulate, cudaStream_t st) {
+    switch (ncol) {
+    case 2:
+        if (analysis) narrow_analysis<T, 2>(p, lam, in, out, accumulate, st); else narrow_synthesis<T, 2>(p, lam, in, out, st);
+        return true;
+    case 4:
+        if (analysis) narrow_analysis<T, 4>(p, lam, in, out, accumulate, st); else narrow_synthesis<T, 4>(p, lam, in, out, st);
+        return true;
+    case 8:
+        if (analysis) narrow_analysis<T, 8>(p, lam, in, out, accumulate, st); else narrow_synthesis<T, 8>(p, lam, in, out, st);
+        return true;
+    default:
+        return false;
+    }
+}
+
 void launch_leg_analysis(const Plan &p, const double *F, int64_t ncol, double *A, bool accumulate,
                          cudaStream_t st) {
+    const bool narrow = p.precision == SFB_MIXED
+                            ? narrow_dispatch<float>(p, p.d_lam32, (const float *)F, ncol, (float *)A, true, accumulate, st)
+                            : narrow_dispatch<double>(p, p.d_lam, F, ncol, A, true, accumulate, st);
+    if (narrow) {
+        note_launch();
+        return;
+    }
     const int maxrows = p.lmax / 2 + 1;
     dim3 grid((unsigned)((ncol + BN - 1) / BN), (unsigned)((maxrows + BM - 1) / BM), (unsigned)(2 * (p.lmax + 1)));
     if (p.precision == SFB_MIXED)
@@ -210,6 +312,13 @@ void launch_leg_analysis(const Plan &p, const double *F, int64_t ncol, double *A
 }
 
 void launch_leg_synthesis(const Plan &p, const double *A, int64_t ncol, double *G, cudaStream_t st) {
+    const bool narrow = p.precision == SFB_MIXED
+                            ? narrow_dispatch<float>(p, p.d_lam32, (const float *)A, ncol, (float *)G, false, false, st)
+                            : narrow_dispatch<double>(p, p.d_lam, A, ncol, G, false, false, st);
+    if (narrow) {
+        note_launch();
+        return;
+    }
     dim3 grid((unsigned)((ncol + BN - 1) / BN), (unsigned)((p.nrn + BM - 1) / BM), (unsigned)(2 * (p.lmax + 1)));
     if (p.precision == SFB_MIXED)
         k_leg_synthesis<float><<<grid, 256, 0, st>>>(p.d_lam32, p.d_lam_off, p.lmax, (int)p.nrn, (const float *)A,
@@ -219,9 +328,64 @@ void launch_leg_synthesis(const Plan &p, const double *A, int64_t ncol, double *
     note_launch();
 }
 
+// Few columns: one thread per (parity, m', ring, complex column), same sums.
+template <typename T>
+__global__ void __launch_bounds__(256) k_fold_residual_narrow(const RingGeom *rings, int nrn, int lmax, double w,
+                                                             const T *__restrict__ F, const T *__restrict__ G,
+                                                             int64_t ncplx, T *__restrict__ R) {
+    const int L1 = lmax + 1;
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t total = (int64_t)2 * L1 * nrn * ncplx;
+    if (idx >= total) return;
+    const int64_t c = idx % ncplx;
+    int64_t t = idx / ncplx;
+    const int r = (int)(t % nrn);
+    t /= nrn;
+    const int mp = (int)(t % L1);
+    const int par = (int)(t / L1);
+    const RingGeom g = rings[r];
+    const int n = g.nph;
+    const int64_t ld = 2 * ncplx;
+    const bool odd_phase = g.phi0_den != 0;
+    const T f = (T)(w * (double)n * g.cfold);
+    const int64_t off = ((int64_t)(par * L1 + mp) * nrn + r) * ld + 2 * c;
+    T sx = 0, sy = 0;
+    const int k = mp % n;
+    const int kk = (n - k) % n;
+    int tt = 0;
+    for (int m = k; m <= lmax; m += n, ++tt) {
+        const T *gp = G + ((int64_t)(par * L1 + m) * nrn + r) * ld + 2 * c;
+        const int dt = tt - mp / n;
+        const T sgn = (odd_phase && (dt & 1)) ? T(-1) : T(1);
+        sx += sgn * gp[0];
+        if (m != 0) sy += sgn * gp[1];
+    }
+    for (int m = (kk == 0 ? n : kk); m <= lmax; m += n) {
+        const T *gp = G + ((int64_t)(par * L1 + m) * nrn + r) * ld + 2 * c;
+        const int q = (m + mp) / n;
+        const T sgn = (odd_phase && (q & 1)) ? T(-1) : T(1);
+        sx += sgn * gp[0];
+        sy -= sgn * gp[1];
+    }
+    R[off] = F[off] - f * sx;
+    R[off + 1] = F[off + 1] - f * sy;
+}
+
 void launch_fold_residual(const Plan &p, const double *F, const double *G, int64_t ncol, double *R,
                           cudaStream_t st) {
     const int64_t ncplx = ncol / 2;
+    if (ncplx <= 4) {
+        const int64_t total = (int64_t)2 * (p.lmax + 1) * p.nrn * ncplx;
+        const unsigned blocks = (unsigned)((total + 255) / 256);
+        const double w = 4.0 * M_PI / (double)p.npix;
+        if (p.precision == SFB_MIXED)
+            k_fold_residual_narrow<float><<<blocks, 256, 0, st>>>(p.d_rings, (int)p.nrn, p.lmax, w, (const float *)F,
+                                                                 (const float *)G, ncplx, (float *)R);
+        else
+            k_fold_residual_narrow<double><<<blocks, 256, 0, st>>>(p.d_rings, (int)p.nrn, p.lmax, w, F, G, ncplx, R);
+        note_launch();
+        return;
+    }
     dim3 grid((unsigned)(p.lmax + 1), (unsigned)p.nrn, 2u);
     const double w = 4.0 * M_PI / (double)p.npix;
     if (p.precision == SFB_MIXED)

@@ -293,12 +293,14 @@ int choose_radial_basis(sfb_plan *h, const sfb_plan_desc *d) {
 // map2alm with niter refinement on nm maps; result in p.alm [lmsize][2*nm] (FP64).
 // In mixed precision the maps are FP32 ([nm][npix] floats); maps_are_fp64 marks
 // FP64 maps that are converted first.
-int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, bool maps_are_fp64 = false) {
+int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, bool maps_are_fp64 = false,
+                 int stage_override = -1) {
     Plan &p = h->p;
+    auto stage = [&](int s) { return stage_override >= 0 ? stage_override : s; };
     if (p.precision == SFB_MIXED && maps_are_fp64) {
         SFB_TRY(grow(p, p.maps32, (size_t)(nm * p.npix + 1) / 2));
         {
-            Stage s(h, SFB_STAGE_OTHER, st);
+            Stage s(h, stage(SFB_STAGE_OTHER), st);
             launch_to_float(maps, nm * p.npix, reinterpret_cast<float *>(p.maps32.ptr), st);
         }
         maps = p.maps32.ptr;
@@ -311,21 +313,29 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, b
         SFB_TRY(grow(p, p.gbuf, fsz));
         SFB_TRY(grow(p, p.rbuf, fsz));
     }
-    { Stage s(h, SFB_STAGE_RING_FFT, st); launch_ring_analysis(p, maps, nm, p.fbuf.ptr, st); }
+    if (p.precision == SFB_MIXED) {
+        SFB_TRY(grow(p, p.erow, (size_t)(p.nrn * nm + 1)));
+        Stage s(h, stage(SFB_STAGE_RING_FFT), st);
+        launch_ring_analysis_tc(p, reinterpret_cast<const float *>(maps), nm, reinterpret_cast<float *>(p.fbuf.ptr),
+                                reinterpret_cast<int *>(p.erow.ptr), st);
+    } else {
+        Stage s(h, stage(SFB_STAGE_RING_FFT), st);
+        launch_ring_analysis(p, maps, nm, p.fbuf.ptr, st);
+    }
     const bool tc = p.precision == SFB_MIXED;
     auto analysis = [&](const double *src, bool acc) {
-        Stage s(h, SFB_STAGE_LEG_ANALYSIS, st);
+        Stage s(h, stage(SFB_STAGE_LEG_ANALYSIS), st);
         if (tc) launch_leg_analysis_tc(p, (const float *)src, ncol, p.alm.ptr, acc, st);
         else launch_leg_analysis(p, src, ncol, p.alm.ptr, acc, st);
     };
     analysis(p.fbuf.ptr, false);
     for (int it = 0; it < p.niter; ++it) {
         {
-            Stage s(h, SFB_STAGE_LEG_SYNTHESIS, st);
+            Stage s(h, stage(SFB_STAGE_LEG_SYNTHESIS), st);
             if (tc) launch_leg_synthesis_tc(p, p.alm.ptr, ncol, (float *)p.gbuf.ptr, st);
             else launch_leg_synthesis(p, p.alm.ptr, ncol, p.gbuf.ptr, st);
         }
-        { Stage s(h, SFB_STAGE_FOLD, st); launch_fold_residual(p, p.fbuf.ptr, p.gbuf.ptr, ncol, p.rbuf.ptr, st); }
+        { Stage s(h, stage(SFB_STAGE_FOLD), st); launch_fold_residual(p, p.fbuf.ptr, p.gbuf.ptr, ncol, p.rbuf.ptr, st); }
         analysis(p.rbuf.ptr, true);
     }
     SFB_CUDA_TRY(cudaGetLastError());
@@ -347,6 +357,20 @@ int finish(sfb_plan *h, const double *out_dev, cudaStream_t st) {
     if (err & ERR_THETA_RANGE) return fail(SFB_ERANGE, "galaxy theta outside [0, pi]");
     if (err & ERR_TC_TIMEOUT) return fail(SFB_ETIMEOUT, "tensor-core kernel: bounded mbarrier wait expired");
     if (err & ERR_NONFINITE_OUTPUT) return fail(SFB_ENONFINITE, "non-finite a_nlm (all(isfinite.(anlm)) failed)");
+    return SFB_OK;
+}
+
+// FP64 a_lm of nref reference maps (mixed precision's mean terms), into
+// ralm[lmsize][2 nref].
+int reference_alm(sfb_plan *h, const double *ref, int64_t nref, double *ralm, cudaStream_t st) {
+    Plan &p = h->p;
+    const int32_t prec = p.precision;
+    p.precision = SFB_FP64;
+    const int rc = sht_analysis(h, ref, nref, st, false, SFB_STAGE_OTHER);
+    p.precision = prec;
+    SFB_TRY(rc);
+    SFB_CUDA_TRY(cudaMemcpyAsync(ralm, p.alm.ptr, (size_t)2 * nref * p.lmsize * sizeof(double),
+                                 cudaMemcpyDeviceToDevice, st));
     return SFB_OK;
 }
 
@@ -375,6 +399,25 @@ int cat2amln_dev(sfb_plan *h, const double *rtp, const double *w, int64_t ngal, 
     SFB_CUDA_TRY(cudaMemsetAsync(p.d_err, 0, sizeof(int), st));
     if (p.radial_mode == SFB_RADIAL_POLY) {
         const int64_t nm = p.nbasis + (wk == SFB_WINDOW_SEPARABLE ? 1 : 0);
+        // Mixed precision: the data maps are split into mu_b C + fluctuation
+        // with C the weighted galaxy count map, the dense window maps into
+        // nu W01 + fluctuation with W01 the window's (l=0, n=1) map; only the
+        // fluctuations pass through the FP32 transform, C_lm and the mask's
+        // (or W01's) a_lm are computed in FP64, so the cancellation between
+        // data and window term happens in FP64.
+        const bool split = p.precision == SFB_MIXED && wk != SFB_WINDOW_ZERO;
+        const double *W01 = wk == SFB_WINDOW_SEPARABLE ? win->mask : win->dense;
+        const int64_t cp = wk == SFB_WINDOW_DENSE ? chunk_pairs(p) : 0;
+        double *Cmap = nullptr, *ralm = nullptr, *mu = nullptr, *nu = nullptr;
+        if (split) {
+            // [C][W01][ralm: lmsize x (C, W01) complex][mu][nu]
+            SFB_TRY(grow(p, p.ref, (size_t)(2 * p.npix + 4 * p.lmsize + p.nbasis + cp)));
+            Cmap = p.ref.ptr;
+            ralm = Cmap + 2 * p.npix;
+            mu = ralm + 4 * p.lmsize;
+            nu = mu + p.nbasis;
+            SFB_CUDA_TRY(cudaMemcpyAsync(Cmap + p.npix, W01, p.npix * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        }
         SFB_TRY(grow(p, p.maps, (size_t)nm * p.npix));
         if (wk == SFB_WINDOW_SEPARABLE) {
             Stage s(h, SFB_STAGE_OTHER, st);
@@ -386,20 +429,25 @@ int cat2amln_dev(sfb_plan *h, const double *rtp, const double *w, int64_t ngal, 
         }
         {
             Stage s(h, SFB_STAGE_DEPOSIT, st);
-            SFB_TRY(deposit_sorted(p, rtp, w, ngal, p.maps.ptr, st));
+            SFB_TRY(deposit_sorted(p, rtp, w, ngal, p.maps.ptr, Cmap, mu, st));
         }
+        if (split) SFB_TRY(reference_alm(h, Cmap, 2, ralm, st));
         SFB_TRY(sht_analysis(h, p.maps.ptr, nm, st));
         {
             Stage s(h, SFB_STAGE_PROJECT, st);
+            if (split)
+                launch_add_mean(p.alm.ptr, 2 * nm, p.nbasis, mu, ralm, ralm + 2, 4, p.lmsize,
+                                wk == SFB_WINDOW_SEPARABLE ? p.nbasis : -1, st);
             launch_project_poly(p, p.alm.ptr, 2 * nm, scale, wk, win->w_ln, p.nbasis, nullptr, 0, out, st);
         }
         if (wk == SFB_WINDOW_DENSE) {
-            const int64_t cp = chunk_pairs(p);
             SFB_TRY(grow(p, p.maps, (size_t)cp * p.npix));
             for (int64_t p0 = 0; p0 < p.npairs; p0 += cp) {
                 const int64_t npc = std::min(cp, p.npairs - p0);
                 launch_gather_dense_chunk(p, p.maps.ptr, win->dense, p0, npc, st);
+                if (split) launch_split_mean(p.maps.ptr, npc, p.npix, W01, nu, st);
                 SFB_TRY(sht_analysis(h, p.maps.ptr, npc, st, true));
+                if (split) launch_add_mean(p.alm.ptr, 2 * npc, npc, nu, ralm + 2, nullptr, 4, p.lmsize, -1, st);
                 launch_sub_window_chunk(p, p.alm.ptr, 2 * npc, p0, npc, out, st);
             }
         }
@@ -582,6 +630,53 @@ int sfb_plan_create(const sfb_plan_desc *d, sfb_plan **out) {
             if ((st = upload(p, &p.d_wphase, wph.data(), wph.size())) != SFB_OK) break;
             if ((st = upload(p, &p.d_twtab32, tw32.data(), tw32.size())) != SFB_OK) break;
             if ((st = upload(p, &p.d_wphase32, wph32.data(), wph32.size())) != SFB_OK) break;
+            // tensor-core ring DFT tables: w cos(pi k / n), k < 2n, sliced on the scale 2^EB > w
+            const int EB = std::ilogb(wq) + 1;
+            std::vector<int64_t> doff(p.nrn);
+            std::vector<uint2> dtw;
+            int64_t eq_off = -1;
+            for (int64_t r = 0; r < p.nrn; ++r) {
+                const int n = p.h_rings[r].nph;
+                const bool eq = r >= ns - 1;
+                if (eq && eq_off >= 0) {
+                    doff[r] = eq_off;
+                    continue;
+                }
+                doff[r] = (int64_t)dtw.size();
+                if (eq) eq_off = doff[r];
+                for (int k = 0; k < 2 * n; ++k) {
+                    // cos(pi k / n) from the reduced angle: k mod 2n in [0, 2n), symmetric about n
+                    const int kk = k <= n ? k : 2 * n - k;
+                    double c;
+                    if (2 * kk == n) c = 0.0;
+                    else if (2 * kk < n) c = std::cos(M_PI * (double)kk / (double)n);
+                    else c = -std::cos(M_PI * (double)(n - kk) / (double)n);
+                    dtw.push_back(dft_slices(wq * c, EB));
+                }
+            }
+            std::vector<int32_t> crings, coff;
+            for (int64_t r = 0; r < ns - 1; ++r) {
+                coff.push_back((int32_t)crings.size());
+                crings.push_back((int32_t)r);
+            }
+            p.n_polar = (int)(ns - 1 > 0 ? ns - 1 : 0);
+            p.n_eq_cls = 0;
+            p.eq_max_rings = 0;
+            for (int type = 0; type < 2; ++type) {
+                const int32_t start = (int32_t)crings.size();
+                for (int64_t r = ns - 1; r < p.nrn; ++r)
+                    if ((p.h_rings[r].phi0_den != 0 ? 1 : 0) == type) crings.push_back((int32_t)r);
+                if ((int32_t)crings.size() > start) {
+                    coff.push_back(start);
+                    p.eq_max_rings = std::max(p.eq_max_rings, (int)crings.size() - start);
+                    ++p.n_eq_cls;
+                }
+            }
+            coff.push_back((int32_t)crings.size());
+            if ((st = upload(p, &p.d_dtw, dtw.data(), dtw.size())) != SFB_OK) break;
+            if ((st = upload(p, &p.d_dtw_off, doff.data(), doff.size())) != SFB_OK) break;
+            if ((st = upload(p, &p.d_cls_rings, crings.data(), crings.size())) != SFB_OK) break;
+            if ((st = upload(p, &p.d_cls_off, coff.data(), coff.size())) != SFB_OK) break;
         }
         std::vector<int64_t> lam_off(2 * (p.lmax + 1));
         int64_t off = 0;
@@ -651,10 +746,11 @@ void sfb_plan_destroy(sfb_plan *h) {
     Plan &p = h->p;
     cudaSetDevice(p.device);
     if (h->stream) cudaStreamSynchronize(h->stream);
-    void *ptrs[] = {p.d_rings, p.d_twtab, p.d_twoff, p.d_phase, p.d_wphase, p.d_twtab32, p.d_wphase32, p.d_lam, p.d_lam32, p.d_lamtc, p.d_lamtc_off, p.d_lamts, p.d_lamts_off, p.d_lam_off, p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp,
+    void *ptrs[] = {p.d_rings, p.d_twtab, p.d_twoff, p.d_phase, p.d_wphase, p.d_twtab32, p.d_wphase32, p.d_dtw,
+                    p.d_dtw_off, p.d_cls_rings, p.d_cls_off, p.d_lam, p.d_lam32, p.d_lamtc, p.d_lamtc_off, p.d_lamts, p.d_lamts_off, p.d_lam_off, p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp,
                     p.d_pair_l, p.d_pair_n, p.d_out_pair, p.d_out_lm, p.d_coef, p.d_err,
                     p.maps.ptr, p.fbuf.ptr, p.gbuf.ptr, p.rbuf.ptr, p.alm.ptr, p.scratch.ptr, p.scratch2.ptr, p.dep.ptr, p.maps32.ptr,
-                    h->d_pair_index, h->d_noff};
+                    p.ref.ptr, p.erow.ptr, h->d_pair_index, h->d_noff};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     collect_stages(h);

@@ -466,6 +466,74 @@ void launch_winweights(const double *weights, int64_t nr, int64_t nside, const d
     note_launch();
 }
 
+__global__ void k_add_mean(double *__restrict__ A, int64_t ldA, int64_t ncol, int64_t nmaps,
+                           const double *__restrict__ mu, const double *__restrict__ rmu,
+                           const double *__restrict__ rset, int64_t ldr, int64_t lmsize, int64_t set_col) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= lmsize * ncol) return;
+    const int64_t lm = e / ncol, j = e - lm * ncol;
+    if (j < nmaps) {
+        double *a = A + lm * ldA + 2 * j;
+        const double m = mu[j];
+        a[0] = fma(m, rmu[lm * ldr], a[0]);
+        a[1] = fma(m, rmu[lm * ldr + 1], a[1]);
+    } else {
+        double *a = A + lm * ldA + 2 * set_col;
+        a[0] = rset[lm * ldr];
+        a[1] = rset[lm * ldr + 1];
+    }
+}
+
+void launch_add_mean(double *A, int64_t ldA, int64_t nmaps, const double *mu, const double *rmu, const double *rset,
+                     int64_t ldr, int64_t lmsize, int64_t set_col, cudaStream_t st) {
+    const int64_t ncol = nmaps + (set_col >= 0 ? 1 : 0);
+    const int64_t n = lmsize * ncol;
+    if (n <= 0) return;
+    k_add_mean<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(A, ldA, ncol, nmaps, mu, rmu, rset, ldr, lmsize, set_col);
+    note_launch();
+}
+
+// One block per map: nu = <m, ref> / <ref, ref>, then m -= nu ref.
+__global__ void __launch_bounds__(512) k_split_mean(double *maps, int64_t npix, const double *__restrict__ ref,
+                                                    double *nu) {
+    __shared__ double red[2][16];
+    double *m = maps + (int64_t)blockIdx.x * npix;
+    double d = 0.0, q = 0.0;
+    for (int64_t p = threadIdx.x; p < npix; p += blockDim.x) {
+        const double r = ref[p];
+        d = fma(m[p], r, d);
+        q = fma(r, r, q);
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        d += __shfl_xor_sync(0xffffffffu, d, off);
+        q += __shfl_xor_sync(0xffffffffu, q, off);
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) {
+        red[0][wid] = d;
+        red[1][wid] = q;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double dd = 0.0, qq = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            dd += red[0][w];
+            qq += red[1][w];
+        }
+        red[0][0] = qq > 0.0 ? dd / qq : 0.0;
+        nu[blockIdx.x] = red[0][0];
+    }
+    __syncthreads();
+    const double v = red[0][0];
+    for (int64_t p = threadIdx.x; p < npix; p += blockDim.x) m[p] = fma(-v, ref[p], m[p]);
+}
+
+void launch_split_mean(double *maps, int64_t nmaps, int64_t npix, const double *ref, double *nu, cudaStream_t st) {
+    if (nmaps <= 0) return;
+    k_split_mean<<<(unsigned)nmaps, 512, 0, st>>>(maps, npix, ref, nu);
+    note_launch();
+}
+
 __global__ void k_fill(double *x, int64_t n, double v) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         x[i] = v;

@@ -1,0 +1,382 @@
+// Ring Fourier analysis of FP32 maps on the tensor cores (mixed precision).
+//
+// For m <= lmax the ring transform is a matrix product: with rows q = (ring,
+// map) of one ring class (all rings of equal length n and phase type) and
+// pixels j as the K dimension,
+//   F_N(q, m) = w sum_j x_N(q, j) e^{-i m (phi0 + 2 pi j / n)},
+// and e^{-i m (phi0 + 2 pi j/n)} = T[k] + i T[k + n/2] with
+// T[k] = cos(pi k / n), k = m (2 j + t) mod 2n, t = 1 if phi0 = pi/n else 0.
+// F+ = F_N + F_S and F- = F_N - F_S go to F[parity][m][ring][2 map + re/im],
+// the layout of the Legendre stage.
+//
+// Error-free splitting (the block-floating-point slicing of Ozaki, Ogita,
+// Oishi and Rump, "Error-free transformations of matrix multiplication by
+// using fast routines of matrix multiplication", Numer. Algorithms 59, 2012):
+// every value of a map row is written on the row's common scale 2^E (max|x| <
+// 2^E) as x = sum_s a_s 2^(E - 6 - 7 s), s = 0..3, with integers |a_s| <= 64;
+// every table value on the table's common scale 2^EB (w < 2^EB) as
+// T = sum_s b_s 2^(EB - 7 - 7 s), |b_0| <= 128, |b_s| <= 64.  Each slice is a
+// BF16 value with at most 8 significant bits.  The products of level
+// v = s_a + s_b (v = 0..3) are integers of one unit U 2^(-7 v) per row and
+// go to their own FP32 TMEM accumulator; every level sum stays below 2^24
+// units for rings of up to 1024 pixels, so it is exact whatever order or
+// rounding the tensor cores use.  Levels v >= 4 (below 2^-27 of the leading
+// term) are dropped.  The epilogue adds the levels and the north/south rows
+// with one significant FP32 rounding (TwoSum on the leading level).
+//
+// Tiles: M = 128 rows = 64 (ring, map) pairs x {north, south} (TMEM lanes
+// 0-63 north, 64-127 south), N = 128 accumulator columns (64 m values x
+// {cos, -sin}), K in chunks of 32 pixels.  The CTA builds the sliced A
+// planes and the B planes (gathered from the ring's sliced table) in shared
+// memory, double-buffered, with the next chunk's map values prefetched into
+// registers while the tensor cores work.  TMEM holds the four level
+// accumulators (4 x 128 columns).  Every mbarrier wait is bounded; on timeout
+// the CTA records ERR_TC_TIMEOUT, waits for its MMAs (bounded again),
+// releases TMEM and returns.
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <cstring>
+
+#include "sfb_internal.h"
+#include "tc_common.cuh"
+
+namespace sfb {
+namespace dft {
+
+using namespace tc;
+
+constexpr int KC = 32;            // pixels per chunk
+constexpr int NPAIR = 64;         // (ring, map) pairs per CTA
+constexpr int NROW = 128;         // A rows (MMA M): pairs x {north, south}
+constexpr int NCOL = 128;         // accumulator columns (MMA N)
+constexpr int NTHR = 128;
+constexpr uint32_t PLANE = NROW * KC * 2;              // bytes of one sliced plane (A or B)
+constexpr uint32_t STAGE = 8 * PLANE;                  // A planes 0..3, B planes 4..7
+constexpr size_t SMEM = 2 * (size_t)STAGE + 64;
+
+// products (s_a, s_b) by level: level 0 = [0], 1 = [1, 3), 2 = [3, 6), 3 = [6, 10)
+__constant__ int kSa[10] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3};
+__constant__ int kSb[10] = {0, 1, 0, 2, 1, 0, 3, 2, 1, 0};
+
+__device__ __forceinline__ uint32_t core_off(int row, int k) {
+    return (uint32_t)((((row >> 3) * (KC / 8) + (k >> 3)) << 7) + ((row & 7) << 4) + ((k & 7) << 1));
+}
+
+__device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + e) << 23); }   // -126 <= e <= 127
+
+__device__ __forceinline__ uint32_t bf16_bits(float v) {     // exact for values with <= 8 significant bits
+    return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v));
+}
+
+// Four slices of 8 values on the scale 2^(E - 6): y = x 2^(6 - E), a_s = rint,
+// remainder times 2^7.  Every step is exact in FP32.
+__device__ __forceinline__ void slice8(const float (&x)[8], int E, uint32_t (&w)[4][4]) {
+    const float up = pow2f(6 - E);
+#pragma unroll
+    for (int t = 0; t < 8; t += 2) {
+        uint32_t lo[4], hi[4];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            float y = x[t + h] * up;
+            float sc = pow2f(E - 6);
+#pragma unroll
+            for (int s = 0; s < 4; ++s) {
+                const float a = rintf(y);
+                y = (y - a) * 128.0f;
+                const uint32_t bits = bf16_bits(a * sc);
+                if (h == 0) lo[s] = bits; else hi[s] = bits;
+                sc *= 0.0078125f;
+            }
+        }
+#pragma unroll
+        for (int s = 0; s < 4; ++s) w[s][t >> 1] = lo[s] | (hi[s] << 16);
+    }
+}
+
+__device__ __forceinline__ void st_shared_v4(unsigned char *p, const uint32_t (&v)[4]) {
+    *reinterpret_cast<uint4 *>(p) = make_uint4(v[0], v[1], v[2], v[3]);
+}
+
+// Per (hemisphere, ring, map): E with max |x| < 2^E over the ring (0 for an
+// all-zero or empty row), raised by ceil(log2 n) - 10 for rings longer than
+// 1024 pixels so that the leading products still sum below 2^23 units.
+// erow layout [2][nrn][nmaps].
+__global__ void __launch_bounds__(128) k_ring_rowexp(const float *__restrict__ maps, int64_t npix, int64_t nmaps,
+                                                     const RingGeom *__restrict__ rings, int nrn, int *erow) {
+    const int r = blockIdx.x;
+    const int64_t b = (int64_t)blockIdx.y * 4 + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (b >= nmaps) return;
+    const RingGeom g = rings[r];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const float *x = maps + b * npix + (h ? g.start_s : g.start_n);
+        float mx = 0.f;
+        for (int j = lane; j < g.nph; j += 32) mx = fmaxf(mx, fabsf(x[j]));
+        for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+        if (lane == 0) {
+            int E = 0;
+            if (mx > 0.f && isfinite(mx)) E = ilogbf(mx) + 1;
+            const int lg = 32 - __clz(g.nph - 1);          // ceil(log2 n)
+            E += max(0, lg - 10);
+            E = max(-90, min(E, 100));
+            erow[((int64_t)h * nrn + r) * nmaps + b] = E;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict__ maps, int64_t npix, int64_t nmaps,
+                                                         const RingGeom *__restrict__ rings, int nrn, int lmax,
+                                                         const int32_t *__restrict__ cls_rings,
+                                                         const int32_t *__restrict__ cls_off,
+                                                         const int *__restrict__ erow, const uint2 *__restrict__ dtw,
+                                                         const int64_t *__restrict__ dtw_off, float *__restrict__ F,
+                                                         int64_t ldF, int *err) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    const int cls = blockIdx.y;
+    const int rb = cls_off[cls];
+    const int64_t npairs = (int64_t)(cls_off[cls + 1] - rb) * nmaps;
+    const int64_t pair0 = (int64_t)blockIdx.x * NPAIR;
+    if (pair0 >= npairs) return;
+    const int u = blockIdx.z;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + 2 * STAGE);
+    uint32_t *slot = reinterpret_cast<uint32_t *>(bars + 2);
+
+    // ring class: all rows share n, the phase type and the table
+    const int ring0 = cls_rings[rb];
+    const RingGeom g0 = rings[ring0];
+    const int n = g0.nph;
+    const int ptype = g0.phi0_den != 0 ? 1 : 0;
+    const int n2 = 2 * n;
+    const uint2 *T = dtw + dtw_off[ring0];
+    const int nch = (n + KC - 1) / KC;
+
+    // this thread's A row: pair tid % 64, hemisphere tid / 64
+    const int hemi = tid >> 6;
+    const int64_t q = pair0 + (tid & (NPAIR - 1));
+    const bool rok = q < npairs;
+    int ring = ring0;
+    int64_t b = 0;
+    if (rok) {
+        ring = cls_rings[rb + (int)(q / nmaps)];
+        b = q % nmaps;
+    }
+    const RingGeom g = rings[ring];
+    const bool live = rok && (hemi == 0 || g.start_s != g.start_n);   // the equator has no south partner
+    const float *x = maps + b * npix + (hemi ? g.start_s : g.start_n);
+    const int E = rok ? erow[((int64_t)hemi * nrn + ring) * nmaps + b] : 0;
+
+    // this thread's B row: column c = tid -> m = 64 u + c/2, part c&1 (0: cos, 1: -sin)
+    const int m = 64 * u + (tid >> 1);
+    const bool mok = m <= lmax;
+    const int step = (int)((2LL * m) % n2);
+    int kidx = (int)(((int64_t)m * ptype + (int64_t)(tid & 1) * (n / 2)) % n2);   // k of pixel j = 0
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
+                     "r"(512)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *slot;
+    const uint32_t idesc = idesc_bf16(NROW, NCOL);
+
+    // raw map values of the next chunk (n is a multiple of 4, ring starts are 16-byte aligned)
+    float4 pre[8];
+    auto load_chunk = [&](int kc) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int j = kc * KC + 4 * i;
+            pre[i] = (live && j < n) ? *reinterpret_cast<const float4 *>(x + j) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    };
+    load_chunk(0);
+
+    bool ok = true;
+    int issued = 0;                 // chunks whose MMAs were committed
+    for (int kc = 0; kc < nch; ++kc) {
+        const int st = kc & 1;
+        if (kc >= 2) {
+            // stage st is free once the MMAs of chunk kc-2 completed
+            if (!mbar_wait(&bars[st], (uint32_t)(((kc - 2) >> 1) & 1))) ok = false;
+            fence_after();
+        }
+        ok = __syncthreads_and(ok);
+        if (!ok) break;
+        unsigned char *sbase = smem + st * STAGE;         // A planes 0..3, B planes 4..7
+        // A row: 32 pixels as 4 groups of 8
+#pragma unroll
+        for (int gq = 0; gq < 4; ++gq) {
+            const float v[8] = {pre[2 * gq].x, pre[2 * gq].y, pre[2 * gq].z, pre[2 * gq].w,
+                                pre[2 * gq + 1].x, pre[2 * gq + 1].y, pre[2 * gq + 1].z, pre[2 * gq + 1].w};
+            uint32_t w[4][4];
+            slice8(v, E, w);
+            const uint32_t off = core_off(tid, 8 * gq);
+#pragma unroll
+            for (int s = 0; s < 4; ++s) st_shared_v4(sbase + s * PLANE + off, w[s]);
+        }
+        // B row: table slices at k = m (2 j + t) + part n/2 (mod 2n)
+        const int j0 = kc * KC;
+#pragma unroll
+        for (int gq = 0; gq < 4; ++gq) {
+            uint32_t w[4][4];
+#pragma unroll
+            for (int t = 0; t < 8; t += 2) {
+                const int j = j0 + 8 * gq + t;
+                uint2 e0 = make_uint2(0u, 0u), e1 = make_uint2(0u, 0u);
+                if (mok && j < n) e0 = T[kidx];
+                kidx += step;
+                if (kidx >= n2) kidx -= n2;
+                if (mok && j + 1 < n) e1 = T[kidx];
+                kidx += step;
+                if (kidx >= n2) kidx -= n2;
+                // e.x = slices 0 | 1 << 16, e.y = slices 2 | 3 << 16
+                w[0][t >> 1] = (e0.x & 0xffffu) | (e1.x << 16);
+                w[1][t >> 1] = (e0.x >> 16) | (e1.x & 0xffff0000u);
+                w[2][t >> 1] = (e0.y & 0xffffu) | (e1.y << 16);
+                w[3][t >> 1] = (e0.y >> 16) | (e1.y & 0xffff0000u);
+            }
+            const uint32_t off = core_off(tid, 8 * gq);
+#pragma unroll
+            for (int s = 0; s < 4; ++s) st_shared_v4(sbase + (4 + s) * PLANE + off, w[s]);
+        }
+        fence_proxy_async();
+        __syncthreads();
+        if (tid == 0) {
+            fence_after();
+            const uint32_t base = smem_u32(sbase);
+            const uint32_t sbo = (KC / 8) * 128;
+#pragma unroll
+            for (int s = 0; s < KC / 16; ++s) {
+                const bool first = kc == 0 && s == 0;
+#pragma unroll
+                for (int p = 0; p < 10; ++p) {
+                    const int lvl = p == 0 ? 0 : (p < 3 ? 1 : (p < 6 ? 2 : 3));
+                    const bool lead = p == 0 || p == 1 || p == 3 || p == 6;     // first product of its level
+                    mma_bf16(tmem + (uint32_t)(128 * lvl), smem_desc(base + kSa[p] * PLANE + s * 256, 128, sbo),
+                             smem_desc(base + (4 + kSb[p]) * PLANE + s * 256, 128, sbo), idesc,
+                             (first && lead) ? 0u : 1u);
+                }
+            }
+            mma_commit(&bars[st]);
+        }
+        ++issued;
+        if (kc + 1 < nch) load_chunk(kc + 1);
+    }
+    // all committed MMAs must be complete before TMEM is read or released
+    if (issued > 0) {
+        const int last = issued - 1;
+        if (!mbar_wait(&bars[last & 1], (uint32_t)((last >> 1) & 1))) ok = false;
+    }
+    fence_after();
+    ok = __syncthreads_and(ok);
+    if (!ok) {
+        if (tid == 0) atomicOr(err, ERR_TC_TIMEOUT);
+    } else {
+        // epilogue: per row, lead = level 0 (exact) and rest = level 1 + (level 2 + level 3); rows exchange
+        // through shared memory; thread t writes F+ (t < 64) or F- (t >= 64) of pair t % 64:
+        //   (s, e) = TwoSum(lead_N +- lead_S), F = s + ((rest_N +- rest_S) + e)
+        float *xch = reinterpret_cast<float *>(smem);      // [16 columns][lead, rest][128 rows]
+        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+        const int L1 = lmax + 1;
+        const int pr = tid & (NPAIR - 1);
+        const float sgn = (tid >> 6) ? -1.0f : 1.0f;
+#pragma unroll 1
+        for (int cg = 0; cg < NCOL / 16; ++cg) {
+            float v0[16], v1[16], v2[16], v3[16];
+            tmem_ld16(tmem + lane_base + (uint32_t)(16 * cg), v0);
+            tmem_ld16(tmem + lane_base + 128u + (uint32_t)(16 * cg), v1);
+            tmem_ld16(tmem + lane_base + 256u + (uint32_t)(16 * cg), v2);
+            tmem_ld16(tmem + lane_base + 384u + (uint32_t)(16 * cg), v3);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                xch[(2 * i) * NROW + tid] = v0[i];
+                xch[(2 * i + 1) * NROW + tid] = v1[i] + (v2[i] + v3[i]);
+            }
+            __syncthreads();
+            if (rok) {
+#pragma unroll
+                for (int t = 0; t < 8; ++t) {
+                    const int mm = 64 * u + 8 * cg + t;
+                    if (mm > lmax) break;
+                    float f[2];
+#pragma unroll
+                    for (int c = 0; c < 2; ++c) {
+                        const int i = 2 * t + c;
+                        const float a = xch[(2 * i) * NROW + pr], bb = sgn * xch[(2 * i) * NROW + pr + NPAIR];
+                        const float s = a + bb;
+                        const float z = s - a;
+                        const float e = (a - (s - z)) + (bb - z);
+                        f[c] = s + ((xch[(2 * i + 1) * NROW + pr] + sgn * xch[(2 * i + 1) * NROW + pr + NPAIR]) + e);
+                    }
+                    *reinterpret_cast<float2 *>(F + ((int64_t)((tid >> 6) * L1 + mm) * nrn + ring) * ldF + 2 * b) =
+                        make_float2(f[0], f[1]);
+                }
+            }
+            __syncthreads();
+        }
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
+}
+
+}  // namespace dft
+
+size_t ring_dft_smem() { return dft::SMEM; }
+
+// Host-side slicing of one table value v (|v| < 2^EB) into four BF16 slices
+// b_s 2^(EB - 7 - 7 s), packed as uint2 {s0 | s1 << 16, s2 | s3 << 16}.
+static uint16_t bf16_of_exact(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return (uint16_t)(u >> 16);      // f has at most 8 significant bits: truncation is exact
+}
+
+uint2 dft_slices(double v, int EB) {
+    double y = std::ldexp(v, 7 - EB);
+    uint16_t s[4];
+    for (int k = 0; k < 4; ++k) {
+        const double a = std::nearbyint(y);
+        y = (y - a) * 128.0;
+        s[k] = bf16_of_exact((float)std::ldexp(a, EB - 7 - 7 * k));
+    }
+    return make_uint2((uint32_t)s[0] | ((uint32_t)s[1] << 16), (uint32_t)s[2] | ((uint32_t)s[3] << 16));
+}
+
+void launch_ring_analysis_tc(const Plan &p, const float *maps, int64_t nmaps, float *F, int *erow, cudaStream_t st) {
+    {
+        dim3 grid((unsigned)p.nrn, (unsigned)((nmaps + 3) / 4));
+        dft::k_ring_rowexp<<<grid, 128, 0, st>>>(maps, p.npix, nmaps, p.d_rings, (int)p.nrn, erow);
+        note_launch();
+    }
+    set_smem(dft::k_ring_dft_tc, dft::SMEM);
+    const unsigned ntn = (unsigned)((p.lmax + 1 + 63) / 64);
+    // polar rings: one class per ring; equatorial rings: two classes (phase 0 and pi/n)
+    if (p.n_polar > 0) {
+        dim3 grid((unsigned)((nmaps + dft::NPAIR - 1) / dft::NPAIR), (unsigned)p.n_polar, ntn);
+        dft::k_ring_dft_tc<<<grid, dft::NTHR, dft::SMEM, st>>>(maps, p.npix, nmaps, p.d_rings, (int)p.nrn, p.lmax,
+                                                               p.d_cls_rings, p.d_cls_off, erow, p.d_dtw,
+                                                               p.d_dtw_off, F, 2 * nmaps, p.d_err);
+        note_launch();
+    }
+    const int64_t eq_tiles = ((int64_t)p.eq_max_rings * nmaps + dft::NPAIR - 1) / dft::NPAIR;
+    dim3 grid((unsigned)eq_tiles, (unsigned)p.n_eq_cls, ntn);
+    dft::k_ring_dft_tc<<<grid, dft::NTHR, dft::SMEM, st>>>(maps, p.npix, nmaps, p.d_rings, (int)p.nrn, p.lmax,
+                                                           p.d_cls_rings, p.d_cls_off + p.n_polar, erow,
+                                                           p.d_dtw, p.d_dtw_off, F, 2 * nmaps, p.d_err);
+    note_launch();
+}
+
+}  // namespace sfb

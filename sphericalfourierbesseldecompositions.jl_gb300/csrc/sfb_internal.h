@@ -87,6 +87,14 @@ struct Plan {
     double2 *d_wphase = nullptr;    // [nrn][lmax+1] (4 pi / npix) e^{-i m phi0(r)}
     float2 *d_twtab32 = nullptr;    // FP32 copies for the mixed-precision ring transform
     float2 *d_wphase32 = nullptr;
+    // tensor-core ring DFT: per-ring sliced tables (uint2 = 4 BF16 slices of
+    // w cos(pi k/n), k < 2n; equatorial rings share one), ring classes
+    // (polar rings one each, then the two equatorial phase classes)
+    uint2 *d_dtw = nullptr;
+    int64_t *d_dtw_off = nullptr;
+    int32_t *d_cls_rings = nullptr;
+    int32_t *d_cls_off = nullptr;      // [n_polar + n_eq_cls + 1]
+    int n_polar = 0, n_eq_cls = 0, eq_max_rings = 0;
     double *d_lam = nullptr;        // Legendre table, FP64
     float *d_lam32 = nullptr;       // the same table rounded to FP32 (mixed precision)
     void *d_lamtc = nullptr;        // split-BF16 table in tensor-core operand layout (analysis)
@@ -111,6 +119,8 @@ struct Plan {
     DevBuf<double> scratch;         // galaxy/window/output staging
     DevBuf<double> scratch2;
     DevBuf<double> dep;             // sorted-deposit workspace
+    DevBuf<double> ref;             // reference-map a_lm (FP64) and mean coefficients (mixed precision)
+    DevBuf<double> erow;            // ring DFT row exponents [2][nrn][nmaps] (int)
     DevBuf<double> maps32;          // FP32 copy of FP64 maps (mixed precision, spline / dense-window paths)
     int64_t device_bytes = 0;
 };
@@ -132,7 +142,17 @@ inline void set_smem(K kernel, size_t bytes) {
 // ---------------------------------------------------------------------------
 void launch_legendre_table(const Plan &p, cudaStream_t st);
 // galaxies -> radial-basis x pixel maps (counting sort + register moments); writes every map element
-int deposit_sorted(Plan &p, const double *rtp, const double *w, int64_t ngal, double *maps, cudaStream_t st);
+// Sorted deposit of the catalogue into the basis maps.  With ref (mixed
+// precision only) the weighted count map C is written to ref[npix], the maps
+// hold D_b - mu_b C and mu[nbasis] receives mu_b.
+int deposit_sorted(Plan &p, const double *rtp, const double *w, int64_t ngal, double *maps, double *ref,
+                   double *mu, cudaStream_t st);
+// A[lm][2j + c] += mu[j] * rmu[lm * ldr + c] for j < nmaps; with set_col >= 0
+// also A[lm][2 set_col + c] = rset[lm * ldr + c].
+void launch_add_mean(double *A, int64_t ldA, int64_t nmaps, const double *mu, const double *rmu, const double *rset,
+                     int64_t ldr, int64_t lmsize, int64_t set_col, cudaStream_t st);
+// maps[j] -= nu[j] ref with nu[j] = <maps[j], ref> / <ref, ref> (FP64, in place).
+void launch_split_mean(double *maps, int64_t nmaps, int64_t npix, const double *ref, double *nu, cudaStream_t st);
 void launch_ring_analysis(const Plan &p, const double *maps, int64_t nmaps, double *F, cudaStream_t st);
 void launch_ring_synthesis(const Plan &p, const double *G, int64_t nmaps, double *maps, cudaStream_t st);
 void launch_leg_analysis(const Plan &p, const double *F, int64_t ncol, double *A, bool accumulate,
@@ -146,6 +166,9 @@ void launch_project_poly(const Plan &p, const double *A, int64_t ldA, double sca
                          const double *w_ln, int64_t mask_col, const double *Awin, int64_t ldW,
                          double *out, cudaStream_t st);
 void launch_to_float(const double *in, int64_t n, float *out, cudaStream_t st);
+// Mixed-precision ring analysis on the tensor cores (FP32 maps -> FP32 F).
+void launch_ring_analysis_tc(const Plan &p, const float *maps, int64_t nmaps, float *F, int *erow, cudaStream_t st);
+uint2 dft_slices(double v, int EB);
 // tensor-core (tcgen05) Legendre analysis, mixed precision
 int64_t tc_table_offsets(const Plan &p, std::vector<int64_t> &off);
 void launch_build_lamtc(const Plan &p, cudaStream_t st);

@@ -1,8 +1,12 @@
 """Mixed precision (FP32 ring FFT, split-BF16 tcgen05 contractions, FP64
 deposit/tables/projection/window) against the FP64 GPU path and the oracle.
 
-Error measure: max|mixed - fp64| / max|fp64| over all a_nlm (global), and the
-per-mode relative error over modes with |a| above 1e-3 max|a| (recorded)."""
+Error measures: the L2 relative error ||a_mixed - a_ref||_2 / ||a_ref||_2
+over the whole a_nlm vector (held to MIXED_TOL everywhere) and the global
+max-norm error max|a_mixed - a_ref| / max|a_ref| (MIXED_TOL on the small
+configurations, 10 x MIXED_TOL on the ~1e6-coefficient full-size one).  The catalogues are
+drawn from the window itself, so the data term and the window term cancel to
+shot noise, as in a survey, which is the case that amplifies rounding."""
 
 import numpy as np
 import pytest
@@ -14,32 +18,65 @@ from oracle import sfb as osfb
 pytestmark = pytest.mark.gpu
 
 
-def _setup(kmax, rmin, rmax, nside, ngal, seed):
+def window_catalogue(ngal, rmin, rmax, fsky, seed, rmid=None, rsig=None):
+    """Galaxies drawn from nbar * phi(r) * mask: r ~ r^2 phi(r) by rejection,
+    directions uniform in the polar cap of gen_mask(fsky); weights U[0.5, 1.5]."""
+    rng = np.random.default_rng(seed)
+    rmid = 0.5 * (rmin + rmax) if rmid is None else rmid
+    rsig = 0.3 * (rmax - rmin) if rsig is None else rsig
+    f = lambda r: r * r * np.exp(-((r - rmid) / rsig) ** 2)
+    fmax = f(np.linspace(rmin, rmax, 4001)).max() * 1.001
+    rs, have = [], 0
+    while have < ngal:
+        r = rng.uniform(rmin, rmax, 2 * (ngal - have) + 1000)
+        r = r[rng.random(r.size) * fmax <= f(r)]
+        rs.append(r)
+        have += r.size
+    r = np.concatenate(rs)[:ngal]
+    mu = rng.uniform(1.0 - 2.0 * fsky, 1.0, ngal)
+    ph = rng.uniform(0.0, 2 * np.pi, ngal)
+    return np.stack([r, np.arccos(mu), ph]), rng.uniform(0.5, 1.5, ngal), (lambda rr: np.exp(-((rr - rmid) / rsig) ** 2))
+
+
+def _setup(kmax, rmin, rmax, nside, ngal, seed, kind="separable"):
     a = sfbgpu.AnlmModes(kmax, rmin, rmax, nside=nside)
-    rtp, w = catalogue(ngal, rmin, rmax, seed=seed, weights=True)
+    rtp, w, phif = window_catalogue(ngal, rmin, rmax, 0.75, seed)
     wm = sfbgpu.ConfigurationSpaceModes(rmin, rmax, 100, nside)
-    phi = np.exp(-((wm.r - 0.5 * (rmin + rmax)) / (0.3 * (rmax - rmin))) ** 2)
+    phi = phif(wm.r)
     mask = sfbgpu.gen_mask(nside, 0.75)
-    win = sfbgpu.win_rhat_ln(sfbgpu.SeparableArray(phi, mask, "phi", "mask"), wm, a)
     nbar = ngal / sfbgpu.integrate_window(sfbgpu.SeparableArray(phi, mask), wm)
+    if kind == "separable":
+        win = sfbgpu.win_rhat_ln(sfbgpu.SeparableArray(phi, mask, "phi", "mask"), wm, a)
+    elif kind == "dense":
+        # separable part plus a direction-dependent radial tilt
+        th, _ = sfbgpu.pix2ang_ring(nside, np.arange(wm.npix))
+        tilt = 1.0 + 0.2 * np.cos(th)[None, :] * ((wm.r - 0.5 * (rmin + rmax)) / (rmax - rmin))[:, None]
+        win = sfbgpu.win_rhat_ln(phi[:, None] * mask[None, :] * tilt, wm, a)
+    else:
+        win = None
     return a, rtp, w, win, nbar
 
 
-# the mixed path's accuracy bar: ||a_mixed - a_ref|| / ||a_ref|| <= 1e-7
+def _errors(x, ref):
+    return float(np.linalg.norm(x - ref) / np.linalg.norm(ref)), rel_err(x, ref)
+
+
+# the mixed path's accuracy bar
 MIXED_TOL = 1e-7
 
 
-@pytest.mark.parametrize("cfg", [(0.03, 500.0, 1000.0, 16, 50_000, 1), (0.05, 500.0, 1000.0, 32, 200_000, 2)])
-def test_mixed_vs_fp64(cfg):
+@pytest.mark.parametrize("cfg,kind", [((0.03, 500.0, 1000.0, 16, 50_000, 1), "separable"),
+                                      ((0.05, 500.0, 1000.0, 32, 200_000, 2), "separable"),
+                                      ((0.03, 500.0, 1000.0, 16, 50_000, 5), "dense"),
+                                      ((0.03, 500.0, 1000.0, 16, 50_000, 6), "zero")])
+def test_mixed_vs_fp64(cfg, kind):
     kmax, rmin, rmax, nside, ngal, seed = cfg
-    a, rtp, w, win, nbar = _setup(*cfg)
+    a, rtp, w, win, nbar = _setup(*cfg, kind=kind)
     f64 = sfbgpu.cat2amln(rtp, a, nbar, win, w, precision="fp64")
     mix = sfbgpu.cat2amln(rtp, a, nbar, win, w, precision="mixed")
-    e = rel_err(mix, f64)
-    big = np.abs(f64) > 1e-3 * np.max(np.abs(f64))
-    per_mode = float(np.max(np.abs(mix - f64)[big] / np.abs(f64)[big]))
-    record(f"mixed_vs_fp64_kmax{kmax}_nside{nside}", e, per_mode_rel_above_1em3=per_mode)
-    assert e < MIXED_TOL
+    e2, emax = _errors(mix, f64)
+    record(f"mixed_vs_fp64_{kind}_kmax{kmax}_nside{nside}", e2, maxnorm=emax)
+    assert e2 < MIXED_TOL and emax < MIXED_TOL
 
 
 def test_mixed_vs_reference_algorithm():
@@ -47,9 +84,30 @@ def test_mixed_vs_reference_algorithm():
     md = modes_dict(a)
     ref = osfb.cat2amln(rtp, md, nbar, ("separable", win.mask, win.w_ln), w)
     mix = sfbgpu.cat2amln(rtp, a, nbar, win, w, precision="mixed")
-    e = rel_err(mix, ref)
-    record("mixed_vs_reference_algorithm", e)
-    assert e < MIXED_TOL
+    e2, emax = _errors(mix, ref)
+    record("mixed_vs_reference_algorithm", e2, maxnorm=emax)
+    assert e2 < MIXED_TOL and emax < MIXED_TOL
+
+
+def test_mixed_full_size():
+    """The full-size geometry (kmax 0.1, r in [500, 2500], nside 256, 7520
+    (n, l) pairs) with 2e6 galaxies in a 60-degree cap x Gaussian shell."""
+    a = sfbgpu.AnlmModes(0.1, 500.0, 2500.0, nside=256)
+    ngal = 2_000_000
+    fsky = (1 - np.cos(np.radians(60.0))) / 2
+    rtp, w, phif = window_catalogue(ngal, 500.0, 2500.0, fsky, 7, rmid=1500.0, rsig=400.0 * np.sqrt(2))
+    wm = sfbgpu.ConfigurationSpaceModes(500.0, 2500.0, 1000, 256)
+    phi = phif(wm.r)
+    mask = sfbgpu.gen_mask(256, fsky)
+    nbar = ngal / sfbgpu.integrate_window(sfbgpu.SeparableArray(phi, mask), wm)
+    win = sfbgpu.win_rhat_ln(sfbgpu.SeparableArray(phi, mask, "phi", "mask"), wm, a, radial="poly")
+    f64 = sfbgpu.cat2amln(rtp, a, nbar, win, w, precision="fp64", radial="poly")
+    mix = sfbgpu.cat2amln(rtp, a, nbar, win, w, precision="mixed", radial="poly")
+    e2, emax = _errors(mix, f64)
+    record("mixed_vs_fp64_full_size_nside256_kmax0.1", e2, maxnorm=emax)
+    # ~1e6 coefficients: the L2 error is the bar; the largest single error,
+    # relative to the largest coefficient, is held to 10x that
+    assert e2 < MIXED_TOL and emax < 10 * MIXED_TOL
 
 
 def test_bounded_wait_times_out_and_context_survives():
