@@ -214,6 +214,91 @@ __global__ void k_deposit_moments(const int32_t *__restrict__ offset, const doub
     }
 }
 
+// Double-float arithmetic (value = hi + lo, |lo| <= ulp(hi)/2): ~48
+// significant bits from FP32 operations, whose throughput on this GPU is
+// many times that of FP64.  TwoSum / TwoProd with FMA (Dekker, Knuth).
+struct dfl {
+    float hi, lo;
+};
+
+__device__ __forceinline__ dfl df_of(double x) {
+    const float h = (float)x;
+    return {h, (float)(x - (double)h)};
+}
+
+__device__ __forceinline__ dfl df_add(dfl a, dfl b) {
+    const float s = a.hi + b.hi;
+    const float z = s - a.hi;
+    const float e = ((a.hi - (s - z)) + (b.hi - z)) + (a.lo + b.lo);
+    const float h = s + e;
+    return {h, e - (h - s)};
+}
+
+__device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
+    const float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+    const float h = p + e;
+    return {h, e - (h - p)};
+}
+
+// Mixed precision: moments with the Legendre recurrence and the sums in
+// double-float; the fluctuation acc - mu_b ref is formed in FP64 and stored
+// as FP32.
+template <int MAXDEG>
+__global__ void k_deposit_moments_df(const int32_t *__restrict__ offset, const double2 *__restrict__ sorted,
+                                     int64_t npix, int pieces, int deg, int64_t nbasis, const double *__restrict__ ref,
+                                     const double *__restrict__ mu, float *__restrict__ maps) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nkeys = (int64_t)(pieces + 2) * npix;
+    if (idx >= nkeys) return;
+    const int slot = (int)(idx / npix);
+    const int64_t pix = idx - (int64_t)slot * npix;
+    const int64_t g0 = offset[idx];
+    const int64_t g1 = offset[idx + 1];
+    const double rv = ref ? ref[pix] : 0.0;
+    if (slot >= pieces) {
+        dfl s = {0.f, 0.f};
+        for (int64_t g = g0; g < g1; ++g) s = df_add(s, df_of(sorted[g].y));
+        const int64_t b = nbasis - 2 + (slot - pieces);
+        double v = (double)s.hi + (double)s.lo;
+        if (ref) v -= mu[b] * rv;
+        maps[b * npix + pix] = (float)v;
+        return;
+    }
+    dfl acc[MAXDEG + 1];
+#pragma unroll
+    for (int k = 0; k <= MAXDEG; ++k) acc[k] = {0.f, 0.f};
+    for (int64_t g = g0; g < g1; ++g) {
+        const double2 xw = sorted[g];
+        const dfl x = df_of(xw.x), w = df_of(xw.y);
+        dfl p0 = {1.f, 0.f}, p1 = x;
+        acc[0] = df_add(acc[0], w);
+        if (MAXDEG >= 1) acc[1] = df_add(acc[1], df_mul(w, x));
+#pragma unroll
+        for (int k = 1; k < MAXDEG; ++k) {
+            if (k >= deg) break;
+            // (k+1) P_{k+1} = (2k+1) x P_k - k P_{k-1}, the ratios as double-float constants
+            const dfl c1 = df_of((double)(2 * k + 1) / (k + 1));
+            const dfl c2 = df_of(-(double)k / (k + 1));
+            const dfl p2 = df_add(df_mul(c1, df_mul(x, p1)), df_mul(c2, p0));
+            acc[k + 1] = df_add(acc[k + 1], df_mul(w, p2));
+            p0 = p1;
+            p1 = p2;
+        }
+    }
+    const int64_t b0 = (int64_t)slot * (deg + 1);
+    float *base = maps + b0 * npix + pix;
+#pragma unroll
+    for (int k = 0; k <= MAXDEG; ++k) {
+        if (k <= deg) {
+            double v = (double)acc[k].hi + (double)acc[k].lo;
+            if (ref) v -= mu[b0 + k] * rv;
+            base[(int64_t)k * npix] = (float)v;
+        }
+    }
+}
+
 constexpr int STATS_STRIDE = 32;
 
 // Sampled projections onto ref over the bins of every STATS_STRIDE-th group of
@@ -292,8 +377,8 @@ static void launch_moments(const Plan &p, const int32_t *counts, const double2 *
     const int64_t nkeys = (int64_t)(p.pieces + 2) * p.npix;
     const unsigned blocks = (unsigned)((nkeys + 127) / 128);
     if (p.precision == SFB_MIXED)
-        k_deposit_moments<MAXDEG, float><<<blocks, 128, 0, st>>>(counts, sorted, p.npix, p.pieces, p.degree,
-                                                                 p.nbasis, ref, mu, reinterpret_cast<float *>(maps));
+        k_deposit_moments_df<MAXDEG><<<blocks, 128, 0, st>>>(counts, sorted, p.npix, p.pieces, p.degree, p.nbasis,
+                                                             ref, mu, reinterpret_cast<float *>(maps));
     else
         k_deposit_moments<MAXDEG, double><<<blocks, 128, 0, st>>>(counts, sorted, p.npix, p.pieces, p.degree,
                                                                   p.nbasis, ref, mu, maps);

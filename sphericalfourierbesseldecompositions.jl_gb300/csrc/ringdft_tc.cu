@@ -50,7 +50,7 @@ constexpr int KC = 32;            // pixels per chunk
 constexpr int NPAIR = 64;         // (ring, map) pairs per CTA
 constexpr int NROW = 128;         // A rows (MMA M): pairs x {north, south}
 constexpr int NCOL = 128;         // accumulator columns (MMA N)
-constexpr int NTHR = 128;
+constexpr int NTHR = 256;        // warps 0-3 build the A rows, warps 4-7 the B rows
 constexpr uint32_t PLANE = NROW * KC * 2;              // bytes of one sliced plane (A or B)
 constexpr uint32_t STAGE = 8 * PLANE;                  // A planes 0..3, B planes 4..7
 constexpr size_t SMEM = 2 * (size_t)STAGE + 64;
@@ -69,28 +69,28 @@ __device__ __forceinline__ uint32_t bf16_bits(float v) {     // exact for values
     return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v));
 }
 
-// Four slices of 8 values on the scale 2^(E - 6): y = x 2^(6 - E), a_s = rint,
-// remainder times 2^7.  Every step is exact in FP32.
-__device__ __forceinline__ void slice8(const float (&x)[8], int E, uint32_t (&w)[4][4]) {
-    const float up = pow2f(6 - E);
+// Four slices of 8 values: s_k = RN(r_k / 2^(E - 6 - 7k)) 2^(E - 6 - 7k) with
+// r_0 = x, r_{k+1} = r_k - s_k, formed as (r + C_k) - C_k with
+// C_k = 1.5 2^(E + 17 - 7k) (the sum's ulp is the slice unit); every step is
+// exact in FP32 and each slice has at most 7 significant bits.
+__device__ __forceinline__ uint32_t bf16x2(float lo, float hi) {
+    uint32_t r;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+    return r;
+}
+
+__device__ __forceinline__ void slice8(const float (&x)[8], const float (&C)[4], uint32_t (&w)[4][4]) {
 #pragma unroll
     for (int t = 0; t < 8; t += 2) {
-        uint32_t lo[4], hi[4];
+        float r0 = x[t], r1 = x[t + 1];
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            float y = x[t + h] * up;
-            float sc = pow2f(E - 6);
-#pragma unroll
-            for (int s = 0; s < 4; ++s) {
-                const float a = rintf(y);
-                y = (y - a) * 128.0f;
-                const uint32_t bits = bf16_bits(a * sc);
-                if (h == 0) lo[s] = bits; else hi[s] = bits;
-                sc *= 0.0078125f;
-            }
+        for (int s = 0; s < 4; ++s) {
+            const float a0 = __fsub_rn(__fadd_rn(r0, C[s]), C[s]);
+            const float a1 = __fsub_rn(__fadd_rn(r1, C[s]), C[s]);
+            w[s][t >> 1] = bf16x2(a0, a1);
+            r0 = __fsub_rn(r0, a0);
+            r1 = __fsub_rn(r1, a1);
         }
-#pragma unroll
-        for (int s = 0; s < 4; ++s) w[s][t >> 1] = lo[s] | (hi[s] << 16);
     }
 }
 
@@ -141,6 +141,8 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
     if (pair0 >= npairs) return;
     const int u = blockIdx.z;
     const int tid = threadIdx.x, warp = tid >> 5;
+    const bool abuild = tid < NROW;          // warps 0-3: A row tid; warps 4-7: B row tid - 128
+    const int ti = tid & (NROW - 1);
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + 2 * STAGE);
     uint32_t *slot = reinterpret_cast<uint32_t *>(bars + 2);
 
@@ -153,9 +155,9 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
     const uint2 *T = dtw + dtw_off[ring0];
     const int nch = (n + KC - 1) / KC;
 
-    // this thread's A row: pair tid % 64, hemisphere tid / 64
-    const int hemi = tid >> 6;
-    const int64_t q = pair0 + (tid & (NPAIR - 1));
+    // A row ti: pair ti % 64, hemisphere ti / 64
+    const int hemi = ti >> 6;
+    const int64_t q = pair0 + (ti & (NPAIR - 1));
     const bool rok = q < npairs;
     int ring = ring0;
     int64_t b = 0;
@@ -164,15 +166,18 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
         b = q % nmaps;
     }
     const RingGeom g = rings[ring];
-    const bool live = rok && (hemi == 0 || g.start_s != g.start_n);   // the equator has no south partner
+    const bool live = abuild && rok && (hemi == 0 || g.start_s != g.start_n);   // the equator has no south row
     const float *x = maps + b * npix + (hemi ? g.start_s : g.start_n);
     const int E = rok ? erow[((int64_t)hemi * nrn + ring) * nmaps + b] : 0;
+    float C[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) C[k] = 1.5f * pow2f(E + 17 - 7 * k);
 
-    // this thread's B row: column c = tid -> m = 64 u + c/2, part c&1 (0: cos, 1: -sin)
-    const int m = 64 * u + (tid >> 1);
+    // B row ti: column c = ti -> m = 64 u + c/2, part c&1 (0: cos, 1: -sin)
+    const int m = 64 * u + (ti >> 1);
     const bool mok = m <= lmax;
     const int step = (int)((2LL * m) % n2);
-    int kidx = (int)(((int64_t)m * ptype + (int64_t)(tid & 1) * (n / 2)) % n2);   // k of pixel j = 0
+    int kidx = (int)(((int64_t)m * ptype + (int64_t)(ti & 1) * (n / 2)) % n2);   // k of pixel j = 0
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
@@ -200,7 +205,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
             pre[i] = (live && j < n) ? *reinterpret_cast<const float4 *>(x + j) : make_float4(0.f, 0.f, 0.f, 0.f);
         }
     };
-    load_chunk(0);
+    if (abuild) load_chunk(0);
 
     bool ok = true;
     int issued = 0;                 // chunks whose MMAs were committed
@@ -214,19 +219,21 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
         ok = __syncthreads_and(ok);
         if (!ok) break;
         unsigned char *sbase = smem + st * STAGE;         // A planes 0..3, B planes 4..7
-        // A row: 32 pixels as 4 groups of 8
-#pragma unroll
-        for (int gq = 0; gq < 4; ++gq) {
-            const float v[8] = {pre[2 * gq].x, pre[2 * gq].y, pre[2 * gq].z, pre[2 * gq].w,
-                                pre[2 * gq + 1].x, pre[2 * gq + 1].y, pre[2 * gq + 1].z, pre[2 * gq + 1].w};
-            uint32_t w[4][4];
-            slice8(v, E, w);
-            const uint32_t off = core_off(tid, 8 * gq);
-#pragma unroll
-            for (int s = 0; s < 4; ++s) st_shared_v4(sbase + s * PLANE + off, w[s]);
-        }
-        // B row: table slices at k = m (2 j + t) + part n/2 (mod 2n)
         const int j0 = kc * KC;
+        if (abuild) {
+            // A row: 32 pixels as 4 groups of 8
+#pragma unroll
+            for (int gq = 0; gq < 4; ++gq) {
+                const float v[8] = {pre[2 * gq].x, pre[2 * gq].y, pre[2 * gq].z, pre[2 * gq].w,
+                                    pre[2 * gq + 1].x, pre[2 * gq + 1].y, pre[2 * gq + 1].z, pre[2 * gq + 1].w};
+                uint32_t w[4][4];
+                slice8(v, C, w);
+                const uint32_t off = core_off(ti, 8 * gq);
+#pragma unroll
+                for (int s = 0; s < 4; ++s) st_shared_v4(sbase + s * PLANE + off, w[s]);
+            }
+        } else {
+        // B row: table slices at k = m (2 j + t) + part n/2 (mod 2n)
 #pragma unroll
         for (int gq = 0; gq < 4; ++gq) {
             uint32_t w[4][4];
@@ -246,9 +253,10 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
                 w[2][t >> 1] = (e0.y & 0xffffu) | (e1.y << 16);
                 w[3][t >> 1] = (e0.y >> 16) | (e1.y & 0xffff0000u);
             }
-            const uint32_t off = core_off(tid, 8 * gq);
+            const uint32_t off = core_off(ti, 8 * gq);
 #pragma unroll
             for (int s = 0; s < 4; ++s) st_shared_v4(sbase + (4 + s) * PLANE + off, w[s]);
+        }
         }
         fence_proxy_async();
         __syncthreads();
@@ -271,7 +279,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
             mma_commit(&bars[st]);
         }
         ++issued;
-        if (kc + 1 < nch) load_chunk(kc + 1);
+        if (abuild && kc + 1 < nch) load_chunk(kc + 1);
     }
     // all committed MMAs must be complete before TMEM is read or released
     if (issued > 0) {
@@ -283,16 +291,30 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
     if (!ok) {
         if (tid == 0) atomicOr(err, ERR_TC_TIMEOUT);
     } else {
-        // epilogue: per row, lead = level 0 (exact) and rest = level 1 + (level 2 + level 3); rows exchange
-        // through shared memory; thread t writes F+ (t < 64) or F- (t >= 64) of pair t % 64:
-        //   (s, e) = TwoSum(lead_N +- lead_S), F = s + ((rest_N +- rest_S) + e)
-        float *xch = reinterpret_cast<float *>(smem);      // [16 columns][lead, rest][128 rows]
-        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+        // epilogue: per row, lead = level 0 (exact) and rest = level 1 + (level 2 + level 3).  Warps w and
+        // w + 4 read the same TMEM lanes (rows) and the column groups cg = it and 4 + it; rows exchange through
+        // shared memory; then thread t writes, for column group (t / 128) * 4 + it, F+ (t % 128 < 64) or
+        // F- of pair t % 64:  (s, e) = TwoSum(lead_N +- lead_S), F = s + ((rest_N +- rest_S) + e)
+        float *xch = reinterpret_cast<float *>(smem);      // [2 halves][16 columns][lead, rest][128 rows]
+        const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+        const int half = tid >> 7;
         const int L1 = lmax + 1;
-        const int pr = tid & (NPAIR - 1);
-        const float sgn = (tid >> 6) ? -1.0f : 1.0f;
+        const int pr = ti & (NPAIR - 1);
+        const int sg = ti >> 6;
+        const float sgn = sg ? -1.0f : 1.0f;
+        // the output pair of this thread (pair pr of the tile)
+        const int64_t qo = pair0 + pr;
+        const bool ook = qo < npairs;
+        int oring = ring0;
+        int64_t ob = 0;
+        if (ook) {
+            oring = cls_rings[rb + (int)(qo / nmaps)];
+            ob = qo % nmaps;
+        }
+        float *xh = xch + half * (32 * NROW);
 #pragma unroll 1
-        for (int cg = 0; cg < NCOL / 16; ++cg) {
+        for (int it = 0; it < 4; ++it) {
+            const int cg = 4 * half + it;
             float v0[16], v1[16], v2[16], v3[16];
             tmem_ld16(tmem + lane_base + (uint32_t)(16 * cg), v0);
             tmem_ld16(tmem + lane_base + 128u + (uint32_t)(16 * cg), v1);
@@ -300,11 +322,11 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
             tmem_ld16(tmem + lane_base + 384u + (uint32_t)(16 * cg), v3);
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
-                xch[(2 * i) * NROW + tid] = v0[i];
-                xch[(2 * i + 1) * NROW + tid] = v1[i] + (v2[i] + v3[i]);
+                xh[(2 * i) * NROW + ti] = v0[i];
+                xh[(2 * i + 1) * NROW + ti] = v1[i] + (v2[i] + v3[i]);
             }
             __syncthreads();
-            if (rok) {
+            if (ook) {
 #pragma unroll
                 for (int t = 0; t < 8; ++t) {
                     const int mm = 64 * u + 8 * cg + t;
@@ -313,13 +335,13 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
 #pragma unroll
                     for (int c = 0; c < 2; ++c) {
                         const int i = 2 * t + c;
-                        const float a = xch[(2 * i) * NROW + pr], bb = sgn * xch[(2 * i) * NROW + pr + NPAIR];
+                        const float a = xh[(2 * i) * NROW + pr], bb = sgn * xh[(2 * i) * NROW + pr + NPAIR];
                         const float s = a + bb;
                         const float z = s - a;
                         const float e = (a - (s - z)) + (bb - z);
-                        f[c] = s + ((xch[(2 * i + 1) * NROW + pr] + sgn * xch[(2 * i + 1) * NROW + pr + NPAIR]) + e);
+                        f[c] = s + ((xh[(2 * i + 1) * NROW + pr] + sgn * xh[(2 * i + 1) * NROW + pr + NPAIR]) + e);
                     }
-                    *reinterpret_cast<float2 *>(F + ((int64_t)((tid >> 6) * L1 + mm) * nrn + ring) * ldF + 2 * b) =
+                    *reinterpret_cast<float2 *>(F + ((int64_t)(sg * L1 + mm) * nrn + oring) * ldF + 2 * ob) =
                         make_float2(f[0], f[1]);
                 }
             }
