@@ -323,16 +323,18 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, b
         launch_ring_analysis(p, maps, nm, p.fbuf.ptr, st);
     }
     const bool tc = p.precision == SFB_MIXED;
+    if (tc) SFB_TRY(grow(p, p.almdf, (size_t)p.lmsize * ncol));
+    float2 *adf = reinterpret_cast<float2 *>(p.almdf.ptr);
     auto analysis = [&](const double *src, bool acc) {
         Stage s(h, stage(SFB_STAGE_LEG_ANALYSIS), st);
-        if (tc) launch_leg_analysis_tc(p, (const float *)src, ncol, p.alm.ptr, acc, st);
+        if (tc) launch_leg_analysis_tc(p, (const float *)src, ncol, p.alm.ptr, adf, acc, st);
         else launch_leg_analysis(p, src, ncol, p.alm.ptr, acc, st);
     };
     analysis(p.fbuf.ptr, false);
     for (int it = 0; it < p.niter; ++it) {
         {
             Stage s(h, stage(SFB_STAGE_LEG_SYNTHESIS), st);
-            if (tc) launch_leg_synthesis_tc(p, p.alm.ptr, ncol, (float *)p.gbuf.ptr, st);
+            if (tc) launch_leg_synthesis_tc(p, adf, ncol, (float *)p.gbuf.ptr, st);
             else launch_leg_synthesis(p, p.alm.ptr, ncol, p.gbuf.ptr, st);
         }
         { Stage s(h, stage(SFB_STAGE_FOLD), st); launch_fold_residual(p, p.fbuf.ptr, p.gbuf.ptr, ncol, p.rbuf.ptr, st); }
@@ -712,12 +714,16 @@ int sfb_plan_create(const sfb_plan_desc *d, sfb_plan **out) {
                 st = fail(SFB_ECUDA, "table clear failed");
                 break;
             }
-            launch_build_lamtc(p, h->stream);
+            // row scales: Ea per (z, li) row over the rings, Es per (z, ring) over the rows
+            const int64_t nrow_tot = off / p.nrn, nes = 2 * (p.lmax + 1) * p.nrn;
+            if ((st = grow(p, p.scratch, (size_t)((nrow_tot + nes) / 2 + 2))) != SFB_OK) break;
+            int *Ea = reinterpret_cast<int *>(p.scratch.ptr), *Es = Ea + nrow_tot;
+            launch_build_lamtc(p, Ea, Es, h->stream);
             std::vector<int64_t> soff;
             const int64_t ssz = tc_synth_table_offsets(p, soff);
             if ((st = upload(p, &p.d_lamts_off, soff.data(), soff.size())) != SFB_OK) break;
             if ((st = upload<uint16_t>(p, (uint16_t **)&p.d_lamts, nullptr, (size_t)ssz)) != SFB_OK) break;
-            launch_build_lamts(p, h->stream);
+            launch_build_lamts(p, Es, h->stream);
         }
         if (cudaGetLastError() != cudaSuccess) {
             st = fail(SFB_ECUDA, "Legendre table kernel failed to launch");
@@ -750,7 +756,7 @@ void sfb_plan_destroy(sfb_plan *h) {
                     p.d_dtw_off, p.d_cls_rings, p.d_cls_off, p.d_lam, p.d_lam32, p.d_lamtc, p.d_lamtc_off, p.d_lamts, p.d_lamts_off, p.d_lam_off, p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp,
                     p.d_pair_l, p.d_pair_n, p.d_out_pair, p.d_out_lm, p.d_coef, p.d_err,
                     p.maps.ptr, p.fbuf.ptr, p.gbuf.ptr, p.rbuf.ptr, p.alm.ptr, p.scratch.ptr, p.scratch2.ptr, p.dep.ptr, p.maps32.ptr,
-                    p.ref.ptr, p.erow.ptr, h->d_pair_index, h->d_noff};
+                    p.ref.ptr, p.erow.ptr, p.almdf.ptr, h->d_pair_index, h->d_noff};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     collect_stages(h);

@@ -63,34 +63,14 @@ __device__ __forceinline__ uint32_t core_off(int row, int k) {
     return (uint32_t)((((row >> 3) * (KC / 8) + (k >> 3)) << 7) + ((row & 7) << 4) + ((k & 7) << 1));
 }
 
-__device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + e) << 23); }   // -126 <= e <= 127
-
-__device__ __forceinline__ uint32_t bf16_bits(float v) {     // exact for values with <= 8 significant bits
-    return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v));
-}
-
-// Four slices of 8 values: s_k = RN(r_k / 2^(E - 6 - 7k)) 2^(E - 6 - 7k) with
-// r_0 = x, r_{k+1} = r_k - s_k, formed as (r + C_k) - C_k with
-// C_k = 1.5 2^(E + 17 - 7k) (the sum's ulp is the slice unit); every step is
-// exact in FP32 and each slice has at most 7 significant bits.
-__device__ __forceinline__ uint32_t bf16x2(float lo, float hi) {
-    uint32_t r;
-    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
-    return r;
-}
-
+// slices of 8 values (see slice_pair), packed as 4 words per plane
 __device__ __forceinline__ void slice8(const float (&x)[8], const float (&C)[4], uint32_t (&w)[4][4]) {
 #pragma unroll
     for (int t = 0; t < 8; t += 2) {
-        float r0 = x[t], r1 = x[t + 1];
+        uint32_t v[4];
+        slice_pair(x[t], x[t + 1], C, v);
 #pragma unroll
-        for (int s = 0; s < 4; ++s) {
-            const float a0 = __fsub_rn(__fadd_rn(r0, C[s]), C[s]);
-            const float a1 = __fsub_rn(__fadd_rn(r1, C[s]), C[s]);
-            w[s][t >> 1] = bf16x2(a0, a1);
-            r0 = __fsub_rn(r0, a0);
-            r1 = __fsub_rn(r1, a1);
-        }
+        for (int s = 0; s < 4; ++s) w[s][t >> 1] = v[s];
     }
 }
 
@@ -116,8 +96,7 @@ __global__ void __launch_bounds__(128) k_ring_rowexp(const float *__restrict__ m
         for (int j = lane; j < g.nph; j += 32) mx = fmaxf(mx, fabsf(x[j]));
         for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
         if (lane == 0) {
-            int E = 0;
-            if (mx > 0.f && isfinite(mx)) E = ilogbf(mx) + 1;
+            int E = scale_exp(mx);
             const int lg = 32 - __clz(g.nph - 1);          // ceil(log2 n)
             E += max(0, lg - 10);
             E = max(-90, min(E, 100));
@@ -170,8 +149,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
     const float *x = maps + b * npix + (hemi ? g.start_s : g.start_n);
     const int E = rok ? erow[((int64_t)hemi * nrn + ring) * nmaps + b] : 0;
     float C[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) C[k] = 1.5f * pow2f(E + 17 - 7 * k);
+    slice_consts(E, C);
 
     // B row ti: column c = ti -> m = 64 u + c/2, part c&1 (0: cos, 1: -sin)
     const int m = 64 * u + (ti >> 1);

@@ -116,6 +116,7 @@ struct Plan {
     DevBuf<double> maps;            // [nmaps_alloc * npix]
     DevBuf<double> fbuf, gbuf, rbuf;// ring Fourier buffers [2][lmax+1][nrn][2*nmaps]
     DevBuf<double> alm;             // [lmsize][2*nmaps]
+    DevBuf<double> almdf;           // double-float copy of alm (float2), mixed precision
     DevBuf<double> scratch;         // galaxy/window/output staging
     DevBuf<double> scratch2;
     DevBuf<double> dep;             // sorted-deposit workspace
@@ -171,11 +172,12 @@ void launch_ring_analysis_tc(const Plan &p, const float *maps, int64_t nmaps, fl
 uint2 dft_slices(double v, int EB);
 // tensor-core (tcgen05) Legendre analysis, mixed precision
 int64_t tc_table_offsets(const Plan &p, std::vector<int64_t> &off);
-void launch_build_lamtc(const Plan &p, cudaStream_t st);
-void launch_leg_analysis_tc(const Plan &p, const float *F, int64_t ncol, double *A, bool accumulate, cudaStream_t st);
+void launch_build_lamtc(const Plan &p, const int *Ea, const int *Es, cudaStream_t st);
+void launch_leg_analysis_tc(const Plan &p, const float *F, int64_t ncol, double *A, float2 *Adf, bool accumulate,
+                            cudaStream_t st);
 int64_t tc_synth_table_offsets(const Plan &p, std::vector<int64_t> &off);
-void launch_build_lamts(const Plan &p, cudaStream_t st);
-void launch_leg_synthesis_tc(const Plan &p, const double *A, int64_t ncol, float *G, cudaStream_t st);
+void launch_build_lamts(const Plan &p, const int *Es, cudaStream_t st);
+void launch_leg_synthesis_tc(const Plan &p, const float2 *Adf, int64_t ncol, float *G, cudaStream_t st);
 void launch_transpose(const double *in, int64_t rows, int64_t cols, double *out, cudaStream_t st);
 void launch_check_finite(const double *x, int64_t n, int *err, cudaStream_t st);
 void launch_ang2pix(int64_t nside, const double *theta, const double *phi, int64_t n, int64_t *pix,

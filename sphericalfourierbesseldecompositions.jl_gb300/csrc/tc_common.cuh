@@ -87,5 +87,68 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// ---- error-free slicing (block floating point, Ozaki et al.) -----------------
+// A value with |x| < 2^E is written as four slices s_k, each a multiple of
+// 2^(E - 6 - 7k) with at most 7 significant bits: s_k = RN(r_k) on that grid,
+// r_0 = x, r_{k+1} = r_k - s_k, formed as (r + C_k) - C_k with
+// C_k = 1.5 * 2^(E + 17 - 7k).  Every step is exact in FP32.
+
+__device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + e) << 23); }   // -126 <= e <= 127
+
+__device__ __forceinline__ void slice_consts(int E, float (&C)[4]) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) C[k] = 1.5f * pow2f(E + 17 - 7 * k);
+}
+
+__device__ __forceinline__ uint32_t bf16x2(float lo, float hi) {
+    uint32_t r;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+    return r;
+}
+
+// slices of the pair (x0, x1) packed as bf16x2 words w[k] (x0 in the low half)
+__device__ __forceinline__ void slice_pair(float x0, float x1, const float (&C)[4], uint32_t (&w)[4]) {
+    float r0 = x0, r1 = x1;
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+        const float a0 = __fsub_rn(__fadd_rn(r0, C[s]), C[s]);
+        const float a1 = __fsub_rn(__fadd_rn(r1, C[s]), C[s]);
+        w[s] = bf16x2(a0, a1);
+        r0 = __fsub_rn(r0, a0);
+        r1 = __fsub_rn(r1, a1);
+    }
+}
+
+// Double-float source (x = hi + lo, |lo| <= ulp(hi)/2): the first slice comes
+// from hi, the remainder (hi - s_0) + lo rounds below the last slice unit.
+__device__ __forceinline__ void slice_pair_df(float h0, float l0, float h1, float l1, const float (&C)[4],
+                                              uint32_t (&w)[4]) {
+    const float a0 = __fsub_rn(__fadd_rn(h0, C[0]), C[0]);
+    const float a1 = __fsub_rn(__fadd_rn(h1, C[0]), C[0]);
+    w[0] = bf16x2(a0, a1);
+    float r0 = __fadd_rn(__fsub_rn(h0, a0), l0), r1 = __fadd_rn(__fsub_rn(h1, a1), l1);
+#pragma unroll
+    for (int s = 1; s < 4; ++s) {
+        const float b0 = __fsub_rn(__fadd_rn(r0, C[s]), C[s]);
+        const float b1 = __fsub_rn(__fadd_rn(r1, C[s]), C[s]);
+        w[s] = bf16x2(b0, b1);
+        r0 = __fsub_rn(r0, b0);
+        r1 = __fsub_rn(r1, b1);
+    }
+}
+
+// exponent E with |v| < 2^E for the largest magnitude v (0 for zero / non-finite)
+__device__ __forceinline__ int scale_exp(float mx) {
+    int E = 0;
+    if (mx > 0.f && isfinite(mx)) E = ilogbf(mx) + 1;
+    return E;
+}
+
+// products (s_a, s_b) of slice levels 0..3: level 0 = [0], 1 = [1, 3), 2 = [3, 6), 3 = [6, 10)
+__device__ __forceinline__ int lvl_a(int p) { return p == 0 ? 0 : p < 3 ? p - 1 : p < 6 ? p - 3 : p - 6; }
+__device__ __forceinline__ int lvl_b(int p) { return p == 0 ? 0 : p < 3 ? 2 - p : p < 6 ? 5 - p : 9 - p; }
+__device__ __forceinline__ int lvl_of(int p) { return p == 0 ? 0 : p < 3 ? 1 : p < 6 ? 2 : 3; }
+__device__ __forceinline__ bool lvl_first(int p) { return p == 0 || p == 1 || p == 3 || p == 6; }
+
 }  // namespace tc
 }  // namespace sfb
