@@ -242,13 +242,15 @@ __device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
     return {h, e - (h - p)};
 }
 
-// Mixed precision: moments with the Legendre recurrence and the sums in
-// double-float; the fluctuation acc - mu_b ref is formed in FP64 and stored
-// as FP32.
+__device__ __forceinline__ dfl df_neg(dfl a) { return {-a.hi, -a.lo}; }
+
+// Mixed precision: moments with the Legendre recurrence, the sums and the
+// fluctuation acc - mu_b ref all in double-float (mudf = mu as hi + lo),
+// stored as FP32.
 template <int MAXDEG>
 __global__ void k_deposit_moments_df(const int32_t *__restrict__ offset, const double2 *__restrict__ sorted,
                                      int64_t npix, int pieces, int deg, int64_t nbasis, const double *__restrict__ ref,
-                                     const double *__restrict__ mu, float *__restrict__ maps) {
+                                     const float2 *__restrict__ mudf, float *__restrict__ maps) {
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t nkeys = (int64_t)(pieces + 2) * npix;
     if (idx >= nkeys) return;
@@ -256,14 +258,19 @@ __global__ void k_deposit_moments_df(const int32_t *__restrict__ offset, const d
     const int64_t pix = idx - (int64_t)slot * npix;
     const int64_t g0 = offset[idx];
     const int64_t g1 = offset[idx + 1];
-    const double rv = ref ? ref[pix] : 0.0;
+    const dfl rv = df_of(ref ? ref[pix] : 0.0);
+    auto fluct = [&](dfl a, int64_t b) -> float {
+        if (ref) {
+            const float2 m = mudf[b];
+            a = df_add(a, df_neg(df_mul({m.x, m.y}, rv)));
+        }
+        return a.hi + a.lo;
+    };
     if (slot >= pieces) {
         dfl s = {0.f, 0.f};
         for (int64_t g = g0; g < g1; ++g) s = df_add(s, df_of(sorted[g].y));
         const int64_t b = nbasis - 2 + (slot - pieces);
-        double v = (double)s.hi + (double)s.lo;
-        if (ref) v -= mu[b] * rv;
-        maps[b * npix + pix] = (float)v;
+        maps[b * npix + pix] = fluct(s, b);
         return;
     }
     dfl acc[MAXDEG + 1];
@@ -290,13 +297,8 @@ __global__ void k_deposit_moments_df(const int32_t *__restrict__ offset, const d
     const int64_t b0 = (int64_t)slot * (deg + 1);
     float *base = maps + b0 * npix + pix;
 #pragma unroll
-    for (int k = 0; k <= MAXDEG; ++k) {
-        if (k <= deg) {
-            double v = (double)acc[k].hi + (double)acc[k].lo;
-            if (ref) v -= mu[b0 + k] * rv;
-            base[(int64_t)k * npix] = (float)v;
-        }
-    }
+    for (int k = 0; k <= MAXDEG; ++k)
+        if (k <= deg) base[(int64_t)k * npix] = fluct(acc[k], b0 + k);
 }
 
 constexpr int STATS_STRIDE = 32;
@@ -349,13 +351,18 @@ __global__ void __launch_bounds__(32) k_deposit_stats(const int32_t *__restrict_
     }
 }
 
-// mu[b] = S[b] / Q[slot(b)] (0 where the sampled reference map is zero).
-__global__ void k_mean_finalize(const double *S, const double *Q, int pieces, int deg, int64_t nbasis, double *mu) {
+// mu[b] = S[b] / Q[slot(b)] (0 where the sampled reference map is zero), and
+// the same as a double-float pair in mudf.
+__global__ void k_mean_finalize(const double *S, const double *Q, int pieces, int deg, int64_t nbasis, double *mu,
+                                float2 *mudf) {
     const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= nbasis) return;
     const int64_t npoly = (int64_t)pieces * (deg + 1);
     const int slot = b < npoly ? (int)(b / (deg + 1)) : pieces + (int)(b - npoly);
-    mu[b] = Q[slot] > 0.0 ? S[b] / Q[slot] : 0.0;
+    const double v = Q[slot] > 0.0 ? S[b] / Q[slot] : 0.0;
+    mu[b] = v;
+    const float h = (float)v;
+    mudf[b] = make_float2(h, (float)(v - (double)h));
 }
 
 // Weighted galaxy count per pixel over all radial slots (FP64).
@@ -373,12 +380,12 @@ __global__ void k_weight_map(const int32_t *__restrict__ offset, const double2 *
 
 template <int MAXDEG>
 static void launch_moments(const Plan &p, const int32_t *counts, const double2 *sorted, const double *ref,
-                           const double *mu, double *maps, cudaStream_t st) {
+                           const double *mu, const float2 *mudf, double *maps, cudaStream_t st) {
     const int64_t nkeys = (int64_t)(p.pieces + 2) * p.npix;
     const unsigned blocks = (unsigned)((nkeys + 127) / 128);
     if (p.precision == SFB_MIXED)
         k_deposit_moments_df<MAXDEG><<<blocks, 128, 0, st>>>(counts, sorted, p.npix, p.pieces, p.degree, p.nbasis,
-                                                             ref, mu, reinterpret_cast<float *>(maps));
+                                                             ref, mudf, reinterpret_cast<float *>(maps));
     else
         k_deposit_moments<MAXDEG, double><<<blocks, 128, 0, st>>>(counts, sorted, p.npix, p.pieces, p.degree,
                                                                   p.nbasis, ref, mu, maps);
@@ -396,7 +403,7 @@ static void launch_stats(const Plan &p, const int32_t *counts, const double2 *so
 }
 
 int deposit_sorted(Plan &p, const double *rtp, const double *w, int64_t ngal, double *maps, double *ref,
-                   double *mu, cudaStream_t st) {
+                   double *mu, cudaEvent_t ref_ready, cudaStream_t st) {
     const int64_t nkeys = (int64_t)(p.pieces + 2) * p.npix;
     const int64_t nscan = nkeys + 1;            // one extra counter: its exclusive prefix is the total
     const int64_t ntiles = (nscan + SCAN_TILE - 1) / SCAN_TILE;
@@ -406,8 +413,8 @@ int deposit_sorted(Plan &p, const double *rtp, const double *w, int64_t ngal, do
     const int64_t off_x = (ints + 1) / 2;
     int64_t off_sorted = off_x + ngal;
     off_sorted += off_sorted & 1;
-    const int64_t off_stats = off_sorted + 2 * ngal + 2;       // S [nbasis], Q [pieces + 2]
-    SFB_TRY(grow(p, p.dep, (size_t)(off_stats + p.nbasis + p.pieces + 2)));
+    const int64_t off_stats = off_sorted + 2 * ngal + 2;       // S [nbasis], Q [pieces + 2], mudf [nbasis]
+    SFB_TRY(grow(p, p.dep, (size_t)(off_stats + 2 * p.nbasis + p.pieces + 2)));
     int32_t *counts = reinterpret_cast<int32_t *>(p.dep.ptr);
     int32_t *tsum = counts + nscan;
     int32_t *key = tsum + ntiles;
@@ -432,23 +439,26 @@ int deposit_sorted(Plan &p, const double *rtp, const double *w, int64_t ngal, do
     }
     if (p.degree > 63) return fail(SFB_ENOTSUP, "radial degree above 63 is not supported by the sorted deposit");
     const bool split = ref != nullptr && p.precision == SFB_MIXED;
+    float2 *mudf = reinterpret_cast<float2 *>(p.dep.ptr + off_stats + p.nbasis + p.pieces + 2);
     if (split) {
         k_weight_map<<<(unsigned)((p.npix + 255) / 256), 256, 0, st>>>(counts, sorted, p.npix, p.pieces + 2, ref);
         note_launch();
+        if (ref_ready) SFB_CUDA_TRY(cudaEventRecord(ref_ready, st));
         double *S = p.dep.ptr + off_stats;
         double *Q = S + p.nbasis;
         SFB_CUDA_TRY(cudaMemsetAsync(S, 0, (size_t)(p.nbasis + p.pieces + 2) * sizeof(double), st));
         if (p.degree <= 15) launch_stats<15>(p, counts, sorted, ref, S, Q, st);
         else if (p.degree <= 31) launch_stats<31>(p, counts, sorted, ref, S, Q, st);
         else launch_stats<63>(p, counts, sorted, ref, S, Q, st);
-        k_mean_finalize<<<(unsigned)((p.nbasis + 127) / 128), 128, 0, st>>>(S, Q, p.pieces, p.degree, p.nbasis, mu);
+        k_mean_finalize<<<(unsigned)((p.nbasis + 127) / 128), 128, 0, st>>>(S, Q, p.pieces, p.degree, p.nbasis, mu,
+                                                                           mudf);
         note_launch();
     }
-    // moments in FP64; the maps are stored in the transform's precision
+    // moments in FP64 (FP64 path) or double-float (mixed); stored in the transform's precision
     const double *r = split ? ref : nullptr;
-    if (p.degree <= 15) launch_moments<15>(p, counts, sorted, r, mu, maps, st);
-    else if (p.degree <= 31) launch_moments<31>(p, counts, sorted, r, mu, maps, st);
-    else launch_moments<63>(p, counts, sorted, r, mu, maps, st);
+    if (p.degree <= 15) launch_moments<15>(p, counts, sorted, r, mu, mudf, maps, st);
+    else if (p.degree <= 31) launch_moments<31>(p, counts, sorted, r, mu, mudf, maps, st);
+    else launch_moments<63>(p, counts, sorted, r, mu, mudf, maps, st);
     SFB_CUDA_TRY(cudaGetLastError());
     return SFB_OK;
 }

@@ -25,8 +25,11 @@
 // The F (analysis) and A (synthesis) tiles are sliced by the CTA's threads
 // into four K-major BF16 planes in shared memory; the lambda planes come
 // pre-sliced from the plan's tables by bulk copy (cp.async.bulk, TMA engine).
-// Three shared-memory stages: the next chunk's lambda planes and operand
-// values are fetched while the tensor cores work on the current one.  The
+// Two shared-memory stages and N <= 64 per CTA (256 TMEM columns), so two
+// CTAs share an SM: the next chunk's lambda planes and operand values are
+// fetched while the tensor cores work on the current one, and the other
+// CTA covers the latencies.  The per-column scales of F come from a
+// separate bandwidth-bound pass (k_colmax).  The
 // analysis keeps a double-float copy of A (float2) beside the FP64 one, which
 // the synthesis slices without FP64 arithmetic.
 //
@@ -51,12 +54,14 @@ namespace tc {
 
 constexpr int KC = 32;          // K elements per chunk
 constexpr int MTILE = 128;      // columns per CTA (MMA M)
+constexpr int NMAX = 64;        // MMA N per CTA: lambda rows (analysis) or rings (synthesis)
 constexpr int NTH = 256;        // threads: two per operand row
-constexpr int NSTAGE = 3;
+constexpr int NSTAGE = 2;
 constexpr uint32_t PLANE_A = MTILE * KC * 2;          // bytes of one operand-A plane
-constexpr uint32_t PLANE_B = 128 * KC * 2;            // bytes of one lambda plane (<= 128 rows)
+constexpr uint32_t PLANE_B = NMAX * KC * 2;           // bytes of one lambda plane (<= NMAX rows)
 constexpr uint32_t STAGE_BYTES = 4 * PLANE_A + 4 * PLANE_B;
-constexpr size_t LEG_SMEM = NSTAGE * (size_t)STAGE_BYTES + 64 + 128 * sizeof(float);
+constexpr uint32_t TMEM_COLS = 4 * NMAX;             // four level accumulators
+constexpr size_t LEG_SMEM = NSTAGE * (size_t)STAGE_BYTES + 64;   // two CTAs per SM
 
 // byte offset of element (row, k) in a K-major no-swizzle plane with KC columns
 __device__ __forceinline__ uint32_t core_off(int row, int k) {
@@ -79,7 +84,6 @@ struct LvlSmem {
     unsigned char *base;
     uint64_t *bb, *bm;
     uint32_t *slot;
-    float *red;               // 128 floats: column maxima of the second thread half
     __device__ __forceinline__ unsigned char *stage(int s) const { return base + s * STAGE_BYTES; }
 };
 
@@ -89,14 +93,13 @@ __device__ __forceinline__ LvlSmem lvl_smem(unsigned char *base) {
     c.bb = reinterpret_cast<uint64_t *>(base + NSTAGE * STAGE_BYTES);
     c.bm = c.bb + NSTAGE;
     c.slot = reinterpret_cast<uint32_t *>(c.bm + NSTAGE);
-    c.red = reinterpret_cast<float *>(base + NSTAGE * STAGE_BYTES + 64);
     return c;
 }
 
 __device__ __forceinline__ uint32_t lvl_setup(LvlSmem &c) {
     if ((threadIdx.x >> 5) == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(c.slot)),
-                     "r"(512)
+                     "r"(TMEM_COLS)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -117,11 +120,11 @@ __device__ __forceinline__ void lvl_teardown(uint32_t tmem) {
     fence_before();
     __syncthreads();
     if ((threadIdx.x >> 5) == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
 }
 
 // The ten level products of one K chunk (two K steps of 16): level v goes to
-// TMEM columns [128 v, 128 v + N).
+// TMEM columns [NMAX v, NMAX v + N).
 __device__ __forceinline__ void lvl_mma(uint32_t tmem, uint32_t a0, uint32_t b0, uint32_t planeB, uint32_t idesc,
                                         bool first_chunk) {
     const uint32_t sbo = (KC / 8) * 128;
@@ -132,7 +135,7 @@ __device__ __forceinline__ void lvl_mma(uint32_t tmem, uint32_t a0, uint32_t b0,
             const uint64_t ad = smem_desc(a0 + lvl_a(p) * PLANE_A + s * 256, 128, sbo);
             const uint64_t bd = smem_desc(b0 + lvl_b(p) * planeB + s * 256, 128, sbo);
             const uint32_t acc = (first_chunk && s == 0 && lvl_first(p)) ? 0u : 1u;
-            mma_bf16(tmem + 128u * (uint32_t)lvl_of(p), ad, bd, idesc, acc);
+            mma_bf16(tmem + (uint32_t)NMAX * (uint32_t)lvl_of(p), ad, bd, idesc, acc);
         }
     }
 }
@@ -148,24 +151,48 @@ __device__ __forceinline__ void lvl_sum(float L0, float L1, float L2, float L3, 
     lo = t - (hi - s);
 }
 
-// Chunk pipeline shared by both kernels: NSTAGE stages; stage of chunk kc is
-// kc % NSTAGE; bb / bm phases advance once per use of the stage.
+// Chunk pipeline shared by both kernels: stage of chunk kc is kc % NSTAGE;
+// bb / bm phases advance once per use of the stage.  In iteration kc the CTA
+// slices chunk kc into its stage, issues its MMAs, then waits for the MMAs
+// of chunk kc - 1 and starts the lambda copy and operand loads of kc + 1.
 __device__ __forceinline__ uint32_t ph_of(int kc) { return (uint32_t)((kc / NSTAGE) & 1); }
 
-// Analysis: grid (column tiles, row tiles of 128, blocks z).
-__global__ void __launch_bounds__(NTH, 1) k_leg_analysis_tc(const __nv_bfloat16 *__restrict__ lamtc,
+// Per (block z, column c): E with max_r |F[parity][m][r][c]| < 2^E, raised by
+// ceil(log2 nrn) - 9 for more than 512 rings (level sums below 2^24 units).
+__global__ void __launch_bounds__(256) k_colmax(const float *__restrict__ F, int64_t ncol, int lmax, int nrn,
+                                                int *__restrict__ Ecol) {
+    const int z = blockIdx.y;
+    const int m = z >> 1, par = z & 1;
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncol) return;
+    const float *Fz = F + ((int64_t)(par * (lmax + 1) + m) * nrn) * ncol + c;
+    float m0 = 0.f, m1 = 0.f, m2 = 0.f, m3 = 0.f;
+    int r = 0;
+    for (; r + 3 < nrn; r += 4) {
+        m0 = fmaxf(m0, fabsf(Fz[(int64_t)r * ncol]));
+        m1 = fmaxf(m1, fabsf(Fz[(int64_t)(r + 1) * ncol]));
+        m2 = fmaxf(m2, fabsf(Fz[(int64_t)(r + 2) * ncol]));
+        m3 = fmaxf(m3, fabsf(Fz[(int64_t)(r + 3) * ncol]));
+    }
+    for (; r < nrn; ++r) m0 = fmaxf(m0, fabsf(Fz[(int64_t)r * ncol]));
+    const int lg = 32 - __clz(nrn > 1 ? nrn - 1 : 1);
+    Ecol[(int64_t)z * ncol + c] = max(-90, min(scale_exp(fmaxf(fmaxf(m0, m1), fmaxf(m2, m3))) + max(0, lg - 9), 100));
+}
+
+// Analysis: grid (column tiles, row tiles of NMAX, blocks z).
+__global__ void __launch_bounds__(NTH, 2) k_leg_analysis_tc(const __nv_bfloat16 *__restrict__ lamtc,
                                                             const int64_t *__restrict__ lamtc_off, int lmax, int nrn,
                                                             int nchunks, const float *__restrict__ F, int64_t ncol,
-                                                            double *__restrict__ A, float2 *__restrict__ Adf,
-                                                            int accumulate, int *err) {
+                                                            const int *__restrict__ Ecol, double *__restrict__ A,
+                                                            float2 *__restrict__ Adf, int accumulate, int *err) {
     extern __shared__ __align__(1024) unsigned char smem[];
     const int z = blockIdx.z;
     const int m = z >> 1, par = z & 1;
     const int nrows = rows_of(m, par, lmax);
     const int NP = pad16(nrows);
-    const int row0 = blockIdx.y * 128;
+    const int row0 = blockIdx.y * NMAX;
     if (row0 >= NP) return;
-    const int NPc = min(128, NP - row0);
+    const int NPc = min(NMAX, NP - row0);
     const int64_t col0 = (int64_t)blockIdx.x * MTILE;
     const int tid = threadIdx.x, warp = tid >> 5;
     const int c = tid & (MTILE - 1), kh = tid >> 7;      // column, ring half of each chunk
@@ -174,25 +201,15 @@ __global__ void __launch_bounds__(NTH, 1) k_leg_analysis_tc(const __nv_bfloat16 
     const __nv_bfloat16 *Lz = lamtc + lamtc_off[z];
     const uint32_t planeB = (uint32_t)NPc * KC * 2;
     LvlSmem cs = lvl_smem(smem);
-
-    // column scale: max |F| over all rings (both thread halves), exponent E
-    float mx = 0.f;
-    if (cok)
-        for (int r = kh; r < nrn; r += 2) mx = fmaxf(mx, fabsf(Fz[(int64_t)r * ncol]));
-    if (kh) cs.red[c] = mx;
-    const uint32_t tmem = lvl_setup(cs);      // includes a __syncthreads
-    if (!kh) cs.red[c] = fmaxf(mx, cs.red[c]);
-    __syncthreads();
     float C[4];
-    slice_consts(scale_exp(cs.red[c]), C);
-    const uint32_t idesc = idesc_bf16(MTILE, NPc);
+    slice_consts(cok ? Ecol[(int64_t)z * ncol + col0 + c] : 0, C);
 
-    float pre[16];
-    auto loadA = [&](int kc) {
+    float pre[2][16];          // operand values of chunks kc (buffer kc & 1) and kc + 1
+    auto loadA = [&](int kc, float (&buf)[16]) {
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
             const int r = kc * KC + 16 * kh + j;
-            pre[j] = (cok && r < nrn) ? Fz[(int64_t)r * ncol] : 0.f;
+            buf[j] = (cok && r < nrn) ? Fz[(int64_t)r * ncol] : 0.f;
         }
     };
     auto issueB = [&](int kc) {
@@ -203,21 +220,16 @@ __global__ void __launch_bounds__(NTH, 1) k_leg_analysis_tc(const __nv_bfloat16 
             bulk_g2s(cs.stage(s) + 4 * PLANE_A + pl * planeB,
                      Lz + kc * chunk_elems + (int64_t)pl * NP * KC + (int64_t)row0 * KC, planeB, &cs.bb[s]);
     };
+    loadA(0, pre[0]);
+    if (nchunks > 1) loadA(1, pre[1]);
+    const uint32_t tmem = lvl_setup(cs);
+    if (tid == 0) issueB(0);
+    const uint32_t idesc = idesc_bf16(MTILE, NPc);
     bool ok = true;
     int issued = 0;
-    if (tid == 0) issueB(0);
-    loadA(0);
-    for (int kc = 0; kc < nchunks; ++kc) {
+    // one chunk: slice, prefetch kc + 2 into the freed buffer, MMAs, start the lambda copy of kc + 1
+    auto chunk = [&](int kc, float (&cur)[16]) -> bool {
         const int s = kc % NSTAGE;
-        // the stage of chunk kc + 1 was last used by chunk kc + 1 - NSTAGE
-        if (kc + 1 < nchunks) {
-            if (kc + 1 >= NSTAGE && !mbar_wait(&cs.bm[(kc + 1) % NSTAGE], ph_of(kc + 1 - NSTAGE))) ok = false;
-            if (ok && tid == 0) {
-                fence_after();
-                issueB(kc + 1);
-            }
-        }
-        // slices of this thread's 16 ring values of column c
         unsigned char *sa = cs.stage(s);
 #pragma unroll
         for (int g = 0; g < 2; ++g) {
@@ -225,7 +237,7 @@ __global__ void __launch_bounds__(NTH, 1) k_leg_analysis_tc(const __nv_bfloat16 
 #pragma unroll
             for (int t = 0; t < 4; ++t) {
                 uint32_t v[4];
-                slice_pair(pre[8 * g + 2 * t], pre[8 * g + 2 * t + 1], C, v);
+                slice_pair(cur[8 * g + 2 * t], cur[8 * g + 2 * t + 1], C, v);
 #pragma unroll
                 for (int q = 0; q < 4; ++q) w[q][t] = v[q];
             }
@@ -233,9 +245,9 @@ __global__ void __launch_bounds__(NTH, 1) k_leg_analysis_tc(const __nv_bfloat16 
 #pragma unroll
             for (int q = 0; q < 4; ++q) st_v4(sa + q * PLANE_A + off, w[q]);
         }
+        if (kc + 2 < nchunks) loadA(kc + 2, cur);
         fence_proxy_async();
-        ok = __syncthreads_and(ok);
-        if (!ok) break;
+        __syncthreads();
         if (tid == 0) {
             if (!mbar_wait(&cs.bb[s], ph_of(kc))) {
                 ok = false;
@@ -246,9 +258,18 @@ __global__ void __launch_bounds__(NTH, 1) k_leg_analysis_tc(const __nv_bfloat16 
                 ++issued;
             }
         }
-        if (kc + 1 < nchunks) loadA(kc + 1);
+        if (kc + 1 < nchunks) {
+            // the stage of chunk kc + 1 held chunk kc - 1: wait for its MMAs
+            if (kc >= 1 && !mbar_wait(&cs.bm[(kc + 1) % NSTAGE], ph_of(kc - 1))) ok = false;
+            fence_after();
+            if (ok && tid == 0) issueB(kc + 1);
+        }
         ok = __syncthreads_and(ok);
-        if (!ok) break;
+        return ok;
+    };
+    for (int kc = 0; kc < nchunks; kc += 2) {
+        if (!chunk(kc, pre[0])) break;
+        if (kc + 1 < nchunks && !chunk(kc + 1, pre[1])) break;
     }
     __shared__ int s_issued;                              // thread 0's count of committed chunks
     if (tid == 0) s_issued = issued;
@@ -260,18 +281,18 @@ __global__ void __launch_bounds__(NTH, 1) k_leg_analysis_tc(const __nv_bfloat16 
     if (!ok || issued != nchunks) {
         if (tid == 0) atomicOr(err, ERR_TC_TIMEOUT);
     } else {
-        // warp w reads TMEM lanes 32 (w % 4).. (columns) and rows li in [64 (w / 4), +64)
+        // warp w reads TMEM lanes 32 (w % 4).. (columns) and rows li in [32 (w / 4), +32)
         const int lq = warp & 3, hg = warp >> 2;
         const uint32_t lane_base = (uint32_t)(lq * 32) << 16;
         const int64_t cc = col0 + lq * 32 + (tid & 31);
-        for (int g = 0; g < 4; ++g) {
-            const int i0 = 64 * hg + 16 * g;
+        for (int g = 0; g < 2; ++g) {
+            const int i0 = 32 * hg + 16 * g;
             if (i0 >= NPc) break;                           // warp-uniform
             float v0[16], v1[16], v2[16], v3[16];
             tmem_ld16(tmem + lane_base + (uint32_t)i0, v0);
-            tmem_ld16(tmem + lane_base + 128u + (uint32_t)i0, v1);
-            tmem_ld16(tmem + lane_base + 256u + (uint32_t)i0, v2);
-            tmem_ld16(tmem + lane_base + 384u + (uint32_t)i0, v3);
+            tmem_ld16(tmem + lane_base + (uint32_t)(NMAX + i0), v1);
+            tmem_ld16(tmem + lane_base + (uint32_t)(2 * NMAX + i0), v2);
+            tmem_ld16(tmem + lane_base + (uint32_t)(3 * NMAX + i0), v3);
             if (cc < ncol) {
 #pragma unroll
                 for (int i = 0; i < 16; ++i) {
@@ -301,12 +322,14 @@ __global__ void __launch_bounds__(NTH, 1) k_leg_analysis_tc(const __nv_bfloat16 
     lvl_teardown(tmem);
 }
 
-// Synthesis: grid (column tiles, ring tiles of NT, blocks z).
-__global__ void __launch_bounds__(NTH, 1) k_leg_synthesis_tc(const __nv_bfloat16 *__restrict__ lamts,
+// Synthesis: grid (column tiles, ring tiles of NT <= NMAX, blocks z).
+__global__ void __launch_bounds__(NTH, 2) k_leg_synthesis_tc(const __nv_bfloat16 *__restrict__ lamts,
                                                              const int64_t *__restrict__ lamts_off, int lmax, int nrn,
                                                              int NT, const float2 *__restrict__ Adf, int64_t ncol,
                                                              float *__restrict__ G, int *err) {
     extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ float red[2][MTILE];
+    __shared__ int s_issued;
     const int z = blockIdx.z;
     const int m = z >> 1, par = z & 1;
     const int nrows = rows_of(m, par, lmax);
@@ -334,21 +357,19 @@ __global__ void __launch_bounds__(NTH, 1) k_leg_synthesis_tc(const __nv_bfloat16
         const int l = m + par + 2 * li;
         return Adf[((int64_t)l * (l + 1) / 2 + m) * ncol + col0 + c];
     };
+    // column scale over the rows (|hi + lo| < 2^E: hi is an FP32 value below 2^E, |lo| <= ulp(hi)/2)
     float mx = 0.f;
     for (int li = kh; li < nrows; li += 2) mx = fmaxf(mx, fabsf(aval(li).x));
-    if (kh) cs.red[c] = mx;
-    const uint32_t tmem = lvl_setup(cs);
-    if (!kh) cs.red[c] = fmaxf(mx, cs.red[c]);
-    __syncthreads();
-    // |hi + lo| < 2^E as well: hi is an FP32 value below 2^E and |lo| <= ulp(hi)/2
+    red[kh][c] = mx;
+    const uint32_t tmem = lvl_setup(cs);      // includes a __syncthreads
     float C[4];
-    slice_consts(scale_exp(cs.red[c]), C);
+    slice_consts(scale_exp(fmaxf(red[0][c], red[1][c])), C);
     const uint32_t idesc = idesc_bf16(MTILE, NT);
 
-    float2 pre[16];
-    auto loadA = [&](int kc) {
+    float2 pre[2][16];
+    auto loadA = [&](int kc, float2 (&buf)[16]) {
 #pragma unroll
-        for (int j = 0; j < 16; ++j) pre[j] = aval(kc * KC + 16 * kh + j);
+        for (int j = 0; j < 16; ++j) buf[j] = aval(kc * KC + 16 * kh + j);
     };
     auto issueB = [&](int kc) {
         const int s = kc % NSTAGE;
@@ -358,16 +379,10 @@ __global__ void __launch_bounds__(NTH, 1) k_leg_synthesis_tc(const __nv_bfloat16
     bool ok = true;
     int issued = 0;
     if (tid == 0) issueB(0);
-    loadA(0);
-    for (int kc = 0; kc < nK; ++kc) {
+    loadA(0, pre[0]);
+    if (nK > 1) loadA(1, pre[1]);
+    auto chunk = [&](int kc, float2 (&cur)[16]) -> bool {
         const int s = kc % NSTAGE;
-        if (kc + 1 < nK) {
-            if (kc + 1 >= NSTAGE && !mbar_wait(&cs.bm[(kc + 1) % NSTAGE], ph_of(kc + 1 - NSTAGE))) ok = false;
-            if (ok && tid == 0) {
-                fence_after();
-                issueB(kc + 1);
-            }
-        }
         unsigned char *sa = cs.stage(s);
 #pragma unroll
         for (int g = 0; g < 2; ++g) {
@@ -375,7 +390,7 @@ __global__ void __launch_bounds__(NTH, 1) k_leg_synthesis_tc(const __nv_bfloat16
 #pragma unroll
             for (int t = 0; t < 4; ++t) {
                 uint32_t v[4];
-                const float2 x0 = pre[8 * g + 2 * t], x1 = pre[8 * g + 2 * t + 1];
+                const float2 x0 = cur[8 * g + 2 * t], x1 = cur[8 * g + 2 * t + 1];
                 slice_pair_df(x0.x, x0.y, x1.x, x1.y, C, v);
 #pragma unroll
                 for (int q = 0; q < 4; ++q) w[q][t] = v[q];
@@ -384,9 +399,9 @@ __global__ void __launch_bounds__(NTH, 1) k_leg_synthesis_tc(const __nv_bfloat16
 #pragma unroll
             for (int q = 0; q < 4; ++q) st_v4(sa + q * PLANE_A + off, w[q]);
         }
+        if (kc + 2 < nK) loadA(kc + 2, cur);
         fence_proxy_async();
-        ok = __syncthreads_and(ok);
-        if (!ok) break;
+        __syncthreads();
         if (tid == 0) {
             if (!mbar_wait(&cs.bb[s], ph_of(kc))) {
                 ok = false;
@@ -397,11 +412,18 @@ __global__ void __launch_bounds__(NTH, 1) k_leg_synthesis_tc(const __nv_bfloat16
                 ++issued;
             }
         }
-        if (kc + 1 < nK) loadA(kc + 1);
+        if (kc + 1 < nK) {
+            if (kc >= 1 && !mbar_wait(&cs.bm[(kc + 1) % NSTAGE], ph_of(kc - 1))) ok = false;
+            fence_after();
+            if (ok && tid == 0) issueB(kc + 1);
+        }
         ok = __syncthreads_and(ok);
-        if (!ok) break;
+        return ok;
+    };
+    for (int kc = 0; kc < nK; kc += 2) {
+        if (!chunk(kc, pre[0])) break;
+        if (kc + 1 < nK && !chunk(kc + 1, pre[1])) break;
     }
-    __shared__ int s_issued;
     if (tid == 0) s_issued = issued;
     __syncthreads();
     issued = s_issued;
@@ -411,17 +433,18 @@ __global__ void __launch_bounds__(NTH, 1) k_leg_synthesis_tc(const __nv_bfloat16
     if (!ok || issued != nK) {
         if (tid == 0) atomicOr(err, ERR_TC_TIMEOUT);
     } else {
+        // warp w reads TMEM lanes 32 (w % 4).. (columns) and rings [32 (w / 4), +32) of the tile
         const int lq = warp & 3, hg = warp >> 2;
         const uint32_t lane_base = (uint32_t)(lq * 32) << 16;
         const int64_t cc = col0 + lq * 32 + lane;
-        for (int g = 0; g < 4; ++g) {
-            const int i0 = 64 * hg + 16 * g;
+        for (int g = 0; g < 2; ++g) {
+            const int i0 = 32 * hg + 16 * g;
             if (i0 >= NT) break;                            // warp-uniform
             float v0[16], v1[16], v2[16], v3[16];
             tmem_ld16(tmem + lane_base + (uint32_t)i0, v0);
-            tmem_ld16(tmem + lane_base + 128u + (uint32_t)i0, v1);
-            tmem_ld16(tmem + lane_base + 256u + (uint32_t)i0, v2);
-            tmem_ld16(tmem + lane_base + 384u + (uint32_t)i0, v3);
+            tmem_ld16(tmem + lane_base + (uint32_t)(NMAX + i0), v1);
+            tmem_ld16(tmem + lane_base + (uint32_t)(2 * NMAX + i0), v2);
+            tmem_ld16(tmem + lane_base + (uint32_t)(3 * NMAX + i0), v3);
             if (cc < ncol) {
 #pragma unroll
                 for (int i = 0; i < 16; ++i) {
@@ -587,13 +610,18 @@ void launch_build_lamtc(const Plan &p, const int *Ea, const int *Es, cudaStream_
     note_launch();
 }
 
-void launch_leg_analysis_tc(const Plan &p, const float *F, int64_t ncol, double *A, float2 *Adf, bool accumulate,
-                            cudaStream_t st) {
+void launch_leg_analysis_tc(const Plan &p, const float *F, int64_t ncol, double *A, float2 *Adf, int *Ecol,
+                            bool accumulate, cudaStream_t st) {
+    {
+        dim3 grid((unsigned)((ncol + 255) / 256), (unsigned)(2 * (p.lmax + 1)));
+        tc::k_colmax<<<grid, 256, 0, st>>>(F, ncol, p.lmax, (int)p.nrn, Ecol);
+        note_launch();
+    }
     set_smem(tc::k_leg_analysis_tc, tc::LEG_SMEM);
-    const int nhalf = (tc_np_max(p) + 127) / 128;
-    dim3 grid((unsigned)((ncol + tc::MTILE - 1) / tc::MTILE), (unsigned)nhalf, (unsigned)(2 * (p.lmax + 1)));
+    const int ntile = (tc_np_max(p) + tc::NMAX - 1) / tc::NMAX;
+    dim3 grid((unsigned)((ncol + tc::MTILE - 1) / tc::MTILE), (unsigned)ntile, (unsigned)(2 * (p.lmax + 1)));
     tc::k_leg_analysis_tc<<<grid, tc::NTH, tc::LEG_SMEM, st>>>((const __nv_bfloat16 *)p.d_lamtc, p.d_lamtc_off,
-                                                              p.lmax, (int)p.nrn, tc_chunks(p), F, ncol, A, Adf,
+                                                              p.lmax, (int)p.nrn, tc_chunks(p), F, ncol, Ecol, A, Adf,
                                                               accumulate ? 1 : 0, p.d_err);
     note_launch();
 }
@@ -605,7 +633,7 @@ namespace sfb {
 int tc_synth_nt(const Plan &p) {
     const int nrn = (int)p.nrn;
     const int nt16 = (nrn + 15) & ~15;
-    return nt16 < 128 ? nt16 : 128;
+    return nt16 < tc::NMAX ? nt16 : tc::NMAX;
 }
 
 int64_t tc_synth_table_offsets(const Plan &p, std::vector<int64_t> &off) {

@@ -90,6 +90,10 @@ void launch_amln2clnn(const double *a1, const double *a2, int64_t nlmsize, const
 struct sfb_plan {
     sfb::Plan p;
     cudaStream_t stream = nullptr;
+    // side stream for the FP64 reference-map transform of the mixed path,
+    // forked / joined with the call's stream through events
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int32_t *d_pair_index = nullptr;
     int64_t *d_noff = nullptr;
     // stage profiling (events on the call's stream)
@@ -314,7 +318,9 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, b
         SFB_TRY(grow(p, p.rbuf, fsz));
     }
     if (p.precision == SFB_MIXED) {
-        SFB_TRY(grow(p, p.erow, (size_t)(p.nrn * nm + 1)));
+        // row scales of the ring DFT, then column scales of the Legendre analysis (ints)
+        SFB_TRY(grow(p, p.erow, (size_t)std::max<int64_t>(p.nrn * nm, (p.lmax + 1) * ncol) + 1));
+        SFB_TRY(grow(p, p.almdf, (size_t)p.lmsize * ncol));
         Stage s(h, stage(SFB_STAGE_RING_FFT), st);
         launch_ring_analysis_tc(p, reinterpret_cast<const float *>(maps), nm, reinterpret_cast<float *>(p.fbuf.ptr),
                                 reinterpret_cast<int *>(p.erow.ptr), st);
@@ -323,11 +329,11 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, b
         launch_ring_analysis(p, maps, nm, p.fbuf.ptr, st);
     }
     const bool tc = p.precision == SFB_MIXED;
-    if (tc) SFB_TRY(grow(p, p.almdf, (size_t)p.lmsize * ncol));
     float2 *adf = reinterpret_cast<float2 *>(p.almdf.ptr);
+    int *ecol = reinterpret_cast<int *>(p.erow.ptr);          // column scales (the row scales are used up)
     auto analysis = [&](const double *src, bool acc) {
         Stage s(h, stage(SFB_STAGE_LEG_ANALYSIS), st);
-        if (tc) launch_leg_analysis_tc(p, (const float *)src, ncol, p.alm.ptr, adf, acc, st);
+        if (tc) launch_leg_analysis_tc(p, (const float *)src, ncol, p.alm.ptr, adf, ecol, acc, st);
         else launch_leg_analysis(p, src, ncol, p.alm.ptr, acc, st);
     };
     analysis(p.fbuf.ptr, false);
@@ -431,9 +437,15 @@ int cat2amln_dev(sfb_plan *h, const double *rtp, const double *w, int64_t ngal, 
         }
         {
             Stage s(h, SFB_STAGE_DEPOSIT, st);
-            SFB_TRY(deposit_sorted(p, rtp, w, ngal, p.maps.ptr, Cmap, mu, st));
+            SFB_TRY(deposit_sorted(p, rtp, w, ngal, p.maps.ptr, Cmap, mu, split ? h->ev_fork : nullptr, st));
         }
-        if (split) SFB_TRY(reference_alm(h, Cmap, 2, ralm, st));
+        if (split) {
+            // the FP64 transform of (C, W01) runs on the side stream while the deposit's moments finish
+            SFB_CUDA_TRY(cudaStreamWaitEvent(h->side, h->ev_fork, 0));
+            SFB_TRY(reference_alm(h, Cmap, 2, ralm, h->side));
+            SFB_CUDA_TRY(cudaEventRecord(h->ev_join, h->side));
+            SFB_CUDA_TRY(cudaStreamWaitEvent(st, h->ev_join, 0));
+        }
         SFB_TRY(sht_analysis(h, p.maps.ptr, nm, st));
         {
             Stage s(h, SFB_STAGE_PROJECT, st);
@@ -590,7 +602,10 @@ int sfb_plan_create(const sfb_plan_desc *d, sfb_plan **out) {
     }
     int st = SFB_OK;
     do {
-        if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess) {
             cudaGetLastError();
             st = fail(SFB_ECUDA, "stream creation failed");
             break;
@@ -762,6 +777,9 @@ void sfb_plan_destroy(sfb_plan *h) {
     collect_stages(h);
     for (cudaEvent_t e : h->pool) cudaEventDestroy(e);
     if (h->stream) cudaStreamDestroy(h->stream);
+    if (h->side) cudaStreamDestroy(h->side);
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
     delete h;
 }
 

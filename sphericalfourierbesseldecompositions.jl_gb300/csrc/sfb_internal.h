@@ -145,9 +145,10 @@ void launch_legendre_table(const Plan &p, cudaStream_t st);
 // galaxies -> radial-basis x pixel maps (counting sort + register moments); writes every map element
 // Sorted deposit of the catalogue into the basis maps.  With ref (mixed
 // precision only) the weighted count map C is written to ref[npix], the maps
-// hold D_b - mu_b C and mu[nbasis] receives mu_b.
+// hold D_b - mu_b C and mu[nbasis] receives mu_b; ref_ready (if given) is
+// recorded on st once C is complete.
 int deposit_sorted(Plan &p, const double *rtp, const double *w, int64_t ngal, double *maps, double *ref,
-                   double *mu, cudaStream_t st);
+                   double *mu, cudaEvent_t ref_ready, cudaStream_t st);
 // A[lm][2j + c] += mu[j] * rmu[lm * ldr + c] for j < nmaps; with set_col >= 0
 // also A[lm][2 set_col + c] = rset[lm * ldr + c].
 void launch_add_mean(double *A, int64_t ldA, int64_t nmaps, const double *mu, const double *rmu, const double *rset,
@@ -173,8 +174,8 @@ uint2 dft_slices(double v, int EB);
 // tensor-core (tcgen05) Legendre analysis, mixed precision
 int64_t tc_table_offsets(const Plan &p, std::vector<int64_t> &off);
 void launch_build_lamtc(const Plan &p, const int *Ea, const int *Es, cudaStream_t st);
-void launch_leg_analysis_tc(const Plan &p, const float *F, int64_t ncol, double *A, float2 *Adf, bool accumulate,
-                            cudaStream_t st);
+void launch_leg_analysis_tc(const Plan &p, const float *F, int64_t ncol, double *A, float2 *Adf, int *Ecol,
+                            bool accumulate, cudaStream_t st);
 int64_t tc_synth_table_offsets(const Plan &p, std::vector<int64_t> &off);
 void launch_build_lamts(const Plan &p, const int *Es, cudaStream_t st);
 void launch_leg_synthesis_tc(const Plan &p, const float2 *Adf, int64_t ncol, float *G, cudaStream_t st);
