@@ -52,16 +52,17 @@
 namespace sfb {
 namespace tc {
 
-constexpr int KC = 32;          // K elements per chunk
+constexpr int KC = 16;          // K elements per chunk (one MMA K step)
 constexpr int MTILE = 128;      // columns per CTA (MMA M)
 constexpr int NMAX = 64;        // MMA N per CTA: lambda rows (analysis) or rings (synthesis)
-constexpr int NTH = 256;        // threads: two per operand row
-constexpr int NSTAGE = 2;
+constexpr int NPROD = 256;      // producer threads: two per operand row (warps 0-7)
+constexpr int NTH = NPROD + 32; // + the MMA warp (warp 8)
+constexpr int NSTAGE = 4;
 constexpr uint32_t PLANE_A = MTILE * KC * 2;          // bytes of one operand-A plane
 constexpr uint32_t PLANE_B = NMAX * KC * 2;           // bytes of one lambda plane (<= NMAX rows)
 constexpr uint32_t STAGE_BYTES = 4 * PLANE_A + 4 * PLANE_B;
 constexpr uint32_t TMEM_COLS = 4 * NMAX;             // four level accumulators
-constexpr size_t LEG_SMEM = NSTAGE * (size_t)STAGE_BYTES + 64;   // two CTAs per SM
+constexpr size_t LEG_SMEM = NSTAGE * (size_t)STAGE_BYTES + 128;  // two CTAs per SM
 
 // byte offset of element (row, k) in a K-major no-swizzle plane with KC columns
 __device__ __forceinline__ uint32_t core_off(int row, int k) {
@@ -78,21 +79,27 @@ __device__ __forceinline__ void st_v4(unsigned char *p, const uint32_t (&v)[4]) 
     *reinterpret_cast<uint4 *>(p) = make_uint4(v[0], v[1], v[2], v[3]);
 }
 
-// Shared state of the level kernels: NSTAGE stages of (A planes, B planes),
-// barriers bb[s] (lambda planes landed) and bm[s] (MMAs of the stage done).
+// Shared state of the level kernels: NSTAGE stages of (A planes, B planes)
+// and the barriers of the producer / MMA pipeline: full_a[s] (every producer
+// warp wrote its slices: one arrival per warp after __syncwarp), full_b[s] (lambda planes landed), empty[s]
+// (the MMAs of the stage completed), done (all MMAs completed).
 struct LvlSmem {
     unsigned char *base;
-    uint64_t *bb, *bm;
+    uint64_t *full_a, *full_b, *empty, *done;
     uint32_t *slot;
+    int *bad;
     __device__ __forceinline__ unsigned char *stage(int s) const { return base + s * STAGE_BYTES; }
 };
 
 __device__ __forceinline__ LvlSmem lvl_smem(unsigned char *base) {
     LvlSmem c;
     c.base = base;
-    c.bb = reinterpret_cast<uint64_t *>(base + NSTAGE * STAGE_BYTES);
-    c.bm = c.bb + NSTAGE;
-    c.slot = reinterpret_cast<uint32_t *>(c.bm + NSTAGE);
+    c.full_a = reinterpret_cast<uint64_t *>(base + NSTAGE * STAGE_BYTES);
+    c.full_b = c.full_a + NSTAGE;
+    c.empty = c.full_b + NSTAGE;
+    c.done = c.empty + NSTAGE;
+    c.slot = reinterpret_cast<uint32_t *>(c.done + 1);
+    c.bad = reinterpret_cast<int *>(c.slot + 1);
     return c;
 }
 
@@ -105,9 +112,12 @@ __device__ __forceinline__ uint32_t lvl_setup(LvlSmem &c) {
     }
     if (threadIdx.x == 0) {
         for (int i = 0; i < NSTAGE; ++i) {
-            mbar_init(&c.bb[i], 1);
-            mbar_init(&c.bm[i], 1);
+            mbar_init(&c.full_a[i], NPROD / 32);
+            mbar_init(&c.full_b[i], 1);
+            mbar_init(&c.empty[i], 1);
         }
+        mbar_init(c.done, 1);
+        *c.bad = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     fence_before();
@@ -123,20 +133,17 @@ __device__ __forceinline__ void lvl_teardown(uint32_t tmem) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
 }
 
-// The ten level products of one K chunk (two K steps of 16): level v goes to
+// The ten level products of one K chunk (one K step of 16): level v goes to
 // TMEM columns [NMAX v, NMAX v + N).
 __device__ __forceinline__ void lvl_mma(uint32_t tmem, uint32_t a0, uint32_t b0, uint32_t planeB, uint32_t idesc,
                                         bool first_chunk) {
     const uint32_t sbo = (KC / 8) * 128;
 #pragma unroll
-    for (int s = 0; s < KC / 16; ++s) {
-#pragma unroll
-        for (int p = 0; p < 10; ++p) {
-            const uint64_t ad = smem_desc(a0 + lvl_a(p) * PLANE_A + s * 256, 128, sbo);
-            const uint64_t bd = smem_desc(b0 + lvl_b(p) * planeB + s * 256, 128, sbo);
-            const uint32_t acc = (first_chunk && s == 0 && lvl_first(p)) ? 0u : 1u;
-            mma_bf16(tmem + (uint32_t)NMAX * (uint32_t)lvl_of(p), ad, bd, idesc, acc);
-        }
+    for (int p = 0; p < 10; ++p) {
+        const uint64_t ad = smem_desc(a0 + lvl_a(p) * PLANE_A, 128, sbo);
+        const uint64_t bd = smem_desc(b0 + lvl_b(p) * planeB, 128, sbo);
+        const uint32_t acc = (first_chunk && lvl_first(p)) ? 0u : 1u;
+        mma_bf16(tmem + (uint32_t)NMAX * (uint32_t)lvl_of(p), ad, bd, idesc, acc);
     }
 }
 
@@ -151,11 +158,44 @@ __device__ __forceinline__ void lvl_sum(float L0, float L1, float L2, float L3, 
     lo = t - (hi - s);
 }
 
-// Chunk pipeline shared by both kernels: stage of chunk kc is kc % NSTAGE;
-// bb / bm phases advance once per use of the stage.  In iteration kc the CTA
-// slices chunk kc into its stage, issues its MMAs, then waits for the MMAs
-// of chunk kc - 1 and starts the lambda copy and operand loads of kc + 1.
+// Chunk kc lives in stage kc % NSTAGE, the (kc / NSTAGE)-th use of that stage.
 __device__ __forceinline__ uint32_t ph_of(int kc) { return (uint32_t)((kc / NSTAGE) & 1); }
+
+// MMA warp (lane 0 issues): for every chunk wait for its A slices and lambda
+// planes, issue the ten products, release the stage; finally commit `done`.
+// Returns the number of chunks issued.
+__device__ __forceinline__ int lvl_mma_loop(const LvlSmem &cs, uint32_t tmem, int nch, uint32_t planeB,
+                                            uint32_t idesc) {
+    int issued = 0;
+    for (int kc = 0; kc < nch; ++kc) {
+        const int s = kc % NSTAGE;
+        if (*(volatile int *)cs.bad) break;
+        if (!mbar_wait(&cs.full_a[s], ph_of(kc)) || !mbar_wait(&cs.full_b[s], ph_of(kc))) {
+            atomicExch(cs.bad, 1);
+            break;
+        }
+        fence_after();
+        const uint32_t sa = smem_u32(cs.stage(s));
+        lvl_mma(tmem, sa, sa + 4 * PLANE_A, planeB, idesc, kc == 0);
+        mma_commit(&cs.empty[s]);
+        ++issued;
+    }
+    mma_commit(cs.done);          // arrives once every MMA issued above has completed
+    return issued;
+}
+
+// Producer side of one chunk: wait until the stage is free (its previous
+// MMAs completed), optionally start the lambda copy, write the A slices and
+// arrive on full_a.  False when a wait expired.
+__device__ __forceinline__ bool lvl_stage_free(const LvlSmem &cs, int kc) {
+    if (kc < NSTAGE) return true;
+    if (*(volatile int *)cs.bad) return false;
+    if (!mbar_wait(&cs.empty[kc % NSTAGE], (uint32_t)(((kc / NSTAGE) - 1) & 1))) {
+        atomicExch(cs.bad, 1);
+        return false;
+    }
+    return true;
+}
 
 // Per (block z, column c): E with max_r |F[parity][m][r][c]| < 2^E, raised by
 // ceil(log2 nrn) - 9 for more than 512 rings (level sums below 2^24 units).
@@ -179,7 +219,8 @@ __global__ void __launch_bounds__(256) k_colmax(const float *__restrict__ F, int
     Ecol[(int64_t)z * ncol + c] = max(-90, min(scale_exp(fmaxf(fmaxf(m0, m1), fmaxf(m2, m3))) + max(0, lg - 9), 100));
 }
 
-// Analysis: grid (column tiles, row tiles of NMAX, blocks z).
+// Analysis: grid (column tiles, row tiles of NMAX, blocks z); warps 0-7
+// produce (thread: column c, half kh of each chunk), warp 8 issues the MMAs.
 __global__ void __launch_bounds__(NTH, 2) k_leg_analysis_tc(const __nv_bfloat16 *__restrict__ lamtc,
                                                             const int64_t *__restrict__ lamtc_off, int lmax, int nrn,
                                                             int nchunks, const float *__restrict__ F, int64_t ncol,
@@ -195,92 +236,75 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_analysis_tc(const __nv_bfloat16 
     const int NPc = min(NMAX, NP - row0);
     const int64_t col0 = (int64_t)blockIdx.x * MTILE;
     const int tid = threadIdx.x, warp = tid >> 5;
-    const int c = tid & (MTILE - 1), kh = tid >> 7;      // column, ring half of each chunk
-    const bool cok = col0 + c < ncol;
+    const int c = tid & (MTILE - 1), kh = (tid >> 7) & 1;
+    const bool prod = tid < NPROD;
+    const bool cok = prod && col0 + c < ncol;
     const float *Fz = F + ((int64_t)(par * (lmax + 1) + m) * nrn) * ncol + col0 + c;
     const __nv_bfloat16 *Lz = lamtc + lamtc_off[z];
     const uint32_t planeB = (uint32_t)NPc * KC * 2;
     LvlSmem cs = lvl_smem(smem);
     float C[4];
     slice_consts(cok ? Ecol[(int64_t)z * ncol + col0 + c] : 0, C);
-
-    float pre[2][16];          // operand values of chunks kc (buffer kc & 1) and kc + 1
-    auto loadA = [&](int kc, float (&buf)[16]) {
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-            const int r = kc * KC + 16 * kh + j;
-            buf[j] = (cok && r < nrn) ? Fz[(int64_t)r * ncol] : 0.f;
-        }
-    };
-    auto issueB = [&](int kc) {
-        const int s = kc % NSTAGE;
-        mbar_expect_tx(&cs.bb[s], 4 * planeB);
-        const int64_t chunk_elems = 4LL * NP * KC;
-        for (int pl = 0; pl < 4; ++pl)
-            bulk_g2s(cs.stage(s) + 4 * PLANE_A + pl * planeB,
-                     Lz + kc * chunk_elems + (int64_t)pl * NP * KC + (int64_t)row0 * KC, planeB, &cs.bb[s]);
-    };
-    loadA(0, pre[0]);
-    if (nchunks > 1) loadA(1, pre[1]);
     const uint32_t tmem = lvl_setup(cs);
-    if (tid == 0) issueB(0);
     const uint32_t idesc = idesc_bf16(MTILE, NPc);
-    bool ok = true;
-    int issued = 0;
-    // one chunk: slice, prefetch kc + 2 into the freed buffer, MMAs, start the lambda copy of kc + 1
-    auto chunk = [&](int kc, float (&cur)[16]) -> bool {
-        const int s = kc % NSTAGE;
-        unsigned char *sa = cs.stage(s);
+
+    if (!prod) {
+        if ((tid & 31) == 0) {
+            const int issued = lvl_mma_loop(cs, tmem, nchunks, planeB, idesc);
+            if (issued != nchunks) atomicExch(cs.bad, 1);
+        }
+    } else {
+        float pre[2][8];          // this thread's 8 ring values of chunks kc and kc + 1
+        auto loadA = [&](int kc, float (&buf)[8]) {
 #pragma unroll
-        for (int g = 0; g < 2; ++g) {
+            for (int j = 0; j < 8; ++j) {
+                const int r = kc * KC + 8 * kh + j;
+                buf[j] = (cok && r < nrn) ? Fz[(int64_t)r * ncol] : 0.f;
+            }
+        };
+        auto chunk = [&](int kc, float (&cur)[8]) -> bool {
+            const int s = kc % NSTAGE;
+            if (!lvl_stage_free(cs, kc)) return false;
+            unsigned char *sa = cs.stage(s);
+            if (tid == 0) {
+                mbar_expect_tx(&cs.full_b[s], 4 * planeB);
+                const int64_t chunk_elems = 4LL * NP * KC;
+                for (int pl = 0; pl < 4; ++pl)
+                    bulk_g2s(sa + 4 * PLANE_A + pl * planeB,
+                             Lz + kc * chunk_elems + (int64_t)pl * NP * KC + (int64_t)row0 * KC, planeB,
+                             &cs.full_b[s]);
+            }
             uint32_t w[4][4];
 #pragma unroll
             for (int t = 0; t < 4; ++t) {
                 uint32_t v[4];
-                slice_pair(cur[8 * g + 2 * t], cur[8 * g + 2 * t + 1], C, v);
+                slice_pair(cur[2 * t], cur[2 * t + 1], C, v);
 #pragma unroll
                 for (int q = 0; q < 4; ++q) w[q][t] = v[q];
             }
-            const uint32_t off = core_off(c, 16 * kh + 8 * g);
+            const uint32_t off = core_off(c, 8 * kh);
 #pragma unroll
             for (int q = 0; q < 4; ++q) st_v4(sa + q * PLANE_A + off, w[q]);
+            if (kc + 2 < nchunks) loadA(kc + 2, cur);
+            fence_proxy_async();
+            __syncwarp();
+            if ((tid & 31) == 0) mbar_arrive(&cs.full_a[s]);       // one arrival per producer warp
+            return true;
+        };
+        loadA(0, pre[0]);
+        if (nchunks > 1) loadA(1, pre[1]);
+        for (int kc = 0; kc < nchunks; kc += 2) {
+            if (!chunk(kc, pre[0])) break;
+            if (kc + 1 < nchunks && !chunk(kc + 1, pre[1])) break;
         }
-        if (kc + 2 < nchunks) loadA(kc + 2, cur);
-        fence_proxy_async();
-        __syncthreads();
-        if (tid == 0) {
-            if (!mbar_wait(&cs.bb[s], ph_of(kc))) {
-                ok = false;
-            } else {
-                fence_after();
-                lvl_mma(tmem, smem_u32(sa), smem_u32(sa + 4 * PLANE_A), planeB, idesc, kc == 0);
-                mma_commit(&cs.bm[s]);
-                ++issued;
-            }
-        }
-        if (kc + 1 < nchunks) {
-            // the stage of chunk kc + 1 held chunk kc - 1: wait for its MMAs
-            if (kc >= 1 && !mbar_wait(&cs.bm[(kc + 1) % NSTAGE], ph_of(kc - 1))) ok = false;
-            fence_after();
-            if (ok && tid == 0) issueB(kc + 1);
-        }
-        ok = __syncthreads_and(ok);
-        return ok;
-    };
-    for (int kc = 0; kc < nchunks; kc += 2) {
-        if (!chunk(kc, pre[0])) break;
-        if (kc + 1 < nchunks && !chunk(kc + 1, pre[1])) break;
     }
-    __shared__ int s_issued;                              // thread 0's count of committed chunks
-    if (tid == 0) s_issued = issued;
-    __syncthreads();
-    issued = s_issued;
-    if (issued > 0 && !mbar_wait(&cs.bm[(issued - 1) % NSTAGE], ph_of(issued - 1))) ok = false;
+    // every thread: wait for all MMAs, then the epilogue
+    bool ok = mbar_wait(cs.done, 0);
     fence_after();
-    ok = __syncthreads_and(ok);
-    if (!ok || issued != nchunks) {
+    ok = __syncthreads_and(ok) && !*(volatile int *)cs.bad;
+    if (!ok) {
         if (tid == 0) atomicOr(err, ERR_TC_TIMEOUT);
-    } else {
+    } else if (prod) {
         // warp w reads TMEM lanes 32 (w % 4).. (columns) and rows li in [32 (w / 4), +32)
         const int lq = warp & 3, hg = warp >> 2;
         const uint32_t lane_base = (uint32_t)(lq * 32) << 16;
@@ -322,14 +346,14 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_analysis_tc(const __nv_bfloat16 
     lvl_teardown(tmem);
 }
 
-// Synthesis: grid (column tiles, ring tiles of NT <= NMAX, blocks z).
+// Synthesis: grid (column tiles, ring tiles of NT <= NMAX, blocks z); warps
+// 0-7 produce, warp 8 issues the MMAs.
 __global__ void __launch_bounds__(NTH, 2) k_leg_synthesis_tc(const __nv_bfloat16 *__restrict__ lamts,
                                                              const int64_t *__restrict__ lamts_off, int lmax, int nrn,
                                                              int NT, const float2 *__restrict__ Adf, int64_t ncol,
                                                              float *__restrict__ G, int *err) {
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ float red[2][MTILE];
-    __shared__ int s_issued;
     const int z = blockIdx.z;
     const int m = z >> 1, par = z & 1;
     const int nrows = rows_of(m, par, lmax);
@@ -347,8 +371,9 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_synthesis_tc(const __nv_bfloat16
         return;
     }
     const int nK = (nrows + KC - 1) / KC;
-    const int c = tid & (MTILE - 1), kh = tid >> 7;
-    const bool cok = col0 + c < ncol;
+    const int c = tid & (MTILE - 1), kh = (tid >> 7) & 1;
+    const bool prod = tid < NPROD;
+    const bool cok = prod && col0 + c < ncol;
     const uint32_t planeB = (uint32_t)NT * KC * 2;
     const __nv_bfloat16 *Lz = lamts + lamts_off[z] + (int64_t)nt * nK * 4 * NT * KC;
     LvlSmem cs = lvl_smem(smem);
@@ -360,79 +385,61 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_synthesis_tc(const __nv_bfloat16
     // column scale over the rows (|hi + lo| < 2^E: hi is an FP32 value below 2^E, |lo| <= ulp(hi)/2)
     float mx = 0.f;
     for (int li = kh; li < nrows; li += 2) mx = fmaxf(mx, fabsf(aval(li).x));
-    red[kh][c] = mx;
+    if (prod) red[kh][c] = mx;
     const uint32_t tmem = lvl_setup(cs);      // includes a __syncthreads
     float C[4];
     slice_consts(scale_exp(fmaxf(red[0][c], red[1][c])), C);
     const uint32_t idesc = idesc_bf16(MTILE, NT);
 
-    float2 pre[2][16];
-    auto loadA = [&](int kc, float2 (&buf)[16]) {
+    if (!prod) {
+        if (lane == 0) {
+            const int issued = lvl_mma_loop(cs, tmem, nK, planeB, idesc);
+            if (issued != nK) atomicExch(cs.bad, 1);
+        }
+    } else {
+        float2 pre[2][8];
+        auto loadA = [&](int kc, float2 (&buf)[8]) {
 #pragma unroll
-        for (int j = 0; j < 16; ++j) buf[j] = aval(kc * KC + 16 * kh + j);
-    };
-    auto issueB = [&](int kc) {
-        const int s = kc % NSTAGE;
-        mbar_expect_tx(&cs.bb[s], 4 * planeB);
-        bulk_g2s(cs.stage(s) + 4 * PLANE_A, Lz + (int64_t)kc * 4 * NT * KC, 4 * planeB, &cs.bb[s]);
-    };
-    bool ok = true;
-    int issued = 0;
-    if (tid == 0) issueB(0);
-    loadA(0, pre[0]);
-    if (nK > 1) loadA(1, pre[1]);
-    auto chunk = [&](int kc, float2 (&cur)[16]) -> bool {
-        const int s = kc % NSTAGE;
-        unsigned char *sa = cs.stage(s);
-#pragma unroll
-        for (int g = 0; g < 2; ++g) {
+            for (int j = 0; j < 8; ++j) buf[j] = aval(kc * KC + 8 * kh + j);
+        };
+        auto chunk = [&](int kc, float2 (&cur)[8]) -> bool {
+            const int s = kc % NSTAGE;
+            if (!lvl_stage_free(cs, kc)) return false;
+            unsigned char *sa = cs.stage(s);
+            if (tid == 0) {
+                mbar_expect_tx(&cs.full_b[s], 4 * planeB);
+                bulk_g2s(sa + 4 * PLANE_A, Lz + (int64_t)kc * 4 * NT * KC, 4 * planeB, &cs.full_b[s]);
+            }
             uint32_t w[4][4];
 #pragma unroll
             for (int t = 0; t < 4; ++t) {
                 uint32_t v[4];
-                const float2 x0 = cur[8 * g + 2 * t], x1 = cur[8 * g + 2 * t + 1];
-                slice_pair_df(x0.x, x0.y, x1.x, x1.y, C, v);
+                slice_pair_df(cur[2 * t].x, cur[2 * t].y, cur[2 * t + 1].x, cur[2 * t + 1].y, C, v);
 #pragma unroll
                 for (int q = 0; q < 4; ++q) w[q][t] = v[q];
             }
-            const uint32_t off = core_off(c, 16 * kh + 8 * g);
+            const uint32_t off = core_off(c, 8 * kh);
 #pragma unroll
             for (int q = 0; q < 4; ++q) st_v4(sa + q * PLANE_A + off, w[q]);
+            if (kc + 2 < nK) loadA(kc + 2, cur);
+            fence_proxy_async();
+            __syncwarp();
+            if ((tid & 31) == 0) mbar_arrive(&cs.full_a[s]);       // one arrival per producer warp
+            return true;
+        };
+        loadA(0, pre[0]);
+        if (nK > 1) loadA(1, pre[1]);
+        for (int kc = 0; kc < nK; kc += 2) {
+            if (!chunk(kc, pre[0])) break;
+            if (kc + 1 < nK && !chunk(kc + 1, pre[1])) break;
         }
-        if (kc + 2 < nK) loadA(kc + 2, cur);
-        fence_proxy_async();
-        __syncthreads();
-        if (tid == 0) {
-            if (!mbar_wait(&cs.bb[s], ph_of(kc))) {
-                ok = false;
-            } else {
-                fence_after();
-                lvl_mma(tmem, smem_u32(sa), smem_u32(sa + 4 * PLANE_A), planeB, idesc, kc == 0);
-                mma_commit(&cs.bm[s]);
-                ++issued;
-            }
-        }
-        if (kc + 1 < nK) {
-            if (kc >= 1 && !mbar_wait(&cs.bm[(kc + 1) % NSTAGE], ph_of(kc - 1))) ok = false;
-            fence_after();
-            if (ok && tid == 0) issueB(kc + 1);
-        }
-        ok = __syncthreads_and(ok);
-        return ok;
-    };
-    for (int kc = 0; kc < nK; kc += 2) {
-        if (!chunk(kc, pre[0])) break;
-        if (kc + 1 < nK && !chunk(kc + 1, pre[1])) break;
     }
-    if (tid == 0) s_issued = issued;
-    __syncthreads();
-    issued = s_issued;
-    if (issued > 0 && !mbar_wait(&cs.bm[(issued - 1) % NSTAGE], ph_of(issued - 1))) ok = false;
+    bool ok = mbar_wait(cs.done, 0);
     fence_after();
-    ok = __syncthreads_and(ok);
-    if (!ok || issued != nK) {
+    ok = __syncthreads_and(ok) && !*(volatile int *)cs.bad;
+    if (!ok) {
         if (tid == 0) atomicOr(err, ERR_TC_TIMEOUT);
-    } else {
+    } else if (prod) {
         // warp w reads TMEM lanes 32 (w % 4).. (columns) and rings [32 (w / 4), +32) of the tile
         const int lq = warp & 3, hg = warp >> 2;
         const uint32_t lane_base = (uint32_t)(lq * 32) << 16;
