@@ -48,17 +48,18 @@ __global__ void k_deposit_keys(const double *__restrict__ rtp, const double *__r
     } else if (th < 0.0 || th > M_PI) {
         atomicOr(err, ERR_THETA_RANGE);
     } else {
-        const int64_t pix = ang2pix_ring_z(nside, cos(th), ph);
+        const int64_t pix = ang2pix_ring_fast(nside, th, ph);
         int slot;
         if (r < rmin) {
             slot = pieces;
         } else if (r > rmax) {
             slot = pieces + 1;
         } else {
-            const double width = (rmax - rmin) / pieces;
-            slot = (int)((r - rmin) / width);
+            // u = (r - rmin) / width in units of the pieces; x in [-1, 1] on the piece
+            const double u = (r - rmin) * ((double)pieces / (rmax - rmin));
+            slot = (int)u;
             if (slot >= pieces) slot = pieces - 1;
-            x = 2.0 * (r - (rmin + slot * width)) / width - 1.0;
+            x = 2.0 * (u - (double)slot) - 1.0;
             x = fmin(1.0, fmax(-1.0, x));
         }
         k = (int32_t)(slot * npix + pix);

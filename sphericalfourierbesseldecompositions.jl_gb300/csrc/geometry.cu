@@ -60,7 +60,7 @@ void launch_legendre_table(const Plan &p, cudaStream_t st) {
 __global__ void k_ang2pix(int64_t nside, const double *theta, const double *phi, int64_t n, int64_t *pix) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    pix[i] = ang2pix_ring_z(nside, cos(theta[i]), phi[i]);
+    pix[i] = ang2pix_ring_fast(nside, theta[i], phi[i]);
 }
 
 void launch_ang2pix(int64_t nside, const double *theta, const double *phi, int64_t n, int64_t *pix,

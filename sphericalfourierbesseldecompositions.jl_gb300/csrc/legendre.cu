@@ -328,6 +328,77 @@ void launch_leg_synthesis(const Plan &p, const double *A, int64_t ncol, double *
     note_launch();
 }
 
+// Column-major variant: one block per (m', parity, tile of complex columns,
+// chunk of FOLD_RC rings), looping over its rings (coalesced over the
+// columns).  With Ecol it also raises the scale exponent of every real column
+// over the rings (atomicMax; Ecol preset to a value below every exponent),
+// the input of the mixed-precision Legendre analysis (as k_colmax computes
+// for F).
+constexpr int FOLD_RC = 64;
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_fold_cols(const RingGeom *__restrict__ rings, int nrn, int lmax, double w,
+                                                   const T *__restrict__ F, const T *__restrict__ G, int64_t ncplx,
+                                                   T *__restrict__ R, int *__restrict__ Ecol) {
+    const int mp = blockIdx.y >> 1, par = blockIdx.y & 1;
+    const int rc0 = blockIdx.z * FOLD_RC;
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncplx) return;
+    const int L1 = lmax + 1;
+    const int64_t ld = 2 * ncplx;
+    float mxr = 0.f, mxi = 0.f;
+    const int rend = min(nrn, rc0 + FOLD_RC);
+#pragma unroll 4
+    for (int r = rc0; r < rend; ++r) {
+        const RingGeom g = rings[r];
+        const int n = g.nph;
+        const bool odd_phase = g.phi0_den != 0;
+        const T f = (T)(w * (double)n * g.cfold);
+        const int64_t off = ((int64_t)(par * L1 + mp) * nrn + r) * ld + 2 * c;
+        T sx, sy;
+        if (n > 2 * lmax) {          // no aliasing on this ring
+            sx = G[off];
+            sy = mp == 0 ? T(0) : G[off + 1];
+        } else {
+            sx = 0;
+            sy = 0;
+            const int k = mp % n;
+            const int kk = (n - k) % n;
+            int tt = 0;
+            for (int m = k; m <= lmax; m += n, ++tt) {
+                const T *gp = G + ((int64_t)(par * L1 + m) * nrn + r) * ld + 2 * c;
+                const int dt = tt - mp / n;
+                const T sgn = (odd_phase && (dt & 1)) ? T(-1) : T(1);
+                sx += sgn * gp[0];
+                if (m != 0) sy += sgn * gp[1];
+            }
+            for (int m = (kk == 0 ? n : kk); m <= lmax; m += n) {
+                const T *gp = G + ((int64_t)(par * L1 + m) * nrn + r) * ld + 2 * c;
+                const int q = (m + mp) / n;
+                const T sgn = (odd_phase && (q & 1)) ? T(-1) : T(1);
+                sx += sgn * gp[0];
+                sy -= sgn * gp[1];
+            }
+        }
+        const T rx = F[off] - f * sx, ry = F[off + 1] - f * sy;
+        R[off] = rx;
+        R[off + 1] = ry;
+        mxr = fmaxf(mxr, fabsf((float)rx));
+        mxi = fmaxf(mxi, fabsf((float)ry));
+    }
+    if (Ecol) {
+        const int lg = 32 - __clz(nrn > 1 ? nrn - 1 : 1);
+        const int extra = max(0, lg - 9);
+        auto ex = [&](float mx) {
+            int E = (mx > 0.f && isfinite(mx)) ? ilogbf(mx) + 1 : 0;
+            return max(-90, min(E + extra, 100));
+        };
+        const int64_t z = 2 * (int64_t)mp + par;
+        atomicMax(Ecol + z * ld + 2 * c, ex(mxr));
+        atomicMax(Ecol + z * ld + 2 * c + 1, ex(mxi));
+    }
+}
+
 // Few columns: one thread per (parity, m', ring, complex column), same sums.
 template <typename T>
 __global__ void __launch_bounds__(256) k_fold_residual_narrow(const RingGeom *rings, int nrn, int lmax, double w,
@@ -372,8 +443,19 @@ __global__ void __launch_bounds__(256) k_fold_residual_narrow(const RingGeom *ri
 }
 
 void launch_fold_residual(const Plan &p, const double *F, const double *G, int64_t ncol, double *R,
-                          cudaStream_t st) {
+                          cudaStream_t st, int *Ecol) {
     const int64_t ncplx = ncol / 2;
+    if (p.precision == SFB_MIXED && ncplx > 4) {
+        // 0x80 bytes: every exponent word starts at -2139062144, below any scale exponent
+        if (Ecol) cudaMemsetAsync(Ecol, 0x80, (size_t)2 * (p.lmax + 1) * ncol * sizeof(int), st);
+        dim3 grid((unsigned)((ncplx + 127) / 128), (unsigned)(2 * (p.lmax + 1)),
+                  (unsigned)((p.nrn + FOLD_RC - 1) / FOLD_RC));
+        const double w = 4.0 * M_PI / (double)p.npix;
+        k_fold_cols<float><<<grid, 128, 0, st>>>(p.d_rings, (int)p.nrn, p.lmax, w, (const float *)F, (const float *)G,
+                                                 ncplx, (float *)R, Ecol);
+        note_launch();
+        return;
+    }
     if (ncplx <= 4) {
         const int64_t total = (int64_t)2 * (p.lmax + 1) * p.nrn * ncplx;
         const unsigned blocks = (unsigned)((total + 255) / 256);

@@ -618,8 +618,8 @@ void launch_build_lamtc(const Plan &p, const int *Ea, const int *Es, cudaStream_
 }
 
 void launch_leg_analysis_tc(const Plan &p, const float *F, int64_t ncol, double *A, float2 *Adf, int *Ecol,
-                            bool accumulate, cudaStream_t st) {
-    {
+                            bool accumulate, cudaStream_t st, bool scales_ready) {
+    if (!scales_ready) {
         dim3 grid((unsigned)((ncol + 255) / 256), (unsigned)(2 * (p.lmax + 1)));
         tc::k_colmax<<<grid, 256, 0, st>>>(F, ncol, p.lmax, (int)p.nrn, Ecol);
         note_launch();

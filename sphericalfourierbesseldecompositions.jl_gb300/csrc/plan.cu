@@ -333,7 +333,8 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, b
     int *ecol = reinterpret_cast<int *>(p.erow.ptr);          // column scales (the row scales are used up)
     auto analysis = [&](const double *src, bool acc) {
         Stage s(h, stage(SFB_STAGE_LEG_ANALYSIS), st);
-        if (tc) launch_leg_analysis_tc(p, (const float *)src, ncol, p.alm.ptr, adf, ecol, acc, st);
+        // after the first pass the fold has written the column scales of its residual
+        if (tc) launch_leg_analysis_tc(p, (const float *)src, ncol, p.alm.ptr, adf, ecol, acc, st, acc);
         else launch_leg_analysis(p, src, ncol, p.alm.ptr, acc, st);
     };
     analysis(p.fbuf.ptr, false);
@@ -343,7 +344,10 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, b
             if (tc) launch_leg_synthesis_tc(p, adf, ncol, (float *)p.gbuf.ptr, st);
             else launch_leg_synthesis(p, p.alm.ptr, ncol, p.gbuf.ptr, st);
         }
-        { Stage s(h, stage(SFB_STAGE_FOLD), st); launch_fold_residual(p, p.fbuf.ptr, p.gbuf.ptr, ncol, p.rbuf.ptr, st); }
+        {
+            Stage s(h, stage(SFB_STAGE_FOLD), st);
+            launch_fold_residual(p, p.fbuf.ptr, p.gbuf.ptr, ncol, p.rbuf.ptr, st, tc ? ecol : nullptr);
+        }
         analysis(p.rbuf.ptr, true);
     }
     SFB_CUDA_TRY(cudaGetLastError());
@@ -416,14 +420,15 @@ int cat2amln_dev(sfb_plan *h, const double *rtp, const double *w, int64_t ngal, 
         const bool split = p.precision == SFB_MIXED && wk != SFB_WINDOW_ZERO;
         const double *W01 = wk == SFB_WINDOW_SEPARABLE ? win->mask : win->dense;
         const int64_t cp = wk == SFB_WINDOW_DENSE ? chunk_pairs(p) : 0;
-        double *Cmap = nullptr, *ralm = nullptr, *mu = nullptr, *nu = nullptr;
+        double *Cmap = nullptr, *ralm = nullptr, *mu = nullptr, *nu = nullptr, *smean = nullptr;
         if (split) {
-            // [C][W01][ralm: lmsize x (C, W01) complex][mu][nu]
-            SFB_TRY(grow(p, p.ref, (size_t)(2 * p.npix + 4 * p.lmsize + p.nbasis + cp)));
+            // [C][W01][ralm: lmsize x (C, W01) complex][mu][nu][per-pair mean parts]
+            SFB_TRY(grow(p, p.ref, (size_t)(2 * p.npix + 4 * p.lmsize + p.nbasis + cp + p.npairs)));
             Cmap = p.ref.ptr;
             ralm = Cmap + 2 * p.npix;
             mu = ralm + 4 * p.lmsize;
             nu = mu + p.nbasis;
+            smean = nu + cp;
             SFB_CUDA_TRY(cudaMemcpyAsync(Cmap + p.npix, W01, p.npix * sizeof(double), cudaMemcpyDeviceToDevice, st));
         }
         SFB_TRY(grow(p, p.maps, (size_t)nm * p.npix));
@@ -449,10 +454,12 @@ int cat2amln_dev(sfb_plan *h, const double *rtp, const double *w, int64_t ngal, 
         SFB_TRY(sht_analysis(h, p.maps.ptr, nm, st));
         {
             Stage s(h, SFB_STAGE_PROJECT, st);
-            if (split)
-                launch_add_mean(p.alm.ptr, 2 * nm, p.nbasis, mu, ralm, ralm + 2, 4, p.lmsize,
-                                wk == SFB_WINDOW_SEPARABLE ? p.nbasis : -1, st);
-            launch_project_poly(p, p.alm.ptr, 2 * nm, scale, wk, win->w_ln, p.nbasis, nullptr, 0, out, st);
+            if (p.precision == SFB_MIXED)
+                launch_project_mixed(p, reinterpret_cast<const float2 *>(p.almdf.ptr), 2 * nm, p.d_coefT, h->d_noff,
+                                     h->d_pair_index, scale, mu, smean, split ? ralm : nullptr, wk, win->w_ln, out,
+                                     st);
+            else
+                launch_project_poly(p, p.alm.ptr, 2 * nm, scale, wk, win->w_ln, p.nbasis, nullptr, 0, out, st);
         }
         if (wk == SFB_WINDOW_DENSE) {
             SFB_TRY(grow(p, p.maps, (size_t)cp * p.npix));
@@ -746,6 +753,10 @@ int sfb_plan_create(const sfb_plan_desc *d, sfb_plan **out) {
         }
         if (p.radial_mode == SFB_RADIAL_POLY) {
             if ((st = choose_radial_basis(h, d)) != SFB_OK) break;
+            // double-float coefficients per (l, basis, n) for the mixed-precision projection
+            const size_t nct = (size_t)(p.lmax + 1) * p.nbasis * p.nmax;
+            if ((st = upload<float2>(p, &p.d_coefT, nullptr, nct)) != SFB_OK) break;
+            launch_coef_df(p, h->d_pair_index, p.d_coefT, h->stream);
         } else {
             p.nbasis = p.npairs;
         }
@@ -769,7 +780,7 @@ void sfb_plan_destroy(sfb_plan *h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     void *ptrs[] = {p.d_rings, p.d_twtab, p.d_twoff, p.d_phase, p.d_wphase, p.d_twtab32, p.d_wphase32, p.d_dtw,
                     p.d_dtw_off, p.d_cls_rings, p.d_cls_off, p.d_lam, p.d_lam32, p.d_lamtc, p.d_lamtc_off, p.d_lamts, p.d_lamts_off, p.d_lam_off, p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp,
-                    p.d_pair_l, p.d_pair_n, p.d_out_pair, p.d_out_lm, p.d_coef, p.d_err,
+                    p.d_pair_l, p.d_pair_n, p.d_out_pair, p.d_out_lm, p.d_coef, p.d_coefT, p.d_err,
                     p.maps.ptr, p.fbuf.ptr, p.gbuf.ptr, p.rbuf.ptr, p.alm.ptr, p.scratch.ptr, p.scratch2.ptr, p.dep.ptr, p.maps32.ptr,
                     p.ref.ptr, p.erow.ptr, p.almdf.ptr, h->d_pair_index, h->d_noff};
     for (void *q : ptrs)

@@ -35,7 +35,7 @@ __global__ void k_deposit_spline(const double *__restrict__ rtp, const double *_
     const double r = rtp[3 * i], th = rtp[3 * i + 1], ph = rtp[3 * i + 2];
     const double w = wgt ? wgt[i] : 1.0;
     if (!galaxy_ok(r, th, ph, w, err)) return;
-    const int64_t pix = ang2pix_ring_z(nside, cos(th), ph);
+    const int64_t pix = ang2pix_ring_fast(nside, th, ph);
     for (int64_t q = blockIdx.y; q < npair_chunk; q += gridDim.y) {
         const int64_t pr = pair0 + q;
         const int64_t o = spl_off[pr], N = spl_off[pr + 1] - o;
@@ -437,7 +437,7 @@ __global__ void k_winweights(const double *__restrict__ weights, int64_t nr, int
         w[i] = NAN;
         return;
     }
-    const int64_t pix = ang2pix_ring_z(nside, cos(th), ph);
+    const int64_t pix = ang2pix_ring_fast(nside, th, ph);
     int64_t bin;
     if (r == rmax) {
         bin = nr;
@@ -490,6 +490,123 @@ void launch_add_mean(double *A, int64_t ldA, int64_t nmaps, const double *mu, co
     const int64_t n = lmsize * ncol;
     if (n <= 0) return;
     k_add_mean<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(A, ldA, ncol, nmaps, mu, rmu, rset, ldr, lmsize, set_col);
+    note_launch();
+}
+
+// ---- mixed-precision radial projection ---------------------------------------
+// Double-float helpers (FP32 pairs, ~48 significant bits).
+struct df2 {
+    float hi, lo;
+};
+__device__ __forceinline__ df2 dfa(df2 a, df2 b) {
+    const float s = a.hi + b.hi;
+    const float z = s - a.hi;
+    const float e = ((a.hi - (s - z)) + (b.hi - z)) + (a.lo + b.lo);
+    const float h = s + e;
+    return {h, e - (h - s)};
+}
+__device__ __forceinline__ df2 dfm(df2 a, df2 b) {
+    const float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+    const float h = p + e;
+    return {h, e - (h - p)};
+}
+
+// CT[(l * nbasis + b) * nmax + n - 1] = coef[pair(n, l)][b] as hi + lo (0 where (n, l) is not a mode).
+__global__ void k_coef_df(const double *__restrict__ coef, const int32_t *__restrict__ pair_index, int lmax, int nmax,
+                          int64_t nbasis, float2 *__restrict__ CT) {
+    const int64_t total = (int64_t)(lmax + 1) * nbasis * nmax;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int n1 = (int)(i % nmax);
+        const int64_t t = i / nmax;
+        const int64_t b = t % nbasis;
+        const int l = (int)(t / nbasis);
+        const int pr = pair_index[(int64_t)n1 * (lmax + 1) + l];
+        const double v = pr >= 0 ? coef[(int64_t)pr * nbasis + b] : 0.0;
+        const float h = (float)v;
+        CT[i] = make_float2(h, (float)(v - (double)h));
+    }
+}
+
+void launch_coef_df(const Plan &p, const int32_t *pair_index, float2 *CT, cudaStream_t st) {
+    k_coef_df<<<1024, 256, 0, st>>>(p.d_coef, pair_index, p.lmax, (int)p.nmax, p.nbasis, CT);
+    note_launch();
+}
+
+// s[pair] = sum_b coef[pair][b] mu_b (FP64): the mean part of every pair.
+__global__ void k_mean_proj(const double *__restrict__ coef, int64_t npairs, int64_t nbasis,
+                            const double *__restrict__ mu, double *__restrict__ s) {
+    const int64_t pr = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (pr >= npairs) return;
+    double a = 0.0;
+    for (int64_t b = 0; b < nbasis; ++b) a = fma(coef[pr * nbasis + b], mu[b], a);
+    s[pr] = a;
+}
+
+// One block per (l, m): the block's threads take n = 1..nmax.
+//   a_nlm = scale * sum_b coef[n,l][b] dA_b[lm]              (double-float)
+//         + scale * s[pair] * C_lm - w_ln(l, n) * M_lm        (FP64)
+// with dA the fluctuation a_lm (double-float copy, row lm of width ldA),
+// C_lm / M_lm the FP64 a_lm of the count map / the mask (ralm [lm][4]);
+// the mean and window terms are skipped when ralm is null / window_kind is
+// not separable.
+__global__ void __launch_bounds__(64) k_project_mixed(const float2 *__restrict__ Adf, int64_t ldA, int64_t nbasis,
+                                                      const float2 *__restrict__ CT, int nmax, int lmax,
+                                                      const int64_t *__restrict__ noff,
+                                                      const int32_t *__restrict__ pair_index, double scale,
+                                                      const double *__restrict__ smean, const double *__restrict__ ralm,
+                                                      int window_kind, const double *__restrict__ w_ln,
+                                                      double *__restrict__ out) {
+    extern __shared__ float2 arow[];
+    const int64_t lm = blockIdx.x;
+    int l = (int)((sqrt(8.0 * (double)lm + 1.0) - 1.0) * 0.5);
+    while ((int64_t)(l + 1) * (l + 2) / 2 <= lm) ++l;
+    while ((int64_t)l * (l + 1) / 2 > lm) --l;
+    for (int64_t j = threadIdx.x; j < 2 * nbasis; j += blockDim.x) arow[j] = Adf[lm * ldA + j];
+    __syncthreads();
+    const float2 *Cl = CT + (int64_t)l * nbasis * nmax;
+    for (int n1 = threadIdx.x; n1 < nmax; n1 += blockDim.x) {
+        const int pr = pair_index[(int64_t)n1 * (lmax + 1) + l];
+        if (pr < 0) continue;
+        df2 re = {0.f, 0.f}, im = {0.f, 0.f};
+        for (int64_t b = 0; b < nbasis; ++b) {
+            const float2 c = Cl[b * nmax + n1];
+            const df2 cc = {c.x, c.y};
+            const float2 ar = arow[2 * b], ai = arow[2 * b + 1];
+            re = dfa(re, dfm(cc, {ar.x, ar.y}));
+            im = dfa(im, dfm(cc, {ai.x, ai.y}));
+        }
+        double vr = scale * ((double)re.hi + (double)re.lo);
+        double vi = scale * ((double)im.hi + (double)im.lo);
+        if (ralm) {
+            const double mu = scale * smean[pr];
+            vr = fma(mu, ralm[4 * lm], vr);
+            vi = fma(mu, ralm[4 * lm + 1], vi);
+            if (window_kind == SFB_WINDOW_SEPARABLE) {
+                const double wl = w_ln[l + (int64_t)(lmax + 1) * n1];
+                vr = fma(-wl, ralm[4 * lm + 2], vr);
+                vi = fma(-wl, ralm[4 * lm + 3], vi);
+            }
+        }
+        const int64_t o = noff[n1] + lm;
+        out[2 * o] = vr;
+        out[2 * o + 1] = vi;
+    }
+}
+
+void launch_project_mixed(const Plan &p, const float2 *Adf, int64_t ldA, const float2 *CT,
+                          const int64_t *noff, const int32_t *pair_index, double scale, const double *mu,
+                          double *smean, const double *ralm, int window_kind, const double *w_ln, double *out,
+                          cudaStream_t st) {
+    if (ralm) {
+        k_mean_proj<<<(unsigned)((p.npairs + 127) / 128), 128, 0, st>>>(p.d_coef, p.npairs, p.nbasis, mu, smean);
+        note_launch();
+    }
+    const size_t smem = (size_t)2 * p.nbasis * sizeof(float2);
+    set_smem(k_project_mixed, smem);
+    k_project_mixed<<<(unsigned)p.lmsize, 64, smem, st>>>(Adf, ldA, p.nbasis, CT, (int)p.nmax, p.lmax, noff,
+                                                          pair_index, scale, smean, ralm, window_kind, w_ln, out);
     note_launch();
 }
 

@@ -50,14 +50,12 @@ constexpr int KC = 32;            // pixels per chunk
 constexpr int NPAIR = 64;         // (ring, map) pairs per CTA
 constexpr int NROW = 128;         // A rows (MMA M): pairs x {north, south}
 constexpr int NCOL = 128;         // accumulator columns (MMA N)
-constexpr int NTHR = 256;        // warps 0-3 build the A rows, warps 4-7 the B rows
+constexpr int NPROD = 256;        // producers: warps 0-3 build the A rows, warps 4-7 the B rows
+constexpr int NTHR = NPROD + 32;  // + the MMA warp (warp 8)
+constexpr int NSTAGE = 3;
 constexpr uint32_t PLANE = NROW * KC * 2;              // bytes of one sliced plane (A or B)
 constexpr uint32_t STAGE = 8 * PLANE;                  // A planes 0..3, B planes 4..7
-constexpr size_t SMEM = 2 * (size_t)STAGE + 64;
-
-// products (s_a, s_b) by level: level 0 = [0], 1 = [1, 3), 2 = [3, 6), 3 = [6, 10)
-__constant__ int kSa[10] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3};
-__constant__ int kSb[10] = {0, 1, 0, 2, 1, 0, 3, 2, 1, 0};
+constexpr size_t SMEM = NSTAGE * (size_t)STAGE + 128;
 
 __device__ __forceinline__ uint32_t core_off(int row, int k) {
     return (uint32_t)((((row >> 3) * (KC / 8) + (k >> 3)) << 7) + ((row & 7) << 4) + ((k & 7) << 1));
@@ -119,11 +117,16 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
     const int64_t pair0 = (int64_t)blockIdx.x * NPAIR;
     if (pair0 >= npairs) return;
     const int u = blockIdx.z;
-    const int tid = threadIdx.x, warp = tid >> 5;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const bool prod = tid < NPROD;
     const bool abuild = tid < NROW;          // warps 0-3: A row tid; warps 4-7: B row tid - 128
     const int ti = tid & (NROW - 1);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + 2 * STAGE);
-    uint32_t *slot = reinterpret_cast<uint32_t *>(bars + 2);
+    // barriers: full[s] (8 producer warps), empty[s] (MMA commit), done (all MMAs)
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + NSTAGE * STAGE);
+    uint64_t *empty = full + NSTAGE;
+    uint64_t *done = empty + NSTAGE;
+    uint32_t *slot = reinterpret_cast<uint32_t *>(done + 1);
+    int *bad = reinterpret_cast<int *>(slot + 1);
 
     // ring class: all rows share n, the phase type and the table
     const int ring0 = cls_rings[rb];
@@ -164,8 +167,12 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
+        for (int i = 0; i < NSTAGE; ++i) {
+            mbar_init(&full[i], NPROD / 32);
+            mbar_init(&empty[i], 1);
+        }
+        mbar_init(done, 1);
+        *bad = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     fence_before();
@@ -174,101 +181,111 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
     const uint32_t tmem = *slot;
     const uint32_t idesc = idesc_bf16(NROW, NCOL);
 
-    // raw map values of the next chunk (n is a multiple of 4, ring starts are 16-byte aligned)
-    float4 pre[8];
-    auto load_chunk = [&](int kc) {
+    if (!prod) {
+        // MMA warp: per chunk wait for both operand halves, issue the ten level products of its two K steps
+        if (lane == 0) {
+            int issued = 0;
+            for (int kc = 0; kc < nch; ++kc) {
+                const int st = kc % NSTAGE;
+                if (*(volatile int *)bad) break;
+                if (!mbar_wait(&full[st], (uint32_t)((kc / NSTAGE) & 1))) {
+                    atomicExch(bad, 1);
+                    break;
+                }
+                fence_after();
+                const uint32_t base = smem_u32(smem + st * STAGE);
+                const uint32_t sbo = (KC / 8) * 128;
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            const int j = kc * KC + 4 * i;
-            pre[i] = (live && j < n) ? *reinterpret_cast<const float4 *>(x + j) : make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-    };
-    if (abuild) load_chunk(0);
-
-    bool ok = true;
-    int issued = 0;                 // chunks whose MMAs were committed
-    for (int kc = 0; kc < nch; ++kc) {
-        const int st = kc & 1;
-        if (kc >= 2) {
-            // stage st is free once the MMAs of chunk kc-2 completed
-            if (!mbar_wait(&bars[st], (uint32_t)(((kc - 2) >> 1) & 1))) ok = false;
-            fence_after();
-        }
-        ok = __syncthreads_and(ok);
-        if (!ok) break;
-        unsigned char *sbase = smem + st * STAGE;         // A planes 0..3, B planes 4..7
-        const int j0 = kc * KC;
-        if (abuild) {
-            // A row: 32 pixels as 4 groups of 8
+                for (int ks = 0; ks < KC / 16; ++ks) {
 #pragma unroll
-            for (int gq = 0; gq < 4; ++gq) {
-                const float v[8] = {pre[2 * gq].x, pre[2 * gq].y, pre[2 * gq].z, pre[2 * gq].w,
-                                    pre[2 * gq + 1].x, pre[2 * gq + 1].y, pre[2 * gq + 1].z, pre[2 * gq + 1].w};
-                uint32_t w[4][4];
-                slice8(v, C, w);
-                const uint32_t off = core_off(ti, 8 * gq);
-#pragma unroll
-                for (int s = 0; s < 4; ++s) st_shared_v4(sbase + s * PLANE + off, w[s]);
+                    for (int p = 0; p < 10; ++p) {
+                        const bool first = kc == 0 && ks == 0 && lvl_first(p);
+                        mma_bf16(tmem + (uint32_t)(128 * lvl_of(p)),
+                                 smem_desc(base + lvl_a(p) * PLANE + ks * 256, 128, sbo),
+                                 smem_desc(base + (4 + lvl_b(p)) * PLANE + ks * 256, 128, sbo), idesc,
+                                 first ? 0u : 1u);
+                    }
+                }
+                mma_commit(&empty[st]);
+                ++issued;
             }
-        } else {
-        // B row: table slices at k = m (2 j + t) + part n/2 (mod 2n)
+            mma_commit(done);
+            if (issued != nch) atomicExch(bad, 1);
+        }
+    } else {
+        // raw map values of the next chunk (n is a multiple of 4, ring starts are 16-byte aligned)
+        float4 pre[8];
+        auto load_chunk = [&](int kc) {
 #pragma unroll
-        for (int gq = 0; gq < 4; ++gq) {
-            uint32_t w[4][4];
-#pragma unroll
-            for (int t = 0; t < 8; t += 2) {
-                const int j = j0 + 8 * gq + t;
-                uint2 e0 = make_uint2(0u, 0u), e1 = make_uint2(0u, 0u);
-                if (mok && j < n) e0 = T[kidx];
-                kidx += step;
-                if (kidx >= n2) kidx -= n2;
-                if (mok && j + 1 < n) e1 = T[kidx];
-                kidx += step;
-                if (kidx >= n2) kidx -= n2;
-                // e.x = slices 0 | 1 << 16, e.y = slices 2 | 3 << 16
-                w[0][t >> 1] = (e0.x & 0xffffu) | (e1.x << 16);
-                w[1][t >> 1] = (e0.x >> 16) | (e1.x & 0xffff0000u);
-                w[2][t >> 1] = (e0.y & 0xffffu) | (e1.y << 16);
-                w[3][t >> 1] = (e0.y >> 16) | (e1.y & 0xffff0000u);
+            for (int i = 0; i < 8; ++i) {
+                const int j = kc * KC + 4 * i;
+                pre[i] = (live && j < n) ? *reinterpret_cast<const float4 *>(x + j) : make_float4(0.f, 0.f, 0.f, 0.f);
             }
-            const uint32_t off = core_off(ti, 8 * gq);
-#pragma unroll
-            for (int s = 0; s < 4; ++s) st_shared_v4(sbase + (4 + s) * PLANE + off, w[s]);
-        }
-        }
-        fence_proxy_async();
-        __syncthreads();
-        if (tid == 0) {
-            fence_after();
-            const uint32_t base = smem_u32(sbase);
-            const uint32_t sbo = (KC / 8) * 128;
-#pragma unroll
-            for (int s = 0; s < KC / 16; ++s) {
-                const bool first = kc == 0 && s == 0;
-#pragma unroll
-                for (int p = 0; p < 10; ++p) {
-                    const int lvl = p == 0 ? 0 : (p < 3 ? 1 : (p < 6 ? 2 : 3));
-                    const bool lead = p == 0 || p == 1 || p == 3 || p == 6;     // first product of its level
-                    mma_bf16(tmem + (uint32_t)(128 * lvl), smem_desc(base + kSa[p] * PLANE + s * 256, 128, sbo),
-                             smem_desc(base + (4 + kSb[p]) * PLANE + s * 256, 128, sbo), idesc,
-                             (first && lead) ? 0u : 1u);
+        };
+        if (abuild) load_chunk(0);
+        for (int kc = 0; kc < nch; ++kc) {
+            const int st = kc % NSTAGE;
+            if (kc >= NSTAGE) {
+                // the stage is free once the MMAs of chunk kc - NSTAGE completed
+                if (*(volatile int *)bad) break;
+                if (!mbar_wait(&empty[st], (uint32_t)(((kc / NSTAGE) - 1) & 1))) {
+                    atomicExch(bad, 1);
+                    break;
                 }
             }
-            mma_commit(&bars[st]);
+            unsigned char *sbase = smem + st * STAGE;         // A planes 0..3, B planes 4..7
+            const int j0 = kc * KC;
+            if (abuild) {
+                // A row: 32 pixels as 4 groups of 8
+#pragma unroll
+                for (int gq = 0; gq < 4; ++gq) {
+                    const float v[8] = {pre[2 * gq].x, pre[2 * gq].y, pre[2 * gq].z, pre[2 * gq].w,
+                                        pre[2 * gq + 1].x, pre[2 * gq + 1].y, pre[2 * gq + 1].z, pre[2 * gq + 1].w};
+                    uint32_t w[4][4];
+                    slice8(v, C, w);
+                    const uint32_t off = core_off(ti, 8 * gq);
+#pragma unroll
+                    for (int s = 0; s < 4; ++s) st_shared_v4(sbase + s * PLANE + off, w[s]);
+                }
+                if (kc + 1 < nch) load_chunk(kc + 1);
+            } else {
+                // B row: table slices at k = m (2 j + t) + part n/2 (mod 2n)
+#pragma unroll
+                for (int gq = 0; gq < 4; ++gq) {
+                    uint32_t w[4][4];
+#pragma unroll
+                    for (int t = 0; t < 8; t += 2) {
+                        const int j = j0 + 8 * gq + t;
+                        uint2 e0 = make_uint2(0u, 0u), e1 = make_uint2(0u, 0u);
+                        if (mok && j < n) e0 = T[kidx];
+                        kidx += step;
+                        if (kidx >= n2) kidx -= n2;
+                        if (mok && j + 1 < n) e1 = T[kidx];
+                        kidx += step;
+                        if (kidx >= n2) kidx -= n2;
+                        // e.x = slices 0 | 1 << 16, e.y = slices 2 | 3 << 16
+                        w[0][t >> 1] = (e0.x & 0xffffu) | (e1.x << 16);
+                        w[1][t >> 1] = (e0.x >> 16) | (e1.x & 0xffff0000u);
+                        w[2][t >> 1] = (e0.y & 0xffffu) | (e1.y << 16);
+                        w[3][t >> 1] = (e0.y >> 16) | (e1.y & 0xffff0000u);
+                    }
+                    const uint32_t off = core_off(ti, 8 * gq);
+#pragma unroll
+                    for (int s = 0; s < 4; ++s) st_shared_v4(sbase + (4 + s) * PLANE + off, w[s]);
+                }
+            }
+            fence_proxy_async();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&full[st]);      // one arrival per producer warp
         }
-        ++issued;
-        if (abuild && kc + 1 < nch) load_chunk(kc + 1);
     }
-    // all committed MMAs must be complete before TMEM is read or released
-    if (issued > 0) {
-        const int last = issued - 1;
-        if (!mbar_wait(&bars[last & 1], (uint32_t)((last >> 1) & 1))) ok = false;
-    }
+    // all MMAs complete before TMEM is read or released
+    bool ok = mbar_wait(done, 0);
     fence_after();
-    ok = __syncthreads_and(ok);
+    ok = __syncthreads_and(ok) && !*(volatile int *)bad;
     if (!ok) {
         if (tid == 0) atomicOr(err, ERR_TC_TIMEOUT);
-    } else {
+    } else if (prod) {
         // epilogue: per row, lead = level 0 (exact) and rest = level 1 + (level 2 + level 3).  Warps w and
         // w + 4 read the same TMEM lanes (rows) and the column groups cg = it and 4 + it; rows exchange through
         // shared memory; then thread t writes, for column group (t / 128) * 4 + it, F+ (t % 128 < 64) or
@@ -280,7 +297,6 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
         const int pr = ti & (NPAIR - 1);
         const int sg = ti >> 6;
         const float sgn = sg ? -1.0f : 1.0f;
-        // the output pair of this thread (pair pr of the tile)
         const int64_t qo = pair0 + pr;
         const bool ook = qo < npairs;
         int oring = ring0;
@@ -303,7 +319,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
                 xh[(2 * i) * NROW + ti] = v0[i];
                 xh[(2 * i + 1) * NROW + ti] = v1[i] + (v2[i] + v3[i]);
             }
-            __syncthreads();
+            asm volatile("bar.sync 1, %0;" ::"r"(NPROD) : "memory");     // producer warps only
             if (ook) {
 #pragma unroll
                 for (int t = 0; t < 8; ++t) {
@@ -311,19 +327,19 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
                     if (mm > lmax) break;
                     float f[2];
 #pragma unroll
-                    for (int c = 0; c < 2; ++c) {
-                        const int i = 2 * t + c;
+                    for (int c2 = 0; c2 < 2; ++c2) {
+                        const int i = 2 * t + c2;
                         const float a = xh[(2 * i) * NROW + pr], bb = sgn * xh[(2 * i) * NROW + pr + NPAIR];
                         const float s = a + bb;
                         const float z = s - a;
                         const float e = (a - (s - z)) + (bb - z);
-                        f[c] = s + ((xh[(2 * i + 1) * NROW + pr] + sgn * xh[(2 * i + 1) * NROW + pr + NPAIR]) + e);
+                        f[c2] = s + ((xh[(2 * i + 1) * NROW + pr] + sgn * xh[(2 * i + 1) * NROW + pr + NPAIR]) + e);
                     }
                     *reinterpret_cast<float2 *>(F + ((int64_t)(sg * L1 + mm) * nrn + oring) * ldF + 2 * ob) =
                         make_float2(f[0], f[1]);
                 }
             }
-            __syncthreads();
+            asm volatile("bar.sync 1, %0;" ::"r"(NPROD) : "memory");
         }
     }
     fence_before();

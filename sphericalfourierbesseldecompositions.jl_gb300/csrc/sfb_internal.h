@@ -111,6 +111,7 @@ struct Plan {
     int32_t *d_out_pair = nullptr;  // [nlmsize] pair index of each a_nlm
     int32_t *d_out_lm = nullptr;    // [nlmsize] l(l+1)/2+m of each a_nlm
     double *d_coef = nullptr;       // [npairs * nbasis] radial coefficients (poly mode)
+    float2 *d_coefT = nullptr;      // [(lmax+1) * nbasis * nmax] the same as double-float, per l and basis
     int *d_err = nullptr;           // device error word
     // workspaces (grow on demand)
     DevBuf<double> maps;            // [nmaps_alloc * npix]
@@ -153,6 +154,13 @@ int deposit_sorted(Plan &p, const double *rtp, const double *w, int64_t ngal, do
 // also A[lm][2 set_col + c] = rset[lm * ldr + c].
 void launch_add_mean(double *A, int64_t ldA, int64_t nmaps, const double *mu, const double *rmu, const double *rset,
                      int64_t ldr, int64_t lmsize, int64_t set_col, cudaStream_t st);
+// Mixed-precision radial projection (double-float sums; FP64 mean and window
+// terms), replacing add_mean + project_poly for the data term.
+void launch_coef_df(const Plan &p, const int32_t *pair_index, float2 *CT, cudaStream_t st);
+void launch_project_mixed(const Plan &p, const float2 *Adf, int64_t ldA, const float2 *CT,
+                          const int64_t *noff, const int32_t *pair_index, double scale, const double *mu,
+                          double *smean, const double *ralm, int window_kind, const double *w_ln, double *out,
+                          cudaStream_t st);
 // maps[j] -= nu[j] ref with nu[j] = <maps[j], ref> / <ref, ref> (FP64, in place).
 void launch_split_mean(double *maps, int64_t nmaps, int64_t npix, const double *ref, double *nu, cudaStream_t st);
 void launch_ring_analysis(const Plan &p, const double *maps, int64_t nmaps, double *F, cudaStream_t st);
@@ -160,8 +168,8 @@ void launch_ring_synthesis(const Plan &p, const double *G, int64_t nmaps, double
 void launch_leg_analysis(const Plan &p, const double *F, int64_t ncol, double *A, bool accumulate,
                          cudaStream_t st);
 void launch_leg_synthesis(const Plan &p, const double *A, int64_t ncol, double *G, cudaStream_t st);
-void launch_fold_residual(const Plan &p, const double *F, const double *G, int64_t ncol, double *R,
-                          cudaStream_t st);
+void launch_fold_residual(const Plan &p, const double *F, const double *G, int64_t ncol, double *R, cudaStream_t st,
+                          int *Ecol = nullptr);
 void launch_radial_coeffs(const Plan &p, const double *gl_x, const double *pq, int Q, double *coef,
                           cudaStream_t st);
 void launch_project_poly(const Plan &p, const double *A, int64_t ldA, double scale, int window_kind,
@@ -174,8 +182,9 @@ uint2 dft_slices(double v, int EB);
 // tensor-core (tcgen05) Legendre analysis, mixed precision
 int64_t tc_table_offsets(const Plan &p, std::vector<int64_t> &off);
 void launch_build_lamtc(const Plan &p, const int *Ea, const int *Es, cudaStream_t st);
+// Ecol: column scales of F; computed here unless scales_ready (the fold wrote them).
 void launch_leg_analysis_tc(const Plan &p, const float *F, int64_t ncol, double *A, float2 *Adf, int *Ecol,
-                            bool accumulate, cudaStream_t st);
+                            bool accumulate, cudaStream_t st, bool scales_ready = false);
 int64_t tc_synth_table_offsets(const Plan &p, std::vector<int64_t> &off);
 void launch_build_lamts(const Plan &p, const int *Es, cudaStream_t st);
 void launch_leg_synthesis_tc(const Plan &p, const float2 *Adf, int64_t ncol, float *G, cudaStream_t st);
@@ -223,6 +232,64 @@ __device__ __forceinline__ int64_t ang2pix_ring_z(int64_t nside, double z, doubl
     ip = ip % (4 * ir);
     if (z > 0) return 2 * ir * (ir - 1) + ip;
     return 12 * ns * ns - 2 * ir * (ir + 1) + ip;
+}
+
+// ang2pix_ring_z(nside, cos(th), ph) with the result taken from an FP32
+// evaluation whenever it provably agrees: every quantity that is floored
+// (tt, jp/jm arguments, ip argument) must lie farther than `margin` from an
+// integer, and |z| farther than 1e-5 from 2/3.  The FP32 errors are bounded
+// by about nside * 1.6e-6 (theta and phi rounded to FP32: 6e-8 relative;
+// sincosf / products / fmodf: a few ulp; |phi| <= 4 pi), so margin =
+// nside * 4e-6 + 1e-6 leaves a factor 2.5; 1 - |z| is formed as
+// 2 sin^2(theta/2) (or 2 cos^2) to keep its relative accuracy near the
+// poles.  Otherwise the FP64 path runs, so the pixel is bit-identical to
+// ang2pix_ring_z.
+__device__ __forceinline__ int64_t ang2pix_ring_fast(int64_t nside, double th, double ph) {
+    if (nside <= (int64_t(1) << 16) && fabs(ph) <= 4.0 * M_PI) {
+        const float ns = (float)nside;
+        const float margin = ns * 4e-6f + 1e-6f;
+        auto far = [margin](float v) {
+            const float f = v - floorf(v);
+            return f > margin && f < 1.0f - margin;
+        };
+        const float th32 = (float)th;
+        float sn, cs;
+        sincosf(th32, &sn, &cs);
+        const float z = cs, za = fabsf(z);
+        float tt = fmodf((float)ph * 0.636619772f, 4.0f);
+        if (tt < 0.0f) tt += 4.0f;
+        if (fabsf(za - 0.6666667f) > 1e-5f && far(tt) && tt < 4.0f - margin) {
+            if (za < 0.6666667f) {
+                const float temp1 = ns * (0.5f + tt), temp2 = ns * z * 0.75f;
+                const float a = temp1 - temp2, b = temp1 + temp2;
+                if (far(a) && far(b)) {
+                    const int64_t jp = (int64_t)floorf(a), jm = (int64_t)floorf(b);
+                    const int64_t ir = nside + 1 + jp - jm;
+                    const int64_t kshift = 1 - (ir & 1);
+                    const int64_t t1 = jp + jm - nside + kshift + 1 + 8 * nside;
+                    const int64_t ip = (t1 >> 1) % (4 * nside);
+                    const int64_t pix = 2 * nside * (nside - 1) + (ir - 1) * 4 * nside + ip;
+                    if (pix >= 0 && pix < 12 * nside * nside) return pix;
+                }
+            } else {
+                float sh, ch;
+                sincosf(0.5f * th32, &sh, &ch);
+                const float omz = 2.0f * (z > 0.0f ? sh * sh : ch * ch);      // 1 - |z|
+                const float tp = tt - floorf(tt);
+                const float tmp = ns * sqrtf(3.0f * omz);
+                const float a = tp * tmp, b = (1.0f - tp) * tmp;
+                if (far(a) && far(b)) {
+                    const int64_t ir = (int64_t)floorf(a) + (int64_t)floorf(b) + 1;
+                    const float q = tt * (float)ir;
+                    if (far(q)) {
+                        const int64_t ip = (int64_t)floorf(q) % (4 * ir);
+                        return z > 0.0f ? 2 * ir * (ir - 1) + ip : 12 * nside * nside - 2 * ir * (ir + 1) + ip;
+                    }
+                }
+            }
+        }
+    }
+    return ang2pix_ring_z(nside, cos(th), ph);
 }
 
 // Cubic spline with boundary extrapolation on knots x[0..N-1]

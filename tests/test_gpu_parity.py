@@ -28,6 +28,41 @@ def small():
 
 
 # ---------------------------------------------------------------- HEALPix ----
+def _near_boundaries(nside, rng, n=20_000):
+    """Directions placed within +-1e-9 .. 1e-3 (in units of the floored
+    quantities) of pixel edges: both edge families of the equatorial belt,
+    the polar edges, |z| = 2/3 and quadrant edges of phi."""
+    ns = float(nside)
+    d = rng.choice([1e-9, -1e-9, 1e-6, -1e-6, 1e-4, -1e-4, 1e-3, -1e-3], n)
+    out_th, out_ph = [], []
+    # equatorial: ns (0.5 + tt) -+ 0.75 ns z = k + d
+    z = rng.uniform(-0.66, 0.66, n)
+    sgn = rng.choice([-1.0, 1.0], n)
+    k = np.floor(ns * (0.5 + rng.uniform(0, 4, n)) - sgn * 0.75 * ns * z)
+    tt = (k + d + sgn * 0.75 * ns * z) / ns - 0.5
+    ok = (tt >= 0) & (tt < 4)
+    out_th.append(np.arccos(z[ok]))
+    out_ph.append(tt[ok] * np.pi / 2)
+    # polar: tp * tmp = k + d (and (1 - tp) * tmp = k + d)
+    za = rng.uniform(0.67, 0.9999, n)
+    tmp = ns * np.sqrt(3 * (1 - za))
+    k = np.floor(rng.uniform(0, 1, n) * tmp)
+    tp = (k + d) / tmp
+    tp = np.where(rng.random(n) < 0.5, tp, 1 - tp)
+    ok = (tp > 0) & (tp < 1)
+    q = rng.integers(0, 4, n)
+    zz = np.where(rng.random(n) < 0.5, za, -za)
+    out_th.append(np.arccos(zz[ok]))
+    out_ph.append((q[ok] + tp[ok]) * np.pi / 2)
+    # |z| = 2/3 and quadrant edges of phi
+    out_th.append(np.arccos(np.array([2 / 3 + 1e-9, 2 / 3 - 1e-9, -2 / 3 + 1e-9, -2 / 3 - 1e-9, 2 / 3, -2 / 3])))
+    out_ph.append(np.array([0.1, 1.0, 2.0, 3.0, 4.0, 5.0]))
+    e = rng.uniform(0.1, 3.0, 400)
+    out_th.append(e)
+    out_ph.append(np.repeat([np.pi / 2, np.pi, 3 * np.pi / 2, 2 * np.pi], 100) + np.tile([1e-12, -1e-12, 1e-7, -1e-7], 100))
+    return np.concatenate(out_th), np.concatenate(out_ph)
+
+
 @pytest.mark.parametrize("nside", [1, 2, 7, 32, 256, 1024])
 def test_ang2pix_bit_exact(nside):
     rng = np.random.default_rng(nside)
@@ -39,8 +74,9 @@ def test_ang2pix_bit_exact(nside):
     cth, cph = ohp.pix2ang_ring(nside, np.arange(min(12 * nside * nside, 50_000)))
     edge_th = np.array([0.0, np.pi, np.pi / 2, 1e-12, np.pi - 1e-12, 0.0, np.pi / 2])
     edge_ph = np.array([0.0, 2 * np.pi, -1e-15, np.pi / 2, 2 * np.pi - 1e-15, 1e300, -7.0])
-    th = np.concatenate([th, cth, edge_th])
-    ph = np.concatenate([ph, cph, edge_ph])
+    bth, bph = _near_boundaries(nside, rng)
+    th = np.concatenate([th, cth, edge_th, bth])
+    ph = np.concatenate([ph, cph, edge_ph, bph])
     gpu = sfbgpu.ang2pix_ring(nside, th, ph)
     ref = ohp.ang2pix_ring(nside, th, ph)
     assert np.all((gpu >= 0) & (gpu < 12 * nside * nside))
