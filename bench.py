@@ -88,7 +88,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + ",".join(self.FIELDS),
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -204,34 +204,35 @@ def run_reference_sample(amodes, gal, w, nbar, mask, wln_arr, steps, warmup, wor
 
 # ----------------------------------------------------------------------------- GPU arm
 def stage_work(stage, precision, nm, ngal, nbasis, niter=3, lmax=238):
-    """Algorithmic work of ONE STEP of a stage: (kind, amount).
+    """Algorithmic work of ONE STEP of a stage: (kind, amount), by the counts
+    of the path's scope table (the N/S ring symmetry and the ten-product
+    slicing are implementation choices and do not change the counts):
 
-    leg_analysis / leg_synthesis: 2 flop per (l, m, north ring, real column)
-    and pass -- the ring sum over the 2*nside north rings (the N/S symmetry is
-    part of the algorithm); 1 + niter analysis passes, niter synthesis passes.
-    ring_fft: mixed precision computes the ring transform for m <= lmax as a
-    tensor-core DFT, 4 flop per (pixel, m, map) (a cos and a sin multiply-add);
-    FP64 runs an FFT, counted as maps read + ring spectra written.
-    fold: F, G read + R written per pass.  deposit: galaxy records read +
-    basis maps written."""
+    leg_analysis / leg_synthesis: 2 (complex) x 2 (multiply-add) flop per
+    (ring of all 4 nside - 1, (l, m) with m <= l, map) and pass; 1 + niter
+    analysis passes, niter synthesis passes.
+    ring_fft: maps read + ring spectra written, nm npix b + nm n_ring (lmax+1)
+    2 b bytes (b = 4 mixed, 8 FP64); the mixed path computes it as a
+    tensor-core DFT, whose 4 flop per (pixel, m, map) is reported beside.
+    fold: F, G read + R written per pass.  deposit: 40 B per galaxy (record
+    read + binning update) + the basis maps written."""
     lmsize = (lmax + 1) * (lmax + 2) // 2
     nrn = 2 * NSIDE
+    n_ring = 4 * NSIDE - 1
     npix = 12 * NSIDE ** 2
     ncol = 2 * nm
     t = 4 if precision == "mixed" else 8
     fsz = 2 * (lmax + 1) * nrn * ncol * t
     if stage == "leg_analysis":
-        return ("flop", (1 + niter) * 2.0 * lmsize * nrn * ncol)
+        return ("flop", (1 + niter) * 4.0 * n_ring * lmsize * nm)
     if stage == "leg_synthesis":
-        return ("flop", niter * 2.0 * lmsize * nrn * ncol)
+        return ("flop", niter * 4.0 * n_ring * lmsize * nm)
     if stage == "ring_fft":
-        if precision == "mixed":
-            return ("flop", 4.0 * nm * npix * (lmax + 1))
-        return ("byte", float(t) * nm * npix + fsz)
+        return ("byte", float(t) * nm * npix + float(nm) * n_ring * (lmax + 1) * 2 * t)
     if stage == "fold":
         return ("byte", niter * 3.0 * fsz)
     if stage == "deposit":
-        return ("byte", 32.0 * ngal + float(t) * nbasis * npix)
+        return ("byte", 40.0 * ngal + float(t) * nbasis * npix)
     return ("byte", None)
 
 
@@ -267,6 +268,13 @@ def roofline_table(stages, precision, nm, ngal, nbasis, peaks, fp64_peak):
             out[st] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                        "per_step": amount, "ms_per_step": ms,
                        "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback"}
+            if st == "ring_fft" and precision == "mixed":
+                lmax = 238
+                dft = 4.0 * nm * 12 * NSIDE ** 2 * (lmax + 1)
+                tp = peaks.get("bf16_tflops_sustained", 1700.0)
+                tach = dft / (ms * 1e-3) / 1e12
+                out[st]["tensor_view"] = {"dft_flop_per_step": dft, "achieved_tflops": tach,
+                                          "frac_of_bf16_sustained": tach / tp, "bf16_issued_frac": 10 * tach / tp}
     return out
 
 
@@ -292,7 +300,7 @@ def fp64_gemm_peak(torch):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])

@@ -167,4 +167,40 @@ function win_rhat_ln(win, wmodes, amodes; kw...)
     return W
 end
 
+"""
+    amln2clnn(anlm, cmodes)    (src/SphericalFourierBesselDecompositions.jl:133-150)
+
+Pseudo-SFB power spectrum C_l(n1, n2) in the order of `cmodes.lnn` (3 × nlnn);
+`anlm` is one a_nlm vector or a matrix of them (one per column).
+"""
+function amln2clnn(anlm, cmodes; kw...)
+    amodes = cmodes.amodesA
+    p = getplan(amodes; kw...)
+    a = Matrix{ComplexF64}(reshape(anlm, p.nlmsize, :))
+    nbatch = size(a, 2)
+    lnn = Matrix{Int64}(cmodes.lnn)
+    nlnn = size(lnn, 2)
+    out = Matrix{Float64}(undef, nlnn, nbatch)
+    GC.@preserve a lnn out check(ccall((:sfb_amln2clnn, libsfb), Cint,
+                                       (Ptr{Cvoid}, Ptr{ComplexF64}, Ptr{ComplexF64}, Int64, Ptr{Int64}, Int64,
+                                        Ptr{Float64}),
+                                       p.handle, a, C_NULL, nbatch, lnn, nlnn, out))
+    return nbatch == 1 ? vec(out) : out
+end
+
+"""
+    winweights2galweights(weights, wmodes, rθϕ)    (src/cat2anlm.jl:218-238)
+"""
+function winweights2galweights(weights, wmodes, rθϕ)
+    W = Matrix{Float64}(weights)              # nr × npix
+    rb = Vector{Float64}(SFB.get_rbounds(wmodes))
+    r = Matrix{Float64}(rθϕ)
+    out = Vector{Float64}(undef, size(r, 2))
+    GC.@preserve W rb r out check(ccall((:sfb_winweights2galweights, libsfb), Cint,
+                                        (Int64, Ptr{Float64}, Int64, Ptr{Float64}, Ptr{Float64}, Int64,
+                                         Ptr{Float64}),
+                                        wmodes.nside, W, wmodes.nr, rb, r, size(r, 2), out))
+    return out
+end
+
 end # module
