@@ -25,6 +25,8 @@
 // (a pixelised mask misses the partly covered boundary pixels).  The FP32
 // rounding then scales with the fluctuation, not with the mean density that
 // the window term later cancels.
+#include <algorithm>
+
 #include "sfb_internal.h"
 
 namespace sfb {
@@ -404,7 +406,8 @@ static void launch_stats(const Plan &p, const int32_t *counts, const double2 *so
 }
 
 int deposit_sorted(Plan &p, const double *rtp, const double *w, int64_t ngal, double *maps, double *ref,
-                   double *mu, cudaEvent_t ref_ready, cudaStream_t st) {
+                   double *mu, cudaEvent_t ref_ready, cudaStream_t st, const cudaEvent_t *chunk_ready,
+                   int nchunks) {
     const int64_t nkeys = (int64_t)(p.pieces + 2) * p.npix;
     const int64_t nscan = nkeys + 1;            // one extra counter: its exclusive prefix is the total
     const int64_t ntiles = (nscan + SCAN_TILE - 1) / SCAN_TILE;
@@ -423,9 +426,16 @@ int deposit_sorted(Plan &p, const double *rtp, const double *w, int64_t ngal, do
     double *xloc = p.dep.ptr + off_x;
     double2 *sorted = reinterpret_cast<double2 *>(p.dep.ptr + off_sorted);
     SFB_CUDA_TRY(cudaMemsetAsync(counts, 0, (size_t)nscan * sizeof(int32_t), st));
-    if (ngal > 0) {
-        k_deposit_keys<<<(unsigned)((ngal + 255) / 256), 256, 0, st>>>(rtp, w, ngal, p.nside, p.npix, p.rmin, p.rmax,
-                                                                       p.pieces, counts, key, rank, xloc, p.d_err);
+    // keys: in nchunks galaxy ranges, each after its event (the host entry's copy pipeline), or at once
+    const int nck = (chunk_ready && nchunks > 0) ? nchunks : 1;
+    const int64_t per = (ngal + nck - 1) / nck;
+    for (int c = 0; c < nck; ++c) {
+        const int64_t g0 = c * per, n = std::min<int64_t>(per, ngal - g0);
+        if (chunk_ready && nchunks > 0) SFB_CUDA_TRY(cudaStreamWaitEvent(st, chunk_ready[c], 0));
+        if (n <= 0) continue;
+        k_deposit_keys<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(rtp + 3 * g0, w ? w + g0 : nullptr, n, p.nside,
+                                                                    p.npix, p.rmin, p.rmax, p.pieces, counts, key + g0,
+                                                                    rank + g0, xloc + g0, p.d_err);
         note_launch();
     }
     k_scan_tiles<<<(unsigned)ntiles, SCAN_THREADS, 0, st>>>(counts, nscan, tsum);

@@ -2,6 +2,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -94,6 +95,9 @@ struct sfb_plan {
     // forked / joined with the call's stream through events
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // host entry: the catalogue copy runs on the side stream in NCOPY chunks
+    static constexpr int NCOPY = 4;
+    cudaEvent_t ev_copy[NCOPY] = {};
     int32_t *d_pair_index = nullptr;
     int64_t *d_noff = nullptr;
     // stage profiling (events on the call's stream)
@@ -395,7 +399,7 @@ int64_t chunk_pairs(const Plan &p) {
 }
 
 int cat2amln_dev(sfb_plan *h, const double *rtp, const double *w, int64_t ngal, double nbar, const sfb_window *win,
-                 double *out, cudaStream_t st) {
+                 double *out, cudaStream_t st, const cudaEvent_t *chunk_ready = nullptr, int nchunks = 0) {
     Plan &p = h->p;
     if (ngal < 0) return fail(SFB_EINVAL, "ngal < 0");
     if (!win) return fail(SFB_EINVAL, "window descriptor is NULL");
@@ -442,7 +446,8 @@ int cat2amln_dev(sfb_plan *h, const double *rtp, const double *w, int64_t ngal, 
         }
         {
             Stage s(h, SFB_STAGE_DEPOSIT, st);
-            SFB_TRY(deposit_sorted(p, rtp, w, ngal, p.maps.ptr, Cmap, mu, split ? h->ev_fork : nullptr, st));
+            SFB_TRY(deposit_sorted(p, rtp, w, ngal, p.maps.ptr, Cmap, mu, split ? h->ev_fork : nullptr, st,
+                                   chunk_ready, nchunks));
         }
         if (split) {
             // the FP64 transform of (C, W01) runs on the side stream while the deposit's moments finish
@@ -473,6 +478,8 @@ int cat2amln_dev(sfb_plan *h, const double *rtp, const double *w, int64_t ngal, 
             }
         }
     } else {
+        // the spline deposit reads the whole catalogue: wait for every chunk of the copy
+        for (int c = 0; chunk_ready && c < nchunks; ++c) SFB_CUDA_TRY(cudaStreamWaitEvent(st, chunk_ready[c], 0));
         // reference order: map = sum w g / (nbar dOmega) - W[:, l, n], then map2alm, keep row l
         const int64_t cp = chunk_pairs(p);
         SFB_TRY(grow(p, p.maps, (size_t)cp * p.npix));
@@ -612,7 +619,12 @@ int sfb_plan_create(const sfb_plan_desc *d, sfb_plan **out) {
         if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
             cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking) != cudaSuccess ||
             cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+            cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+            [&] {
+                for (auto &e : h->ev_copy)
+                    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return true;
+                return false;
+            }()) {
             cudaGetLastError();
             st = fail(SFB_ECUDA, "stream creation failed");
             break;
@@ -701,6 +713,25 @@ int sfb_plan_create(const sfb_plan_desc *d, sfb_plan **out) {
             if ((st = upload(p, &p.d_dtw_off, doff.data(), doff.size())) != SFB_OK) break;
             if ((st = upload(p, &p.d_cls_rings, crings.data(), crings.size())) != SFB_OK) break;
             if ((st = upload(p, &p.d_cls_off, coff.data(), coff.size())) != SFB_OK) break;
+            // B operand image: the polar classes too while the whole image stays under
+            // SFBGPU_DFT_IMAGE_MAX_BYTES (default 2 GiB; the equatorial classes are always imaged)
+            {
+                int64_t IMG_BUDGET = 1LL << 31;
+                if (const char *e = std::getenv("SFBGPU_DFT_IMAGE_MAX_BYTES")) IMG_BUDGET = std::atoll(e);
+                constexpr int64_t CHUNK_BYTES = 32768;
+                std::vector<int64_t> ioff;
+                int max_nch = 1;
+                p.dtimg_polar = true;
+                int64_t nimg = dft_image_offsets(p, crings, coff, true, ioff, max_nch);
+                if (nimg * CHUNK_BYTES > IMG_BUDGET) {
+                    p.dtimg_polar = false;
+                    nimg = dft_image_offsets(p, crings, coff, false, ioff, max_nch);
+                }
+                if ((st = upload(p, &p.d_dtimg_off, ioff.data(), ioff.size())) != SFB_OK) break;
+                if ((st = upload<unsigned char>(p, &p.d_dtimg, nullptr, (size_t)(nimg * CHUNK_BYTES))) != SFB_OK)
+                    break;
+                launch_build_dft_image(p, max_nch, h->stream);
+            }
         }
         std::vector<int64_t> lam_off(2 * (p.lmax + 1));
         int64_t off = 0;
@@ -779,7 +810,7 @@ void sfb_plan_destroy(sfb_plan *h) {
     cudaSetDevice(p.device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     void *ptrs[] = {p.d_rings, p.d_twtab, p.d_twoff, p.d_phase, p.d_wphase, p.d_twtab32, p.d_wphase32, p.d_dtw,
-                    p.d_dtw_off, p.d_cls_rings, p.d_cls_off, p.d_lam, p.d_lam32, p.d_lamtc, p.d_lamtc_off, p.d_lamts, p.d_lamts_off, p.d_lam_off, p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp,
+                    p.d_dtw_off, p.d_dtimg, p.d_dtimg_off, p.d_cls_rings, p.d_cls_off, p.d_lam, p.d_lam32, p.d_lamtc, p.d_lamtc_off, p.d_lamts, p.d_lamts_off, p.d_lam_off, p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp,
                     p.d_pair_l, p.d_pair_n, p.d_out_pair, p.d_out_lm, p.d_coef, p.d_coefT, p.d_err,
                     p.maps.ptr, p.fbuf.ptr, p.gbuf.ptr, p.rbuf.ptr, p.alm.ptr, p.scratch.ptr, p.scratch2.ptr, p.dep.ptr, p.maps32.ptr,
                     p.ref.ptr, p.erow.ptr, p.almdf.ptr, h->d_pair_index, h->d_noff};
@@ -791,6 +822,8 @@ void sfb_plan_destroy(sfb_plan *h) {
     if (h->side) cudaStreamDestroy(h->side);
     if (h->ev_fork) cudaEventDestroy(h->ev_fork);
     if (h->ev_join) cudaEventDestroy(h->ev_join);
+    for (auto e : h->ev_copy)
+        if (e) cudaEventDestroy(e);
     delete h;
 }
 
@@ -865,9 +898,24 @@ int sfb_cat2amln(sfb_plan *h, const double *rtp, const double *weight, int64_t n
     double *d_w = weight ? d_rtp + 3 * ngal : nullptr;
     double *d_out = d_rtp + 3 * ngal + (weight ? ngal : 0);
     double *d_win = d_out + 2 * p.nlmsize;
+    // the catalogue goes up in NCOPY galaxy ranges on the side stream; the binning of range c
+    // starts on the call's stream as soon as range c has landed
+    const int ncopy = ngal > 0 ? sfb_plan::NCOPY : 0;
     if (ngal > 0) {
-        SFB_CUDA_TRY(cudaMemcpyAsync(d_rtp, rtp, 3 * ngal * sizeof(double), cudaMemcpyHostToDevice, st));
-        if (weight) SFB_CUDA_TRY(cudaMemcpyAsync(d_w, weight, ngal * sizeof(double), cudaMemcpyHostToDevice, st));
+        SFB_CUDA_TRY(cudaEventRecord(h->ev_join, st));          // inputs are the caller's: order after prior work
+        SFB_CUDA_TRY(cudaStreamWaitEvent(h->side, h->ev_join, 0));
+        const int64_t per = (ngal + ncopy - 1) / ncopy;
+        for (int c = 0; c < ncopy; ++c) {
+            const int64_t g0 = c * per, n = std::min<int64_t>(per, ngal - g0);
+            if (n > 0) {
+                SFB_CUDA_TRY(cudaMemcpyAsync(d_rtp + 3 * g0, rtp + 3 * g0, 3 * n * sizeof(double),
+                                             cudaMemcpyHostToDevice, h->side));
+                if (weight)
+                    SFB_CUDA_TRY(cudaMemcpyAsync(d_w + g0, weight + g0, n * sizeof(double), cudaMemcpyHostToDevice,
+                                                 h->side));
+            }
+            SFB_CUDA_TRY(cudaEventRecord(h->ev_copy[c], h->side));
+        }
     }
     sfb_window dw = *window;
     if (window->kind == SFB_WINDOW_SEPARABLE) {
@@ -882,7 +930,8 @@ int sfb_cat2amln(sfb_plan *h, const double *rtp, const double *weight, int64_t n
         SFB_CUDA_TRY(cudaMemcpyAsync(d_win, window->dense, (size_t)wlen * sizeof(double), cudaMemcpyHostToDevice, st));
         dw.dense = d_win;
     }
-    SFB_TRY(cat2amln_dev(h, ngal > 0 ? d_rtp : nullptr, d_w, ngal, nbar, &dw, d_out, st));
+    SFB_TRY(cat2amln_dev(h, ngal > 0 ? d_rtp : nullptr, d_w, ngal, nbar, &dw, d_out, st, ncopy ? h->ev_copy : nullptr,
+                         ncopy));
     SFB_CUDA_TRY(cudaMemcpyAsync(anlm_out, d_out, 2 * p.nlmsize * sizeof(double), cudaMemcpyDeviceToHost, st));
     SFB_CUDA_TRY(cudaStreamSynchronize(st));
     return SFB_OK;

@@ -103,12 +103,19 @@ __global__ void __launch_bounds__(128) k_ring_rowexp(const float *__restrict__ m
     }
 }
 
+// IMG: the B operand of every chunk comes from the precomputed image (one
+// 32 KB bulk copy per stage, issued by thread 0) and all eight producer warps
+// slice the map rows, two threads per row; otherwise warps 4-7 gather B from
+// the ring's sliced table.
+template <bool IMG>
 __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict__ maps, int64_t npix, int64_t nmaps,
                                                          const RingGeom *__restrict__ rings, int nrn, int lmax,
                                                          const int32_t *__restrict__ cls_rings,
                                                          const int32_t *__restrict__ cls_off,
                                                          const int *__restrict__ erow, const uint2 *__restrict__ dtw,
-                                                         const int64_t *__restrict__ dtw_off, float *__restrict__ F,
+                                                         const int64_t *__restrict__ dtw_off,
+                                                         const unsigned char *__restrict__ img,
+                                                         const int64_t *__restrict__ img_off, float *__restrict__ F,
                                                          int64_t ldF, int *err) {
     extern __shared__ __align__(1024) unsigned char smem[];
     const int cls = blockIdx.y;
@@ -119,9 +126,10 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
     const int u = blockIdx.z;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const bool prod = tid < NPROD;
-    const bool abuild = tid < NROW;          // warps 0-3: A row tid; warps 4-7: B row tid - 128
+    const bool abuild = IMG ? prod : tid < NROW;   // IMG: all producers build A; else warps 0-3 A, 4-7 B
     const int ti = tid & (NROW - 1);
-    // barriers: full[s] (8 producer warps), empty[s] (MMA commit), done (all MMAs)
+    const int ahalf = IMG ? (tid >> 7) & 1 : 0;    // IMG: which 16 pixels of the chunk this thread slices
+    // barriers: full[s] (8 producer warps + the image copy), empty[s] (MMA commit), done (all MMAs)
     uint64_t *full = reinterpret_cast<uint64_t *>(smem + NSTAGE * STAGE);
     uint64_t *empty = full + NSTAGE;
     uint64_t *done = empty + NSTAGE;
@@ -136,6 +144,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
     const int n2 = 2 * n;
     const uint2 *T = dtw + dtw_off[ring0];
     const int nch = (n + KC - 1) / KC;
+    const unsigned char *bimg = IMG ? img + (size_t)(img_off[cls] + (int64_t)u * nch) * (4 * PLANE) : nullptr;
 
     // A row ti: pair ti % 64, hemisphere ti / 64
     const int hemi = ti >> 6;
@@ -154,7 +163,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
     float C[4];
     slice_consts(E, C);
 
-    // B row ti: column c = ti -> m = 64 u + c/2, part c&1 (0: cos, 1: -sin)
+    // B row ti (gather variant): column c = ti -> m = 64 u + c/2, part c&1 (0: cos, 1: -sin)
     const int m = 64 * u + (ti >> 1);
     const bool mok = m <= lmax;
     const int step = (int)((2LL * m) % n2);
@@ -168,7 +177,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
     }
     if (tid == 0) {
         for (int i = 0; i < NSTAGE; ++i) {
-            mbar_init(&full[i], NPROD / 32);
+            mbar_init(&full[i], NPROD / 32 + (IMG ? 1 : 0));
             mbar_init(&empty[i], 1);
         }
         mbar_init(done, 1);
@@ -180,6 +189,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
     fence_after();
     const uint32_t tmem = *slot;
     const uint32_t idesc = idesc_bf16(NROW, NCOL);
+    int ncopied = 0;                                   // thread 0 (IMG): image chunks whose copy was issued
 
     if (!prod) {
         // MMA warp: per chunk wait for both operand halves, issue the ten level products of its two K steps
@@ -214,11 +224,12 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
         }
     } else {
         // raw map values of the next chunk (n is a multiple of 4, ring starts are 16-byte aligned)
-        float4 pre[8];
+        constexpr int NV4 = IMG ? 4 : 8;          // float4 loads per thread per chunk
+        float4 pre[NV4];
         auto load_chunk = [&](int kc) {
 #pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                const int j = kc * KC + 4 * i;
+            for (int i = 0; i < NV4; ++i) {
+                const int j = kc * KC + 16 * ahalf + 4 * i;
                 pre[i] = (live && j < n) ? *reinterpret_cast<const float4 *>(x + j) : make_float4(0.f, 0.f, 0.f, 0.f);
             }
         };
@@ -235,20 +246,26 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
             }
             unsigned char *sbase = smem + st * STAGE;         // A planes 0..3, B planes 4..7
             const int j0 = kc * KC;
+            if (IMG && tid == 0) {
+                // B planes of this chunk: one bulk copy from the image
+                mbar_expect_tx(&full[st], 4 * PLANE);
+                bulk_g2s(sbase + 4 * PLANE, bimg + (size_t)kc * (4 * PLANE), 4 * PLANE, &full[st]);
+                ncopied = kc + 1;
+            }
             if (abuild) {
-                // A row: 32 pixels as 4 groups of 8
+                // A row: this thread's pixels as groups of 8
 #pragma unroll
-                for (int gq = 0; gq < 4; ++gq) {
+                for (int gq = 0; gq < NV4 / 2; ++gq) {
                     const float v[8] = {pre[2 * gq].x, pre[2 * gq].y, pre[2 * gq].z, pre[2 * gq].w,
                                         pre[2 * gq + 1].x, pre[2 * gq + 1].y, pre[2 * gq + 1].z, pre[2 * gq + 1].w};
                     uint32_t w[4][4];
                     slice8(v, C, w);
-                    const uint32_t off = core_off(ti, 8 * gq);
+                    const uint32_t off = core_off(ti, 16 * ahalf + 8 * gq);
 #pragma unroll
                     for (int s = 0; s < 4; ++s) st_shared_v4(sbase + s * PLANE + off, w[s]);
                 }
                 if (kc + 1 < nch) load_chunk(kc + 1);
-            } else {
+            } else if constexpr (!IMG) {
                 // B row: table slices at k = m (2 j + t) + part n/2 (mod 2n)
 #pragma unroll
                 for (int gq = 0; gq < 4; ++gq) {
@@ -284,7 +301,12 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
     fence_after();
     ok = __syncthreads_and(ok) && !*(volatile int *)bad;
     if (!ok) {
-        if (tid == 0) atomicOr(err, ERR_TC_TIMEOUT);
+        if (tid == 0) {
+            atomicOr(err, ERR_TC_TIMEOUT);
+            // image copies still in flight land before the CTA leaves (bounded waits on their stages)
+            for (int kc = ncopied - NSTAGE < 0 ? 0 : ncopied - NSTAGE; kc < ncopied; ++kc)
+                mbar_wait(&full[kc % NSTAGE], (uint32_t)((kc / NSTAGE) & 1));
+        }
     } else if (prod) {
         // epilogue: per row, lead = level 0 (exact) and rest = level 1 + (level 2 + level 3).  Warps w and
         // w + 4 read the same TMEM lanes (rows) and the column groups cg = it and 4 + it; rows exchange through
@@ -348,9 +370,83 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
 }
 
+// The B operand image: for class c, column block u and chunk kc, the four
+// sliced planes of the twiddle tile in the shared-memory core-matrix layout,
+// the same bits the gather variant builds (chunk (c, u, kc) at img_off[c] +
+// u nch_c + kc, 32 KB each).  Grid (max chunks, classes, column blocks), 128
+// threads (one per column).
+__global__ void __launch_bounds__(NROW) k_build_dft_image(const RingGeom *__restrict__ rings, int lmax,
+                                                          const int32_t *__restrict__ cls_rings,
+                                                          const int32_t *__restrict__ cls_off,
+                                                          const uint2 *__restrict__ dtw,
+                                                          const int64_t *__restrict__ dtw_off,
+                                                          const int64_t *__restrict__ img_off,
+                                                          unsigned char *__restrict__ img) {
+    const int kc = blockIdx.x, cls = blockIdx.y, u = blockIdx.z, ti = threadIdx.x;
+    if (img_off[cls] < 0) return;
+    const int ring0 = cls_rings[cls_off[cls]];
+    const RingGeom g0 = rings[ring0];
+    const int n = g0.nph, n2 = 2 * n;
+    const int nch = (n + KC - 1) / KC;
+    if (kc >= nch) return;
+    const int ptype = g0.phi0_den != 0 ? 1 : 0;
+    const uint2 *T = dtw + dtw_off[ring0];
+    const int m = 64 * u + (ti >> 1);
+    const bool mok = m <= lmax;
+    unsigned char *dst = img + (size_t)(img_off[cls] + (int64_t)u * nch + kc) * (4 * PLANE);
+#pragma unroll 1
+    for (int gq = 0; gq < 4; ++gq) {
+        uint32_t w[4][4];
+        for (int t = 0; t < 8; t += 2) {
+            uint2 e[2];
+            for (int h = 0; h < 2; ++h) {
+                const int j = kc * KC + 8 * gq + t + h;
+                const int64_t k = ((int64_t)m * (2 * j + ptype) + (int64_t)(ti & 1) * (n / 2)) % n2;
+                e[h] = (mok && j < n) ? T[k] : make_uint2(0u, 0u);
+            }
+            w[0][t >> 1] = (e[0].x & 0xffffu) | (e[1].x << 16);
+            w[1][t >> 1] = (e[0].x >> 16) | (e[1].x & 0xffff0000u);
+            w[2][t >> 1] = (e[0].y & 0xffffu) | (e[1].y << 16);
+            w[3][t >> 1] = (e[0].y >> 16) | (e[1].y & 0xffff0000u);
+        }
+        const uint32_t off = core_off(ti, 8 * gq);
+        for (int s = 0; s < 4; ++s) st_shared_v4(dst + s * PLANE + off, w[s]);
+    }
+}
+
 }  // namespace dft
 
 size_t ring_dft_smem() { return dft::SMEM; }
+
+// Image offsets (in 32 KB chunks) per ring class, -1 for a class left to the
+// gather variant: the equatorial classes always, the polar ones when
+// with_polar.  Returns the total number of chunks; max_nch gets the longest
+// class in chunks.
+int64_t dft_image_offsets(const Plan &p, const std::vector<int32_t> &crings, const std::vector<int32_t> &coff,
+                          bool with_polar, std::vector<int64_t> &off, int &max_nch) {
+    const int64_t ntn = (p.lmax + 1 + 63) / 64;
+    const int ncls = p.n_polar + p.n_eq_cls;
+    off.assign((size_t)ncls, -1);
+    int64_t tot = 0;
+    max_nch = 1;
+    for (int c = 0; c < ncls; ++c) {
+        if (c < p.n_polar && !with_polar) continue;
+        const int nch = (p.h_rings[crings[coff[c]]].nph + dft::KC - 1) / dft::KC;
+        off[c] = tot;
+        tot += ntn * nch;
+        max_nch = std::max(max_nch, nch);
+    }
+    return tot;
+}
+
+void launch_build_dft_image(const Plan &p, int max_nch, cudaStream_t st) {
+    const int ncls = p.n_polar + p.n_eq_cls;
+    if (ncls <= 0 || !p.d_dtimg) return;
+    dim3 grid((unsigned)max_nch, (unsigned)ncls, (unsigned)((p.lmax + 1 + 63) / 64));
+    dft::k_build_dft_image<<<grid, dft::NROW, 0, st>>>(p.d_rings, p.lmax, p.d_cls_rings, p.d_cls_off, p.d_dtw,
+                                                       p.d_dtw_off, p.d_dtimg_off, p.d_dtimg);
+    note_launch();
+}
 
 // Host-side slicing of one table value v (|v| < 2^EB) into four BF16 slices
 // b_s 2^(EB - 7 - 7 s), packed as uint2 {s0 | s1 << 16, s2 | s3 << 16}.
@@ -377,22 +473,26 @@ void launch_ring_analysis_tc(const Plan &p, const float *maps, int64_t nmaps, fl
         dft::k_ring_rowexp<<<grid, 128, 0, st>>>(maps, p.npix, nmaps, p.d_rings, (int)p.nrn, erow);
         note_launch();
     }
-    set_smem(dft::k_ring_dft_tc, dft::SMEM);
+    set_smem(dft::k_ring_dft_tc<true>, dft::SMEM);
+    set_smem(dft::k_ring_dft_tc<false>, dft::SMEM);
     const unsigned ntn = (unsigned)((p.lmax + 1 + 63) / 64);
-    // polar rings: one class per ring; equatorial rings: two classes (phase 0 and pi/n)
-    if (p.n_polar > 0) {
-        dim3 grid((unsigned)((nmaps + dft::NPAIR - 1) / dft::NPAIR), (unsigned)p.n_polar, ntn);
-        dft::k_ring_dft_tc<<<grid, dft::NTHR, dft::SMEM, st>>>(maps, p.npix, nmaps, p.d_rings, (int)p.nrn, p.lmax,
-                                                               p.d_cls_rings, p.d_cls_off, erow, p.d_dtw,
-                                                               p.d_dtw_off, F, 2 * nmaps, p.d_err);
+    // imaged classes read B from the image, the others gather it from the ring table
+    auto launch = [&](dim3 grid, int c0, bool img) {
+        if (img)
+            dft::k_ring_dft_tc<true><<<grid, dft::NTHR, dft::SMEM, st>>>(
+                maps, p.npix, nmaps, p.d_rings, (int)p.nrn, p.lmax, p.d_cls_rings, p.d_cls_off + c0, erow, p.d_dtw,
+                p.d_dtw_off, p.d_dtimg, p.d_dtimg_off + c0, F, 2 * nmaps, p.d_err);
+        else
+            dft::k_ring_dft_tc<false><<<grid, dft::NTHR, dft::SMEM, st>>>(
+                maps, p.npix, nmaps, p.d_rings, (int)p.nrn, p.lmax, p.d_cls_rings, p.d_cls_off + c0, erow, p.d_dtw,
+                p.d_dtw_off, nullptr, nullptr, F, 2 * nmaps, p.d_err);
         note_launch();
-    }
+    };
+    const unsigned mtiles = (unsigned)((nmaps + dft::NPAIR - 1) / dft::NPAIR);
+    // polar rings: one class per ring, imaged when the whole polar set fits the image
+    if (p.n_polar > 0) launch(dim3(mtiles, (unsigned)p.n_polar, ntn), 0, p.dtimg_polar);
     const int64_t eq_tiles = ((int64_t)p.eq_max_rings * nmaps + dft::NPAIR - 1) / dft::NPAIR;
-    dim3 grid((unsigned)eq_tiles, (unsigned)p.n_eq_cls, ntn);
-    dft::k_ring_dft_tc<<<grid, dft::NTHR, dft::SMEM, st>>>(maps, p.npix, nmaps, p.d_rings, (int)p.nrn, p.lmax,
-                                                           p.d_cls_rings, p.d_cls_off + p.n_polar, erow,
-                                                           p.d_dtw, p.d_dtw_off, F, 2 * nmaps, p.d_err);
-    note_launch();
+    launch(dim3((unsigned)eq_tiles, (unsigned)p.n_eq_cls, ntn), p.n_polar, p.d_dtimg != nullptr);
 }
 
 }  // namespace sfb

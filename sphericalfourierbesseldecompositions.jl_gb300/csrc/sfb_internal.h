@@ -95,6 +95,12 @@ struct Plan {
     int32_t *d_cls_rings = nullptr;
     int32_t *d_cls_off = nullptr;      // [n_polar + n_eq_cls + 1]
     int n_polar = 0, n_eq_cls = 0, eq_max_rings = 0;
+    // B operand image of the tensor-core ring DFT: per class, column block and
+    // 32-pixel chunk the four sliced twiddle planes in shared-memory layout
+    // (32 KB); offsets in chunks per class, -1 where the class gathers instead
+    unsigned char *d_dtimg = nullptr;
+    int64_t *d_dtimg_off = nullptr;
+    bool dtimg_polar = false;
     double *d_lam = nullptr;        // Legendre table, FP64
     float *d_lam32 = nullptr;       // the same table rounded to FP32 (mixed precision)
     void *d_lamtc = nullptr;        // split-BF16 table in tensor-core operand layout (analysis)
@@ -148,8 +154,11 @@ void launch_legendre_table(const Plan &p, cudaStream_t st);
 // precision only) the weighted count map C is written to ref[npix], the maps
 // hold D_b - mu_b C and mu[nbasis] receives mu_b; ref_ready (if given) is
 // recorded on st once C is complete.
+// chunk_ready / nchunks: the catalogue arrives in nchunks equal galaxy ranges,
+// range c complete when chunk_ready[c] fires (keys wait per range).
 int deposit_sorted(Plan &p, const double *rtp, const double *w, int64_t ngal, double *maps, double *ref,
-                   double *mu, cudaEvent_t ref_ready, cudaStream_t st);
+                   double *mu, cudaEvent_t ref_ready, cudaStream_t st, const cudaEvent_t *chunk_ready = nullptr,
+                   int nchunks = 0);
 // A[lm][2j + c] += mu[j] * rmu[lm * ldr + c] for j < nmaps; with set_col >= 0
 // also A[lm][2 set_col + c] = rset[lm * ldr + c].
 void launch_add_mean(double *A, int64_t ldA, int64_t nmaps, const double *mu, const double *rmu, const double *rset,
@@ -179,6 +188,9 @@ void launch_to_float(const double *in, int64_t n, float *out, cudaStream_t st);
 // Mixed-precision ring analysis on the tensor cores (FP32 maps -> FP32 F).
 void launch_ring_analysis_tc(const Plan &p, const float *maps, int64_t nmaps, float *F, int *erow, cudaStream_t st);
 uint2 dft_slices(double v, int EB);
+int64_t dft_image_offsets(const Plan &p, const std::vector<int32_t> &crings, const std::vector<int32_t> &coff,
+                          bool with_polar, std::vector<int64_t> &off, int &max_nch);
+void launch_build_dft_image(const Plan &p, int max_nch, cudaStream_t st);
 // tensor-core (tcgen05) Legendre analysis, mixed precision
 int64_t tc_table_offsets(const Plan &p, std::vector<int64_t> &off);
 void launch_build_lamtc(const Plan &p, const int *Ea, const int *Es, cudaStream_t st);

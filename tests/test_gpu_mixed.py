@@ -79,6 +79,24 @@ def test_mixed_vs_fp64(cfg, kind):
     assert e2 < MIXED_TOL and emax < MIXED_TOL
 
 
+def test_dft_twiddle_image_matches_gather(monkeypatch):
+    """The ring DFT takes its twiddle operand from the precomputed image, or,
+    for polar rings past the image budget, gathers it from the ring tables:
+    both feed the tensor cores the same slices, so the a_nlm agree to the
+    run-to-run rounding of the deposit."""
+    cfg = (0.05, 500.0, 1000.0, 32, 200_000, 8)
+    a, rtp, w, win, nbar = _setup(*cfg)
+    img = sfbgpu.cat2amln(rtp, a, nbar, win, w, precision="mixed")
+    monkeypatch.setenv("SFBGPU_DFT_IMAGE_MAX_BYTES", "0")
+    b = sfbgpu.AnlmModes(*cfg[:3], nside=cfg[3])
+    gat = sfbgpu.cat2amln(rtp, b, nbar, win, w, precision="mixed")
+    f64 = sfbgpu.cat2amln(rtp, a, nbar, win, w, precision="fp64")
+    e_ig = _errors(gat, img)[0]
+    record("dft_image_vs_gather", e_ig)
+    assert e_ig < 1e-9
+    assert _errors(gat, f64)[0] < MIXED_TOL and _errors(img, f64)[0] < MIXED_TOL
+
+
 def test_mixed_vs_reference_algorithm():
     a, rtp, w, win, nbar = _setup(0.03, 500.0, 1000.0, 16, 50_000, 3)
     md = modes_dict(a)
