@@ -301,9 +301,19 @@ int choose_radial_basis(sfb_plan *h, const sfb_plan_desc *d) {
 // map2alm with niter refinement on nm maps; result in p.alm [lmsize][2*nm] (FP64).
 // In mixed precision the maps are FP32 ([nm][npix] floats); maps_are_fp64 marks
 // FP64 maps that are converted first.
+// The ring Fourier buffers and the a_lm of one transform: the plan's own, or
+// the side stream's set for the FP64 reference transform that overlaps the
+// main one.
+struct ShtWork {
+    DevBuf<double> *f, *g, *r, *alm;
+};
+
 int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, bool maps_are_fp64 = false,
-                 int stage_override = -1) {
+                 int stage_override = -1, const ShtWork *ws = nullptr) {
     Plan &p = h->p;
+    const ShtWork own{&p.fbuf, &p.gbuf, &p.rbuf, &p.alm};
+    if (!ws) ws = &own;
+    DevBuf<double> &fbuf = *ws->f, &gbuf = *ws->g, &rbuf = *ws->r, &alm = *ws->alm;
     auto stage = [&](int s) { return stage_override >= 0 ? stage_override : s; };
     if (p.precision == SFB_MIXED && maps_are_fp64) {
         SFB_TRY(grow(p, p.maps32, (size_t)(nm * p.npix + 1) / 2));
@@ -315,22 +325,22 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, b
     }
     const int64_t ncol = 2 * nm;
     const size_t fsz = (size_t)2 * (p.lmax + 1) * p.nrn * ncol;
-    SFB_TRY(grow(p, p.fbuf, fsz));
-    SFB_TRY(grow(p, p.alm, (size_t)p.lmsize * ncol));
+    SFB_TRY(grow(p, fbuf, fsz));
+    SFB_TRY(grow(p, alm, (size_t)p.lmsize * ncol));
     if (p.niter > 0) {
-        SFB_TRY(grow(p, p.gbuf, fsz));
-        SFB_TRY(grow(p, p.rbuf, fsz));
+        SFB_TRY(grow(p, gbuf, fsz));
+        SFB_TRY(grow(p, rbuf, fsz));
     }
     if (p.precision == SFB_MIXED) {
         // row scales of the ring DFT, then column scales of the Legendre analysis (ints)
         SFB_TRY(grow(p, p.erow, (size_t)std::max<int64_t>(p.nrn * nm, (p.lmax + 1) * ncol) + 1));
         SFB_TRY(grow(p, p.almdf, (size_t)p.lmsize * ncol));
         Stage s(h, stage(SFB_STAGE_RING_FFT), st);
-        launch_ring_analysis_tc(p, reinterpret_cast<const float *>(maps), nm, reinterpret_cast<float *>(p.fbuf.ptr),
+        launch_ring_analysis_tc(p, reinterpret_cast<const float *>(maps), nm, reinterpret_cast<float *>(fbuf.ptr),
                                 reinterpret_cast<int *>(p.erow.ptr), st);
     } else {
         Stage s(h, stage(SFB_STAGE_RING_FFT), st);
-        launch_ring_analysis(p, maps, nm, p.fbuf.ptr, st);
+        launch_ring_analysis(p, maps, nm, fbuf.ptr, st);
     }
     const bool tc = p.precision == SFB_MIXED;
     float2 *adf = reinterpret_cast<float2 *>(p.almdf.ptr);
@@ -338,21 +348,21 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, b
     auto analysis = [&](const double *src, bool acc) {
         Stage s(h, stage(SFB_STAGE_LEG_ANALYSIS), st);
         // after the first pass the fold has written the column scales of its residual
-        if (tc) launch_leg_analysis_tc(p, (const float *)src, ncol, p.alm.ptr, adf, ecol, acc, st, acc);
-        else launch_leg_analysis(p, src, ncol, p.alm.ptr, acc, st);
+        if (tc) launch_leg_analysis_tc(p, (const float *)src, ncol, alm.ptr, adf, ecol, acc, st, acc);
+        else launch_leg_analysis(p, src, ncol, alm.ptr, acc, st);
     };
-    analysis(p.fbuf.ptr, false);
+    analysis(fbuf.ptr, false);
     for (int it = 0; it < p.niter; ++it) {
         {
             Stage s(h, stage(SFB_STAGE_LEG_SYNTHESIS), st);
-            if (tc) launch_leg_synthesis_tc(p, adf, ncol, (float *)p.gbuf.ptr, st);
-            else launch_leg_synthesis(p, p.alm.ptr, ncol, p.gbuf.ptr, st);
+            if (tc) launch_leg_synthesis_tc(p, adf, ncol, (float *)gbuf.ptr, st);
+            else launch_leg_synthesis(p, alm.ptr, ncol, gbuf.ptr, st);
         }
         {
             Stage s(h, stage(SFB_STAGE_FOLD), st);
-            launch_fold_residual(p, p.fbuf.ptr, p.gbuf.ptr, ncol, p.rbuf.ptr, st, tc ? ecol : nullptr);
+            launch_fold_residual(p, fbuf.ptr, gbuf.ptr, ncol, rbuf.ptr, st, tc ? ecol : nullptr);
         }
-        analysis(p.rbuf.ptr, true);
+        analysis(rbuf.ptr, true);
     }
     SFB_CUDA_TRY(cudaGetLastError());
     return SFB_OK;
@@ -382,10 +392,11 @@ int reference_alm(sfb_plan *h, const double *ref, int64_t nref, double *ralm, cu
     Plan &p = h->p;
     const int32_t prec = p.precision;
     p.precision = SFB_FP64;
-    const int rc = sht_analysis(h, ref, nref, st, false, SFB_STAGE_OTHER);
+    const ShtWork ws{&p.rf, &p.rg, &p.rr, &p.ralm};
+    const int rc = sht_analysis(h, ref, nref, st, false, SFB_STAGE_OTHER, &ws);
     p.precision = prec;
     SFB_TRY(rc);
-    SFB_CUDA_TRY(cudaMemcpyAsync(ralm, p.alm.ptr, (size_t)2 * nref * p.lmsize * sizeof(double),
+    SFB_CUDA_TRY(cudaMemcpyAsync(ralm, p.ralm.ptr, (size_t)2 * nref * p.lmsize * sizeof(double),
                                  cudaMemcpyDeviceToDevice, st));
     return SFB_OK;
 }
@@ -450,13 +461,14 @@ int cat2amln_dev(sfb_plan *h, const double *rtp, const double *w, int64_t ngal, 
                                    chunk_ready, nchunks));
         }
         if (split) {
-            // the FP64 transform of (C, W01) runs on the side stream while the deposit's moments finish
+            // the FP64 transform of (C, W01) runs on the side stream, in its own workspace, beside
+            // the rest of the deposit and the main transform; the projection waits for it
             SFB_CUDA_TRY(cudaStreamWaitEvent(h->side, h->ev_fork, 0));
             SFB_TRY(reference_alm(h, Cmap, 2, ralm, h->side));
             SFB_CUDA_TRY(cudaEventRecord(h->ev_join, h->side));
-            SFB_CUDA_TRY(cudaStreamWaitEvent(st, h->ev_join, 0));
         }
         SFB_TRY(sht_analysis(h, p.maps.ptr, nm, st));
+        if (split) SFB_CUDA_TRY(cudaStreamWaitEvent(st, h->ev_join, 0));
         {
             Stage s(h, SFB_STAGE_PROJECT, st);
             if (p.precision == SFB_MIXED)
@@ -813,7 +825,7 @@ void sfb_plan_destroy(sfb_plan *h) {
                     p.d_dtw_off, p.d_dtimg, p.d_dtimg_off, p.d_cls_rings, p.d_cls_off, p.d_lam, p.d_lam32, p.d_lamtc, p.d_lamtc_off, p.d_lamts, p.d_lamts_off, p.d_lam_off, p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp,
                     p.d_pair_l, p.d_pair_n, p.d_out_pair, p.d_out_lm, p.d_coef, p.d_coefT, p.d_err,
                     p.maps.ptr, p.fbuf.ptr, p.gbuf.ptr, p.rbuf.ptr, p.alm.ptr, p.scratch.ptr, p.scratch2.ptr, p.dep.ptr, p.maps32.ptr,
-                    p.ref.ptr, p.erow.ptr, p.almdf.ptr, h->d_pair_index, h->d_noff};
+                    p.ref.ptr, p.rf.ptr, p.rg.ptr, p.rr.ptr, p.ralm.ptr, p.erow.ptr, p.almdf.ptr, h->d_pair_index, h->d_noff};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     collect_stages(h);

@@ -128,6 +128,7 @@ struct Plan {
     DevBuf<double> scratch2;
     DevBuf<double> dep;             // sorted-deposit workspace
     DevBuf<double> ref;             // reference-map a_lm (FP64) and mean coefficients (mixed precision)
+    DevBuf<double> rf, rg, rr, ralm;// workspace of the FP64 reference transform on the side stream
     DevBuf<double> erow;            // ring DFT row exponents [2][nrn][nmaps] (int)
     DevBuf<double> maps32;          // FP32 copy of FP64 maps (mixed precision, spline / dense-window paths)
     int64_t device_bytes = 0;
