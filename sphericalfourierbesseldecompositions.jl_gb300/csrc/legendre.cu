@@ -336,10 +336,12 @@ void launch_leg_synthesis(const Plan &p, const double *A, int64_t ncol, double *
 // for F).
 constexpr int FOLD_RC = 64;
 
+// F == nullptr: R = -w n cfold Fold(G) (the aliased-ring term of the Gram
+// refinement).  Only rings r < rlim are written.
 template <typename T>
-__global__ void __launch_bounds__(128) k_fold_cols(const RingGeom *__restrict__ rings, int nrn, int lmax, double w,
-                                                   const T *__restrict__ F, const T *__restrict__ G, int64_t ncplx,
-                                                   T *__restrict__ R, int *__restrict__ Ecol) {
+__global__ void __launch_bounds__(128) k_fold_cols(const RingGeom *__restrict__ rings, int nrn, int rlim, int lmax,
+                                                   double w, const T *__restrict__ F, const T *__restrict__ G,
+                                                   int64_t ncplx, T *__restrict__ R, int *__restrict__ Ecol) {
     const int mp = blockIdx.y >> 1, par = blockIdx.y & 1;
     const int rc0 = blockIdx.z * FOLD_RC;
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -347,7 +349,7 @@ __global__ void __launch_bounds__(128) k_fold_cols(const RingGeom *__restrict__ 
     const int L1 = lmax + 1;
     const int64_t ld = 2 * ncplx;
     float mxr = 0.f, mxi = 0.f;
-    const int rend = min(nrn, rc0 + FOLD_RC);
+    const int rend = min(rlim, rc0 + FOLD_RC);
 #pragma unroll 4
     for (int r = rc0; r < rend; ++r) {
         const RingGeom g = rings[r];
@@ -380,7 +382,7 @@ __global__ void __launch_bounds__(128) k_fold_cols(const RingGeom *__restrict__ 
                 sy -= sgn * gp[1];
             }
         }
-        const T rx = F[off] - f * sx, ry = F[off + 1] - f * sy;
+        const T rx = (F ? F[off] : T(0)) - f * sx, ry = (F ? F[off + 1] : T(0)) - f * sy;
         R[off] = rx;
         R[off + 1] = ry;
         mxr = fmaxf(mxr, fabsf((float)rx));
@@ -443,16 +445,17 @@ __global__ void __launch_bounds__(256) k_fold_residual_narrow(const RingGeom *ri
 }
 
 void launch_fold_residual(const Plan &p, const double *F, const double *G, int64_t ncol, double *R,
-                          cudaStream_t st, int *Ecol) {
+                          cudaStream_t st, int *Ecol, int rlim) {
     const int64_t ncplx = ncol / 2;
+    if (rlim < 0 || rlim > p.nrn) rlim = (int)p.nrn;
     if (p.precision == SFB_MIXED && ncplx > 4) {
         // 0x80 bytes: every exponent word starts at -2139062144, below any scale exponent
         if (Ecol) cudaMemsetAsync(Ecol, 0x80, (size_t)2 * (p.lmax + 1) * ncol * sizeof(int), st);
         dim3 grid((unsigned)((ncplx + 127) / 128), (unsigned)(2 * (p.lmax + 1)),
-                  (unsigned)((p.nrn + FOLD_RC - 1) / FOLD_RC));
+                  (unsigned)((rlim + FOLD_RC - 1) / FOLD_RC));
         const double w = 4.0 * M_PI / (double)p.npix;
-        k_fold_cols<float><<<grid, 128, 0, st>>>(p.d_rings, (int)p.nrn, p.lmax, w, (const float *)F, (const float *)G,
-                                                 ncplx, (float *)R, Ecol);
+        k_fold_cols<float><<<grid, 128, 0, st>>>(p.d_rings, (int)p.nrn, rlim, p.lmax, w, (const float *)F,
+                                                 (const float *)G, ncplx, (float *)R, Ecol);
         note_launch();
         return;
     }

@@ -221,11 +221,13 @@ __global__ void __launch_bounds__(256) k_colmax(const float *__restrict__ F, int
 
 // Analysis: grid (column tiles, row tiles of NMAX, blocks z); warps 0-7
 // produce (thread: column c, half kh of each chunk), warp 8 issues the MMAs.
+// Rings r >= rlim count as zero (the sum over the first rlim rings only).
 __global__ void __launch_bounds__(NTH, 2) k_leg_analysis_tc(const __nv_bfloat16 *__restrict__ lamtc,
                                                             const int64_t *__restrict__ lamtc_off, int lmax, int nrn,
-                                                            int nchunks, const float *__restrict__ F, int64_t ncol,
-                                                            const int *__restrict__ Ecol, double *__restrict__ A,
-                                                            float2 *__restrict__ Adf, int accumulate, int *err) {
+                                                            int nchunks, int rlim, const float *__restrict__ F,
+                                                            int64_t ncol, const int *__restrict__ Ecol,
+                                                            double *__restrict__ A, float2 *__restrict__ Adf,
+                                                            int accumulate, int *err) {
     extern __shared__ __align__(1024) unsigned char smem[];
     const int z = blockIdx.z;
     const int m = z >> 1, par = z & 1;
@@ -259,7 +261,7 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_analysis_tc(const __nv_bfloat16 
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
                 const int r = kc * KC + 8 * kh + j;
-                buf[j] = (cok && r < nrn) ? Fz[(int64_t)r * ncol] : 0.f;
+                buf[j] = (cok && r < rlim) ? Fz[(int64_t)r * ncol] : 0.f;
             }
         };
         auto chunk = [&](int kc, float (&cur)[8]) -> bool {
@@ -348,10 +350,18 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_analysis_tc(const __nv_bfloat16 
 
 // Synthesis: grid (column tiles, ring tiles of NT <= NMAX, blocks z); warps
 // 0-7 produce, warp 8 issues the MMAs.
+//
+// Update mode (Anew != nullptr): the table holds the Gram matrices of the
+// alias-free rings, "rings" r are output rows li (nrn = rows of the largest
+// block), and the epilogue writes, instead of G,
+//   Anew[l(r)] = Acur[l(r)] + (A0[l(r)] - sum_li M[r][li] Acur[l(li)])
+// in FP64 and double-float (Acur in FP64 from A, in double-float from Adf).
 __global__ void __launch_bounds__(NTH, 2) k_leg_synthesis_tc(const __nv_bfloat16 *__restrict__ lamts,
                                                              const int64_t *__restrict__ lamts_off, int lmax, int nrn,
                                                              int NT, const float2 *__restrict__ Adf, int64_t ncol,
-                                                             float *__restrict__ G, int *err) {
+                                                             float *__restrict__ G, const double *__restrict__ Acur,
+                                                             const float2 *__restrict__ A0, double *__restrict__ Anew,
+                                                             float2 *__restrict__ Adfnew, int *err) {
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ float red[2][MTILE];
     const int z = blockIdx.z;
@@ -361,7 +371,9 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_synthesis_tc(const __nv_bfloat16
     const int r0 = nt * NT;
     const int64_t col0 = (int64_t)blockIdx.x * MTILE;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    float *Gz = G + ((int64_t)(par * (lmax + 1) + m) * nrn) * ncol;
+    const bool upd = Anew != nullptr;
+    if (upd && r0 >= nrows) return;          // no output row of this block in the tile
+    float *Gz = upd ? nullptr : G + ((int64_t)(par * (lmax + 1) + m) * nrn) * ncol;
     if (nrows == 0) {      // no l for this (m, parity): the block is zero
         for (int rr = warp; rr < NT; rr += NTH / 32) {
             const int r = r0 + rr;
@@ -452,7 +464,7 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_synthesis_tc(const __nv_bfloat16
             tmem_ld16(tmem + lane_base + (uint32_t)(NMAX + i0), v1);
             tmem_ld16(tmem + lane_base + (uint32_t)(2 * NMAX + i0), v2);
             tmem_ld16(tmem + lane_base + (uint32_t)(3 * NMAX + i0), v3);
-            if (cc < ncol) {
+            if (cc < ncol && !upd) {
 #pragma unroll
                 for (int i = 0; i < 16; ++i) {
                     const int r = r0 + i0 + i;
@@ -460,6 +472,27 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_synthesis_tc(const __nv_bfloat16
                     float hi, lo;
                     lvl_sum(v0[i], v1[i], v2[i], v3[i], hi, lo);
                     Gz[(int64_t)r * ncol + cc] = hi;
+                }
+            } else if (cc < ncol) {
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    const int r = r0 + i0 + i;
+                    if (r >= nrows) break;
+                    float hi, lo;
+                    lvl_sum(v0[i], v1[i], v2[i], v3[i], hi, lo);
+                    const int l = m + par + 2 * r;
+                    const int64_t o = ((int64_t)l * (l + 1) / 2 + m) * ncol + cc;
+                    // d = A0 - (hi, lo) and Adf + d in double-float (TwoSum, renormalised)
+                    const float2 a0 = A0[o], ac = Adf[o];
+                    float s = a0.x - hi, z2 = s - a0.x;
+                    float e = ((a0.x - (s - z2)) + (-hi - z2)) + (a0.y - lo);
+                    float dh = s + e, dl = e - (dh - s);
+                    s = ac.x + dh;
+                    z2 = s - ac.x;
+                    e = ((ac.x - (s - z2)) + (dh - z2)) + (ac.y + dl);
+                    const float nh = s + e;
+                    Adfnew[o] = make_float2(nh, e - (nh - s));
+                    Anew[o] = Acur[o] + ((double)dh + (double)dl);
                 }
             }
         }
@@ -618,7 +651,8 @@ void launch_build_lamtc(const Plan &p, const int *Ea, const int *Es, cudaStream_
 }
 
 void launch_leg_analysis_tc(const Plan &p, const float *F, int64_t ncol, double *A, float2 *Adf, int *Ecol,
-                            bool accumulate, cudaStream_t st, bool scales_ready) {
+                            bool accumulate, cudaStream_t st, bool scales_ready, int rlim) {
+    if (rlim < 0 || rlim > p.nrn) rlim = (int)p.nrn;
     if (!scales_ready) {
         dim3 grid((unsigned)((ncol + 255) / 256), (unsigned)(2 * (p.lmax + 1)));
         tc::k_colmax<<<grid, 256, 0, st>>>(F, ncol, p.lmax, (int)p.nrn, Ecol);
@@ -628,8 +662,8 @@ void launch_leg_analysis_tc(const Plan &p, const float *F, int64_t ncol, double 
     const int ntile = (tc_np_max(p) + tc::NMAX - 1) / tc::NMAX;
     dim3 grid((unsigned)((ncol + tc::MTILE - 1) / tc::MTILE), (unsigned)ntile, (unsigned)(2 * (p.lmax + 1)));
     tc::k_leg_analysis_tc<<<grid, tc::NTH, tc::LEG_SMEM, st>>>((const __nv_bfloat16 *)p.d_lamtc, p.d_lamtc_off,
-                                                              p.lmax, (int)p.nrn, tc_chunks(p), F, ncol, Ecol, A, Adf,
-                                                              accumulate ? 1 : 0, p.d_err);
+                                                              p.lmax, (int)p.nrn, (rlim + tc::KC - 1) / tc::KC, rlim,
+                                                              F, ncol, Ecol, A, Adf, accumulate ? 1 : 0, p.d_err);
     note_launch();
 }
 
@@ -637,15 +671,18 @@ void launch_leg_analysis_tc(const Plan &p, const float *F, int64_t ncol, double 
 
 namespace sfb {
 
-int tc_synth_nt(const Plan &p) {
-    const int nrn = (int)p.nrn;
+int tc_synth_nt(int nrn) {
     const int nt16 = (nrn + 15) & ~15;
     return nt16 < tc::NMAX ? nt16 : tc::NMAX;
 }
+int tc_synth_nt(const Plan &p) { return tc_synth_nt((int)p.nrn); }
 
-int64_t tc_synth_table_offsets(const Plan &p, std::vector<int64_t> &off) {
-    const int NT = tc_synth_nt(p);
-    const int ntiles = (int)((p.nrn + NT - 1) / NT);
+// offsets of every block of a synthesis-layout table over nrn "rings"
+// (the rings of the plan, or the output rows of the Gram tables)
+int64_t tc_synth_table_offsets(const Plan &p, std::vector<int64_t> &off, int64_t nrn) {
+    if (nrn <= 0) nrn = p.nrn;
+    const int NT = tc_synth_nt((int)nrn);
+    const int ntiles = (int)((nrn + NT - 1) / NT);
     off.assign(2 * (p.lmax + 1) + 1, 0);
     int64_t o = 0;
     for (int z = 0; z < 2 * (p.lmax + 1); ++z) {
@@ -665,14 +702,143 @@ void launch_build_lamts(const Plan &p, const int *Es, cudaStream_t st) {
     note_launch();
 }
 
-void launch_leg_synthesis_tc(const Plan &p, const float2 *Adf, int64_t ncol, float *G, cudaStream_t st) {
+void launch_leg_synthesis_tc(const Plan &p, const float2 *Adf, int64_t ncol, float *G, cudaStream_t st, int rlim) {
     const int NT = tc_synth_nt(p);
+    if (rlim < 0 || rlim > p.nrn) rlim = (int)p.nrn;
     set_smem(tc::k_leg_synthesis_tc, tc::LEG_SMEM);
-    dim3 grid((unsigned)((ncol + tc::MTILE - 1) / tc::MTILE), (unsigned)((p.nrn + NT - 1) / NT),
+    // ring tiles covering the first rlim rings (a tile's rings past rlim are computed as well)
+    dim3 grid((unsigned)((ncol + tc::MTILE - 1) / tc::MTILE), (unsigned)((rlim + NT - 1) / NT),
               (unsigned)(2 * (p.lmax + 1)));
     tc::k_leg_synthesis_tc<<<grid, tc::NTH, tc::LEG_SMEM, st>>>((const __nv_bfloat16 *)p.d_lamts, p.d_lamts_off,
-                                                               p.lmax, (int)p.nrn, NT, Adf, ncol, G, p.d_err);
+                                                               p.lmax, (int)p.nrn, NT, Adf, ncol, G, nullptr, nullptr,
+                                                               nullptr, nullptr, p.d_err);
     note_launch();
+}
+
+void launch_gram_update(const Plan &p, const double *A, const float2 *Adf, const float2 *A0, int64_t ncol,
+                        double *Anew, float2 *Adfnew, cudaStream_t st) {
+    const int NT = tc_synth_nt(p.gram_rows);
+    set_smem(tc::k_leg_synthesis_tc, tc::LEG_SMEM);
+    dim3 grid((unsigned)((ncol + tc::MTILE - 1) / tc::MTILE), (unsigned)((p.gram_rows + NT - 1) / NT),
+              (unsigned)(2 * (p.lmax + 1)));
+    tc::k_leg_synthesis_tc<<<grid, tc::NTH, tc::LEG_SMEM, st>>>((const __nv_bfloat16 *)p.d_gramts, p.d_gramts_off,
+                                                               p.lmax, p.gram_rows, NT, Adf, ncol, nullptr, A, A0,
+                                                               Anew, Adfnew, p.d_err);
+    note_launch();
+}
+
+// Gram tables of the alias-free rings r >= p.ral, per block z:
+//   M_z[li][li'] = sum_r lambda_z(li, r) w n_r cfold_r lambda_z(li', r),
+// formed with the FP64 synthesis (of unit coefficient vectors) and analysis
+// kernels, then sliced into the synthesis layout with the output rows as rings.
+namespace tc {
+__global__ void k_unit_alm(int lmax, int R, double *E) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t lmsize = (int64_t)(lmax + 1) * (lmax + 2) / 2;
+    if (idx >= lmsize * R) return;
+    const int64_t lm = idx / R;
+    const int c = (int)(idx - lm * R);
+    int l = (int)((sqrt(8.0 * (double)lm + 1.0) - 1.0) / 2.0);
+    while ((int64_t)(l + 1) * (l + 2) / 2 <= lm) ++l;
+    while ((int64_t)l * (l + 1) / 2 > lm) --l;
+    const int m = (int)(lm - (int64_t)l * (l + 1) / 2);
+    E[idx] = (c == ((l - m) >> 1)) ? 1.0 : 0.0;
+}
+
+__global__ void k_gram_weights(const RingGeom *__restrict__ rings, int nrn, int lmax, int ral, double w, int R,
+                               double *G) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t total = (int64_t)2 * (lmax + 1) * nrn * R;
+    if (idx >= total) return;
+    const int r = (int)((idx / R) % nrn);
+    const RingGeom g = rings[r];
+    G[idx] = r < ral ? 0.0 : G[idx] * (w * (double)g.nph * g.cfold);
+}
+
+__global__ void k_gram_gather(int lmax, int R, const double *__restrict__ A, const int64_t *__restrict__ gram_off,
+                              double *__restrict__ gram) {
+    const int z = blockIdx.y;
+    const int m = z >> 1, par = z & 1;
+    const int nrows = rows_of(m, par, lmax);
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < nrows * R; idx += gridDim.x * blockDim.x) {
+        const int li = idx / R, ro = idx - li * R;             // input row li, output row ro
+        double v = 0.0;
+        if (ro < nrows) {
+            const int l = m + par + 2 * ro;
+            v = A[((int64_t)l * (l + 1) / 2 + m) * R + li];
+        }
+        gram[gram_off[z] + (int64_t)li * R + ro] = v;
+    }
+}
+}  // namespace tc
+
+int build_gram_tables(Plan &p, cudaStream_t st) {
+    const int R = p.gram_rows;
+    const int64_t L1 = p.lmax + 1;
+    const int64_t nE = p.lmsize * R, nG = 2 * L1 * p.nrn * R;
+    std::vector<int64_t> goff(2 * L1 + 1, 0);
+    int64_t o = 0;
+    for (int z = 0; z < 2 * L1; ++z) {
+        const int m = z >> 1, par = z & 1;
+        goff[z] = o;
+        o += (int64_t)((m + par <= p.lmax) ? (p.lmax - m - par) / 2 + 1 : 0) * R;
+    }
+    goff[2 * L1] = o;
+    double *E = nullptr, *G = nullptr, *A = nullptr, *gram = nullptr;
+    int *Ea = nullptr;
+    int64_t *d_goff = nullptr;
+    const int nEa = (int)(o / R) + 1, nEs = (int)(2 * L1 * R);
+    auto cleanup = [&] {
+        cudaFree(E);
+        cudaFree(G);
+        cudaFree(A);
+        cudaFree(gram);
+        cudaFree(Ea);
+        cudaFree(d_goff);
+    };
+    if (cudaMalloc(&E, nE * sizeof(double)) != cudaSuccess || cudaMalloc(&G, nG * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&A, nE * sizeof(double)) != cudaSuccess || cudaMalloc(&gram, (o + 1) * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&Ea, (size_t)(nEa + nEs) * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&d_goff, goff.size() * sizeof(int64_t)) != cudaSuccess) {
+        cudaGetLastError();
+        cleanup();
+        return fail(SFB_ENOMEM, "device allocation failed (Gram tables)");
+    }
+    int *Es = Ea + nEa;
+    cudaMemcpy(d_goff, goff.data(), goff.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
+    const int32_t prec = p.precision;
+    p.precision = SFB_FP64;
+    tc::k_unit_alm<<<(unsigned)((nE + 255) / 256), 256, 0, st>>>(p.lmax, R, E);
+    note_launch();
+    launch_leg_synthesis(p, E, R, G, st);
+    tc::k_gram_weights<<<(unsigned)((nG + 255) / 256), 256, 0, st>>>(p.d_rings, (int)p.nrn, p.lmax, p.ral,
+                                                                     4.0 * M_PI / (double)p.npix, R, G);
+    note_launch();
+    launch_leg_analysis(p, G, R, A, false, st);
+    p.precision = prec;
+    tc::k_gram_gather<<<dim3(16, (unsigned)(2 * L1)), 256, 0, st>>>(p.lmax, R, A, d_goff, gram);
+    note_launch();
+    tc::k_lam_rowexp<<<dim3(8, (unsigned)(2 * L1)), 256, 0, st>>>(gram, d_goff, p.lmax, R, Ea, Es);
+    note_launch();
+    std::vector<int64_t> soff;
+    const int64_t ssz = tc_synth_table_offsets(p, soff, R);
+    int rc = SFB_OK;
+    if (cudaMalloc(&p.d_gramts, (size_t)(ssz + 1) * 2) != cudaSuccess ||
+        cudaMalloc(&p.d_gramts_off, soff.size() * sizeof(int64_t)) != cudaSuccess) {
+        cudaGetLastError();
+        rc = fail(SFB_ENOMEM, "device allocation failed (Gram tables)");
+    } else {
+        p.device_bytes += (ssz + 1) * 2 + (int64_t)(soff.size() * sizeof(int64_t));
+        cudaMemcpy(p.d_gramts_off, soff.data(), soff.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
+        tc::k_build_lamts<<<dim3(64, (unsigned)(2 * L1)), 256, 0, st>>>(gram, d_goff, p.lmax, R, tc_synth_nt(R), Es,
+                                                                        p.d_gramts_off,
+                                                                        (__nv_bfloat16 *)p.d_gramts);
+        note_launch();
+    }
+    if (cudaStreamSynchronize(st) != cudaSuccess && rc == SFB_OK)
+        rc = fail(SFB_ECUDA, std::string("Gram table setup failed: ") + cudaGetErrorString(cudaGetLastError()));
+    cleanup();
+    return rc;
 }
 
 }  // namespace sfb

@@ -351,6 +351,45 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, b
         if (tc) launch_leg_analysis_tc(p, (const float *)src, ncol, alm.ptr, adf, ecol, acc, st, acc);
         else launch_leg_analysis(p, src, ncol, alm.ptr, acc, st);
     };
+    if (tc && ncol / 2 > 4 && p.d_gramts && p.niter > 0) {
+        // Gram refinement: a <- a + (a0 - M a) - A_al(Fold(S_al a)), M the Gram matrix of the
+        // alias-free rings (fold = identity there), S_al / A_al the synthesis and analysis
+        // over the aliased rings r < ral.  Each pass writes the other (A, Adf) buffer; the
+        // last one lands in the plan's.
+        SFB_TRY(grow(p, p.alm2, (size_t)p.lmsize * ncol));
+        SFB_TRY(grow(p, p.almdf2, (size_t)p.lmsize * ncol));
+        SFB_TRY(grow(p, p.adf0, (size_t)p.lmsize * ncol));
+        double *Ab[2] = {alm.ptr, p.alm2.ptr};
+        float2 *Db[2] = {adf, reinterpret_cast<float2 *>(p.almdf2.ptr)};
+        const float2 *a0 = reinterpret_cast<const float2 *>(p.adf0.ptr);
+        int cur = p.niter & 1;
+        {
+            Stage s(h, stage(SFB_STAGE_LEG_ANALYSIS), st);
+            launch_leg_analysis_tc(p, (const float *)fbuf.ptr, ncol, Ab[cur], Db[cur], ecol, false, st, false);
+        }
+        SFB_CUDA_TRY(cudaMemcpyAsync(p.adf0.ptr, Db[cur], (size_t)p.lmsize * ncol * sizeof(float2),
+                                     cudaMemcpyDeviceToDevice, st));
+        for (int it = 0; it < p.niter; ++it) {
+            const int nxt = cur ^ 1;
+            {
+                Stage s(h, stage(SFB_STAGE_LEG_SYNTHESIS), st);
+                if (p.ral > 0) launch_leg_synthesis_tc(p, Db[cur], ncol, (float *)gbuf.ptr, st, p.ral);
+                launch_gram_update(p, Ab[cur], Db[cur], a0, ncol, Ab[nxt], Db[nxt], st);
+            }
+            if (p.ral > 0) {
+                {
+                    Stage s(h, stage(SFB_STAGE_FOLD), st);
+                    launch_fold_residual(p, nullptr, gbuf.ptr, ncol, rbuf.ptr, st, ecol, p.ral);
+                }
+                Stage s(h, stage(SFB_STAGE_LEG_ANALYSIS), st);
+                launch_leg_analysis_tc(p, (const float *)rbuf.ptr, ncol, Ab[nxt], Db[nxt], ecol, true, st, true,
+                                       p.ral);
+            }
+            cur = nxt;
+        }
+        SFB_CUDA_TRY(cudaGetLastError());
+        return SFB_OK;
+    }
     analysis(fbuf.ptr, false);
     for (int it = 0; it < p.niter; ++it) {
         {
@@ -790,6 +829,22 @@ int sfb_plan_create(const sfb_plan_desc *d, sfb_plan **out) {
             if ((st = upload<uint16_t>(p, (uint16_t **)&p.d_lamts, nullptr, (size_t)ssz)) != SFB_OK) break;
             launch_build_lamts(p, Es, h->stream);
         }
+        {
+            // rings that alias (nph <= 2 lmax) form a prefix: the polar rings grow to the equatorial length
+            int ral = 0;
+            while (ral < p.nrn && p.h_rings[ral].nph <= 2 * p.lmax) ++ral;
+            p.ral = ral;
+            p.gram_rows = (int)(p.lmax / 2 + 1);
+            // worth it while most rings are alias-free; the FP64 build holds a
+            // [2 (lmax+1)][nrn][gram_rows] transient, kept under 4 GiB
+            const double build_bytes = 8.0 * 2 * (p.lmax + 1) * (double)p.nrn * p.gram_rows;
+            // (SFBGPU_GRAM_REFINEMENT=0 keeps the full synthesis / fold / analysis passes)
+            const char *ge = std::getenv("SFBGPU_GRAM_REFINEMENT");
+            const bool allowed = !ge || std::atoi(ge) != 0;
+            if (allowed && p.niter > 0 && 4 * (int64_t)ral <= 3 * p.nrn && build_bytes <= 4.0 * (1LL << 30)) {
+                if ((st = build_gram_tables(p, h->stream)) != SFB_OK) break;
+            }
+        }
         if (cudaGetLastError() != cudaSuccess) {
             st = fail(SFB_ECUDA, "Legendre table kernel failed to launch");
             break;
@@ -822,10 +877,10 @@ void sfb_plan_destroy(sfb_plan *h) {
     cudaSetDevice(p.device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     void *ptrs[] = {p.d_rings, p.d_twtab, p.d_twoff, p.d_phase, p.d_wphase, p.d_twtab32, p.d_wphase32, p.d_dtw,
-                    p.d_dtw_off, p.d_dtimg, p.d_dtimg_off, p.d_cls_rings, p.d_cls_off, p.d_lam, p.d_lam32, p.d_lamtc, p.d_lamtc_off, p.d_lamts, p.d_lamts_off, p.d_lam_off, p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp,
+                    p.d_dtw_off, p.d_dtimg, p.d_dtimg_off, p.d_gramts, p.d_gramts_off, p.d_cls_rings, p.d_cls_off, p.d_lam, p.d_lam32, p.d_lamtc, p.d_lamtc_off, p.d_lamts, p.d_lamts_off, p.d_lam_off, p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp,
                     p.d_pair_l, p.d_pair_n, p.d_out_pair, p.d_out_lm, p.d_coef, p.d_coefT, p.d_err,
                     p.maps.ptr, p.fbuf.ptr, p.gbuf.ptr, p.rbuf.ptr, p.alm.ptr, p.scratch.ptr, p.scratch2.ptr, p.dep.ptr, p.maps32.ptr,
-                    p.ref.ptr, p.rf.ptr, p.rg.ptr, p.rr.ptr, p.ralm.ptr, p.erow.ptr, p.almdf.ptr, h->d_pair_index, h->d_noff};
+                    p.ref.ptr, p.rf.ptr, p.rg.ptr, p.rr.ptr, p.ralm.ptr, p.alm2.ptr, p.almdf2.ptr, p.adf0.ptr, p.erow.ptr, p.almdf.ptr, h->d_pair_index, h->d_noff};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     collect_stages(h);

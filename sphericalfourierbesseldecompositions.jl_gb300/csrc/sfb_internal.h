@@ -101,6 +101,12 @@ struct Plan {
     unsigned char *d_dtimg = nullptr;
     int64_t *d_dtimg_off = nullptr;
     bool dtimg_polar = false;
+    // Gram refinement (mixed precision): rings r < ral alias (nph <= 2 lmax);
+    // per block z the Gram matrix of the other rings, sliced in the synthesis
+    // layout with its gram_rows output rows as rings (null: not used)
+    int ral = 0, gram_rows = 0;
+    void *d_gramts = nullptr;
+    int64_t *d_gramts_off = nullptr;
     double *d_lam = nullptr;        // Legendre table, FP64
     float *d_lam32 = nullptr;       // the same table rounded to FP32 (mixed precision)
     void *d_lamtc = nullptr;        // split-BF16 table in tensor-core operand layout (analysis)
@@ -129,6 +135,7 @@ struct Plan {
     DevBuf<double> dep;             // sorted-deposit workspace
     DevBuf<double> ref;             // reference-map a_lm (FP64) and mean coefficients (mixed precision)
     DevBuf<double> rf, rg, rr, ralm;// workspace of the FP64 reference transform on the side stream
+    DevBuf<double> alm2, almdf2, adf0;  // Gram refinement: second (A, Adf) and the first pass's Adf
     DevBuf<double> erow;            // ring DFT row exponents [2][nrn][nmaps] (int)
     DevBuf<double> maps32;          // FP32 copy of FP64 maps (mixed precision, spline / dense-window paths)
     int64_t device_bytes = 0;
@@ -178,8 +185,9 @@ void launch_ring_synthesis(const Plan &p, const double *G, int64_t nmaps, double
 void launch_leg_analysis(const Plan &p, const double *F, int64_t ncol, double *A, bool accumulate,
                          cudaStream_t st);
 void launch_leg_synthesis(const Plan &p, const double *A, int64_t ncol, double *G, cudaStream_t st);
+// rlim: only rings r < rlim (-1: all); F == nullptr (mixed, many columns): R = -w n cfold Fold(G)
 void launch_fold_residual(const Plan &p, const double *F, const double *G, int64_t ncol, double *R, cudaStream_t st,
-                          int *Ecol = nullptr);
+                          int *Ecol = nullptr, int rlim = -1);
 void launch_radial_coeffs(const Plan &p, const double *gl_x, const double *pq, int Q, double *coef,
                           cudaStream_t st);
 void launch_project_poly(const Plan &p, const double *A, int64_t ldA, double scale, int window_kind,
@@ -196,11 +204,19 @@ void launch_build_dft_image(const Plan &p, int max_nch, cudaStream_t st);
 int64_t tc_table_offsets(const Plan &p, std::vector<int64_t> &off);
 void launch_build_lamtc(const Plan &p, const int *Ea, const int *Es, cudaStream_t st);
 // Ecol: column scales of F; computed here unless scales_ready (the fold wrote them).
+// rlim: the sum runs over the first rlim rings only (-1: all).
 void launch_leg_analysis_tc(const Plan &p, const float *F, int64_t ncol, double *A, float2 *Adf, int *Ecol,
-                            bool accumulate, cudaStream_t st, bool scales_ready = false);
-int64_t tc_synth_table_offsets(const Plan &p, std::vector<int64_t> &off);
+                            bool accumulate, cudaStream_t st, bool scales_ready = false, int rlim = -1);
+int64_t tc_synth_table_offsets(const Plan &p, std::vector<int64_t> &off, int64_t nrn = -1);
 void launch_build_lamts(const Plan &p, const int *Es, cudaStream_t st);
-void launch_leg_synthesis_tc(const Plan &p, const float2 *Adf, int64_t ncol, float *G, cudaStream_t st);
+// rlim: ring tiles covering the first rlim rings only (-1: all)
+void launch_leg_synthesis_tc(const Plan &p, const float2 *Adf, int64_t ncol, float *G, cudaStream_t st,
+                             int rlim = -1);
+// Gram refinement step of the mixed transform (alias-free rings):
+//   Anew = A + (A0 - M A) per block, A in FP64 (A) and double-float (Adf)
+void launch_gram_update(const Plan &p, const double *A, const float2 *Adf, const float2 *A0, int64_t ncol,
+                        double *Anew, float2 *Adfnew, cudaStream_t st);
+int build_gram_tables(Plan &p, cudaStream_t st);
 void launch_transpose(const double *in, int64_t rows, int64_t cols, double *out, cudaStream_t st);
 void launch_check_finite(const double *x, int64_t n, int *err, cudaStream_t st);
 void launch_ang2pix(int64_t nside, const double *theta, const double *phi, int64_t n, int64_t *pix,

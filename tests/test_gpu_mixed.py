@@ -97,6 +97,24 @@ def test_dft_twiddle_image_matches_gather(monkeypatch):
     assert _errors(gat, f64)[0] < MIXED_TOL and _errors(img, f64)[0] < MIXED_TOL
 
 
+def test_gram_refinement_matches_full_passes(monkeypatch):
+    """The refinement passes of the mixed transform use the Gram matrices of
+    the alias-free rings plus synthesis / fold / analysis over the aliased
+    rings only; the full passes over every ring (SFBGPU_GRAM_REFINEMENT=0)
+    compute the same a_lm up to rounding."""
+    cfg = (0.05, 500.0, 1000.0, 32, 200_000, 9)
+    a, rtp, w, win, nbar = _setup(*cfg)
+    gram = sfbgpu.cat2amln(rtp, a, nbar, win, w, precision="mixed")
+    monkeypatch.setenv("SFBGPU_GRAM_REFINEMENT", "0")
+    b = sfbgpu.AnlmModes(*cfg[:3], nside=cfg[3])
+    full = sfbgpu.cat2amln(rtp, b, nbar, win, w, precision="mixed")
+    f64 = sfbgpu.cat2amln(rtp, a, nbar, win, w, precision="fp64")
+    e_gf = _errors(gram, full)[0]
+    e_g, e_f = _errors(gram, f64)[0], _errors(full, f64)[0]
+    record("gram_vs_full_refinement", e_gf, gram_vs_fp64=e_g, full_vs_fp64=e_f)
+    assert e_g < MIXED_TOL and e_f < MIXED_TOL and e_gf < MIXED_TOL
+
+
 def test_mixed_vs_reference_algorithm():
     a, rtp, w, win, nbar = _setup(0.03, 500.0, 1000.0, 16, 50_000, 3)
     md = modes_dict(a)
