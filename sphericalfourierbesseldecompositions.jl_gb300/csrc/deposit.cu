@@ -36,7 +36,7 @@ constexpr int SCAN_ITEMS = 16;                    // per thread
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 
 __global__ void k_deposit_keys(const double *__restrict__ rtp, const double *__restrict__ wgt, int64_t ngal,
-                               int64_t nside, int64_t npix, double rmin, double rmax, int pieces,
+                               int64_t nside, int64_t npix, double rmin, double rmax, double inv_width, int pieces,
                                int32_t *__restrict__ counts, int32_t *__restrict__ key, int32_t *__restrict__ rank,
                                double *__restrict__ xloc, int *err) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -57,8 +57,9 @@ __global__ void k_deposit_keys(const double *__restrict__ rtp, const double *__r
         } else if (r > rmax) {
             slot = pieces + 1;
         } else {
-            // u = (r - rmin) / width in units of the pieces; x in [-1, 1] on the piece
-            const double u = (r - rmin) * ((double)pieces / (rmax - rmin));
+            // u = (r - rmin) / width in units of the pieces (inv_width = pieces / (rmax - rmin),
+            // formed once on the host); x in [-1, 1] on the piece
+            const double u = (r - rmin) * inv_width;
             slot = (int)u;
             if (slot >= pieces) slot = pieces - 1;
             x = 2.0 * (u - (double)slot) - 1.0;
@@ -434,7 +435,9 @@ int deposit_sorted(Plan &p, const double *rtp, const double *w, int64_t ngal, do
         if (chunk_ready && nchunks > 0) SFB_CUDA_TRY(cudaStreamWaitEvent(st, chunk_ready[c], 0));
         if (n <= 0) continue;
         k_deposit_keys<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(rtp + 3 * g0, w ? w + g0 : nullptr, n, p.nside,
-                                                                    p.npix, p.rmin, p.rmax, p.pieces, counts, key + g0,
+                                                                    p.npix, p.rmin, p.rmax,
+                                                                    (double)p.pieces / (p.rmax - p.rmin), p.pieces,
+                                                                    counts, key + g0,
                                                                     rank + g0, xloc + g0, p.d_err);
         note_launch();
     }

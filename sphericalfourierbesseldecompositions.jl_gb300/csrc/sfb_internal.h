@@ -292,12 +292,14 @@ __device__ __forceinline__ int64_t ang2pix_ring_fast(int64_t nside, double th, d
                 const float temp1 = ns * (0.5f + tt), temp2 = ns * z * 0.75f;
                 const float a = temp1 - temp2, b = temp1 + temp2;
                 if (far(a) && far(b)) {
-                    const int64_t jp = (int64_t)floorf(a), jm = (int64_t)floorf(b);
-                    const int64_t ir = nside + 1 + jp - jm;
-                    const int64_t kshift = 1 - (ir & 1);
-                    const int64_t t1 = jp + jm - nside + kshift + 1 + 8 * nside;
-                    const int64_t ip = (t1 >> 1) % (4 * nside);
-                    const int64_t pix = 2 * nside * (nside - 1) + (ir - 1) * 4 * nside + ip;
+                    // ring and in-ring indices fit 32 bits for nside <= 2^16
+                    const int n32 = (int)nside;
+                    const int jp = (int)floorf(a), jm = (int)floorf(b);
+                    const int ir = n32 + 1 + jp - jm;
+                    const int kshift = 1 - (ir & 1);
+                    const int t1 = jp + jm - n32 + kshift + 1 + 8 * n32;
+                    const int ip = (int)((unsigned)(t1 >> 1) % (unsigned)(4 * n32));
+                    const int64_t pix = 2 * nside * (nside - 1) + (int64_t)(ir - 1) * 4 * nside + ip;
                     if (pix >= 0 && pix < 12 * nside * nside) return pix;
                 }
             } else {
@@ -308,11 +310,12 @@ __device__ __forceinline__ int64_t ang2pix_ring_fast(int64_t nside, double th, d
                 const float tmp = ns * sqrtf(3.0f * omz);
                 const float a = tp * tmp, b = (1.0f - tp) * tmp;
                 if (far(a) && far(b)) {
-                    const int64_t ir = (int64_t)floorf(a) + (int64_t)floorf(b) + 1;
+                    const int ir = (int)floorf(a) + (int)floorf(b) + 1;
                     const float q = tt * (float)ir;
                     if (far(q)) {
-                        const int64_t ip = (int64_t)floorf(q) % (4 * ir);
-                        return z > 0.0f ? 2 * ir * (ir - 1) + ip : 12 * nside * nside - 2 * ir * (ir + 1) + ip;
+                        const int ip = (int)((unsigned)floorf(q) % (unsigned)(4 * ir));
+                        const int64_t ir64 = ir;
+                        return z > 0.0f ? 2 * ir64 * (ir64 - 1) + ip : 12 * nside * nside - 2 * ir64 * (ir64 + 1) + ip;
                     }
                 }
             }
