@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_analysis_tc(const __nv_bfloat16 
                                                             int nchunks, int rlim, const float *__restrict__ F,
                                                             int64_t ncol, const int *__restrict__ Ecol,
                                                             double *__restrict__ A, float2 *__restrict__ Adf,
-                                                            int accumulate, int *err) {
+                                                            int accumulate, int *__restrict__ Eout, int *err) {
     extern __shared__ __align__(1024) unsigned char smem[];
     const int z = blockIdx.z;
     const int m = z >> 1, par = z & 1;
@@ -256,7 +256,7 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_analysis_tc(const __nv_bfloat16 
             if (issued != nchunks) atomicExch(cs.bad, 1);
         }
     } else {
-        float pre[2][8];          // this thread's 8 ring values of chunks kc and kc + 1
+        float pre[4][8];          // this thread's 8 ring values of chunks kc .. kc + 3
         auto loadA = [&](int kc, float (&buf)[8]) {
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
@@ -287,17 +287,20 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_analysis_tc(const __nv_bfloat16 
             const uint32_t off = core_off(c, 8 * kh);
 #pragma unroll
             for (int q = 0; q < 4; ++q) st_v4(sa + q * PLANE_A + off, w[q]);
-            if (kc + 2 < nchunks) loadA(kc + 2, cur);
+            if (kc + 4 < nchunks) loadA(kc + 4, cur);
             fence_proxy_async();
             __syncwarp();
             if ((tid & 31) == 0) mbar_arrive(&cs.full_a[s]);       // one arrival per producer warp
             return true;
         };
-        loadA(0, pre[0]);
-        if (nchunks > 1) loadA(1, pre[1]);
-        for (int kc = 0; kc < nchunks; kc += 2) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (q < nchunks) loadA(q, pre[q]);
+        for (int kc = 0; kc < nchunks; kc += 4) {
             if (!chunk(kc, pre[0])) break;
             if (kc + 1 < nchunks && !chunk(kc + 1, pre[1])) break;
+            if (kc + 2 < nchunks && !chunk(kc + 2, pre[2])) break;
+            if (kc + 3 < nchunks && !chunk(kc + 3, pre[3])) break;
         }
     }
     // every thread: wait for all MMAs, then the epilogue
@@ -307,43 +310,58 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_analysis_tc(const __nv_bfloat16 
     if (!ok) {
         if (tid == 0) atomicOr(err, ERR_TC_TIMEOUT);
     } else if (prod) {
-        // warp w reads TMEM lanes 32 (w % 4).. (columns) and rows li in [32 (w / 4), +32)
+        // warp w reads TMEM lanes 32 (w % 4).. (columns) and rows li in [32 (w / 4), +32), eight rows at a
+        // time: the eight rows' old values are loaded together (no dependent round trips)
         const int lq = warp & 3, hg = warp >> 2;
         const uint32_t lane_base = (uint32_t)(lq * 32) << 16;
         const int64_t cc = col0 + lq * 32 + (tid & 31);
-        for (int g = 0; g < 2; ++g) {
-            const int i0 = 32 * hg + 16 * g;
+        float mx = 0.f;
+        for (int g = 0; g < 4; ++g) {
+            const int i0 = 32 * hg + 8 * g;
             if (i0 >= NPc) break;                           // warp-uniform
-            float v0[16], v1[16], v2[16], v3[16];
-            tmem_ld16(tmem + lane_base + (uint32_t)i0, v0);
-            tmem_ld16(tmem + lane_base + (uint32_t)(NMAX + i0), v1);
-            tmem_ld16(tmem + lane_base + (uint32_t)(2 * NMAX + i0), v2);
-            tmem_ld16(tmem + lane_base + (uint32_t)(3 * NMAX + i0), v3);
+            float v0[8], v1[8], v2[8], v3[8];
+            tmem_ld8(tmem + lane_base + (uint32_t)i0, v0);
+            tmem_ld8(tmem + lane_base + (uint32_t)(NMAX + i0), v1);
+            tmem_ld8(tmem + lane_base + (uint32_t)(2 * NMAX + i0), v2);
+            tmem_ld8(tmem + lane_base + (uint32_t)(3 * NMAX + i0), v3);
             if (cc < ncol) {
+                auto off = [&](int i) {
+                    const int l = m + par + 2 * (row0 + i0 + i);
+                    return ((int64_t)l * (l + 1) / 2 + m) * ncol + cc;
+                };
+                double aold[8];
+                float2 dold[8];
 #pragma unroll
-                for (int i = 0; i < 16; ++i) {
-                    const int li = row0 + i0 + i;
-                    if (li >= nrows) break;
+                for (int i = 0; i < 8; ++i) {
+                    aold[i] = 0.0;
+                    dold[i] = make_float2(0.f, 0.f);
+                    if (accumulate && row0 + i0 + i < nrows) {
+                        const int64_t o = off(i);
+                        aold[i] = A[o];
+                        dold[i] = Adf[o];
+                    }
+                }
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    if (row0 + i0 + i >= nrows) continue;
+                    const int64_t o = off(i);
                     float hi, lo;
                     lvl_sum(v0[i], v1[i], v2[i], v3[i], hi, lo);
-                    const int l = m + par + 2 * li;
-                    const int64_t o = ((int64_t)l * (l + 1) / 2 + m) * ncol + cc;
-                    if (accumulate) {
-                        A[o] = A[o] + ((double)hi + (double)lo);
-                        float2 d = Adf[o];
-                        // double-float accumulation of (hi, lo) into d
-                        const float s = d.x + hi;
-                        const float zz = s - d.x;
-                        const float e = ((d.x - (s - zz)) + (hi - zz)) + (d.y + lo);
-                        const float h2 = s + e;
-                        Adf[o] = make_float2(h2, e - (h2 - s));
-                    } else {
-                        A[o] = (double)hi + (double)lo;
-                        Adf[o] = make_float2(hi, lo);
-                    }
+                    // double-float accumulation of (hi, lo) into the old value (zero without accumulate)
+                    const float2 d = dold[i];
+                    const float s = d.x + hi;
+                    const float zz = s - d.x;
+                    const float e = ((d.x - (s - zz)) + (hi - zz)) + (d.y + lo);
+                    const float h2 = s + e;
+                    Adf[o] = make_float2(h2, e - (h2 - s));
+                    A[o] = aold[i] + ((double)hi + (double)lo);
+                    mx = fmaxf(mx, fabsf(h2));
                 }
             }
         }
+        // column exponent of the new coefficients (the synthesis-side slicing scale)
+        // (threads without a row in range, or with only zeros, leave the column's preset value)
+        if (Eout && cc < ncol && mx > 0.f) atomicMax(Eout + (int64_t)z * ncol + cc, scale_exp(mx));
     }
     lvl_teardown(tmem);
 }
@@ -361,7 +379,8 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_synthesis_tc(const __nv_bfloat16
                                                              int NT, const float2 *__restrict__ Adf, int64_t ncol,
                                                              float *__restrict__ G, const double *__restrict__ Acur,
                                                              const float2 *__restrict__ A0, double *__restrict__ Anew,
-                                                             float2 *__restrict__ Adfnew, int *err) {
+                                                             float2 *__restrict__ Adfnew, const int *__restrict__ Ein,
+                                                             int *__restrict__ Eout, int *err) {
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ float red[2][MTILE];
     const int z = blockIdx.z;
@@ -394,13 +413,24 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_synthesis_tc(const __nv_bfloat16
         const int l = m + par + 2 * li;
         return Adf[((int64_t)l * (l + 1) / 2 + m) * ncol + col0 + c];
     };
-    // column scale over the rows (|hi + lo| < 2^E: hi is an FP32 value below 2^E, |lo| <= ulp(hi)/2)
-    float mx = 0.f;
-    for (int li = kh; li < nrows; li += 2) mx = fmaxf(mx, fabsf(aval(li).x));
-    if (prod) red[kh][c] = mx;
+    // column scale over the rows (|hi + lo| < 2^E: hi is an FP32 value below 2^E, |lo| <= ulp(hi)/2):
+    // given by the kernel that wrote the coefficients (Ein), or a pass over them here
+    if (!Ein) {
+        float mx = 0.f;
+        for (int li = kh; li < nrows; li += 2) mx = fmaxf(mx, fabsf(aval(li).x));
+        if (prod) red[kh][c] = mx;
+    }
     const uint32_t tmem = lvl_setup(cs);      // includes a __syncthreads
     float C[4];
-    slice_consts(scale_exp(fmaxf(red[0][c], red[1][c])), C);
+    int Ecl = 0;
+    if (Ein) {
+        // an all-zero column keeps the preset (below any exponent): any scale slices zeros exactly
+        const int ev = cok ? Ein[(int64_t)z * ncol + col0 + c] : 0;
+        Ecl = ev < -1000 ? 0 : ev;
+    } else {
+        Ecl = scale_exp(fmaxf(red[0][c], red[1][c]));
+    }
+    slice_consts(Ecl, C);
     const uint32_t idesc = idesc_bf16(MTILE, NT);
 
     if (!prod) {
@@ -456,17 +486,18 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_synthesis_tc(const __nv_bfloat16
         const int lq = warp & 3, hg = warp >> 2;
         const uint32_t lane_base = (uint32_t)(lq * 32) << 16;
         const int64_t cc = col0 + lq * 32 + lane;
-        for (int g = 0; g < 2; ++g) {
-            const int i0 = 32 * hg + 16 * g;
+        float umx = 0.f;          // update mode: largest new |coefficient| of this column
+        for (int g = 0; g < 4; ++g) {
+            const int i0 = 32 * hg + 8 * g;
             if (i0 >= NT) break;                            // warp-uniform
-            float v0[16], v1[16], v2[16], v3[16];
-            tmem_ld16(tmem + lane_base + (uint32_t)i0, v0);
-            tmem_ld16(tmem + lane_base + (uint32_t)(NMAX + i0), v1);
-            tmem_ld16(tmem + lane_base + (uint32_t)(2 * NMAX + i0), v2);
-            tmem_ld16(tmem + lane_base + (uint32_t)(3 * NMAX + i0), v3);
+            float v0[8], v1[8], v2[8], v3[8];
+            tmem_ld8(tmem + lane_base + (uint32_t)i0, v0);
+            tmem_ld8(tmem + lane_base + (uint32_t)(NMAX + i0), v1);
+            tmem_ld8(tmem + lane_base + (uint32_t)(2 * NMAX + i0), v2);
+            tmem_ld8(tmem + lane_base + (uint32_t)(3 * NMAX + i0), v3);
             if (cc < ncol && !upd) {
 #pragma unroll
-                for (int i = 0; i < 16; ++i) {
+                for (int i = 0; i < 8; ++i) {
                     const int r = r0 + i0 + i;
                     if (r >= nrn) break;
                     float hi, lo;
@@ -474,28 +505,45 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_synthesis_tc(const __nv_bfloat16
                     Gz[(int64_t)r * ncol + cc] = hi;
                 }
             } else if (cc < ncol) {
+                // the eight rows' old values are loaded together (no dependent round trips)
+                auto off = [&](int i) {
+                    const int l = m + par + 2 * (r0 + i0 + i);
+                    return ((int64_t)l * (l + 1) / 2 + m) * ncol + cc;
+                };
+                float2 a0[8], ac[8];
+                double acur[8];
 #pragma unroll
-                for (int i = 0; i < 16; ++i) {
-                    const int r = r0 + i0 + i;
-                    if (r >= nrows) break;
+                for (int i = 0; i < 8; ++i) {
+                    a0[i] = ac[i] = make_float2(0.f, 0.f);
+                    acur[i] = 0.0;
+                    if (r0 + i0 + i < nrows) {
+                        const int64_t o = off(i);
+                        a0[i] = A0[o];
+                        ac[i] = Adf[o];
+                        acur[i] = Acur[o];
+                    }
+                }
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    if (r0 + i0 + i >= nrows) continue;
+                    const int64_t o = off(i);
                     float hi, lo;
                     lvl_sum(v0[i], v1[i], v2[i], v3[i], hi, lo);
-                    const int l = m + par + 2 * r;
-                    const int64_t o = ((int64_t)l * (l + 1) / 2 + m) * ncol + cc;
                     // d = A0 - (hi, lo) and Adf + d in double-float (TwoSum, renormalised)
-                    const float2 a0 = A0[o], ac = Adf[o];
-                    float s = a0.x - hi, z2 = s - a0.x;
-                    float e = ((a0.x - (s - z2)) + (-hi - z2)) + (a0.y - lo);
-                    float dh = s + e, dl = e - (dh - s);
-                    s = ac.x + dh;
-                    z2 = s - ac.x;
-                    e = ((ac.x - (s - z2)) + (dh - z2)) + (ac.y + dl);
+                    float s = a0[i].x - hi, z2 = s - a0[i].x;
+                    float e = ((a0[i].x - (s - z2)) + (-hi - z2)) + (a0[i].y - lo);
+                    const float dh = s + e, dl = e - (dh - s);
+                    s = ac[i].x + dh;
+                    z2 = s - ac[i].x;
+                    e = ((ac[i].x - (s - z2)) + (dh - z2)) + (ac[i].y + dl);
                     const float nh = s + e;
                     Adfnew[o] = make_float2(nh, e - (nh - s));
-                    Anew[o] = Acur[o] + ((double)dh + (double)dl);
+                    Anew[o] = acur[i] + ((double)dh + (double)dl);
+                    umx = fmaxf(umx, fabsf(nh));
                 }
             }
         }
+        if (upd && Eout && cc < ncol && umx > 0.f) atomicMax(Eout + (int64_t)z * ncol + cc, scale_exp(umx));
     }
     lvl_teardown(tmem);
 }
@@ -651,7 +699,7 @@ void launch_build_lamtc(const Plan &p, const int *Ea, const int *Es, cudaStream_
 }
 
 void launch_leg_analysis_tc(const Plan &p, const float *F, int64_t ncol, double *A, float2 *Adf, int *Ecol,
-                            bool accumulate, cudaStream_t st, bool scales_ready, int rlim) {
+                            bool accumulate, cudaStream_t st, bool scales_ready, int rlim, int *Eout) {
     if (rlim < 0 || rlim > p.nrn) rlim = (int)p.nrn;
     if (!scales_ready) {
         dim3 grid((unsigned)((ncol + 255) / 256), (unsigned)(2 * (p.lmax + 1)));
@@ -663,7 +711,8 @@ void launch_leg_analysis_tc(const Plan &p, const float *F, int64_t ncol, double 
     dim3 grid((unsigned)((ncol + tc::MTILE - 1) / tc::MTILE), (unsigned)ntile, (unsigned)(2 * (p.lmax + 1)));
     tc::k_leg_analysis_tc<<<grid, tc::NTH, tc::LEG_SMEM, st>>>((const __nv_bfloat16 *)p.d_lamtc, p.d_lamtc_off,
                                                               p.lmax, (int)p.nrn, (rlim + tc::KC - 1) / tc::KC, rlim,
-                                                              F, ncol, Ecol, A, Adf, accumulate ? 1 : 0, p.d_err);
+                                                              F, ncol, Ecol, A, Adf, accumulate ? 1 : 0, Eout,
+                                                              p.d_err);
     note_launch();
 }
 
@@ -702,7 +751,8 @@ void launch_build_lamts(const Plan &p, const int *Es, cudaStream_t st) {
     note_launch();
 }
 
-void launch_leg_synthesis_tc(const Plan &p, const float2 *Adf, int64_t ncol, float *G, cudaStream_t st, int rlim) {
+void launch_leg_synthesis_tc(const Plan &p, const float2 *Adf, int64_t ncol, float *G, cudaStream_t st, int rlim,
+                             const int *Ein) {
     const int NT = tc_synth_nt(p);
     if (rlim < 0 || rlim > p.nrn) rlim = (int)p.nrn;
     set_smem(tc::k_leg_synthesis_tc, tc::LEG_SMEM);
@@ -711,19 +761,19 @@ void launch_leg_synthesis_tc(const Plan &p, const float2 *Adf, int64_t ncol, flo
               (unsigned)(2 * (p.lmax + 1)));
     tc::k_leg_synthesis_tc<<<grid, tc::NTH, tc::LEG_SMEM, st>>>((const __nv_bfloat16 *)p.d_lamts, p.d_lamts_off,
                                                                p.lmax, (int)p.nrn, NT, Adf, ncol, G, nullptr, nullptr,
-                                                               nullptr, nullptr, p.d_err);
+                                                               nullptr, nullptr, Ein, nullptr, p.d_err);
     note_launch();
 }
 
 void launch_gram_update(const Plan &p, const double *A, const float2 *Adf, const float2 *A0, int64_t ncol,
-                        double *Anew, float2 *Adfnew, cudaStream_t st) {
+                        double *Anew, float2 *Adfnew, cudaStream_t st, const int *Ein, int *Eout) {
     const int NT = tc_synth_nt(p.gram_rows);
     set_smem(tc::k_leg_synthesis_tc, tc::LEG_SMEM);
     dim3 grid((unsigned)((ncol + tc::MTILE - 1) / tc::MTILE), (unsigned)((p.gram_rows + NT - 1) / NT),
               (unsigned)(2 * (p.lmax + 1)));
     tc::k_leg_synthesis_tc<<<grid, tc::NTH, tc::LEG_SMEM, st>>>((const __nv_bfloat16 *)p.d_gramts, p.d_gramts_off,
                                                                p.lmax, p.gram_rows, NT, Adf, ncol, nullptr, A, A0,
-                                                               Anew, Adfnew, p.d_err);
+                                                               Anew, Adfnew, Ein, Eout, p.d_err);
     note_launch();
 }
 

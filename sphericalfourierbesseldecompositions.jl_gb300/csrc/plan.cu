@@ -359,22 +359,31 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, b
         SFB_TRY(grow(p, p.alm2, (size_t)p.lmsize * ncol));
         SFB_TRY(grow(p, p.almdf2, (size_t)p.lmsize * ncol));
         SFB_TRY(grow(p, p.adf0, (size_t)p.lmsize * ncol));
+        // column exponents of each (A, Adf) set, written by whichever kernel completes the set
+        const int64_t nE = 2 * (p.lmax + 1) * ncol;
+        SFB_TRY(grow(p, p.ecoef, (size_t)nE + 1));
         double *Ab[2] = {alm.ptr, p.alm2.ptr};
         float2 *Db[2] = {adf, reinterpret_cast<float2 *>(p.almdf2.ptr)};
+        int *Eb[2] = {reinterpret_cast<int *>(p.ecoef.ptr), reinterpret_cast<int *>(p.ecoef.ptr) + nE};
         const float2 *a0 = reinterpret_cast<const float2 *>(p.adf0.ptr);
         int cur = p.niter & 1;
+        // 0x80 bytes: every exponent word starts below any scale exponent (atomicMax)
+        SFB_CUDA_TRY(cudaMemsetAsync(Eb[cur], 0x80, (size_t)nE * sizeof(int), st));
         {
             Stage s(h, stage(SFB_STAGE_LEG_ANALYSIS), st);
-            launch_leg_analysis_tc(p, (const float *)fbuf.ptr, ncol, Ab[cur], Db[cur], ecol, false, st, false);
+            launch_leg_analysis_tc(p, (const float *)fbuf.ptr, ncol, Ab[cur], Db[cur], ecol, false, st, false, -1,
+                                   Eb[cur]);
         }
         SFB_CUDA_TRY(cudaMemcpyAsync(p.adf0.ptr, Db[cur], (size_t)p.lmsize * ncol * sizeof(float2),
                                      cudaMemcpyDeviceToDevice, st));
         for (int it = 0; it < p.niter; ++it) {
             const int nxt = cur ^ 1;
+            SFB_CUDA_TRY(cudaMemsetAsync(Eb[nxt], 0x80, (size_t)nE * sizeof(int), st));
             {
                 Stage s(h, stage(SFB_STAGE_LEG_SYNTHESIS), st);
-                if (p.ral > 0) launch_leg_synthesis_tc(p, Db[cur], ncol, (float *)gbuf.ptr, st, p.ral);
-                launch_gram_update(p, Ab[cur], Db[cur], a0, ncol, Ab[nxt], Db[nxt], st);
+                if (p.ral > 0) launch_leg_synthesis_tc(p, Db[cur], ncol, (float *)gbuf.ptr, st, p.ral, Eb[cur]);
+                launch_gram_update(p, Ab[cur], Db[cur], a0, ncol, Ab[nxt], Db[nxt], st, Eb[cur],
+                                   p.ral > 0 ? nullptr : Eb[nxt]);
             }
             if (p.ral > 0) {
                 {
@@ -383,7 +392,7 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, b
                 }
                 Stage s(h, stage(SFB_STAGE_LEG_ANALYSIS), st);
                 launch_leg_analysis_tc(p, (const float *)rbuf.ptr, ncol, Ab[nxt], Db[nxt], ecol, true, st, true,
-                                       p.ral);
+                                       p.ral, Eb[nxt]);
             }
             cur = nxt;
         }
@@ -880,7 +889,7 @@ void sfb_plan_destroy(sfb_plan *h) {
                     p.d_dtw_off, p.d_dtimg, p.d_dtimg_off, p.d_gramts, p.d_gramts_off, p.d_cls_rings, p.d_cls_off, p.d_lam, p.d_lam32, p.d_lamtc, p.d_lamtc_off, p.d_lamts, p.d_lamts_off, p.d_lam_off, p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp,
                     p.d_pair_l, p.d_pair_n, p.d_out_pair, p.d_out_lm, p.d_coef, p.d_coefT, p.d_err,
                     p.maps.ptr, p.fbuf.ptr, p.gbuf.ptr, p.rbuf.ptr, p.alm.ptr, p.scratch.ptr, p.scratch2.ptr, p.dep.ptr, p.maps32.ptr,
-                    p.ref.ptr, p.rf.ptr, p.rg.ptr, p.rr.ptr, p.ralm.ptr, p.alm2.ptr, p.almdf2.ptr, p.adf0.ptr, p.erow.ptr, p.almdf.ptr, h->d_pair_index, h->d_noff};
+                    p.ref.ptr, p.rf.ptr, p.rg.ptr, p.rr.ptr, p.ralm.ptr, p.alm2.ptr, p.almdf2.ptr, p.adf0.ptr, p.ecoef.ptr, p.erow.ptr, p.almdf.ptr, h->d_pair_index, h->d_noff};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     collect_stages(h);

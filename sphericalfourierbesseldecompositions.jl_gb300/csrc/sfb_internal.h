@@ -136,6 +136,7 @@ struct Plan {
     DevBuf<double> ref;             // reference-map a_lm (FP64) and mean coefficients (mixed precision)
     DevBuf<double> rf, rg, rr, ralm;// workspace of the FP64 reference transform on the side stream
     DevBuf<double> alm2, almdf2, adf0;  // Gram refinement: second (A, Adf) and the first pass's Adf
+    DevBuf<double> ecoef;               // Gram refinement: column exponents of both (A, Adf) sets (ints)
     DevBuf<double> erow;            // ring DFT row exponents [2][nrn][nmaps] (int)
     DevBuf<double> maps32;          // FP32 copy of FP64 maps (mixed precision, spline / dense-window paths)
     int64_t device_bytes = 0;
@@ -205,17 +206,21 @@ int64_t tc_table_offsets(const Plan &p, std::vector<int64_t> &off);
 void launch_build_lamtc(const Plan &p, const int *Ea, const int *Es, cudaStream_t st);
 // Ecol: column scales of F; computed here unless scales_ready (the fold wrote them).
 // rlim: the sum runs over the first rlim rings only (-1: all).
+// Eout (optional): atomicMax of each output column's exponent per block z (preset below every exponent).
 void launch_leg_analysis_tc(const Plan &p, const float *F, int64_t ncol, double *A, float2 *Adf, int *Ecol,
-                            bool accumulate, cudaStream_t st, bool scales_ready = false, int rlim = -1);
+                            bool accumulate, cudaStream_t st, bool scales_ready = false, int rlim = -1,
+                            int *Eout = nullptr);
 int64_t tc_synth_table_offsets(const Plan &p, std::vector<int64_t> &off, int64_t nrn = -1);
 void launch_build_lamts(const Plan &p, const int *Es, cudaStream_t st);
 // rlim: ring tiles covering the first rlim rings only (-1: all)
+// Ein (optional): the column exponents of Adf per block z, as the analysis wrote them
 void launch_leg_synthesis_tc(const Plan &p, const float2 *Adf, int64_t ncol, float *G, cudaStream_t st,
-                             int rlim = -1);
+                             int rlim = -1, const int *Ein = nullptr);
 // Gram refinement step of the mixed transform (alias-free rings):
 //   Anew = A + (A0 - M A) per block, A in FP64 (A) and double-float (Adf)
 void launch_gram_update(const Plan &p, const double *A, const float2 *Adf, const float2 *A0, int64_t ncol,
-                        double *Anew, float2 *Adfnew, cudaStream_t st);
+                        double *Anew, float2 *Adfnew, cudaStream_t st, const int *Ein = nullptr,
+                        int *Eout = nullptr);
 int build_gram_tables(Plan &p, cudaStream_t st);
 void launch_transpose(const double *in, int64_t rows, int64_t cols, double *out, cudaStream_t st);
 void launch_check_finite(const double *x, int64_t n, int *err, cudaStream_t st);
