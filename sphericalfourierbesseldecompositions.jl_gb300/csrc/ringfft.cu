@@ -27,13 +27,89 @@ __device__ __forceinline__ cx<T> cmul(cx<T> a, cx<T> b) {
 
 __device__ __forceinline__ int bitrev(int v, int s) { return s == 0 ? 0 : (int)(__brev((unsigned)v) >> (32 - s)); }
 
+namespace {
+// Double-float (FP32 pair) arithmetic for the odd-length stage of the FP64
+// transform: FP64 throughput is a small fraction of FP32 on this part, and
+// the pair keeps about 48 significant bits.
+struct df2 {
+    float hi, lo;
+};
+__device__ __forceinline__ df2 d2_of(double x) {
+    const float h = (float)x;
+    return {h, (float)(x - (double)h)};
+}
+__device__ __forceinline__ df2 d2_add(df2 a, df2 b) {
+    const float s = a.hi + b.hi;
+    const float z = s - a.hi;
+    const float e = ((a.hi - (s - z)) + (b.hi - z)) + (a.lo + b.lo);
+    const float h = s + e;
+    return {h, e - (h - s)};
+}
+__device__ __forceinline__ df2 d2_mul(df2 a, df2 b) {
+    const float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+    const float h = p + e;
+    return {h, e - (h - p)};
+}
+__device__ __forceinline__ df2 d2_neg(df2 a) { return {-a.hi, -a.lo}; }
+}  // namespace
+
+// The odd-stage input of the FP64 transform is staged as double-float
+// (re.hi, re.lo, im.hi, im.lo); other precisions stage their own type.
+template <typename T>
+__device__ __forceinline__ void store_src(cx<T> *src, int64_t i, cx<T> v) {
+    if constexpr (sizeof(T) == 8) {
+        const df2 a = d2_of(v.x), b = d2_of(v.y);
+        reinterpret_cast<float4 *>(src)[i] = make_float4(a.hi, a.lo, b.hi, b.lo);
+    } else {
+        src[i] = v;
+    }
+}
+
 // Four-step DFT of MT packed sequences held in `src` (natural order, only used
 // when o > 1) / `buf`; result in `buf`, element k at (k % o) * P + k / o.
 // dir = -1 forward (W = e^{-2 pi i/n}), +1 inverse.  `tw` holds W_n^t.
+// FP64 (T = double): the length-o DFTs run in double-float with the odd
+// roots W_o^t = W_n^{P t} staged in twd (o entries, double-float); `src` holds
+// double-float input (store_src).
 template <typename T>
-__device__ void four_step(cx<T> *buf, cx<T> *src, const cx<T> *tw, int n, int o, int s, int MT) {
+__device__ void four_step(cx<T> *buf, cx<T> *src, const cx<T> *tw, int n, int o, int s, int MT,
+                          float4 *twd = nullptr) {
     const int P = n / o;
-    if (o > 1) {
+    if constexpr (sizeof(T) == 8) {
+        if (o > 1) {
+            for (int t = threadIdx.x; t < o; t += blockDim.x) {
+                const cx<T> w = tw[P * t];
+                const df2 a = d2_of(w.x), b = d2_of(w.y);
+                twd[t] = make_float4(a.hi, a.lo, b.hi, b.lo);
+            }
+            __syncthreads();
+            const float4 *srcd = reinterpret_cast<const float4 *>(src);
+            for (int idx = threadIdx.x; idx < MT * n; idx += blockDim.x) {
+                const int b = idx / n;
+                const int rem = idx - b * n;
+                const int k1 = rem / P;
+                const int j2 = rem - k1 * P;
+                const float4 *x = srcd + (int64_t)b * n;
+                df2 ar = {0.f, 0.f}, ai = {0.f, 0.f};
+                int e = 0;                    // (j1*k1) mod o, advanced incrementally
+                for (int j1 = 0; j1 < o; ++j1) {
+                    const float4 v = x[P * j1 + j2];
+                    const float4 w = twd[e];
+                    const df2 vr = {v.x, v.y}, vi = {v.z, v.w}, wr = {w.x, w.y}, wi = {w.z, w.w};
+                    ar = d2_add(ar, d2_add(d2_mul(vr, wr), d2_neg(d2_mul(vi, wi))));
+                    ai = d2_add(ai, d2_add(d2_mul(vr, wi), d2_mul(vi, wr)));
+                    e += k1;
+                    if (e >= o) e -= o;
+                }
+                cx<T> acc = {(T)((double)ar.hi + (double)ar.lo), (T)((double)ai.hi + (double)ai.lo)};
+                acc = cmul(acc, tw[j2 * k1]);   // j2*k1 < n
+                buf[(int64_t)b * n + k1 * P + bitrev(j2, s)] = acc;
+            }
+            __syncthreads();
+        }
+    } else if (o > 1) {
         for (int idx = threadIdx.x; idx < MT * n; idx += blockDim.x) {
             const int b = idx / n;
             const int rem = idx - b * n;
@@ -111,6 +187,7 @@ __global__ void __launch_bounds__(256) k_ring_analysis(const RingGeom *rings, in
     cx<T> *tw = reinterpret_cast<cx<T> *>(smem_raw);
     cx<T> *buf = tw + n;
     cx<T> *src = buf + (int64_t)MT * n;
+    float4 *twd = reinterpret_cast<float4 *>(src + (int64_t)MT * n);     // odd roots (FP64 transform, o > 1)
     for (int t = threadIdx.x; t < n; t += blockDim.x) {
         const TW v = twtab[twoff[r] + t];
         tw[t] = {(T)v.x, (T)v.y};
@@ -128,7 +205,7 @@ __global__ void __launch_bounds__(256) k_ring_analysis(const RingGeom *rings, in
             v.x = (T)maps[mb * npix + g.start_n + j];
             if (paired) v.y = (T)maps[mb * npix + g.start_s + j];
         }
-        if (o > 1) src[(int64_t)b * n + j] = v;
+        if (o > 1) store_src(src, (int64_t)b * n + j, v);
         else buf[(int64_t)b * n + bitrev(j, s)] = v;
     }
     __syncthreads();
@@ -161,7 +238,7 @@ __global__ void __launch_bounds__(256) k_ring_analysis(const RingGeom *rings, in
         }
         __syncthreads();
     }
-    four_step<T>(buf, src, tw, n, o, s, MT);
+    four_step<T>(buf, src, tw, n, o, s, MT, twd);
     // unpack, phase, weight; write F+ and F-
     const int L1 = lmax + 1;
     for (int idx = threadIdx.x; idx < MT * L1; idx += blockDim.x) {
@@ -214,6 +291,7 @@ __global__ void __launch_bounds__(256) k_ring_synthesis(const RingGeom *rings, i
     cx<T> *tw = reinterpret_cast<cx<T> *>(smem_raw);
     cx<T> *buf = tw + n;
     cx<T> *src = buf + (int64_t)MT * n;
+    float4 *twd = reinterpret_cast<float4 *>(src + (int64_t)MT * n);     // odd roots (o > 1)
     fill_twiddles(tw, twtab + twoff[r], n, +1);
     const int L1 = lmax + 1;
     // spectrum of the packed sequence: c_k = CN_k + i CS_k
@@ -250,11 +328,11 @@ __global__ void __launch_bounds__(256) k_ring_synthesis(const RingGeom *rings, i
         }
         // c = CN + i CS
         const cx<T> v = {(T)(cnx - csy), (T)(cny + csx)};
-        if (o > 1) src[(int64_t)b * n + k] = v;
+        if (o > 1) store_src(src, (int64_t)b * n + k, v);
         else buf[(int64_t)b * n + bitrev(k, s)] = v;
     }
     __syncthreads();
-    four_step<T>(buf, src, tw, n, o, s, MT);
+    four_step<T>(buf, src, tw, n, o, s, MT, twd);
     for (int idx = threadIdx.x; idx < MT * n; idx += blockDim.x) {
         const int b = idx / n;
         const int j = idx - b * n;
@@ -266,9 +344,15 @@ __global__ void __launch_bounds__(256) k_ring_synthesis(const RingGeom *rings, i
     }
 }
 
+// shared memory of one CTA: twiddles, buf (and src) per map, and with src the
+// odd roots (n 16-byte entries at most)
+static size_t ring_smem(size_t n, size_t elem, bool two_buffers, int mt) {
+    return n * elem * (1 + (two_buffers ? 2 : 1) * (size_t)mt) + (two_buffers ? n * 16 : 0);
+}
+
 static int ring_mt(size_t n, size_t elem, bool two_buffers) {
     for (int mt = 8; mt >= 1; mt >>= 1)
-        if (n * elem * (1 + (two_buffers ? 2 : 1) * (size_t)mt) <= 96 * 1024) return mt;   // <= 2 CTAs per SM
+        if (ring_smem(n, elem, two_buffers, mt) <= 112 * 1024) return mt;   // <= 2 CTAs per SM
     return 1;
 }
 
@@ -286,7 +370,7 @@ static void ring_analysis_t(const Plan &p, const TI *maps, int64_t nmaps, T *F, 
     for (const Group &gr : groups) {
         if (gr.nr <= 0) continue;
         const int MT = ring_mt(gr.n, sizeof(cx<T>), gr.two);
-        const size_t smem = gr.n * sizeof(cx<T>) * (1 + (gr.two ? 2 : 1) * (size_t)MT);
+        const size_t smem = ring_smem(gr.n, sizeof(cx<T>), gr.two, MT);
         set_smem(k_ring_analysis<T, TI, TW>, smem);
         dim3 grid((unsigned)gr.nr, (unsigned)((nmaps + MT - 1) / MT));
         k_ring_analysis<T, TI, TW><<<grid, 256, smem, st>>>(p.d_rings, (int)p.nrn, p.lmax, p.npix, maps, nmaps, MT,
@@ -311,7 +395,7 @@ void launch_ring_synthesis(const Plan &p, const double *G, int64_t nmaps, double
     for (const Group &gr : groups) {
         if (gr.nr <= 0) continue;
         const int MT = ring_mt(gr.n, sizeof(cx<double>), gr.two);
-        const size_t smem = gr.n * sizeof(cx<double>) * (1 + (gr.two ? 2 : 1) * (size_t)MT);
+        const size_t smem = ring_smem(gr.n, sizeof(cx<double>), gr.two, MT);
         set_smem(k_ring_synthesis<double>, smem);
         dim3 grid((unsigned)gr.nr, (unsigned)((nmaps + MT - 1) / MT));
         k_ring_synthesis<double><<<grid, 256, smem, st>>>(p.d_rings, (int)p.nrn, p.lmax, G, 2 * nmaps, nmaps, MT,
