@@ -223,25 +223,25 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
             if (issued != nch) atomicExch(bad, 1);
         }
     } else {
-        // raw map values of the next chunk (n is a multiple of 4, ring starts are 16-byte aligned)
+        // raw map values of the next PD chunks (n is a multiple of 4, ring starts are 16-byte aligned)
         constexpr int NV4 = IMG ? 4 : 8;          // float4 loads per thread per chunk
-        float4 pre[NV4];
-        auto load_chunk = [&](int kc) {
+        constexpr int PD = IMG ? 2 : 1;           // chunks loaded ahead
+        float4 pre[PD][NV4];
+        auto load_chunk = [&](int kc, float4 (&buf)[NV4]) {
 #pragma unroll
             for (int i = 0; i < NV4; ++i) {
                 const int j = kc * KC + 16 * ahalf + 4 * i;
-                pre[i] = (live && j < n) ? *reinterpret_cast<const float4 *>(x + j) : make_float4(0.f, 0.f, 0.f, 0.f);
+                buf[i] = (live && j < n) ? *reinterpret_cast<const float4 *>(x + j) : make_float4(0.f, 0.f, 0.f, 0.f);
             }
         };
-        if (abuild) load_chunk(0);
-        for (int kc = 0; kc < nch; ++kc) {
+        auto do_chunk = [&](int kc, float4 (&cur)[NV4]) -> bool {
             const int st = kc % NSTAGE;
             if (kc >= NSTAGE) {
                 // the stage is free once the MMAs of chunk kc - NSTAGE completed
-                if (*(volatile int *)bad) break;
+                if (*(volatile int *)bad) return false;
                 if (!mbar_wait(&empty[st], (uint32_t)(((kc / NSTAGE) - 1) & 1))) {
                     atomicExch(bad, 1);
-                    break;
+                    return false;
                 }
             }
             unsigned char *sbase = smem + st * STAGE;         // A planes 0..3, B planes 4..7
@@ -256,15 +256,15 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
                 // A row: this thread's pixels as groups of 8
 #pragma unroll
                 for (int gq = 0; gq < NV4 / 2; ++gq) {
-                    const float v[8] = {pre[2 * gq].x, pre[2 * gq].y, pre[2 * gq].z, pre[2 * gq].w,
-                                        pre[2 * gq + 1].x, pre[2 * gq + 1].y, pre[2 * gq + 1].z, pre[2 * gq + 1].w};
+                    const float v[8] = {cur[2 * gq].x, cur[2 * gq].y, cur[2 * gq].z, cur[2 * gq].w,
+                                        cur[2 * gq + 1].x, cur[2 * gq + 1].y, cur[2 * gq + 1].z, cur[2 * gq + 1].w};
                     uint32_t w[4][4];
                     slice8(v, C, w);
                     const uint32_t off = core_off(ti, 16 * ahalf + 8 * gq);
 #pragma unroll
                     for (int s = 0; s < 4; ++s) st_shared_v4(sbase + s * PLANE + off, w[s]);
                 }
-                if (kc + 1 < nch) load_chunk(kc + 1);
+                if (kc + PD < nch) load_chunk(kc + PD, cur);
             } else if constexpr (!IMG) {
                 // B row: table slices at k = m (2 j + t) + part n/2 (mod 2n)
 #pragma unroll
@@ -294,6 +294,18 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
             fence_proxy_async();
             __syncwarp();
             if (lane == 0) mbar_arrive(&full[st]);      // one arrival per producer warp
+            return true;
+        };
+        if (abuild) {
+#pragma unroll
+            for (int q = 0; q < PD; ++q)
+                if (q < nch) load_chunk(q, pre[q]);
+        }
+        for (int kc = 0; kc < nch; kc += PD) {
+            if (!do_chunk(kc, pre[0])) break;
+            if constexpr (PD > 1) {
+                if (kc + 1 < nch && !do_chunk(kc + 1, pre[1])) break;
+            }
         }
     }
     // all MMAs complete before TMEM is read or released
