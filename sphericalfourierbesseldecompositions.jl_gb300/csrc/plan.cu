@@ -864,6 +864,9 @@ int sfb_plan_create(const sfb_plan_desc *d, sfb_plan **out) {
             const size_t nct = (size_t)(p.lmax + 1) * p.nbasis * p.nmax;
             if ((st = upload<float2>(p, &p.d_coefT, nullptr, nct)) != SFB_OK) break;
             launch_coef_df(p, h->d_pair_index, p.d_coefT, h->stream);
+            const std::vector<int3> tiles = project_tiles(pair_index, (int)p.lmax, (int)p.nmax);
+            p.n_proj_tiles = (int64_t)tiles.size();
+            if ((st = upload(p, &p.d_proj_tiles, tiles.data(), tiles.size())) != SFB_OK) break;
         } else {
             p.nbasis = p.npairs;
         }
@@ -887,7 +890,7 @@ void sfb_plan_destroy(sfb_plan *h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     void *ptrs[] = {p.d_rings, p.d_twtab, p.d_twoff, p.d_phase, p.d_wphase, p.d_twtab32, p.d_wphase32, p.d_dtw,
                     p.d_dtw_off, p.d_dtimg, p.d_dtimg_off, p.d_gramts, p.d_gramts_off, p.d_cls_rings, p.d_cls_off, p.d_lam, p.d_lam32, p.d_lamtc, p.d_lamtc_off, p.d_lamts, p.d_lamts_off, p.d_lam_off, p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp,
-                    p.d_pair_l, p.d_pair_n, p.d_out_pair, p.d_out_lm, p.d_coef, p.d_coefT, p.d_err,
+                    p.d_pair_l, p.d_pair_n, p.d_out_pair, p.d_out_lm, p.d_coef, p.d_coefT, p.d_proj_tiles, p.d_err,
                     p.maps.ptr, p.fbuf.ptr, p.gbuf.ptr, p.rbuf.ptr, p.alm.ptr, p.scratch.ptr, p.scratch2.ptr, p.dep.ptr, p.maps32.ptr,
                     p.ref.ptr, p.rf.ptr, p.rg.ptr, p.rr.ptr, p.ralm.ptr, p.alm2.ptr, p.almdf2.ptr, p.adf0.ptr, p.ecoef.ptr, p.erow.ptr, p.almdf.ptr, h->d_pair_index, h->d_noff};
     for (void *q : ptrs)

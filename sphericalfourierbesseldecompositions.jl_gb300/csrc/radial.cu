@@ -9,6 +9,8 @@
 // instead of one per (n,l).  Galaxies below rmin / above rmax use the
 // spline's boundary extrapolation (src/Splines.jl:72-77) through two
 // constant basis maps.
+#include <vector>
+
 #include "sfb_internal.h"
 
 namespace sfb {
@@ -544,41 +546,72 @@ __global__ void k_mean_proj(const double *__restrict__ coef, int64_t npairs, int
     s[pr] = a;
 }
 
-// One block per (l, m): the block's threads take n = 1..nmax.
+// Tiles of the projection: block (l, m0, n0) of the plan's tile list covers
+// m = m0 .. m0 + 63 (thread = m) and n = n0 + 1 .. n0 + 8 (eight accumulators
+// per thread):
 //   a_nlm = scale * sum_b coef[n,l][b] dA_b[lm]              (double-float)
 //         + scale * s[pair] * C_lm - w_ln(l, n) * M_lm        (FP64)
 // with dA the fluctuation a_lm (double-float copy, row lm of width ldA),
-// C_lm / M_lm the FP64 a_lm of the count map / the mask (ralm [lm][4]);
-// the mean and window terms are skipped when ralm is null / window_kind is
-// not separable.
-__global__ void __launch_bounds__(64) k_project_mixed(const float2 *__restrict__ Adf, int64_t ldA, int64_t nbasis,
-                                                      const float2 *__restrict__ CT, int nmax, int lmax,
-                                                      const int64_t *__restrict__ noff,
-                                                      const int32_t *__restrict__ pair_index, double scale,
-                                                      const double *__restrict__ smean, const double *__restrict__ ralm,
-                                                      int window_kind, const double *__restrict__ w_ln,
-                                                      double *__restrict__ out) {
-    extern __shared__ float2 arow[];
-    const int64_t lm = blockIdx.x;
-    int l = (int)((sqrt(8.0 * (double)lm + 1.0) - 1.0) * 0.5);
-    while ((int64_t)(l + 1) * (l + 2) / 2 <= lm) ++l;
-    while ((int64_t)l * (l + 1) / 2 > lm) --l;
-    for (int64_t j = threadIdx.x; j < 2 * nbasis; j += blockDim.x) arow[j] = Adf[lm * ldA + j];
-    __syncthreads();
+// C_lm / M_lm the FP64 a_lm of the count map / the mask (ralm [lm][4]); the
+// mean and window terms are skipped when ralm is null / window_kind is not
+// separable.  The coefficient rows (CT, per (l, b) contiguous in n) and the
+// tile's dA rows are staged in shared memory in chunks of PJ_BK basis
+// functions, so each coefficient is read once per tile, not once per m.
+constexpr int PJ_M = 64, PJ_N = 8, PJ_BK = 32;
+
+__global__ void __launch_bounds__(PJ_M) k_project_mixed(const float2 *__restrict__ Adf, int64_t ldA, int64_t nbasis,
+                                                        const float2 *__restrict__ CT, int nmax, int lmax,
+                                                        const int3 *__restrict__ tiles,
+                                                        const int64_t *__restrict__ noff,
+                                                        const int32_t *__restrict__ pair_index, double scale,
+                                                        const double *__restrict__ smean,
+                                                        const double *__restrict__ ralm, int window_kind,
+                                                        const double *__restrict__ w_ln, double *__restrict__ out) {
+    __shared__ float2 cts[PJ_BK][PJ_N];
+    __shared__ float2 as[2 * PJ_BK][PJ_M + 1];       // [2 b + re/im][m], padded against bank conflicts
+    const int3 t = tiles[blockIdx.x];
+    const int l = t.x, m0 = t.y, n0 = t.z;
+    const int tid = threadIdx.x;
+    const int64_t lm0 = (int64_t)l * (l + 1) / 2 + m0;
+    const int mrows = min(PJ_M, l + 1 - m0);
+    df2 re[PJ_N], im[PJ_N];
+#pragma unroll
+    for (int j = 0; j < PJ_N; ++j) re[j] = im[j] = df2{0.f, 0.f};
     const float2 *Cl = CT + (int64_t)l * nbasis * nmax;
-    for (int n1 = threadIdx.x; n1 < nmax; n1 += blockDim.x) {
+    for (int64_t b0 = 0; b0 < nbasis; b0 += PJ_BK) {
+        __syncthreads();
+        for (int i = tid; i < PJ_BK * PJ_N; i += PJ_M) {
+            const int64_t b = b0 + i / PJ_N;
+            const int n1 = n0 + i % PJ_N;
+            cts[i / PJ_N][i % PJ_N] = (b < nbasis && n1 < nmax) ? Cl[b * nmax + n1] : make_float2(0.f, 0.f);
+        }
+        for (int i = tid; i < PJ_M * 2 * PJ_BK; i += PJ_M) {
+            const int mi = i / (2 * PJ_BK), q = i % (2 * PJ_BK);
+            as[q][mi] = (mi < mrows && b0 + q / 2 < nbasis) ? Adf[(lm0 + mi) * ldA + 2 * b0 + q] : make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+        const int bl_end = (int)(nbasis - b0 < PJ_BK ? nbasis - b0 : PJ_BK);
+        for (int bl = 0; bl < bl_end; ++bl) {
+            const float2 ar = as[2 * bl][tid], ai = as[2 * bl + 1][tid];
+#pragma unroll
+            for (int j = 0; j < PJ_N; ++j) {
+                const float2 c = cts[bl][j];
+                const df2 cc = {c.x, c.y};
+                re[j] = dfa(re[j], dfm(cc, {ar.x, ar.y}));
+                im[j] = dfa(im[j], dfm(cc, {ai.x, ai.y}));
+            }
+        }
+    }
+    if (tid >= mrows) return;
+    const int64_t lm = lm0 + tid;
+#pragma unroll
+    for (int j = 0; j < PJ_N; ++j) {
+        const int n1 = n0 + j;
+        if (n1 >= nmax) break;
         const int pr = pair_index[(int64_t)n1 * (lmax + 1) + l];
         if (pr < 0) continue;
-        df2 re = {0.f, 0.f}, im = {0.f, 0.f};
-        for (int64_t b = 0; b < nbasis; ++b) {
-            const float2 c = Cl[b * nmax + n1];
-            const df2 cc = {c.x, c.y};
-            const float2 ar = arow[2 * b], ai = arow[2 * b + 1];
-            re = dfa(re, dfm(cc, {ar.x, ar.y}));
-            im = dfa(im, dfm(cc, {ai.x, ai.y}));
-        }
-        double vr = scale * ((double)re.hi + (double)re.lo);
-        double vi = scale * ((double)im.hi + (double)im.lo);
+        double vr = scale * ((double)re[j].hi + (double)re[j].lo);
+        double vi = scale * ((double)im[j].hi + (double)im[j].lo);
         if (ralm) {
             const double mu = scale * smean[pr];
             vr = fma(mu, ralm[4 * lm], vr);
@@ -595,6 +628,19 @@ __global__ void __launch_bounds__(64) k_project_mixed(const float2 *__restrict__
     }
 }
 
+// Tile list of the projection: (l, m0, n0) for m0 = 0, 64, .. <= l and n0 = 0,
+// 8, .. below the number of radial modes of l (the valid n form a prefix).
+std::vector<int3> project_tiles(const std::vector<int32_t> &pair_index, int lmax, int nmax) {
+    std::vector<int3> t;
+    for (int l = 0; l <= lmax; ++l) {
+        int nl = 0;
+        while (nl < nmax && pair_index[(size_t)nl * (lmax + 1) + l] >= 0) ++nl;
+        for (int m0 = 0; m0 <= l; m0 += PJ_M)
+            for (int n0 = 0; n0 < nl; n0 += PJ_N) t.push_back(make_int3(l, m0, n0));
+    }
+    return t;
+}
+
 void launch_project_mixed(const Plan &p, const float2 *Adf, int64_t ldA, const float2 *CT,
                           const int64_t *noff, const int32_t *pair_index, double scale, const double *mu,
                           double *smean, const double *ralm, int window_kind, const double *w_ln, double *out,
@@ -603,10 +649,10 @@ void launch_project_mixed(const Plan &p, const float2 *Adf, int64_t ldA, const f
         k_mean_proj<<<(unsigned)((p.npairs + 127) / 128), 128, 0, st>>>(p.d_coef, p.npairs, p.nbasis, mu, smean);
         note_launch();
     }
-    const size_t smem = (size_t)2 * p.nbasis * sizeof(float2);
-    set_smem(k_project_mixed, smem);
-    k_project_mixed<<<(unsigned)p.lmsize, 64, smem, st>>>(Adf, ldA, p.nbasis, CT, (int)p.nmax, p.lmax, noff,
-                                                          pair_index, scale, smean, ralm, window_kind, w_ln, out);
+    if (p.n_proj_tiles <= 0) return;
+    k_project_mixed<<<(unsigned)p.n_proj_tiles, PJ_M, 0, st>>>(Adf, ldA, p.nbasis, CT, (int)p.nmax, p.lmax,
+                                                               p.d_proj_tiles, noff, pair_index, scale, smean, ralm,
+                                                               window_kind, w_ln, out);
     note_launch();
 }
 

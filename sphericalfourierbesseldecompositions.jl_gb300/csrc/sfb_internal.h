@@ -105,6 +105,9 @@ struct Plan {
     // per block z the Gram matrix of the other rings, sliced in the synthesis
     // layout with its gram_rows output rows as rings (null: not used)
     int ral = 0, gram_rows = 0;
+    // tiles (l, m0, n0) of the mixed-precision projection
+    int3 *d_proj_tiles = nullptr;
+    int64_t n_proj_tiles = 0;
     void *d_gramts = nullptr;
     int64_t *d_gramts_off = nullptr;
     double *d_lam = nullptr;        // Legendre table, FP64
@@ -222,6 +225,7 @@ void launch_gram_update(const Plan &p, const double *A, const float2 *Adf, const
                         double *Anew, float2 *Adfnew, cudaStream_t st, const int *Ein = nullptr,
                         int *Eout = nullptr);
 int build_gram_tables(Plan &p, cudaStream_t st);
+std::vector<int3> project_tiles(const std::vector<int32_t> &pair_index, int lmax, int nmax);
 void launch_transpose(const double *in, int64_t rows, int64_t cols, double *out, cudaStream_t st);
 void launch_check_finite(const double *x, int64_t n, int *err, cudaStream_t st);
 void launch_ang2pix(int64_t nside, const double *theta, const double *phi, int64_t n, int64_t *pix,

@@ -40,8 +40,11 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
 }
 
 // Bounded wait for the given phase parity; false on timeout.  Each try
-// suspends the thread until the phase completes or about 1 us passes, so
-// waiting warps do not take issue slots from working ones.
+// suspends the thread until the phase completes or SFB_MBAR_HINT_NS passes,
+// so waiting warps do not take issue slots from working ones.
+#ifndef SFB_MBAR_HINT_NS
+#define SFB_MBAR_HINT_NS 1000u
+#endif
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
     const uint32_t a = smem_u32(bar);
     for (uint32_t it = 0; it < SPIN_LIMIT; ++it) {
@@ -50,7 +53,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
             " selp.u32 %0, 1, 0, p;\n}\n"
             : "=r"(done)
-            : "r"(a), "r"(parity), "r"(1000u)
+            : "r"(a), "r"(parity), "r"((uint32_t)(SFB_MBAR_HINT_NS))
             : "memory");
         if (done) return true;
     }
