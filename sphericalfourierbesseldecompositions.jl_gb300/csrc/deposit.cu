@@ -305,6 +305,107 @@ __global__ void k_deposit_moments_df(const int32_t *__restrict__ offset, const d
         if (k <= deg) base[(int64_t)k * npix] = fluct(acc[k], b0 + k);
 }
 
+// The same moments with the block's bins handed to its threads in order of
+// decreasing galaxy count (a counting sort of the 128 counts in shared
+// memory), so the threads of a warp walk bins of nearly equal length instead
+// of waiting on the longest bin of 32 neighbours.  The basis values are
+// carried as q_k = w P_k(x) through (k+1) q_{k+1} = (2k+1) x q_k - k q_{k-1}.
+// Results pass through shared memory and are written with consecutive
+// threads on consecutive pixels.  Needs npix >= 128 (a block spans at most
+// two slots).
+template <int MAXDEG>
+__global__ void __launch_bounds__(128) k_deposit_moments_bal(const int32_t *__restrict__ offset,
+                                                             const double2 *__restrict__ sorted, int64_t npix,
+                                                             int pieces, int deg, int64_t nbasis,
+                                                             const double *__restrict__ ref,
+                                                             const float2 *__restrict__ mudf,
+                                                             float *__restrict__ maps) {
+    __shared__ int hist[64];
+    __shared__ int perm[128];
+    __shared__ float out[(MAXDEG + 1) * 128];
+    const int t = threadIdx.x;
+    const int64_t nkeys = (int64_t)(pieces + 2) * npix;
+    const int64_t B0 = (int64_t)blockIdx.x * 128;
+    const int slot0 = (int)(B0 / npix);
+    const int64_t bnd = (int64_t)(slot0 + 1) * npix;
+    const int64_t bt = B0 + t;
+    const int cnt = bt < nkeys ? offset[bt + 1] - offset[bt] : 0;
+    if (t < 64) hist[t] = 0;
+    __syncthreads();
+    const int key = 63 - min(cnt, 63);                 // longest bins first
+    atomicAdd(&hist[key], 1);
+    __syncthreads();
+    if (t < 32) {
+        const int h0 = hist[2 * t], h1 = hist[2 * t + 1];
+        int sc = h0 + h1;
+        for (int off = 1; off < 32; off <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, sc, off);
+            if (t >= off) sc += v;
+        }
+        const int base = sc - (h0 + h1);
+        hist[2 * t] = base;
+        hist[2 * t + 1] = base + h0;
+    }
+    __syncthreads();
+    perm[atomicAdd(&hist[key], 1)] = t;
+    __syncthreads();
+    const int q = perm[t];
+    const int64_t b = B0 + q;
+    if (b < nkeys) {
+        const int slot = b < bnd ? slot0 : slot0 + 1;
+        const int64_t pix = b - (int64_t)slot * npix;
+        const int64_t g0 = offset[b], g1 = offset[b + 1];
+        const dfl rv = df_of(ref ? ref[pix] : 0.0);
+        auto fluct = [&](dfl a, int64_t bi) -> float {
+            if (ref) {
+                const float2 m = mudf[bi];
+                a = df_add(a, df_neg(df_mul({m.x, m.y}, rv)));
+            }
+            return a.hi + a.lo;
+        };
+        if (slot >= pieces) {
+            dfl sw = {0.f, 0.f};
+            for (int64_t g = g0; g < g1; ++g) sw = df_add(sw, df_of(sorted[g].y));
+            out[q] = fluct(sw, nbasis - 2 + (slot - pieces));
+        } else {
+            dfl acc[MAXDEG + 1];
+#pragma unroll
+            for (int k = 0; k <= MAXDEG; ++k) acc[k] = {0.f, 0.f};
+            for (int64_t g = g0; g < g1; ++g) {
+                const double2 xw = sorted[g];
+                const dfl x = df_of(xw.x);
+                dfl q0 = df_of(xw.y), q1 = df_mul(q0, x);
+                acc[0] = df_add(acc[0], q0);
+                if (MAXDEG >= 1) acc[1] = df_add(acc[1], q1);
+#pragma unroll
+                for (int k = 1; k < MAXDEG; ++k) {
+                    if (k >= deg) break;
+                    const dfl c1 = df_of((double)(2 * k + 1) / (k + 1));
+                    const dfl c2 = df_of(-(double)k / (k + 1));
+                    const dfl q2 = df_add(df_mul(c1, df_mul(x, q1)), df_mul(c2, q0));
+                    acc[k + 1] = df_add(acc[k + 1], q2);
+                    q0 = q1;
+                    q1 = q2;
+                }
+            }
+            const int64_t bb = (int64_t)slot * (deg + 1);
+#pragma unroll
+            for (int k = 0; k <= MAXDEG; ++k)
+                if (k <= deg) out[k * 128 + q] = fluct(acc[k], bb + k);
+        }
+    }
+    __syncthreads();
+    if (bt >= nkeys) return;
+    const int slot = bt < bnd ? slot0 : slot0 + 1;
+    const int64_t pix = bt - (int64_t)slot * npix;
+    if (slot >= pieces) {
+        maps[(nbasis - 2 + (slot - pieces)) * npix + pix] = out[t];
+        return;
+    }
+    float *base = maps + (int64_t)slot * (deg + 1) * npix + pix;
+    for (int k = 0; k <= deg; ++k) base[(int64_t)k * npix] = out[k * 128 + t];
+}
+
 constexpr int STATS_STRIDE = 32;
 
 // Sampled projections onto ref over the bins of every STATS_STRIDE-th group of
@@ -387,7 +488,10 @@ static void launch_moments(const Plan &p, const int32_t *counts, const double2 *
                            const double *mu, const float2 *mudf, double *maps, cudaStream_t st) {
     const int64_t nkeys = (int64_t)(p.pieces + 2) * p.npix;
     const unsigned blocks = (unsigned)((nkeys + 127) / 128);
-    if (p.precision == SFB_MIXED)
+    if (p.precision == SFB_MIXED && MAXDEG <= 31 && p.npix >= 128)
+        k_deposit_moments_bal<MAXDEG><<<blocks, 128, 0, st>>>(counts, sorted, p.npix, p.pieces, p.degree, p.nbasis,
+                                                              ref, mudf, reinterpret_cast<float *>(maps));
+    else if (p.precision == SFB_MIXED)
         k_deposit_moments_df<MAXDEG><<<blocks, 128, 0, st>>>(counts, sorted, p.npix, p.pieces, p.degree, p.nbasis,
                                                              ref, mudf, reinterpret_cast<float *>(maps));
     else

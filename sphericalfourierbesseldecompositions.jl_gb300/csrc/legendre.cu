@@ -11,6 +11,8 @@
 //   R = F - w * nph * cfold * Fold(G)
 // where Fold sums the synthesised coefficients that alias onto each m on a
 // ring of nph pixels (exactly what the ring FFT of the synthesised map sees).
+#include <algorithm>
+
 #include "sfb_internal.h"
 
 namespace sfb {
@@ -401,6 +403,109 @@ __global__ void __launch_bounds__(128) k_fold_cols(const RingGeom *__restrict__ 
     }
 }
 
+// Aliased-ring fold of the Gram refinement (F = 0, rings r < ral):
+//   R[p][m'][r][c] = -w nph cfold Fold(G[p][.][r][c])[m']
+// computed per ring through residue buckets instead of per-output alias
+// loops: P[k] = sum_{m = k mod n} s_m G[m] (s_m = (-1)^floor(m/n) for rings
+// with the half-pixel phase, else 1; m = 0 adds its real part only), then
+//   Fold[m'] = s(m') P[m' mod n] + s(c) conj(P'[(n - m' mod n) mod n]),
+// c = (kk + m') / n, P' = P without the m = 0 term — the same sums as
+// k_fold_cols, O(lmax) per ring and column instead of O(lmax^2 / n).
+// Block: parity, FC complex columns, a group of rings; shared memory holds
+// the ring's G rows, the buckets and the running column maxima (exponents for
+// the analysis).
+template <int FC>
+__global__ void __launch_bounds__(256) k_fold_alias(const RingGeom *__restrict__ rings, int nrn, int ral, int rpb,
+                                                    int nbk, int lmax, double w, const float *__restrict__ G,
+                                                    int64_t ncplx, float *__restrict__ R, int *__restrict__ Ecol) {
+    extern __shared__ float2 fsm[];
+    const int par = blockIdx.y;
+    const int64_t c0 = (int64_t)blockIdx.x * FC;
+    const int r0 = blockIdx.z * rpb, r1 = min(ral, r0 + rpb);
+    const int L1 = lmax + 1;
+    const int64_t ld = 2 * ncplx;
+    float2 *P = fsm;                                  // [nbk][FC], nbk = the longest of the rings
+    float2 *mx = fsm + (int64_t)nbk * FC;             // [L1][FC] (re, im maxima)
+    float2 *Gs = mx + (int64_t)L1 * FC;               // [L1][FC] the ring's G rows
+    const int tid = threadIdx.x;
+    for (int i = tid; i < L1 * FC; i += 256) mx[i] = make_float2(0.f, 0.f);
+    for (int r = r0; r < r1; ++r) {
+        const RingGeom g = rings[r];
+        const int n = min(g.nph, nbk);
+        const bool odd = g.phi0_den != 0;
+        const float f = (float)(w * (double)n * g.cfold);
+        __syncthreads();
+        // the ring's G rows into shared memory, eight loads in flight per thread
+        for (int i0 = tid; i0 < L1 * FC; i0 += 8 * 256) {
+            float2 gv[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int i = i0 + q * 256;
+                const int m = i / FC, cc = i - m * FC;
+                gv[q] = make_float2(0.f, 0.f);
+                if (i < L1 * FC && c0 + cc < ncplx)
+                    gv[q] = *reinterpret_cast<const float2 *>(G + ((int64_t)(par * L1 + m) * nrn + r) * ld +
+                                                              2 * (c0 + cc));
+            }
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                if (i0 + q * 256 < L1 * FC) Gs[i0 + q * 256] = gv[q];
+        }
+        __syncthreads();
+        // buckets, each summed by one thread in a fixed order (deterministic)
+        for (int i = tid; i < n * FC; i += 256) {
+            const int k = i / FC, cc = i - k * FC;
+            float sx = 0.f, sy = 0.f;
+            int t = 0;
+            for (int m = k; m <= lmax; m += n, ++t) {
+                const float2 gv = Gs[m * FC + cc];
+                const float sg = (odd && (t & 1)) ? -1.f : 1.f;
+                sx += sg * gv.x;
+                if (m != 0) sy += sg * gv.y;
+            }
+            P[i] = make_float2(sx, sy);
+        }
+        __syncthreads();
+        for (int i = tid; i < L1 * FC; i += 256) {
+            const int mp = i / FC, cc = i - mp * FC;
+            const int64_t c = c0 + cc;
+            if (c >= ncplx) continue;
+            const int k = mp % n;
+            const int kk = (n - k) % n;
+            const float2 p1 = P[k * FC + cc];
+            float2 p2 = P[kk * FC + cc];
+            if (kk == 0) p2.x -= Gs[cc].x;                  // P' excludes m = 0
+            const float s1 = (odd && ((mp / n) & 1)) ? -1.f : 1.f;
+            const float s2 = (odd && (((kk + mp) / n) & 1)) ? -1.f : 1.f;
+            const float sx = s1 * p1.x + s2 * p2.x, sy = s1 * p1.y - s2 * p2.y;
+            const float rx = -f * sx, ry = -f * sy;
+            const int64_t off = ((int64_t)(par * L1 + mp) * nrn + r) * ld + 2 * c;
+            R[off] = rx;
+            R[off + 1] = ry;
+            float2 m2 = mx[i];
+            m2.x = fmaxf(m2.x, fabsf(rx));
+            m2.y = fmaxf(m2.y, fabsf(ry));
+            mx[i] = m2;
+        }
+    }
+    if (!Ecol) return;
+    __syncthreads();
+    const int lg = 32 - __clz(nrn > 1 ? nrn - 1 : 1);
+    const int extra = max(0, lg - 9);
+    auto ex = [&](float v) {
+        int E = (v > 0.f && isfinite(v)) ? ilogbf(v) + 1 : 0;
+        return max(-90, min(E + extra, 100));
+    };
+    for (int i = tid; i < L1 * FC; i += 256) {
+        const int mp = i / FC, cc = i - mp * FC;
+        const int64_t c = c0 + cc;
+        if (c >= ncplx) continue;
+        const int64_t z = 2 * (int64_t)mp + par;
+        atomicMax(Ecol + z * ld + 2 * c, ex(mx[i].x));
+        atomicMax(Ecol + z * ld + 2 * c + 1, ex(mx[i].y));
+    }
+}
+
 // Few columns: one thread per (parity, m', ring, complex column), same sums.
 template <typename T>
 __global__ void __launch_bounds__(256) k_fold_residual_narrow(const RingGeom *rings, int nrn, int lmax, double w,
@@ -451,6 +556,23 @@ void launch_fold_residual(const Plan &p, const double *F, const double *G, int64
     if (p.precision == SFB_MIXED && ncplx > 4) {
         // 0x80 bytes: every exponent word starts at -2139062144, below any scale exponent
         if (Ecol) cudaMemsetAsync(Ecol, 0x80, (size_t)2 * (p.lmax + 1) * ncol * sizeof(int), st);
+        if (!F && rlim > 0 && rlim <= p.ral) {
+            // aliased rings of the Gram refinement: residue buckets (shared memory within limits)
+            constexpr int FC = 8;
+            int nbk = 1;
+            for (int r = 0; r < rlim; ++r) nbk = std::max(nbk, p.h_rings[r].nph);
+            const size_t smem = ((size_t)nbk + 2 * (size_t)(p.lmax + 1)) * FC * sizeof(float2);
+            if (smem <= 200 * 1024) {
+                const int rpb = 8;
+                set_smem(k_fold_alias<FC>, smem);
+                dim3 grid((unsigned)((ncplx + FC - 1) / FC), 2, (unsigned)((rlim + rpb - 1) / rpb));
+                k_fold_alias<FC><<<grid, 256, smem, st>>>(p.d_rings, (int)p.nrn, rlim, rpb, nbk, p.lmax,
+                                                          4.0 * M_PI / (double)p.npix, (const float *)G, ncplx,
+                                                          (float *)R, Ecol);
+                note_launch();
+                return;
+            }
+        }
         dim3 grid((unsigned)((ncplx + 127) / 128), (unsigned)(2 * (p.lmax + 1)),
                   (unsigned)((rlim + FOLD_RC - 1) / FOLD_RC));
         const double w = 4.0 * M_PI / (double)p.npix;
