@@ -203,18 +203,33 @@ def run_reference_sample(amodes, gal, w, nbar, mask, wln_arr, steps, warmup, wor
 
 
 # ----------------------------------------------------------------------------- GPU arm
+def gram_geometry(lmax, niter=3):
+    """Aliased rings (nph <= 2 lmax, a prefix of the north rings) and whether the
+    mixed path's Gram refinement runs (most rings alias-free, niter > 0)."""
+    ral = 0
+    while ral < 2 * NSIDE and (4 * (ral + 1) if ral < NSIDE - 1 else 4 * NSIDE) <= 2 * lmax:
+        ral += 1
+    on = niter > 0 and 4 * ral <= 3 * 2 * NSIDE and os.environ.get("SFBGPU_GRAM_REFINEMENT", "1") != "0"
+    return ral, on
+
+
 def stage_work(stage, precision, nm, ngal, nbasis, niter=3, lmax=238):
-    """Algorithmic work of ONE STEP of a stage: (kind, amount), by the counts
-    of the path's scope table (the N/S ring symmetry and the ten-product
-    slicing are implementation choices and do not change the counts):
+    """Algorithmic work of ONE STEP of a stage as this path computes it:
+    (kind, amount).  The N/S ring symmetry and the ten-product slicing are
+    implementation choices and do not change the counts.
 
     leg_analysis / leg_synthesis: 2 (complex) x 2 (multiply-add) flop per
-    (ring of all 4 nside - 1, (l, m) with m <= l, map) and pass; 1 + niter
-    analysis passes, niter synthesis passes.
+    (ring, (l, m) with m <= l, map).  FP64 path: 1 + niter analysis and niter
+    synthesis passes over all 4 nside - 1 rings.  Mixed path (Gram
+    refinement): one analysis pass over all rings, then per refinement pass a
+    synthesis and an analysis over the 2 ral aliased rings and the Gram
+    product, 2 (complex) x 2 flop per (block z, output row, input row, map)
+    (counted under leg_synthesis).
     ring_fft: maps read + ring spectra written, nm npix b + nm n_ring (lmax+1)
     2 b bytes (b = 4 mixed, 8 FP64); the mixed path computes it as a
     tensor-core DFT, whose 4 flop per (pixel, m, map) is reported beside.
-    fold: F, G read + R written per pass.  deposit: 40 B per galaxy (record
+    fold: G read + R written per pass (mixed: the aliased rings only; FP64:
+    F, G read + R written over all rings).  deposit: 40 B per galaxy (record
     read + binning update) + the basis maps written."""
     lmsize = (lmax + 1) * (lmax + 2) // 2
     nrn = 2 * NSIDE
@@ -223,13 +238,24 @@ def stage_work(stage, precision, nm, ngal, nbasis, niter=3, lmax=238):
     ncol = 2 * nm
     t = 4 if precision == "mixed" else 8
     fsz = 2 * (lmax + 1) * nrn * ncol * t
+    ral, gram = gram_geometry(lmax, niter)
+    gram = gram and precision == "mixed" and nm > 4
+    n_al = 2 * ral                                   # aliased rings, both hemispheres
+    rows = [((lmax - m - par) // 2 + 1) if m + par <= lmax else 0 for m in range(lmax + 1) for par in (0, 1)]
+    gram_flop = 4.0 * nm * sum(r * r for r in rows)
     if stage == "leg_analysis":
+        if gram:
+            return ("flop", 4.0 * n_ring * lmsize * nm + niter * 4.0 * n_al * lmsize * nm)
         return ("flop", (1 + niter) * 4.0 * n_ring * lmsize * nm)
     if stage == "leg_synthesis":
+        if gram:
+            return ("flop", niter * (4.0 * n_al * lmsize * nm + gram_flop))
         return ("flop", niter * 4.0 * n_ring * lmsize * nm)
     if stage == "ring_fft":
         return ("byte", float(t) * nm * npix + float(nm) * n_ring * (lmax + 1) * 2 * t)
     if stage == "fold":
+        if gram:
+            return ("byte", niter * 2.0 * 2 * (lmax + 1) * ral * ncol * t)
         return ("byte", niter * 3.0 * fsz)
     if stage == "deposit":
         return ("byte", 40.0 * ngal + float(t) * nbasis * npix)
@@ -269,12 +295,18 @@ def roofline_table(stages, precision, nm, ngal, nbasis, peaks, fp64_peak):
                        "per_step": amount, "ms_per_step": ms,
                        "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback"}
             if st == "ring_fft" and precision == "mixed":
+                # the mixed ring transform is a tensor-core DFT: its bound is the tensor pipe (fed from
+                # shared memory), so it is reported as such, with the HBM bytes beside
                 lmax = 238
                 dft = 4.0 * nm * 12 * NSIDE ** 2 * (lmax + 1)
                 tp = peaks.get("bf16_tflops_sustained", 1700.0)
                 tach = dft / (ms * 1e-3) / 1e12
-                out[st]["tensor_view"] = {"dft_flop_per_step": dft, "achieved_tflops": tach,
-                                          "frac_of_bf16_sustained": tach / tp, "bf16_issued_frac": 10 * tach / tp}
+                hbm_view = {k: out[st][k] for k in ("achieved", "peak", "unit", "frac", "per_step")}
+                out[st] = {"bound": "tensor", "achieved": tach, "peak": tp, "unit": "TFLOP/s", "frac": tach / tp,
+                           "per_step": dft, "ms_per_step": ms,
+                           "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained" if "bf16_tflops_sustained"
+                           in peaks else "fallback (sustained bf16)",
+                           "bf16_issued_frac": 10 * tach / tp, "hbm_view": hbm_view}
     return out
 
 
