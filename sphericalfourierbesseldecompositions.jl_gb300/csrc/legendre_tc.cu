@@ -44,6 +44,7 @@
 // releases its TMEM and returns.
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cmath>
 
 #include "sfb_internal.h"
@@ -337,7 +338,7 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_analysis_tc(const __nv_bfloat16 
                     dold[i] = make_float2(0.f, 0.f);
                     if (accumulate && row0 + i0 + i < nrows) {
                         const int64_t o = off(i);
-                        aold[i] = A[o];
+                        if (A) aold[i] = A[o];
                         dold[i] = Adf[o];
                     }
                 }
@@ -354,7 +355,7 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_analysis_tc(const __nv_bfloat16 
                     const float e = ((d.x - (s - zz)) + (hi - zz)) + (d.y + lo);
                     const float h2 = s + e;
                     Adf[o] = make_float2(h2, e - (h2 - s));
-                    A[o] = aold[i] + ((double)hi + (double)lo);
+                    if (A) A[o] = aold[i] + ((double)hi + (double)lo);
                     mx = fmaxf(mx, fabsf(h2));
                 }
             }
@@ -369,11 +370,11 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_analysis_tc(const __nv_bfloat16 
 // Synthesis: grid (column tiles, ring tiles of NT <= NMAX, blocks z); warps
 // 0-7 produce, warp 8 issues the MMAs.
 //
-// Update mode (Anew != nullptr): the table holds the Gram matrices of the
+// Update mode (Adfnew != nullptr): the table holds the Gram matrices of the
 // alias-free rings, "rings" r are output rows li (nrn = rows of the largest
 // block), and the epilogue writes, instead of G,
 //   Anew[l(r)] = Acur[l(r)] + (A0[l(r)] - sum_li M[r][li] Acur[l(li)])
-// in FP64 and double-float (Acur in FP64 from A, in double-float from Adf).
+// in double-float (Acur from Adf) and, when Anew is given, in FP64 (from Acur).
 __global__ void __launch_bounds__(NTH, 2) k_leg_synthesis_tc(const __nv_bfloat16 *__restrict__ lamts,
                                                              const int64_t *__restrict__ lamts_off, int lmax, int nrn,
                                                              int NT, const float2 *__restrict__ Adf, int64_t ncol,
@@ -390,7 +391,7 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_synthesis_tc(const __nv_bfloat16
     const int r0 = nt * NT;
     const int64_t col0 = (int64_t)blockIdx.x * MTILE;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const bool upd = Anew != nullptr;
+    const bool upd = Adfnew != nullptr;
     if (upd && r0 >= nrows) return;          // no output row of this block in the tile
     float *Gz = upd ? nullptr : G + ((int64_t)(par * (lmax + 1) + m) * nrn) * ncol;
     if (nrows == 0) {      // no l for this (m, parity): the block is zero
@@ -520,7 +521,7 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_synthesis_tc(const __nv_bfloat16
                         const int64_t o = off(i);
                         a0[i] = A0[o];
                         ac[i] = Adf[o];
-                        acur[i] = Acur[o];
+                        if (Acur) acur[i] = Acur[o];
                     }
                 }
 #pragma unroll
@@ -538,7 +539,7 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_synthesis_tc(const __nv_bfloat16
                     e = ((ac[i].x - (s - z2)) + (dh - z2)) + (ac[i].y + dl);
                     const float nh = s + e;
                     Adfnew[o] = make_float2(nh, e - (nh - s));
-                    Anew[o] = acur[i] + ((double)dh + (double)dl);
+                    if (Anew) Anew[o] = acur[i] + ((double)dh + (double)dl);
                     umx = fmaxf(umx, fabsf(nh));
                 }
             }
@@ -762,6 +763,22 @@ void launch_leg_synthesis_tc(const Plan &p, const float2 *Adf, int64_t ncol, flo
     tc::k_leg_synthesis_tc<<<grid, tc::NTH, tc::LEG_SMEM, st>>>((const __nv_bfloat16 *)p.d_lamts, p.d_lamts_off,
                                                                p.lmax, (int)p.nrn, NT, Adf, ncol, G, nullptr, nullptr,
                                                                nullptr, nullptr, Ein, nullptr, p.d_err);
+    note_launch();
+}
+
+namespace tc {
+__global__ void k_df_to_fp64(const float2 *__restrict__ a, int64_t n, double *__restrict__ out) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float2 v = a[i];
+        out[i] = (double)v.x + (double)v.y;
+    }
+}
+}  // namespace tc
+
+void launch_df_to_fp64(const float2 *a, int64_t n, double *out, cudaStream_t st) {
+    if (n <= 0) return;
+    const int64_t blocks = std::min<int64_t>((n + 255) / 256, 152 * 16);
+    tc::k_df_to_fp64<<<(unsigned)blocks, 256, 0, st>>>(a, n, out);
     note_launch();
 }
 

@@ -308,8 +308,10 @@ struct ShtWork {
     DevBuf<double> *f, *g, *r, *alm;
 };
 
+// fp64_out: the FP64 a_lm (alm) is wanted besides the double-float copy (almdf, mixed precision); the
+// Gram refinement carries only the double-float one and converts at the end when asked.
 int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, bool maps_are_fp64 = false,
-                 int stage_override = -1, const ShtWork *ws = nullptr) {
+                 int stage_override = -1, const ShtWork *ws = nullptr, bool fp64_out = true) {
     Plan &p = h->p;
     const ShtWork own{&p.fbuf, &p.gbuf, &p.rbuf, &p.alm};
     if (!ws) ws = &own;
@@ -356,13 +358,12 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, b
         // alias-free rings (fold = identity there), S_al / A_al the synthesis and analysis
         // over the aliased rings r < ral.  Each pass writes the other (A, Adf) buffer; the
         // last one lands in the plan's.
-        SFB_TRY(grow(p, p.alm2, (size_t)p.lmsize * ncol));
         SFB_TRY(grow(p, p.almdf2, (size_t)p.lmsize * ncol));
         SFB_TRY(grow(p, p.adf0, (size_t)p.lmsize * ncol));
         // column exponents of each (A, Adf) set, written by whichever kernel completes the set
         const int64_t nE = 2 * (p.lmax + 1) * ncol;
         SFB_TRY(grow(p, p.ecoef, (size_t)nE + 1));
-        double *Ab[2] = {alm.ptr, p.alm2.ptr};
+        double *Ab[2] = {nullptr, nullptr};          // FP64 a_lm: formed once at the end (fp64_out)
         float2 *Db[2] = {adf, reinterpret_cast<float2 *>(p.almdf2.ptr)};
         int *Eb[2] = {reinterpret_cast<int *>(p.ecoef.ptr), reinterpret_cast<int *>(p.ecoef.ptr) + nE};
         const float2 *a0 = reinterpret_cast<const float2 *>(p.adf0.ptr);
@@ -396,6 +397,7 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, b
             }
             cur = nxt;
         }
+        if (fp64_out) launch_df_to_fp64(Db[cur], p.lmsize * ncol, alm.ptr, st);
         SFB_CUDA_TRY(cudaGetLastError());
         return SFB_OK;
     }
@@ -515,7 +517,8 @@ int cat2amln_dev(sfb_plan *h, const double *rtp, const double *w, int64_t ngal, 
             SFB_TRY(reference_alm(h, Cmap, 2, ralm, h->side));
             SFB_CUDA_TRY(cudaEventRecord(h->ev_join, h->side));
         }
-        SFB_TRY(sht_analysis(h, p.maps.ptr, nm, st));
+        // the mixed projection reads the double-float a_lm only
+        SFB_TRY(sht_analysis(h, p.maps.ptr, nm, st, false, -1, nullptr, p.precision != SFB_MIXED));
         if (split) SFB_CUDA_TRY(cudaStreamWaitEvent(st, h->ev_join, 0));
         {
             Stage s(h, SFB_STAGE_PROJECT, st);
@@ -892,7 +895,7 @@ void sfb_plan_destroy(sfb_plan *h) {
                     p.d_dtw_off, p.d_dtimg, p.d_dtimg_off, p.d_gramts, p.d_gramts_off, p.d_cls_rings, p.d_cls_off, p.d_lam, p.d_lam32, p.d_lamtc, p.d_lamtc_off, p.d_lamts, p.d_lamts_off, p.d_lam_off, p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp,
                     p.d_pair_l, p.d_pair_n, p.d_out_pair, p.d_out_lm, p.d_coef, p.d_coefT, p.d_proj_tiles, p.d_err,
                     p.maps.ptr, p.fbuf.ptr, p.gbuf.ptr, p.rbuf.ptr, p.alm.ptr, p.scratch.ptr, p.scratch2.ptr, p.dep.ptr, p.maps32.ptr,
-                    p.ref.ptr, p.rf.ptr, p.rg.ptr, p.rr.ptr, p.ralm.ptr, p.alm2.ptr, p.almdf2.ptr, p.adf0.ptr, p.ecoef.ptr, p.erow.ptr, p.almdf.ptr, h->d_pair_index, h->d_noff};
+                    p.ref.ptr, p.rf.ptr, p.rg.ptr, p.rr.ptr, p.ralm.ptr, p.almdf2.ptr, p.adf0.ptr, p.ecoef.ptr, p.erow.ptr, p.almdf.ptr, h->d_pair_index, h->d_noff};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     collect_stages(h);

@@ -138,8 +138,8 @@ struct Plan {
     DevBuf<double> dep;             // sorted-deposit workspace
     DevBuf<double> ref;             // reference-map a_lm (FP64) and mean coefficients (mixed precision)
     DevBuf<double> rf, rg, rr, ralm;// workspace of the FP64 reference transform on the side stream
-    DevBuf<double> alm2, almdf2, adf0;  // Gram refinement: second (A, Adf) and the first pass's Adf
-    DevBuf<double> ecoef;               // Gram refinement: column exponents of both (A, Adf) sets (ints)
+    DevBuf<double> almdf2, adf0;    // Gram refinement: second double-float a_lm, the first pass's copy
+    DevBuf<double> ecoef;           // Gram refinement: column exponents of both a_lm sets (ints)
     DevBuf<double> erow;            // ring DFT row exponents [2][nrn][nmaps] (int)
     DevBuf<double> maps32;          // FP32 copy of FP64 maps (mixed precision, spline / dense-window paths)
     int64_t device_bytes = 0;
@@ -225,6 +225,7 @@ void launch_gram_update(const Plan &p, const double *A, const float2 *Adf, const
                         double *Anew, float2 *Adfnew, cudaStream_t st, const int *Ein = nullptr,
                         int *Eout = nullptr);
 int build_gram_tables(Plan &p, cudaStream_t st);
+void launch_df_to_fp64(const float2 *a, int64_t n, double *out, cudaStream_t st);
 std::vector<int3> project_tiles(const std::vector<int32_t> &pair_index, int lmax, int nmax);
 void launch_transpose(const double *in, int64_t rows, int64_t cols, double *out, cudaStream_t st);
 void launch_check_finite(const double *x, int64_t n, int *err, cudaStream_t st);
