@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(128) k_fold_residual(const RingGeom *rings, in
 // (coalesced lambda rows), warp-reduced.
 template <typename T, int NC>
 __global__ void __launch_bounds__(256) k_leg_analysis_narrow(const T *__restrict__ lam, const int64_t *lam_off,
-                                                             int lmax, int nrn, const T *__restrict__ F,
+                                                             int lmax, int nrn, int rlim, const T *__restrict__ F,
                                                              T *__restrict__ A, int accumulate) {
     const int z = blockIdx.y;
     const int m = z >> 1, par = z & 1;
@@ -216,7 +216,7 @@ __global__ void __launch_bounds__(256) k_leg_analysis_narrow(const T *__restrict
     T acc[NC];
 #pragma unroll
     for (int c = 0; c < NC; ++c) acc[c] = T(0);
-    for (int r = lane; r < nrn; r += 32) {
+    for (int r = lane; r < rlim; r += 32) {      // rings r >= rlim count as zero
         const T l = L[r];
 #pragma unroll
         for (int c = 0; c < NC; ++c) acc[c] = fma(l, B[(int64_t)r * NC + c], acc[c]);
@@ -239,13 +239,13 @@ __global__ void __launch_bounds__(256) k_leg_analysis_narrow(const T *__restrict
 // (lambda reads coalesced over r, a_lm broadcast).
 template <typename T, int NC>
 __global__ void __launch_bounds__(128) k_leg_synthesis_narrow(const T *__restrict__ lam, const int64_t *lam_off,
-                                                              int lmax, int nrn, const T *__restrict__ A,
+                                                              int lmax, int nrn, int rlim, const T *__restrict__ A,
                                                               T *__restrict__ G) {
     const int z = blockIdx.y;
     const int m = z >> 1, par = z & 1;
     const int nrows = nrows_of(m, par, lmax);
     const int r = blockIdx.x * 128 + threadIdx.x;
-    if (r >= nrn) return;
+    if (r >= rlim) return;                        // only the first rlim rings are formed
     const T *L = lam + lam_off[z] + r;
     T acc[NC];
 #pragma unroll
@@ -263,41 +263,74 @@ __global__ void __launch_bounds__(128) k_leg_synthesis_narrow(const T *__restric
 }
 
 template <typename T, int NC>
-static void narrow_analysis(const Plan &p, const T *lam, const T *F, T *A, bool accumulate, cudaStream_t st) {
+static void narrow_analysis(const Plan &p, const T *lam, const T *F, T *A, bool accumulate, int rlim,
+                            cudaStream_t st) {
     const int maxrows = p.lmax / 2 + 1;
     dim3 grid((unsigned)((maxrows + 7) / 8), (unsigned)(2 * (p.lmax + 1)));
-    k_leg_analysis_narrow<T, NC><<<grid, 256, 0, st>>>(lam, p.d_lam_off, p.lmax, (int)p.nrn, F, A, accumulate ? 1 : 0);
+    k_leg_analysis_narrow<T, NC><<<grid, 256, 0, st>>>(lam, p.d_lam_off, p.lmax, (int)p.nrn, rlim, F, A,
+                                                       accumulate ? 1 : 0);
 }
 
 template <typename T, int NC>
-static void narrow_synthesis(const Plan &p, const T *lam, const T *A, T *G, cudaStream_t st) {
-    dim3 grid((unsigned)((p.nrn + 127) / 128), (unsigned)(2 * (p.lmax + 1)));
-    k_leg_synthesis_narrow<T, NC><<<grid, 128, 0, st>>>(lam, p.d_lam_off, p.lmax, (int)p.nrn, A, G);
+static void narrow_synthesis(const Plan &p, const T *lam, const T *A, T *G, int rlim, cudaStream_t st) {
+    dim3 grid((unsigned)((rlim + 127) / 128), (unsigned)(2 * (p.lmax + 1)));
+    k_leg_synthesis_narrow<T, NC><<<grid, 128, 0, st>>>(lam, p.d_lam_off, p.lmax, (int)p.nrn, rlim, A, G);
 }
 
 template <typename T>
 static bool narrow_dispatch(const Plan &p, const T *lam, const T *in, int64_t ncol, T *out, bool analysis,
-                            bool accumulate, cudaStream_t st) {
+                            bool accumulate, cudaStream_t st, int rlim = -1) {
+    if (rlim < 0 || rlim > p.nrn) rlim = (int)p.nrn;
     switch (ncol) {
     case 2:
-        if (analysis) narrow_analysis<T, 2>(p, lam, in, out, accumulate, st); else narrow_synthesis<T, 2>(p, lam, in, out, st);
+        if (analysis) narrow_analysis<T, 2>(p, lam, in, out, accumulate, rlim, st);
+        else narrow_synthesis<T, 2>(p, lam, in, out, rlim, st);
         return true;
     case 4:
-        if (analysis) narrow_analysis<T, 4>(p, lam, in, out, accumulate, st); else narrow_synthesis<T, 4>(p, lam, in, out, st);
+        if (analysis) narrow_analysis<T, 4>(p, lam, in, out, accumulate, rlim, st);
+        else narrow_synthesis<T, 4>(p, lam, in, out, rlim, st);
         return true;
     case 8:
-        if (analysis) narrow_analysis<T, 8>(p, lam, in, out, accumulate, st); else narrow_synthesis<T, 8>(p, lam, in, out, st);
+        if (analysis) narrow_analysis<T, 8>(p, lam, in, out, accumulate, rlim, st);
+        else narrow_synthesis<T, 8>(p, lam, in, out, rlim, st);
         return true;
     default:
         return false;
     }
 }
 
+// FP64 Gram refinement step for few columns (the narrow transforms):
+//   Anew[l(r)] = Acur[l(r)] + (A0[l(r)] - sum_li M_z[r][li] Acur[l(li)])
+// one thread per (block z, output row r, column); M_z from the plan's FP64
+// Gram tables (element [li][r] at gram_off[z] + li R + r).
+template <int NC>
+__global__ void __launch_bounds__(128) k_gram_update_fp64(const double *__restrict__ gram,
+                                                          const int64_t *__restrict__ gram_off, int R, int lmax,
+                                                          const double *__restrict__ Acur,
+                                                          const double *__restrict__ A0, double *__restrict__ Anew) {
+    const int z = blockIdx.y;
+    const int m = z >> 1, par = z & 1;
+    const int nrows = nrows_of(m, par, lmax);
+    const int idx = blockIdx.x * 128 + threadIdx.x;
+    const int r = idx / NC, c = idx - r * NC;
+    if (r >= nrows) return;
+    const double *M = gram + gram_off[z] + r;
+    double acc = 0.0;
+    for (int li = 0; li < nrows; ++li) {
+        const int l = m + par + 2 * li;
+        acc = fma(M[(int64_t)li * R], Acur[((int64_t)l * (l + 1) / 2 + m) * NC + c], acc);
+    }
+    const int l = m + par + 2 * r;
+    const int64_t o = ((int64_t)l * (l + 1) / 2 + m) * NC + c;
+    Anew[o] = Acur[o] + (A0[o] - acc);
+}
+
 void launch_leg_analysis(const Plan &p, const double *F, int64_t ncol, double *A, bool accumulate,
-                         cudaStream_t st) {
+                         cudaStream_t st, int rlim) {
     const bool narrow = p.precision == SFB_MIXED
-                            ? narrow_dispatch<float>(p, p.d_lam32, (const float *)F, ncol, (float *)A, true, accumulate, st)
-                            : narrow_dispatch<double>(p, p.d_lam, F, ncol, A, true, accumulate, st);
+                            ? narrow_dispatch<float>(p, p.d_lam32, (const float *)F, ncol, (float *)A, true, accumulate, st,
+                                                     rlim)
+                            : narrow_dispatch<double>(p, p.d_lam, F, ncol, A, true, accumulate, st, rlim);
     if (narrow) {
         note_launch();
         return;
@@ -313,10 +346,11 @@ void launch_leg_analysis(const Plan &p, const double *F, int64_t ncol, double *A
     note_launch();
 }
 
-void launch_leg_synthesis(const Plan &p, const double *A, int64_t ncol, double *G, cudaStream_t st) {
+void launch_leg_synthesis(const Plan &p, const double *A, int64_t ncol, double *G, cudaStream_t st, int rlim) {
     const bool narrow = p.precision == SFB_MIXED
-                            ? narrow_dispatch<float>(p, p.d_lam32, (const float *)A, ncol, (float *)G, false, false, st)
-                            : narrow_dispatch<double>(p, p.d_lam, A, ncol, G, false, false, st);
+                            ? narrow_dispatch<float>(p, p.d_lam32, (const float *)A, ncol, (float *)G, false, false, st,
+                                                     rlim)
+                            : narrow_dispatch<double>(p, p.d_lam, A, ncol, G, false, false, st, rlim);
     if (narrow) {
         note_launch();
         return;
@@ -508,17 +542,18 @@ __global__ void __launch_bounds__(256) k_fold_alias(const RingGeom *__restrict__
 
 // Few columns: one thread per (parity, m', ring, complex column), same sums.
 template <typename T>
-__global__ void __launch_bounds__(256) k_fold_residual_narrow(const RingGeom *rings, int nrn, int lmax, double w,
-                                                             const T *__restrict__ F, const T *__restrict__ G,
-                                                             int64_t ncplx, T *__restrict__ R) {
+__global__ void __launch_bounds__(256) k_fold_residual_narrow(const RingGeom *rings, int nrn, int rlim, int lmax,
+                                                             double w, const T *__restrict__ F,
+                                                             const T *__restrict__ G, int64_t ncplx,
+                                                             T *__restrict__ R) {
     const int L1 = lmax + 1;
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t total = (int64_t)2 * L1 * nrn * ncplx;
+    const int64_t total = (int64_t)2 * L1 * rlim * ncplx;     // rings r < rlim only
     if (idx >= total) return;
     const int64_t c = idx % ncplx;
     int64_t t = idx / ncplx;
-    const int r = (int)(t % nrn);
-    t /= nrn;
+    const int r = (int)(t % rlim);
+    t /= rlim;
     const int mp = (int)(t % L1);
     const int par = (int)(t / L1);
     const RingGeom g = rings[r];
@@ -545,8 +580,23 @@ __global__ void __launch_bounds__(256) k_fold_residual_narrow(const RingGeom *ri
         sx += sgn * gp[0];
         sy -= sgn * gp[1];
     }
-    R[off] = F[off] - f * sx;
-    R[off + 1] = F[off + 1] - f * sy;
+    R[off] = (F ? F[off] : T(0)) - f * sx;
+    R[off + 1] = (F ? F[off + 1] : T(0)) - f * sy;
+}
+
+bool launch_gram_update_fp64(const Plan &p, const double *Acur, const double *A0, int64_t ncol, double *Anew,
+                             cudaStream_t st) {
+    if (!p.d_gram64) return false;
+    const int maxrows = p.lmax / 2 + 1;
+    dim3 grid((unsigned)((maxrows * ncol + 127) / 128), (unsigned)(2 * (p.lmax + 1)));
+    switch (ncol) {
+    case 2: k_gram_update_fp64<2><<<grid, 128, 0, st>>>(p.d_gram64, p.d_gram_off, p.gram_rows, p.lmax, Acur, A0, Anew); break;
+    case 4: k_gram_update_fp64<4><<<grid, 128, 0, st>>>(p.d_gram64, p.d_gram_off, p.gram_rows, p.lmax, Acur, A0, Anew); break;
+    case 8: k_gram_update_fp64<8><<<grid, 128, 0, st>>>(p.d_gram64, p.d_gram_off, p.gram_rows, p.lmax, Acur, A0, Anew); break;
+    default: return false;
+    }
+    note_launch();
+    return true;
 }
 
 void launch_fold_residual(const Plan &p, const double *F, const double *G, int64_t ncol, double *R,
@@ -582,14 +632,16 @@ void launch_fold_residual(const Plan &p, const double *F, const double *G, int64
         return;
     }
     if (ncplx <= 4) {
-        const int64_t total = (int64_t)2 * (p.lmax + 1) * p.nrn * ncplx;
+        const int64_t total = (int64_t)2 * (p.lmax + 1) * rlim * ncplx;
         const unsigned blocks = (unsigned)((total + 255) / 256);
         const double w = 4.0 * M_PI / (double)p.npix;
         if (p.precision == SFB_MIXED)
-            k_fold_residual_narrow<float><<<blocks, 256, 0, st>>>(p.d_rings, (int)p.nrn, p.lmax, w, (const float *)F,
-                                                                 (const float *)G, ncplx, (float *)R);
+            k_fold_residual_narrow<float><<<blocks, 256, 0, st>>>(p.d_rings, (int)p.nrn, rlim, p.lmax, w,
+                                                                 (const float *)F, (const float *)G, ncplx,
+                                                                 (float *)R);
         else
-            k_fold_residual_narrow<double><<<blocks, 256, 0, st>>>(p.d_rings, (int)p.nrn, p.lmax, w, F, G, ncplx, R);
+            k_fold_residual_narrow<double><<<blocks, 256, 0, st>>>(p.d_rings, (int)p.nrn, rlim, p.lmax, w, F, G,
+                                                                  ncplx, R);
         note_launch();
         return;
     }

@@ -904,6 +904,14 @@ int build_gram_tables(Plan &p, cudaStream_t st) {
     }
     if (cudaStreamSynchronize(st) != cudaSuccess && rc == SFB_OK)
         rc = fail(SFB_ECUDA, std::string("Gram table setup failed: ") + cudaGetErrorString(cudaGetLastError()));
+    if (rc == SFB_OK) {
+        // the FP64 tables stay for the few-column (FP64) refinement
+        p.d_gram64 = gram;
+        p.d_gram_off = d_goff;
+        p.device_bytes += (o + 1) * 8 + (int64_t)(goff.size() * sizeof(int64_t));
+        gram = nullptr;
+        d_goff = nullptr;
+    }
     cleanup();
     return rc;
 }

@@ -401,6 +401,39 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, b
         SFB_CUDA_TRY(cudaGetLastError());
         return SFB_OK;
     }
+    if (!tc && (ncol == 2 || ncol == 4 || ncol == 8) && p.d_gram64 && p.niter > 0) {
+        // FP64 Gram refinement for few columns (reference maps, small map2alm batches): the same
+        // identity as above, in FP64 with the narrow kernels.  alm holds [current | next | first pass].
+        const int64_t na = p.lmsize * ncol;
+        SFB_TRY(grow(p, alm, (size_t)(3 * na)));
+        double *Ab[2] = {alm.ptr, alm.ptr + na};
+        double *a0 = alm.ptr + 2 * na;
+        int cur = p.niter & 1;
+        {
+            Stage s(h, stage(SFB_STAGE_LEG_ANALYSIS), st);
+            launch_leg_analysis(p, fbuf.ptr, ncol, Ab[cur], false, st);
+        }
+        SFB_CUDA_TRY(cudaMemcpyAsync(a0, Ab[cur], (size_t)na * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        for (int it = 0; it < p.niter; ++it) {
+            const int nxt = cur ^ 1;
+            {
+                Stage s(h, stage(SFB_STAGE_LEG_SYNTHESIS), st);
+                if (p.ral > 0) launch_leg_synthesis(p, Ab[cur], ncol, gbuf.ptr, st, p.ral);
+                launch_gram_update_fp64(p, Ab[cur], a0, ncol, Ab[nxt], st);
+            }
+            if (p.ral > 0) {
+                {
+                    Stage s(h, stage(SFB_STAGE_FOLD), st);
+                    launch_fold_residual(p, nullptr, gbuf.ptr, ncol, rbuf.ptr, st, nullptr, p.ral);
+                }
+                Stage s(h, stage(SFB_STAGE_LEG_ANALYSIS), st);
+                launch_leg_analysis(p, rbuf.ptr, ncol, Ab[nxt], true, st, p.ral);
+            }
+            cur = nxt;
+        }
+        SFB_CUDA_TRY(cudaGetLastError());
+        return SFB_OK;
+    }
     analysis(fbuf.ptr, false);
     for (int it = 0; it < p.niter; ++it) {
         {
@@ -892,7 +925,7 @@ void sfb_plan_destroy(sfb_plan *h) {
     cudaSetDevice(p.device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     void *ptrs[] = {p.d_rings, p.d_twtab, p.d_twoff, p.d_phase, p.d_wphase, p.d_twtab32, p.d_wphase32, p.d_dtw,
-                    p.d_dtw_off, p.d_dtimg, p.d_dtimg_off, p.d_gramts, p.d_gramts_off, p.d_cls_rings, p.d_cls_off, p.d_lam, p.d_lam32, p.d_lamtc, p.d_lamtc_off, p.d_lamts, p.d_lamts_off, p.d_lam_off, p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp,
+                    p.d_dtw_off, p.d_dtimg, p.d_dtimg_off, p.d_gramts, p.d_gramts_off, p.d_gram64, p.d_gram_off, p.d_cls_rings, p.d_cls_off, p.d_lam, p.d_lam32, p.d_lamtc, p.d_lamtc_off, p.d_lamts, p.d_lamts_off, p.d_lam_off, p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp,
                     p.d_pair_l, p.d_pair_n, p.d_out_pair, p.d_out_lm, p.d_coef, p.d_coefT, p.d_proj_tiles, p.d_err,
                     p.maps.ptr, p.fbuf.ptr, p.gbuf.ptr, p.rbuf.ptr, p.alm.ptr, p.scratch.ptr, p.scratch2.ptr, p.dep.ptr, p.maps32.ptr,
                     p.ref.ptr, p.rf.ptr, p.rg.ptr, p.rr.ptr, p.ralm.ptr, p.almdf2.ptr, p.adf0.ptr, p.ecoef.ptr, p.erow.ptr, p.almdf.ptr, h->d_pair_index, h->d_noff};

@@ -110,6 +110,8 @@ struct Plan {
     int64_t n_proj_tiles = 0;
     void *d_gramts = nullptr;
     int64_t *d_gramts_off = nullptr;
+    double *d_gram64 = nullptr;        // the same Gram matrices in FP64, [li][r] at d_gram_off[z] + li R + r
+    int64_t *d_gram_off = nullptr;
     double *d_lam = nullptr;        // Legendre table, FP64
     float *d_lam32 = nullptr;       // the same table rounded to FP32 (mixed precision)
     void *d_lamtc = nullptr;        // split-BF16 table in tensor-core operand layout (analysis)
@@ -186,9 +188,13 @@ void launch_project_mixed(const Plan &p, const float2 *Adf, int64_t ldA, const f
 void launch_split_mean(double *maps, int64_t nmaps, int64_t npix, const double *ref, double *nu, cudaStream_t st);
 void launch_ring_analysis(const Plan &p, const double *maps, int64_t nmaps, double *F, cudaStream_t st);
 void launch_ring_synthesis(const Plan &p, const double *G, int64_t nmaps, double *maps, cudaStream_t st);
+// rlim (few columns only): rings r < rlim (analysis: the sum; synthesis: the rings formed); -1 = all
 void launch_leg_analysis(const Plan &p, const double *F, int64_t ncol, double *A, bool accumulate,
-                         cudaStream_t st);
-void launch_leg_synthesis(const Plan &p, const double *A, int64_t ncol, double *G, cudaStream_t st);
+                         cudaStream_t st, int rlim = -1);
+void launch_leg_synthesis(const Plan &p, const double *A, int64_t ncol, double *G, cudaStream_t st, int rlim = -1);
+// FP64 Gram refinement step for 2, 4 or 8 columns; false when not available
+bool launch_gram_update_fp64(const Plan &p, const double *Acur, const double *A0, int64_t ncol, double *Anew,
+                             cudaStream_t st);
 // rlim: only rings r < rlim (-1: all); F == nullptr (mixed, many columns): R = -w n cfold Fold(G)
 void launch_fold_residual(const Plan &p, const double *F, const double *G, int64_t ncol, double *R, cudaStream_t st,
                           int *Ecol = nullptr, int rlim = -1);

@@ -115,6 +115,23 @@ def test_map2alm_few_maps_vs_oracle(nmaps):
     assert e < 1e-12
 
 
+@pytest.mark.parametrize("nmaps", [1, 2, 4])
+def test_map2alm_gram_refinement_vs_oracle(nmaps):
+    """Few maps on a geometry where most rings are alias-free (nside 32,
+    lmax 40: the 20 polar rings with nph <= 80 alias): the refinement passes
+    run through the FP64 Gram matrices plus the aliased rings."""
+    nside, lmax = 32, 40
+    a = sfbgpu.AnlmModes.from_nmax_lmax(1, lmax, 500.0, 1000.0, nside=nside, cache=True)
+    rng = np.random.default_rng(10 + nmaps)
+    maps = rng.normal(size=(nmaps, 12 * nside * nside)) + 2.0
+    out = sfbgpu.cat2anlm.map2alm(maps, a, niter=3, radial="spline")
+    ref = osht.SHT(nside, lmax).map2alm(maps, niter=3)
+    tri = np.array([ref[b, l, m] for b in range(nmaps) for l in range(lmax + 1) for m in range(l + 1)])
+    e = rel_err(out.ravel(), tri)
+    record(f"map2alm_gram_{nmaps}maps_nside{nside}_lmax{lmax}_niter3", e)
+    assert e < 1e-12
+
+
 # ---------------------------------------------------------------- cat2amln ---
 def _sep_window(a, nside, nr=50):
     wm = sfbgpu.ConfigurationSpaceModes(a.rmin, a.rmax, nr, nside)
