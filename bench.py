@@ -39,6 +39,8 @@ METRIC = "cat2amln galaxies/s at nside256 kmax0.1: mixed vs FP64 GPU, ≤1e-7 re
 KMAX, RMIN, RMAX, NSIDE, NR = 0.1, 500.0, 2500.0, 256, 1000
 NGAL_MEAN = 10_000_000
 CAP_DEG, RMEAN, RSIG = 60.0, 1500.0, 400.0
+# measured with ncu (dram__bytes_read.sum + dram__bytes_write.sum) over the two ring-DFT launches of one call
+DFT_DRAM_BYTES_PER_CALL = (892.93 + 308.77 + 699.78 + 295.97) * 1e6
 WORKLOAD = "cat2amln kmax=0.1 rmin=500 rmax=2500 nside=256 nr=1000 N~Poisson(1e7) cap60 x gauss(1500,400) w~U[0.5,1.5]"
 
 
@@ -544,6 +546,11 @@ def main():
     roof = dict(table[dom])
     roof["kernel_stage"] = dom
     roof["traffic"] = None
+    if dom == "ring_fft" and args.precision == "mixed" and not args.profile_case:
+        # DRAM bytes (read + write) of the stage's two DFT launches in one call, from the single-pass
+        # ncu capture of this workload recorded in profiles/launches_cat2amln_nside256_kmax0.1_mixed.md
+        roof["traffic"] = DFT_DRAM_BYTES_PER_CALL
+        roof["traffic_source"] = "ncu dram__bytes_read.sum + dram__bytes_write.sum, k_ring_dft_tc x2, full workload"
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -118,12 +118,14 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
                                                          const int64_t *__restrict__ img_off, float *__restrict__ F,
                                                          int64_t ldF, int *err) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    const int cls = blockIdx.y;
+    // grid (column blocks u, row tiles, classes): the column blocks of one row tile are launched
+    // together and read its map rows through L2 once
+    const int cls = blockIdx.z;
     const int rb = cls_off[cls];
     const int64_t npairs = (int64_t)(cls_off[cls + 1] - rb) * nmaps;
-    const int64_t pair0 = (int64_t)blockIdx.x * NPAIR;
+    const int64_t pair0 = (int64_t)blockIdx.y * NPAIR;
     if (pair0 >= npairs) return;
-    const int u = blockIdx.z;
+    const int u = blockIdx.x;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const bool prod = tid < NPROD;
     const bool abuild = IMG ? prod : tid < NROW;   // IMG: all producers build A; else warps 0-3 A, 4-7 B
@@ -502,9 +504,9 @@ void launch_ring_analysis_tc(const Plan &p, const float *maps, int64_t nmaps, fl
     };
     const unsigned mtiles = (unsigned)((nmaps + dft::NPAIR - 1) / dft::NPAIR);
     // polar rings: one class per ring, imaged when the whole polar set fits the image
-    if (p.n_polar > 0) launch(dim3(mtiles, (unsigned)p.n_polar, ntn), 0, p.dtimg_polar);
+    if (p.n_polar > 0) launch(dim3(ntn, mtiles, (unsigned)p.n_polar), 0, p.dtimg_polar);
     const int64_t eq_tiles = ((int64_t)p.eq_max_rings * nmaps + dft::NPAIR - 1) / dft::NPAIR;
-    launch(dim3((unsigned)eq_tiles, (unsigned)p.n_eq_cls, ntn), p.n_polar, p.d_dtimg != nullptr);
+    launch(dim3(ntn, (unsigned)eq_tiles, (unsigned)p.n_eq_cls), p.n_polar, p.d_dtimg != nullptr);
 }
 
 }  // namespace sfb
