@@ -134,17 +134,19 @@ __device__ __forceinline__ void lvl_teardown(uint32_t tmem) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
 }
 
-// The ten level products of one K chunk (one K step of 16): level v goes to
-// TMEM columns [NMAX v, NMAX v + N).
-__device__ __forceinline__ void lvl_mma(uint32_t tmem, uint32_t a0, uint32_t b0, uint32_t planeB, uint32_t idesc,
+// The ten level products of one K chunk (one K step of 16) as six MMAs
+// (tc_common.cuh): level v goes to TMEM columns [LS v, LS v + LS), LS = the
+// MMA's N (lambda rows or rings of this CTA).
+__device__ __forceinline__ void lvl_mma(uint32_t tmem, uint32_t a0, uint32_t b0, uint32_t planeB, int LS,
                                         bool first_chunk) {
     const uint32_t sbo = (KC / 8) * 128;
+    const uint32_t id1 = idesc_bf16(MTILE, LS), id2 = idesc_bf16(MTILE, 2 * LS);
 #pragma unroll
-    for (int p = 0; p < 10; ++p) {
-        const uint64_t ad = smem_desc(a0 + lvl_a(p) * PLANE_A, 128, sbo);
-        const uint64_t bd = smem_desc(b0 + lvl_b(p) * planeB, 128, sbo);
-        const uint32_t acc = (first_chunk && lvl_first(p)) ? 0u : 1u;
-        mma_bf16(tmem + (uint32_t)NMAX * (uint32_t)lvl_of(p), ad, bd, idesc, acc);
+    for (int q = 0; q < NMERGED; ++q) {
+        const uint64_t ad = smem_desc(a0 + mg_a(q) * PLANE_A, 128, sbo);
+        const uint64_t bd = smem_desc(b0 + mg_b(q) * planeB, 128, sbo);
+        const uint32_t acc = (first_chunk && mg_first(q)) ? 0u : 1u;
+        mma_bf16(tmem + (uint32_t)LS * (uint32_t)mg_lvl(q), ad, bd, mg_two(q) ? id2 : id1, acc);
     }
 }
 
@@ -165,8 +167,7 @@ __device__ __forceinline__ uint32_t ph_of(int kc) { return (uint32_t)((kc / NSTA
 // MMA warp (lane 0 issues): for every chunk wait for its A slices and lambda
 // planes, issue the ten products, release the stage; finally commit `done`.
 // Returns the number of chunks issued.
-__device__ __forceinline__ int lvl_mma_loop(const LvlSmem &cs, uint32_t tmem, int nch, uint32_t planeB,
-                                            uint32_t idesc) {
+__device__ __forceinline__ int lvl_mma_loop(const LvlSmem &cs, uint32_t tmem, int nch, uint32_t planeB, int LS) {
     int issued = 0;
     for (int kc = 0; kc < nch; ++kc) {
         const int s = kc % NSTAGE;
@@ -177,7 +178,7 @@ __device__ __forceinline__ int lvl_mma_loop(const LvlSmem &cs, uint32_t tmem, in
         }
         fence_after();
         const uint32_t sa = smem_u32(cs.stage(s));
-        lvl_mma(tmem, sa, sa + 4 * PLANE_A, planeB, idesc, kc == 0);
+        lvl_mma(tmem, sa, sa + 4 * PLANE_A, planeB, LS, kc == 0);
         mma_commit(&cs.empty[s]);
         ++issued;
     }
@@ -249,11 +250,11 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_analysis_tc(const __nv_bfloat16 
     float C[4];
     slice_consts(cok ? Ecol[(int64_t)z * ncol + col0 + c] : 0, C);
     const uint32_t tmem = lvl_setup(cs);
-    const uint32_t idesc = idesc_bf16(MTILE, NPc);
+    const int LS = NPc;                         // MMA N and TMEM level stride
 
     if (!prod) {
         if ((tid & 31) == 0) {
-            const int issued = lvl_mma_loop(cs, tmem, nchunks, planeB, idesc);
+            const int issued = lvl_mma_loop(cs, tmem, nchunks, planeB, LS);
             if (issued != nchunks) atomicExch(cs.bad, 1);
         }
     } else {
@@ -322,9 +323,9 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_analysis_tc(const __nv_bfloat16 
             if (i0 >= NPc) break;                           // warp-uniform
             float v0[8], v1[8], v2[8], v3[8];
             tmem_ld8(tmem + lane_base + (uint32_t)i0, v0);
-            tmem_ld8(tmem + lane_base + (uint32_t)(NMAX + i0), v1);
-            tmem_ld8(tmem + lane_base + (uint32_t)(2 * NMAX + i0), v2);
-            tmem_ld8(tmem + lane_base + (uint32_t)(3 * NMAX + i0), v3);
+            tmem_ld8(tmem + lane_base + (uint32_t)(LS + i0), v1);
+            tmem_ld8(tmem + lane_base + (uint32_t)(2 * LS + i0), v2);
+            tmem_ld8(tmem + lane_base + (uint32_t)(3 * LS + i0), v3);
             if (cc < ncol) {
                 auto off = [&](int i) {
                     const int l = m + par + 2 * (row0 + i0 + i);
@@ -432,11 +433,11 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_synthesis_tc(const __nv_bfloat16
         Ecl = scale_exp(fmaxf(red[0][c], red[1][c]));
     }
     slice_consts(Ecl, C);
-    const uint32_t idesc = idesc_bf16(MTILE, NT);
+    const int LS = NT;                          // MMA N and TMEM level stride
 
     if (!prod) {
         if (lane == 0) {
-            const int issued = lvl_mma_loop(cs, tmem, nK, planeB, idesc);
+            const int issued = lvl_mma_loop(cs, tmem, nK, planeB, LS);
             if (issued != nK) atomicExch(cs.bad, 1);
         }
     } else {
@@ -493,9 +494,9 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_synthesis_tc(const __nv_bfloat16
             if (i0 >= NT) break;                            // warp-uniform
             float v0[8], v1[8], v2[8], v3[8];
             tmem_ld8(tmem + lane_base + (uint32_t)i0, v0);
-            tmem_ld8(tmem + lane_base + (uint32_t)(NMAX + i0), v1);
-            tmem_ld8(tmem + lane_base + (uint32_t)(2 * NMAX + i0), v2);
-            tmem_ld8(tmem + lane_base + (uint32_t)(3 * NMAX + i0), v3);
+            tmem_ld8(tmem + lane_base + (uint32_t)(LS + i0), v1);
+            tmem_ld8(tmem + lane_base + (uint32_t)(2 * LS + i0), v2);
+            tmem_ld8(tmem + lane_base + (uint32_t)(3 * LS + i0), v3);
             if (cc < ncol && !upd) {
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {

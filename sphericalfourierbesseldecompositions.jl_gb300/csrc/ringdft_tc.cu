@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
     __syncthreads();
     fence_after();
     const uint32_t tmem = *slot;
-    const uint32_t idesc = idesc_bf16(NROW, NCOL);
+    const uint32_t id1 = idesc_bf16(NROW, NCOL), id2 = idesc_bf16(NROW, 2 * NCOL);
     int ncopied = 0;                                   // thread 0 (IMG): image chunks whose copy was issued
 
     if (!prod) {
@@ -207,14 +207,15 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
                 fence_after();
                 const uint32_t base = smem_u32(smem + st * STAGE);
                 const uint32_t sbo = (KC / 8) * 128;
+                // the ten level products as six MMAs (tc_common.cuh); level v at TMEM columns 128 v
 #pragma unroll
                 for (int ks = 0; ks < KC / 16; ++ks) {
 #pragma unroll
-                    for (int p = 0; p < 10; ++p) {
-                        const bool first = kc == 0 && ks == 0 && lvl_first(p);
-                        mma_bf16(tmem + (uint32_t)(128 * lvl_of(p)),
-                                 smem_desc(base + lvl_a(p) * PLANE + ks * 256, 128, sbo),
-                                 smem_desc(base + (4 + lvl_b(p)) * PLANE + ks * 256, 128, sbo), idesc,
+                    for (int q = 0; q < NMERGED; ++q) {
+                        const bool first = kc == 0 && ks == 0 && mg_first(q);
+                        mma_bf16(tmem + (uint32_t)(NCOL * mg_lvl(q)),
+                                 smem_desc(base + mg_a(q) * PLANE + ks * 256, 128, sbo),
+                                 smem_desc(base + (4 + mg_b(q)) * PLANE + ks * 256, 128, sbo), mg_two(q) ? id2 : id1,
                                  first ? 0u : 1u);
                     }
                 }

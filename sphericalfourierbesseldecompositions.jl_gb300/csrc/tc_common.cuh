@@ -164,11 +164,21 @@ __device__ __forceinline__ int scale_exp(float mx) {
     return E;
 }
 
-// products (s_a, s_b) of slice levels 0..3: level 0 = [0], 1 = [1, 3), 2 = [3, 6), 3 = [6, 10)
-__device__ __forceinline__ int lvl_a(int p) { return p == 0 ? 0 : p < 3 ? p - 1 : p < 6 ? p - 3 : p - 6; }
-__device__ __forceinline__ int lvl_b(int p) { return p == 0 ? 0 : p < 3 ? 2 - p : p < 6 ? 5 - p : 9 - p; }
-__device__ __forceinline__ int lvl_of(int p) { return p == 0 ? 0 : p < 3 ? 1 : p < 6 ? 2 : 3; }
-__device__ __forceinline__ bool lvl_first(int p) { return p == 0 || p == 1 || p == 3 || p == 6; }
+// The ten products (s_a, s_b), s_a + s_b <= 3, issued as six MMAs: products
+// that share the A slice and land on adjacent levels go as one MMA of twice
+// the N over two consecutive B planes (the planes are stored back to back, so
+// the second plane's rows continue the first's at the same stride, and level v
+// occupies TMEM columns [v LS, (v + 1) LS) for the kernel's level stride LS =
+// N):  q0 A0 x [B0|B1] -> levels 0, 1;  q1 A0 x [B2|B3] -> 2, 3;
+// q2 A1 x [B0|B1] -> 1, 2;  q3 A1 x B2 -> 3;  q4 A2 x [B0|B1] -> 2, 3;
+// q5 A3 x B0 -> 3.  q0 and q1 write every level first (no accumulate on the
+// first K step).
+constexpr int NMERGED = 6;
+__device__ __forceinline__ int mg_a(int q) { return q < 2 ? 0 : q < 4 ? 1 : q < 5 ? 2 : 3; }
+__device__ __forceinline__ int mg_b(int q) { return (q == 1 || q == 3) ? 2 : 0; }
+__device__ __forceinline__ int mg_lvl(int q) { return q == 0 ? 0 : q == 2 ? 1 : (q == 1 || q == 4) ? 2 : 3; }
+__device__ __forceinline__ bool mg_two(int q) { return q != 3 && q != 5; }
+__device__ __forceinline__ bool mg_first(int q) { return q < 2; }
 
 }  // namespace tc
 }  // namespace sfb
