@@ -371,8 +371,10 @@ __global__ void __launch_bounds__(128) k_deposit_moments_bal(const int32_t *__re
             dfl acc[MAXDEG + 1];
 #pragma unroll
             for (int k = 0; k <= MAXDEG; ++k) acc[k] = {0.f, 0.f};
+            double2 nxt = g0 < g1 ? sorted[g0] : make_double2(0.0, 0.0);
             for (int64_t g = g0; g < g1; ++g) {
-                const double2 xw = sorted[g];
+                const double2 xw = nxt;
+                if (g + 1 < g1) nxt = sorted[g + 1];          // next galaxy's load overlaps this one's basis
                 const dfl x = df_of(xw.x);
                 dfl q0 = df_of(xw.y), q1 = df_mul(q0, x);
                 acc[0] = df_add(acc[0], q0);

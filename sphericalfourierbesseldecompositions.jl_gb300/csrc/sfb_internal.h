@@ -301,8 +301,11 @@ __device__ __forceinline__ int64_t ang2pix_ring_fast(int64_t nside, double th, d
         float sn, cs;
         sincosf(th32, &sn, &cs);
         const float z = cs, za = fabsf(z);
-        float tt = fmodf((float)ph * 0.636619772f, 4.0f);
-        if (tt < 0.0f) tt += 4.0f;
+        // phi in quarter turns, reduced to [0, 4): t - 4 floor(t / 4) rounds exactly as
+        // fmodf(t, 4) (+ 4 when negative) does: the subtraction is exact for t >= 0 and a single
+        // rounding of t + 4 m otherwise
+        const float t4 = (float)ph * 0.636619772f;
+        const float tt = t4 - 4.0f * floorf(t4 * 0.25f);      // may round to 4: the margin test then falls back
         if (fabsf(za - 0.6666667f) > 1e-5f && far(tt) && tt < 4.0f - margin) {
             if (za < 0.6666667f) {
                 const float temp1 = ns * (0.5f + tt), temp2 = ns * z * 0.75f;
