@@ -114,11 +114,39 @@ int sfb_set_precision(sfb_plan *plan, int32_t precision);
 int sfb_cat2amln(sfb_plan *plan, const double *rtp, const double *weight, int64_t ngal,
                  double nbar, const sfb_window *window, double *anlm_out);
 
+/* Batched mocks: nmocks catalogues sharing one plan and one window (the
+ * per-mock loop a caller of cat2amln runs over mock catalogues, reference
+ * src/cat2anlm.jl:257-310 per mock).  Mock k is galaxies
+ * [offsets[k], offsets[k+1]) of rtp (3 x offsets[nmocks], as in sfb_cat2amln)
+ * and weight (NULL for ones), with nbar[k].  anlm_out: [nmocks][2*nlmsize].
+ * The next mock's catalogue is copied while the current one is transformed;
+ * errors of any mock are reported once for the batch. */
+int sfb_cat2amln_batched(sfb_plan *plan, const double *rtp, const double *weight, const int64_t *offsets,
+                         int64_t nmocks, const double *nbar, const sfb_window *window, double *anlm_out);
+
 /* Same as sfb_cat2amln with every pointer (rtp, weight, window arrays and
  * anlm_out) in device memory, launched on `stream` (cudaStream_t or NULL for
  * the legacy default stream).  Returns after the result is complete. */
 int sfb_cat2amln_device(sfb_plan *plan, const double *rtp, const double *weight, int64_t ngal,
                         double nbar, const sfb_window *window, double *anlm_out, void *stream);
+
+/* Adjoints (vector-Jacobian products), FP64, no reference counterpart (the
+ * reference's transforms are libsharp calls without derivatives): for a real
+ * loss L of the coefficients, abar = dL/dRe(a) + i dL/dIm(a) per coefficient
+ * ([2*nlmsize] interleaved, the a_nlm layout).
+ *
+ * sfb_cat2amln_vjp: dL/dw_i for the galaxy weights of sfb_cat2amln
+ * (rtp as there, the plan's radial basis; needs SFB_RADIAL_POLY); the window
+ * term does not depend on the weights.  dw_out: [ngal]. */
+int sfb_cat2amln_vjp(sfb_plan *plan, const double *rtp, int64_t ngal, double nbar, const double *abar,
+                     double *dw_out);
+
+/* dL/df for sfb_field2anlm: df_out [nr * npix], element (ir, p) at ir + nr*p. */
+int sfb_field2anlm_vjp(sfb_plan *plan, const double *abar, int64_t nr, double rmin, double rmax, double *df_out);
+
+/* Transpose of sfb_map2alm (niter refinement included): abar [nmaps][lmsize]
+ * complex (map2alm's output layout), maps_out [nmaps][npix]. */
+int sfb_map2alm_adjoint(sfb_plan *plan, const double *abar, int64_t nmaps, double *maps_out);
 
 /* field2anlm(f_xyz, wmodes, amodes) (reference field2anlm_v2, src/cat2anlm.jl:323-357).
  * f: [nr * npix] host array, element (ir, p) at ir + nr*p (Julia nr x npix matrix).

@@ -484,6 +484,42 @@ int reference_alm(sfb_plan *h, const double *ref, int64_t nref, double *ralm, cu
     return SFB_OK;
 }
 
+// Transpose of sht_analysis in FP64 (adjoint.cu): abar [lmsize][2 nm] on the device becomes E abar;
+// maps_out [nm][npix] FP64 receives w S sum_j (I - A S)^j E abar.
+int sht_analysis_adjoint(sfb_plan *h, double *abar, int64_t nm, double *maps_out, cudaStream_t st) {
+    Plan &p = h->p;
+    const int32_t prec = p.precision;
+    p.precision = SFB_FP64;
+    struct Restore {
+        Plan &p;
+        int32_t v;
+        ~Restore() { p.precision = v; }
+    } restore{p, prec};
+    const int64_t ncol = 2 * nm;
+    const size_t fsz = (size_t)2 * (p.lmax + 1) * p.nrn * ncol;
+    SFB_TRY(grow(p, p.gbuf, fsz));
+    SFB_TRY(grow(p, p.alm, (size_t)p.lmsize * ncol));
+    launch_halve_m(abar, p.lmsize, ncol, st);
+    double *x = p.alm.ptr;
+    SFB_CUDA_TRY(cudaMemcpyAsync(x, abar, (size_t)p.lmsize * ncol * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    if (p.niter > 0) {
+        SFB_TRY(grow(p, p.fbuf, fsz));
+        SFB_TRY(grow(p, p.rbuf, fsz));
+        SFB_CUDA_TRY(cudaMemsetAsync(p.fbuf.ptr, 0, fsz * sizeof(double), st));     // F = 0: the fold gives -A S x
+    }
+    for (int it = 0; it < p.niter; ++it) {
+        launch_leg_synthesis(p, x, ncol, p.gbuf.ptr, st);
+        launch_fold_residual(p, p.fbuf.ptr, p.gbuf.ptr, ncol, p.rbuf.ptr, st);
+        launch_leg_analysis(p, p.rbuf.ptr, ncol, x, true, st);                     // x - A S x
+        launch_axpy(x, abar, p.lmsize * ncol, st);                                   // + b
+    }
+    launch_leg_synthesis(p, x, ncol, p.gbuf.ptr, st);
+    launch_ring_synthesis(p, p.gbuf.ptr, nm, maps_out, st);
+    launch_scale(maps_out, nm * p.npix, 4.0 * M_PI / (double)p.npix, st);
+    SFB_CUDA_TRY(cudaGetLastError());
+    return SFB_OK;
+}
+
 int64_t chunk_pairs(const Plan &p) {
     // keep the per-chunk SHT workspace near 2 GB
     const double per_map = 8.0 * (p.npix + 3.0 * 2 * (p.lmax + 1) * p.nrn * 2 + 2.0 * p.lmsize);
@@ -492,8 +528,11 @@ int64_t chunk_pairs(const Plan &p) {
     return c;
 }
 
+// defer_finish (batched calls): the device error word is neither cleared nor read here and the
+// call does not wait for the device; the caller clears it once and checks it at the end.
 int cat2amln_dev(sfb_plan *h, const double *rtp, const double *w, int64_t ngal, double nbar, const sfb_window *win,
-                 double *out, cudaStream_t st, const cudaEvent_t *chunk_ready = nullptr, int nchunks = 0) {
+                 double *out, cudaStream_t st, const cudaEvent_t *chunk_ready = nullptr, int nchunks = 0,
+                 bool defer_finish = false) {
     Plan &p = h->p;
     if (ngal < 0) return fail(SFB_EINVAL, "ngal < 0");
     if (!win) return fail(SFB_EINVAL, "window descriptor is NULL");
@@ -506,7 +545,7 @@ int cat2amln_dev(sfb_plan *h, const double *rtp, const double *w, int64_t ngal, 
     if (wk == SFB_WINDOW_DENSE && !win->dense) return fail(SFB_EINVAL, "dense window pointer is NULL");
     const double dOmega = 4.0 * M_PI / (double)p.npix;
     const double scale = 1.0 / (nbar * dOmega);
-    SFB_CUDA_TRY(cudaMemsetAsync(p.d_err, 0, sizeof(int), st));
+    if (!defer_finish) SFB_CUDA_TRY(cudaMemsetAsync(p.d_err, 0, sizeof(int), st));
     if (p.radial_mode == SFB_RADIAL_POLY) {
         const int64_t nm = p.nbasis + (wk == SFB_WINDOW_SEPARABLE ? 1 : 0);
         // Mixed precision: the data maps are split into mu_b C + fluctuation
@@ -590,6 +629,11 @@ int cat2amln_dev(sfb_plan *h, const double *rtp, const double *w, int64_t ngal, 
         }
     }
     SFB_CUDA_TRY(cudaGetLastError());
+    if (defer_finish) {
+        Stage s(h, SFB_STAGE_OTHER, st);
+        launch_check_finite(out, 2 * p.nlmsize, p.d_err, st);
+        return SFB_OK;
+    }
     return finish(h, out, st);
 }
 
@@ -1048,6 +1092,216 @@ int sfb_cat2amln(sfb_plan *h, const double *rtp, const double *weight, int64_t n
     SFB_TRY(cat2amln_dev(h, ngal > 0 ? d_rtp : nullptr, d_w, ngal, nbar, &dw, d_out, st, ncopy ? h->ev_copy : nullptr,
                          ncopy));
     SFB_CUDA_TRY(cudaMemcpyAsync(anlm_out, d_out, 2 * p.nlmsize * sizeof(double), cudaMemcpyDeviceToHost, st));
+    SFB_CUDA_TRY(cudaStreamSynchronize(st));
+    return SFB_OK;
+}
+
+// Batched catalogues (mock batches): mock k's galaxies go up on a copy stream into one of two
+// staging buffers while mock k - 1 is transformed on the plan's stream; results come back
+// per mock.  The device error word collects every mock's errors and is read once.
+int sfb_cat2amln_batched(sfb_plan *h, const double *rtp, const double *weight, const int64_t *offsets,
+                         int64_t nmocks, const double *nbar, const sfb_window *window, double *anlm_out) {
+    SFB_TRY(check_plan(h));
+    SFB_TRY(set_device_of(h));
+    if (nmocks < 0 || (nmocks > 0 && (!offsets || !nbar || !anlm_out)) || !window)
+        return fail(SFB_EINVAL, "bad batched cat2amln arguments");
+    if (nmocks == 0) return SFB_OK;
+    int64_t nmax_gal = 0;
+    for (int64_t k = 0; k < nmocks; ++k) {
+        const int64_t n = offsets[k + 1] - offsets[k];
+        if (offsets[k] < 0 || n < 0) return fail(SFB_EINVAL, "offsets must be non-decreasing from 0");
+        if (!(std::isfinite(nbar[k]) && nbar[k] != 0.0)) return fail(SFB_ENONFINITE, "nbar must be finite and non-zero");
+        nmax_gal = std::max(nmax_gal, n);
+    }
+    if (offsets[nmocks] > 0 && !rtp) return fail(SFB_EINVAL, "rtp is NULL");
+    Plan &p = h->p;
+    cudaStream_t st = h->stream;
+    const int64_t wlen = window->kind == SFB_WINDOW_SEPARABLE ? p.npix + (int64_t)(p.lmax + 1) * p.nmax
+                       : window->kind == SFB_WINDOW_DENSE ? p.npix * (int64_t)(p.lmax + 1) * p.nmax : 0;
+    // [window][2 x (rtp 3 nmax_gal, w nmax_gal, out 2 nlmsize)]
+    const int64_t per_buf = 3 * nmax_gal + (weight ? nmax_gal : 0) + 2 * p.nlmsize;
+    SFB_TRY(grow(p, p.scratch, (size_t)(wlen + 2 * per_buf + 1)));
+    double *d_win = p.scratch.ptr;
+    sfb_window dw = *window;
+    if (window->kind == SFB_WINDOW_SEPARABLE) {
+        if (!window->mask || !window->w_ln) return fail(SFB_EINVAL, "separable window needs mask and w_ln");
+        SFB_CUDA_TRY(cudaMemcpyAsync(d_win, window->mask, p.npix * sizeof(double), cudaMemcpyHostToDevice, st));
+        SFB_CUDA_TRY(cudaMemcpyAsync(d_win + p.npix, window->w_ln, (size_t)(p.lmax + 1) * p.nmax * sizeof(double),
+                                     cudaMemcpyHostToDevice, st));
+        dw.mask = d_win;
+        dw.w_ln = d_win + p.npix;
+    } else if (window->kind == SFB_WINDOW_DENSE) {
+        if (!window->dense) return fail(SFB_EINVAL, "dense window pointer is NULL");
+        SFB_CUDA_TRY(cudaMemcpyAsync(d_win, window->dense, (size_t)wlen * sizeof(double), cudaMemcpyHostToDevice, st));
+        dw.dense = d_win;
+    } else if (window->kind != SFB_WINDOW_ZERO) {
+        return fail(SFB_EINVAL, "unknown window kind");
+    }
+    cudaStream_t cs = nullptr;
+    cudaEvent_t ev[2][sfb_plan::NCOPY + 1] = {};   // per buffer: chunk copies landed, buffer free
+    auto release = [&] {
+        for (auto &b : ev)
+            for (auto &e : b)
+                if (e) cudaEventDestroy(e);
+        if (cs) cudaStreamDestroy(cs);
+    };
+    if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(SFB_ECUDA, "stream creation failed");
+    }
+    for (auto &b : ev)
+        for (auto &e : b)
+            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+                cudaGetLastError();
+                release();
+                return fail(SFB_ECUDA, "event creation failed");
+            }
+    int rc = SFB_OK;
+    if (cudaMemsetAsync(p.d_err, 0, sizeof(int), st) != cudaSuccess) rc = fail(SFB_ECUDA, "error word reset failed");
+    // the copy stream starts after the plan stream's earlier work (the window copy included)
+    if (rc == SFB_OK && (cudaEventRecord(ev[1][sfb_plan::NCOPY], st) != cudaSuccess ||
+                         cudaEventRecord(ev[0][sfb_plan::NCOPY], st) != cudaSuccess))
+        rc = fail(SFB_ECUDA, "event record failed");
+    auto dbuf = [&](int64_t k) { return d_win + wlen + (k & 1) * per_buf; };
+    // copies of mock k into buffer k & 1, once mock k - 2 released it
+    auto enqueue_copy = [&](int64_t k) -> int {
+        const int b = (int)(k & 1);
+        double *d_rtp = dbuf(k);
+        double *d_w = weight ? d_rtp + 3 * nmax_gal : nullptr;
+        const int64_t g0 = offsets[k], ngal = offsets[k + 1] - offsets[k];
+        if (cudaStreamWaitEvent(cs, ev[b][sfb_plan::NCOPY], 0) != cudaSuccess) return fail(SFB_ECUDA, "stream wait failed");
+        const int ncopy = sfb_plan::NCOPY;
+        const int64_t per = ngal > 0 ? (ngal + ncopy - 1) / ncopy : 0;
+        for (int c = 0; c < ncopy; ++c) {
+            const int64_t c0 = c * per, n = std::min<int64_t>(per, ngal - c0);
+            if (n > 0) {
+                if (cudaMemcpyAsync(d_rtp + 3 * c0, rtp + 3 * (g0 + c0), 3 * n * sizeof(double),
+                                    cudaMemcpyHostToDevice, cs) != cudaSuccess ||
+                    (weight && cudaMemcpyAsync(d_w + c0, weight + g0 + c0, n * sizeof(double), cudaMemcpyHostToDevice,
+                                               cs) != cudaSuccess))
+                    return fail(SFB_ECUDA, "catalogue copy failed");
+            }
+            if (cudaEventRecord(ev[b][c], cs) != cudaSuccess) return fail(SFB_ECUDA, "event record failed");
+        }
+        return SFB_OK;
+    };
+    if (rc == SFB_OK) rc = enqueue_copy(0);
+    for (int64_t k = 0; k < nmocks && rc == SFB_OK; ++k) {
+        // the next mock's copy is queued before this mock's result is read back (which blocks the host
+        // for pageable output), so it overlaps this mock's transform
+        if (k + 1 < nmocks && (rc = enqueue_copy(k + 1)) != SFB_OK) break;
+        const int b = (int)(k & 1);
+        double *d_rtp = dbuf(k);
+        double *d_w = weight ? d_rtp + 3 * nmax_gal : nullptr;
+        double *d_out = d_rtp + 3 * nmax_gal + (weight ? nmax_gal : 0);
+        const int64_t ngal = offsets[k + 1] - offsets[k];
+        rc = cat2amln_dev(h, ngal > 0 ? d_rtp : nullptr, d_w, ngal, nbar[k], &dw, d_out, st, ev[b],
+                          sfb_plan::NCOPY, true);
+        if (rc != SFB_OK) break;
+        if (cudaEventRecord(ev[b][sfb_plan::NCOPY], st) != cudaSuccess ||
+            cudaMemcpyAsync(anlm_out + 2 * p.nlmsize * k, d_out, 2 * p.nlmsize * sizeof(double),
+                            cudaMemcpyDeviceToHost, st) != cudaSuccess)
+            rc = fail(SFB_ECUDA, "result copy failed");
+    }
+    int err = 0;
+    if (rc == SFB_OK && (cudaMemcpyAsync(&err, p.d_err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                         cudaStreamSynchronize(st) != cudaSuccess))
+        rc = fail(SFB_ECUDA, std::string("batched cat2amln failed: ") + cudaGetErrorString(cudaGetLastError()));
+    cudaStreamSynchronize(cs);
+    release();
+    SFB_TRY(rc);
+    collect_stages(h);
+    if (err & ERR_NONFINITE_INPUT) return fail(SFB_ENONFINITE, "non-finite galaxy coordinate or weight");
+    if (err & ERR_THETA_RANGE) return fail(SFB_ERANGE, "galaxy theta outside [0, pi]");
+    if (err & ERR_TC_TIMEOUT) return fail(SFB_ETIMEOUT, "tensor-core kernel: bounded mbarrier wait expired");
+    if (err & ERR_NONFINITE_OUTPUT) return fail(SFB_ENONFINITE, "non-finite a_nlm (all(isfinite.(anlm)) failed)");
+    return SFB_OK;
+}
+
+int sfb_map2alm_adjoint(sfb_plan *h, const double *abar, int64_t nmaps, double *maps_out) {
+    SFB_TRY(check_plan(h));
+    SFB_TRY(set_device_of(h));
+    if (nmaps <= 0 || !abar || !maps_out) return fail(SFB_EINVAL, "bad map2alm adjoint arguments");
+    Plan &p = h->p;
+    cudaStream_t st = h->stream;
+    // abar [nmaps][lmsize] complex (map2alm's output layout) -> [lmsize][2 nmaps] on the device
+    std::vector<double> A((size_t)p.lmsize * 2 * nmaps);
+    for (int64_t b = 0; b < nmaps; ++b)
+        for (int64_t lm = 0; lm < p.lmsize; ++lm) {
+            A[(size_t)lm * 2 * nmaps + 2 * b] = abar[(b * p.lmsize + lm) * 2];
+            A[(size_t)lm * 2 * nmaps + 2 * b + 1] = abar[(b * p.lmsize + lm) * 2 + 1];
+        }
+    SFB_TRY(grow(p, p.scratch, A.size()));
+    SFB_TRY(grow(p, p.maps, (size_t)nmaps * p.npix));
+    SFB_CUDA_TRY(cudaMemcpyAsync(p.scratch.ptr, A.data(), A.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    SFB_TRY(sht_analysis_adjoint(h, p.scratch.ptr, nmaps, p.maps.ptr, st));
+    SFB_CUDA_TRY(cudaMemcpyAsync(maps_out, p.maps.ptr, (size_t)nmaps * p.npix * sizeof(double), cudaMemcpyDeviceToHost,
+                                 st));
+    SFB_CUDA_TRY(cudaStreamSynchronize(st));
+    return SFB_OK;
+}
+
+int sfb_cat2amln_vjp(sfb_plan *h, const double *rtp, int64_t ngal, double nbar, const double *abar, double *dw_out) {
+    SFB_TRY(check_plan(h));
+    SFB_TRY(set_device_of(h));
+    if (ngal < 0 || (ngal > 0 && (!rtp || !dw_out)) || !abar) return fail(SFB_EINVAL, "bad cat2amln vjp arguments");
+    if (!(std::isfinite(nbar) && nbar != 0.0)) return fail(SFB_ENONFINITE, "nbar must be finite and non-zero");
+    Plan &p = h->p;
+    if (p.radial_mode != SFB_RADIAL_POLY)
+        return fail(SFB_ENOTSUP, "the cat2amln adjoint needs the piecewise-polynomial radial basis (SFB_RADIAL_POLY)");
+    if (ngal == 0) return SFB_OK;
+    cudaStream_t st = h->stream;
+    const double scale = 1.0 / (nbar * 4.0 * M_PI / (double)p.npix);
+    const int64_t nbc = std::max<int64_t>(1, std::min<int64_t>(p.nbasis, chunk_pairs(p)));
+    // [rtp 3N][dw N][abar 2 nlmsize][Abar lmsize x 2 nbc]
+    SFB_TRY(grow(p, p.scratch, (size_t)(4 * ngal + 2 * p.nlmsize + p.lmsize * 2 * nbc)));
+    SFB_TRY(grow(p, p.maps, (size_t)nbc * p.npix));
+    double *d_rtp = p.scratch.ptr, *d_dw = d_rtp + 3 * ngal, *d_ab = d_dw + ngal, *d_A = d_ab + 2 * p.nlmsize;
+    SFB_CUDA_TRY(cudaMemcpyAsync(d_rtp, rtp, 3 * ngal * sizeof(double), cudaMemcpyHostToDevice, st));
+    SFB_CUDA_TRY(cudaMemcpyAsync(d_ab, abar, 2 * p.nlmsize * sizeof(double), cudaMemcpyHostToDevice, st));
+    SFB_CUDA_TRY(cudaMemsetAsync(d_dw, 0, ngal * sizeof(double), st));
+    SFB_CUDA_TRY(cudaMemsetAsync(p.d_err, 0, sizeof(int), st));
+    for (int64_t b0 = 0; b0 < p.nbasis; b0 += nbc) {
+        const int64_t nb = std::min(nbc, p.nbasis - b0);
+        launch_proj_adjoint(p, d_ab, h->d_pair_index, h->d_noff, b0, nb, scale, d_A, st);
+        SFB_TRY(sht_analysis_adjoint(h, d_A, nb, p.maps.ptr, st));
+        launch_deposit_adjoint(p, d_rtp, ngal, p.maps.ptr, b0, nb, d_dw, st);
+    }
+    int err = 0;
+    SFB_CUDA_TRY(cudaMemcpyAsync(&err, p.d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    SFB_CUDA_TRY(cudaMemcpyAsync(dw_out, d_dw, ngal * sizeof(double), cudaMemcpyDeviceToHost, st));
+    SFB_CUDA_TRY(cudaStreamSynchronize(st));
+    if (err & ERR_NONFINITE_INPUT) return fail(SFB_ENONFINITE, "non-finite galaxy coordinate");
+    if (err & ERR_THETA_RANGE) return fail(SFB_ERANGE, "galaxy theta outside [0, pi]");
+    return SFB_OK;
+}
+
+int sfb_field2anlm_vjp(sfb_plan *h, const double *abar, int64_t nr, double rmin, double rmax, double *df_out) {
+    SFB_TRY(check_plan(h));
+    SFB_TRY(set_device_of(h));
+    if (!abar || !df_out || nr < 1 || !(rmin < rmax)) return fail(SFB_EINVAL, "bad field2anlm vjp arguments");
+    Plan &p = h->p;
+    cudaStream_t st = h->stream;
+    const double dr = (rmax - rmin) / (double)nr;
+    const int64_t cs = std::max<int64_t>(1, std::min<int64_t>(nr, chunk_pairs(p)));
+    // [abar 2 nlmsize][gtab npairs x nr][field nr x npix][Abar lmsize x 2 cs]
+    SFB_TRY(grow(p, p.scratch, (size_t)(2 * p.nlmsize + p.npairs * nr + nr * p.npix + p.lmsize * 2 * cs)));
+    double *d_ab = p.scratch.ptr, *d_g = d_ab + 2 * p.nlmsize, *d_f = d_g + p.npairs * nr, *d_A = d_f + nr * p.npix;
+    SFB_CUDA_TRY(cudaMemcpyAsync(d_ab, abar, 2 * p.nlmsize * sizeof(double), cudaMemcpyHostToDevice, st));
+    launch_gtab(p, nr, rmin, dr, 1, d_g, st);                // g_nl(r_s) r_s^2 dr, the field2anlm weights
+    SFB_TRY(grow(p, p.scratch2, (size_t)cs * p.npairs));
+    SFB_TRY(grow(p, p.maps, (size_t)cs * p.npix));
+    for (int64_t s0 = 0; s0 < nr; s0 += cs) {
+        const int64_t nsc = std::min(cs, nr - s0);
+        SFB_CUDA_TRY(cudaMemcpy2DAsync(p.scratch2.ptr, nsc * sizeof(double), d_g + s0, nr * sizeof(double),
+                                       nsc * sizeof(double), p.npairs, cudaMemcpyDeviceToDevice, st));
+        // Abar_s[lm] = sum_n g_nl(r_s) r_s^2 dr abar_nlm (the transpose of the radial sum)
+        launch_shell_alm_g(p, h->d_pair_index, h->d_noff, p.scratch2.ptr, nsc, d_ab, d_A, 2 * nsc, st);
+        SFB_TRY(sht_analysis_adjoint(h, d_A, nsc, p.maps.ptr, st));
+        launch_transpose_ld(p.maps.ptr, p.npix, nsc, p.npix, d_f + s0, nr, st);
+    }
+    SFB_CUDA_TRY(cudaGetLastError());
+    SFB_CUDA_TRY(cudaMemcpyAsync(df_out, d_f, (size_t)nr * p.npix * sizeof(double), cudaMemcpyDeviceToHost, st));
     SFB_CUDA_TRY(cudaStreamSynchronize(st));
     return SFB_OK;
 }

@@ -232,6 +232,13 @@ void launch_gram_update(const Plan &p, const double *A, const float2 *Adf, const
                         int *Eout = nullptr);
 int build_gram_tables(Plan &p, cudaStream_t st);
 void launch_df_to_fp64(const float2 *a, int64_t n, double *out, cudaStream_t st);
+// adjoint (adjoint.cu)
+void launch_halve_m(double *alm, int64_t lmsize, int64_t ncol, cudaStream_t st);
+void launch_scale(double *x, int64_t n, double s, cudaStream_t st);
+void launch_proj_adjoint(const Plan &p, const double *abar, const int32_t *pair_index, const int64_t *noff, int64_t b0,
+                         int64_t nbc, double s, double *Abar, cudaStream_t st);
+void launch_deposit_adjoint(const Plan &p, const double *rtp, int64_t ngal, const double *Dbar, int64_t b0,
+                            int64_t nbc, double *dw, cudaStream_t st);
 std::vector<int3> project_tiles(const std::vector<int32_t> &pair_index, int lmax, int nmax);
 void launch_transpose(const double *in, int64_t rows, int64_t cols, double *out, cudaStream_t st);
 void launch_check_finite(const double *x, int64_t n, int *err, cudaStream_t st);

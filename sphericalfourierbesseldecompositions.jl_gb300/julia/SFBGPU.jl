@@ -121,6 +121,31 @@ end
 const cat2nlm = cat2amln
 
 """
+    cat2amln_batched(catalogues, amodes, nbars, win_rhat_ln, weights=nothing; kw...)
+
+Mock batches: `catalogues` a vector of 3×N_k matrices, `nbars` one n̄ per mock;
+returns nlmsize × nmocks, column k = `SFB.cat2amln(catalogues[k], amodes,
+nbars[k], win_rhat_ln, weights[k])` (src/cat2anlm.jl:257-310 per mock).
+"""
+function cat2amln_batched(catalogues, amodes, nbars, win_rhat_ln, weights=nothing; kw...)
+    p = getplan(amodes; kw...)
+    sizes = [size(c, 2) for c in catalogues]
+    offsets = Int64[0; cumsum(sizes)]
+    r = isempty(catalogues) ? zeros(3, 0) : reduce(hcat, [Matrix{Float64}(c) for c in catalogues])
+    w = weights === nothing ? C_NULL : Vector{Float64}(reduce(vcat, weights))
+    nb = Vector{Float64}(nbars)
+    anlm = Matrix{ComplexF64}(undef, p.nlmsize, length(catalogues))
+    win, keep = window(win_rhat_ln, amodes)
+    GC.@preserve r w nb offsets keep anlm begin
+        check(ccall((:sfb_cat2amln_batched, libsfb), Cint,
+                    (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Int64}, Int64, Ptr{Float64}, Ref{Window},
+                     Ptr{ComplexF64}),
+                    p.handle, offsets[end] == 0 ? C_NULL : r, w, offsets, length(catalogues), nb, win, anlm))
+    end
+    return anlm
+end
+
+"""
     field2anlm(f_xyz, wmodes, amodes)    (src/cat2anlm.jl:323-357)
 """
 function field2anlm(f_xyz, wmodes, amodes; kw...)

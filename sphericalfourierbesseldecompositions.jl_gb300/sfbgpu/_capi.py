@@ -50,6 +50,11 @@ _PROTOS = [
     ("sfb_set_precision", C.c_int, [C.c_void_p, C.c_int32]),
     ("sfb_cat2amln", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_double, C.POINTER(Window),
                                C.c_void_p]),
+    ("sfb_cat2amln_vjp", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_double, C.c_void_p, C.c_void_p]),
+    ("sfb_field2anlm_vjp", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_double, C.c_double, C.c_void_p]),
+    ("sfb_map2alm_adjoint", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
+    ("sfb_cat2amln_batched", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
+                                       C.POINTER(Window), C.c_void_p]),
     ("sfb_cat2amln_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_double,
                                       C.POINTER(Window), C.c_void_p, C.c_void_p]),
     ("sfb_field2anlm", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_double, C.c_double, C.c_void_p]),

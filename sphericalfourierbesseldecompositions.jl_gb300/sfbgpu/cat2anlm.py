@@ -149,6 +149,38 @@ def cat2amln(rtp, amodes, nbar, win_rhat_ln, weight=None, **plan_opts):
 cat2nlm = cat2amln
 
 
+def cat2amln_batched(catalogues, amodes, nbars, win_rhat_ln, weights=None, **plan_opts):
+    """a_nlm of a batch of mock catalogues sharing the geometry and window:
+    ``catalogues`` is a sequence of (3, N_k) arrays, ``nbars`` one n̄ per mock,
+    ``weights`` None or a sequence of (N_k,) arrays (None entries for ones).
+    Returns (nmocks, nlmsize) complex, row k = cat2amln(catalogues[k], ...)."""
+    plan = get_plan(amodes, **plan_opts)
+    cats = [np.asarray(c, float) for c in catalogues]
+    if any(c.ndim != 2 or c.shape[0] != 3 for c in cats):
+        raise ValueError("every catalogue must be a 3 x N array")
+    nmocks = len(cats)
+    if len(nbars) != nmocks:
+        raise ValueError("one nbar per mock")
+    sizes = [c.shape[1] for c in cats]
+    offsets = np.zeros(nmocks + 1, np.int64)
+    offsets[1:] = np.cumsum(sizes)
+    gal = np.ascontiguousarray(np.concatenate([c.T for c in cats], axis=0)) if offsets[-1] else np.zeros((0, 3))
+    w = None
+    if weights is not None:
+        w = np.concatenate([np.ones(n) if wk is None else np.asarray(wk, float) for wk, n in zip(weights, sizes)])
+        if w.shape != (offsets[-1],):
+            raise ValueError("weights must match the catalogues")
+        w = np.ascontiguousarray(w)
+    nb = np.ascontiguousarray(nbars, float)
+    keep = []
+    win = _window_struct(win_rhat_ln, amodes, plan.npix, keep)
+    out = np.empty((nmocks, plan.nlmsize), np.complex128)
+    capi.check(capi.lib.sfb_cat2amln_batched(plan.handle, capi.ptr(gal) if offsets[-1] else None, capi.ptr(w),
+                                             capi.ptr(offsets), nmocks, capi.ptr(nb), capi.C.byref(win),
+                                             capi.ptr(out)))
+    return out
+
+
 def field2anlm(f_xyz, wmodes, amodes, **plan_opts):
     """SFB coefficients of an (nr, npix) field (reference field2anlm_v2, src/cat2anlm.jl:323-357)."""
     plan = get_plan(amodes, **plan_opts)
@@ -204,6 +236,39 @@ def map2alm(maps, amodes, **plan_opts):
     L = amodes.lmax
     out = np.empty((m.shape[0], (L + 1) * (L + 2) // 2), np.complex128)
     capi.check(capi.lib.sfb_map2alm(plan.handle, capi.ptr(m), m.shape[0], capi.ptr(out)))
+    return out
+
+
+def cat2amln_vjp(rtp, amodes, nbar, abar, **plan_opts):
+    """dL/dw for the galaxy weights of cat2amln, given abar = dL/dRe(a) + i dL/dIm(a)
+    (FP64 adjoint of the transform; the plan's piecewise-polynomial radial basis)."""
+    plan = get_plan(amodes, **plan_opts)
+    gal = np.ascontiguousarray(np.asarray(rtp, float).T)
+    ab = np.ascontiguousarray(abar, np.complex128)
+    if ab.shape != (plan.nlmsize,):
+        raise ValueError("abar must have getnlmsize(amodes) entries")
+    out = np.empty(gal.shape[0])
+    capi.check(capi.lib.sfb_cat2amln_vjp(plan.handle, capi.ptr(gal) if gal.shape[0] else None, gal.shape[0],
+                                         float(nbar), capi.ptr(ab), capi.ptr(out)))
+    return out
+
+
+def field2anlm_vjp(abar, wmodes, amodes, **plan_opts):
+    """dL/df (nr, npix) for field2anlm, given abar = dL/dRe(a) + i dL/dIm(a)."""
+    plan = get_plan(amodes, **plan_opts)
+    ab = np.ascontiguousarray(abar, np.complex128)
+    out = np.empty((wmodes.nr, plan.npix), order="F")
+    capi.check(capi.lib.sfb_field2anlm_vjp(plan.handle, capi.ptr(ab), wmodes.nr, wmodes.rmin, wmodes.rmax,
+                                           capi.ptr(out)))
+    return out
+
+
+def map2alm_adjoint(abar, amodes, **plan_opts):
+    """Transpose of map2alm (niter refinement included): (nmaps, lmsize) complex -> (nmaps, npix)."""
+    plan = get_plan(amodes, **plan_opts)
+    ab = np.ascontiguousarray(np.atleast_2d(abar), np.complex128)
+    out = np.empty((ab.shape[0], plan.npix))
+    capi.check(capi.lib.sfb_map2alm_adjoint(plan.handle, capi.ptr(ab), ab.shape[0], capi.ptr(out)))
     return out
 
 
