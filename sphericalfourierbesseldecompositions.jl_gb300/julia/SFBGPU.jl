@@ -214,6 +214,38 @@ function amln2clnn(anlm, cmodes; kw...)
 end
 
 """
+    cat2amln_vjp(rθϕ, amodes, nbar, abar; kw...) -> dL/dw
+
+Gradient of a real loss L through `cat2amln` with respect to the galaxy
+weights, given `abar = ∂L/∂Re(a) + i ∂L/∂Im(a)` (FP64 adjoint; a ChainRules
+`rrule` for `cat2amln` returns `(NoTangent(), …, cat2amln_vjp(...))` for the
+weight argument).
+"""
+function cat2amln_vjp(rθϕ, amodes, nbar, abar; kw...)
+    p = getplan(amodes; kw...)
+    r = Matrix{Float64}(rθϕ)
+    a = Vector{ComplexF64}(abar)
+    dw = Vector{Float64}(undef, size(r, 2))
+    GC.@preserve r a dw check(ccall((:sfb_cat2amln_vjp, libsfb), Cint,
+                                    (Ptr{Cvoid}, Ptr{Float64}, Int64, Float64, Ptr{ComplexF64}, Ptr{Float64}),
+                                    p.handle, size(r, 2) == 0 ? C_NULL : r, size(r, 2), nbar, a, dw))
+    return dw
+end
+
+"""
+    field2anlm_vjp(abar, wmodes, amodes; kw...) -> dL/df  (nr × npix)
+"""
+function field2anlm_vjp(abar, wmodes, amodes; kw...)
+    p = getplan(amodes; kw...)
+    a = Vector{ComplexF64}(abar)
+    df = Matrix{Float64}(undef, wmodes.nr, p.npix)
+    GC.@preserve a df check(ccall((:sfb_field2anlm_vjp, libsfb), Cint,
+                                  (Ptr{Cvoid}, Ptr{ComplexF64}, Int64, Float64, Float64, Ptr{Float64}),
+                                  p.handle, a, wmodes.nr, wmodes.rmin, wmodes.rmax, df))
+    return df
+end
+
+"""
     winweights2galweights(weights, wmodes, rθϕ)    (src/cat2anlm.jl:218-238)
 """
 function winweights2galweights(weights, wmodes, rθϕ)
