@@ -150,7 +150,9 @@ int sfb_map2alm_adjoint(sfb_plan *plan, const double *abar, int64_t nmaps, doubl
 
 /* field2anlm(f_xyz, wmodes, amodes) (reference field2anlm_v2, src/cat2anlm.jl:323-357).
  * f: [nr * npix] host array, element (ir, p) at ir + nr*p (Julia nr x npix matrix).
- * ConfigurationSpaceModes(rmin, rmax, nr, nside) shells (src/windows.jl:98-103). */
+ * ConfigurationSpaceModes(rmin, rmax, nr, nside) shells (src/windows.jl:98-103).
+ * The shell transforms run in the plan's precision (SFB_MIXED: the tensor-core
+ * transform of the FP32-rounded shells; the radial sum in FP64). */
 int sfb_field2anlm(sfb_plan *plan, const double *f, int64_t nr, double rmin, double rmax,
                    double *anlm_out);
 

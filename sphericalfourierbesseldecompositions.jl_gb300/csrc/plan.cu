@@ -1349,7 +1349,7 @@ static int sfb_field2anlm_impl(sfb_plan *h, const double *f, int64_t nr, double 
         SFB_TRY(grow(p, p.maps, (size_t)nsc * p.npix));
         // maps[s][p] = f[s0+s + nr p]
         launch_transpose_ld(d_f + s0, nr, p.npix, nsc, p.maps.ptr, p.npix, st);
-        SFB_TRY(sht_analysis(h, p.maps.ptr, nsc, st));
+        SFB_TRY(sht_analysis(h, p.maps.ptr, nsc, st, true));     // FP64 maps (converted in mixed precision)
         // gtab for this chunk: rows pair, cols nsc (copy sub-block)
         SFB_CUDA_TRY(cudaMemcpy2DAsync(p.scratch2.ptr, nsc * sizeof(double), d_g + s0, nr * sizeof(double),
                                        nsc * sizeof(double), p.npairs, cudaMemcpyDeviceToDevice, st));
@@ -1544,12 +1544,8 @@ int sfb_map2alm(sfb_plan *h, const double *maps, int64_t nmaps, double *alm_out)
 
 int sfb_field2anlm(sfb_plan *h, const double *f, int64_t nr, double rmin, double rmax, double *anlm_out) {
     SFB_TRY(check_plan(h));
-    // these transforms run in FP64 whatever the plan's cat2amln precision
-    const int saved = h->p.precision;
-    h->p.precision = SFB_FP64;
-    const int rc = sfb_field2anlm_impl(h, f, nr, rmin, rmax, anlm_out);
-    h->p.precision = saved;
-    return rc;
+    // the shell maps go through the plan's transform (FP64, or the mixed tensor-core one)
+    return sfb_field2anlm_impl(h, f, nr, rmin, rmax, anlm_out);
 }
 
 int sfb_anlm2field(sfb_plan *h, const double *anlm, int64_t nr, double rmin, double rmax, double *f_out) {

@@ -146,6 +146,20 @@ def test_mixed_full_size():
     assert e2 < MIXED_TOL and emax < 10 * MIXED_TOL
 
 
+def test_field2anlm_mixed_vs_fp64():
+    """field2anlm on a plan in mixed precision (tensor-core shell transforms of
+    the FP32-rounded field, FP64 radial sum) against the FP64 plan."""
+    a = sfbgpu.AnlmModes(0.05, 500.0, 1000.0, nside=32)
+    wm = sfbgpu.ConfigurationSpaceModes(a.rmin, a.rmax, 64, a.nside)
+    rng = np.random.default_rng(11)
+    f = rng.normal(size=(wm.nr, wm.npix)).astype(np.float32).astype(float)
+    f64 = sfbgpu.field2anlm(f, wm, a, precision="fp64")
+    mix = sfbgpu.field2anlm(f, wm, a, precision="mixed")
+    e2, emax = _errors(mix, f64)
+    record("field2anlm_mixed_vs_fp64", e2, maxnorm=emax)
+    assert e2 < MIXED_TOL and emax < 10 * MIXED_TOL
+
+
 def test_bounded_wait_times_out_and_context_survives():
     """A device wait with no arrival expires, is reported as SFB_ETIMEOUT, and
     the next transform still runs (failure detection without a GPU fault)."""
