@@ -35,10 +35,30 @@ constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ITEMS = 16;                    // per thread
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 
+// Slot and local coordinate of radius r: u = (r - rmin) / width in units of
+// the pieces (inv_width = pieces / (rmax - rmin), formed once on the host),
+// x in [-1, 1] on the piece; slots pieces / pieces + 1 below / above.
+__device__ __forceinline__ int slot_of(double r, double rmin, double rmax, double inv_width, int pieces, double &x) {
+    x = 0.0;
+    if (r < rmin) return pieces;
+    if (r > rmax) return pieces + 1;
+    const double u = (r - rmin) * inv_width;
+    int slot = (int)u;
+    if (slot >= pieces) slot = pieces - 1;
+    x = 2.0 * (u - (double)slot) - 1.0;
+    x = fmin(1.0, fmax(-1.0, x));
+    return slot;
+}
+
+// Keys of galaxies [0, ngal) of this chunk (global index gbase + i).  A galaxy
+// whose pixel the FP32 evaluation cannot settle goes to fb_list and gets its
+// key and rank from k_deposit_keys_fallback (FP64), so no warp runs the FP64
+// pixel path for one lane.
 __global__ void k_deposit_keys(const double *__restrict__ rtp, const double *__restrict__ wgt, int64_t ngal,
-                               int64_t nside, int64_t npix, double rmin, double rmax, double inv_width, int pieces,
-                               int32_t *__restrict__ counts, int32_t *__restrict__ key, int32_t *__restrict__ rank,
-                               double *__restrict__ xloc, int *err) {
+                               int64_t gbase, int64_t nside, int64_t npix, double rmin, double rmax,
+                               double inv_width, int pieces, int32_t *__restrict__ counts,
+                               int32_t *__restrict__ key, int32_t *__restrict__ rank, double *__restrict__ xloc,
+                               int32_t *__restrict__ fb_list, int32_t *__restrict__ fb_count, int *err) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ngal) return;
     const double r = rtp[3 * i], th = rtp[3 * i + 1], ph = rtp[3 * i + 2];
@@ -50,26 +70,36 @@ __global__ void k_deposit_keys(const double *__restrict__ rtp, const double *__r
     } else if (th < 0.0 || th > M_PI) {
         atomicOr(err, ERR_THETA_RANGE);
     } else {
-        const int64_t pix = ang2pix_ring_fast(nside, th, ph);
-        int slot;
-        if (r < rmin) {
-            slot = pieces;
-        } else if (r > rmax) {
-            slot = pieces + 1;
+        const int64_t pix = ang2pix_ring_try(nside, th, ph);
+        const int slot = slot_of(r, rmin, rmax, inv_width, pieces, x);
+        if (pix >= 0) {
+            k = (int32_t)(slot * npix + pix);
+            rank[i] = atomicAdd(counts + k, 1);
         } else {
-            // u = (r - rmin) / width in units of the pieces (inv_width = pieces / (rmax - rmin),
-            // formed once on the host); x in [-1, 1] on the piece
-            const double u = (r - rmin) * inv_width;
-            slot = (int)u;
-            if (slot >= pieces) slot = pieces - 1;
-            x = 2.0 * (u - (double)slot) - 1.0;
-            x = fmin(1.0, fmax(-1.0, x));
+            fb_list[atomicAdd(fb_count, 1)] = (int32_t)(gbase + i);
         }
-        k = (int32_t)(slot * npix + pix);
-        rank[i] = atomicAdd(counts + k, 1);
     }
     key[i] = k;
     xloc[i] = x;
+}
+
+// The galaxies the FP32 pixel evaluation left: exact FP64 pixel, then key and
+// rank as above (rtp, key, rank indexed globally).
+__global__ void k_deposit_keys_fallback(const double *__restrict__ rtp, int64_t nside, int64_t npix, double rmin,
+                                        double rmax, double inv_width, int pieces, int32_t *__restrict__ counts,
+                                        int32_t *__restrict__ key, int32_t *__restrict__ rank,
+                                        const int32_t *__restrict__ fb_list, const int32_t *__restrict__ fb_count) {
+    const int n = *fb_count;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int64_t i = fb_list[t];
+        const double r = rtp[3 * i], th = rtp[3 * i + 1], ph = rtp[3 * i + 2];
+        const int64_t pix = ang2pix_ring_z(nside, cos(th), ph);
+        double x;
+        const int slot = slot_of(r, rmin, rmax, inv_width, pieces, x);
+        const int32_t k = (int32_t)(slot * npix + pix);
+        rank[i] = atomicAdd(counts + k, 1);
+        key[i] = k;
+    }
 }
 
 // Exclusive scan, tile pass: each block scans SCAN_TILE counters in place and
@@ -247,6 +277,35 @@ __device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
 }
 
 __device__ __forceinline__ dfl df_neg(dfl a) { return {-a.hi, -a.lo}; }
+
+// bin_moments in double-float on the FP32 units (the sampled mean estimate:
+// the summation order, set by the atomic ranks, moves it by ~1e-14 only)
+template <int MAXDEG>
+__device__ __forceinline__ void bin_moments_df(const double2 *__restrict__ sorted, int64_t g0, int64_t g1, int deg,
+                                               double (&out)[MAXDEG + 1]) {
+    dfl acc[MAXDEG + 1];
+#pragma unroll
+    for (int k = 0; k <= MAXDEG; ++k) acc[k] = {0.f, 0.f};
+    for (int64_t g = g0; g < g1; ++g) {
+        const double2 xw = sorted[g];
+        const dfl x = df_of(xw.x);
+        dfl q0 = df_of(xw.y), q1 = df_mul(q0, x);
+        acc[0] = df_add(acc[0], q0);
+        if (MAXDEG >= 1) acc[1] = df_add(acc[1], q1);
+#pragma unroll
+        for (int k = 1; k < MAXDEG; ++k) {
+            if (k >= deg) break;
+            const dfl c1 = df_of((double)(2 * k + 1) / (k + 1));
+            const dfl c2 = df_of(-(double)k / (k + 1));
+            const dfl q2 = df_add(df_mul(c1, df_mul(x, q1)), df_mul(c2, q0));
+            acc[k + 1] = df_add(acc[k + 1], q2);
+            q0 = q1;
+            q1 = q2;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k <= MAXDEG; ++k) out[k] = (double)acc[k].hi + (double)acc[k].lo;
+}
 
 // Mixed precision: moments with the Legendre recurrence, the sums and the
 // fluctuation acc - mu_b ref all in double-float (mudf = mu as hi + lo),
@@ -429,7 +488,7 @@ __global__ void __launch_bounds__(32) k_deposit_stats(const int32_t *__restrict_
     const double rv = valid ? ref[pix] : 0.0;
     double acc[MAXDEG + 1];
     if (valid) {
-        bin_moments<MAXDEG>(sorted, offset[idx], offset[idx + 1], slot < pieces ? deg : 0, acc);
+        bin_moments_df<MAXDEG>(sorted, offset[idx], offset[idx + 1], slot < pieces ? deg : 0, acc);
     } else {
 #pragma unroll
         for (int k = 0; k <= MAXDEG; ++k) acc[k] = 0.0;
@@ -520,7 +579,7 @@ int deposit_sorted(Plan &p, const double *rtp, const double *w, int64_t ngal, do
     const int64_t ntiles = (nscan + SCAN_TILE - 1) / SCAN_TILE;
     // workspace: counters/offsets [nscan] int32, tile sums [ntiles] int32, key and rank [ngal] int32,
     // local coordinate [ngal] double, sorted (x, w) [ngal] double2
-    const int64_t ints = nscan + ntiles + 2 * ngal;
+    const int64_t ints = nscan + ntiles + 3 * ngal + 1;      // + FP64-pixel list [ngal] and its count
     const int64_t off_x = (ints + 1) / 2;
     int64_t off_sorted = off_x + ngal;
     off_sorted += off_sorted & 1;
@@ -530,9 +589,13 @@ int deposit_sorted(Plan &p, const double *rtp, const double *w, int64_t ngal, do
     int32_t *tsum = counts + nscan;
     int32_t *key = tsum + ntiles;
     int32_t *rank = key + ngal;
+    int32_t *fb_list = rank + ngal;
+    int32_t *fb_count = fb_list + ngal;
     double *xloc = p.dep.ptr + off_x;
     double2 *sorted = reinterpret_cast<double2 *>(p.dep.ptr + off_sorted);
     SFB_CUDA_TRY(cudaMemsetAsync(counts, 0, (size_t)nscan * sizeof(int32_t), st));
+    SFB_CUDA_TRY(cudaMemsetAsync(fb_count, 0, sizeof(int32_t), st));
+    const double inv_width = (double)p.pieces / (p.rmax - p.rmin);
     // keys: in nchunks galaxy ranges, each after its event (the host entry's copy pipeline), or at once
     const int nck = (chunk_ready && nchunks > 0) ? nchunks : 1;
     const int64_t per = (ngal + nck - 1) / nck;
@@ -540,11 +603,15 @@ int deposit_sorted(Plan &p, const double *rtp, const double *w, int64_t ngal, do
         const int64_t g0 = c * per, n = std::min<int64_t>(per, ngal - g0);
         if (chunk_ready && nchunks > 0) SFB_CUDA_TRY(cudaStreamWaitEvent(st, chunk_ready[c], 0));
         if (n <= 0) continue;
-        k_deposit_keys<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(rtp + 3 * g0, w ? w + g0 : nullptr, n, p.nside,
-                                                                    p.npix, p.rmin, p.rmax,
-                                                                    (double)p.pieces / (p.rmax - p.rmin), p.pieces,
-                                                                    counts, key + g0,
-                                                                    rank + g0, xloc + g0, p.d_err);
+        k_deposit_keys<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(rtp + 3 * g0, w ? w + g0 : nullptr, n, g0,
+                                                                    p.nside, p.npix, p.rmin, p.rmax, inv_width,
+                                                                    p.pieces, counts, key + g0, rank + g0,
+                                                                    xloc + g0, fb_list, fb_count, p.d_err);
+        note_launch();
+    }
+    if (ngal > 0) {
+        k_deposit_keys_fallback<<<304, 256, 0, st>>>(rtp, p.nside, p.npix, p.rmin, p.rmax, inv_width, p.pieces,
+                                                     counts, key, rank, fb_list, fb_count);
         note_launch();
     }
     k_scan_tiles<<<(unsigned)ntiles, SCAN_THREADS, 0, st>>>(counts, nscan, tsum);

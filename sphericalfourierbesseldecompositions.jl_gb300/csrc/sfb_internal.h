@@ -295,8 +295,9 @@ __device__ __forceinline__ int64_t ang2pix_ring_z(int64_t nside, double z, doubl
 // nside * 4e-6 + 1e-6 leaves a factor 2.5; 1 - |z| is formed as
 // 2 sin^2(theta/2) (or 2 cos^2) to keep its relative accuracy near the
 // poles.  Otherwise the FP64 path runs, so the pixel is bit-identical to
-// ang2pix_ring_z.
-__device__ __forceinline__ int64_t ang2pix_ring_fast(int64_t nside, double th, double ph) {
+// ang2pix_ring_z.  ang2pix_ring_try returns -1 instead of running it (callers
+// that collect those points for a separate FP64 pass).
+__device__ __forceinline__ int64_t ang2pix_ring_try(int64_t nside, double th, double ph) {
     if (nside <= (int64_t(1) << 16) && fabs(ph) <= 4.0 * M_PI) {
         const float ns = (float)nside;
         const float margin = ns * 4e-6f + 1e-6f;
@@ -347,7 +348,12 @@ __device__ __forceinline__ int64_t ang2pix_ring_fast(int64_t nside, double th, d
             }
         }
     }
-    return ang2pix_ring_z(nside, cos(th), ph);
+    return -1;
+}
+
+__device__ __forceinline__ int64_t ang2pix_ring_fast(int64_t nside, double th, double ph) {
+    const int64_t pix = ang2pix_ring_try(nside, th, ph);
+    return pix >= 0 ? pix : ang2pix_ring_z(nside, cos(th), ph);
 }
 
 // Cubic spline with boundary extrapolation on knots x[0..N-1]
