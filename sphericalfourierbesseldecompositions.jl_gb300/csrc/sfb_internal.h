@@ -297,22 +297,23 @@ __device__ __forceinline__ int64_t ang2pix_ring_z(int64_t nside, double z, doubl
 // poles.  Otherwise the FP64 path runs, so the pixel is bit-identical to
 // ang2pix_ring_z.  ang2pix_ring_try returns -1 instead of running it (callers
 // that collect those points for a separate FP64 pass).
-__device__ __forceinline__ int64_t ang2pix_ring_try(int64_t nside, double th, double ph) {
-    if (nside <= (int64_t(1) << 16) && fabs(ph) <= 4.0 * M_PI) {
+// ang2pix_ring_try32 is the FP32 evaluation itself, on th32 = (float)th and
+// ph32 = (float)ph, for callers that checked nside <= 2^16 and |ph| <= 4 pi.
+__device__ __forceinline__ int64_t ang2pix_ring_try32(int64_t nside, float th32, float ph32) {
+    {
         const float ns = (float)nside;
         const float margin = ns * 4e-6f + 1e-6f;
         auto far = [margin](float v) {
             const float f = v - floorf(v);
             return f > margin && f < 1.0f - margin;
         };
-        const float th32 = (float)th;
         float sn, cs;
         sincosf(th32, &sn, &cs);
         const float z = cs, za = fabsf(z);
         // phi in quarter turns, reduced to [0, 4): t - 4 floor(t / 4) rounds exactly as
         // fmodf(t, 4) (+ 4 when negative) does: the subtraction is exact for t >= 0 and a single
         // rounding of t + 4 m otherwise
-        const float t4 = (float)ph * 0.636619772f;
+        const float t4 = ph32 * 0.636619772f;
         const float tt = t4 - 4.0f * floorf(t4 * 0.25f);      // may round to 4: the margin test then falls back
         if (fabsf(za - 0.6666667f) > 1e-5f && far(tt) && tt < 4.0f - margin) {
             if (za < 0.6666667f) {
@@ -348,6 +349,11 @@ __device__ __forceinline__ int64_t ang2pix_ring_try(int64_t nside, double th, do
             }
         }
     }
+    return -1;
+}
+
+__device__ __forceinline__ int64_t ang2pix_ring_try(int64_t nside, double th, double ph) {
+    if (nside <= (int64_t(1) << 16) && fabs(ph) <= 4.0 * M_PI) return ang2pix_ring_try32(nside, (float)th, (float)ph);
     return -1;
 }
 
