@@ -536,82 +536,107 @@ void launch_coef_df(const Plan &p, const int32_t *pair_index, float2 *CT, cudaSt
     note_launch();
 }
 
-// s[pair] = sum_b coef[pair][b] mu_b (FP64): the mean part of every pair.
+// s[pair] = sum_b coef[pair][b] mu_b (FP64): the mean part of every pair, one
+// warp per pair (lanes over b, coalesced rows).
 __global__ void k_mean_proj(const double *__restrict__ coef, int64_t npairs, int64_t nbasis,
                             const double *__restrict__ mu, double *__restrict__ s) {
-    const int64_t pr = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t pr = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (pr >= npairs) return;
     double a = 0.0;
-    for (int64_t b = 0; b < nbasis; ++b) a = fma(coef[pr * nbasis + b], mu[b], a);
-    s[pr] = a;
+    for (int64_t b = lane; b < nbasis; b += 32) a = fma(coef[pr * nbasis + b], mu[b], a);
+    for (int off = 16; off > 0; off >>= 1) a += __shfl_xor_sync(0xffffffffu, a, off);
+    if (lane == 0) s[pr] = a;
 }
 
-// Tiles of the projection: block (l, m0, n0) of the plan's tile list covers
-// m = m0 .. m0 + 63 (thread = m) and n = n0 + 1 .. n0 + 8 (eight accumulators
-// per thread):
+// Tiles of the projection: block (l, m0, n0, npt) of the plan's tile list
+// covers m = m0 .. m0 + 31 (lane = m) and n = n0 + 1 .. n0 + npt (npt <= 8
+// accumulators per thread); its PJ_KS warps split the basis range and add
+// their partial sums at the end:
 //   a_nlm = scale * sum_b coef[n,l][b] dA_b[lm]              (double-float)
 //         + scale * s[pair] * C_lm - w_ln(l, n) * M_lm        (FP64)
-// with dA the fluctuation a_lm (double-float copy, row lm of width ldA),
-// C_lm / M_lm the FP64 a_lm of the count map / the mask (ralm [lm][4]); the
-// mean and window terms are skipped when ralm is null / window_kind is not
-// separable.  The coefficient rows (CT, per (l, b) contiguous in n) and the
-// tile's dA rows are staged in shared memory in chunks of PJ_BK basis
-// functions, so each coefficient is read once per tile, not once per m.
-constexpr int PJ_M = 64, PJ_N = 8, PJ_BK = 32;
+// with dA the fluctuation a_lm (double-float copy, row lm of width ldA, the
+// pairs re, im of basis b side by side), C_lm / M_lm the FP64 a_lm of the
+// count map / the mask (ralm [lm][4]); the mean and window terms are skipped
+// when ralm is null / window_kind is not separable.  The coefficient rows CT
+// (per (l, b) contiguous in n) are read through L1, each load a broadcast to
+// the warp.  The products are formed exactly (TwoProd) and summed with
+// TwoSum into the high word; the low word gathers the rounding errors and the
+// cross terms, unnormalised until the end.
+constexpr int PJ_NPT = 8, PJ_KS = 2;
 
-__global__ void __launch_bounds__(PJ_M) k_project_mixed(const float2 *__restrict__ Adf, int64_t ldA, int64_t nbasis,
-                                                        const float2 *__restrict__ CT, int nmax, int lmax,
-                                                        const int3 *__restrict__ tiles,
-                                                        const int64_t *__restrict__ noff,
-                                                        const int32_t *__restrict__ pair_index, double scale,
-                                                        const double *__restrict__ smean,
-                                                        const double *__restrict__ ralm, int window_kind,
-                                                        const double *__restrict__ w_ln, double *__restrict__ out) {
-    __shared__ float2 cts[PJ_BK][PJ_N];
-    __shared__ float2 as[2 * PJ_BK][PJ_M + 1];       // [2 b + re/im][m], padded against bank conflicts
+struct pacc {
+    float hi, lo;
+};
+
+__device__ __forceinline__ void pj_mac(pacc &a, float2 c, float xh, float xl) {
+    const float p = c.x * xh;
+    const float e = fmaf(c.x, xh, -p);
+    const float s = a.hi + p;
+    const float z = s - a.hi;
+    const float err = (a.hi - (s - z)) + (p - z);
+    a.hi = s;
+    a.lo = fmaf(c.y, xh, fmaf(c.x, xl, (a.lo + err) + e));
+}
+
+__global__ void __launch_bounds__(32 * PJ_KS) k_project_mixed(const float2 *__restrict__ Adf, int64_t ldA,
+                                                              int64_t nbasis, const float2 *__restrict__ CT, int nmax,
+                                                              int lmax, const int3 *__restrict__ tiles,
+                                                              const int64_t *__restrict__ noff,
+                                                              const int32_t *__restrict__ pair_index, double scale,
+                                                              const double *__restrict__ smean,
+                                                              const double *__restrict__ ralm, int window_kind,
+                                                              const double *__restrict__ w_ln,
+                                                              double *__restrict__ out) {
+    __shared__ float4 part[PJ_KS - 1][PJ_NPT][32];
     const int3 t = tiles[blockIdx.x];
-    const int l = t.x, m0 = t.y, n0 = t.z;
-    const int tid = threadIdx.x;
-    const int64_t lm0 = (int64_t)l * (l + 1) / 2 + m0;
-    const int mrows = min(PJ_M, l + 1 - m0);
-    df2 re[PJ_N], im[PJ_N];
+    const int l = t.x, m0 = t.y, n0 = t.z & 0xffff, npt = t.z >> 16;
+    const int lane = threadIdx.x & 31, ks = threadIdx.x >> 5;
+    const int m = m0 + lane;
+    const bool live = m <= l;
+    const int64_t lm = (int64_t)l * (l + 1) / 2 + (live ? m : l);      // lanes past l read a valid row
+    const int64_t kper = (nbasis + PJ_KS - 1) / PJ_KS;
+    const int64_t kb0 = ks * kper, kb1 = kb0 + kper < nbasis ? kb0 + kper : nbasis;
+    const float4 *arow = reinterpret_cast<const float4 *>(Adf + lm * ldA);
+    const float2 *Cl = CT + (int64_t)l * nbasis * nmax + n0;
+    pacc re[PJ_NPT], im[PJ_NPT];
 #pragma unroll
-    for (int j = 0; j < PJ_N; ++j) re[j] = im[j] = df2{0.f, 0.f};
-    const float2 *Cl = CT + (int64_t)l * nbasis * nmax;
-    for (int64_t b0 = 0; b0 < nbasis; b0 += PJ_BK) {
-        __syncthreads();
-        for (int i = tid; i < PJ_BK * PJ_N; i += PJ_M) {
-            const int64_t b = b0 + i / PJ_N;
-            const int n1 = n0 + i % PJ_N;
-            cts[i / PJ_N][i % PJ_N] = (b < nbasis && n1 < nmax) ? Cl[b * nmax + n1] : make_float2(0.f, 0.f);
-        }
-        for (int i = tid; i < PJ_M * 2 * PJ_BK; i += PJ_M) {
-            const int mi = i / (2 * PJ_BK), q = i % (2 * PJ_BK);
-            as[q][mi] = (mi < mrows && b0 + q / 2 < nbasis) ? Adf[(lm0 + mi) * ldA + 2 * b0 + q] : make_float2(0.f, 0.f);
-        }
-        __syncthreads();
-        const int bl_end = (int)(nbasis - b0 < PJ_BK ? nbasis - b0 : PJ_BK);
-        for (int bl = 0; bl < bl_end; ++bl) {
-            const float2 ar = as[2 * bl][tid], ai = as[2 * bl + 1][tid];
+    for (int j = 0; j < PJ_NPT; ++j) re[j] = im[j] = pacc{0.f, 0.f};
+#pragma unroll 2
+    for (int64_t b = kb0; b < kb1; ++b) {
+        const float4 a = arow[b];                 // re.hi, re.lo, im.hi, im.lo
+        const float2 *cb = Cl + b * nmax;
 #pragma unroll
-            for (int j = 0; j < PJ_N; ++j) {
-                const float2 c = cts[bl][j];
-                const df2 cc = {c.x, c.y};
-                re[j] = dfa(re[j], dfm(cc, {ar.x, ar.y}));
-                im[j] = dfa(im[j], dfm(cc, {ai.x, ai.y}));
+        for (int j = 0; j < PJ_NPT; ++j) {
+            if (j < npt) {
+                const float2 c = __ldg(cb + j);
+                pj_mac(re[j], c, a.x, a.y);
+                pj_mac(im[j], c, a.z, a.w);
             }
         }
     }
-    if (tid >= mrows) return;
-    const int64_t lm = lm0 + tid;
+    if (ks > 0) {
 #pragma unroll
-    for (int j = 0; j < PJ_N; ++j) {
+        for (int j = 0; j < PJ_NPT; ++j) part[ks - 1][j][lane] = make_float4(re[j].hi, re[j].lo, im[j].hi, im[j].lo);
+    }
+    __syncthreads();
+    if (ks > 0 || !live) return;
+#pragma unroll
+    for (int j = 0; j < PJ_NPT; ++j) {
         const int n1 = n0 + j;
-        if (n1 >= nmax) break;
+        if (j >= npt) break;
         const int pr = pair_index[(int64_t)n1 * (lmax + 1) + l];
+        double vr = (double)re[j].hi + (double)re[j].lo;
+        double vi = (double)im[j].hi + (double)im[j].lo;
+#pragma unroll
+        for (int q = 0; q < PJ_KS - 1; ++q) {
+            const float4 v = part[q][j][lane];
+            vr += (double)v.x + (double)v.y;
+            vi += (double)v.z + (double)v.w;
+        }
         if (pr < 0) continue;
-        double vr = scale * ((double)re[j].hi + (double)re[j].lo);
-        double vi = scale * ((double)im[j].hi + (double)im[j].lo);
+        vr *= scale;
+        vi *= scale;
         if (ralm) {
             const double mu = scale * smean[pr];
             vr = fma(mu, ralm[4 * lm], vr);
@@ -628,15 +653,17 @@ __global__ void __launch_bounds__(PJ_M) k_project_mixed(const float2 *__restrict
     }
 }
 
-// Tile list of the projection: (l, m0, n0) for m0 = 0, 64, .. <= l and n0 = 0,
-// 8, .. below the number of radial modes of l (the valid n form a prefix).
+// Tile list of the projection: (l, m0, n0 | npt << 16) for m0 = 0, 32, .. <= l
+// and n0 = 0, 8, .. below the number of radial modes of l (the valid n form a
+// prefix), npt = the modes left from n0 (at most 8).
 std::vector<int3> project_tiles(const std::vector<int32_t> &pair_index, int lmax, int nmax) {
     std::vector<int3> t;
     for (int l = 0; l <= lmax; ++l) {
         int nl = 0;
         while (nl < nmax && pair_index[(size_t)nl * (lmax + 1) + l] >= 0) ++nl;
-        for (int m0 = 0; m0 <= l; m0 += PJ_M)
-            for (int n0 = 0; n0 < nl; n0 += PJ_N) t.push_back(make_int3(l, m0, n0));
+        for (int m0 = 0; m0 <= l; m0 += 32)
+            for (int n0 = 0; n0 < nl; n0 += PJ_NPT)
+                t.push_back(make_int3(l, m0, n0 | (std::min(PJ_NPT, nl - n0) << 16)));
     }
     return t;
 }
@@ -646,11 +673,11 @@ void launch_project_mixed(const Plan &p, const float2 *Adf, int64_t ldA, const f
                           double *smean, const double *ralm, int window_kind, const double *w_ln, double *out,
                           cudaStream_t st) {
     if (ralm) {
-        k_mean_proj<<<(unsigned)((p.npairs + 127) / 128), 128, 0, st>>>(p.d_coef, p.npairs, p.nbasis, mu, smean);
+        k_mean_proj<<<(unsigned)((p.npairs + 3) / 4), 128, 0, st>>>(p.d_coef, p.npairs, p.nbasis, mu, smean);
         note_launch();
     }
     if (p.n_proj_tiles <= 0) return;
-    k_project_mixed<<<(unsigned)p.n_proj_tiles, PJ_M, 0, st>>>(Adf, ldA, p.nbasis, CT, (int)p.nmax, p.lmax,
+    k_project_mixed<<<(unsigned)p.n_proj_tiles, 32 * PJ_KS, 0, st>>>(Adf, ldA, p.nbasis, CT, (int)p.nmax, p.lmax,
                                                                p.d_proj_tiles, noff, pair_index, scale, smean, ralm,
                                                                window_kind, w_ln, out);
     note_launch();
