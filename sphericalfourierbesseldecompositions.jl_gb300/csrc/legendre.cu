@@ -463,29 +463,39 @@ __global__ void __launch_bounds__(256) k_fold_alias(const RingGeom *__restrict__
     float2 *Gs = mx + (int64_t)L1 * FC;               // [L1][FC] the ring's G rows
     const int tid = threadIdx.x;
     for (int i = tid; i < L1 * FC; i += 256) mx[i] = make_float2(0.f, 0.f);
+    // a ring's G rows: element i = m * FC + cc at thread tid + 256 q; FOLD_PF loads per thread in
+    // registers, the next ring's issued before this ring's buckets (more rows loop through Gs directly)
+    constexpr int FOLD_PF = 8;
+    float2 gv[FOLD_PF];
+    auto load_ring = [&](int r) {
+#pragma unroll
+        for (int q = 0; q < FOLD_PF; ++q) {
+            const int i = tid + q * 256;
+            const int m = i / FC, cc = i - m * FC;
+            gv[q] = make_float2(0.f, 0.f);
+            if (i < L1 * FC && c0 + cc < ncplx)
+                gv[q] = *reinterpret_cast<const float2 *>(G + ((int64_t)(par * L1 + m) * nrn + r) * ld +
+                                                          2 * (c0 + cc));
+        }
+    };
+    if (r0 < r1) load_ring(r0);
     for (int r = r0; r < r1; ++r) {
         const RingGeom g = rings[r];
         const int n = min(g.nph, nbk);
         const bool odd = g.phi0_den != 0;
         const float f = (float)(w * (double)n * g.cfold);
         __syncthreads();
-        // the ring's G rows into shared memory, eight loads in flight per thread
-        for (int i0 = tid; i0 < L1 * FC; i0 += 8 * 256) {
-            float2 gv[8];
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                const int i = i0 + q * 256;
-                const int m = i / FC, cc = i - m * FC;
-                gv[q] = make_float2(0.f, 0.f);
-                if (i < L1 * FC && c0 + cc < ncplx)
-                    gv[q] = *reinterpret_cast<const float2 *>(G + ((int64_t)(par * L1 + m) * nrn + r) * ld +
-                                                              2 * (c0 + cc));
-            }
-#pragma unroll
-            for (int q = 0; q < 8; ++q)
-                if (i0 + q * 256 < L1 * FC) Gs[i0 + q * 256] = gv[q];
+        for (int q = 0; q < FOLD_PF; ++q)
+            if (tid + q * 256 < L1 * FC) Gs[tid + q * 256] = gv[q];
+        for (int i = tid + FOLD_PF * 256; i < L1 * FC; i += 256) {
+            const int m = i / FC, cc = i - m * FC;
+            Gs[i] = c0 + cc < ncplx ? *reinterpret_cast<const float2 *>(G + ((int64_t)(par * L1 + m) * nrn + r) * ld +
+                                                                       2 * (c0 + cc))
+                                    : make_float2(0.f, 0.f);
         }
         __syncthreads();
+        if (r + 1 < r1) load_ring(r + 1);
         // buckets, each summed by one thread in a fixed order (deterministic)
         for (int i = tid; i < n * FC; i += 256) {
             const int k = i / FC, cc = i - k * FC;

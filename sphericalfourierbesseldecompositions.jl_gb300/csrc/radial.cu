@@ -563,7 +563,7 @@ __global__ void k_mean_proj(const double *__restrict__ coef, int64_t npairs, int
 // the warp.  The products are formed exactly (TwoProd) and summed with
 // TwoSum into the high word; the low word gathers the rounding errors and the
 // cross terms, unnormalised until the end.
-constexpr int PJ_NPT = 8, PJ_KS = 2;
+constexpr int PJ_NPT = 8, PJ_KS = 4;
 
 struct pacc {
     float hi, lo;
@@ -579,7 +579,8 @@ __device__ __forceinline__ void pj_mac(pacc &a, float2 c, float xh, float xl) {
     a.lo = fmaf(c.y, xh, fmaf(c.x, xl, (a.lo + err) + e));
 }
 
-__global__ void __launch_bounds__(32 * PJ_KS) k_project_mixed(const float2 *__restrict__ Adf, int64_t ldA,
+template <int KS>
+__global__ void __launch_bounds__(32 * KS) k_project_mixed(const float2 *__restrict__ Adf, int64_t ldA,
                                                               int64_t nbasis, const float2 *__restrict__ CT, int nmax,
                                                               int lmax, const int3 *__restrict__ tiles,
                                                               const int64_t *__restrict__ noff,
@@ -588,14 +589,14 @@ __global__ void __launch_bounds__(32 * PJ_KS) k_project_mixed(const float2 *__re
                                                               const double *__restrict__ ralm, int window_kind,
                                                               const double *__restrict__ w_ln,
                                                               double *__restrict__ out) {
-    __shared__ float4 part[PJ_KS - 1][PJ_NPT][32];
+    __shared__ float4 part[KS - 1][PJ_NPT][32];
     const int3 t = tiles[blockIdx.x];
     const int l = t.x, m0 = t.y, n0 = t.z & 0xffff, npt = t.z >> 16;
     const int lane = threadIdx.x & 31, ks = threadIdx.x >> 5;
     const int m = m0 + lane;
     const bool live = m <= l;
     const int64_t lm = (int64_t)l * (l + 1) / 2 + (live ? m : l);      // lanes past l read a valid row
-    const int64_t kper = (nbasis + PJ_KS - 1) / PJ_KS;
+    const int64_t kper = (nbasis + KS - 1) / KS;
     const int64_t kb0 = ks * kper, kb1 = kb0 + kper < nbasis ? kb0 + kper : nbasis;
     const float4 *arow = reinterpret_cast<const float4 *>(Adf + lm * ldA);
     const float2 *Cl = CT + (int64_t)l * nbasis * nmax + n0;
@@ -629,7 +630,7 @@ __global__ void __launch_bounds__(32 * PJ_KS) k_project_mixed(const float2 *__re
         double vr = (double)re[j].hi + (double)re[j].lo;
         double vi = (double)im[j].hi + (double)im[j].lo;
 #pragma unroll
-        for (int q = 0; q < PJ_KS - 1; ++q) {
+        for (int q = 0; q < KS - 1; ++q) {
             const float4 v = part[q][j][lane];
             vr += (double)v.x + (double)v.y;
             vi += (double)v.z + (double)v.w;
@@ -677,9 +678,9 @@ void launch_project_mixed(const Plan &p, const float2 *Adf, int64_t ldA, const f
         note_launch();
     }
     if (p.n_proj_tiles <= 0) return;
-    k_project_mixed<<<(unsigned)p.n_proj_tiles, 32 * PJ_KS, 0, st>>>(Adf, ldA, p.nbasis, CT, (int)p.nmax, p.lmax,
-                                                               p.d_proj_tiles, noff, pair_index, scale, smean, ralm,
-                                                               window_kind, w_ln, out);
+    k_project_mixed<PJ_KS><<<(unsigned)p.n_proj_tiles, 32 * PJ_KS, 0, st>>>(
+        Adf, ldA, p.nbasis, CT, (int)p.nmax, p.lmax, p.d_proj_tiles, noff, pair_index, scale, smean, ralm, window_kind,
+        w_ln, out);
     note_launch();
 }
 
