@@ -422,13 +422,15 @@ __global__ void k_deposit_moments(const int32_t *__restrict__ offset, const doub
 
 // One step of the basis recurrence on q_k = w P_k(x):
 // (k+1) q_{k+1} = (2k+1) x q_k - k q_{k-1}, the ratios as double-float
-// constants; products and the sum unnormalised, q_{k+1} renormalised.
+// constants, every operation unnormalised: where the sum cancels, lo keeps
+// its absolute accuracy (~2^-46 of the terms), which is all the moments need
+// before their FP32 store.
 template <int K>
 __device__ __forceinline__ dfl leg_step(dfl x, dfl q1, dfl q0) {
     constexpr double C1 = (double)(2 * K + 1) / (K + 1), C2 = -(double)K / (K + 1);
     constexpr float C1H = (float)C1, C2H = (float)C2;
     constexpr float C1L = (float)(C1 - (double)C1H), C2L = (float)(C2 - (double)C2H);
-    return df_renorm(dfs_add(dfs_mul({C1H, C1L}, dfs_mul(x, q1)), dfs_mul({C2H, C2L}, q0)));
+    return dfs_add(dfs_mul({C1H, C1L}, dfs_mul(x, q1)), dfs_mul({C2H, C2L}, q0));
 }
 
 // acc[k+1] += q_{k+1} for K <= k < min(deg, MAXDEG), q0 = q_{K-1}, q1 = q_K
@@ -455,7 +457,7 @@ __device__ __forceinline__ void bin_moments_df(const float4 *__restrict__ sorted
         const float4 v = nxt;
         if (g + 1 < g1) nxt = sorted[g + 1];
         const dfl x = {v.x, v.y};
-        dfl q0 = {v.z, v.w}, q1 = df_renorm(dfs_mul(q0, x));
+        dfl q0 = {v.z, v.w}, q1 = dfs_mul(q0, x);
         acc[0] = dfs_add(acc[0], q0);
         if (MAXDEG >= 1) acc[1] = dfs_add(acc[1], q1);
         leg_chain<1, MAXDEG>(x, q0, q1, acc, deg);
@@ -483,7 +485,7 @@ __global__ void k_deposit_moments_df(const int32_t *__restrict__ offset, const f
     auto fluct = [&](dfl a, int64_t b) -> float {
         if (cdf) {
             const float2 m = mudf[b];
-            a = df_add(a, df_neg(df_mul({m.x, m.y}, rv)));
+            a = dfs_add(a, df_neg(dfs_mul({m.x, m.y}, rv)));
         }
         return a.hi + a.lo;
     };
@@ -530,6 +532,24 @@ __global__ void __launch_bounds__(128) k_deposit_moments_bal(const int32_t *__re
     const int64_t bnd = (int64_t)(slot0 + 1) * npix;
     const int64_t bt = B0 + t;
     const int cnt = bt < nkeys ? offset[bt + 1] - offset[bt] : 0;
+    // blocks of empty bins on pixels where the reference map is zero (outside the survey) write zeros
+    bool busy = cnt != 0;
+    if (cdf && bt < nkeys) {
+        const int sl = bt < bnd ? slot0 : slot0 + 1;
+        busy = busy || cdf[bt - (int64_t)sl * npix].x != 0.f;
+    }
+    if (!__syncthreads_or(busy)) {
+        if (bt >= nkeys) return;
+        const int sl = bt < bnd ? slot0 : slot0 + 1;
+        const int64_t px = bt - (int64_t)sl * npix;
+        if (sl >= pieces) {
+            maps[(nbasis - 2 + (sl - pieces)) * npix + px] = 0.f;
+            return;
+        }
+        float *z = maps + (int64_t)sl * (deg + 1) * npix + px;
+        for (int k = 0; k <= deg; ++k) z[(int64_t)k * npix] = 0.f;
+        return;
+    }
     if (t < 64) hist[t] = 0;
     __syncthreads();
     const int key = 63 - min(cnt, 63);                 // longest bins first
@@ -560,7 +580,7 @@ __global__ void __launch_bounds__(128) k_deposit_moments_bal(const int32_t *__re
         auto fluct = [&](dfl a, int64_t bi) -> float {
             if (cdf) {
                 const float2 m = mudf[bi];
-                a = df_add(a, df_neg(df_mul({m.x, m.y}, rv)));
+                a = dfs_add(a, df_neg(dfs_mul({m.x, m.y}, rv)));
             }
             return a.hi + a.lo;
         };
