@@ -229,7 +229,8 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_analysis_tc(const __nv_bfloat16 
                                                             int nchunks, int rlim, const float *__restrict__ F,
                                                             int64_t ncol, const int *__restrict__ Ecol,
                                                             double *__restrict__ A, float2 *__restrict__ Adf,
-                                                            int accumulate, int *__restrict__ Eout, int *err) {
+                                                            int accumulate, int *__restrict__ Eout,
+                                                            const int *__restrict__ nzr, int *err) {
     extern __shared__ __align__(1024) unsigned char smem[];
     const int z = blockIdx.z;
     const int m = z >> 1, par = z & 1;
@@ -243,8 +244,21 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_analysis_tc(const __nv_bfloat16 
     const int c = tid & (MTILE - 1), kh = (tid >> 7) & 1;
     const bool prod = tid < NPROD;
     const bool cok = prod && col0 + c < ncol;
-    const float *Fz = F + ((int64_t)(par * (lmax + 1) + m) * nrn) * ncol + col0 + c;
-    const __nv_bfloat16 *Lz = lamtc + lamtc_off[z];
+    // nzr: the ring pairs outside [nzr[0], nzr[1]] carry zero spectra, and the chunks holding only
+    // such rings are left out (at least one chunk stays, so the accumulators are written)
+    int kc0 = 0;
+    if (nzr) {
+        const int lo = nzr[0], hi = nzr[1];
+        if (hi >= lo) {
+            kc0 = lo / KC;
+            nchunks = min(nchunks, hi / KC + 1) - kc0;
+        } else {
+            nchunks = 1;
+        }
+    }
+    const float *Fz = F + ((int64_t)(par * (lmax + 1) + m) * nrn + (int64_t)kc0 * KC) * ncol + col0 + c;
+    const __nv_bfloat16 *Lz = lamtc + lamtc_off[z] + (int64_t)kc0 * 4 * pad16(rows_of(m, par, lmax)) * KC;
+    rlim -= kc0 * KC;
     const uint32_t planeB = (uint32_t)NPc * KC * 2;
     LvlSmem cs = lvl_smem(smem);
     float C[4];
@@ -701,7 +715,8 @@ void launch_build_lamtc(const Plan &p, const int *Ea, const int *Es, cudaStream_
 }
 
 void launch_leg_analysis_tc(const Plan &p, const float *F, int64_t ncol, double *A, float2 *Adf, int *Ecol,
-                            bool accumulate, cudaStream_t st, bool scales_ready, int rlim, int *Eout) {
+                            bool accumulate, cudaStream_t st, bool scales_ready, int rlim, int *Eout,
+                            const int *nzr) {
     if (rlim < 0 || rlim > p.nrn) rlim = (int)p.nrn;
     if (!scales_ready) {
         dim3 grid((unsigned)((ncol + 255) / 256), (unsigned)(2 * (p.lmax + 1)));
@@ -714,7 +729,7 @@ void launch_leg_analysis_tc(const Plan &p, const float *F, int64_t ncol, double 
     tc::k_leg_analysis_tc<<<grid, tc::NTH, tc::LEG_SMEM, st>>>((const __nv_bfloat16 *)p.d_lamtc, p.d_lamtc_off,
                                                               p.lmax, (int)p.nrn, (rlim + tc::KC - 1) / tc::KC, rlim,
                                                               F, ncol, Ecol, A, Adf, accumulate ? 1 : 0, Eout,
-                                                              p.d_err);
+                                                              nzr, p.d_err);
     note_launch();
 }
 

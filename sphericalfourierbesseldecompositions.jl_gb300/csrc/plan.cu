@@ -333,13 +333,16 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, b
         SFB_TRY(grow(p, gbuf, fsz));
         SFB_TRY(grow(p, rbuf, fsz));
     }
+    // the non-zero ring-pair range of the DFT input, in the two ints past both scale arrays
+    int *nzr = nullptr;
     if (p.precision == SFB_MIXED) {
         // row scales of the ring DFT, then column scales of the Legendre analysis (ints)
         SFB_TRY(grow(p, p.erow, (size_t)std::max<int64_t>(p.nrn * nm, (p.lmax + 1) * ncol) + 1));
         SFB_TRY(grow(p, p.almdf, (size_t)p.lmsize * ncol));
+        nzr = reinterpret_cast<int *>(p.erow.ptr) + 2 * std::max<int64_t>(p.nrn * nm, (p.lmax + 1) * ncol);
         Stage s(h, stage(SFB_STAGE_RING_FFT), st);
         launch_ring_analysis_tc(p, reinterpret_cast<const float *>(maps), nm, reinterpret_cast<float *>(fbuf.ptr),
-                                reinterpret_cast<int *>(p.erow.ptr), st);
+                                reinterpret_cast<int *>(p.erow.ptr), nzr, st);
     } else {
         Stage s(h, stage(SFB_STAGE_RING_FFT), st);
         launch_ring_analysis(p, maps, nm, fbuf.ptr, st);
@@ -350,7 +353,9 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, b
     auto analysis = [&](const double *src, bool acc) {
         Stage s(h, stage(SFB_STAGE_LEG_ANALYSIS), st);
         // after the first pass the fold has written the column scales of its residual
-        if (tc) launch_leg_analysis_tc(p, (const float *)src, ncol, alm.ptr, adf, ecol, acc, st, acc);
+        // the first pass reads the DFT output, zero outside the non-zero ring range
+        if (tc) launch_leg_analysis_tc(p, (const float *)src, ncol, alm.ptr, adf, ecol, acc, st, acc, -1, nullptr,
+                                       acc ? nullptr : nzr);
         else launch_leg_analysis(p, src, ncol, alm.ptr, acc, st);
     };
     if (tc && ncol / 2 > 4 && p.d_gramts && p.niter > 0) {
@@ -373,7 +378,7 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, b
         {
             Stage s(h, stage(SFB_STAGE_LEG_ANALYSIS), st);
             launch_leg_analysis_tc(p, (const float *)fbuf.ptr, ncol, Ab[cur], Db[cur], ecol, false, st, false, -1,
-                                   Eb[cur]);
+                                   Eb[cur], nzr);
         }
         SFB_CUDA_TRY(cudaMemcpyAsync(p.adf0.ptr, Db[cur], (size_t)p.lmsize * ncol * sizeof(float2),
                                      cudaMemcpyDeviceToDevice, st));

@@ -46,6 +46,7 @@ namespace dft {
 
 using namespace tc;
 
+constexpr int ZERO_ROW_E = -127;  // row exponent of an all-zero ring row
 constexpr int KC = 32;            // pixels per chunk
 constexpr int NPAIR = 64;         // (ring, map) pairs per CTA
 constexpr int NROW = 128;         // A rows (MMA M): pairs x {north, south}
@@ -76,30 +77,48 @@ __device__ __forceinline__ void st_shared_v4(unsigned char *p, const uint32_t (&
     *reinterpret_cast<uint4 *>(p) = make_uint4(v[0], v[1], v[2], v[3]);
 }
 
-// Per (hemisphere, ring, map): E with max |x| < 2^E over the ring (0 for an
-// all-zero or empty row), raised by ceil(log2 n) - 10 for rings longer than
-// 1024 pixels so that the leading products still sum below 2^23 units.
-// erow layout [2][nrn][nmaps].
+// Per (hemisphere, ring, map): E with max |x| < 2^E over the ring, raised by
+// ceil(log2 n) - 10 for rings longer than 1024 pixels so that the leading
+// products still sum below 2^23 units; ZERO_ROW_E for a row of zeros (a ring
+// outside the survey), whose tiles the DFT skips.  A row holding a
+// non-finite value keeps an ordinary exponent, so the value reaches the
+// spectra and the transform's finiteness check.  erow layout [2][nrn][nmaps];
+// nzr[0] / nzr[1] get the first / last ring pair with a non-zero row (preset
+// to a large value / -1).
 __global__ void __launch_bounds__(128) k_ring_rowexp(const float *__restrict__ maps, int64_t npix, int64_t nmaps,
-                                                     const RingGeom *__restrict__ rings, int nrn, int *erow) {
+                                                     const RingGeom *__restrict__ rings, int nrn, int *erow,
+                                                     int *nzr) {
     const int r = blockIdx.x;
     const int64_t b = (int64_t)blockIdx.y * 4 + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     if (b >= nmaps) return;
     const RingGeom g = rings[r];
+    bool any = false;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
         const float *x = maps + b * npix + (h ? g.start_s : g.start_n);
         float mx = 0.f;
-        for (int j = lane; j < g.nph; j += 32) mx = fmaxf(mx, fabsf(x[j]));
+        bool fin = true;
+        for (int j = lane; j < g.nph; j += 32) {
+            const float v = x[j];
+            fin = fin && isfinite(v);
+            mx = fmaxf(mx, fabsf(v));
+        }
         for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+        fin = __all_sync(0xffffffffu, fin);
         if (lane == 0) {
             int E = scale_exp(mx);
             const int lg = 32 - __clz(g.nph - 1);          // ceil(log2 n)
             E += max(0, lg - 10);
             E = max(-90, min(E, 100));
+            if (mx == 0.f && fin) E = ZERO_ROW_E;
+            else any = true;
             erow[((int64_t)h * nrn + r) * nmaps + b] = E;
         }
+    }
+    if (lane == 0 && any) {
+        atomicMin(nzr, r);
+        atomicMax(nzr + 1, r);
     }
 }
 
@@ -161,9 +180,23 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
     const RingGeom g = rings[ring];
     const bool live = abuild && rok && (hemi == 0 || g.start_s != g.start_n);   // the equator has no south row
     const float *x = maps + b * npix + (hemi ? g.start_s : g.start_n);
-    const int E = rok ? erow[((int64_t)hemi * nrn + ring) * nmaps + b] : 0;
+    const int E = rok ? erow[((int64_t)hemi * nrn + ring) * nmaps + b] : ZERO_ROW_E;
     float C[4];
-    slice_consts(E, C);
+    slice_consts(E == ZERO_ROW_E ? 0 : E, C);
+    const int L1 = lmax + 1;
+    // a tile of zero rows (rings outside the survey) has zero spectra: written without MMAs
+    if (!__syncthreads_or(live && E != ZERO_ROW_E)) {
+        for (int i = tid; i < 2 * 64 * NPAIR; i += NTHR) {
+            const int pr = i & (NPAIR - 1), mo = (i / NPAIR) & 63, sg = i / (64 * NPAIR);
+            const int mm = 64 * u + mo;
+            const int64_t qo = pair0 + pr;
+            if (mm > lmax || qo >= npairs) continue;
+            const int oring = cls_rings[rb + (int)(qo / nmaps)];
+            *reinterpret_cast<float2 *>(F + ((int64_t)(sg * L1 + mm) * nrn + oring) * ldF + 2 * (qo % nmaps)) =
+                make_float2(0.f, 0.f);
+        }
+        return;
+    }
 
     // B row ti (gather variant): column c = ti -> m = 64 u + c/2, part c&1 (0: cos, 1: -sin)
     const int m = 64 * u + (ti >> 1);
@@ -330,7 +363,6 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
         float *xch = reinterpret_cast<float *>(smem);      // [2 halves][16 columns][lead, rest][128 rows]
         const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
         const int half = tid >> 7;
-        const int L1 = lmax + 1;
         const int pr = ti & (NPAIR - 1);
         const int sg = ti >> 6;
         const float sgn = sg ? -1.0f : 1.0f;
@@ -482,10 +514,14 @@ uint2 dft_slices(double v, int EB) {
     return make_uint2((uint32_t)s[0] | ((uint32_t)s[1] << 16), (uint32_t)s[2] | ((uint32_t)s[3] << 16));
 }
 
-void launch_ring_analysis_tc(const Plan &p, const float *maps, int64_t nmaps, float *F, int *erow, cudaStream_t st) {
+void launch_ring_analysis_tc(const Plan &p, const float *maps, int64_t nmaps, float *F, int *erow, int *nzr,
+                             cudaStream_t st) {
     {
+        // nzr[0] = 0x7f7f7f7f (above any ring index), nzr[1] = -1
+        cudaMemsetAsync(nzr, 0x7f, sizeof(int), st);
+        cudaMemsetAsync(nzr + 1, 0xff, sizeof(int), st);
         dim3 grid((unsigned)p.nrn, (unsigned)((nmaps + 3) / 4));
-        dft::k_ring_rowexp<<<grid, 128, 0, st>>>(maps, p.npix, nmaps, p.d_rings, (int)p.nrn, erow);
+        dft::k_ring_rowexp<<<grid, 128, 0, st>>>(maps, p.npix, nmaps, p.d_rings, (int)p.nrn, erow, nzr);
         note_launch();
     }
     set_smem(dft::k_ring_dft_tc<true>, dft::SMEM);

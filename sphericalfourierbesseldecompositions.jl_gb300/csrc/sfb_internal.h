@@ -205,7 +205,9 @@ void launch_project_poly(const Plan &p, const double *A, int64_t ldA, double sca
                          double *out, cudaStream_t st);
 void launch_to_float(const double *in, int64_t n, float *out, cudaStream_t st);
 // Mixed-precision ring analysis on the tensor cores (FP32 maps -> FP32 F).
-void launch_ring_analysis_tc(const Plan &p, const float *maps, int64_t nmaps, float *F, int *erow, cudaStream_t st);
+// nzr[0..1] receives the first and last ring pair holding a non-zero map row.
+void launch_ring_analysis_tc(const Plan &p, const float *maps, int64_t nmaps, float *F, int *erow, int *nzr,
+                             cudaStream_t st);
 uint2 dft_slices(double v, int EB);
 int64_t dft_image_offsets(const Plan &p, const std::vector<int32_t> &crings, const std::vector<int32_t> &coff,
                           bool with_polar, std::vector<int64_t> &off, int &max_nch);
@@ -216,9 +218,10 @@ void launch_build_lamtc(const Plan &p, const int *Ea, const int *Es, cudaStream_
 // Ecol: column scales of F; computed here unless scales_ready (the fold wrote them).
 // rlim: the sum runs over the first rlim rings only (-1: all).
 // Eout (optional): atomicMax of each output column's exponent per block z (preset below every exponent).
+// nzr (optional, device): F is zero on the ring pairs outside [nzr[0], nzr[1]]; the sum skips them.
 void launch_leg_analysis_tc(const Plan &p, const float *F, int64_t ncol, double *A, float2 *Adf, int *Ecol,
                             bool accumulate, cudaStream_t st, bool scales_ready = false, int rlim = -1,
-                            int *Eout = nullptr);
+                            int *Eout = nullptr, const int *nzr = nullptr);
 int64_t tc_synth_table_offsets(const Plan &p, std::vector<int64_t> &off, int64_t nrn = -1);
 void launch_build_lamts(const Plan &p, const int *Es, cudaStream_t st);
 // rlim: ring tiles covering the first rlim rings only (-1: all)

@@ -79,6 +79,32 @@ def test_mixed_vs_fp64(cfg, kind):
     assert e2 < MIXED_TOL and emax < MIXED_TOL
 
 
+@pytest.mark.parametrize("zlim", [(-0.3, 0.3), (-1.0, -0.4)])
+def test_mixed_vs_fp64_partial_sky(zlim):
+    """Surveys that leave rings empty at the start of the ring range (a band
+    |z| < 0.3) or in the north (a southern cap): the ring DFT skips tiles of
+    zero rows and the first analysis pass skips the zero ring chunks, which
+    must leave the a_nlm unchanged."""
+    z0, z1 = zlim
+    a = sfbgpu.AnlmModes(0.05, 500.0, 1000.0, nside=32)
+    rng = np.random.default_rng(12)
+    n = 150_000
+    r = np.cbrt(rng.uniform(a.rmin ** 3, a.rmax ** 3, n))
+    rtp = np.stack([r, np.arccos(rng.uniform(z0, z1, n)), rng.uniform(0, 2 * np.pi, n)])
+    w = rng.uniform(0.5, 1.5, n)
+    wm = sfbgpu.ConfigurationSpaceModes(a.rmin, a.rmax, 100, a.nside)
+    th, _ = sfbgpu.pix2ang_ring(a.nside, np.arange(wm.npix))
+    mask = ((np.cos(th) > z0) & (np.cos(th) < z1)).astype(float)
+    phi = np.ones(wm.nr)
+    win = sfbgpu.win_rhat_ln(sfbgpu.SeparableArray(phi, mask, "phi", "mask"), wm, a)
+    nbar = n / sfbgpu.integrate_window(sfbgpu.SeparableArray(phi, mask), wm)
+    f64 = sfbgpu.cat2amln(rtp, a, nbar, win, w, precision="fp64")
+    mix = sfbgpu.cat2amln(rtp, a, nbar, win, w, precision="mixed")
+    e2, emax = _errors(mix, f64)
+    record(f"mixed_vs_fp64_partial_sky_z{z0}_{z1}", e2, maxnorm=emax)
+    assert e2 < MIXED_TOL and emax < 10 * MIXED_TOL
+
+
 def test_dft_twiddle_image_matches_gather(monkeypatch):
     """The ring DFT takes its twiddle operand from the precomputed image, or,
     for polar rings past the image budget, gathers it from the ring tables:
