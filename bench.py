@@ -215,7 +215,43 @@ def gram_geometry(lmax, niter=3):
     return ral, on
 
 
-def stage_work(stage, precision, nm, ngal, nbasis, niter=3, lmax=238):
+def sky_rings(sfbgpu, nside, theta, phi):
+    """Ring pairs (north ring i and its mirror 4 nside - i, 0-based pair
+    i - 1) that hold galaxies: (pixels on those pairs, number of rings in the
+    span from the first to the last such pair).  Outside them every map of the
+    mixed path is zero: the ring DFT skips those rows and the first analysis
+    pass sums over the span only, so the algorithmic work below is counted
+    over the same rings."""
+    ns = int(nside)
+    npix = 12 * ns * ns
+    ncap = 2 * ns * (ns - 1)
+    p = np.arange(npix, dtype=np.int64)
+
+    def cap_ring(q):
+        i = (1 + np.floor(np.sqrt(1 + 2 * q)).astype(np.int64)) >> 1
+        i = np.where(2 * i * (i - 1) > q, i - 1, i)
+        return np.where(2 * (i + 1) * i <= q, i + 1, i)
+
+    ring = np.empty(npix, np.int64)
+    north, south = p < ncap, p >= npix - ncap
+    eq = ~(north | south)
+    ring[north] = cap_ring(p[north])
+    ring[eq] = (p[eq] - ncap) // (4 * ns) + ns
+    ring[south] = 4 * ns - cap_ring(npix - 1 - p[south])
+    pair = np.minimum(ring, 4 * ns - ring) - 1
+    pix_per_pair = np.bincount(pair, minlength=2 * ns)
+    gp = sfbgpu.ang2pix_ring(ns, theta, phi)
+    used = np.zeros(2 * ns, bool)
+    used[np.unique(pair[gp])] = True
+    idx = np.nonzero(used)[0]
+    if idx.size == 0:
+        return 0, 0
+    lo, hi = int(idx[0]), int(idx[-1])
+    rings = 2 * (hi - lo + 1) - (1 if hi == 2 * ns - 1 else 0)
+    return int(pix_per_pair[used].sum()), rings
+
+
+def stage_work(stage, precision, nm, ngal, nbasis, niter=3, lmax=238, sky=None):
     """Algorithmic work of ONE STEP of a stage as this path computes it:
     (kind, amount).  The N/S ring symmetry and the ten-product slicing are
     implementation choices and do not change the counts.
@@ -230,6 +266,9 @@ def stage_work(stage, precision, nm, ngal, nbasis, niter=3, lmax=238):
     ring_fft: maps read + ring spectra written, nm npix b + nm n_ring (lmax+1)
     2 b bytes (b = 4 mixed, 8 FP64); the mixed path computes it as a
     tensor-core DFT, whose 4 flop per (pixel, m, map) is reported beside.
+    sky = sky_rings(...): in the mixed path the DFT flops count the pixels of
+    the ring pairs with galaxies and the first analysis pass the rings of
+    their span (the rows elsewhere are zero and skipped).
     fold: G read + R written per pass (mixed: the aliased rings only; FP64:
     F, G read + R written over all rings).  deposit: 40 B per galaxy (record
     read + binning update) + the basis maps written."""
@@ -247,7 +286,8 @@ def stage_work(stage, precision, nm, ngal, nbasis, niter=3, lmax=238):
     gram_flop = 4.0 * nm * sum(r * r for r in rows)
     if stage == "leg_analysis":
         if gram:
-            return ("flop", 4.0 * n_ring * lmsize * nm + niter * 4.0 * n_al * lmsize * nm)
+            first = sky[1] if (sky and precision == "mixed") else n_ring
+            return ("flop", 4.0 * first * lmsize * nm + niter * 4.0 * n_al * lmsize * nm)
         return ("flop", (1 + niter) * 4.0 * n_ring * lmsize * nm)
     if stage == "leg_synthesis":
         if gram:
@@ -264,7 +304,7 @@ def stage_work(stage, precision, nm, ngal, nbasis, niter=3, lmax=238):
     return ("byte", None)
 
 
-def roofline_table(stages, precision, nm, ngal, nbasis, peaks, fp64_peak):
+def roofline_table(stages, precision, nm, ngal, nbasis, peaks, fp64_peak, sky=None):
     """Per stage: algorithmic work of a step / the stage's time in the step.
     Tensor-core stages of the mixed path issue 10 BF16 products per
     algorithmic multiply-add (four-slice error-free splitting); `achieved`
@@ -272,7 +312,7 @@ def roofline_table(stages, precision, nm, ngal, nbasis, peaks, fp64_peak):
     out = {}
     for st, v in stages.items():
         ms = v["ms_per_step"]
-        kind, amount = stage_work(st, precision, nm, ngal, nbasis)
+        kind, amount = stage_work(st, precision, nm, ngal, nbasis, sky=sky)
         if amount is None or ms <= 0:
             continue
         if kind == "flop":
@@ -300,7 +340,8 @@ def roofline_table(stages, precision, nm, ngal, nbasis, peaks, fp64_peak):
                 # the mixed ring transform is a tensor-core DFT: its bound is the tensor pipe (fed from
                 # shared memory), so it is reported as such, with the HBM bytes beside
                 lmax = 238
-                dft = 4.0 * nm * 12 * NSIDE ** 2 * (lmax + 1)
+                dpix = sky[0] if sky else 12 * NSIDE ** 2
+                dft = 4.0 * nm * dpix * (lmax + 1)
                 tp = peaks.get("bf16_tflops_sustained", 1700.0)
                 tach = dft / (ms * 1e-3) / 1e12
                 hbm_view = {k: out[st][k] for k in ("achieved", "peak", "unit", "frac", "per_step")}
@@ -308,7 +349,8 @@ def roofline_table(stages, precision, nm, ngal, nbasis, peaks, fp64_peak):
                            "per_step": dft, "ms_per_step": ms,
                            "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained" if "bf16_tflops_sustained"
                            in peaks else "fallback (sustained bf16)",
-                           "bf16_issued_frac": 10 * tach / tp, "hbm_view": hbm_view}
+                           "bf16_issued_frac": 10 * tach / tp, "hbm_view": hbm_view,
+                           "dft_pixels": dpix, "dft_pixels_frac": dpix / (12 * NSIDE ** 2)}
     return out
 
 
@@ -541,7 +583,8 @@ def main():
     except OSError:
         pass
     fp64_peak = fp64_gemm_peak(torch) if args.precision == "fp64" else None
-    table = roofline_table(stages, args.precision, nm, N, info["nbasis"], peaks, fp64_peak)
+    sky = sky_rings(sfbgpu, NSIDE, gal[:, 1], gal[:, 2]) if args.precision == "mixed" else None
+    table = roofline_table(stages, args.precision, nm, N, info["nbasis"], peaks, fp64_peak, sky)
     dom = max(table, key=lambda k: stages[k]["ms_per_step"])
     roof = dict(table[dom])
     roof["kernel_stage"] = dom

@@ -521,7 +521,8 @@ __global__ void __launch_bounds__(128) k_deposit_moments_bal(const int32_t *__re
                                                              int pieces, int deg, int64_t nbasis,
                                                              const float2 *__restrict__ cdf,
                                                              const float2 *__restrict__ mudf,
-                                                             float *__restrict__ maps) {
+                                                             float *__restrict__ maps, int64_t nside,
+                                                             const int *__restrict__ ring_live) {
     __shared__ int hist[64];
     __shared__ int perm[128];
     __shared__ float out[(MAXDEG + 1) * 128];
@@ -542,6 +543,8 @@ __global__ void __launch_bounds__(128) k_deposit_moments_bal(const int32_t *__re
         if (bt >= nkeys) return;
         const int sl = bt < bnd ? slot0 : slot0 + 1;
         const int64_t px = bt - (int64_t)sl * npix;
+        // rings without galaxies are not written at all (their readers treat them as zero)
+        if (ring_live && !ring_live[ring_of_pixel(nside, px)]) return;
         if (sl >= pieces) {
             maps[(nbasis - 2 + (sl - pieces)) * npix + px] = 0.f;
             return;
@@ -686,33 +689,40 @@ __global__ void k_mean_finalize(const double *S, const double *Q, int pieces, in
 // Weighted galaxy count per pixel over all radial slots (the reference map of
 // the mixed deposit), in double-float from the sorted pairs, stored as the
 // FP64 value hi + lo (exact) and as the pair itself.
+// ring_live[ring] is set to 1 for every ring holding a galaxy (preset to 0).
 __global__ void k_weight_map_mixed(const int32_t *__restrict__ offset, const float4 *__restrict__ sorted,
-                                   int64_t npix, int nslots, double *__restrict__ C, float2 *__restrict__ cdf) {
+                                   int64_t nside, int64_t npix, int nslots, double *__restrict__ C,
+                                   float2 *__restrict__ cdf, int *__restrict__ ring_live) {
     const int64_t pix = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (pix >= npix) return;
     dfl s = {0.f, 0.f};
+    bool any = false;
     for (int sl = 0; sl < nslots; ++sl) {
         const int64_t k = (int64_t)sl * npix + pix;
-        for (int64_t g = offset[k]; g < offset[k + 1]; ++g) {
+        const int64_t g0 = offset[k], g1 = offset[k + 1];
+        any = any || g1 > g0;
+        for (int64_t g = g0; g < g1; ++g) {
             const float4 v = sorted[g];
             s = df_add(s, {v.z, v.w});
         }
     }
     C[pix] = (double)s.hi + (double)s.lo;
     cdf[pix] = make_float2(s.hi, s.lo);
+    if (any) ring_live[ring_of_pixel(nside, pix)] = 1;
 }
 
 // FP64 path: double (x, w); mixed: double-float pairs and the count map as cdf
 template <int MAXDEG>
 static void launch_moments(const Plan &p, const int32_t *counts, const void *sorted, const double *ref,
-                           const double *mu, const float2 *cdf, const float2 *mudf, double *maps, cudaStream_t st) {
+                           const double *mu, const float2 *cdf, const float2 *mudf, double *maps, cudaStream_t st,
+                           const int *ring_live) {
     const int64_t nkeys = (int64_t)(p.pieces + 2) * p.npix;
     const unsigned blocks = (unsigned)((nkeys + 127) / 128);
     const float4 *s4 = static_cast<const float4 *>(sorted);
     float *mf = reinterpret_cast<float *>(maps);
     if (p.precision == SFB_MIXED && MAXDEG <= 31 && p.npix >= 128)
         k_deposit_moments_bal<MAXDEG><<<blocks, 128, 0, st>>>(counts, s4, p.npix, p.pieces, p.degree, p.nbasis, cdf,
-                                                              mudf, mf);
+                                                              mudf, mf, p.nside, ring_live);
     else if (p.precision == SFB_MIXED)
         k_deposit_moments_df<MAXDEG><<<blocks, 128, 0, st>>>(counts, s4, p.npix, p.pieces, p.degree, p.nbasis, cdf,
                                                              mudf, mf);
@@ -744,8 +754,9 @@ static void by_degree(int deg, F &&f) {
 
 int deposit_sorted(Plan &p, const double *rtp, const double *w, int64_t ngal, double *maps, double *ref,
                    double *mu, cudaEvent_t ref_ready, cudaStream_t st, const cudaEvent_t *chunk_ready,
-                   int nchunks) {
+                   int nchunks, const int **ring_live) {
     const bool mixed = p.precision == SFB_MIXED;
+    if (ring_live) *ring_live = nullptr;
     const int64_t nkeys = (int64_t)(p.pieces + 2) * p.npix;
     const int64_t nscan = nkeys + 1;            // one extra counter: its exclusive prefix is the total
     const int64_t ntiles = (nscan + SCAN_TILE - 1) / SCAN_TILE;
@@ -758,7 +769,9 @@ int deposit_sorted(Plan &p, const double *rtp, const double *w, int64_t ngal, do
     off_sorted += off_sorted & 1;
     const int64_t off_stats = off_sorted + 2 * ngal + 2;
     const int64_t off_cdf = off_stats + 2 * p.nbasis + p.pieces + 2;
-    SFB_TRY(grow(p, p.dep, (size_t)(off_cdf + p.npix)));
+    const int64_t nrings = 4 * p.nside - 1;
+    const int64_t off_live = off_cdf + p.npix;               // ring_live [nrings] int
+    SFB_TRY(grow(p, p.dep, (size_t)(off_live + (nrings + 1) / 2)));
     int32_t *counts = reinterpret_cast<int32_t *>(p.dep.ptr);
     int32_t *tsum = counts + nscan;
     int32_t *key = tsum + ntiles;
@@ -770,6 +783,7 @@ int deposit_sorted(Plan &p, const double *rtp, const double *w, int64_t ngal, do
     void *sorted = p.dep.ptr + off_sorted;
     float4 *sorted4 = static_cast<float4 *>(sorted);
     float2 *cdf = reinterpret_cast<float2 *>(p.dep.ptr + off_cdf);
+    int *live = reinterpret_cast<int *>(p.dep.ptr + off_live);
     SFB_CUDA_TRY(cudaMemsetAsync(counts, 0, (size_t)nscan * sizeof(int32_t), st));
     SFB_CUDA_TRY(cudaMemsetAsync(fb_count, 0, sizeof(int32_t), st));
     const double inv_width = (double)p.pieces / (p.rmax - p.rmin);
@@ -821,8 +835,9 @@ int deposit_sorted(Plan &p, const double *rtp, const double *w, int64_t ngal, do
     const bool split = ref != nullptr && mixed;
     float2 *mudf = reinterpret_cast<float2 *>(p.dep.ptr + off_stats + p.nbasis + p.pieces + 2);
     if (split) {
-        k_weight_map_mixed<<<(unsigned)((p.npix + 255) / 256), 256, 0, st>>>(counts, sorted4, p.npix, p.pieces + 2,
-                                                                            ref, cdf);
+        SFB_CUDA_TRY(cudaMemsetAsync(live, 0, (size_t)nrings * sizeof(int), st));
+        k_weight_map_mixed<<<(unsigned)((p.npix + 255) / 256), 256, 0, st>>>(counts, sorted4, p.nside, p.npix,
+                                                                            p.pieces + 2, ref, cdf, live);
         note_launch();
         if (ref_ready) SFB_CUDA_TRY(cudaEventRecord(ref_ready, st));
         double *S = p.dep.ptr + off_stats;
@@ -834,10 +849,12 @@ int deposit_sorted(Plan &p, const double *rtp, const double *w, int64_t ngal, do
         note_launch();
     }
     // moments in FP64 (FP64 path) or double-float (mixed); stored in the transform's precision
+    const bool skip_empty = split && ring_live && p.npix >= 128 && p.degree <= 31;   // the balanced kernel
     by_degree(p.degree, [&](auto D) {
         launch_moments<decltype(D)::value>(p, counts, sorted, split ? ref : nullptr, mu, split ? cdf : nullptr, mudf,
-                                           maps, st);
+                                           maps, st, skip_empty ? live : nullptr);
     });
+    if (skip_empty) *ring_live = live;
     SFB_CUDA_TRY(cudaGetLastError());
     return SFB_OK;
 }

@@ -201,22 +201,27 @@ __device__ __forceinline__ bool lvl_stage_free(const LvlSmem &cs, int kc) {
 
 // Per (block z, column c): E with max_r |F[parity][m][r][c]| < 2^E, raised by
 // ceil(log2 nrn) - 9 for more than 512 rings (level sums below 2^24 units).
+// (nzr: F is zero outside the ring pairs [nzr[0], nzr[1]], which are the only ones read)
 __global__ void __launch_bounds__(256) k_colmax(const float *__restrict__ F, int64_t ncol, int lmax, int nrn,
-                                                int *__restrict__ Ecol) {
+                                                int *__restrict__ Ecol, const int *__restrict__ nzr) {
     const int z = blockIdx.y;
     const int m = z >> 1, par = z & 1;
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncol) return;
     const float *Fz = F + ((int64_t)(par * (lmax + 1) + m) * nrn) * ncol + c;
     float m0 = 0.f, m1 = 0.f, m2 = 0.f, m3 = 0.f;
-    int r = 0;
-    for (; r + 3 < nrn; r += 4) {
+    int r = 0, r1 = nrn;
+    if (nzr) {
+        r = nzr[0];
+        r1 = min(nrn, nzr[1] + 1);
+    }
+    for (; r + 3 < r1; r += 4) {
         m0 = fmaxf(m0, fabsf(Fz[(int64_t)r * ncol]));
         m1 = fmaxf(m1, fabsf(Fz[(int64_t)(r + 1) * ncol]));
         m2 = fmaxf(m2, fabsf(Fz[(int64_t)(r + 2) * ncol]));
         m3 = fmaxf(m3, fabsf(Fz[(int64_t)(r + 3) * ncol]));
     }
-    for (; r < nrn; ++r) m0 = fmaxf(m0, fabsf(Fz[(int64_t)r * ncol]));
+    for (; r < r1; ++r) m0 = fmaxf(m0, fabsf(Fz[(int64_t)r * ncol]));
     const int lg = 32 - __clz(nrn > 1 ? nrn - 1 : 1);
     Ecol[(int64_t)z * ncol + c] = max(-90, min(scale_exp(fmaxf(fmaxf(m0, m1), fmaxf(m2, m3))) + max(0, lg - 9), 100));
 }
@@ -720,7 +725,7 @@ void launch_leg_analysis_tc(const Plan &p, const float *F, int64_t ncol, double 
     if (rlim < 0 || rlim > p.nrn) rlim = (int)p.nrn;
     if (!scales_ready) {
         dim3 grid((unsigned)((ncol + 255) / 256), (unsigned)(2 * (p.lmax + 1)));
-        tc::k_colmax<<<grid, 256, 0, st>>>(F, ncol, p.lmax, (int)p.nrn, Ecol);
+        tc::k_colmax<<<grid, 256, 0, st>>>(F, ncol, p.lmax, (int)p.nrn, Ecol, nzr);
         note_launch();
     }
     set_smem(tc::k_leg_analysis_tc, tc::LEG_SMEM);

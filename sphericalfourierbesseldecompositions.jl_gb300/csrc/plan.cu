@@ -310,8 +310,11 @@ struct ShtWork {
 
 // fp64_out: the FP64 a_lm (alm) is wanted besides the double-float copy (almdf, mixed precision); the
 // Gram refinement carries only the double-float one and converts at the end when asked.
+// ring_live / nlive (mixed precision): rings marked 0 hold zeros in maps [0, nlive), left unwritten by the
+// deposit (deposit_sorted's ring_live).
 int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, bool maps_are_fp64 = false,
-                 int stage_override = -1, const ShtWork *ws = nullptr, bool fp64_out = true) {
+                 int stage_override = -1, const ShtWork *ws = nullptr, bool fp64_out = true,
+                 const int *ring_live = nullptr, int64_t nlive = 0) {
     Plan &p = h->p;
     const ShtWork own{&p.fbuf, &p.gbuf, &p.rbuf, &p.alm};
     if (!ws) ws = &own;
@@ -342,7 +345,7 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, b
         nzr = reinterpret_cast<int *>(p.erow.ptr) + 2 * std::max<int64_t>(p.nrn * nm, (p.lmax + 1) * ncol);
         Stage s(h, stage(SFB_STAGE_RING_FFT), st);
         launch_ring_analysis_tc(p, reinterpret_cast<const float *>(maps), nm, reinterpret_cast<float *>(fbuf.ptr),
-                                reinterpret_cast<int *>(p.erow.ptr), nzr, st);
+                                reinterpret_cast<int *>(p.erow.ptr), nzr, st, ring_live, nlive);
     } else {
         Stage s(h, stage(SFB_STAGE_RING_FFT), st);
         launch_ring_analysis(p, maps, nm, fbuf.ptr, st);
@@ -574,6 +577,7 @@ int cat2amln_dev(sfb_plan *h, const double *rtp, const double *w, int64_t ngal, 
             SFB_CUDA_TRY(cudaMemcpyAsync(Cmap + p.npix, W01, p.npix * sizeof(double), cudaMemcpyDeviceToDevice, st));
         }
         SFB_TRY(grow(p, p.maps, (size_t)nm * p.npix));
+        const int *ring_live = nullptr;          // rings the deposit wrote (mixed precision)
         if (wk == SFB_WINDOW_SEPARABLE) {
             Stage s(h, SFB_STAGE_OTHER, st);
             if (p.precision == SFB_MIXED)
@@ -585,7 +589,7 @@ int cat2amln_dev(sfb_plan *h, const double *rtp, const double *w, int64_t ngal, 
         {
             Stage s(h, SFB_STAGE_DEPOSIT, st);
             SFB_TRY(deposit_sorted(p, rtp, w, ngal, p.maps.ptr, Cmap, mu, split ? h->ev_fork : nullptr, st,
-                                   chunk_ready, nchunks));
+                                   chunk_ready, nchunks, &ring_live));
         }
         if (split) {
             // the FP64 transform of (C, W01) runs on the side stream, in its own workspace, beside
@@ -595,7 +599,8 @@ int cat2amln_dev(sfb_plan *h, const double *rtp, const double *w, int64_t ngal, 
             SFB_CUDA_TRY(cudaEventRecord(h->ev_join, h->side));
         }
         // the mixed projection reads the double-float a_lm only
-        SFB_TRY(sht_analysis(h, p.maps.ptr, nm, st, false, -1, nullptr, p.precision != SFB_MIXED));
+        SFB_TRY(sht_analysis(h, p.maps.ptr, nm, st, false, -1, nullptr, p.precision != SFB_MIXED, ring_live,
+                             p.nbasis));
         if (split) SFB_CUDA_TRY(cudaStreamWaitEvent(st, h->ev_join, 0));
         {
             Stage s(h, SFB_STAGE_PROJECT, st);

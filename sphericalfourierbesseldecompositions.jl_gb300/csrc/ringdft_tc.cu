@@ -84,10 +84,12 @@ __device__ __forceinline__ void st_shared_v4(unsigned char *p, const uint32_t (&
 // non-finite value keeps an ordinary exponent, so the value reaches the
 // spectra and the transform's finiteness check.  erow layout [2][nrn][nmaps];
 // nzr[0] / nzr[1] get the first / last ring pair with a non-zero row (preset
-// to a large value / -1).
+// to a large value / -1).  With ring_live, the rows of maps b < nlive on the
+// rings marked 0 are zero by construction and are not read.
 __global__ void __launch_bounds__(128) k_ring_rowexp(const float *__restrict__ maps, int64_t npix, int64_t nmaps,
                                                      const RingGeom *__restrict__ rings, int nrn, int *erow,
-                                                     int *nzr) {
+                                                     int *nzr, const int *__restrict__ ring_live, int64_t nlive,
+                                                     int nrings) {
     const int r = blockIdx.x;
     const int64_t b = (int64_t)blockIdx.y * 4 + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
@@ -96,6 +98,10 @@ __global__ void __launch_bounds__(128) k_ring_rowexp(const float *__restrict__ m
     bool any = false;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
+        if (ring_live && b < nlive && !ring_live[h ? nrings - 1 - r : r]) {
+            if (lane == 0) erow[((int64_t)h * nrn + r) * nmaps + b] = ZERO_ROW_E;
+            continue;
+        }
         const float *x = maps + b * npix + (h ? g.start_s : g.start_n);
         float mx = 0.f;
         bool fin = true;
@@ -178,14 +184,15 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
         b = q % nmaps;
     }
     const RingGeom g = rings[ring];
-    const bool live = abuild && rok && (hemi == 0 || g.start_s != g.start_n);   // the equator has no south row
-    const float *x = maps + b * npix + (hemi ? g.start_s : g.start_n);
     const int E = rok ? erow[((int64_t)hemi * nrn + ring) * nmaps + b] : ZERO_ROW_E;
+    // zero rows are not read (on rings without galaxies they are not even written)
+    const bool live = abuild && rok && (hemi == 0 || g.start_s != g.start_n) && E != ZERO_ROW_E;
+    const float *x = maps + b * npix + (hemi ? g.start_s : g.start_n);
     float C[4];
     slice_consts(E == ZERO_ROW_E ? 0 : E, C);
     const int L1 = lmax + 1;
     // a tile of zero rows (rings outside the survey) has zero spectra: written without MMAs
-    if (!__syncthreads_or(live && E != ZERO_ROW_E)) {
+    if (!__syncthreads_or(live)) {
         for (int i = tid; i < 2 * 64 * NPAIR; i += NTHR) {
             const int pr = i & (NPAIR - 1), mo = (i / NPAIR) & 63, sg = i / (64 * NPAIR);
             const int mm = 64 * u + mo;
@@ -515,13 +522,14 @@ uint2 dft_slices(double v, int EB) {
 }
 
 void launch_ring_analysis_tc(const Plan &p, const float *maps, int64_t nmaps, float *F, int *erow, int *nzr,
-                             cudaStream_t st) {
+                             cudaStream_t st, const int *ring_live, int64_t nlive) {
     {
         // nzr[0] = 0x7f7f7f7f (above any ring index), nzr[1] = -1
         cudaMemsetAsync(nzr, 0x7f, sizeof(int), st);
         cudaMemsetAsync(nzr + 1, 0xff, sizeof(int), st);
         dim3 grid((unsigned)p.nrn, (unsigned)((nmaps + 3) / 4));
-        dft::k_ring_rowexp<<<grid, 128, 0, st>>>(maps, p.npix, nmaps, p.d_rings, (int)p.nrn, erow, nzr);
+        dft::k_ring_rowexp<<<grid, 128, 0, st>>>(maps, p.npix, nmaps, p.d_rings, (int)p.nrn, erow, nzr, ring_live,
+                                                 nlive, (int)(4 * p.nside - 1));
         note_launch();
     }
     set_smem(dft::k_ring_dft_tc<true>, dft::SMEM);

@@ -170,9 +170,26 @@ void launch_legendre_table(const Plan &p, cudaStream_t st);
 // recorded on st once C is complete.
 // chunk_ready / nchunks: the catalogue arrives in nchunks equal galaxy ranges,
 // range c complete when chunk_ready[c] fires (keys wait per range).
+// ring_live (mixed precision with a reference map): receives a device array of 4 nside - 1 ints, 1 for the
+// rings that hold a galaxy; the basis maps are left unwritten on the other rings (they are zero there),
+// and the ring DFT must be given the array (launch_ring_analysis_tc) so that it does not read them.
 int deposit_sorted(Plan &p, const double *rtp, const double *w, int64_t ngal, double *maps, double *ref,
                    double *mu, cudaEvent_t ref_ready, cudaStream_t st, const cudaEvent_t *chunk_ready = nullptr,
-                   int nchunks = 0);
+                   int nchunks = 0, const int **ring_live = nullptr);
+
+// 0-based ring (1 .. 4 nside - 1 minus one) of a RING-scheme pixel
+__host__ __device__ __forceinline__ int ring_of_pixel(int64_t nside, int64_t pix) {
+    const int64_t npix = 12 * nside * nside, ncap = 2 * nside * (nside - 1);
+    auto cap = [](int64_t q) {
+        int64_t i = (int64_t)((1.0f + sqrtf(1.0f + 2.0f * (float)q)) * 0.5f);
+        while (i > 1 && 2 * i * (i - 1) > q) --i;
+        while (2 * (i + 1) * i <= q) ++i;
+        return i;
+    };
+    if (pix < ncap) return (int)cap(pix) - 1;
+    if (pix >= npix - ncap) return (int)(4 * nside - cap(npix - 1 - pix)) - 1;
+    return (int)((pix - ncap) / (4 * nside) + nside) - 1;
+}
 // A[lm][2j + c] += mu[j] * rmu[lm * ldr + c] for j < nmaps; with set_col >= 0
 // also A[lm][2 set_col + c] = rset[lm * ldr + c].
 void launch_add_mean(double *A, int64_t ldA, int64_t nmaps, const double *mu, const double *rmu, const double *rset,
@@ -206,8 +223,9 @@ void launch_project_poly(const Plan &p, const double *A, int64_t ldA, double sca
 void launch_to_float(const double *in, int64_t n, float *out, cudaStream_t st);
 // Mixed-precision ring analysis on the tensor cores (FP32 maps -> FP32 F).
 // nzr[0..1] receives the first and last ring pair holding a non-zero map row.
+// ring_live (optional): rings whose entry is 0 hold zeros in maps [0, nlive) and are not read.
 void launch_ring_analysis_tc(const Plan &p, const float *maps, int64_t nmaps, float *F, int *erow, int *nzr,
-                             cudaStream_t st);
+                             cudaStream_t st, const int *ring_live = nullptr, int64_t nlive = 0);
 uint2 dft_slices(double v, int EB);
 int64_t dft_image_offsets(const Plan &p, const std::vector<int32_t> &crings, const std::vector<int32_t> &coff,
                           bool with_polar, std::vector<int64_t> &off, int &max_nch);
