@@ -148,10 +148,26 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
     const int cls = blockIdx.z;
     const int rb = cls_off[cls];
     const int64_t npairs = (int64_t)(cls_off[cls + 1] - rb) * nmaps;
-    const int64_t pair0 = (int64_t)blockIdx.y * NPAIR;
+    const int ty = blockIdx.y;
+    const int64_t pair0 = (int64_t)ty * NPAIR;
     if (pair0 >= npairs) return;
     const int u = blockIdx.x;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // north-only tiles: where the south rows of this tile and of its partner tile ty ^ 1 are all zero
+    // (southern rings outside the survey), the even tile takes the north rows of both, 128 pairs, with
+    // F+ = F- = F_N, and the odd one has nothing left to do
+    bool snz = false;
+    if (tid < 2 * NPAIR) {
+        const int64_t qq = (int64_t)(ty & ~1) * NPAIR + tid;
+        if (qq < npairs) {
+            const int rg = cls_rings[rb + (int)(qq / nmaps)];
+            if (rings[rg].start_s != rings[rg].start_n)
+                snz = erow[((int64_t)nrn + rg) * nmaps + qq % nmaps] != ZERO_ROW_E;
+        }
+    }
+    const bool nonly = !__syncthreads_or(snz);
+    if (nonly && (ty & 1)) return;
+    const int npr = nonly ? 2 * NPAIR : NPAIR;      // (ring, map) pairs of this tile
     const bool prod = tid < NPROD;
     const bool abuild = IMG ? prod : tid < NROW;   // IMG: all producers build A; else warps 0-3 A, 4-7 B
     const int ti = tid & (NROW - 1);
@@ -173,9 +189,9 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
     const int nch = (n + KC - 1) / KC;
     const unsigned char *bimg = IMG ? img + (size_t)(img_off[cls] + (int64_t)u * nch) * (4 * PLANE) : nullptr;
 
-    // A row ti: pair ti % 64, hemisphere ti / 64
-    const int hemi = ti >> 6;
-    const int64_t q = pair0 + (ti & (NPAIR - 1));
+    // A row ti: pair ti % 64, hemisphere ti / 64 (north-only tiles: pair ti, north)
+    const int hemi = nonly ? 0 : ti >> 6;
+    const int64_t q = pair0 + (nonly ? ti : (ti & (NPAIR - 1)));
     const bool rok = q < npairs;
     int ring = ring0;
     int64_t b = 0;
@@ -193,8 +209,8 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
     const int L1 = lmax + 1;
     // a tile of zero rows (rings outside the survey) has zero spectra: written without MMAs
     if (!__syncthreads_or(live)) {
-        for (int i = tid; i < 2 * 64 * NPAIR; i += NTHR) {
-            const int pr = i & (NPAIR - 1), mo = (i / NPAIR) & 63, sg = i / (64 * NPAIR);
+        for (int i = tid; i < 2 * 64 * npr; i += NTHR) {
+            const int pr = i % npr, mo = (i / npr) & 63, sg = i / (64 * npr);
             const int mm = 64 * u + mo;
             const int64_t qo = pair0 + pr;
             if (mm > lmax || qo >= npairs) continue;
@@ -361,6 +377,38 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
             // image copies still in flight land before the CTA leaves (bounded waits on their stages)
             for (int kc = ncopied - NSTAGE < 0 ? 0 : ncopied - NSTAGE; kc < ncopied; ++kc)
                 mbar_wait(&full[kc % NSTAGE], (uint32_t)((kc / NSTAGE) & 1));
+        }
+    } else if (prod && nonly) {
+        // north-only epilogue: row = pair pair0 + lane index, F+ = F- = lead + rest (the south terms of
+        // the general epilogue are zero)
+        const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+        const int half = tid >> 7;
+        const int64_t qo = pair0 + (warp & 3) * 32 + lane;
+        const bool ook = qo < npairs;
+        int oring = ring0;
+        int64_t ob = 0;
+        if (ook) {
+            oring = cls_rings[rb + (int)(qo / nmaps)];
+            ob = qo % nmaps;
+        }
+#pragma unroll 1
+        for (int it = 0; it < 4; ++it) {
+            const int cg = 4 * half + it;
+            float v0[16], v1[16], v2[16], v3[16];
+            tmem_ld16(tmem + lane_base + (uint32_t)(16 * cg), v0);
+            tmem_ld16(tmem + lane_base + 128u + (uint32_t)(16 * cg), v1);
+            tmem_ld16(tmem + lane_base + 256u + (uint32_t)(16 * cg), v2);
+            tmem_ld16(tmem + lane_base + 384u + (uint32_t)(16 * cg), v3);
+            if (!ook) continue;
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+                const int mm = 64 * u + 8 * cg + t;
+                if (mm > lmax) break;
+                const float2 f = make_float2(v0[2 * t] + (v1[2 * t] + (v2[2 * t] + v3[2 * t])),
+                                             v0[2 * t + 1] + (v1[2 * t + 1] + (v2[2 * t + 1] + v3[2 * t + 1])));
+                *reinterpret_cast<float2 *>(F + ((int64_t)mm * nrn + oring) * ldF + 2 * ob) = f;
+                *reinterpret_cast<float2 *>(F + ((int64_t)(L1 + mm) * nrn + oring) * ldF + 2 * ob) = f;
+            }
         }
     } else if (prod) {
         // epilogue: per row, lead = level 0 (exact) and rest = level 1 + (level 2 + level 3).  Warps w and
