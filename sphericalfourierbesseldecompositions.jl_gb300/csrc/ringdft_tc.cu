@@ -93,11 +93,11 @@ __global__ void __launch_bounds__(128) k_ring_rowexp(const float *__restrict__ m
     const int r = blockIdx.x;
     const int64_t b = (int64_t)blockIdx.y * 4 + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
-    if (b >= nmaps) return;
     const RingGeom g = rings[r];
     bool any = false;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
+        if (b >= nmaps) break;
         if (ring_live && b < nlive && !ring_live[h ? nrings - 1 - r : r]) {
             if (lane == 0) erow[((int64_t)h * nrn + r) * nmaps + b] = ZERO_ROW_E;
             continue;
@@ -107,24 +107,23 @@ __global__ void __launch_bounds__(128) k_ring_rowexp(const float *__restrict__ m
         bool fin = true;
         for (int j = lane; j < g.nph; j += 32) {
             const float v = x[j];
-            fin = fin && isfinite(v);
+            fin &= isfinite(v);
             mx = fmaxf(mx, fabsf(v));
         }
         for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
         fin = __all_sync(0xffffffffu, fin);
-        if (lane == 0) {
-            int E = scale_exp(mx);
-            const int lg = 32 - __clz(g.nph - 1);          // ceil(log2 n)
-            E += max(0, lg - 10);
-            E = max(-90, min(E, 100));
-            if (mx == 0.f && fin) E = ZERO_ROW_E;
-            else any = true;
-            erow[((int64_t)h * nrn + r) * nmaps + b] = E;
-        }
+        int E = scale_exp(mx);
+        const int lg = 32 - __clz(g.nph - 1);              // ceil(log2 n)
+        E += max(0, lg - 10);
+        E = max(-90, min(E, 100));
+        if (mx == 0.f && fin) E = ZERO_ROW_E;
+        else any = true;
+        if (lane == 0) erow[((int64_t)h * nrn + r) * nmaps + b] = E;
     }
-    if (lane == 0 && any) {
-        atomicMin(nzr, r);
-        atomicMax(nzr + 1, r);
+    // the ring-pair range: one thread per block, and an atomic only where it moves a bound
+    if (__syncthreads_or(any) && threadIdx.x == 0) {
+        if (r < *(volatile int *)nzr) atomicMin(nzr, r);
+        if (r > *(volatile int *)(nzr + 1)) atomicMax(nzr + 1, r);
     }
 }
 
