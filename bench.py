@@ -40,7 +40,11 @@ KMAX, RMIN, RMAX, NSIDE, NR = 0.1, 500.0, 2500.0, 256, 1000
 NGAL_MEAN = 10_000_000
 CAP_DEG, RMEAN, RSIG = 60.0, 1500.0, 400.0
 # measured with ncu (dram__bytes_read.sum + dram__bytes_write.sum) over the two ring-DFT launches of one call
-DFT_DRAM_BYTES_PER_CALL = (892.93 + 308.77 + 699.78 + 295.97) * 1e6
+# DRAM bytes (read + write) per call of the stages' kernels on this workload, from the single-pass ncu
+# capture recorded in profiles/launches_cat2amln_nside256_kmax0.1_mixed.md (second call of the run)
+DFT_DRAM_BYTES_PER_CALL = (720.60 + 300.21 + 96.09 + 260.42) * 1e6          # k_ring_dft_tc x2
+DEPOSIT_DRAM_BYTES_PER_CALL = (332.81 + 133.19 + 18.76 + 0.04 + 47.20 + 0.02 + 0.02 + 47.20 + 498.99 + 283.26
+                               + 207.17 + 3.61 + 8.61 + 0.01 + 221.04 + 211.19) * 1e6   # keys .. moments
 WORKLOAD = "cat2amln kmax=0.1 rmin=500 rmax=2500 nside=256 nr=1000 N~Poisson(1e7) cap60 x gauss(1500,400) w~U[0.5,1.5]"
 
 
@@ -221,7 +225,8 @@ def sky_rings(sfbgpu, nside, theta, phi):
     span from the first to the last such pair).  Outside them every map of the
     mixed path is zero: the ring DFT skips those rows and the first analysis
     pass sums over the span only, so the algorithmic work below is counted
-    over the same rings."""
+    over the same rings.  Third value: the pixels of the rings that hold
+    galaxies, the only ones whose basis-map rows the mixed deposit writes."""
     ns = int(nside)
     npix = 12 * ns * ns
     ncap = 2 * ns * (ns - 1)
@@ -243,12 +248,15 @@ def sky_rings(sfbgpu, nside, theta, phi):
     gp = sfbgpu.ang2pix_ring(ns, theta, phi)
     used = np.zeros(2 * ns, bool)
     used[np.unique(pair[gp])] = True
+    live_ring = np.zeros(4 * ns - 1, bool)
+    live_ring[np.unique(ring[gp]) - 1] = True
+    live_pix = int(np.bincount(ring - 1, minlength=4 * ns - 1)[live_ring].sum())
     idx = np.nonzero(used)[0]
     if idx.size == 0:
-        return 0, 0
+        return 0, 0, 0
     lo, hi = int(idx[0]), int(idx[-1])
     rings = 2 * (hi - lo + 1) - (1 if hi == 2 * ns - 1 else 0)
-    return int(pix_per_pair[used].sum()), rings
+    return int(pix_per_pair[used].sum()), rings, live_pix
 
 
 def stage_work(stage, precision, nm, ngal, nbasis, niter=3, lmax=238, sky=None):
@@ -271,7 +279,8 @@ def stage_work(stage, precision, nm, ngal, nbasis, niter=3, lmax=238, sky=None):
     their span (the rows elsewhere are zero and skipped).
     fold: G read + R written per pass (mixed: the aliased rings only; FP64:
     F, G read + R written over all rings).  deposit: 40 B per galaxy (record
-    read + binning update) + the basis maps written."""
+    read + binning update) + the basis maps written (mixed: on the rings
+    holding galaxies, sky[2] pixels)."""
     lmsize = (lmax + 1) * (lmax + 2) // 2
     nrn = 2 * NSIDE
     n_ring = 4 * NSIDE - 1
@@ -300,7 +309,8 @@ def stage_work(stage, precision, nm, ngal, nbasis, niter=3, lmax=238, sky=None):
             return ("byte", niter * 2.0 * 2 * (lmax + 1) * ral * ncol * t)
         return ("byte", niter * 3.0 * fsz)
     if stage == "deposit":
-        return ("byte", 40.0 * ngal + float(t) * nbasis * npix)
+        mpix = sky[2] if (sky and precision == "mixed") else npix
+        return ("byte", 40.0 * ngal + float(t) * nbasis * mpix)
     return ("byte", None)
 
 
@@ -589,11 +599,16 @@ def main():
     roof = dict(table[dom])
     roof["kernel_stage"] = dom
     roof["traffic"] = None
-    if dom == "ring_fft" and args.precision == "mixed" and not args.profile_case:
-        # DRAM bytes (read + write) of the stage's two DFT launches in one call, from the single-pass
-        # ncu capture of this workload recorded in profiles/launches_cat2amln_nside256_kmax0.1_mixed.md
-        roof["traffic"] = DFT_DRAM_BYTES_PER_CALL
-        roof["traffic_source"] = "ncu dram__bytes_read.sum + dram__bytes_write.sum, k_ring_dft_tc x2, full workload"
+    if args.precision == "mixed" and not args.profile_case and NGAL_MEAN == 10_000_000:
+        # DRAM bytes (read + write) of the stage's kernels in one call of this workload, from the
+        # single-pass ncu capture recorded in profiles/launches_cat2amln_nside256_kmax0.1_mixed.md
+        if dom == "ring_fft":
+            roof["traffic"] = DFT_DRAM_BYTES_PER_CALL
+            roof["traffic_source"] = "ncu dram__bytes_read.sum + dram__bytes_write.sum, k_ring_dft_tc x2"
+        elif dom == "deposit":
+            roof["traffic"] = DEPOSIT_DRAM_BYTES_PER_CALL
+            roof["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum, deposit kernels "
+                                      "(keys, fallback, scans, scatter, count map, stats, moments)")
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
