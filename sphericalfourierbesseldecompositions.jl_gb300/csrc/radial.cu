@@ -627,17 +627,17 @@ __global__ void __launch_bounds__(32 * KS) k_project_mixed(const float2 *__restr
         const int n1 = n0 + j;
         if (j >= npt) break;
         const int pr = pair_index[(int64_t)n1 * (lmax + 1) + l];
-        double vr = (double)re[j].hi + (double)re[j].lo;
-        double vi = (double)im[j].hi + (double)im[j].lo;
+        if (pr < 0) continue;
+        // the parts added in double-float (FP32 units), one conversion to FP64
+        df2 sr = df2{re[j].hi, re[j].lo}, si = df2{im[j].hi, im[j].lo};
 #pragma unroll
         for (int q = 0; q < KS - 1; ++q) {
             const float4 v = part[q][j][lane];
-            vr += (double)v.x + (double)v.y;
-            vi += (double)v.z + (double)v.w;
+            sr = dfa(sr, df2{v.x, v.y});
+            si = dfa(si, df2{v.z, v.w});
         }
-        if (pr < 0) continue;
-        vr *= scale;
-        vi *= scale;
+        double vr = scale * ((double)sr.hi + (double)sr.lo);
+        double vi = scale * ((double)si.hi + (double)si.lo);
         if (ralm) {
             const double mu = scale * smean[pr];
             vr = fma(mu, ralm[4 * lm], vr);
