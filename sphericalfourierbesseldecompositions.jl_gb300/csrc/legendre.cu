@@ -448,7 +448,11 @@ __global__ void __launch_bounds__(128) k_fold_cols(const RingGeom *__restrict__ 
 // Block: parity, FC complex columns, a group of rings; shared memory holds
 // the ring's G rows, the buckets and the running column maxima (exponents for
 // the analysis).
-template <int FC>
+// MXREG: (lmax + 1) FC <= 256 MXQ, and each thread keeps the maxima of its output elements
+// (i = tid + 256 q) in registers instead of shared memory (a smaller footprint, more CTAs per SM).
+constexpr int FOLD_MXQ = 8;
+
+template <int FC, bool MXREG>
 __global__ void __launch_bounds__(256) k_fold_alias(const RingGeom *__restrict__ rings, int nrn, int ral, int rpb,
                                                     int nbk, int lmax, double w, const float *__restrict__ G,
                                                     int64_t ncplx, float *__restrict__ R, int *__restrict__ Ecol) {
@@ -459,10 +463,14 @@ __global__ void __launch_bounds__(256) k_fold_alias(const RingGeom *__restrict__
     const int L1 = lmax + 1;
     const int64_t ld = 2 * ncplx;
     float2 *P = fsm;                                  // [nbk][FC], nbk = the longest of the rings
-    float2 *mx = fsm + (int64_t)nbk * FC;             // [L1][FC] (re, im maxima)
-    float2 *Gs = mx + (int64_t)L1 * FC;               // [L1][FC] the ring's G rows
+    float2 *mx = fsm + (int64_t)nbk * FC;             // [L1][FC] (re, im maxima; not MXREG)
+    float2 *Gs = mx + (MXREG ? 0 : (int64_t)L1 * FC); // [L1][FC] the ring's G rows
     const int tid = threadIdx.x;
-    for (int i = tid; i < L1 * FC; i += 256) mx[i] = make_float2(0.f, 0.f);
+    float2 mxr[MXREG ? FOLD_MXQ : 1];
+#pragma unroll
+    for (int q = 0; q < (MXREG ? FOLD_MXQ : 1); ++q) mxr[q] = make_float2(0.f, 0.f);
+    if (!MXREG)
+        for (int i = tid; i < L1 * FC; i += 256) mx[i] = make_float2(0.f, 0.f);
     // a ring's G rows: element i = m * FC + cc at thread tid + 256 q; FOLD_PF loads per thread in
     // registers, the next ring's issued before this ring's buckets (more rows loop through Gs directly)
     constexpr int FOLD_PF = 8;
@@ -510,7 +518,10 @@ __global__ void __launch_bounds__(256) k_fold_alias(const RingGeom *__restrict__
             P[i] = make_float2(sx, sy);
         }
         __syncthreads();
-        for (int i = tid; i < L1 * FC; i += 256) {
+#pragma unroll
+        for (int q = 0; q < (MXREG ? FOLD_MXQ : 1 << 30); ++q) {
+            const int i = tid + 256 * q;
+            if (i >= L1 * FC) break;
             const int mp = i / FC, cc = i - mp * FC;
             const int64_t c = c0 + cc;
             if (c >= ncplx) continue;
@@ -526,10 +537,15 @@ __global__ void __launch_bounds__(256) k_fold_alias(const RingGeom *__restrict__
             const int64_t off = ((int64_t)(par * L1 + mp) * nrn + r) * ld + 2 * c;
             R[off] = rx;
             R[off + 1] = ry;
-            float2 m2 = mx[i];
-            m2.x = fmaxf(m2.x, fabsf(rx));
-            m2.y = fmaxf(m2.y, fabsf(ry));
-            mx[i] = m2;
+            if constexpr (MXREG) {
+                mxr[q].x = fmaxf(mxr[q].x, fabsf(rx));
+                mxr[q].y = fmaxf(mxr[q].y, fabsf(ry));
+            } else {
+                float2 m2 = mx[i];
+                m2.x = fmaxf(m2.x, fabsf(rx));
+                m2.y = fmaxf(m2.y, fabsf(ry));
+                mx[i] = m2;
+            }
         }
     }
     if (!Ecol) return;
@@ -540,13 +556,17 @@ __global__ void __launch_bounds__(256) k_fold_alias(const RingGeom *__restrict__
         int E = (v > 0.f && isfinite(v)) ? ilogbf(v) + 1 : 0;
         return max(-90, min(E + extra, 100));
     };
-    for (int i = tid; i < L1 * FC; i += 256) {
+#pragma unroll
+    for (int q = 0; q < (MXREG ? FOLD_MXQ : 1 << 30); ++q) {
+        const int i = tid + 256 * q;
+        if (i >= L1 * FC) break;
         const int mp = i / FC, cc = i - mp * FC;
         const int64_t c = c0 + cc;
         if (c >= ncplx) continue;
         const int64_t z = 2 * (int64_t)mp + par;
-        atomicMax(Ecol + z * ld + 2 * c, ex(mx[i].x));
-        atomicMax(Ecol + z * ld + 2 * c + 1, ex(mx[i].y));
+        const float2 m2 = MXREG ? mxr[MXREG ? q : 0] : mx[i];
+        atomicMax(Ecol + z * ld + 2 * c, ex(m2.x));
+        atomicMax(Ecol + z * ld + 2 * c + 1, ex(m2.y));
     }
 }
 
@@ -621,14 +641,21 @@ void launch_fold_residual(const Plan &p, const double *F, const double *G, int64
             constexpr int FC = 8;
             int nbk = 1;
             for (int r = 0; r < rlim; ++r) nbk = std::max(nbk, p.h_rings[r].nph);
-            const size_t smem = ((size_t)nbk + 2 * (size_t)(p.lmax + 1)) * FC * sizeof(float2);
+            const bool mxreg = (p.lmax + 1) * FC <= 256 * FOLD_MXQ;
+            const size_t smem = ((size_t)nbk + (mxreg ? 1 : 2) * (size_t)(p.lmax + 1)) * FC * sizeof(float2);
             if (smem <= 200 * 1024) {
                 const int rpb = 8;
-                set_smem(k_fold_alias<FC>, smem);
                 dim3 grid((unsigned)((ncplx + FC - 1) / FC), 2, (unsigned)((rlim + rpb - 1) / rpb));
-                k_fold_alias<FC><<<grid, 256, smem, st>>>(p.d_rings, (int)p.nrn, rlim, rpb, nbk, p.lmax,
-                                                          4.0 * M_PI / (double)p.npix, (const float *)G, ncplx,
-                                                          (float *)R, Ecol);
+                const double w = 4.0 * M_PI / (double)p.npix;
+                if (mxreg) {
+                    set_smem(k_fold_alias<FC, true>, smem);
+                    k_fold_alias<FC, true><<<grid, 256, smem, st>>>(p.d_rings, (int)p.nrn, rlim, rpb, nbk, p.lmax,
+                                                                    w, (const float *)G, ncplx, (float *)R, Ecol);
+                } else {
+                    set_smem(k_fold_alias<FC, false>, smem);
+                    k_fold_alias<FC, false><<<grid, 256, smem, st>>>(p.d_rings, (int)p.nrn, rlim, rpb, nbk, p.lmax,
+                                                                     w, (const float *)G, ncplx, (float *)R, Ecol);
+                }
                 note_launch();
                 return;
             }
