@@ -196,6 +196,7 @@ __global__ void __launch_bounds__(256) k_ring_analysis(const RingGeom *rings, in
     // in double-float (FP32 TwoSum) and replace the FFT's bin 0.
     constexpr bool reduced = sizeof(T) < sizeof(double);
     __shared__ float ring_hi[2 * 8], ring_lo[2 * 8];
+    bool nz = false;
     for (int idx = threadIdx.x; idx < MT * n; idx += blockDim.x) {
         const int b = idx / n;
         const int j = idx - b * n;
@@ -205,10 +206,23 @@ __global__ void __launch_bounds__(256) k_ring_analysis(const RingGeom *rings, in
             v.x = (T)maps[mb * npix + g.start_n + j];
             if (paired) v.y = (T)maps[mb * npix + g.start_s + j];
         }
+        nz |= (v.x != (T)0) | (v.y != (T)0);           // NaN counts as non-zero
         if (o > 1) store_src(src, (int64_t)b * n + j, v);
         else buf[(int64_t)b * n + bitrev(j, s)] = v;
     }
-    __syncthreads();
+    const int L1 = lmax + 1;
+    if (!__syncthreads_or(nz)) {
+        // both rings are zero in every map of the block (outside the survey): zero spectra, no FFT
+        for (int idx = threadIdx.x; idx < MT * L1; idx += blockDim.x) {
+            const int m = idx / MT;
+            const int64_t mb = b0 + (idx - m * MT);
+            if (mb >= nmaps) continue;
+            T *dp = F + ((int64_t)(0 * L1 + m) * nrn + r) * ldF + 2 * mb;
+            T *dq = F + ((int64_t)(1 * L1 + m) * nrn + r) * ldF + 2 * mb;
+            dp[0] = dp[1] = dq[0] = dq[1] = (T)0;
+        }
+        return;
+    }
     if (reduced) {
         // one warp per (map, ring of the pair): double-float sum of the staged values
         const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -240,7 +254,6 @@ __global__ void __launch_bounds__(256) k_ring_analysis(const RingGeom *rings, in
     }
     four_step<T>(buf, src, tw, n, o, s, MT, twd);
     // unpack, phase, weight; write F+ and F-
-    const int L1 = lmax + 1;
     for (int idx = threadIdx.x; idx < MT * L1; idx += blockDim.x) {
         const int m = idx / MT;
         const int b = idx - m * MT;
