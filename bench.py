@@ -383,6 +383,22 @@ def fp64_gemm_peak(torch):
     return 2 * 8192 ** 3 / (best * 1e-3) / 1e12
 
 
+def aggregate_replicas(ms, ngal, world, device=None):
+    """Replica runs (one independent catalogue per rank): the job's step time is
+    the slowest rank's, and its throughput counts every rank's galaxies.
+    Returns (ms_max, ngal_total, galaxies/s); collective over the initialised
+    process group when world > 1 (NCCL on the GPUs, gloo in the CPU tests)."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        n = torch.tensor([float(ngal)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(n, op=dist.ReduceOp.SUM)
+        ms, ngal = float(t.item()), int(round(n.item()))
+    return ms, ngal, ngal / (ms * 1e-3)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -505,18 +521,13 @@ def main():
         dist.barrier()
     clk = clocks.stop()
     launches = capi.lib.sfb_launch_count() - l0
-    ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms, n_job, value = aggregate_replicas(e0.elapsed_time(e1) / args.steps, N, world, dev)
     stage_ms = (capi.C.c_double * 7)()
     stage_n = (capi.C.c_int64 * 7)()
     capi.check(capi.lib.sfb_get_stage_times(plan.handle, stage_ms, stage_n))
     capi.check(capi.lib.sfb_set_profiling(plan.handle, 0))
     stages = {nm: {"ms_per_step": stage_ms[i] / args.steps, "launches_per_step": stage_n[i] / args.steps}
               for i, nm in enumerate(capi.STAGES)}
-    value = N * world / (ms * 1e-3)
 
     if args.profile_case:
         if rank == 0:
@@ -544,6 +555,7 @@ def main():
     for _ in range(args.steps):
         host_step()
     e2e_s = (time.perf_counter() - t0) / args.steps
+    _, _, e2e_value = aggregate_replicas(e2e_s * 1e3, N, world, dev)
     h2d = 8 * (3 * N + N + mask.size + wln.size)
     d2h = 16 * nlmsize
     res_dev = d_out.cpu().numpy()
@@ -577,11 +589,11 @@ def main():
             step64()
         f1.record(stream)
         torch.cuda.synchronize()
-        ms64 = f0.elapsed_time(f1) / args.steps
+        ms64, _, value64 = aggregate_replicas(f0.elapsed_time(f1) / args.steps, N, world, dev)
         step()
         torch.cuda.synchronize()
         a_mix, a_64 = d_out.cpu().numpy(), d_out64.cpu().numpy()
-        vs64 = {"fp64_value": N * world / (ms64 * 1e-3), "fp64_ms_per_step": ms64, "speedup": ms64 / ms,
+        vs64 = {"fp64_value": value64, "fp64_ms_per_step": ms64, "speedup": ms64 / ms,
                 "rel_err": float(np.linalg.norm(a_mix - a_64) / np.linalg.norm(a_64)),
                 "rel_err_definition": "||a_mixed - a_fp64||_2 / ||a_fp64||_2 over the a_nlm vector"}
 
@@ -633,7 +645,7 @@ def main():
                            "l2": "inputs (320 MB) and maps larger than L2; no flush",
                            "parallelism": "replicas" if world > 1 else "single"},
                 "roofline": roof, "cpu_baseline": cpu,
-                "e2e": {"value": N / e2e_s, "unit": "galaxies/s", "h2d_bytes_per_step": int(h2d),
+                "e2e": {"value": e2e_value, "unit": "galaxies/s", "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(d2h), "host_vs_device_result_rel_diff": same},
                 "mixed_vs_fp64": vs64,
                 "stages": stages, "stage_roofline": table, "clocks": clk, "gpu_launches": int(launches)}
