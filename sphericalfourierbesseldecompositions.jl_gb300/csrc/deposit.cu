@@ -16,10 +16,14 @@
 // Summation order inside a bin follows the int-atomic ranks, so repeated
 // calls agree to rounding, not bit for bit.
 //
-// Mixed precision stores the maps in FP32.  With a reference angular map C,
-// each map is written as the fluctuation D_b - mu_b C, with
-// mu_b = <D_b, C> / <C, C> estimated in FP64 on every STATS_STRIDE-th group
-// of 32 bins; the caller adds mu_b C_lm back in FP64 after the transform.
+// Mixed precision runs no FP64 instruction per galaxy (integer range tests and
+// double-float splits; the records are double-float pairs) and stores the
+// maps in FP32.  With a reference angular map C, each map is written as the
+// fluctuation D_b - mu_b C, with mu_b = <D_b, C> / <C, C> estimated in
+// double-float (sums in FP64) on every STATS_STRIDE-th group of 32 bins; the
+// caller adds mu_b C_lm back in FP64 after the transform.  Rings holding no
+// galaxy are then left unwritten (ring_live), their readers treating them as
+// zero.
 // C is the weighted galaxy count map of all radial slots, so it carries the
 // mean density and the survey boundary exactly as the galaxies sample them
 // (a pixelised mask misses the partly covered boundary pixels).  The FP32
