@@ -33,6 +33,11 @@
 // accumulators (4 x 128 columns).  Every mbarrier wait is bounded; on timeout
 // the CTA records ERR_TC_TIMEOUT, waits for its MMAs (bounded again),
 // releases TMEM and returns.
+//
+// Survey footprint: rows that are zero (rings outside the survey, marked by
+// the row-exponent pass with ZERO_ROW_E) are never read.  A tile with no live
+// row writes zero spectra without MMAs.  Two tiles whose southern rows are all
+// zero run as one tile of 128 northern rows (F+ = F- = F_N).  Both are exact.
 #include <cuda_bf16.h>
 
 #include <cmath>
