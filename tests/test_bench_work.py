@@ -1,0 +1,78 @@
+"""The algorithmic work bench.py reports: the rings holding galaxies
+(`sky_rings`, with the oracle's ang2pix standing in for the GPU one) and the
+per-stage counts built on them (`stage_work`)."""
+
+import importlib.util
+import os
+import types
+
+import numpy as np
+import pytest
+
+from oracle import healpix as oh
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _bench():
+    spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(ROOT, "bench.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+STUB = types.SimpleNamespace(ang2pix_ring=lambda ns, th, ph: np.asarray(oh.ang2pix_ring(ns, th, ph)))
+
+
+def _ring_lengths(ns):
+    return np.array([4 * i if i < ns else (4 * ns if i <= 3 * ns else 4 * (4 * ns - i)) for i in range(1, 4 * ns)])
+
+
+@pytest.mark.parametrize("ns", [4, 16])
+def test_sky_rings_full_sky(ns):
+    b = _bench()
+    rng = np.random.default_rng(ns)
+    n = 200 * 12 * ns * ns
+    th, ph = np.arccos(rng.uniform(-1, 1, n)), rng.uniform(0, 2 * np.pi, n)
+    pix, rings, live = b.sky_rings(STUB, ns, th, ph)
+    assert pix == 12 * ns * ns and live == 12 * ns * ns and rings == 4 * ns - 1
+
+
+def test_sky_rings_cap_and_band():
+    b = _bench()
+    ns = 16
+    lens = _ring_lengths(ns)
+    rng = np.random.default_rng(3)
+    # northern cap z > 0.5: rings counted from the pixels the galaxies fall in
+    th, ph = np.arccos(rng.uniform(0.5, 1, 200_000)), rng.uniform(0, 2 * np.pi, 200_000)
+    pix, rings, live = b.sky_rings(STUB, ns, th, ph)
+    gp = np.asarray(oh.ang2pix_ring(ns, th, ph))
+    starts = np.concatenate([[0], np.cumsum(lens)])
+    ring_of = np.searchsorted(starts, gp, side="right") - 1          # 0-based ring of each galaxy
+    used = np.unique(ring_of)
+    assert live == lens[used].sum()
+    k = used.max() + 1                                                # pairs 0 .. k-1 (all northern)
+    assert rings == 2 * k and pix == 2 * lens[:k].sum()
+    # a band |z| < 0.3: the span starts past the pole
+    th = np.arccos(rng.uniform(-0.3, 0.3, 200_000))
+    pix, rings, live = b.sky_rings(STUB, ns, th, ph)
+    ring_of = np.searchsorted(starts, np.asarray(oh.ang2pix_ring(ns, th, ph)), side="right") - 1
+    pairs = np.unique(np.minimum(ring_of, 4 * ns - 2 - ring_of))
+    lo, hi = pairs.min(), pairs.max()
+    assert rings == 2 * (hi - lo + 1) - (1 if hi == 2 * ns - 1 else 0)
+    assert live == lens[np.unique(ring_of)].sum()
+
+
+def test_stage_work_counts_the_rings_with_data():
+    b = _bench()
+    nm, ngal, nbasis = 328, 10_000_000, 327
+    npix = 12 * b.NSIDE ** 2
+    sky = (npix // 2, 640, npix // 4)
+    full = dict((st, b.stage_work(st, "mixed", nm, ngal, nbasis)) for st in ("deposit", "leg_analysis"))
+    part = dict((st, b.stage_work(st, "mixed", nm, ngal, nbasis, sky=sky)) for st in ("deposit", "leg_analysis"))
+    assert part["deposit"][1] == pytest.approx(40.0 * ngal + 4.0 * nbasis * npix / 4)
+    assert full["deposit"][1] == pytest.approx(40.0 * ngal + 4.0 * nbasis * npix)
+    assert part["leg_analysis"][1] < full["leg_analysis"][1]
+    # the FP64 path computes every ring: the sky does not change its counts
+    assert b.stage_work("deposit", "fp64", nm, ngal, nbasis, sky=sky) == b.stage_work("deposit", "fp64", nm, ngal,
+                                                                                       nbasis)
