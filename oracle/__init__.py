@@ -1,6 +1,7 @@
 """CPU oracle for the catalogue -> SFB coefficient path.  TEST INFRASTRUCTURE.
 
-This package is the checker, not the product.  Only the test-suite, the
+This package is the oracle the GPU results are tested against, not the
+product.  Only the test-suite, the
 ``smoke()`` check and the ``cpu_baseline`` / ``--impl reference`` legs of the
 benchmark import it.  Nothing in the shipped library calls it.
 
