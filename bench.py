@@ -70,6 +70,71 @@ def make_catalogue(seed=2):
     return np.ascontiguousarray(np.stack([r, th, ph], axis=1)), w    # (N, 3) = Julia 3xN memory
 
 
+# the reference's CPU-runnable configuration: full sky, r ~ r^2, unit weights
+C1 = dict(kmax=0.05, rmin=500.0, rmax=1000.0, nside=32, nr=250, ngal=200_000)
+C1_WORKLOAD = "cat2amln kmax=0.05 rmin=500 rmax=1000 nside=32 nr=250 N=2e5 full sky r~r^2 w=1 (C1)"
+
+
+def c1_catalogue(seed=1):
+    """N = 2e5, r = (rmin^3 + u (rmax^3 - rmin^3))^(1/3), cos(theta) ~ U[-1, 1], phi ~ U[0, 2 pi)."""
+    rng = np.random.default_rng(seed)
+    n, a, b = C1["ngal"], C1["rmin"], C1["rmax"]
+    r = np.cbrt(a ** 3 + rng.random(n) * (b ** 3 - a ** 3))
+    th = np.arccos(rng.uniform(-1.0, 1.0, n))
+    ph = rng.uniform(0.0, 2 * np.pi, n)
+    return np.ascontiguousarray(np.stack([r, th, ph], axis=1)), np.ones(n)
+
+
+def c1_setup(sfbgpu):
+    """AnlmModes, catalogue, window (full-sky constant) and nbar = N / V of C1."""
+    amodes = sfbgpu.AnlmModes(C1["kmax"], C1["rmin"], C1["rmax"], nside=C1["nside"])
+    gal, w = c1_catalogue()
+    wm = sfbgpu.ConfigurationSpaceModes(C1["rmin"], C1["rmax"], C1["nr"], C1["nside"])
+    phi, mask = np.ones(wm.nr), np.ones(wm.npix)
+    nbar = gal.shape[0] / (4 * np.pi / 3 * (C1["rmax"] ** 3 - C1["rmin"] ** 3))
+    return amodes, gal, w, wm, phi, mask, nbar
+
+
+def c1_cpu_full(sfbgpu, workers, runs=3):
+    """The reference algorithm on the whole C1 catalogue (every (n,l) pair, no
+    extrapolation) on `workers` host processes: median galaxies/s of `runs` calls."""
+    from oracle import sfb as osfb
+    amodes, gal, w, wm, phi, mask, nbar = c1_setup(sfbgpu)
+    md = dict(nmax=amodes.nmax, lmax=amodes.lmax, lmax_n=[int(v) for v in amodes.lmax_n], nside=C1["nside"],
+              splines=amodes.basisfunctions.spline, noff=amodes._noff)
+    _, wln = osfb.win_rhat_ln_separable(phi, mask, C1["rmin"], C1["rmax"], C1["nr"], md)
+    npairs = len(amodes.pairs())
+    vals, t_setup = run_reference_sample(amodes, gal, w, nbar, mask, wln, runs, 1, workers, npairs,
+                                         nside=C1["nside"])
+    v = float(np.median(vals))
+    return {"value": v, "unit": "galaxies/s", "cores": workers, "kind": "port", "runs": runs,
+            "ms_per_call": gal.shape[0] / v * 1e3, "workload": C1_WORKLOAD,
+            "sample": f"the whole C1 call: all {npairs} (n,l) pairs (spline scatter + niter=3 map2alm each) on "
+                      f"{workers} processes plus the sort/ang2pix ({t_setup:.2f} s); median of {runs} calls after "
+                      f"one warm-up"}
+
+
+def c1_gpu(sfbgpu, steps=10, warmup=3):
+    """C1 through the public host-pointer call (copies included), mixed and FP64,
+    with the mixed path's errors against the FP64 one."""
+    amodes, gal, w, wm, phi, mask, nbar = c1_setup(sfbgpu)
+    rtp = gal.T
+    out, res = {"workload": C1_WORKLOAD, "ngal": int(gal.shape[0])}, {}
+    for prec in ("mixed", "fp64"):
+        win = sfbgpu.win_rhat_ln(sfbgpu.SeparableArray(phi, mask, "phi", "mask"), wm, amodes, precision=prec,
+                                 radial="poly")
+        for _ in range(warmup):
+            sfbgpu.cat2amln(rtp, amodes, nbar, win, None, precision=prec, radial="poly")
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            res[prec] = sfbgpu.cat2amln(rtp, amodes, nbar, win, None, precision=prec, radial="poly")
+        dt = (time.perf_counter() - t0) / steps
+        out[prec] = {"value": gal.shape[0] / dt, "unit": "galaxies/s", "ms_per_call": dt * 1e3,
+                     "timing": f"host wall clock over {steps} calls of sfb_cat2amln (host buffers, copies inside)"}
+    out["mixed_vs_fp64"] = error_report(res["mixed"], res["fp64"])
+    return out
+
+
 def window_arrays(sfbgpu, amodes):
     wm = sfbgpu.ConfigurationSpaceModes(RMIN, RMAX, NR, NSIDE)
     phi = np.exp(-(wm.r - RMEAN) ** 2 / (2 * RSIG ** 2))
@@ -164,8 +229,9 @@ def _ref_worker_pair(args):
 
 
 def run_reference_sample(amodes, gal, w, nbar, mask, wln_arr, steps, warmup, workers, pairs_per_step,
-                         emit=True, config=None):
-    """Time the CPU reference algorithm on a sample of (n,l) pairs; returns galaxies/s per step."""
+                         nside=NSIDE):
+    """Time the CPU reference algorithm on a sample of (n,l) pairs (all of them when
+    pairs_per_step is the pair count); returns galaxies/s per step."""
     import multiprocessing as mp
     from concurrent.futures import ProcessPoolExecutor
     from multiprocessing import shared_memory
@@ -175,7 +241,7 @@ def run_reference_sample(amodes, gal, w, nbar, mask, wln_arr, steps, warmup, wor
     t0 = time.perf_counter()
     p = np.argsort(gal[:, 0], kind="stable")
     r = np.ascontiguousarray(gal[p, 0])
-    pix = ohp.ang2pix_ring(NSIDE, gal[p, 1], gal[p, 2])
+    pix = ohp.ang2pix_ring(nside, gal[p, 1], gal[p, 2])
     ws = np.ascontiguousarray(w[p])
     t_setup = time.perf_counter() - t0
     shms = {}
@@ -189,7 +255,7 @@ def run_reference_sample(amodes, gal, w, nbar, mask, wln_arr, steps, warmup, wor
     vals = []
     try:
         with ProcessPoolExecutor(workers, mp_context=ctx, initializer=_ref_worker_init,
-                                 initargs=({k: s.name for k, s in shms.items()}, N, amodes.lmax, NSIDE)) as ex:
+                                 initargs=({k: s.name for k, s in shms.items()}, N, amodes.lmax, nside)) as ex:
             list(ex.map(_ref_worker_pair, [(pairs[0], spl[pairs[0]], nbar, mask, wln_arr[0, 0])] * workers))
             for step in range(warmup + steps):
                 idx = np.linspace(0, len(pairs) - 1, pairs_per_step).astype(int)
@@ -383,6 +449,35 @@ def fp64_gemm_peak(torch):
     return 2 * 8192 ** 3 / (best * 1e-3) / 1e12
 
 
+PER_MODE_FLOOR = 1e-2        # per-mode relative errors over |a_fp64| >= this x max|a_fp64|
+MAX_NORM_BAR = 1e-7
+
+
+def error_report(a, ref, floor=PER_MODE_FLOOR):
+    """Errors of the mixed a_nlm against the FP64 ones (complex vectors):
+    L2 relative, global max-norm max|da| / max|a|, absolute max / rms, and the
+    per-mode relative error |da_i| / |a_i| over the modes whose magnitude is at
+    least `floor` times the largest (the relative error of near-zero modes is
+    not meaningful)."""
+    a = np.asarray(a)
+    ref = np.asarray(ref)
+    d = np.abs(a - ref)
+    mag = np.abs(ref)
+    amax = float(mag.max())
+    sel = mag >= floor * amax
+    rel = d[sel] / mag[sel]
+    q = np.quantile(rel, [0.5, 0.99, 0.999]) if rel.size else [float("nan")] * 3
+    mx = float(d.max() / amax)
+    return {"l2": float(np.linalg.norm(a - ref) / np.linalg.norm(ref)), "max_norm": mx,
+            "max_norm_bar": MAX_NORM_BAR, "max_norm_met": bool(mx <= MAX_NORM_BAR),
+            "abs_max": float(d.max()), "abs_rms": float(np.sqrt(np.mean(d * d))), "max_abs_a": amax,
+            "per_mode": {"floor_frac_of_max": floor, "modes": int(sel.sum()), "of": int(d.size),
+                         "max": float(rel.max()) if rel.size else None, "median": float(q[0]),
+                         "p99": float(q[1]), "p999": float(q[2])},
+            "definitions": "l2 = ||da||_2/||a||_2; max_norm = max|da|/max|a|; per_mode = |da_i|/|a_i| over "
+                           "|a_i| >= floor x max|a|"}
+
+
 def aggregate_replicas(ms, ngal, world, device=None):
     """Replica runs (one independent catalogue per rank): the job's step time is
     the slowest rank's, and its throughput counts every rank's galaxies.
@@ -409,6 +504,7 @@ def main():
     ap.add_argument("--no-fp64-leg", action="store_true", help="skip timing the FP64 path beside the mixed one")
     ap.add_argument("--ngal", type=int, default=0, help="override the catalogue size (testing)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-c1", action="store_true", help="skip the C1 (nside 32) GPU timings")
     ap.add_argument("--cpu-workers", type=int, default=0)
     ap.add_argument("--cpu-pairs", type=int, default=0)
     ap.add_argument("--profile-case", action="store_true",
@@ -421,6 +517,7 @@ def main():
     if args.profile_case:
         args.ngal = args.ngal or 1_000_000
         args.no_cpu_baseline = True
+        args.no_c1 = True
         plan_extra = {"pieces": 2, "degree": 15}
 
     rank = int(os.environ.get("RANK", "0"))
@@ -457,7 +554,8 @@ def main():
                 "cpu_baseline": {"value": v, "unit": "galaxies/s", "cores": workers, "kind": "port",
                                  "sample": f"{ppst} of {len(amodes.pairs())} (n,l) pairs per step (spline scatter "
                                            f"+ niter=3 map2alm each) on {workers} processes, extrapolated by pair "
-                                           f"count, plus the once-per-call sort/ang2pix ({t_setup:.2f} s)"},
+                                           f"count, plus the once-per-call sort/ang2pix ({t_setup:.2f} s)",
+                                 "c1_full": c1_cpu_full(sfbgpu, workers)},
                 "e2e": {"value": v, "unit": "galaxies/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
@@ -564,38 +662,60 @@ def main():
     # the metric compares the mixed path with the FP64 GPU path on the same catalogue
     vs64 = None
     if args.precision == "mixed" and not args.no_fp64_leg:
-        plan64 = sfbgpu.get_plan(amodes, precision="fp64", radial="poly", **plan_extra)
         wln64 = np.asfortranarray(sfbgpu.win_rhat_ln(sfbgpu.SeparableArray(phi, mask, "phi", "mask"), wm, amodes,
                                                      precision="fp64", radial="poly", **plan_extra).w_ln)
         d_wln64 = torch.from_numpy(np.ascontiguousarray(wln64.T)).to(dev)
-        d_out64 = torch.empty_like(d_out)
         win64 = capi.Window()
         win64.kind = capi.SFB_WINDOW_SEPARABLE
         win64.mask = capi.C.cast(d_mask.data_ptr(), capi._dp)
         win64.w_ln = capi.C.cast(d_wln64.data_ptr(), capi._dp)
 
-        def step64():
-            capi.check(capi.lib.sfb_cat2amln_device(plan64.handle, capi.C.c_void_p(d_gal.data_ptr()),
-                                                    capi.C.c_void_p(d_w.data_ptr()), N, float(nbar),
-                                                    capi.C.byref(win64), capi.C.c_void_p(d_out64.data_ptr()),
-                                                    capi.C.c_void_p(stream.cuda_stream)))
-        for _ in range(args.warmup):
-            step64()
-        torch.cuda.synchronize()
-        f0 = torch.cuda.Event(enable_timing=True)
-        f1 = torch.cuda.Event(enable_timing=True)
-        f0.record(stream)
-        for _ in range(args.steps):
-            step64()
-        f1.record(stream)
-        torch.cuda.synchronize()
-        ms64, _, value64 = aggregate_replicas(f0.elapsed_time(f1) / args.steps, N, world, dev)
+        def time_fp64(plan64, d_res, steps):
+            def step64():
+                capi.check(capi.lib.sfb_cat2amln_device(plan64.handle, capi.C.c_void_p(d_gal.data_ptr()),
+                                                        capi.C.c_void_p(d_w.data_ptr()), N, float(nbar),
+                                                        capi.C.byref(win64), capi.C.c_void_p(d_res.data_ptr()),
+                                                        capi.C.c_void_p(stream.cuda_stream)))
+            for _ in range(args.warmup):
+                step64()
+            torch.cuda.synchronize()
+            f0 = torch.cuda.Event(enable_timing=True)
+            f1 = torch.cuda.Event(enable_timing=True)
+            f0.record(stream)
+            for _ in range(steps):
+                step64()
+            f1.record(stream)
+            torch.cuda.synchronize()
+            return aggregate_replicas(f0.elapsed_time(f1) / steps, N, world, dev)
+
+        # (1) the same algorithm as the mixed path (Gram refinement, first pass over the rings with data)
+        plan64 = sfbgpu.get_plan(amodes, precision="fp64", radial="poly", **plan_extra)
+        d_out64 = torch.empty_like(d_out)
+        ms64, _, value64 = time_fp64(plan64, d_out64, args.steps)
+        # (2) the FP64 path with full synthesis / fold / analysis refinement passes over every ring
+        os.environ["SFBGPU_GRAM_REFINEMENT"] = "0"
+        try:
+            plan64f = sfbgpu.GPUPlan(amodes, precision="fp64", radial="poly", **plan_extra)
+        finally:
+            os.environ.pop("SFBGPU_GRAM_REFINEMENT", None)
+        d_out64f = torch.empty_like(d_out)
+        ms64f, _, value64f = time_fp64(plan64f, d_out64f, min(args.steps, 5))
+        plan64f.close()
         step()
         torch.cuda.synchronize()
-        a_mix, a_64 = d_out.cpu().numpy(), d_out64.cpu().numpy()
+        a_mix, a_64, a_64f = (x.cpu().numpy().view(np.complex128) for x in (d_out, d_out64, d_out64f))
         vs64 = {"fp64_value": value64, "fp64_ms_per_step": ms64, "speedup": ms64 / ms,
+                "fp64_algorithm": "same as the mixed path: Gram refinement of the alias-free rings, first "
+                                  "analysis pass over the ring pairs with data",
+                "errors": error_report(a_mix, a_64),
                 "rel_err": float(np.linalg.norm(a_mix - a_64) / np.linalg.norm(a_64)),
-                "rel_err_definition": "||a_mixed - a_fp64||_2 / ||a_fp64||_2 over the a_nlm vector"}
+                "rel_err_definition": "||a_mixed - a_fp64||_2 / ||a_fp64||_2 over the a_nlm vector",
+                "fp64_full_passes": {"value": value64f, "ms_per_step": ms64f, "speedup": ms64f / ms,
+                                     "steps": min(args.steps, 5),
+                                     "algorithm": "FP64 with full synthesis / fold / analysis refinement "
+                                                  "passes over all rings (no Gram refinement, no ring span)",
+                                     "rel_diff_vs_fp64": float(np.linalg.norm(a_64f - a_64) /
+                                                               np.linalg.norm(a_64))}}
 
     # roofline of every stage; the headline is the dominant one
     nm = info["nbasis"] + 1
@@ -632,7 +752,11 @@ def main():
         cpu = {"value": float(vals[0]), "unit": "galaxies/s", "cores": workers, "kind": "port",
                "sample": f"{ppst} of {len(amodes.pairs())} (n,l) pairs (spline scatter + niter=3 map2alm each) on "
                          f"{workers} processes, extrapolated by pair count, plus the once-per-call sort/ang2pix "
-                         f"({t_setup:.2f} s)"}
+                         f"({t_setup:.2f} s)",
+               "c1_full": c1_cpu_full(sfbgpu, workers)}
+    c1 = c1_gpu(sfbgpu) if (rank == 0 and world == 1 and not args.no_c1) else None
+    if c1 and cpu:
+        c1["mixed"]["vs_cpu_c1_full"] = c1["mixed"]["value"] / cpu["c1_full"]["value"]
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "galaxies/s", "n_gpus": world, "steps": args.steps,
@@ -647,7 +771,7 @@ def main():
                 "roofline": roof, "cpu_baseline": cpu,
                 "e2e": {"value": e2e_value, "unit": "galaxies/s", "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(d2h), "host_vs_device_result_rel_diff": same},
-                "mixed_vs_fp64": vs64,
+                "mixed_vs_fp64": vs64, "c1": c1,
                 "stages": stages, "stage_roofline": table, "clocks": clk, "gpu_launches": int(launches)}
         print(json.dumps(line), flush=True)
     if world > 1:

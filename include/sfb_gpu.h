@@ -38,6 +38,12 @@ typedef enum {
     SFB_MIXED = 1        /* FP64 binning/tables/window term, FP32 ring FFT, tensor-core contractions */
 } sfb_precision;
 
+/* Element type of a shell x pixel field (sfb_field2anlm_typed and its VJP). */
+typedef enum {
+    SFB_F64 = 0,         /* double (Julia Matrix{Float64}) */
+    SFB_F32 = 1          /* float (Julia Matrix{Float32}) */
+} sfb_dtype;
+
 typedef enum {
     /* Galaxy radii enter through a piecewise-Legendre expansion of every
      * g_nl spline (projection error below radial_tol); the spherical-harmonic
@@ -156,6 +162,23 @@ int sfb_map2alm_adjoint(sfb_plan *plan, const double *abar, int64_t nmaps, doubl
 int sfb_field2anlm(sfb_plan *plan, const double *f, int64_t nr, double rmin, double rmax,
                    double *anlm_out);
 
+/* field2anlm with the field's element type given (reference field2anlm_v2,
+ * src/cat2anlm.jl:323-357, whose field may be any real matrix): f is
+ * [nr * npix] elements of `dtype` (sfb_dtype), element (ir, p) at ir + nr*p.
+ * An FP32 field is read as it is (no FP64 copy on the host or the device; the
+ * mixed-precision transform takes its shells directly).  The field is held on
+ * the device when it fits (SFBGPU_FIELD_MAX_BYTES at plan creation, else half
+ * of the free device memory); a larger field streams through the device one
+ * chunk of shells at a time. */
+int sfb_field2anlm_typed(sfb_plan *plan, const void *f, int32_t dtype, int64_t nr, double rmin, double rmax,
+                         double *anlm_out);
+
+/* dL/df of sfb_field2anlm_typed written as `dtype` elements (df_out [nr * npix],
+ * element (ir, p) at ir + nr*p), with the same shell streaming.  No counterpart
+ * in the reference (its transforms have no derivatives). */
+int sfb_field2anlm_vjp_typed(sfb_plan *plan, const double *abar, int64_t nr, double rmin, double rmax,
+                             void *df_out, int32_t dtype);
+
 /* anlm2field(f_nlm, wmodes, amodes) (reference src/cat2anlm.jl:383-422).
  * anlm: [2*nlmsize] interleaved complex; f_out: [nr * npix], element (ir,p) at ir + nr*p. */
 int sfb_anlm2field(sfb_plan *plan, const double *anlm, int64_t nr, double rmin, double rmax,
@@ -202,7 +225,12 @@ int sfb_winweights2galweights(int64_t nside, const double *weights, int64_t nr, 
  * allocate mid-pipeline.  Limit: nr*npix + nr + 1 <= 2080736 doubles
  * (e.g. nside 64 with nr <= 42), else SFB_EINVAL.  The first call on a
  * device does its set-up (device address lookup) and should come before any
- * stream capture.  Calls on one device are serialised inside the library. */
+ * stream capture.  Calls on one device are serialised inside the library.
+ * The call is synchronous: its copies and its kernel run on the legacy
+ * default stream, so it waits for, and holds up, work on every blocking
+ * stream of the process.  The device address found at set-up is kept for the
+ * life of the process; after a cudaDeviceReset of that device it is stale,
+ * and such a process must not call this entry point again. */
 int sfb_winweights2galweights_noalloc(int64_t nside, const double *weights, int64_t nr,
                                       const double *rbounds, const double *rtp, int64_t ngal,
                                       double *w_out);

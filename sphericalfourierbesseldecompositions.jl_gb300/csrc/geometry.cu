@@ -92,9 +92,10 @@ void launch_transpose(const double *in, int64_t rows, int64_t cols, double *out,
     note_launch();
 }
 
-// out[c * ldo + r] = in[r * ldi + c] for r < rows, c < cols.
-__global__ void k_transpose_ld(const double *in, int64_t ldi, int64_t rows, int64_t cols, double *out, int64_t ldo) {
-    __shared__ double tile[32][33];
+// out[c * ldo + r] = in[r * ldi + c] for r < rows, c < cols (converted to TO).
+template <typename TI, typename TO>
+__global__ void k_transpose_ld(const TI *in, int64_t ldi, int64_t rows, int64_t cols, TO *out, int64_t ldo) {
+    __shared__ TI tile[32][33];
     const int64_t c0 = (int64_t)blockIdx.x * 32, r0 = (int64_t)blockIdx.y * 32;
     for (int j = threadIdx.y; j < 32; j += 8) {
         const int64_t r = r0 + j, c = c0 + threadIdx.x;
@@ -103,16 +104,34 @@ __global__ void k_transpose_ld(const double *in, int64_t ldi, int64_t rows, int6
     __syncthreads();
     for (int j = threadIdx.y; j < 32; j += 8) {
         const int64_t c = c0 + j, r = r0 + threadIdx.x;
-        if (r < rows && c < cols) out[c * ldo + r] = tile[threadIdx.x][j];
+        if (r < rows && c < cols) out[c * ldo + r] = (TO)tile[threadIdx.x][j];
     }
+}
+
+template <typename TI, typename TO>
+static void transpose_ld(const TI *in, int64_t ldi, int64_t rows, int64_t cols, TO *out, int64_t ldo,
+                         cudaStream_t st) {
+    if (rows <= 0 || cols <= 0) return;
+    dim3 grid((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32));
+    k_transpose_ld<TI, TO><<<grid, dim3(32, 8), 0, st>>>(in, ldi, rows, cols, out, ldo);
+    note_launch();
 }
 
 void launch_transpose_ld(const double *in, int64_t ldi, int64_t rows, int64_t cols, double *out, int64_t ldo,
                          cudaStream_t st) {
-    if (rows <= 0 || cols <= 0) return;
-    dim3 grid((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32));
-    k_transpose_ld<<<grid, dim3(32, 8), 0, st>>>(in, ldi, rows, cols, out, ldo);
-    note_launch();
+    transpose_ld(in, ldi, rows, cols, out, ldo, st);
+}
+void launch_transpose_ld(const float *in, int64_t ldi, int64_t rows, int64_t cols, double *out, int64_t ldo,
+                         cudaStream_t st) {
+    transpose_ld(in, ldi, rows, cols, out, ldo, st);
+}
+void launch_transpose_ld(const float *in, int64_t ldi, int64_t rows, int64_t cols, float *out, int64_t ldo,
+                         cudaStream_t st) {
+    transpose_ld(in, ldi, rows, cols, out, ldo, st);
+}
+void launch_transpose_ld(const double *in, int64_t ldi, int64_t rows, int64_t cols, float *out, int64_t ldo,
+                         cudaStream_t st) {
+    transpose_ld(in, ldi, rows, cols, out, ldo, st);
 }
 
 __global__ void k_check_finite(const double *x, int64_t n, int *err) {

@@ -25,10 +25,14 @@ __device__ __forceinline__ int nrows_of(int m, int par, int lmax) {
 }
 }  // namespace
 
+// Ring range of the sum: rings r < rlim; with nzr, only the ring pairs
+// [nzr[0], nzr[1]] (F is zero outside them: the ring transform recorded the
+// span of ring pairs holding data; an empty span sums nothing).
 template <typename T>
 __global__ void __launch_bounds__(256) k_leg_analysis(const T *__restrict__ lam, const int64_t *lam_off,
                                                       int lmax, int nrn, const T *__restrict__ F,
-                                                      int64_t ncol, T *__restrict__ A, int accumulate) {
+                                                      int64_t ncol, T *__restrict__ A, int accumulate, int rlim,
+                                                      const int *__restrict__ nzr) {
     const int z = blockIdx.z;
     const int m = z >> 1, par = z & 1;
     const int nrows = nrows_of(m, par, lmax);
@@ -41,18 +45,24 @@ __global__ void __launch_bounds__(256) k_leg_analysis(const T *__restrict__ lam,
     __shared__ T Bs[BK][BN];
     const int tid = threadIdx.x;
     const int tx = tid & 15, ty = tid >> 4;
+    int kend = min(rlim, nrn), kbeg = 0;
+    if (nzr) {
+        const int lo = nzr[0], hi = nzr[1];
+        kend = min(kend, hi + 1);
+        kbeg = lo < kend ? (lo / BK) * BK : kend;
+    }
     T acc[4][4] = {};
-    for (int k0 = 0; k0 < nrn; k0 += BK) {
+    for (int k0 = kbeg; k0 < kend; k0 += BK) {
         for (int i = tid; i < BM * BK; i += 256) {
             const int rr = i / BK, kk = i % BK;
             const int row = row0 + rr, k = k0 + kk;
-            As[kk][rr] = (row < nrows && k < nrn) ? L[(int64_t)row * nrn + k] : T(0);
+            As[kk][rr] = (row < nrows && k < kend) ? L[(int64_t)row * nrn + k] : T(0);
         }
         for (int i = tid; i < BK * BN; i += 256) {
             const int kk = i / BN, cc = i % BN;
             const int k = k0 + kk;
             const int64_t col = col0 + cc;
-            Bs[kk][cc] = (k < nrn && col < ncol) ? B[(int64_t)k * ncol + col] : T(0);
+            Bs[kk][cc] = (k < kend && col < ncol) ? B[(int64_t)k * ncol + col] : T(0);
         }
         __syncthreads();
 #pragma unroll
@@ -85,15 +95,16 @@ __global__ void __launch_bounds__(256) k_leg_analysis(const T *__restrict__ lam,
     }
 }
 
+// Only the rings r < rlim are formed.
 template <typename T>
 __global__ void __launch_bounds__(256) k_leg_synthesis(const T *__restrict__ lam, const int64_t *lam_off,
                                                        int lmax, int nrn, const T *__restrict__ A,
-                                                       int64_t ncol, T *__restrict__ G) {
+                                                       int64_t ncol, T *__restrict__ G, int rlim) {
     const int z = blockIdx.z;
     const int m = z >> 1, par = z & 1;
     const int nrows = nrows_of(m, par, lmax);   // K dimension
     const int r0 = blockIdx.y * BM;
-    if (r0 >= nrn) return;
+    if (r0 >= rlim) return;
     const int64_t col0 = (int64_t)blockIdx.x * BN;
     const T *L = lam + lam_off[z];
     __shared__ T As[BK][BM + 1];
@@ -137,7 +148,7 @@ __global__ void __launch_bounds__(256) k_leg_synthesis(const T *__restrict__ lam
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         const int r = r0 + ty * 4 + i;
-        if (r >= nrn) continue;
+        if (r >= rlim) continue;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const int64_t col = col0 + tx + 16 * j;
@@ -325,8 +336,75 @@ __global__ void __launch_bounds__(128) k_gram_update_fp64(const double *__restri
     Anew[o] = Acur[o] + (A0[o] - acc);
 }
 
+// Many columns: the same update as a tiled GEMM per block z (output rows r x
+// columns, K = the rows li), with the update in the epilogue.
+__global__ void __launch_bounds__(256) k_gram_update_wide(const double *__restrict__ gram,
+                                                          const int64_t *__restrict__ gram_off, int R, int lmax,
+                                                          const double *__restrict__ Acur,
+                                                          const double *__restrict__ A0, int64_t ncol,
+                                                          double *__restrict__ Anew) {
+    const int z = blockIdx.z;
+    const int m = z >> 1, par = z & 1;
+    const int nrows = nrows_of(m, par, lmax);
+    const int r0 = blockIdx.y * BM;
+    if (r0 >= nrows) return;
+    const int64_t col0 = (int64_t)blockIdx.x * BN;
+    const double *M = gram + gram_off[z];
+    __shared__ double As[BK][BM + 1];
+    __shared__ double Bs[BK][BN];
+    const int tid = threadIdx.x;
+    const int tx = tid & 15, ty = tid >> 4;
+    double acc[4][4] = {};
+    for (int k0 = 0; k0 < nrows; k0 += BK) {
+        for (int i = tid; i < BM * BK; i += 256) {
+            const int kk = i / BM, rr = i % BM;
+            const int k = k0 + kk, r = r0 + rr;
+            As[kk][rr] = (k < nrows && r < nrows) ? M[(int64_t)k * R + r] : 0.0;
+        }
+        for (int i = tid; i < BK * BN; i += 256) {
+            const int kk = i / BN, cc = i % BN;
+            const int k = k0 + kk;
+            const int64_t col = col0 + cc;
+            double v = 0.0;
+            if (k < nrows && col < ncol) {
+                const int l = m + par + 2 * k;
+                v = Acur[((int64_t)l * (l + 1) / 2 + m) * ncol + col];
+            }
+            Bs[kk][cc] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < BK; ++kk) {
+            double a[4], b[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) a[i] = As[kk][ty * 4 + i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int r = r0 + ty * 4 + i;
+        if (r >= nrows) continue;
+        const int l = m + par + 2 * r;
+        const int64_t base = ((int64_t)l * (l + 1) / 2 + m) * ncol;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int64_t col = col0 + tx + 16 * j;
+            if (col >= ncol) continue;
+            const int64_t o = base + col;
+            Anew[o] = Acur[o] + (A0[o] - acc[i][j]);
+        }
+    }
+}
+
 void launch_leg_analysis(const Plan &p, const double *F, int64_t ncol, double *A, bool accumulate,
-                         cudaStream_t st, int rlim) {
+                         cudaStream_t st, int rlim, const int *nzr) {
     const bool narrow = p.precision == SFB_MIXED
                             ? narrow_dispatch<float>(p, p.d_lam32, (const float *)F, ncol, (float *)A, true, accumulate, st,
                                                      rlim)
@@ -336,13 +414,14 @@ void launch_leg_analysis(const Plan &p, const double *F, int64_t ncol, double *A
         return;
     }
     const int maxrows = p.lmax / 2 + 1;
+    if (rlim < 0 || rlim > p.nrn) rlim = (int)p.nrn;
     dim3 grid((unsigned)((ncol + BN - 1) / BN), (unsigned)((maxrows + BM - 1) / BM), (unsigned)(2 * (p.lmax + 1)));
     if (p.precision == SFB_MIXED)
         k_leg_analysis<float><<<grid, 256, 0, st>>>(p.d_lam32, p.d_lam_off, p.lmax, (int)p.nrn, (const float *)F,
-                                                    ncol, (float *)A, accumulate ? 1 : 0);
+                                                    ncol, (float *)A, accumulate ? 1 : 0, rlim, nzr);
     else
         k_leg_analysis<double><<<grid, 256, 0, st>>>(p.d_lam, p.d_lam_off, p.lmax, (int)p.nrn, F, ncol, A,
-                                                     accumulate ? 1 : 0);
+                                                     accumulate ? 1 : 0, rlim, nzr);
     note_launch();
 }
 
@@ -355,12 +434,14 @@ void launch_leg_synthesis(const Plan &p, const double *A, int64_t ncol, double *
         note_launch();
         return;
     }
-    dim3 grid((unsigned)((ncol + BN - 1) / BN), (unsigned)((p.nrn + BM - 1) / BM), (unsigned)(2 * (p.lmax + 1)));
+    if (rlim < 0 || rlim > p.nrn) rlim = (int)p.nrn;
+    if (rlim == 0) return;
+    dim3 grid((unsigned)((ncol + BN - 1) / BN), (unsigned)((rlim + BM - 1) / BM), (unsigned)(2 * (p.lmax + 1)));
     if (p.precision == SFB_MIXED)
         k_leg_synthesis<float><<<grid, 256, 0, st>>>(p.d_lam32, p.d_lam_off, p.lmax, (int)p.nrn, (const float *)A,
-                                                     ncol, (float *)G);
+                                                     ncol, (float *)G, rlim);
     else
-        k_leg_synthesis<double><<<grid, 256, 0, st>>>(p.d_lam, p.d_lam_off, p.lmax, (int)p.nrn, A, ncol, G);
+        k_leg_synthesis<double><<<grid, 256, 0, st>>>(p.d_lam, p.d_lam_off, p.lmax, (int)p.nrn, A, ncol, G, rlim);
     note_launch();
 }
 
@@ -623,7 +704,11 @@ bool launch_gram_update_fp64(const Plan &p, const double *Acur, const double *A0
     case 2: k_gram_update_fp64<2><<<grid, 128, 0, st>>>(p.d_gram64, p.d_gram_off, p.gram_rows, p.lmax, Acur, A0, Anew); break;
     case 4: k_gram_update_fp64<4><<<grid, 128, 0, st>>>(p.d_gram64, p.d_gram_off, p.gram_rows, p.lmax, Acur, A0, Anew); break;
     case 8: k_gram_update_fp64<8><<<grid, 128, 0, st>>>(p.d_gram64, p.d_gram_off, p.gram_rows, p.lmax, Acur, A0, Anew); break;
-    default: return false;
+    default: {
+        dim3 wg((unsigned)((ncol + BN - 1) / BN), (unsigned)((maxrows + BM - 1) / BM), (unsigned)(2 * (p.lmax + 1)));
+        k_gram_update_wide<<<wg, 256, 0, st>>>(p.d_gram64, p.d_gram_off, p.gram_rows, p.lmax, Acur, A0, ncol, Anew);
+        break;
+    }
     }
     note_launch();
     return true;
@@ -665,6 +750,17 @@ void launch_fold_residual(const Plan &p, const double *F, const double *G, int64
         const double w = 4.0 * M_PI / (double)p.npix;
         k_fold_cols<float><<<grid, 128, 0, st>>>(p.d_rings, (int)p.nrn, rlim, p.lmax, w, (const float *)F,
                                                  (const float *)G, ncplx, (float *)R, Ecol);
+        note_launch();
+        return;
+    }
+    if (!F && ncplx > 4) {
+        // FP64 Gram refinement, many columns: the aliased-ring term over rings r < rlim
+        dim3 grid((unsigned)((ncplx + 127) / 128), (unsigned)(2 * (p.lmax + 1)),
+                  (unsigned)((rlim + FOLD_RC - 1) / FOLD_RC));
+        const double w = 4.0 * M_PI / (double)p.npix;
+        if (rlim > 0)
+            k_fold_cols<double><<<grid, 128, 0, st>>>(p.d_rings, (int)p.nrn, rlim, p.lmax, w, nullptr, G, ncplx, R,
+                                                      nullptr);
         note_launch();
         return;
     }

@@ -80,6 +80,12 @@ void launch_subtract_sep_chunk(const Plan &p, double *maps, const double *mask, 
                                int64_t npc, cudaStream_t st);
 void launch_transpose_ld(const double *in, int64_t ldi, int64_t rows, int64_t cols, double *out, int64_t ldo,
                          cudaStream_t st);
+void launch_transpose_ld(const float *in, int64_t ldi, int64_t rows, int64_t cols, double *out, int64_t ldo,
+                         cudaStream_t st);
+void launch_transpose_ld(const float *in, int64_t ldi, int64_t rows, int64_t cols, float *out, int64_t ldo,
+                         cudaStream_t st);
+void launch_transpose_ld(const double *in, int64_t ldi, int64_t rows, int64_t cols, float *out, int64_t ldo,
+                         cudaStream_t st);
 void launch_axpy(double *y, const double *x, int64_t n, cudaStream_t st);
 void launch_winweights(const double *weights, int64_t nr, int64_t nside, const double *rbounds, double rmax,
                        const double *rtp, int64_t ngal, double *w, int *err, cudaStream_t st);
@@ -347,8 +353,16 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, b
         launch_ring_analysis_tc(p, reinterpret_cast<const float *>(maps), nm, reinterpret_cast<float *>(fbuf.ptr),
                                 reinterpret_cast<int *>(p.erow.ptr), nzr, st, ring_live, nlive);
     } else {
+        // many columns: the FFT records the span of ring pairs with data, over which the
+        // first analysis pass sums (the spectra are zero elsewhere)
+        if (ncol > 8) {
+            SFB_TRY(grow(p, p.nzr64, 1));
+            nzr = reinterpret_cast<int *>(p.nzr64.ptr);
+            SFB_CUDA_TRY(cudaMemsetAsync(nzr, 0x7f, sizeof(int), st));          // first: a large value
+            SFB_CUDA_TRY(cudaMemsetAsync(nzr + 1, 0xff, sizeof(int), st));      // last: -1
+        }
         Stage s(h, stage(SFB_STAGE_RING_FFT), st);
-        launch_ring_analysis(p, maps, nm, fbuf.ptr, st);
+        launch_ring_analysis(p, maps, nm, fbuf.ptr, st, nzr);
     }
     const bool tc = p.precision == SFB_MIXED;
     float2 *adf = reinterpret_cast<float2 *>(p.almdf.ptr);
@@ -409,9 +423,10 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, b
         SFB_CUDA_TRY(cudaGetLastError());
         return SFB_OK;
     }
-    if (!tc && (ncol == 2 || ncol == 4 || ncol == 8) && p.d_gram64 && p.niter > 0) {
-        // FP64 Gram refinement for few columns (reference maps, small map2alm batches): the same
-        // identity as above, in FP64 with the narrow kernels.  alm holds [current | next | first pass].
+    if (!tc && p.d_gram64 && p.niter > 0) {
+        // FP64 Gram refinement: the same identity as above, in FP64 (narrow kernels for 2, 4 or 8
+        // columns: reference maps, small map2alm batches; tiled GEMMs for more, the first pass over
+        // the ring pairs with data).  alm holds [current | next | first pass].
         const int64_t na = p.lmsize * ncol;
         SFB_TRY(grow(p, alm, (size_t)(3 * na)));
         double *Ab[2] = {alm.ptr, alm.ptr + na};
@@ -419,7 +434,7 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, b
         int cur = p.niter & 1;
         {
             Stage s(h, stage(SFB_STAGE_LEG_ANALYSIS), st);
-            launch_leg_analysis(p, fbuf.ptr, ncol, Ab[cur], false, st);
+            launch_leg_analysis(p, fbuf.ptr, ncol, Ab[cur], false, st, -1, nzr);
         }
         SFB_CUDA_TRY(cudaMemcpyAsync(a0, Ab[cur], (size_t)na * sizeof(double), cudaMemcpyDeviceToDevice, st));
         for (int it = 0; it < p.niter; ++it) {
@@ -938,6 +953,7 @@ int sfb_plan_create(const sfb_plan_desc *d, sfb_plan **out) {
             // [2 (lmax+1)][nrn][gram_rows] transient, kept under 4 GiB
             const double build_bytes = 8.0 * 2 * (p.lmax + 1) * (double)p.nrn * p.gram_rows;
             // (SFBGPU_GRAM_REFINEMENT=0 keeps the full synthesis / fold / analysis passes)
+            if (const char *fe = std::getenv("SFBGPU_FIELD_MAX_BYTES")) p.field_max_bytes = std::atoll(fe);
             const char *ge = std::getenv("SFBGPU_GRAM_REFINEMENT");
             const bool allowed = !ge || std::atoi(ge) != 0;
             if (allowed && p.niter > 0 && 4 * (int64_t)ral <= 3 * p.nrn && build_bytes <= 4.0 * (1LL << 30)) {
@@ -982,7 +998,7 @@ void sfb_plan_destroy(sfb_plan *h) {
                     p.d_dtw_off, p.d_dtimg, p.d_dtimg_off, p.d_gramts, p.d_gramts_off, p.d_gram64, p.d_gram_off, p.d_cls_rings, p.d_cls_off, p.d_lam, p.d_lam32, p.d_lamtc, p.d_lamtc_off, p.d_lamts, p.d_lamts_off, p.d_lam_off, p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp,
                     p.d_pair_l, p.d_pair_n, p.d_out_pair, p.d_out_lm, p.d_coef, p.d_coefT, p.d_proj_tiles, p.d_err,
                     p.maps.ptr, p.fbuf.ptr, p.gbuf.ptr, p.rbuf.ptr, p.alm.ptr, p.scratch.ptr, p.scratch2.ptr, p.dep.ptr, p.maps32.ptr,
-                    p.ref.ptr, p.rf.ptr, p.rg.ptr, p.rr.ptr, p.ralm.ptr, p.almdf2.ptr, p.adf0.ptr, p.ecoef.ptr, p.erow.ptr, p.almdf.ptr, h->d_pair_index, h->d_noff};
+                    p.ref.ptr, p.rf.ptr, p.rg.ptr, p.rr.ptr, p.ralm.ptr, p.almdf2.ptr, p.adf0.ptr, p.ecoef.ptr, p.erow.ptr, p.almdf.ptr, p.nzr64.ptr, h->d_pair_index, h->d_noff};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     collect_stages(h);
@@ -1286,17 +1302,46 @@ int sfb_cat2amln_vjp(sfb_plan *h, const double *rtp, int64_t ngal, double nbar, 
     return SFB_OK;
 }
 
-int sfb_field2anlm_vjp(sfb_plan *h, const double *abar, int64_t nr, double rmin, double rmax, double *df_out) {
+// Field staging of field2anlm and its VJP: the whole nr x npix field is held on
+// the device when it fits the budget (SFBGPU_FIELD_MAX_BYTES at plan creation,
+// else half of the free device memory at the call); otherwise the shells go
+// through HBM one chunk at a time, copied between the host field and a
+// [npix][chunk] staging buffer with strided (2-D) copies.
+// Returns whether the whole field stays resident; otherwise lowers *cs (shells per chunk) so that a
+// chunk's staging buffer fits the budget too.
+static bool field_resident(const Plan &p, int64_t nr, size_t es, int64_t *cs) {
+    int64_t budget = p.field_max_bytes;
+    if (budget <= 0) {
+        size_t fr = 0, tot = 0;
+        if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+            cudaGetLastError();
+            fr = 0;
+        }
+        budget = (int64_t)(fr / 2);
+    }
+    const int64_t shell = p.npix * (int64_t)es;
+    if (nr * shell <= budget) return true;
+    *cs = std::max<int64_t>(1, std::min<int64_t>(*cs, budget / shell));
+    return false;
+}
+
+static int field2anlm_vjp_impl(sfb_plan *h, const double *abar, int64_t nr, double rmin, double rmax, void *df_out,
+                               int32_t dtype) {
     SFB_TRY(check_plan(h));
     SFB_TRY(set_device_of(h));
     if (!abar || !df_out || nr < 1 || !(rmin < rmax)) return fail(SFB_EINVAL, "bad field2anlm vjp arguments");
+    if (dtype != SFB_F64 && dtype != SFB_F32) return fail(SFB_EINVAL, "unknown field dtype");
     Plan &p = h->p;
     cudaStream_t st = h->stream;
     const double dr = (rmax - rmin) / (double)nr;
-    const int64_t cs = std::max<int64_t>(1, std::min<int64_t>(nr, chunk_pairs(p)));
-    // [abar 2 nlmsize][gtab npairs x nr][field nr x npix][Abar lmsize x 2 cs]
-    SFB_TRY(grow(p, p.scratch, (size_t)(2 * p.nlmsize + p.npairs * nr + nr * p.npix + p.lmsize * 2 * cs)));
-    double *d_ab = p.scratch.ptr, *d_g = d_ab + 2 * p.nlmsize, *d_f = d_g + p.npairs * nr, *d_A = d_f + nr * p.npix;
+    int64_t cs = std::max<int64_t>(1, std::min<int64_t>(nr, chunk_pairs(p)));
+    const size_t es = dtype == SFB_F32 ? sizeof(float) : sizeof(double);
+    const bool resident = field_resident(p, nr, es, &cs);
+    const int64_t fld = ((resident ? nr : cs) * p.npix * (int64_t)es + 7) / 8;     // field / staging, in doubles
+    // [abar 2 nlmsize][gtab npairs x nr][Abar lmsize x 2 cs][field or staging]
+    SFB_TRY(grow(p, p.scratch, (size_t)(2 * p.nlmsize + p.npairs * nr + p.lmsize * 2 * cs + fld)));
+    double *d_ab = p.scratch.ptr, *d_g = d_ab + 2 * p.nlmsize, *d_A = d_g + p.npairs * nr;
+    double *d_f = d_A + p.lmsize * 2 * cs;
     SFB_CUDA_TRY(cudaMemcpyAsync(d_ab, abar, 2 * p.nlmsize * sizeof(double), cudaMemcpyHostToDevice, st));
     launch_gtab(p, nr, rmin, dr, 1, d_g, st);                // g_nl(r_s) r_s^2 dr, the field2anlm weights
     SFB_TRY(grow(p, p.scratch2, (size_t)cs * p.npairs));
@@ -1308,12 +1353,30 @@ int sfb_field2anlm_vjp(sfb_plan *h, const double *abar, int64_t nr, double rmin,
         // Abar_s[lm] = sum_n g_nl(r_s) r_s^2 dr abar_nlm (the transpose of the radial sum)
         launch_shell_alm_g(p, h->d_pair_index, h->d_noff, p.scratch2.ptr, nsc, d_ab, d_A, 2 * nsc, st);
         SFB_TRY(sht_analysis_adjoint(h, d_A, nsc, p.maps.ptr, st));
-        launch_transpose_ld(p.maps.ptr, p.npix, nsc, p.npix, d_f + s0, nr, st);
+        // shells s0 .. s0+nsc of df: (ir, p) at ir + nr p (resident) or ir - s0 + nsc p (staging)
+        const int64_t ld = resident ? nr : nsc, off = resident ? s0 : 0;
+        if (dtype == SFB_F32)
+            launch_transpose_ld(p.maps.ptr, p.npix, nsc, p.npix, reinterpret_cast<float *>(d_f) + off, ld, st);
+        else
+            launch_transpose_ld(p.maps.ptr, p.npix, nsc, p.npix, d_f + off, ld, st);
+        if (!resident)
+            SFB_CUDA_TRY(cudaMemcpy2DAsync(static_cast<char *>(df_out) + s0 * es, nr * es, d_f, nsc * es, nsc * es,
+                                           p.npix, cudaMemcpyDeviceToHost, st));
     }
     SFB_CUDA_TRY(cudaGetLastError());
-    SFB_CUDA_TRY(cudaMemcpyAsync(df_out, d_f, (size_t)nr * p.npix * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (resident)
+        SFB_CUDA_TRY(cudaMemcpyAsync(df_out, d_f, (size_t)nr * p.npix * es, cudaMemcpyDeviceToHost, st));
     SFB_CUDA_TRY(cudaStreamSynchronize(st));
     return SFB_OK;
+}
+
+int sfb_field2anlm_vjp(sfb_plan *h, const double *abar, int64_t nr, double rmin, double rmax, double *df_out) {
+    return field2anlm_vjp_impl(h, abar, nr, rmin, rmax, df_out, SFB_F64);
+}
+
+int sfb_field2anlm_vjp_typed(sfb_plan *h, const double *abar, int64_t nr, double rmin, double rmax, void *df_out,
+                             int32_t dtype) {
+    return field2anlm_vjp_impl(h, abar, nr, rmin, rmax, df_out, dtype);
 }
 
 static int sfb_map2alm_impl(sfb_plan *h, const double *maps, int64_t nmaps, double *alm_out) {
@@ -1336,30 +1399,51 @@ static int sfb_map2alm_impl(sfb_plan *h, const double *maps, int64_t nmaps, doub
     return SFB_OK;
 }
 
-static int sfb_field2anlm_impl(sfb_plan *h, const double *f, int64_t nr, double rmin, double rmax, double *anlm_out) {
+static int sfb_field2anlm_impl(sfb_plan *h, const void *f, int32_t dtype, int64_t nr, double rmin, double rmax,
+                               double *anlm_out) {
     SFB_TRY(check_plan(h));
     SFB_TRY(set_device_of(h));
     if (!f || !anlm_out || nr < 1 || !(rmin < rmax)) return fail(SFB_EINVAL, "bad field2anlm arguments");
+    if (dtype != SFB_F64 && dtype != SFB_F32) return fail(SFB_EINVAL, "unknown field dtype");
     Plan &p = h->p;
     cudaStream_t st = h->stream;
     const double dr = (rmax - rmin) / (double)nr;
-    // [field nr*npix][gtab npairs*nr][out 2*nlmsize][acc 2*nlmsize]
-    SFB_TRY(grow(p, p.scratch, (size_t)(nr * p.npix + p.npairs * nr + 4 * p.nlmsize)));
-    double *d_f = p.scratch.ptr;
-    double *d_g = d_f + nr * p.npix;
+    int64_t cs = std::max<int64_t>(1, std::min<int64_t>(nr, chunk_pairs(p)));
+    const size_t es = dtype == SFB_F32 ? sizeof(float) : sizeof(double);
+    const bool resident = field_resident(p, nr, es, &cs);
+    const int64_t fld = ((resident ? nr : cs) * p.npix * (int64_t)es + 7) / 8;     // field / staging, in doubles
+    // [gtab npairs*nr][out 2*nlmsize][acc 2*nlmsize][field or staging]
+    SFB_TRY(grow(p, p.scratch, (size_t)(p.npairs * nr + 4 * p.nlmsize + fld)));
+    double *d_g = p.scratch.ptr;
     double *d_out = d_g + p.npairs * nr;
     double *d_acc = d_out + 2 * p.nlmsize;
-    SFB_CUDA_TRY(cudaMemcpyAsync(d_f, f, (size_t)nr * p.npix * sizeof(double), cudaMemcpyHostToDevice, st));
+    double *d_f = d_acc + 2 * p.nlmsize;
+    if (resident) SFB_CUDA_TRY(cudaMemcpyAsync(d_f, f, (size_t)nr * p.npix * es, cudaMemcpyHostToDevice, st));
     launch_gtab(p, nr, rmin, dr, 1, d_g, st);
     SFB_CUDA_TRY(cudaMemsetAsync(d_acc, 0, 2 * p.nlmsize * sizeof(double), st));
-    const int64_t cs = std::max<int64_t>(1, std::min<int64_t>(nr, chunk_pairs(p)));
     SFB_TRY(grow(p, p.scratch2, (size_t)cs * p.npairs));
+    const bool mixed = p.precision == SFB_MIXED;
     for (int64_t s0 = 0; s0 < nr; s0 += cs) {
         const int64_t nsc = std::min(cs, nr - s0);
         SFB_TRY(grow(p, p.maps, (size_t)nsc * p.npix));
-        // maps[s][p] = f[s0+s + nr p]
-        launch_transpose_ld(d_f + s0, nr, p.npix, nsc, p.maps.ptr, p.npix, st);
-        SFB_TRY(sht_analysis(h, p.maps.ptr, nsc, st, true));     // FP64 maps (converted in mixed precision)
+        if (!resident)
+            SFB_CUDA_TRY(cudaMemcpy2DAsync(d_f, nsc * es, static_cast<const char *>(f) + s0 * es, nr * es, nsc * es,
+                                           p.npix, cudaMemcpyHostToDevice, st));
+        const int64_t ld = resident ? nr : nsc, off = resident ? s0 : 0;
+        // maps[s][p] = f[s0+s + nr p]: FP32 maps straight from an FP32 field in mixed precision, else FP64
+        bool maps64 = true;
+        if (dtype == SFB_F32) {
+            const float *src = reinterpret_cast<const float *>(d_f) + off;
+            if (mixed) {
+                launch_transpose_ld(src, ld, p.npix, nsc, reinterpret_cast<float *>(p.maps.ptr), p.npix, st);
+                maps64 = false;
+            } else {
+                launch_transpose_ld(src, ld, p.npix, nsc, p.maps.ptr, p.npix, st);
+            }
+        } else {
+            launch_transpose_ld(d_f + off, ld, p.npix, nsc, p.maps.ptr, p.npix, st);
+        }
+        SFB_TRY(sht_analysis(h, p.maps.ptr, nsc, st, maps64));     // FP64 maps are converted in mixed precision
         // gtab for this chunk: rows pair, cols nsc (copy sub-block)
         SFB_CUDA_TRY(cudaMemcpy2DAsync(p.scratch2.ptr, nsc * sizeof(double), d_g + s0, nr * sizeof(double),
                                        nsc * sizeof(double), p.npairs, cudaMemcpyDeviceToDevice, st));
@@ -1555,7 +1639,13 @@ int sfb_map2alm(sfb_plan *h, const double *maps, int64_t nmaps, double *alm_out)
 int sfb_field2anlm(sfb_plan *h, const double *f, int64_t nr, double rmin, double rmax, double *anlm_out) {
     SFB_TRY(check_plan(h));
     // the shell maps go through the plan's transform (FP64, or the mixed tensor-core one)
-    return sfb_field2anlm_impl(h, f, nr, rmin, rmax, anlm_out);
+    return sfb_field2anlm_impl(h, f, SFB_F64, nr, rmin, rmax, anlm_out);
+}
+
+int sfb_field2anlm_typed(sfb_plan *h, const void *f, int32_t dtype, int64_t nr, double rmin, double rmax,
+                         double *anlm_out) {
+    SFB_TRY(check_plan(h));
+    return sfb_field2anlm_impl(h, f, dtype, nr, rmin, rmax, anlm_out);
 }
 
 int sfb_anlm2field(sfb_plan *h, const double *anlm, int64_t nr, double rmin, double rmax, double *f_out) {

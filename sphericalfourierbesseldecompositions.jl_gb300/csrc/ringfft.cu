@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(256) k_ring_analysis(const RingGeom *rings, in
                                                        int MT, T *F, int64_t ldF, int r0,
                                                        const TW *__restrict__ twtab,
                                                        const int64_t *__restrict__ twoff,
-                                                       const TW *__restrict__ wphase) {
+                                                       const TW *__restrict__ wphase, int *nzr) {
     extern __shared__ unsigned char smem_raw[];
     const int r = r0 + blockIdx.x;
     const int64_t b0 = (int64_t)blockIdx.y * MT;
@@ -222,6 +222,10 @@ __global__ void __launch_bounds__(256) k_ring_analysis(const RingGeom *rings, in
             dp[0] = dp[1] = dq[0] = dq[1] = (T)0;
         }
         return;
+    }
+    if (nzr && threadIdx.x == 0) {   // span of the ring pairs with data (the analysis sums over it only)
+        atomicMin(nzr, r);
+        atomicMax(nzr + 1, r);
     }
     if (reduced) {
         // one warp per (map, ring of the pair): double-float sum of the staged values
@@ -374,7 +378,7 @@ static int ring_mt(size_t n, size_t elem, bool two_buffers) {
 // power of two).  Each group is one launch with its own shared-memory size.
 template <typename T, typename TI, typename TW>
 static void ring_analysis_t(const Plan &p, const TI *maps, int64_t nmaps, T *F, const TW *tw, const TW *wph,
-                            cudaStream_t st) {
+                            cudaStream_t st, int *nzr = nullptr) {
     const int ns = (int)p.nside;
     const bool pow2 = (ns & (ns - 1)) == 0;
     struct Group { int r0, nr; size_t n; bool two; } groups[2] = {
@@ -387,16 +391,16 @@ static void ring_analysis_t(const Plan &p, const TI *maps, int64_t nmaps, T *F, 
         set_smem(k_ring_analysis<T, TI, TW>, smem);
         dim3 grid((unsigned)gr.nr, (unsigned)((nmaps + MT - 1) / MT));
         k_ring_analysis<T, TI, TW><<<grid, 256, smem, st>>>(p.d_rings, (int)p.nrn, p.lmax, p.npix, maps, nmaps, MT,
-                                                            F, 2 * nmaps, gr.r0, tw, p.d_twoff, wph);
+                                                            F, 2 * nmaps, gr.r0, tw, p.d_twoff, wph, nzr);
         note_launch();
     }
 }
 
-void launch_ring_analysis(const Plan &p, const double *maps, int64_t nmaps, double *F, cudaStream_t st) {
+void launch_ring_analysis(const Plan &p, const double *maps, int64_t nmaps, double *F, cudaStream_t st, int *nzr) {
     if (p.precision == SFB_MIXED)
         ring_analysis_t<float, float, float2>(p, (const float *)maps, nmaps, (float *)F, p.d_twtab32, p.d_wphase32, st);
     else
-        ring_analysis_t<double, double, double2>(p, maps, nmaps, F, p.d_twtab, p.d_wphase, st);
+        ring_analysis_t<double, double, double2>(p, maps, nmaps, F, p.d_twtab, p.d_wphase, st, nzr);
 }
 
 void launch_ring_synthesis(const Plan &p, const double *G, int64_t nmaps, double *maps, cudaStream_t st) {

@@ -105,6 +105,9 @@ struct Plan {
     // per block z the Gram matrix of the other rings, sliced in the synthesis
     // layout with its gram_rows output rows as rings (null: not used)
     int ral = 0, gram_rows = 0;
+    // field2anlm / its VJP hold the whole shell x pixel field on the device up to this many bytes
+    // (0: half of the free device memory at the call), else stream it in chunks of shells
+    int64_t field_max_bytes = 0;
     // tiles (l, m0, n0) of the mixed-precision projection
     int3 *d_proj_tiles = nullptr;
     int64_t n_proj_tiles = 0;
@@ -144,6 +147,7 @@ struct Plan {
     DevBuf<double> ecoef;           // Gram refinement: column exponents of both a_lm sets (ints)
     DevBuf<double> erow;            // ring DFT row exponents [2][nrn][nmaps] (int)
     DevBuf<double> maps32;          // FP32 copy of FP64 maps (mixed precision, spline / dense-window paths)
+    DevBuf<double> nzr64;           // FP64 many-column transform: first / last ring pair with data (2 ints)
     int64_t device_bytes = 0;
 };
 
@@ -203,16 +207,20 @@ void launch_project_mixed(const Plan &p, const float2 *Adf, int64_t ldA, const f
                           cudaStream_t st);
 // maps[j] -= nu[j] ref with nu[j] = <maps[j], ref> / <ref, ref> (FP64, in place).
 void launch_split_mean(double *maps, int64_t nmaps, int64_t npix, const double *ref, double *nu, cudaStream_t st);
-void launch_ring_analysis(const Plan &p, const double *maps, int64_t nmaps, double *F, cudaStream_t st);
+// nzr (FP64): receives the first / last ring pair holding a non-zero value in any map
+// (preset by the caller to a large value / -1).
+void launch_ring_analysis(const Plan &p, const double *maps, int64_t nmaps, double *F, cudaStream_t st,
+                          int *nzr = nullptr);
 void launch_ring_synthesis(const Plan &p, const double *G, int64_t nmaps, double *maps, cudaStream_t st);
-// rlim (few columns only): rings r < rlim (analysis: the sum; synthesis: the rings formed); -1 = all
+// rlim: rings r < rlim (analysis: the sum; synthesis: the rings formed); -1 = all.
+// nzr (many columns): the analysis sums over the ring pairs [nzr[0], nzr[1]] only.
 void launch_leg_analysis(const Plan &p, const double *F, int64_t ncol, double *A, bool accumulate,
-                         cudaStream_t st, int rlim = -1);
+                         cudaStream_t st, int rlim = -1, const int *nzr = nullptr);
 void launch_leg_synthesis(const Plan &p, const double *A, int64_t ncol, double *G, cudaStream_t st, int rlim = -1);
-// FP64 Gram refinement step for 2, 4 or 8 columns; false when not available
+// FP64 Gram refinement step (any column count); false when the plan has no Gram tables
 bool launch_gram_update_fp64(const Plan &p, const double *Acur, const double *A0, int64_t ncol, double *Anew,
                              cudaStream_t st);
-// rlim: only rings r < rlim (-1: all); F == nullptr (mixed, many columns): R = -w n cfold Fold(G)
+// rlim: only rings r < rlim (-1: all); F == nullptr (Gram refinement): R = -w n cfold Fold(G)
 void launch_fold_residual(const Plan &p, const double *F, const double *G, int64_t ncol, double *R, cudaStream_t st,
                           int *Ecol = nullptr, int rlim = -1);
 void launch_radial_coeffs(const Plan &p, const double *gl_x, const double *pq, int Q, double *coef,

@@ -21,6 +21,13 @@
 // Set-up: the first call on a device (with that device current) looks up the
 // array's device address with cudaGetSymbolAddress; this loads the library's
 // device code on that device.  Make that first call before any stream capture.
+// The address is kept for the life of the process: a cudaDeviceReset of the
+// device invalidates it, and a process that resets a device must not call this
+// entry point on it again.
+//
+// Streams: every copy and the kernel go to the legacy default stream with
+// synchronous cudaMemcpy, so the call returns with its result on the host and
+// serialises with every blocking stream of the process.
 //
 // Overlapping calls on one device would race on the single scratch array; the
 // calls are serialised by a per-device lock, so concurrent callers on one

@@ -6,15 +6,27 @@
 # src/windows.jl:244-270) with the same argument meaning.  The device plan is
 # built once per AnlmModes (its k_nl, spline tables and ordering) and freed by
 # a finalizer.  Errors map to the exceptions the reference raises.
+#
+# Differentiation: ChainRulesCore.rrule methods for cat2amln (with respect to
+# the galaxy weights) and field2anlm (with respect to the shell x pixel field)
+# pull a cotangent ā = ∂L/∂Re(a) + i ∂L/∂Im(a) back through the library's
+# hand-written adjoint kernels (sfb_cat2amln_vjp, sfb_field2anlm_vjp_typed).
+# Both transforms are linear in the differentiated argument, so the pullbacks
+# keep no activations: the only state is the inputs the caller already holds.
+# A field larger than the device budget streams through HBM one chunk of
+# shells at a time in the forward and in the pullback alike.
 module SFBGPU
 
 using SphericalFourierBesselDecompositions
 const SFB = SphericalFourierBesselDecompositions
+import ChainRulesCore
+using ChainRulesCore: NoTangent, ZeroTangent, AbstractZero, unthunk, @not_implemented
 
 const libsfb = get(ENV, "SFBGPU_LIB", joinpath(@__DIR__, "..", "libsfbgpu.so"))
 
 const SFB_OK, SFB_EINVAL, SFB_ENOMEM, SFB_ENONFINITE, SFB_ERANGE, SFB_ETIMEOUT, SFB_ECUDA, SFB_ENOTSUP = 0:7
 const PRECISION = Dict(:fp64 => Int32(0), :mixed => Int32(1))
+const DTYPE = Dict(Float64 => Int32(0), Float32 => Int32(1))     # sfb_dtype
 const RADIAL = Dict(:poly => Int32(0), :spline => Int32(1))
 
 # Field order and types follow sfb_plan_desc / sfb_window exactly.
@@ -147,14 +159,18 @@ end
 
 """
     field2anlm(f_xyz, wmodes, amodes)    (src/cat2anlm.jl:323-357)
+
+A `Matrix{Float32}` field is passed as it is (no Float64 copy); any other
+real matrix is converted to `Matrix{Float64}`.
 """
 function field2anlm(f_xyz, wmodes, amodes; kw...)
     p = getplan(amodes; kw...)
-    f = Matrix{Float64}(f_xyz)
+    T = eltype(f_xyz) === Float32 ? Float32 : Float64
+    f = Matrix{T}(f_xyz)
     out = Vector{ComplexF64}(undef, p.nlmsize)
-    GC.@preserve f out check(ccall((:sfb_field2anlm, libsfb), Cint,
-                                   (Ptr{Cvoid}, Ptr{Float64}, Int64, Float64, Float64, Ptr{ComplexF64}),
-                                   p.handle, f, wmodes.nr, wmodes.rmin, wmodes.rmax, out))
+    GC.@preserve f out check(ccall((:sfb_field2anlm_typed, libsfb), Cint,
+                                   (Ptr{Cvoid}, Ptr{Cvoid}, Int32, Int64, Float64, Float64, Ptr{ComplexF64}),
+                                   p.handle, f, DTYPE[T], wmodes.nr, wmodes.rmin, wmodes.rmax, out))
     return out
 end
 
@@ -217,9 +233,8 @@ end
     cat2amln_vjp(rθϕ, amodes, nbar, abar; kw...) -> dL/dw
 
 Gradient of a real loss L through `cat2amln` with respect to the galaxy
-weights, given `abar = ∂L/∂Re(a) + i ∂L/∂Im(a)` (FP64 adjoint; a ChainRules
-`rrule` for `cat2amln` returns `(NoTangent(), …, cat2amln_vjp(...))` for the
-weight argument).
+weights, given `abar = ∂L/∂Re(a) + i ∂L/∂Im(a)` (FP64 adjoint; the pullback of
+the `ChainRulesCore.rrule` for `cat2amln` below).
 """
 function cat2amln_vjp(rθϕ, amodes, nbar, abar; kw...)
     p = getplan(amodes; kw...)
@@ -233,16 +248,47 @@ function cat2amln_vjp(rθϕ, amodes, nbar, abar; kw...)
 end
 
 """
-    field2anlm_vjp(abar, wmodes, amodes; kw...) -> dL/df  (nr × npix)
+    field2anlm_vjp(abar, wmodes, amodes; eltype=Float64, kw...) -> dL/df  (nr × npix)
+
+`eltype=Float32` writes the gradient in Float32 (the element type of an FP32 field).
 """
-function field2anlm_vjp(abar, wmodes, amodes; kw...)
+function field2anlm_vjp(abar, wmodes, amodes; eltype=Float64, kw...)
     p = getplan(amodes; kw...)
+    T = eltype === Float32 ? Float32 : Float64
     a = Vector{ComplexF64}(abar)
-    df = Matrix{Float64}(undef, wmodes.nr, p.npix)
-    GC.@preserve a df check(ccall((:sfb_field2anlm_vjp, libsfb), Cint,
-                                  (Ptr{Cvoid}, Ptr{ComplexF64}, Int64, Float64, Float64, Ptr{Float64}),
-                                  p.handle, a, wmodes.nr, wmodes.rmin, wmodes.rmax, df))
+    df = Matrix{T}(undef, wmodes.nr, p.npix)
+    GC.@preserve a df check(ccall((:sfb_field2anlm_vjp_typed, libsfb), Cint,
+                                  (Ptr{Cvoid}, Ptr{ComplexF64}, Int64, Float64, Float64, Ptr{Cvoid}, Int32),
+                                  p.handle, a, wmodes.nr, wmodes.rmin, wmodes.rmax, df, DTYPE[T]))
     return df
+end
+
+# ---------------------------------------------------------------- rrules ----
+# cat2amln(rθϕ, amodes, nbar, win_rhat_ln[, weight]): the weight cotangent is
+# the adjoint kernel's dL/dw; positions, n̄ and the window are not
+# differentiated by this library (@not_implemented), amodes is not a tangent.
+function ChainRulesCore.rrule(::typeof(cat2amln), rθϕ, amodes, nbar, win_rhat_ln,
+                              weight=ones(size(rθϕ, 2)); kw...)
+    a = cat2amln(rθϕ, amodes, nbar, win_rhat_ln, weight; kw...)
+    function cat2amln_pullback(ā)
+        ā = unthunk(ā)
+        dw = ā isa AbstractZero ? ZeroTangent() : cat2amln_vjp(rθϕ, amodes, nbar, ā; kw...)
+        return (NoTangent(), @not_implemented("galaxy positions"), NoTangent(), @not_implemented("nbar"),
+                @not_implemented("win_rhat_ln"), dw)
+    end
+    return a, cat2amln_pullback
+end
+
+# field2anlm(f_xyz, wmodes, amodes): the field cotangent has the field's element type.
+function ChainRulesCore.rrule(::typeof(field2anlm), f_xyz, wmodes, amodes; kw...)
+    a = field2anlm(f_xyz, wmodes, amodes; kw...)
+    T = eltype(f_xyz) === Float32 ? Float32 : Float64
+    function field2anlm_pullback(ā)
+        ā = unthunk(ā)
+        df = ā isa AbstractZero ? ZeroTangent() : field2anlm_vjp(ā, wmodes, amodes; eltype=T, kw...)
+        return (NoTangent(), df, NoTangent(), NoTangent())
+    end
+    return a, field2anlm_pullback
 end
 
 """

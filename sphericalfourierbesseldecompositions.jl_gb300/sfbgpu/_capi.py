@@ -14,6 +14,7 @@ LIB_PATH = os.path.join(os.path.dirname(_HERE), "libsfbgpu.so")
 
 SFB_OK, SFB_EINVAL, SFB_ENOMEM, SFB_ENONFINITE, SFB_ERANGE, SFB_ETIMEOUT, SFB_ECUDA, SFB_ENOTSUP = range(8)
 SFB_FP64, SFB_MIXED = 0, 1
+SFB_F64, SFB_F32 = 0, 1
 SFB_RADIAL_POLY, SFB_RADIAL_SPLINE = 0, 1
 SFB_WINDOW_ZERO, SFB_WINDOW_SEPARABLE, SFB_WINDOW_DENSE = 0, 1, 2
 
@@ -58,6 +59,10 @@ _PROTOS = [
     ("sfb_cat2amln_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_double,
                                       C.POINTER(Window), C.c_void_p, C.c_void_p]),
     ("sfb_field2anlm", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_double, C.c_double, C.c_void_p]),
+    ("sfb_field2anlm_typed", C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int64, C.c_double, C.c_double,
+                                       C.c_void_p]),
+    ("sfb_field2anlm_vjp_typed", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_double, C.c_double, C.c_void_p,
+                                           C.c_int32]),
     ("sfb_anlm2field", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_double, C.c_double, C.c_void_p]),
     ("sfb_win_rhat_ln_separable", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_double, C.c_double,
                                             C.c_void_p]),

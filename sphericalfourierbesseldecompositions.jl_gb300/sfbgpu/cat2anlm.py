@@ -182,13 +182,17 @@ def cat2amln_batched(catalogues, amodes, nbars, win_rhat_ln, weights=None, **pla
 
 
 def field2anlm(f_xyz, wmodes, amodes, **plan_opts):
-    """SFB coefficients of an (nr, npix) field (reference field2anlm_v2, src/cat2anlm.jl:323-357)."""
+    """SFB coefficients of an (nr, npix) field (reference field2anlm_v2, src/cat2anlm.jl:323-357).
+    A float32 field is passed as it is (sfb_field2anlm_typed), anything else as float64."""
     plan = get_plan(amodes, **plan_opts)
-    f = np.asfortranarray(f_xyz, float)
+    dt = np.float32 if np.asarray(f_xyz).dtype == np.float32 else np.float64
+    f = np.asfortranarray(f_xyz, dt)
     if f.shape != (wmodes.nr, plan.npix):
         raise ValueError("field must be nr x npix")
     out = np.empty(plan.nlmsize, np.complex128)
-    capi.check(capi.lib.sfb_field2anlm(plan.handle, capi.ptr(f), wmodes.nr, wmodes.rmin, wmodes.rmax, capi.ptr(out)))
+    code = capi.SFB_F32 if dt == np.float32 else capi.SFB_F64
+    capi.check(capi.lib.sfb_field2anlm_typed(plan.handle, capi.ptr(f), code, wmodes.nr, wmodes.rmin, wmodes.rmax,
+                                             capi.ptr(out)))
     return out
 
 
@@ -253,13 +257,20 @@ def cat2amln_vjp(rtp, amodes, nbar, abar, **plan_opts):
     return out
 
 
-def field2anlm_vjp(abar, wmodes, amodes, **plan_opts):
-    """dL/df (nr, npix) for field2anlm, given abar = dL/dRe(a) + i dL/dIm(a)."""
+def field2anlm_vjp(abar, wmodes, amodes, dtype=np.float64, **plan_opts):
+    """dL/df (nr, npix) for field2anlm, given abar = dL/dRe(a) + i dL/dIm(a);
+    dtype float32 writes the gradient in FP32 (the element type of an FP32 field)."""
     plan = get_plan(amodes, **plan_opts)
     ab = np.ascontiguousarray(abar, np.complex128)
-    out = np.empty((wmodes.nr, plan.npix), order="F")
-    capi.check(capi.lib.sfb_field2anlm_vjp(plan.handle, capi.ptr(ab), wmodes.nr, wmodes.rmin, wmodes.rmax,
-                                           capi.ptr(out)))
+    if ab.shape != (plan.nlmsize,):
+        raise ValueError("abar must have getnlmsize(amodes) entries")
+    dt = np.dtype(dtype)
+    if dt not in (np.dtype(np.float32), np.dtype(np.float64)):
+        raise ValueError("dtype must be float32 or float64")
+    out = np.empty((wmodes.nr, plan.npix), dtype=dt, order="F")
+    code = capi.SFB_F32 if dt == np.float32 else capi.SFB_F64
+    capi.check(capi.lib.sfb_field2anlm_vjp_typed(plan.handle, capi.ptr(ab), wmodes.nr, wmodes.rmin, wmodes.rmax,
+                                                 capi.ptr(out), code))
     return out
 
 

@@ -137,3 +137,34 @@ def test_field2anlm_gradient_finite_differences():
         e = _rel(fd, g[s, p])
         record("field2anlm_gradient_vs_fd", e)
         assert e < 1e-6, (s, p, fd, g[s, p])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_field2anlm_fp32_field_and_shell_streaming(precision, monkeypatch):
+    """An FP32 field (sfb_field2anlm_typed) gives exactly what its FP64 copy
+    gives; the FP32 gradient is the FP64 one rounded; and a field streamed
+    through the device one shell at a time (SFBGPU_FIELD_MAX_BYTES below one
+    shell) matches the resident field to the rounding of the radial sum's
+    grouping (1e-12)."""
+    a = sfbgpu.AnlmModes(0.03, 500.0, 1000.0, nside=16)
+    wm = sfbgpu.ConfigurationSpaceModes(a.rmin, a.rmax, 24, a.nside)
+    rng = np.random.default_rng(31)
+    f32 = rng.normal(size=(wm.nr, wm.npix)).astype(np.float32)
+    r64 = sfbgpu.field2anlm(f32.astype(float), wm, a, precision=precision)
+    r32 = sfbgpu.field2anlm(f32, wm, a, precision=precision)
+    np.testing.assert_array_equal(r32, r64)
+    ab = rng.normal(size=r64.size) + 1j * rng.normal(size=r64.size)
+    g64 = sfbgpu.field2anlm_vjp(ab, wm, a, precision=precision)
+    g32 = sfbgpu.field2anlm_vjp(ab, wm, a, dtype=np.float32, precision=precision)
+    assert g32.dtype == np.float32
+    np.testing.assert_array_equal(g32, g64.astype(np.float32))
+    monkeypatch.setenv("SFBGPU_FIELD_MAX_BYTES", "1")
+    b = sfbgpu.AnlmModes(0.03, 500.0, 1000.0, nside=16)
+    s32 = sfbgpu.field2anlm(f32, wm, b, precision=precision)
+    gs = sfbgpu.field2anlm_vjp(ab, wm, b, precision=precision)
+    gs32 = sfbgpu.field2anlm_vjp(ab, wm, b, dtype=np.float32, precision=precision)
+    e = float(np.max(np.abs(s32 - r32)) / np.max(np.abs(r32)))
+    eg = float(np.max(np.abs(gs - g64)) / np.max(np.abs(g64)))
+    record(f"field2anlm_streamed_vs_resident_{precision}", e, vjp=eg)
+    assert e < 1e-12 and eg < 1e-12
+    np.testing.assert_array_equal(gs32, gs.astype(np.float32))

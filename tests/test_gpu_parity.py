@@ -115,11 +115,12 @@ def test_map2alm_few_maps_vs_oracle(nmaps):
     assert e < 1e-12
 
 
-@pytest.mark.parametrize("nmaps", [1, 2, 4])
+@pytest.mark.parametrize("nmaps", [1, 2, 3, 4, 12])
 def test_map2alm_gram_refinement_vs_oracle(nmaps):
-    """Few maps on a geometry where most rings are alias-free (nside 32,
-    lmax 40: the 20 polar rings with nph <= 80 alias): the refinement passes
-    run through the FP64 Gram matrices plus the aliased rings."""
+    """A geometry where most rings are alias-free (nside 32, lmax 40: the 20
+    polar rings with nph <= 80 alias): the refinement passes run through the
+    FP64 Gram matrices plus the aliased rings (matrix-vector kernels for 1, 2
+    and 4 maps, tiled GEMMs for 3 and 12)."""
     nside, lmax = 32, 40
     a = sfbgpu.AnlmModes.from_nmax_lmax(1, lmax, 500.0, 1000.0, nside=nside, cache=True)
     rng = np.random.default_rng(10 + nmaps)
@@ -129,6 +130,25 @@ def test_map2alm_gram_refinement_vs_oracle(nmaps):
     tri = np.array([ref[b, l, m] for b in range(nmaps) for l in range(lmax + 1) for m in range(l + 1)])
     e = rel_err(out.ravel(), tri)
     record(f"map2alm_gram_{nmaps}maps_nside{nside}_lmax{lmax}_niter3", e)
+    assert e < 1e-12
+
+
+@pytest.mark.parametrize("zlim", [(0.5, 1.0), (-0.3, 0.3), (-1.0, -0.6)])
+def test_map2alm_gram_partial_sky_vs_oracle(zlim):
+    """Many maps that are zero outside a cap or band: the FP64 ring transform
+    records the span of ring pairs with data and the first analysis pass sums
+    over that span only."""
+    nside, lmax, nmaps = 32, 40, 10
+    a = sfbgpu.AnlmModes.from_nmax_lmax(1, lmax, 500.0, 1000.0, nside=nside, cache=True)
+    rng = np.random.default_rng(40)
+    th, _ = sfbgpu.pix2ang_ring(nside, np.arange(12 * nside * nside))
+    z = np.cos(th)
+    maps = (rng.normal(size=(nmaps, 12 * nside * nside)) + 2.0) * ((z > zlim[0]) & (z < zlim[1]))
+    out = sfbgpu.cat2anlm.map2alm(maps, a, niter=3, radial="spline")
+    ref = osht.SHT(nside, lmax).map2alm(maps, niter=3)
+    tri = np.array([ref[b, l, m] for b in range(nmaps) for l in range(lmax + 1) for m in range(l + 1)])
+    e = rel_err(out.ravel(), tri)
+    record(f"map2alm_gram_partial_sky_z{zlim[0]}_{zlim[1]}", e)
     assert e < 1e-12
 
 

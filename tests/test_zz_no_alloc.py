@@ -69,3 +69,36 @@ def test_noalloc_rejects_table_beyond_scratch():
     st, _ = _call(capi.lib.sfb_winweights2galweights_noalloc, nside, W, rb, gal)
     assert st == capi.SFB_EINVAL
     assert "static scratch maximum" in capi.last_error()
+
+
+def test_noalloc_runs_with_device_memory_taken():
+    """The property the entry point exists for: with nearly all device memory
+    held by another allocator (here a PyTorch tensor), the allocating entry
+    point fails with SFB_ENOMEM while the allocation-free one still returns
+    the same weights."""
+    torch = pytest.importorskip("torch")
+    nside, nr = 64, 30
+    W, rb, gal = _inputs(nside, nr, 2_000_000, 41)      # the allocating call needs ~76 MB
+    st, ref = _call(capi.lib.sfb_winweights2galweights, nside, W, rb, gal)
+    assert st == capi.SFB_OK, capi.last_error()
+    st, _ = _call(capi.lib.sfb_winweights2galweights_noalloc, nside, W, rb, gal[:10])   # set-up done
+    assert st == capi.SFB_OK, capi.last_error()
+    torch.cuda.synchronize()
+    keep = 32 << 20
+    hold = None
+    try:
+        free, _ = torch.cuda.mem_get_info()
+        hold = torch.empty(max(free - keep, 0), dtype=torch.uint8, device="cuda")
+        free_after, _ = torch.cuda.mem_get_info()
+        assert free_after < 64 << 20
+        st, _ = _call(capi.lib.sfb_winweights2galweights, nside, W, rb, gal)
+        assert st == capi.SFB_ENOMEM
+        for _ in range(2):
+            st, out = _call(capi.lib.sfb_winweights2galweights_noalloc, nside, W, rb, gal)
+            assert st == capi.SFB_OK, capi.last_error()
+            np.testing.assert_array_equal(out, ref)
+        # no device memory taken by the calls (the driver may release some of its own)
+        assert torch.cuda.mem_get_info()[0] >= free_after
+    finally:
+        del hold
+        torch.cuda.empty_cache()
