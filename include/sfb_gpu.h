@@ -235,6 +235,29 @@ int sfb_winweights2galweights_noalloc(int64_t nside, const double *weights, int6
                                       const double *rbounds, const double *rtp, int64_t ngal,
                                       double *w_out);
 
+/* apply_window(rθϕ, win, rmin, rmax, win_r, win_Δr; rng) (reference
+ * src/windows.jl:169-216): the galaxies of rtp ([3*ngal], as in sfb_cat2amln)
+ * kept by the window, in input order, written to rtp_out ([3*ngal] capacity),
+ * their number to *nkept.  Galaxy i is kept when rmin <= r_i <= rmax, its
+ * shell ceil((r_i - rmin)/dr) (0 becoming 1) is at most nr, and
+ * u_i <= win[shell, pix_i] * (1 / max(win)); win: [nr * npix], element (ir, p)
+ * at ir + nr*p (a Julia nr x npix matrix), pix_i the RING pixel.  u_i =
+ * uniform[i] when `uniform` is given (the reference's rand(rng) per galaxy:
+ * a caller passing the same draws gets the reference's result exactly), else
+ * the counter-based stream (splitmix64(seed + (i+1) * 0x9E3779B97F4A7C15) >> 11)
+ * * 2^-53.  A NaN window value or a non-finite direction of a galaxy inside
+ * the shells returns SFB_ENONFINITE, theta outside [0, pi] SFB_ERANGE. */
+int sfb_apply_window(int64_t nside, const double *win, int64_t nr, double rmin, double rmax, double dr,
+                     const double *rtp, int64_t ngal, const double *uniform, uint64_t seed, double *rtp_out,
+                     int64_t *nkept);
+
+/* The same with win, rtp, uniform and rtp_out in device memory, on `stream`
+ * (cudaStream_t or NULL); returns after *nkept (a host pointer) is known.
+ * Thins mock catalogues on the device for sfb_cat2amln_device. */
+int sfb_apply_window_device(int64_t nside, const double *win, int64_t nr, double rmin, double rmax, double dr,
+                            const double *rtp, int64_t ngal, const double *uniform, uint64_t seed,
+                            double *rtp_out, int64_t *nkept, void *stream);
+
 /* HEALPix RING pixel (0-based; Healpix.jl ang2pixRing returns this + 1) of
  * n directions, computed on the device with the binning kernel's arithmetic. */
 int sfb_ang2pix_ring(int64_t nside, const double *theta, const double *phi, int64_t n,

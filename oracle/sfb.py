@@ -11,6 +11,8 @@ and follows one reference function:
 * ``integrate_window`` src/windows.jl:219-228
 * ``amln2clnn``      src/SphericalFourierBesselDecompositions.jl:114-150
 * ``winweights2galweights`` src/cat2anlm.jl:218-238
+* ``apply_window``   src/windows.jl:169-216 (the uniform draws passed in;
+  ``splitmix64_uniform`` restates the library's counter-based stream)
 
 ``modes`` arguments are dicts with ``nmax``, ``lmax``, ``lmax_n`` (list over n),
 ``nside``, ``splines`` {(n, l): (x, y, ypp)} and ``noff`` (offset of each n
@@ -198,3 +200,39 @@ def winweights2galweights(weights, rbounds, nside, rtp):
     if np.any((b < 1) | (b > nr)):
         raise ValueError("r out of bounds")
     return weights[b - 1, pix]
+
+
+def splitmix64(seed, n):
+    """The first n outputs of SplitMix64 (Steele, Lea, Flood 2014) from state
+    `seed`: z_i = mix(seed + i * 0x9E3779B97F4A7C15), i = 1..n."""
+    with np.errstate(over="ignore"):
+        i = np.arange(1, n + 1, dtype=np.uint64)
+        z = np.uint64(seed) + i * np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+
+
+def splitmix64_uniform(seed, n):
+    """u_i = (z_i >> 11) * 2^-53 in [0, 1): the library's per-galaxy draws."""
+    return (splitmix64(seed, n) >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
+
+
+def apply_window(rtp, win, rmin, rmax, dr, nside, uniform):
+    """Galaxies kept by apply_window (src/windows.jl:169-216), in input order,
+    with the per-galaxy draws `uniform` standing in for rand(rng): kept when
+    rmin <= r <= rmax, shell ceil((r - rmin)/dr) (0 -> 1) <= nr and
+    u <= win[shell, pix] * (1 / maximum(win))."""
+    rtp = np.asarray(rtp, float)
+    r, th, ph = rtp
+    nr = win.shape[0]
+    oow = 1.0 / np.max(win)
+    keep = np.zeros(r.size, bool)
+    idx = np.nonzero((rmin <= r) & (r <= rmax))[0]
+    ir = np.ceil((r[idx] - rmin) / dr).astype(np.int64)
+    ir[ir == 0] = 1
+    ok = ir <= nr
+    idx, ir = idx[ok], ir[ok]
+    pix = ang2pix_ring(nside, th[idx], ph[idx])
+    keep[idx] = uniform[idx] <= win[ir - 1, pix] * oow
+    return rtp[:, keep]

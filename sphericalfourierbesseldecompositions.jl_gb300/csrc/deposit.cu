@@ -756,6 +756,18 @@ static void by_degree(int deg, F &&f) {
     else f(std::integral_constant<int, 63>());
 }
 
+int64_t scan_tile_count(int64_t n) { return (n + SCAN_TILE - 1) / SCAN_TILE; }
+
+void launch_exclusive_scan(int32_t *data, int64_t n, int32_t *tile_sums, cudaStream_t st) {
+    const int64_t ntiles = scan_tile_count(n);
+    k_scan_tiles<<<(unsigned)ntiles, SCAN_THREADS, 0, st>>>(data, n, tile_sums);
+    note_launch();
+    k_scan_sums<<<1, 1024, 0, st>>>(tile_sums, ntiles);
+    note_launch();
+    k_scan_add<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(data, n, tile_sums);
+    note_launch();
+}
+
 int deposit_sorted(Plan &p, const double *rtp, const double *w, int64_t ngal, double *maps, double *ref,
                    double *mu, cudaEvent_t ref_ready, cudaStream_t st, const cudaEvent_t *chunk_ready,
                    int nchunks, const int **ring_live) {
@@ -820,12 +832,7 @@ int deposit_sorted(Plan &p, const double *rtp, const double *w, int64_t ngal, do
         k_deposit_keys_fallback<<<304, 256, 0, st>>>(rtp, p.nside, p.npix, counts, key, rank, fb_list, fb_count);
         note_launch();
     }
-    k_scan_tiles<<<(unsigned)ntiles, SCAN_THREADS, 0, st>>>(counts, nscan, tsum);
-    note_launch();
-    k_scan_sums<<<1, 1024, 0, st>>>(tsum, ntiles);
-    note_launch();
-    k_scan_add<<<(unsigned)((nscan + 255) / 256), 256, 0, st>>>(counts, nscan, tsum);
-    note_launch();
+    launch_exclusive_scan(counts, nscan, tsum, st);
     if (ngal > 0) {
         if (mixed)
             k_deposit_scatter_mixed<<<(unsigned)((ngal + 255) / 256), 256, 0, st>>>(w, ngal, key, rank, xdf, counts,

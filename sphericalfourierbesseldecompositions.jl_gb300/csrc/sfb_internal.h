@@ -209,6 +209,9 @@ void launch_project_mixed(const Plan &p, const float2 *Adf, int64_t ldA, const f
 void launch_split_mean(double *maps, int64_t nmaps, int64_t npix, const double *ref, double *nu, cudaStream_t st);
 // nzr (FP64): receives the first / last ring pair holding a non-zero value in any map
 // (preset by the caller to a large value / -1).
+// Exclusive prefix sum of n int32 counters in place; tile_sums holds scan_tile_count(n) ints.
+int64_t scan_tile_count(int64_t n);
+void launch_exclusive_scan(int32_t *data, int64_t n, int32_t *tile_sums, cudaStream_t st);
 void launch_ring_analysis(const Plan &p, const double *maps, int64_t nmaps, double *F, cudaStream_t st,
                           int *nzr = nullptr);
 void launch_ring_synthesis(const Plan &p, const double *G, int64_t nmaps, double *maps, cudaStream_t st);

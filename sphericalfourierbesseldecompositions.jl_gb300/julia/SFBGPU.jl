@@ -19,6 +19,7 @@ module SFBGPU
 
 using SphericalFourierBesselDecompositions
 const SFB = SphericalFourierBesselDecompositions
+using Random
 import ChainRulesCore
 using ChainRulesCore: NoTangent, ZeroTangent, AbstractZero, unthunk, @not_implemented
 
@@ -289,6 +290,30 @@ function ChainRulesCore.rrule(::typeof(field2anlm), f_xyz, wmodes, amodes; kw...
         return (NoTangent(), df, NoTangent(), NoTangent())
     end
     return a, field2anlm_pullback
+end
+
+"""
+    apply_window(rθϕ, win, wmodes; rng=Random.GLOBAL_RNG)    (src/windows.jl:169-216)
+
+Same contract as `SFB.apply_window`: the galaxies kept by the window, in input
+order.  The uniform draws come from `rand(rng, N)` on the host, so the same
+`rng` state gives the reference's selection; the test on each galaxy runs on
+the GPU.
+"""
+function apply_window(rθϕ, win, wmodes; rng=Random.GLOBAL_RNG)
+    r = Matrix{Float64}(rθϕ)
+    N = size(r, 2)
+    W = Matrix{Float64}(win)                  # nr × npix
+    u = rand(rng, N)
+    out = Matrix{Float64}(undef, 3, N)
+    kept = Ref{Int64}(0)
+    GC.@preserve r W u out check(ccall((:sfb_apply_window, libsfb), Cint,
+                                       (Int64, Ptr{Float64}, Int64, Float64, Float64, Float64, Ptr{Float64}, Int64,
+                                        Ptr{Float64}, UInt64, Ptr{Float64}, Ref{Int64}),
+                                       wmodes.nside, W, size(W, 1), wmodes.rmin, wmodes.rmax, wmodes.Δr,
+                                       N == 0 ? C_NULL : r, N, N == 0 ? C_NULL : u, UInt64(0),
+                                       N == 0 ? C_NULL : out, kept))
+    return out[:, 1:kept[]]
 end
 
 """

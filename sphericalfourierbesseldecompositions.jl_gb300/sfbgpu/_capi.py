@@ -75,6 +75,12 @@ _PROTOS = [
     ("sfb_winweights2galweights_noalloc", C.c_int, [C.c_int64, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
                                                     C.c_int64, C.c_void_p]),
     ("sfb_ang2pix_ring", C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
+    ("sfb_apply_window", C.c_int, [C.c_int64, C.c_void_p, C.c_int64, C.c_double, C.c_double, C.c_double,
+                                   C.c_void_p, C.c_int64, C.c_void_p, C.c_uint64, C.c_void_p,
+                                   C.POINTER(C.c_int64)]),
+    ("sfb_apply_window_device", C.c_int, [C.c_int64, C.c_void_p, C.c_int64, C.c_double, C.c_double, C.c_double,
+                                          C.c_void_p, C.c_int64, C.c_void_p, C.c_uint64, C.c_void_p,
+                                          C.POINTER(C.c_int64), C.c_void_p]),
     ("sfb_set_profiling", C.c_int, [C.c_void_p, C.c_int32]),
     ("sfb_get_stage_times", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     ("sfb_launch_count", C.c_int64, []),

@@ -20,7 +20,7 @@ from .modes import getnlmsize
 from .windows import SeparableArray
 
 __all__ = ["GPUPlan", "get_plan", "cat2amln", "cat2nlm", "field2anlm", "anlm2field", "win_rhat_ln",
-           "map2alm", "ang2pix_ring", "amln2clnn", "anlm2clnn", "winweights2galweights"]
+           "map2alm", "ang2pix_ring", "amln2clnn", "anlm2clnn", "winweights2galweights", "apply_window"]
 
 _PRECISION = {"fp64": capi.SFB_FP64, "mixed": capi.SFB_MIXED}
 _RADIAL = {"poly": capi.SFB_RADIAL_POLY, "spline": capi.SFB_RADIAL_SPLINE}
@@ -325,3 +325,27 @@ def winweights2galweights(weights, wmodes, rtp):
     capi.check(capi.lib.sfb_winweights2galweights(wmodes.nside, capi.ptr(W), W.shape[0], capi.ptr(rb),
                                                   capi.ptr(gal), gal.shape[0], capi.ptr(out)))
     return out
+
+
+def apply_window(rtp, win, wmodes, seed=0, uniform=None):
+    """Galaxies of rtp (3, N) kept by the (nr, npix) window (reference
+    apply_window, src/windows.jl:169-216), in input order: kept when
+    rmin <= r <= rmax and u <= win[shell, pix] / max(win), with u the given
+    ``uniform`` draws (one per galaxy, like the reference's rand(rng)) or the
+    library's counter-based stream for ``seed``.  Returns (3, nkept)."""
+    W = np.asfortranarray(win, float)
+    if W.shape != (wmodes.nr, nside2npix(wmodes.nside)):
+        raise ValueError("window must be nr x npix")
+    gal = np.ascontiguousarray(np.asarray(rtp, float).T)
+    n = gal.shape[0]
+    u = None
+    if uniform is not None:
+        u = np.ascontiguousarray(uniform, float)
+        if u.shape != (n,):
+            raise ValueError("one uniform draw per galaxy")
+    out = np.empty((max(n, 1), 3))
+    kept = capi.C.c_int64(0)
+    capi.check(capi.lib.sfb_apply_window(wmodes.nside, capi.ptr(W), wmodes.nr, wmodes.rmin, wmodes.rmax,
+                                         wmodes.dr, capi.ptr(gal) if n else None, n, capi.ptr(u),
+                                         int(seed) & 0xFFFFFFFFFFFFFFFF, capi.ptr(out), capi.C.byref(kept)))
+    return np.ascontiguousarray(out[:kept.value].T)

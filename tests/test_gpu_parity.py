@@ -362,3 +362,48 @@ def test_winweights2galweights_vs_oracle():
     with pytest.raises(capi.SFBError) as e:
         sfbgpu.winweights2galweights(W, wm, bad)
     assert e.value.status == capi.SFB_ERANGE
+
+
+@pytest.mark.parametrize("draws", ["uniform", "seed"])
+def test_apply_window_vs_oracle(draws):
+    """Device thinning (sfb_apply_window) against the oracle, bit-exact: the same
+    kept galaxies in the same order, with the caller's draws or the library's
+    counter-based stream; edge radii r == rmin, r == rmax and r beyond included."""
+    nside, nr, rmin, rmax = 64, 40, 500.0, 1000.0
+    wm = sfbgpu.ConfigurationSpaceModes(rmin, rmax, nr, nside)
+    rng = np.random.default_rng(12)
+    th, _ = sfbgpu.pix2ang_ring(nside, np.arange(wm.npix))
+    win = np.exp(-((wm.r[:, None] - 750.0) / 150.0) ** 2) * (np.cos(th)[None, :] > -0.2)
+    win = win * rng.uniform(0.5, 1.0, win.shape)
+    rtp, _ = catalogue(300_000, rmin, rmax, seed=13, rpad=25.0)
+    rtp[0, :4] = [rmin, rmax, rmin + 7 * wm.dr, rmax + 1e-9]
+    n = rtp.shape[1]
+    if draws == "uniform":
+        u = rng.random(n)
+        gpu = sfbgpu.apply_window(rtp, win, wm, uniform=u)
+    else:
+        u = osfb.splitmix64_uniform(2024, n)
+        gpu = sfbgpu.apply_window(rtp, win, wm, seed=2024)
+    ref = osfb.apply_window(rtp, win, rmin, rmax, wm.dr, nside, u)
+    record(f"apply_window_{draws}_kept", float(gpu.shape[1]), of=n)
+    assert gpu.shape == ref.shape and np.array_equal(gpu, ref)
+
+
+def test_apply_window_edges():
+    nside, nr = 4, 5
+    wm = sfbgpu.ConfigurationSpaceModes(500.0, 1000.0, nr, nside)
+    win = np.ones((nr, wm.npix))
+    empty = sfbgpu.apply_window(np.zeros((3, 0)), win, wm)
+    assert empty.shape == (3, 0)
+    rtp = np.array([[700.0, 800.0], [1.0, 4.0], [0.5, 0.5]])        # theta > pi inside the shells
+    with pytest.raises(capi.SFBError) as e:
+        sfbgpu.apply_window(rtp, win, wm)
+    assert e.value.status == capi.SFB_ERANGE
+    bad = win.copy()
+    bad[0, 0] = np.nan
+    with pytest.raises(capi.SFBError) as e:
+        sfbgpu.apply_window(rtp[:, :1], bad, wm)
+    assert e.value.status == capi.SFB_ENONFINITE
+    # every galaxy kept where win == max(win)
+    rtp, _ = catalogue(1000, 500.0, 1000.0, seed=3)
+    assert np.array_equal(sfbgpu.apply_window(rtp, win, wm, seed=1), rtp)
