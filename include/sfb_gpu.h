@@ -195,6 +195,19 @@ int sfb_win_rhat_ln_separable(sfb_plan *plan, const double *phi, int64_t nr, dou
 int sfb_win_rhat_ln_dense(sfb_plan *plan, const double *win, int64_t nr, double rmin,
                           double rmax, double *w_out);
 
+/* win_lnn(win, wmodes, cmodes) (reference src/windows.jl:382-392 with
+ * calc_intr_gg_fn :394-422): for every column i of lnn (ClnnModes.lnn,
+ * 3 x nlnn column-major: l, n1, n2 with 1-based n),
+ *   out[i] = sum_s r_s^2 dr g_{n1 l}(r_s) g_{n2 l}(r_s) W00_s / sqrt(4 pi),
+ * r_s the shell midpoints of ConfigurationSpaceModes(rmin, rmax, nr) and W00_s
+ * the a_00 of shell s of the window (map2alm to lmax 2 lmax with the plan's
+ * niter, as the reference's calc_Wr_lm(win, 2 lmax, nside)).  win: [nr * npix]
+ * at the plan's nside, element (ir, p) at ir + nr*p.  A shell with a negative
+ * mean makes the reference's square roots NaN: SFB_ENONFINITE here.  The first
+ * call builds the plan's transform at 2 lmax (needs 2 lmax <= 4 nside). */
+int sfb_win_lnn(sfb_plan *plan, const double *win, int64_t nr, double rmin, double rmax, const int64_t *lnn,
+                int64_t nlnn, double *out);
+
 /* Batched map2alm with the plan's niter (the transform behind mymap2alm!,
  * src/healpix_helpers.jl:50-56).  maps: [nmaps * npix], map b at b*npix.
  * alm_out: [nmaps * 2 * lmsize], lmsize = (lmax+1)(lmax+2)/2, index l(l+1)/2+m. */

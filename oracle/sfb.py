@@ -11,6 +11,7 @@ and follows one reference function:
 * ``integrate_window`` src/windows.jl:219-228
 * ``amln2clnn``      src/SphericalFourierBesselDecompositions.jl:114-150
 * ``winweights2galweights`` src/cat2anlm.jl:218-238
+* ``win_lnn``        src/windows.jl:382-422 (W00 from map2alm at 2 lmax, trapezoidal radial sum)
 * ``apply_window``   src/windows.jl:169-216 (the uniform draws passed in;
   ``splitmix64_uniform`` restates the library's counter-based stream)
 
@@ -236,3 +237,23 @@ def apply_window(rtp, win, rmin, rmax, dr, nside, uniform):
     pix = ang2pix_ring(nside, th[idx], ph[idx])
     keep[idx] = uniform[idx] <= win[ir - 1, pix] * oow
     return rtp[:, keep]
+
+
+def win_lnn(win, rmin, rmax, nr, modes, lnn, niter=3):
+    """win_lnn (src/windows.jl:382-392) with calc_intr_gg_fn (:394-422):
+    W00 = a_00 of every shell from map2alm to lmax 2 lmax (calc_Wr_lm), then
+    sum over the shell midpoints of (g r sqrt(dr) sqrt(f)) (g' r sqrt(dr) sqrt(f)),
+    f = W00 / sqrt(4 pi), for every column (l, n, n') of lnn (3 x nlnn)."""
+    dr = (rmax - rmin) / nr
+    rs = np.linspace(rmin + dr / 2, rmax - dr / 2, nr)
+    L2 = 2 * modes["lmax"]
+    alm = SHT(modes["nside"], L2).map2alm(np.asarray(win, float), niter=niter)
+    f = alm[:, 0, 0].real / np.sqrt(4 * np.pi)
+    meas = rs * np.sqrt(dr) * np.sqrt(f)
+    out = np.empty(lnn.shape[1])
+    for i in range(lnn.shape[1]):
+        l, n1, n2 = (int(v) for v in lnn[:, i])
+        g1 = spline_eval(*modes["splines"][(n1, l)], rs) * meas
+        g2 = spline_eval(*modes["splines"][(n2, l)], rs) * meas
+        out[i] = g1 @ g2
+    return out

@@ -91,6 +91,9 @@ void launch_winweights(const double *weights, int64_t nr, int64_t nside, const d
                        const double *rtp, int64_t ngal, double *w, int *err, cudaStream_t st);
 void launch_amln2clnn(const double *a1, const double *a2, int64_t nlmsize, const int64_t *lnn, int64_t nlnn,
                       int64_t nbatch, const int64_t *noff, double *out, cudaStream_t st);
+void launch_win_lnn(const Plan &p, const int32_t *pair_index, const double *gtab, int64_t nr, double rmin, double dr,
+                    const double *w00, const int64_t *lnn, int64_t nlnn, double *out, cudaStream_t st);
+void launch_extract_a00(const double *alm, int64_t ldA, int64_t nm, double *w00, cudaStream_t st);
 
 }  // namespace sfb
 
@@ -106,6 +109,9 @@ struct sfb_plan {
     cudaEvent_t ev_copy[NCOPY] = {};
     int32_t *d_pair_index = nullptr;
     int64_t *d_noff = nullptr;
+    // FP64 transform at lmax 2 lmax for the window harmonics of win_lnn (the reference's
+    // calc_Wr_lm), created on first use
+    sfb_plan *aux = nullptr;
     // stage profiling (events on the call's stream)
     bool profile = false;
     struct Rec {
@@ -1001,6 +1007,7 @@ void sfb_plan_destroy(sfb_plan *h) {
                     p.ref.ptr, p.rf.ptr, p.rg.ptr, p.rr.ptr, p.ralm.ptr, p.almdf2.ptr, p.adf0.ptr, p.ecoef.ptr, p.erow.ptr, p.almdf.ptr, p.nzr64.ptr, h->d_pair_index, h->d_noff};
     for (void *q : ptrs)
         if (q) cudaFree(q);
+    if (h->aux) sfb_plan_destroy(h->aux);
     collect_stages(h);
     for (cudaEvent_t e : h->pool) cudaEventDestroy(e);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -1490,6 +1497,99 @@ static int sfb_anlm2field_impl(sfb_plan *h, const double *anlm, int64_t nr, doub
     SFB_CUDA_TRY(cudaGetLastError());
     SFB_CUDA_TRY(cudaMemcpyAsync(f_out, d_f, (size_t)nr * p.npix * sizeof(double), cudaMemcpyDeviceToHost, st));
     SFB_CUDA_TRY(cudaStreamSynchronize(st));
+    return SFB_OK;
+}
+
+// The plan's auxiliary FP64 transform at lmax 2 lmax (same nside and niter): one radial
+// mode, placeholder splines (it only runs map2alm).
+static int aux_plan(sfb_plan *h, sfb_plan **out) {
+    if (!h->aux) {
+        const Plan &p = h->p;
+        const int64_t L = 2 * (int64_t)p.lmax;
+        std::vector<int64_t> lmax_n{L}, off((size_t)L + 2);
+        std::vector<double> x, zero((size_t)(2 * (L + 1)), 0.0);
+        for (int64_t l = 0; l <= L + 1; ++l) off[(size_t)l] = 2 * l;
+        for (int64_t l = 0; l <= L; ++l) {
+            x.push_back(p.rmin);
+            x.push_back(p.rmax);
+        }
+        sfb_plan_desc d{};
+        d.nside = p.nside;
+        d.lmax = L;
+        d.nmax = 1;
+        d.lmax_n = lmax_n.data();
+        d.rmin = p.rmin;
+        d.rmax = p.rmax;
+        d.spl_offset = off.data();
+        d.spl_x = x.data();
+        d.spl_y = zero.data();
+        d.spl_ypp = zero.data();
+        d.niter = p.niter;
+        d.precision = SFB_FP64;
+        d.radial_mode = SFB_RADIAL_SPLINE;
+        SFB_TRY(sfb_plan_create(&d, &h->aux));
+    }
+    *out = h->aux;
+    return SFB_OK;
+}
+
+// a_00 of every shell of a window field win [nr * npix] ((ir, p) at ir + nr p, host), from
+// map2alm at lmax 2 lmax with the plan's niter (the reference's calc_Wr_lm(win, 2 lmax, nside)[:, 1]);
+// w00 [nr] on the device of h.
+static int window_a00(sfb_plan *h, const double *win, int64_t nr, double *w00) {
+    sfb_plan *ax = nullptr;
+    SFB_TRY(aux_plan(h, &ax));
+    Plan &q = ax->p;
+    cudaStream_t st = ax->stream;
+    const int64_t cs = std::max<int64_t>(1, std::min<int64_t>(nr, chunk_pairs(q)));
+    SFB_TRY(grow(q, q.scratch, (size_t)(nr * q.npix)));
+    SFB_CUDA_TRY(cudaMemcpyAsync(q.scratch.ptr, win, (size_t)nr * q.npix * sizeof(double), cudaMemcpyHostToDevice,
+                                 st));
+    for (int64_t s0 = 0; s0 < nr; s0 += cs) {
+        const int64_t nsc = std::min(cs, nr - s0);
+        SFB_TRY(grow(q, q.maps, (size_t)nsc * q.npix));
+        launch_transpose_ld(q.scratch.ptr + s0, nr, q.npix, nsc, q.maps.ptr, q.npix, st);
+        SFB_TRY(sht_analysis(ax, q.maps.ptr, nsc, st));
+        launch_extract_a00(q.alm.ptr, 2 * nsc, nsc, w00 + s0, st);
+    }
+    SFB_CUDA_TRY(cudaStreamSynchronize(st));
+    SFB_CUDA_TRY(cudaGetLastError());
+    return SFB_OK;
+}
+
+int sfb_win_lnn(sfb_plan *h, const double *win, int64_t nr, double rmin, double rmax, const int64_t *lnn,
+                int64_t nlnn, double *out) {
+    SFB_TRY(check_plan(h));
+    SFB_TRY(set_device_of(h));
+    if (!win || !lnn || nlnn < 0 || (nlnn > 0 && !out) || nr < 1 || !(rmin < rmax))
+        return fail(SFB_EINVAL, "bad win_lnn arguments");
+    if (nlnn == 0) return SFB_OK;
+    Plan &p = h->p;
+    if (2 * (int64_t)p.lmax > 4 * p.nside)
+        return fail(SFB_ERANGE, "win_lnn: window harmonics to 2 lmax need 2 lmax <= 4 nside");
+    for (int64_t i = 0; i < nlnn; ++i) {
+        const int64_t l = lnn[3 * i], n1 = lnn[3 * i + 1], n2 = lnn[3 * i + 2];
+        if (l < 0 || l > p.lmax || n1 < 1 || n2 < 1 || n1 > p.lmax_n.size() || n2 > p.lmax_n.size() ||
+            l > p.lmax_n[n1 - 1] || l > p.lmax_n[n2 - 1])
+            return fail(SFB_EINVAL, "win_lnn: (l, n, n') outside the modes");
+    }
+    cudaStream_t st = h->stream;
+    // [w00 nr][gtab npairs x nr][lnn 3 nlnn (int64)][out nlnn]
+    SFB_TRY(grow(p, p.scratch2, (size_t)(nr + p.npairs * nr + 3 * nlnn + nlnn)));
+    double *d_w00 = p.scratch2.ptr, *d_g = d_w00 + nr;
+    int64_t *d_lnn = reinterpret_cast<int64_t *>(d_g + p.npairs * nr);
+    double *d_out = reinterpret_cast<double *>(d_lnn + 3 * nlnn);
+    SFB_TRY(window_a00(h, win, nr, d_w00));
+    const double dr = (rmax - rmin) / (double)nr;
+    launch_gtab(p, nr, rmin, dr, 0, d_g, st);                  // g_nl(r_s) at the shell midpoints
+    SFB_CUDA_TRY(cudaMemcpyAsync(d_lnn, lnn, (size_t)3 * nlnn * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    launch_win_lnn(p, h->d_pair_index, d_g, nr, rmin, dr, d_w00, d_lnn, nlnn, d_out, st);
+    SFB_CUDA_TRY(cudaMemcpyAsync(out, d_out, (size_t)nlnn * sizeof(double), cudaMemcpyDeviceToHost, st));
+    SFB_CUDA_TRY(cudaStreamSynchronize(st));
+    SFB_CUDA_TRY(cudaGetLastError());
+    for (int64_t i = 0; i < nlnn; ++i)
+        if (!std::isfinite(out[i]))
+            return fail(SFB_ENONFINITE, "win_lnn: non-finite result (a shell with a negative window mean)");
     return SFB_OK;
 }
 

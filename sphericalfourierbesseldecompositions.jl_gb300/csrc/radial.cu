@@ -739,3 +739,49 @@ void launch_fill(double *x, int64_t n, double v, cudaStream_t st) {
 }
 
 }  // namespace sfb
+
+namespace sfb {
+
+// w00[s] = Re a_00 of map s of an FP64 a_lm set (row lm = 0, columns 2 s / 2 s + 1)
+__global__ void k_extract_a00(const double *alm, int64_t nm, double *w00) {
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < nm) w00[s] = alm[2 * s];
+}
+
+void launch_extract_a00(const double *alm, int64_t ldA, int64_t nm, double *w00, cudaStream_t st) {
+    (void)ldA;
+    k_extract_a00<<<(unsigned)((nm + 127) / 128), 128, 0, st>>>(alm, nm, w00);
+    note_launch();
+}
+
+// win_lnn radial integrals (reference calc_intr_gg_fn, src/windows.jl:394-422, trapezoidal
+// nodes = shell midpoints, weights = dr, f = W00 / sqrt(4 pi)): one warp per column i of lnn,
+//   out[i] = sum_s (g_nl(r_s) r_s sqrt(dr) sqrt(f_s)) (g_n'l(r_s) r_s sqrt(dr) sqrt(f_s)).
+__global__ void k_win_lnn(const int32_t *__restrict__ pair_index, int lmax, const double *__restrict__ gtab,
+                          int64_t nr, double rmin, double dr, const double *__restrict__ w00,
+                          const int64_t *__restrict__ lnn, int64_t nlnn, double *__restrict__ out) {
+    const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= nlnn) return;
+    const int64_t l = lnn[3 * i], n1 = lnn[3 * i + 1], n2 = lnn[3 * i + 2];
+    const double *g1 = gtab + (int64_t)pair_index[(n1 - 1) * (lmax + 1) + l] * nr;
+    const double *g2 = gtab + (int64_t)pair_index[(n2 - 1) * (lmax + 1) + l] * nr;
+    const double sdr = sqrt(dr), inv4pi = 1.0 / sqrt(4.0 * M_PI);
+    double acc = 0.0;
+    for (int64_t s = lane; s < nr; s += 32) {
+        const double r = rmin + dr / 2 + s * dr;                 // the shell midpoints of k_gtab
+        const double w = r * sdr * sqrt(w00[s] * inv4pi);
+        acc = fma(g1[s] * w, g2[s] * w, acc);
+    }
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+    if (lane == 0) out[i] = acc;
+}
+
+void launch_win_lnn(const Plan &p, const int32_t *pair_index, const double *gtab, int64_t nr, double rmin, double dr,
+                    const double *w00, const int64_t *lnn, int64_t nlnn, double *out, cudaStream_t st) {
+    k_win_lnn<<<(unsigned)((nlnn * 32 + 127) / 128), 128, 0, st>>>(pair_index, p.lmax, gtab, nr, rmin, dr, w00, lnn,
+                                                                    nlnn, out);
+    note_launch();
+}
+
+}  // namespace sfb

@@ -20,7 +20,7 @@ from .modes import getnlmsize
 from .windows import SeparableArray
 
 __all__ = ["GPUPlan", "get_plan", "cat2amln", "cat2nlm", "field2anlm", "anlm2field", "win_rhat_ln",
-           "map2alm", "ang2pix_ring", "amln2clnn", "anlm2clnn", "winweights2galweights", "apply_window"]
+           "map2alm", "ang2pix_ring", "amln2clnn", "anlm2clnn", "winweights2galweights", "apply_window", "win_lnn"]
 
 _PRECISION = {"fp64": capi.SFB_FP64, "mixed": capi.SFB_MIXED}
 _RADIAL = {"poly": capi.SFB_RADIAL_POLY, "spline": capi.SFB_RADIAL_SPLINE}
@@ -349,3 +349,17 @@ def apply_window(rtp, win, wmodes, seed=0, uniform=None):
                                          wmodes.dr, capi.ptr(gal) if n else None, n, capi.ptr(u),
                                          int(seed) & 0xFFFFFFFFFFFFFFFF, capi.ptr(out), capi.C.byref(kept)))
     return np.ascontiguousarray(out[:kept.value].T)
+
+
+def win_lnn(win, wmodes, cmodes, **plan_opts):
+    """W_l(n, n') = sum_s r_s^2 dr g_nl(r_s) g_n'l(r_s) W00(r_s) / sqrt(4 pi) for every (l, n, n')
+    of cmodes.lnn (reference win_lnn, src/windows.jl:382-392); win is (nr, npix)."""
+    plan = get_plan(cmodes.amodesA, **plan_opts)
+    W = np.asfortranarray(win, float)
+    if W.shape != (wmodes.nr, plan.npix):
+        raise ValueError("window must be nr x npix at the plan's nside")
+    lnn = np.ascontiguousarray(cmodes.lnn.T, np.int64)
+    out = np.empty(lnn.shape[0])
+    capi.check(capi.lib.sfb_win_lnn(plan.handle, capi.ptr(W), wmodes.nr, wmodes.rmin, wmodes.rmax, capi.ptr(lnn),
+                                    lnn.shape[0], capi.ptr(out)))
+    return out

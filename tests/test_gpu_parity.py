@@ -407,3 +407,25 @@ def test_apply_window_edges():
     # every galaxy kept where win == max(win)
     rtp, _ = catalogue(1000, 500.0, 1000.0, seed=3)
     assert np.array_equal(sfbgpu.apply_window(rtp, win, wm, seed=1), rtp)
+
+
+def test_win_lnn_vs_oracle():
+    """W_l(n, n') of a window (radial selection x a mask tilted with
+    direction) against the oracle's restatement of the reference: the shell
+    a_00 from map2alm at 2 lmax, the trapezoidal radial sum.  FP64: 1e-12."""
+    a = sfbgpu.AnlmModes(0.05, 500.0, 1000.0, nside=32)
+    wm = sfbgpu.ConfigurationSpaceModes(a.rmin, a.rmax, 60, a.nside)
+    th, ph = sfbgpu.pix2ang_ring(a.nside, np.arange(wm.npix))
+    win = np.exp(-((wm.r[:, None] - 700.0) / 180.0) ** 2) * (1.0 + 0.3 * np.cos(th)[None, :]
+                                                            + 0.1 * np.sin(3 * ph)[None, :] * np.sin(th)[None, :])
+    cm = sfbgpu.ClnnModes(a, dnmax=3)
+    gpu = sfbgpu.win_lnn(win, wm, cm)
+    ref = osfb.win_lnn(win, a.rmin, a.rmax, wm.nr, modes_dict(a), cm.lnn)
+    e = rel_err(gpu, ref)
+    record("win_lnn_vs_oracle", e, nlnn=int(cm.lnn.shape[1]))
+    assert e < 1e-12
+    neg = win.copy()
+    neg[3] = -1.0
+    with pytest.raises(capi.SFBError) as ex:
+        sfbgpu.win_lnn(neg, wm, cm)
+    assert ex.value.status == capi.SFB_ENONFINITE
