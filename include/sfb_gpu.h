@@ -208,6 +208,21 @@ int sfb_win_rhat_ln_dense(sfb_plan *plan, const double *win, int64_t nr, double 
 int sfb_win_lnn(sfb_plan *plan, const double *win, int64_t nr, double rmin, double rmax, const int64_t *lnn,
                 int64_t nlnn, double *out);
 
+/* calc_wmix(win, wmodes, amodes; neg_m) (reference src/windows.jl:299-366,
+ * calc_wmix_ii :273-296, calc_gaunts_L :451-465): the window mixing matrix
+ *   W[(n l m), (n' l' m')] = (-1)^m sum_L G(l, l', L; -m, m')
+ *                            sum_s g_nl(r_s) g_n'l'(r_s) r_s^2 dr W_{L, m - m'}(r_s),
+ * G the Gaunt coefficient sqrt((2L+1)(2l+1)(2l'+1)/4 pi) (l l' L; 0 0 0)
+ * (L l l'; m - m', -m, m'), m = 0..l (m = -0..-l when neg_m), m' = 0..l',
+ * W_LM(r_s) the a_lm of window shell s to lmax 2 lmax (map2alm with the
+ * plan's niter, the reference's calc_Wr_lm), W_{L,-M} = (-1)^M conj(W_LM).
+ * win: [nr * npix] at the plan's nside, element (ir, p) at ir + nr*p.
+ * wmix_out: [nlmsize x nlmsize] complex, column-major like Julia's
+ * Matrix{ComplexF64}: element (i, j) at 2 (i + nlmsize j).  Supports
+ * lmax <= 128 (SFB_ENOTSUP beyond); the output alone is 16 nlmsize^2 bytes. */
+int sfb_calc_wmix(sfb_plan *plan, const double *win, int64_t nr, double rmin, double rmax, int32_t neg_m,
+                  double *wmix_out);
+
 /* Batched map2alm with the plan's niter (the transform behind mymap2alm!,
  * src/healpix_helpers.jl:50-56).  maps: [nmaps * npix], map b at b*npix.
  * alm_out: [nmaps * 2 * lmsize], lmsize = (lmax+1)(lmax+2)/2, index l(l+1)/2+m. */

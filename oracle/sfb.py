@@ -12,6 +12,7 @@ and follows one reference function:
 * ``amln2clnn``      src/SphericalFourierBesselDecompositions.jl:114-150
 * ``winweights2galweights`` src/cat2anlm.jl:218-238
 * ``win_lnn``        src/windows.jl:382-422 (W00 from map2alm at 2 lmax, trapezoidal radial sum)
+* ``calc_wmix``      src/windows.jl:299-366, 273-296, 451-465 (exact Racah 3j symbols)
 * ``apply_window``   src/windows.jl:169-216 (the uniform draws passed in;
   ``splitmix64_uniform`` restates the library's counter-based stream)
 
@@ -256,4 +257,56 @@ def win_lnn(win, rmin, rmax, nr, modes, lnn, niter=3):
         g1 = spline_eval(*modes["splines"][(n1, l)], rs) * meas
         g2 = spline_eval(*modes["splines"][(n2, l)], rs) * meas
         out[i] = g1 @ g2
+    return out
+
+
+def wigner3j(j1, j2, j3, m1, m2, m3):
+    """Wigner 3j symbol from the Racah formula in exact integer arithmetic."""
+    import math
+    from fractions import Fraction
+    if (m1 + m2 + m3 != 0 or not (abs(j1 - j2) <= j3 <= j1 + j2) or abs(m1) > j1 or abs(m2) > j2
+            or abs(m3) > j3):
+        return 0.0
+    f = math.factorial
+    pre = Fraction(f(j1 + j2 - j3) * f(j1 - j2 + j3) * f(-j1 + j2 + j3), f(j1 + j2 + j3 + 1))
+    pre *= f(j1 + m1) * f(j1 - m1) * f(j2 + m2) * f(j2 - m2) * f(j3 + m3) * f(j3 - m3)
+    s = 0
+    for k in range(max(0, j2 - j3 - m1, j1 - j3 + m2), min(j1 + j2 - j3, j1 - m1, j2 + m2) + 1):
+        s += Fraction((-1) ** k, f(k) * f(j1 + j2 - j3 - k) * f(j1 - m1 - k) * f(j2 + m2 - k)
+                      * f(j3 - j2 + m1 + k) * f(j3 - j1 - m2 + k))
+    if s == 0:
+        return 0.0
+    return (-1) ** (j1 - j2 - m3) * (1 if s > 0 else -1) * math.sqrt(float(s * s * pre))
+
+
+def calc_wmix(win, rmin, rmax, nr, modes, neg_m=False, niter=3):
+    """Window mixing matrix (src/windows.jl:299-366 with calc_wmix_ii :273-296 and
+    calc_gaunts_L :451-465), nlmsize x nlmsize complex."""
+    from functools import lru_cache
+    dr = (rmax - rmin) / nr
+    rs = np.linspace(rmin + dr / 2, rmax - dr / 2, nr)
+    L2 = 2 * modes["lmax"]
+    Wlm = SHT(modes["nside"], L2).map2alm(np.asarray(win, float), niter=niter)     # [s, L, M]
+    w3 = lru_cache(maxsize=None)(wigner3j)
+    g = {pr: spline_eval(*modes["splines"][pr], rs) * rs * np.sqrt(dr) for pr in pairs(modes)}
+    N = nlmsize(modes)
+    out = np.full((N, N), np.nan + 1j * np.nan)
+    for (n, l) in pairs(modes):
+        for (n2, l2) in pairs(modes):
+            gg = g[(n, l)] * g[(n2, l2)]
+            H = np.einsum("s,sLM->LM", gg, Wlm)
+            for am in range(l + 1):
+                m = -am if neg_m else am
+                for m2 in range(l2 + 1):
+                    M = m - m2
+                    w = 0j
+                    for L in range(abs(l - l2), l + l2 + 1):
+                        if abs(M) > L:
+                            continue
+                        gnt = np.sqrt((2 * L + 1) * (2 * l + 1) * (2 * l2 + 1) / (4 * np.pi)) \
+                            * w3(l, l2, L, 0, 0, 0) * w3(L, l, l2, M, -m, m2)
+                        w += gnt * H[L, abs(M)]
+                    if M < 0:
+                        w = (-1) ** M * np.conj(w)
+                    out[_idx0(modes, n, l, am), _idx0(modes, n2, l2, m2)] = (-1) ** m * w
     return out

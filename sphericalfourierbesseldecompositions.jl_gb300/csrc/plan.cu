@@ -1593,6 +1593,71 @@ int sfb_win_lnn(sfb_plan *h, const double *win, int64_t nr, double rmin, double 
     return SFB_OK;
 }
 
+int sfb_calc_wmix(sfb_plan *h, const double *win, int64_t nr, double rmin, double rmax, int32_t neg_m,
+                  double *wmix_out) {
+    SFB_TRY(check_plan(h));
+    SFB_TRY(set_device_of(h));
+    if (!win || !wmix_out || nr < 1 || !(rmin < rmax)) return fail(SFB_EINVAL, "bad calc_wmix arguments");
+    Plan &p = h->p;
+    if (p.lmax > WMIX_LMAX) return fail(SFB_ENOTSUP, "calc_wmix: lmax above " + std::to_string(WMIX_LMAX));
+    if (2 * (int64_t)p.lmax > 4 * p.nside)
+        return fail(SFB_ERANGE, "calc_wmix: window harmonics to 2 lmax need 2 lmax <= 4 nside");
+    const size_t smem = wmix_smem_bytes((int)p.lmax, (int)p.lmax, nr, neg_m ? 1 : 0);
+    if (smem > 200 * 1024) return fail(SFB_ENOTSUP, "calc_wmix: too many shells for one CTA's shared memory");
+    const int64_t LW = 2 * (int64_t)p.lmax, lmsW = (LW + 1) * (LW + 2) / 2;
+    const size_t outn = (size_t)2 * p.nlmsize * p.nlmsize;
+    // [window harmonics lmsW x 2 nr (shell-major rows)][g table npairs x nr][wmix 2 nlmsize^2]
+    double *d = nullptr;
+    const size_t total = (size_t)lmsW * 2 * nr + (size_t)p.npairs * nr + outn;
+    if (cudaMalloc(&d, total * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(SFB_ENOMEM, "calc_wmix: device allocation failed");
+    }
+    double *WT = d, *d_g = WT + (size_t)lmsW * 2 * nr, *d_out = d_g + (size_t)p.npairs * nr;
+    int st = SFB_OK;
+    do {
+        sfb_plan *ax = nullptr;
+        if ((st = aux_plan(h, &ax)) != SFB_OK) break;
+        Plan &q = ax->p;
+        cudaStream_t as = ax->stream;
+        const int64_t cs = std::max<int64_t>(1, std::min<int64_t>(nr, chunk_pairs(q)));
+        if ((st = grow(q, q.scratch, (size_t)(nr * q.npix))) != SFB_OK) break;
+        if (cudaMemcpyAsync(q.scratch.ptr, win, (size_t)nr * q.npix * sizeof(double), cudaMemcpyHostToDevice, as) !=
+            cudaSuccess) {
+            st = fail(SFB_ECUDA, "calc_wmix: window copy failed");
+            break;
+        }
+        for (int64_t s0 = 0; s0 < nr && st == SFB_OK; s0 += cs) {
+            const int64_t nsc = std::min(cs, nr - s0);
+            if ((st = grow(q, q.maps, (size_t)nsc * q.npix)) != SFB_OK) break;
+            launch_transpose_ld(q.scratch.ptr + s0, nr, q.npix, nsc, q.maps.ptr, q.npix, as);
+            if ((st = sht_analysis(ax, q.maps.ptr, nsc, as)) != SFB_OK) break;
+            // rows lm of the chunk's a_lm (2 nsc doubles) into columns 2 s0 .. of WT's rows
+            if (cudaMemcpy2DAsync(WT + 2 * s0, 2 * nr * sizeof(double), q.alm.ptr, 2 * nsc * sizeof(double),
+                                  2 * nsc * sizeof(double), (size_t)lmsW, cudaMemcpyDeviceToDevice, as) != cudaSuccess) {
+                st = fail(SFB_ECUDA, "calc_wmix: harmonics copy failed");
+                break;
+            }
+        }
+        if (st != SFB_OK) break;
+        if (cudaStreamSynchronize(as) != cudaSuccess) {
+            st = fail(SFB_ECUDA, cudaGetErrorString(cudaGetLastError()));
+            break;
+        }
+        cudaStream_t ms = h->stream;
+        const double dr = (rmax - rmin) / (double)nr;
+        launch_gtab(p, nr, rmin, dr, 0, d_g, ms);
+        launch_wmix(p, h->d_noff, d_g, nr, rmin, dr, WT, 2 * nr, (int)LW, neg_m ? 1 : 0, d_out, smem, ms);
+        if (cudaMemcpyAsync(wmix_out, d_out, outn * sizeof(double), cudaMemcpyDeviceToHost, ms) != cudaSuccess ||
+            cudaStreamSynchronize(ms) != cudaSuccess) {
+            st = fail(SFB_ECUDA, cudaGetErrorString(cudaGetLastError()));
+            break;
+        }
+    } while (0);
+    cudaFree(d);
+    return st;
+}
+
 int sfb_win_rhat_ln_separable(sfb_plan *h, const double *phi, int64_t nr, double rmin, double rmax, double *w_ln_out) {
     SFB_TRY(check_plan(h));
     SFB_TRY(set_device_of(h));

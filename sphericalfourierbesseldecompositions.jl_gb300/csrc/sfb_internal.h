@@ -209,6 +209,12 @@ void launch_project_mixed(const Plan &p, const float2 *Adf, int64_t ldA, const f
 void launch_split_mean(double *maps, int64_t nmaps, int64_t npix, const double *ref, double *nu, cudaStream_t st);
 // nzr (FP64): receives the first / last ring pair holding a non-zero value in any map
 // (preset by the caller to a large value / -1).
+// Window mixing matrix (wmix.cu): largest lmax it supports, shared memory of one CTA for the
+// radial modes (l, l'), and the launch over every pair of radial modes.
+constexpr int WMIX_LMAX = 128;
+size_t wmix_smem_bytes(int l, int lp, int64_t nr, int neg_m);
+void launch_wmix(const Plan &p, const int64_t *noff, const double *gtab, int64_t nr, double rmin, double dr,
+                 const double *WT, int64_t ldW, int LW, int neg_m, double *out, size_t smem, cudaStream_t st);
 // Exclusive prefix sum of n int32 counters in place; tile_sums holds scan_tile_count(n) ints.
 int64_t scan_tile_count(int64_t n);
 void launch_exclusive_scan(int32_t *data, int64_t n, int32_t *tile_sums, cudaStream_t st);

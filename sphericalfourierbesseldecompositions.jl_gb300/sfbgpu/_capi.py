@@ -68,6 +68,8 @@ _PROTOS = [
                                             C.c_void_p]),
     ("sfb_win_rhat_ln_dense", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_double, C.c_double, C.c_void_p]),
     ("sfb_map2alm", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
+    ("sfb_calc_wmix", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_double, C.c_double, C.c_int32,
+                                C.c_void_p]),
     ("sfb_win_lnn", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_double, C.c_double, C.c_void_p, C.c_int64,
                               C.c_void_p]),
     ("sfb_amln2clnn", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,

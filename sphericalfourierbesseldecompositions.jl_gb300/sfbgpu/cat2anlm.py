@@ -20,7 +20,7 @@ from .modes import getnlmsize
 from .windows import SeparableArray
 
 __all__ = ["GPUPlan", "get_plan", "cat2amln", "cat2nlm", "field2anlm", "anlm2field", "win_rhat_ln",
-           "map2alm", "ang2pix_ring", "amln2clnn", "anlm2clnn", "winweights2galweights", "apply_window", "win_lnn"]
+           "map2alm", "ang2pix_ring", "amln2clnn", "anlm2clnn", "winweights2galweights", "apply_window", "win_lnn", "calc_wmix"]
 
 _PRECISION = {"fp64": capi.SFB_FP64, "mixed": capi.SFB_MIXED}
 _RADIAL = {"poly": capi.SFB_RADIAL_POLY, "spline": capi.SFB_RADIAL_SPLINE}
@@ -362,4 +362,17 @@ def win_lnn(win, wmodes, cmodes, **plan_opts):
     out = np.empty(lnn.shape[0])
     capi.check(capi.lib.sfb_win_lnn(plan.handle, capi.ptr(W), wmodes.nr, wmodes.rmin, wmodes.rmax, capi.ptr(lnn),
                                     lnn.shape[0], capi.ptr(out)))
+    return out
+
+
+def calc_wmix(win, wmodes, amodes, neg_m=False, **plan_opts):
+    """Window mixing matrix W[(n l m), (n' l' m')] (reference calc_wmix, src/windows.jl:299-366) of an
+    (nr, npix) window: (nlmsize, nlmsize) complex."""
+    plan = get_plan(amodes, **plan_opts)
+    W = np.asfortranarray(win, float)
+    if W.shape != (wmodes.nr, plan.npix):
+        raise ValueError("window must be nr x npix at the plan's nside")
+    out = np.empty((plan.nlmsize, plan.nlmsize), np.complex128, order="F")
+    capi.check(capi.lib.sfb_calc_wmix(plan.handle, capi.ptr(W), wmodes.nr, wmodes.rmin, wmodes.rmax,
+                                      1 if neg_m else 0, capi.C.c_void_p(out.ctypes.data)))
     return out
