@@ -837,8 +837,11 @@ int sfb_plan_create(const sfb_plan_desc *d, sfb_plan **out) {
             if ((st = upload(p, &p.d_wphase, wph.data(), wph.size())) != SFB_OK) break;
             if ((st = upload(p, &p.d_twtab32, tw32.data(), tw32.size())) != SFB_OK) break;
             if ((st = upload(p, &p.d_wphase32, wph32.data(), wph32.size())) != SFB_OK) break;
-            // tensor-core ring DFT tables: w cos(pi k / n), k < 2n, sliced on the scale 2^EB > w
-            const int EB = std::ilogb(wq) + 1;
+            // tensor-core ring DFT tables: cos(pi k / n), k < 2n, sliced on the scale 2^EB = 2 > |cos|; the
+            // quadrature weight is applied in the DFT's epilogue, so cos 0 = 1 is one exact slice (a weighted
+            // table entry w would lose its tail slices to the dropped product levels for the small values of
+            // a ring, the same loss for every pixel at m = 0, which then adds up instead of averaging out)
+            const int EB = 1;
             std::vector<int64_t> doff(p.nrn);
             std::vector<uint2> dtw;
             int64_t eq_off = -1;
@@ -858,7 +861,7 @@ int sfb_plan_create(const sfb_plan_desc *d, sfb_plan **out) {
                     if (2 * kk == n) c = 0.0;
                     else if (2 * kk < n) c = std::cos(M_PI * (double)kk / (double)n);
                     else c = -std::cos(M_PI * (double)(n - kk) / (double)n);
-                    dtw.push_back(dft_slices(wq * c, EB));
+                    dtw.push_back(dft_slices(c, EB));
                 }
             }
             std::vector<int32_t> crings, coff;
@@ -1506,13 +1509,12 @@ static int aux_plan(sfb_plan *h, sfb_plan **out) {
     if (!h->aux) {
         const Plan &p = h->p;
         const int64_t L = 2 * (int64_t)p.lmax;
+        // four knots per spline (the plan's minimum), zero values
         std::vector<int64_t> lmax_n{L}, off((size_t)L + 2);
-        std::vector<double> x, zero((size_t)(2 * (L + 1)), 0.0);
-        for (int64_t l = 0; l <= L + 1; ++l) off[(size_t)l] = 2 * l;
-        for (int64_t l = 0; l <= L; ++l) {
-            x.push_back(p.rmin);
-            x.push_back(p.rmax);
-        }
+        std::vector<double> x, zero((size_t)(4 * (L + 1)), 0.0);
+        for (int64_t l = 0; l <= L + 1; ++l) off[(size_t)l] = 4 * l;
+        for (int64_t l = 0; l <= L; ++l)
+            for (int k = 0; k < 4; ++k) x.push_back(p.rmin + (p.rmax - p.rmin) * k / 3.0);
         sfb_plan_desc d{};
         d.nside = p.nside;
         d.lmax = L;

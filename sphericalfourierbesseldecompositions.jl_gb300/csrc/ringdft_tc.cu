@@ -6,6 +6,8 @@
 //   F_N(q, m) = w sum_j x_N(q, j) e^{-i m (phi0 + 2 pi j / n)},
 // and e^{-i m (phi0 + 2 pi j/n)} = T[k] + i T[k + n/2] with
 // T[k] = cos(pi k / n), k = m (2 j + t) mod 2n, t = 1 if phi0 = pi/n else 0.
+// The product runs on the unweighted table and the epilogue multiplies by the
+// quadrature weight w = 4 pi / npix (a double-float constant, one rounding).
 // F+ = F_N + F_S and F- = F_N - F_S go to F[parity][m][ring][2 map + re/im],
 // the layout of the Legendre stage.
 //
@@ -14,7 +16,7 @@
 // using fast routines of matrix multiplication", Numer. Algorithms 59, 2012):
 // every value of a map row is written on the row's common scale 2^E (max|x| <
 // 2^E) as x = sum_s a_s 2^(E - 6 - 7 s), s = 0..3, with integers |a_s| <= 64;
-// every table value on the table's common scale 2^EB (w < 2^EB) as
+// every table value on the table's common scale 2^EB (|T| <= 1 < 2^EB = 2) as
 // T = sum_s b_s 2^(EB - 7 - 7 s), |b_0| <= 128, |b_s| <= 64.  Each slice is a
 // BF16 value with at most 8 significant bits.  The products of level
 // v = s_a + s_b (v = 0..3) are integers of one unit U 2^(-7 v) per row and
@@ -22,7 +24,12 @@
 // units for rings of up to 1024 pixels, so it is exact whatever order or
 // rounding the tensor cores use.  Levels v >= 4 (below 2^-27 of the leading
 // term) are dropped.  The epilogue adds the levels and the north/south rows
-// with one significant FP32 rounding (TwoSum on the leading level).
+// with one significant FP32 rounding (TwoSum on the leading level).  The
+// table is unweighted so that cos 0 = 1 is exact in one slice: for m = 0
+// every pixel shares one table value, and a value far below its ring's
+// maximum (a smooth background beside a single galaxy's spike) multiplies
+// only the leading slices of it, so a truncated weighted entry would bias the
+// m = 0 ring sums coherently.
 //
 // Tiles: M = 128 rows = 64 (ring, map) pairs x {north, south} (TMEM lanes
 // 0-63 north, 64-127 south), N = 128 accumulator columns (64 m values x
@@ -52,6 +59,11 @@ namespace dft {
 using namespace tc;
 
 constexpr int ZERO_ROW_E = -127;  // row exponent of an all-zero ring row
+
+// w (hi + lo) rounded once: w = (w.x, w.y) a double-float constant
+__device__ __forceinline__ float wmul(float2 w, float hi, float lo) {
+    return fmaf(w.x, hi, fmaf(w.y, hi, w.x * lo));
+}
 constexpr int KC = 32;            // pixels per chunk
 constexpr int NPAIR = 64;         // (ring, map) pairs per CTA
 constexpr int NROW = 128;         // A rows (MMA M): pairs x {north, south}
@@ -145,7 +157,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
                                                          const int64_t *__restrict__ dtw_off,
                                                          const unsigned char *__restrict__ img,
                                                          const int64_t *__restrict__ img_off, float *__restrict__ F,
-                                                         int64_t ldF, int *err) {
+                                                         int64_t ldF, float2 wdf, int *err) {
     extern __shared__ __align__(1024) unsigned char smem[];
     // grid (column blocks u, row tiles, classes): the column blocks of one row tile are launched
     // together and read its map rows through L2 once
@@ -408,8 +420,9 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
             for (int t = 0; t < 8; ++t) {
                 const int mm = 64 * u + 8 * cg + t;
                 if (mm > lmax) break;
-                const float2 f = make_float2(v0[2 * t] + (v1[2 * t] + (v2[2 * t] + v3[2 * t])),
-                                             v0[2 * t + 1] + (v1[2 * t + 1] + (v2[2 * t + 1] + v3[2 * t + 1])));
+                const float2 f = make_float2(
+                    wmul(wdf, v0[2 * t], v1[2 * t] + (v2[2 * t] + v3[2 * t])),
+                    wmul(wdf, v0[2 * t + 1], v1[2 * t + 1] + (v2[2 * t + 1] + v3[2 * t + 1])));
                 *reinterpret_cast<float2 *>(F + ((int64_t)mm * nrn + oring) * ldF + 2 * ob) = f;
                 *reinterpret_cast<float2 *>(F + ((int64_t)(L1 + mm) * nrn + oring) * ldF + 2 * ob) = f;
             }
@@ -461,7 +474,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
                         const float s = a + bb;
                         const float z = s - a;
                         const float e = (a - (s - z)) + (bb - z);
-                        f[c2] = s + ((xh[(2 * i + 1) * NROW + pr] + sgn * xh[(2 * i + 1) * NROW + pr + NPAIR]) + e);
+                        f[c2] = wmul(wdf, s, (xh[(2 * i + 1) * NROW + pr] + sgn * xh[(2 * i + 1) * NROW + pr + NPAIR]) + e);
                     }
                     *reinterpret_cast<float2 *>(F + ((int64_t)(sg * L1 + mm) * nrn + oring) * ldF + 2 * ob) =
                         make_float2(f[0], f[1]);
@@ -587,16 +600,18 @@ void launch_ring_analysis_tc(const Plan &p, const float *maps, int64_t nmaps, fl
     set_smem(dft::k_ring_dft_tc<true>, dft::SMEM);
     set_smem(dft::k_ring_dft_tc<false>, dft::SMEM);
     const unsigned ntn = (unsigned)((p.lmax + 1 + 63) / 64);
+    const double wq = 4.0 * M_PI / (double)p.npix;
+    const float2 wdf = make_float2((float)wq, (float)(wq - (double)(float)wq));
     // imaged classes read B from the image, the others gather it from the ring table
     auto launch = [&](dim3 grid, int c0, bool img) {
         if (img)
             dft::k_ring_dft_tc<true><<<grid, dft::NTHR, dft::SMEM, st>>>(
                 maps, p.npix, nmaps, p.d_rings, (int)p.nrn, p.lmax, p.d_cls_rings, p.d_cls_off + c0, erow, p.d_dtw,
-                p.d_dtw_off, p.d_dtimg, p.d_dtimg_off + c0, F, 2 * nmaps, p.d_err);
+                p.d_dtw_off, p.d_dtimg, p.d_dtimg_off + c0, F, 2 * nmaps, wdf, p.d_err);
         else
             dft::k_ring_dft_tc<false><<<grid, dft::NTHR, dft::SMEM, st>>>(
                 maps, p.npix, nmaps, p.d_rings, (int)p.nrn, p.lmax, p.d_cls_rings, p.d_cls_off + c0, erow, p.d_dtw,
-                p.d_dtw_off, nullptr, nullptr, F, 2 * nmaps, p.d_err);
+                p.d_dtw_off, nullptr, nullptr, F, 2 * nmaps, wdf, p.d_err);
         note_launch();
     };
     const unsigned mtiles = (unsigned)((nmaps + dft::NPAIR - 1) / dft::NPAIR);

@@ -69,10 +69,10 @@ __device__ int w3j_family(int j2, int j3, int m2, int m3, double *f, int *nf) {
                 ++k;
             }
         }
-        // backward from jmax down to index k, stored past the forward values' end
+        // backward from jmax down to index k (nothing to do when the forward values grew to jmax)
         const double fk = f[k];
         double nxt = 0.0, cur = 1.0;
-        f[n - 1] = 1.0;
+        if (k < n - 1) f[n - 1] = 1.0;
         for (int i = n - 1; i > k; --i) {
             const int j = jmin + i;
             const double pv = -(w3j_B(j, j2, j3, m2, m3, m1) * cur + j * w3j_A(j + 1, j2, j3, m1) * nxt) /
@@ -81,9 +81,11 @@ __device__ int w3j_family(int j2, int j3, int m2, int m3, double *f, int *nf) {
             cur = pv;
             if (i - 1 > k) f[i - 1] = pv;
             else {
-                // index k: scale the forward part to meet the backward value
-                const double sc = pv / fk;
-                for (int q = 0; q < k; ++q) f[q] *= sc;
+                // index k: scale the forward part (if any) to meet the backward value
+                if (k > 0) {
+                    const double sc = pv / fk;
+                    for (int q = 0; q < k; ++q) f[q] *= sc;
+                }
                 f[k] = pv;
             }
         }

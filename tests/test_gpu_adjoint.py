@@ -143,9 +143,11 @@ def test_field2anlm_gradient_finite_differences():
 def test_field2anlm_fp32_field_and_shell_streaming(precision, monkeypatch):
     """An FP32 field (sfb_field2anlm_typed) gives exactly what its FP64 copy
     gives; the FP32 gradient is the FP64 one rounded; and a field streamed
-    through the device one shell at a time (SFBGPU_FIELD_MAX_BYTES below one
-    shell) matches the resident field to the rounding of the radial sum's
-    grouping (1e-12)."""
+    through the device six shells at a time (SFBGPU_FIELD_MAX_BYTES of six
+    FP32 shells) matches the resident field to the rounding of the radial
+    sum's grouping (1e-12).  Six shells per chunk keep the mixed transform on
+    the same refinement scheme as the resident 24-shell batch (a batch of at
+    most four maps takes the full refinement passes, a different rounding)."""
     a = sfbgpu.AnlmModes(0.03, 500.0, 1000.0, nside=16)
     wm = sfbgpu.ConfigurationSpaceModes(a.rmin, a.rmax, 24, a.nside)
     rng = np.random.default_rng(31)
@@ -158,7 +160,7 @@ def test_field2anlm_fp32_field_and_shell_streaming(precision, monkeypatch):
     g32 = sfbgpu.field2anlm_vjp(ab, wm, a, dtype=np.float32, precision=precision)
     assert g32.dtype == np.float32
     np.testing.assert_array_equal(g32, g64.astype(np.float32))
-    monkeypatch.setenv("SFBGPU_FIELD_MAX_BYTES", "1")
+    monkeypatch.setenv("SFBGPU_FIELD_MAX_BYTES", str(6 * 4 * wm.npix))
     b = sfbgpu.AnlmModes(0.03, 500.0, 1000.0, nside=16)
     s32 = sfbgpu.field2anlm(f32, wm, b, precision=precision)
     gs = sfbgpu.field2anlm_vjp(ab, wm, b, precision=precision)

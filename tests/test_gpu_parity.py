@@ -448,6 +448,7 @@ def test_calc_wmix_vs_oracle(neg_m):
     record(f"calc_wmix_vs_oracle_negm{int(neg_m)}", e, nlmsize=int(gpu.shape[0]))
     assert np.all(np.isfinite(gpu)) and e < 1e-12
     if not neg_m:
-        one = sfbgpu.calc_wmix(np.ones_like(win), wm, a)
-        eye = np.eye(one.shape[0])
-        assert np.max(np.abs(one - eye)) < 2e-2
+        # 400 shells: the midpoint rule of the radial overlap integrals to ~1e-3
+        wf = sfbgpu.ConfigurationSpaceModes(a.rmin, a.rmax, 400, a.nside)
+        one = sfbgpu.calc_wmix(np.ones((wf.nr, wf.npix)), wf, a)
+        assert np.max(np.abs(one - np.eye(one.shape[0]))) < 5e-3
