@@ -39,13 +39,31 @@ METRIC = "cat2amln galaxies/s at nside256 kmax0.1: mixed vs FP64 GPU, ≤1e-7 re
 KMAX, RMIN, RMAX, NSIDE, NR = 0.1, 500.0, 2500.0, 256, 1000
 NGAL_MEAN = 10_000_000
 CAP_DEG, RMEAN, RSIG = 60.0, 1500.0, 400.0
-# measured with ncu (dram__bytes_read.sum + dram__bytes_write.sum) over the two ring-DFT launches of one call
-# DRAM bytes (read + write) per call of the stages' kernels on this workload, from the single-pass ncu
-# capture recorded in profiles/launches_cat2amln_nside256_kmax0.1_mixed.md (second call of the run)
-DFT_DRAM_BYTES_PER_CALL = (720.60 + 300.21 + 96.09 + 260.42) * 1e6          # k_ring_dft_tc x2
-DEPOSIT_DRAM_BYTES_PER_CALL = (332.81 + 133.19 + 18.76 + 0.04 + 47.20 + 0.02 + 0.02 + 47.20 + 498.99 + 283.26
-                               + 207.17 + 3.61 + 8.61 + 0.01 + 221.04 + 211.19) * 1e6   # keys .. moments
+# per-kernel DRAM bytes of one call of the profile case (ncu, one kernel per capture), one line per kernel:
+# stage, kernel, launches, read bytes, write bytes, the unit its traffic scales with, units in the capture
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "dram_traffic_nside256_kmax0.1_profile_case.txt")
 WORKLOAD = "cat2amln kmax=0.1 rmin=500 rmax=2500 nside=256 nr=1000 N~Poisson(1e7) cap60 x gauss(1500,400) w~U[0.5,1.5]"
+
+
+def stage_traffic(stage, units):
+    """DRAM bytes (read + write) of one call's kernels of `stage`, scaled from the profile-case ncu
+    captures: each kernel's bytes x (units of this run / units of the capture), the unit being maps
+    for the map-sized kernels and galaxies for the sort.  (None, []) without a capture of the stage."""
+    try:
+        with open(TRAFFIC_FILE) as fh:
+            lines = fh.read().splitlines()
+    except OSError:
+        return None, []
+    total, parts = 0.0, []
+    for ln in lines:
+        f = ln.split()
+        if not f or f[0].startswith("#") or f[0] != stage:
+            continue
+        kern, nl, rd, wr, unit, cap = f[1], int(f[2]), float(f[3]), float(f[4]), f[5], float(f[6])
+        scale = units[unit] / cap
+        total += (rd + wr) * scale
+        parts.append(f"{kern} x{nl} ({unit} x{scale:.4g})")
+    return (total if parts else None), parts
 
 
 def make_catalogue(seed=2):
@@ -727,20 +745,18 @@ def main():
     fp64_peak = fp64_gemm_peak(torch) if args.precision == "fp64" else None
     sky = sky_rings(sfbgpu, NSIDE, gal[:, 1], gal[:, 2]) if args.precision == "mixed" else None
     table = roofline_table(stages, args.precision, nm, N, info["nbasis"], peaks, fp64_peak, sky)
+    if args.precision == "mixed":
+        for k in table:
+            traffic, parts = stage_traffic(k, {"maps": nm, "galaxies": N})
+            table[k]["traffic"] = traffic
+            if traffic is not None:
+                table[k]["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum per call on the "
+                                              "profile case (nside 256, 35 maps, 1e6 galaxies), one kernel per "
+                                              "capture, scaled to this run: " + ", ".join(parts))
     dom = max(table, key=lambda k: stages[k]["ms_per_step"])
     roof = dict(table[dom])
     roof["kernel_stage"] = dom
-    roof["traffic"] = None
-    if args.precision == "mixed" and not args.profile_case and NGAL_MEAN == 10_000_000:
-        # DRAM bytes (read + write) of the stage's kernels in one call of this workload, from the
-        # single-pass ncu capture recorded in profiles/launches_cat2amln_nside256_kmax0.1_mixed.md
-        if dom == "ring_fft":
-            roof["traffic"] = DFT_DRAM_BYTES_PER_CALL
-            roof["traffic_source"] = "ncu dram__bytes_read.sum + dram__bytes_write.sum, k_ring_dft_tc x2"
-        elif dom == "deposit":
-            roof["traffic"] = DEPOSIT_DRAM_BYTES_PER_CALL
-            roof["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum, deposit kernels "
-                                      "(keys, fallback, scans, scatter, count map, stats, moments)")
+    roof.setdefault("traffic", None)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

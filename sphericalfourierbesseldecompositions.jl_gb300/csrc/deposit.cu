@@ -18,17 +18,17 @@
 //
 // Mixed precision runs no FP64 instruction per galaxy (integer range tests and
 // double-float splits; the records are double-float pairs) and stores the
-// maps in FP32.  With a reference angular map C, each map is written as the
-// fluctuation D_b - mu_b C, with mu_b = <D_b, C> / <C, C> estimated in
-// double-float (sums in FP64) on every STATS_STRIDE-th group of 32 bins; the
-// caller adds mu_b C_lm back in FP64 after the transform.  Rings holding no
-// galaxy are then left unwritten (ring_live), their readers treating them as
-// zero.
+// maps as double-float pairs (hi, lo), which the ring DFT slices exactly.
+// With a reference angular map C, each map is written as the fluctuation
+// D_b - mu_b C, with mu_b = <D_b, C> / <C, C> estimated in double-float (sums
+// in FP64) on every STATS_STRIDE-th group of 32 bins; the caller adds
+// mu_b C_lm back in FP64 after the transform.  Rings holding no galaxy are
+// then left unwritten (ring_live), their readers treating them as zero.
 // C is the weighted galaxy count map of all radial slots, so it carries the
 // mean density and the survey boundary exactly as the galaxies sample them
-// (a pixelised mask misses the partly covered boundary pixels).  The FP32
-// rounding then scales with the fluctuation, not with the mean density that
-// the window term later cancels.
+// (a pixelised mask misses the partly covered boundary pixels).  The reduced
+// precision of the transform then scales with the fluctuation, not with the
+// mean density that the window term later cancels.
 #include <algorithm>
 #include <cstring>
 
@@ -472,11 +472,11 @@ __device__ __forceinline__ void bin_moments_df(const float4 *__restrict__ sorted
 
 // Mixed precision, one thread per (slot, pixel): the moments and the
 // fluctuation acc - mu_b ref all in double-float (mudf = mu and cdf = ref as
-// hi + lo pairs), stored as FP32.
+// hi + lo pairs), stored as normalised double-float pairs.
 template <int MAXDEG>
 __global__ void k_deposit_moments_df(const int32_t *__restrict__ offset, const float4 *__restrict__ sorted,
                                      int64_t npix, int pieces, int deg, int64_t nbasis, const float2 *__restrict__ cdf,
-                                     const float2 *__restrict__ mudf, float *__restrict__ maps) {
+                                     const float2 *__restrict__ mudf, float2 *__restrict__ maps) {
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t nkeys = (int64_t)(pieces + 2) * npix;
     if (idx >= nkeys) return;
@@ -486,12 +486,13 @@ __global__ void k_deposit_moments_df(const int32_t *__restrict__ offset, const f
     const int64_t g1 = offset[idx + 1];
     const float2 c = cdf ? cdf[pix] : make_float2(0.f, 0.f);
     const dfl rv = {c.x, c.y};
-    auto fluct = [&](dfl a, int64_t b) -> float {
+    auto fluct = [&](dfl a, int64_t b) -> float2 {
         if (cdf) {
             const float2 m = mudf[b];
             a = dfs_add(a, df_neg(dfs_mul({m.x, m.y}, rv)));
         }
-        return a.hi + a.lo;
+        a = df_renorm(a);
+        return make_float2(a.hi, a.lo);
     };
     if (slot >= pieces) {
         dfl sw = {0.f, 0.f};
@@ -506,7 +507,7 @@ __global__ void k_deposit_moments_df(const int32_t *__restrict__ offset, const f
     dfl acc[MAXDEG + 1];
     bin_moments_df<MAXDEG>(sorted, g0, g1, deg, acc);
     const int64_t b0 = (int64_t)slot * (deg + 1);
-    float *base = maps + b0 * npix + pix;
+    float2 *base = maps + b0 * npix + pix;
 #pragma unroll
     for (int k = 0; k <= MAXDEG; ++k)
         if (k <= deg) base[(int64_t)k * npix] = fluct(acc[k], b0 + k);
@@ -525,11 +526,11 @@ __global__ void __launch_bounds__(128) k_deposit_moments_bal(const int32_t *__re
                                                              int pieces, int deg, int64_t nbasis,
                                                              const float2 *__restrict__ cdf,
                                                              const float2 *__restrict__ mudf,
-                                                             float *__restrict__ maps, int64_t nside,
+                                                             float2 *__restrict__ maps, int64_t nside,
                                                              const int *__restrict__ ring_live) {
     __shared__ int hist[64];
     __shared__ int perm[128];
-    __shared__ float out[(MAXDEG + 1) * 128];
+    __shared__ float2 out[(MAXDEG + 1) * 128];
     const int t = threadIdx.x;
     const int64_t nkeys = (int64_t)(pieces + 2) * npix;
     const int64_t B0 = (int64_t)blockIdx.x * 128;
@@ -550,11 +551,11 @@ __global__ void __launch_bounds__(128) k_deposit_moments_bal(const int32_t *__re
         // rings without galaxies are not written at all (their readers treat them as zero)
         if (ring_live && !ring_live[ring_of_pixel(nside, px)]) return;
         if (sl >= pieces) {
-            maps[(nbasis - 2 + (sl - pieces)) * npix + px] = 0.f;
+            maps[(nbasis - 2 + (sl - pieces)) * npix + px] = make_float2(0.f, 0.f);
             return;
         }
-        float *z = maps + (int64_t)sl * (deg + 1) * npix + px;
-        for (int k = 0; k <= deg; ++k) z[(int64_t)k * npix] = 0.f;
+        float2 *z = maps + (int64_t)sl * (deg + 1) * npix + px;
+        for (int k = 0; k <= deg; ++k) z[(int64_t)k * npix] = make_float2(0.f, 0.f);
         return;
     }
     if (t < 64) hist[t] = 0;
@@ -584,12 +585,13 @@ __global__ void __launch_bounds__(128) k_deposit_moments_bal(const int32_t *__re
         const int64_t g0 = offset[b], g1 = offset[b + 1];
         const float2 c = cdf ? cdf[pix] : make_float2(0.f, 0.f);
         const dfl rv = {c.x, c.y};
-        auto fluct = [&](dfl a, int64_t bi) -> float {
+        auto fluct = [&](dfl a, int64_t bi) -> float2 {
             if (cdf) {
                 const float2 m = mudf[bi];
                 a = dfs_add(a, df_neg(dfs_mul({m.x, m.y}, rv)));
             }
-            return a.hi + a.lo;
+            a = df_renorm(a);
+            return make_float2(a.hi, a.lo);
         };
         if (slot >= pieces) {
             dfl sw = {0.f, 0.f};
@@ -615,7 +617,7 @@ __global__ void __launch_bounds__(128) k_deposit_moments_bal(const int32_t *__re
         maps[(nbasis - 2 + (slot - pieces)) * npix + pix] = out[t];
         return;
     }
-    float *base = maps + (int64_t)slot * (deg + 1) * npix + pix;
+    float2 *base = maps + (int64_t)slot * (deg + 1) * npix + pix;
     for (int k = 0; k <= deg; ++k) base[(int64_t)k * npix] = out[k * 128 + t];
 }
 
@@ -723,11 +725,17 @@ static void launch_moments(const Plan &p, const int32_t *counts, const void *sor
     const int64_t nkeys = (int64_t)(p.pieces + 2) * p.npix;
     const unsigned blocks = (unsigned)((nkeys + 127) / 128);
     const float4 *s4 = static_cast<const float4 *>(sorted);
-    float *mf = reinterpret_cast<float *>(maps);
-    if (p.precision == SFB_MIXED && MAXDEG <= 31 && p.npix >= 128)
-        k_deposit_moments_bal<MAXDEG><<<blocks, 128, 0, st>>>(counts, s4, p.npix, p.pieces, p.degree, p.nbasis, cdf,
-                                                              mudf, mf, p.nside, ring_live);
-    else if (p.precision == SFB_MIXED)
+    float2 *mf = reinterpret_cast<float2 *>(maps);
+    bool done = false;
+    if constexpr (MAXDEG <= 31) {
+        if (p.precision == SFB_MIXED && p.npix >= 128) {
+            k_deposit_moments_bal<MAXDEG><<<blocks, 128, 0, st>>>(counts, s4, p.npix, p.pieces, p.degree, p.nbasis,
+                                                                  cdf, mudf, mf, p.nside, ring_live);
+            done = true;
+        }
+    }
+    if (done) {
+    } else if (p.precision == SFB_MIXED)
         k_deposit_moments_df<MAXDEG><<<blocks, 128, 0, st>>>(counts, s4, p.npix, p.pieces, p.degree, p.nbasis, cdf,
                                                              mudf, mf);
     else

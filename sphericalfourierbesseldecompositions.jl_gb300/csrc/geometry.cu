@@ -92,7 +92,12 @@ void launch_transpose(const double *in, int64_t rows, int64_t cols, double *out,
     note_launch();
 }
 
-// out[c * ldo + r] = in[r * ldi + c] for r < rows, c < cols (converted to TO).
+__device__ __forceinline__ float2 convert_elem(float v, float2 *) { return make_float2(v, 0.f); }
+template <typename TI, typename TO>
+__device__ __forceinline__ TO convert_elem(TI v, TO *) { return (TO)v; }
+
+// out[c * ldo + r] = in[r * ldi + c] for r < rows, c < cols (converted to TO; float -> double-float
+// pairs with a zero low word).
 template <typename TI, typename TO>
 __global__ void k_transpose_ld(const TI *in, int64_t ldi, int64_t rows, int64_t cols, TO *out, int64_t ldo) {
     __shared__ TI tile[32][33];
@@ -104,7 +109,7 @@ __global__ void k_transpose_ld(const TI *in, int64_t ldi, int64_t rows, int64_t 
     __syncthreads();
     for (int j = threadIdx.y; j < 32; j += 8) {
         const int64_t c = c0 + j, r = r0 + threadIdx.x;
-        if (r < rows && c < cols) out[c * ldo + r] = (TO)tile[threadIdx.x][j];
+        if (r < rows && c < cols) out[c * ldo + r] = convert_elem(tile[threadIdx.x][j], (TO *)nullptr);
     }
 }
 
@@ -130,6 +135,10 @@ void launch_transpose_ld(const float *in, int64_t ldi, int64_t rows, int64_t col
     transpose_ld(in, ldi, rows, cols, out, ldo, st);
 }
 void launch_transpose_ld(const double *in, int64_t ldi, int64_t rows, int64_t cols, float *out, int64_t ldo,
+                         cudaStream_t st) {
+    transpose_ld(in, ldi, rows, cols, out, ldo, st);
+}
+void launch_transpose_ld(const float *in, int64_t ldi, int64_t rows, int64_t cols, float2 *out, int64_t ldo,
                          cudaStream_t st) {
     transpose_ld(in, ldi, rows, cols, out, ldo, st);
 }

@@ -311,9 +311,9 @@ static bool narrow_dispatch(const Plan &p, const T *lam, const T *in, int64_t nc
 }
 
 // FP64 Gram refinement step for few columns (the narrow transforms):
-//   Anew[l(r)] = Acur[l(r)] + (A0[l(r)] - sum_li M_z[r][li] Acur[l(li)])
-// one thread per (block z, output row r, column); M_z from the plan's FP64
-// Gram tables (element [li][r] at gram_off[z] + li R + r).
+//   Anew[l(r)] = A0[l(r)] - sum_li D_z[r][li] Acur[l(li)]   (= Acur + (A0 - M_z Acur))
+// one thread per (block z, output row r, column); D_z = M_z - I from the plan's
+// FP64 Gram tables (element [li][r] at gram_off[z] + li R + r).
 template <int NC>
 __global__ void __launch_bounds__(128) k_gram_update_fp64(const double *__restrict__ gram,
                                                           const int64_t *__restrict__ gram_off, int R, int lmax,
@@ -333,7 +333,7 @@ __global__ void __launch_bounds__(128) k_gram_update_fp64(const double *__restri
     }
     const int l = m + par + 2 * r;
     const int64_t o = ((int64_t)l * (l + 1) / 2 + m) * NC + c;
-    Anew[o] = Acur[o] + (A0[o] - acc);
+    Anew[o] = A0[o] - acc;
 }
 
 // Many columns: the same update as a tiled GEMM per block z (output rows r x
@@ -398,7 +398,7 @@ __global__ void __launch_bounds__(256) k_gram_update_wide(const double *__restri
             const int64_t col = col0 + tx + 16 * j;
             if (col >= ncol) continue;
             const int64_t o = base + col;
-            Anew[o] = Acur[o] + (A0[o] - acc[i][j]);
+            Anew[o] = A0[o] - acc[i][j];
         }
     }
 }
@@ -452,6 +452,81 @@ void launch_leg_synthesis(const Plan &p, const double *A, int64_t ncol, double *
 // the input of the mixed-precision Legendre analysis (as k_colmax computes
 // for F).
 constexpr int FOLD_RC = 64;
+
+// Mixed precision: F and R are normalised double-float pairs.  r = F - f s with
+// the product f s exact (TwoProd) and the sum in double-float.
+__device__ __forceinline__ float2 df_resid(float2 F, float f, float s) {
+    const float p = -f * s;
+    const float e = fmaf(-f, s, -p);
+    const float h = F.x + p;
+    const float z = h - F.x;
+    const float l = ((F.x - (h - z)) + (p - z)) + (F.y + e);
+    const float h2 = h + l;
+    return make_float2(h2, l - (h2 - h));
+}
+
+// Mixed-precision column-major fold (as k_fold_cols): F (nullable) and R double-float, G FP32.
+__global__ void __launch_bounds__(128) k_fold_cols_df(const RingGeom *__restrict__ rings, int nrn, int rlim, int lmax,
+                                                      double w, const float2 *__restrict__ F,
+                                                      const float *__restrict__ G, int64_t ncplx,
+                                                      float2 *__restrict__ R, int *__restrict__ Ecol) {
+    const int mp = blockIdx.y >> 1, par = blockIdx.y & 1;
+    const int rc0 = blockIdx.z * FOLD_RC;
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncplx) return;
+    const int L1 = lmax + 1;
+    const int64_t ld = 2 * ncplx;
+    float mxr = 0.f, mxi = 0.f;
+    const int rend = min(rlim, rc0 + FOLD_RC);
+    for (int r = rc0; r < rend; ++r) {
+        const RingGeom g = rings[r];
+        const int n = g.nph;
+        const bool odd_phase = g.phi0_den != 0;
+        const float f = (float)(w * (double)n * g.cfold);
+        const int64_t off = ((int64_t)(par * L1 + mp) * nrn + r) * ld + 2 * c;
+        float sx, sy;
+        if (n > 2 * lmax) {
+            sx = G[off];
+            sy = mp == 0 ? 0.f : G[off + 1];
+        } else {
+            sx = 0.f;
+            sy = 0.f;
+            const int k = mp % n;
+            const int kk = (n - k) % n;
+            int tt = 0;
+            for (int m = k; m <= lmax; m += n, ++tt) {
+                const float *gp = G + ((int64_t)(par * L1 + m) * nrn + r) * ld + 2 * c;
+                const int dt = tt - mp / n;
+                const float sgn = (odd_phase && (dt & 1)) ? -1.f : 1.f;
+                sx += sgn * gp[0];
+                if (m != 0) sy += sgn * gp[1];
+            }
+            for (int m = (kk == 0 ? n : kk); m <= lmax; m += n) {
+                const float *gp = G + ((int64_t)(par * L1 + m) * nrn + r) * ld + 2 * c;
+                const int q = (m + mp) / n;
+                const float sgn = (odd_phase && (q & 1)) ? -1.f : 1.f;
+                sx += sgn * gp[0];
+                sy -= sgn * gp[1];
+            }
+        }
+        const float2 fx = F ? F[off] : make_float2(0.f, 0.f), fy = F ? F[off + 1] : make_float2(0.f, 0.f);
+        const float2 rx = df_resid(fx, f, sx), ry = df_resid(fy, f, sy);
+        *reinterpret_cast<float4 *>(R + off) = make_float4(rx.x, rx.y, ry.x, ry.y);
+        mxr = fmaxf(mxr, fabsf(rx.x));
+        mxi = fmaxf(mxi, fabsf(ry.x));
+    }
+    if (Ecol) {
+        const int lg = 32 - __clz(nrn > 1 ? nrn - 1 : 1);
+        const int extra = max(0, lg - 9);
+        auto ex = [&](float mx) {
+            int E = (mx > 0.f && isfinite(mx)) ? ilogbf(mx) + 1 : 0;
+            return max(-90, min(E + extra, 100));
+        };
+        const int64_t z = 2 * (int64_t)mp + par;
+        atomicMax(Ecol + z * ld + 2 * c, ex(mxr));
+        atomicMax(Ecol + z * ld + 2 * c + 1, ex(mxi));
+    }
+}
 
 // F == nullptr: R = -w n cfold Fold(G) (the aliased-ring term of the Gram
 // refinement).  Only rings r < rlim are written.
@@ -536,7 +611,7 @@ constexpr int FOLD_MXQ = 8;
 template <int FC, bool MXREG>
 __global__ void __launch_bounds__(256) k_fold_alias(const RingGeom *__restrict__ rings, int nrn, int ral, int rpb,
                                                     int nbk, int lmax, double w, const float *__restrict__ G,
-                                                    int64_t ncplx, float *__restrict__ R, int *__restrict__ Ecol) {
+                                                    int64_t ncplx, float2 *__restrict__ R, int *__restrict__ Ecol) {
     extern __shared__ float2 fsm[];
     const int par = blockIdx.y;
     const int64_t c0 = (int64_t)blockIdx.x * FC;
@@ -616,8 +691,8 @@ __global__ void __launch_bounds__(256) k_fold_alias(const RingGeom *__restrict__
             const float sx = s1 * p1.x + s2 * p2.x, sy = s1 * p1.y - s2 * p2.y;
             const float rx = -f * sx, ry = -f * sy;
             const int64_t off = ((int64_t)(par * L1 + mp) * nrn + r) * ld + 2 * c;
-            R[off] = rx;
-            R[off + 1] = ry;
+            // double-float storage: the exact product error as the low word
+            *reinterpret_cast<float4 *>(R + off) = make_float4(rx, fmaf(-f, sx, -rx), ry, fmaf(-f, sy, -ry));
             if constexpr (MXREG) {
                 mxr[q].x = fmaxf(mxr[q].x, fabsf(rx));
                 mxr[q].y = fmaxf(mxr[q].y, fabsf(ry));
@@ -652,11 +727,19 @@ __global__ void __launch_bounds__(256) k_fold_alias(const RingGeom *__restrict__
 }
 
 // Few columns: one thread per (parity, m', ring, complex column), same sums.
-template <typename T>
+__device__ __forceinline__ double resid_of(const double *F, int64_t off, double f, double s) {
+    return (F ? F[off] : 0.0) - f * s;
+}
+__device__ __forceinline__ float2 resid_of(const float2 *F, int64_t off, float f, float s) {
+    return df_resid(F ? F[off] : make_float2(0.f, 0.f), f, s);
+}
+
+// TF: element type of F and R (double, or the double-float pairs of the mixed transform)
+template <typename T, typename TF>
 __global__ void __launch_bounds__(256) k_fold_residual_narrow(const RingGeom *rings, int nrn, int rlim, int lmax,
-                                                             double w, const T *__restrict__ F,
+                                                             double w, const TF *__restrict__ F,
                                                              const T *__restrict__ G, int64_t ncplx,
-                                                             T *__restrict__ R) {
+                                                             TF *__restrict__ R) {
     const int L1 = lmax + 1;
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t total = (int64_t)2 * L1 * rlim * ncplx;     // rings r < rlim only
@@ -691,8 +774,8 @@ __global__ void __launch_bounds__(256) k_fold_residual_narrow(const RingGeom *ri
         sx += sgn * gp[0];
         sy -= sgn * gp[1];
     }
-    R[off] = (F ? F[off] : T(0)) - f * sx;
-    R[off + 1] = (F ? F[off + 1] : T(0)) - f * sy;
+    R[off] = resid_of(F, off, f, sx);
+    R[off + 1] = resid_of(F, off + 1, f, sy);
 }
 
 bool launch_gram_update_fp64(const Plan &p, const double *Acur, const double *A0, int64_t ncol, double *Anew,
@@ -735,11 +818,11 @@ void launch_fold_residual(const Plan &p, const double *F, const double *G, int64
                 if (mxreg) {
                     set_smem(k_fold_alias<FC, true>, smem);
                     k_fold_alias<FC, true><<<grid, 256, smem, st>>>(p.d_rings, (int)p.nrn, rlim, rpb, nbk, p.lmax,
-                                                                    w, (const float *)G, ncplx, (float *)R, Ecol);
+                                                                    w, (const float *)G, ncplx, (float2 *)R, Ecol);
                 } else {
                     set_smem(k_fold_alias<FC, false>, smem);
                     k_fold_alias<FC, false><<<grid, 256, smem, st>>>(p.d_rings, (int)p.nrn, rlim, rpb, nbk, p.lmax,
-                                                                     w, (const float *)G, ncplx, (float *)R, Ecol);
+                                                                     w, (const float *)G, ncplx, (float2 *)R, Ecol);
                 }
                 note_launch();
                 return;
@@ -748,8 +831,8 @@ void launch_fold_residual(const Plan &p, const double *F, const double *G, int64
         dim3 grid((unsigned)((ncplx + 127) / 128), (unsigned)(2 * (p.lmax + 1)),
                   (unsigned)((rlim + FOLD_RC - 1) / FOLD_RC));
         const double w = 4.0 * M_PI / (double)p.npix;
-        k_fold_cols<float><<<grid, 128, 0, st>>>(p.d_rings, (int)p.nrn, rlim, p.lmax, w, (const float *)F,
-                                                 (const float *)G, ncplx, (float *)R, Ecol);
+        k_fold_cols_df<<<grid, 128, 0, st>>>(p.d_rings, (int)p.nrn, rlim, p.lmax, w, (const float2 *)F,
+                                             (const float *)G, ncplx, (float2 *)R, Ecol);
         note_launch();
         return;
     }
@@ -769,22 +852,36 @@ void launch_fold_residual(const Plan &p, const double *F, const double *G, int64
         const unsigned blocks = (unsigned)((total + 255) / 256);
         const double w = 4.0 * M_PI / (double)p.npix;
         if (p.precision == SFB_MIXED)
-            k_fold_residual_narrow<float><<<blocks, 256, 0, st>>>(p.d_rings, (int)p.nrn, rlim, p.lmax, w,
-                                                                 (const float *)F, (const float *)G, ncplx,
-                                                                 (float *)R);
+            k_fold_residual_narrow<float, float2><<<blocks, 256, 0, st>>>(p.d_rings, (int)p.nrn, rlim, p.lmax, w,
+                                                                         (const float2 *)F, (const float *)G, ncplx,
+                                                                         (float2 *)R);
         else
-            k_fold_residual_narrow<double><<<blocks, 256, 0, st>>>(p.d_rings, (int)p.nrn, rlim, p.lmax, w, F, G,
-                                                                  ncplx, R);
+            k_fold_residual_narrow<double, double><<<blocks, 256, 0, st>>>(p.d_rings, (int)p.nrn, rlim, p.lmax, w, F,
+                                                                          G, ncplx, R);
         note_launch();
         return;
     }
+    // FP64, many columns, full residual (the mixed transform returned above)
     dim3 grid((unsigned)(p.lmax + 1), (unsigned)p.nrn, 2u);
     const double w = 4.0 * M_PI / (double)p.npix;
-    if (p.precision == SFB_MIXED)
-        k_fold_residual<float><<<grid, 128, 0, st>>>(p.d_rings, (int)p.nrn, p.lmax, w, (const float *)F,
-                                                     (const float *)G, ncplx, (float *)R);
-    else
-        k_fold_residual<double><<<grid, 128, 0, st>>>(p.d_rings, (int)p.nrn, p.lmax, w, F, G, ncplx, R);
+    k_fold_residual<double><<<grid, 128, 0, st>>>(p.d_rings, (int)p.nrn, p.lmax, w, F, G, ncplx, R);
+    note_launch();
+}
+
+// double -> normalised double-float pairs (the mixed transform's map format)
+__global__ void k_to_df(const double *in, int64_t n, float2 *out) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double v = in[i];
+        const float h = (float)v;
+        out[i] = make_float2(h, (float)(v - (double)h));
+    }
+}
+
+void launch_to_df(const double *in, int64_t n, float2 *out, cudaStream_t st) {
+    if (n <= 0) return;
+    int64_t blocks = (n + 255) / 256;
+    if (blocks > 8192) blocks = 8192;
+    k_to_df<<<(unsigned)blocks, 256, 0, st>>>(in, n, out);
     note_launch();
 }
 

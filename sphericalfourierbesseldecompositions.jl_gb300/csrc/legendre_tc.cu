@@ -202,13 +202,13 @@ __device__ __forceinline__ bool lvl_stage_free(const LvlSmem &cs, int kc) {
 // Per (block z, column c): E with max_r |F[parity][m][r][c]| < 2^E, raised by
 // ceil(log2 nrn) - 9 for more than 512 rings (level sums below 2^24 units).
 // (nzr: F is zero outside the ring pairs [nzr[0], nzr[1]], which are the only ones read)
-__global__ void __launch_bounds__(256) k_colmax(const float *__restrict__ F, int64_t ncol, int lmax, int nrn,
+__global__ void __launch_bounds__(256) k_colmax(const float2 *__restrict__ F, int64_t ncol, int lmax, int nrn,
                                                 int *__restrict__ Ecol, const int *__restrict__ nzr) {
     const int z = blockIdx.y;
     const int m = z >> 1, par = z & 1;
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncol) return;
-    const float *Fz = F + ((int64_t)(par * (lmax + 1) + m) * nrn) * ncol + c;
+    const float2 *Fz = F + ((int64_t)(par * (lmax + 1) + m) * nrn) * ncol + c;
     float m0 = 0.f, m1 = 0.f, m2 = 0.f, m3 = 0.f;
     int r = 0, r1 = nrn;
     if (nzr) {
@@ -216,12 +216,12 @@ __global__ void __launch_bounds__(256) k_colmax(const float *__restrict__ F, int
         r1 = min(nrn, nzr[1] + 1);
     }
     for (; r + 3 < r1; r += 4) {
-        m0 = fmaxf(m0, fabsf(Fz[(int64_t)r * ncol]));
-        m1 = fmaxf(m1, fabsf(Fz[(int64_t)(r + 1) * ncol]));
-        m2 = fmaxf(m2, fabsf(Fz[(int64_t)(r + 2) * ncol]));
-        m3 = fmaxf(m3, fabsf(Fz[(int64_t)(r + 3) * ncol]));
+        m0 = fmaxf(m0, fabsf(Fz[(int64_t)r * ncol].x));
+        m1 = fmaxf(m1, fabsf(Fz[(int64_t)(r + 1) * ncol].x));
+        m2 = fmaxf(m2, fabsf(Fz[(int64_t)(r + 2) * ncol].x));
+        m3 = fmaxf(m3, fabsf(Fz[(int64_t)(r + 3) * ncol].x));
     }
-    for (; r < r1; ++r) m0 = fmaxf(m0, fabsf(Fz[(int64_t)r * ncol]));
+    for (; r < r1; ++r) m0 = fmaxf(m0, fabsf(Fz[(int64_t)r * ncol].x));
     const int lg = 32 - __clz(nrn > 1 ? nrn - 1 : 1);
     Ecol[(int64_t)z * ncol + c] = max(-90, min(scale_exp(fmaxf(fmaxf(m0, m1), fmaxf(m2, m3))) + max(0, lg - 9), 100));
 }
@@ -231,7 +231,7 @@ __global__ void __launch_bounds__(256) k_colmax(const float *__restrict__ F, int
 // Rings r >= rlim count as zero (the sum over the first rlim rings only).
 __global__ void __launch_bounds__(NTH, 2) k_leg_analysis_tc(const __nv_bfloat16 *__restrict__ lamtc,
                                                             const int64_t *__restrict__ lamtc_off, int lmax, int nrn,
-                                                            int nchunks, int rlim, const float *__restrict__ F,
+                                                            int nchunks, int rlim, const float2 *__restrict__ F,
                                                             int64_t ncol, const int *__restrict__ Ecol,
                                                             double *__restrict__ A, float2 *__restrict__ Adf,
                                                             int accumulate, int *__restrict__ Eout,
@@ -261,7 +261,7 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_analysis_tc(const __nv_bfloat16 
             nchunks = 1;
         }
     }
-    const float *Fz = F + ((int64_t)(par * (lmax + 1) + m) * nrn + (int64_t)kc0 * KC) * ncol + col0 + c;
+    const float2 *Fz = F + ((int64_t)(par * (lmax + 1) + m) * nrn + (int64_t)kc0 * KC) * ncol + col0 + c;
     const __nv_bfloat16 *Lz = lamtc + lamtc_off[z] + (int64_t)kc0 * 4 * pad16(rows_of(m, par, lmax)) * KC;
     rlim -= kc0 * KC;
     const uint32_t planeB = (uint32_t)NPc * KC * 2;
@@ -277,15 +277,15 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_analysis_tc(const __nv_bfloat16 
             if (issued != nchunks) atomicExch(cs.bad, 1);
         }
     } else {
-        float pre[4][8];          // this thread's 8 ring values of chunks kc .. kc + 3
-        auto loadA = [&](int kc, float (&buf)[8]) {
+        float2 pre[2][8];         // this thread's 8 double-float ring values of chunks kc, kc + 1
+        auto loadA = [&](int kc, float2 (&buf)[8]) {
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
                 const int r = kc * KC + 8 * kh + j;
-                buf[j] = (cok && r < rlim) ? Fz[(int64_t)r * ncol] : 0.f;
+                buf[j] = (cok && r < rlim) ? Fz[(int64_t)r * ncol] : make_float2(0.f, 0.f);
             }
         };
-        auto chunk = [&](int kc, float (&cur)[8]) -> bool {
+        auto chunk = [&](int kc, float2 (&cur)[8]) -> bool {
             const int s = kc % NSTAGE;
             if (!lvl_stage_free(cs, kc)) return false;
             unsigned char *sa = cs.stage(s);
@@ -301,27 +301,25 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_analysis_tc(const __nv_bfloat16 
 #pragma unroll
             for (int t = 0; t < 4; ++t) {
                 uint32_t v[4];
-                slice_pair(cur[2 * t], cur[2 * t + 1], C, v);
+                slice_pair_df(cur[2 * t].x, cur[2 * t].y, cur[2 * t + 1].x, cur[2 * t + 1].y, C, v);
 #pragma unroll
                 for (int q = 0; q < 4; ++q) w[q][t] = v[q];
             }
             const uint32_t off = core_off(c, 8 * kh);
 #pragma unroll
             for (int q = 0; q < 4; ++q) st_v4(sa + q * PLANE_A + off, w[q]);
-            if (kc + 4 < nchunks) loadA(kc + 4, cur);
+            if (kc + 2 < nchunks) loadA(kc + 2, cur);
             fence_proxy_async();
             __syncwarp();
             if ((tid & 31) == 0) mbar_arrive(&cs.full_a[s]);       // one arrival per producer warp
             return true;
         };
 #pragma unroll
-        for (int q = 0; q < 4; ++q)
+        for (int q = 0; q < 2; ++q)
             if (q < nchunks) loadA(q, pre[q]);
-        for (int kc = 0; kc < nchunks; kc += 4) {
+        for (int kc = 0; kc < nchunks; kc += 2) {
             if (!chunk(kc, pre[0])) break;
             if (kc + 1 < nchunks && !chunk(kc + 1, pre[1])) break;
-            if (kc + 2 < nchunks && !chunk(kc + 2, pre[2])) break;
-            if (kc + 3 < nchunks && !chunk(kc + 3, pre[3])) break;
         }
     }
     // every thread: wait for all MMAs, then the epilogue
@@ -390,11 +388,13 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_analysis_tc(const __nv_bfloat16 
 // Synthesis: grid (column tiles, ring tiles of NT <= NMAX, blocks z); warps
 // 0-7 produce, warp 8 issues the MMAs.
 //
-// Update mode (Adfnew != nullptr): the table holds the Gram matrices of the
-// alias-free rings, "rings" r are output rows li (nrn = rows of the largest
-// block), and the epilogue writes, instead of G,
-//   Anew[l(r)] = Acur[l(r)] + (A0[l(r)] - sum_li M[r][li] Acur[l(li)])
-// in double-float (Acur from Adf) and, when Anew is given, in FP64 (from Acur).
+// Update mode (Adfnew != nullptr): the table holds D = M - I, M the Gram
+// matrices of the alias-free rings; "rings" r are output rows li (nrn = rows of
+// the largest block), and the epilogue writes, instead of G,
+//   Anew[l(r)] = A0[l(r)] - sum_li D[r][li] Acur[l(li)]
+// (= Acur + (A0 - M Acur)) in double-float and, when Anew is given, in FP64.
+// |D| is the polar rings' share of the quadrature, so the product's FP32
+// accumulation error is that share of |Acur|, not all of it.
 __global__ void __launch_bounds__(NTH, 2) k_leg_synthesis_tc(const __nv_bfloat16 *__restrict__ lamts,
                                                              const int64_t *__restrict__ lamts_off, int lmax, int nrn,
                                                              int NT, const float2 *__restrict__ Adf, int64_t ncol,
@@ -531,18 +531,11 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_synthesis_tc(const __nv_bfloat16
                     const int l = m + par + 2 * (r0 + i0 + i);
                     return ((int64_t)l * (l + 1) / 2 + m) * ncol + cc;
                 };
-                float2 a0[8], ac[8];
-                double acur[8];
+                float2 a0[8];
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
-                    a0[i] = ac[i] = make_float2(0.f, 0.f);
-                    acur[i] = 0.0;
-                    if (r0 + i0 + i < nrows) {
-                        const int64_t o = off(i);
-                        a0[i] = A0[o];
-                        ac[i] = Adf[o];
-                        if (Acur) acur[i] = Acur[o];
-                    }
+                    a0[i] = make_float2(0.f, 0.f);
+                    if (r0 + i0 + i < nrows) a0[i] = A0[off(i)];
                 }
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
@@ -550,16 +543,12 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_synthesis_tc(const __nv_bfloat16
                     const int64_t o = off(i);
                     float hi, lo;
                     lvl_sum(v0[i], v1[i], v2[i], v3[i], hi, lo);
-                    // d = A0 - (hi, lo) and Adf + d in double-float (TwoSum, renormalised)
-                    float s = a0[i].x - hi, z2 = s - a0[i].x;
-                    float e = ((a0[i].x - (s - z2)) + (-hi - z2)) + (a0[i].y - lo);
-                    const float dh = s + e, dl = e - (dh - s);
-                    s = ac[i].x + dh;
-                    z2 = s - ac[i].x;
-                    e = ((ac[i].x - (s - z2)) + (dh - z2)) + (ac[i].y + dl);
-                    const float nh = s + e;
-                    Adfnew[o] = make_float2(nh, e - (nh - s));
-                    if (Anew) Anew[o] = acur[i] + ((double)dh + (double)dl);
+                    // A0 - (hi, lo) in double-float (TwoSum, renormalised)
+                    const float s = a0[i].x - hi, z2 = s - a0[i].x;
+                    const float e = ((a0[i].x - (s - z2)) + (-hi - z2)) + (a0[i].y - lo);
+                    const float nh = s + e, nl = e - (nh - s);
+                    Adfnew[o] = make_float2(nh, nl);
+                    if (Anew) Anew[o] = (double)nh + (double)nl;
                     umx = fmaxf(umx, fabsf(nh));
                 }
             }
@@ -719,7 +708,7 @@ void launch_build_lamtc(const Plan &p, const int *Ea, const int *Es, cudaStream_
     note_launch();
 }
 
-void launch_leg_analysis_tc(const Plan &p, const float *F, int64_t ncol, double *A, float2 *Adf, int *Ecol,
+void launch_leg_analysis_tc(const Plan &p, const float2 *F, int64_t ncol, double *A, float2 *Adf, int *Ecol,
                             bool accumulate, cudaStream_t st, bool scales_ready, int rlim, int *Eout,
                             const int *nzr) {
     if (rlim < 0 || rlim > p.nrn) rlim = (int)p.nrn;
@@ -815,8 +804,9 @@ void launch_gram_update(const Plan &p, const double *A, const float2 *Adf, const
     note_launch();
 }
 
-// Gram tables of the alias-free rings r >= p.ral, per block z:
-//   M_z[li][li'] = sum_r lambda_z(li, r) w n_r cfold_r lambda_z(li', r),
+// Gram tables of the alias-free rings r >= p.ral, per block z, stored as the
+// deviation from the identity:
+//   D_z[li][li'] = sum_r lambda_z(li, r) w n_r cfold_r lambda_z(li', r) - delta(li, li'),
 // formed with the FP64 synthesis (of unit coefficient vectors) and analysis
 // kernels, then sliced into the synthesis layout with the output rows as rings.
 namespace tc {
@@ -853,7 +843,7 @@ __global__ void k_gram_gather(int lmax, int R, const double *__restrict__ A, con
         double v = 0.0;
         if (ro < nrows) {
             const int l = m + par + 2 * ro;
-            v = A[((int64_t)l * (l + 1) / 2 + m) * R + li];
+            v = A[((int64_t)l * (l + 1) / 2 + m) * R + li] - (ro == li ? 1.0 : 0.0);
         }
         gram[gram_off[z] + (int64_t)li * R + ro] = v;
     }

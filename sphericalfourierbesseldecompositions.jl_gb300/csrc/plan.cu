@@ -86,6 +86,8 @@ void launch_transpose_ld(const float *in, int64_t ldi, int64_t rows, int64_t col
                          cudaStream_t st);
 void launch_transpose_ld(const double *in, int64_t ldi, int64_t rows, int64_t cols, float *out, int64_t ldo,
                          cudaStream_t st);
+void launch_transpose_ld(const float *in, int64_t ldi, int64_t rows, int64_t cols, float2 *out, int64_t ldo,
+                         cudaStream_t st);
 void launch_axpy(double *y, const double *x, int64_t n, cudaStream_t st);
 void launch_winweights(const double *weights, int64_t nr, int64_t nside, const double *rbounds, double rmax,
                        const double *rtp, int64_t ngal, double *w, int *err, cudaStream_t st);
@@ -333,10 +335,10 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, b
     DevBuf<double> &fbuf = *ws->f, &gbuf = *ws->g, &rbuf = *ws->r, &alm = *ws->alm;
     auto stage = [&](int s) { return stage_override >= 0 ? stage_override : s; };
     if (p.precision == SFB_MIXED && maps_are_fp64) {
-        SFB_TRY(grow(p, p.maps32, (size_t)(nm * p.npix + 1) / 2));
+        SFB_TRY(grow(p, p.maps32, (size_t)(nm * p.npix)));
         {
             Stage s(h, stage(SFB_STAGE_OTHER), st);
-            launch_to_float(maps, nm * p.npix, reinterpret_cast<float *>(p.maps32.ptr), st);
+            launch_to_df(maps, nm * p.npix, reinterpret_cast<float2 *>(p.maps32.ptr), st);
         }
         maps = p.maps32.ptr;
     }
@@ -356,7 +358,7 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, b
         SFB_TRY(grow(p, p.almdf, (size_t)p.lmsize * ncol));
         nzr = reinterpret_cast<int *>(p.erow.ptr) + 2 * std::max<int64_t>(p.nrn * nm, (p.lmax + 1) * ncol);
         Stage s(h, stage(SFB_STAGE_RING_FFT), st);
-        launch_ring_analysis_tc(p, reinterpret_cast<const float *>(maps), nm, reinterpret_cast<float *>(fbuf.ptr),
+        launch_ring_analysis_tc(p, reinterpret_cast<const float2 *>(maps), nm, reinterpret_cast<float2 *>(fbuf.ptr),
                                 reinterpret_cast<int *>(p.erow.ptr), nzr, st, ring_live, nlive);
     } else {
         // many columns: the FFT records the span of ring pairs with data, over which the
@@ -377,15 +379,15 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, b
         Stage s(h, stage(SFB_STAGE_LEG_ANALYSIS), st);
         // after the first pass the fold has written the column scales of its residual
         // the first pass reads the DFT output, zero outside the non-zero ring range
-        if (tc) launch_leg_analysis_tc(p, (const float *)src, ncol, alm.ptr, adf, ecol, acc, st, acc, -1, nullptr,
+        if (tc) launch_leg_analysis_tc(p, (const float2 *)src, ncol, alm.ptr, adf, ecol, acc, st, acc, -1, nullptr,
                                        acc ? nullptr : nzr);
         else launch_leg_analysis(p, src, ncol, alm.ptr, acc, st);
     };
     if (tc && ncol / 2 > 4 && p.d_gramts && p.niter > 0) {
-        // Gram refinement: a <- a + (a0 - M a) - A_al(Fold(S_al a)), M the Gram matrix of the
-        // alias-free rings (fold = identity there), S_al / A_al the synthesis and analysis
-        // over the aliased rings r < ral.  Each pass writes the other (A, Adf) buffer; the
-        // last one lands in the plan's.
+        // Gram refinement: a <- a + (a0 - M a) - A_al(Fold(S_al a)) = a0 - D a - A_al(Fold(S_al a)),
+        // M the Gram matrix of the alias-free rings (fold = identity there), D = M - I as the
+        // tables store it, S_al / A_al the synthesis and analysis over the aliased rings r < ral.
+        // Each pass writes the other (A, Adf) buffer; the last one lands in the plan's.
         SFB_TRY(grow(p, p.almdf2, (size_t)p.lmsize * ncol));
         SFB_TRY(grow(p, p.adf0, (size_t)p.lmsize * ncol));
         // column exponents of each (A, Adf) set, written by whichever kernel completes the set
@@ -400,7 +402,7 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, b
         SFB_CUDA_TRY(cudaMemsetAsync(Eb[cur], 0x80, (size_t)nE * sizeof(int), st));
         {
             Stage s(h, stage(SFB_STAGE_LEG_ANALYSIS), st);
-            launch_leg_analysis_tc(p, (const float *)fbuf.ptr, ncol, Ab[cur], Db[cur], ecol, false, st, false, -1,
+            launch_leg_analysis_tc(p, (const float2 *)fbuf.ptr, ncol, Ab[cur], Db[cur], ecol, false, st, false, -1,
                                    Eb[cur], nzr);
         }
         SFB_CUDA_TRY(cudaMemcpyAsync(p.adf0.ptr, Db[cur], (size_t)p.lmsize * ncol * sizeof(float2),
@@ -420,7 +422,7 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, b
                     launch_fold_residual(p, nullptr, gbuf.ptr, ncol, rbuf.ptr, st, ecol, p.ral);
                 }
                 Stage s(h, stage(SFB_STAGE_LEG_ANALYSIS), st);
-                launch_leg_analysis_tc(p, (const float *)rbuf.ptr, ncol, Ab[nxt], Db[nxt], ecol, true, st, true,
+                launch_leg_analysis_tc(p, (const float2 *)rbuf.ptr, ncol, Ab[nxt], Db[nxt], ecol, true, st, true,
                                        p.ral, Eb[nxt]);
             }
             cur = nxt;
@@ -602,7 +604,7 @@ int cat2amln_dev(sfb_plan *h, const double *rtp, const double *w, int64_t ngal, 
         if (wk == SFB_WINDOW_SEPARABLE) {
             Stage s(h, SFB_STAGE_OTHER, st);
             if (p.precision == SFB_MIXED)
-                launch_to_float(win->mask, p.npix, reinterpret_cast<float *>(p.maps.ptr) + p.nbasis * p.npix, st);
+                launch_to_df(win->mask, p.npix, reinterpret_cast<float2 *>(p.maps.ptr) + p.nbasis * p.npix, st);
             else
                 SFB_CUDA_TRY(cudaMemcpyAsync(p.maps.ptr + p.nbasis * p.npix, win->mask, p.npix * sizeof(double),
                                              cudaMemcpyDeviceToDevice, st));
@@ -1445,7 +1447,7 @@ static int sfb_field2anlm_impl(sfb_plan *h, const void *f, int32_t dtype, int64_
         if (dtype == SFB_F32) {
             const float *src = reinterpret_cast<const float *>(d_f) + off;
             if (mixed) {
-                launch_transpose_ld(src, ld, p.npix, nsc, reinterpret_cast<float *>(p.maps.ptr), p.npix, st);
+                launch_transpose_ld(src, ld, p.npix, nsc, reinterpret_cast<float2 *>(p.maps.ptr), p.npix, st);
                 maps64 = false;
             } else {
                 launch_transpose_ld(src, ld, p.npix, nsc, p.maps.ptr, p.npix, st);

@@ -60,9 +60,14 @@ using namespace tc;
 
 constexpr int ZERO_ROW_E = -127;  // row exponent of an all-zero ring row
 
-// w (hi + lo) rounded once: w = (w.x, w.y) a double-float constant
-__device__ __forceinline__ float wmul(float2 w, float hi, float lo) {
-    return fmaf(w.x, hi, fmaf(w.y, hi, w.x * lo));
+// w (hi + lo) as a normalised double-float pair: w = (w.x, w.y) a double-float
+// constant, the leading product's rounding error kept (TwoProd by FMA)
+__device__ __forceinline__ float2 wmul_df(float2 w, float hi, float lo) {
+    const float p = w.x * hi;
+    const float e = fmaf(w.x, hi, -p);
+    const float t = e + fmaf(w.y, hi, w.x * lo);
+    const float h = p + t;
+    return make_float2(h, t - (h - p));
 }
 constexpr int KC = 32;            // pixels per chunk
 constexpr int NPAIR = 64;         // (ring, map) pairs per CTA
@@ -79,12 +84,13 @@ __device__ __forceinline__ uint32_t core_off(int row, int k) {
     return (uint32_t)((((row >> 3) * (KC / 8) + (k >> 3)) << 7) + ((row & 7) << 4) + ((k & 7) << 1));
 }
 
-// slices of 8 values (see slice_pair), packed as 4 words per plane
-__device__ __forceinline__ void slice8(const float (&x)[8], const float (&C)[4], uint32_t (&w)[4][4]) {
+// slices of 8 double-float values (hi, lo) (see slice_pair_df), packed as 4 words per plane
+__device__ __forceinline__ void slice8_df(const float (&h)[8], const float (&l)[8], const float (&C)[4],
+                                          uint32_t (&w)[4][4]) {
 #pragma unroll
     for (int t = 0; t < 8; t += 2) {
         uint32_t v[4];
-        slice_pair(x[t], x[t + 1], C, v);
+        slice_pair_df(h[t], l[t], h[t + 1], l[t + 1], C, v);
 #pragma unroll
         for (int s = 0; s < 4; ++s) w[s][t >> 1] = v[s];
     }
@@ -103,7 +109,7 @@ __device__ __forceinline__ void st_shared_v4(unsigned char *p, const uint32_t (&
 // nzr[0] / nzr[1] get the first / last ring pair with a non-zero row (preset
 // to a large value / -1).  With ring_live, the rows of maps b < nlive on the
 // rings marked 0 are zero by construction and are not read.
-__global__ void __launch_bounds__(128) k_ring_rowexp(const float *__restrict__ maps, int64_t npix, int64_t nmaps,
+__global__ void __launch_bounds__(128) k_ring_rowexp(const float2 *__restrict__ maps, int64_t npix, int64_t nmaps,
                                                      const RingGeom *__restrict__ rings, int nrn, int *erow,
                                                      int *nzr, const int *__restrict__ ring_live, int64_t nlive,
                                                      int nrings) {
@@ -119,13 +125,13 @@ __global__ void __launch_bounds__(128) k_ring_rowexp(const float *__restrict__ m
             if (lane == 0) erow[((int64_t)h * nrn + r) * nmaps + b] = ZERO_ROW_E;
             continue;
         }
-        const float *x = maps + b * npix + (h ? g.start_s : g.start_n);
+        const float2 *x = maps + b * npix + (h ? g.start_s : g.start_n);
         float mx = 0.f;
         bool fin = true;
         for (int j = lane; j < g.nph; j += 32) {
-            const float v = x[j];
-            fin &= isfinite(v);
-            mx = fmaxf(mx, fabsf(v));
+            const float2 v = x[j];                       // |hi + lo| < 2^E when |hi| < 2^E
+            fin &= isfinite(v.x) && isfinite(v.y);
+            mx = fmaxf(mx, fabsf(v.x));
         }
         for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
         fin = __all_sync(0xffffffffu, fin);
@@ -149,14 +155,14 @@ __global__ void __launch_bounds__(128) k_ring_rowexp(const float *__restrict__ m
 // slice the map rows, two threads per row; otherwise warps 4-7 gather B from
 // the ring's sliced table.
 template <bool IMG>
-__global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict__ maps, int64_t npix, int64_t nmaps,
+__global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float2 *__restrict__ maps, int64_t npix, int64_t nmaps,
                                                          const RingGeom *__restrict__ rings, int nrn, int lmax,
                                                          const int32_t *__restrict__ cls_rings,
                                                          const int32_t *__restrict__ cls_off,
                                                          const int *__restrict__ erow, const uint2 *__restrict__ dtw,
                                                          const int64_t *__restrict__ dtw_off,
                                                          const unsigned char *__restrict__ img,
-                                                         const int64_t *__restrict__ img_off, float *__restrict__ F,
+                                                         const int64_t *__restrict__ img_off, float2 *__restrict__ F,
                                                          int64_t ldF, float2 wdf, int *err) {
     extern __shared__ __align__(1024) unsigned char smem[];
     // grid (column blocks u, row tiles, classes): the column blocks of one row tile are launched
@@ -219,7 +225,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
     const int E = rok ? erow[((int64_t)hemi * nrn + ring) * nmaps + b] : ZERO_ROW_E;
     // zero rows are not read (on rings without galaxies they are not even written)
     const bool live = abuild && rok && (hemi == 0 || g.start_s != g.start_n) && E != ZERO_ROW_E;
-    const float *x = maps + b * npix + (hemi ? g.start_s : g.start_n);
+    const float2 *x = maps + b * npix + (hemi ? g.start_s : g.start_n);
     float C[4];
     slice_consts(E == ZERO_ROW_E ? 0 : E, C);
     const int L1 = lmax + 1;
@@ -231,8 +237,8 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
             const int64_t qo = pair0 + pr;
             if (mm > lmax || qo >= npairs) continue;
             const int oring = cls_rings[rb + (int)(qo / nmaps)];
-            *reinterpret_cast<float2 *>(F + ((int64_t)(sg * L1 + mm) * nrn + oring) * ldF + 2 * (qo % nmaps)) =
-                make_float2(0.f, 0.f);
+            *reinterpret_cast<float4 *>(F + ((int64_t)(sg * L1 + mm) * nrn + oring) * ldF + 2 * (qo % nmaps)) =
+                make_float4(0.f, 0.f, 0.f, 0.f);
         }
         return;
     }
@@ -298,14 +304,15 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
             if (issued != nch) atomicExch(bad, 1);
         }
     } else {
-        // raw map values of the next PD chunks (n is a multiple of 4, ring starts are 16-byte aligned)
-        constexpr int NV4 = IMG ? 4 : 8;          // float4 loads per thread per chunk
+        // double-float map values (hi, lo) of the next PD chunks, two per float4 load (n is a multiple
+        // of 4, ring starts are even, so every load is 16-byte aligned)
+        constexpr int NV4 = IMG ? 8 : 16;         // float4 loads per thread per chunk (16 or 32 values)
         constexpr int PD = IMG ? 2 : 1;           // chunks loaded ahead
         float4 pre[PD][NV4];
         auto load_chunk = [&](int kc, float4 (&buf)[NV4]) {
 #pragma unroll
             for (int i = 0; i < NV4; ++i) {
-                const int j = kc * KC + 16 * ahalf + 4 * i;
+                const int j = kc * KC + 16 * ahalf + 2 * i;
                 buf[i] = (live && j < n) ? *reinterpret_cast<const float4 *>(x + j) : make_float4(0.f, 0.f, 0.f, 0.f);
             }
         };
@@ -330,11 +337,12 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
             if (abuild) {
                 // A row: this thread's pixels as groups of 8
 #pragma unroll
-                for (int gq = 0; gq < NV4 / 2; ++gq) {
-                    const float v[8] = {cur[2 * gq].x, cur[2 * gq].y, cur[2 * gq].z, cur[2 * gq].w,
-                                        cur[2 * gq + 1].x, cur[2 * gq + 1].y, cur[2 * gq + 1].z, cur[2 * gq + 1].w};
+                for (int gq = 0; gq < NV4 / 4; ++gq) {
+                    const float4 *c4 = cur + 4 * gq;
+                    const float vh[8] = {c4[0].x, c4[0].z, c4[1].x, c4[1].z, c4[2].x, c4[2].z, c4[3].x, c4[3].z};
+                    const float vl[8] = {c4[0].y, c4[0].w, c4[1].y, c4[1].w, c4[2].y, c4[2].w, c4[3].y, c4[3].w};
                     uint32_t w[4][4];
-                    slice8(v, C, w);
+                    slice8_df(vh, vl, C, w);
                     const uint32_t off = core_off(ti, 16 * ahalf + 8 * gq);
 #pragma unroll
                     for (int s = 0; s < 4; ++s) st_shared_v4(sbase + s * PLANE + off, w[s]);
@@ -420,11 +428,11 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
             for (int t = 0; t < 8; ++t) {
                 const int mm = 64 * u + 8 * cg + t;
                 if (mm > lmax) break;
-                const float2 f = make_float2(
-                    wmul(wdf, v0[2 * t], v1[2 * t] + (v2[2 * t] + v3[2 * t])),
-                    wmul(wdf, v0[2 * t + 1], v1[2 * t + 1] + (v2[2 * t + 1] + v3[2 * t + 1])));
-                *reinterpret_cast<float2 *>(F + ((int64_t)mm * nrn + oring) * ldF + 2 * ob) = f;
-                *reinterpret_cast<float2 *>(F + ((int64_t)(L1 + mm) * nrn + oring) * ldF + 2 * ob) = f;
+                const float2 fr = wmul_df(wdf, v0[2 * t], v1[2 * t] + (v2[2 * t] + v3[2 * t]));
+                const float2 fi = wmul_df(wdf, v0[2 * t + 1], v1[2 * t + 1] + (v2[2 * t + 1] + v3[2 * t + 1]));
+                const float4 f = make_float4(fr.x, fr.y, fi.x, fi.y);
+                *reinterpret_cast<float4 *>(F + ((int64_t)mm * nrn + oring) * ldF + 2 * ob) = f;
+                *reinterpret_cast<float4 *>(F + ((int64_t)(L1 + mm) * nrn + oring) * ldF + 2 * ob) = f;
             }
         }
     } else if (prod) {
@@ -466,7 +474,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
                 for (int t = 0; t < 8; ++t) {
                     const int mm = 64 * u + 8 * cg + t;
                     if (mm > lmax) break;
-                    float f[2];
+                    float2 f[2];
 #pragma unroll
                     for (int c2 = 0; c2 < 2; ++c2) {
                         const int i = 2 * t + c2;
@@ -474,10 +482,10 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float *__restrict
                         const float s = a + bb;
                         const float z = s - a;
                         const float e = (a - (s - z)) + (bb - z);
-                        f[c2] = wmul(wdf, s, (xh[(2 * i + 1) * NROW + pr] + sgn * xh[(2 * i + 1) * NROW + pr + NPAIR]) + e);
+                        f[c2] = wmul_df(wdf, s, (xh[(2 * i + 1) * NROW + pr] + sgn * xh[(2 * i + 1) * NROW + pr + NPAIR]) + e);
                     }
-                    *reinterpret_cast<float2 *>(F + ((int64_t)(sg * L1 + mm) * nrn + oring) * ldF + 2 * ob) =
-                        make_float2(f[0], f[1]);
+                    *reinterpret_cast<float4 *>(F + ((int64_t)(sg * L1 + mm) * nrn + oring) * ldF + 2 * ob) =
+                        make_float4(f[0].x, f[0].y, f[1].x, f[1].y);
                 }
             }
             asm volatile("bar.sync 1, %0;" ::"r"(NPROD) : "memory");
@@ -586,7 +594,7 @@ uint2 dft_slices(double v, int EB) {
     return make_uint2((uint32_t)s[0] | ((uint32_t)s[1] << 16), (uint32_t)s[2] | ((uint32_t)s[3] << 16));
 }
 
-void launch_ring_analysis_tc(const Plan &p, const float *maps, int64_t nmaps, float *F, int *erow, int *nzr,
+void launch_ring_analysis_tc(const Plan &p, const float2 *maps, int64_t nmaps, float2 *F, int *erow, int *nzr,
                              cudaStream_t st, const int *ring_live, int64_t nlive) {
     {
         // nzr[0] = 0x7f7f7f7f (above any ring index), nzr[1] = -1

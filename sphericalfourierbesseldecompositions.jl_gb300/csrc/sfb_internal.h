@@ -238,10 +238,12 @@ void launch_project_poly(const Plan &p, const double *A, int64_t ldA, double sca
                          const double *w_ln, int64_t mask_col, const double *Awin, int64_t ldW,
                          double *out, cudaStream_t st);
 void launch_to_float(const double *in, int64_t n, float *out, cudaStream_t st);
-// Mixed-precision ring analysis on the tensor cores (FP32 maps -> FP32 F).
+// double -> normalised double-float pairs (maps of the mixed-precision transform)
+void launch_to_df(const double *in, int64_t n, float2 *out, cudaStream_t st);
+// Mixed-precision ring analysis on the tensor cores (double-float maps -> double-float F).
 // nzr[0..1] receives the first and last ring pair holding a non-zero map row.
 // ring_live (optional): rings whose entry is 0 hold zeros in maps [0, nlive) and are not read.
-void launch_ring_analysis_tc(const Plan &p, const float *maps, int64_t nmaps, float *F, int *erow, int *nzr,
+void launch_ring_analysis_tc(const Plan &p, const float2 *maps, int64_t nmaps, float2 *F, int *erow, int *nzr,
                              cudaStream_t st, const int *ring_live = nullptr, int64_t nlive = 0);
 uint2 dft_slices(double v, int EB);
 int64_t dft_image_offsets(const Plan &p, const std::vector<int32_t> &crings, const std::vector<int32_t> &coff,
@@ -250,11 +252,12 @@ void launch_build_dft_image(const Plan &p, int max_nch, cudaStream_t st);
 // tensor-core (tcgen05) Legendre analysis, mixed precision
 int64_t tc_table_offsets(const Plan &p, std::vector<int64_t> &off);
 void launch_build_lamtc(const Plan &p, const int *Ea, const int *Es, cudaStream_t st);
-// Ecol: column scales of F; computed here unless scales_ready (the fold wrote them).
+// F: double-float (hi, lo) per element.  Ecol: column scales of F; computed here unless scales_ready
+// (the fold wrote them).
 // rlim: the sum runs over the first rlim rings only (-1: all).
 // Eout (optional): atomicMax of each output column's exponent per block z (preset below every exponent).
 // nzr (optional, device): F is zero on the ring pairs outside [nzr[0], nzr[1]]; the sum skips them.
-void launch_leg_analysis_tc(const Plan &p, const float *F, int64_t ncol, double *A, float2 *Adf, int *Ecol,
+void launch_leg_analysis_tc(const Plan &p, const float2 *F, int64_t ncol, double *A, float2 *Adf, int *Ecol,
                             bool accumulate, cudaStream_t st, bool scales_ready = false, int rlim = -1,
                             int *Eout = nullptr, const int *nzr = nullptr);
 int64_t tc_synth_table_offsets(const Plan &p, std::vector<int64_t> &off, int64_t nrn = -1);

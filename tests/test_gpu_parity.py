@@ -448,7 +448,12 @@ def test_calc_wmix_vs_oracle(neg_m):
     record(f"calc_wmix_vs_oracle_negm{int(neg_m)}", e, nlmsize=int(gpu.shape[0]))
     assert np.all(np.isfinite(gpu)) and e < 1e-12
     if not neg_m:
-        # 400 shells: the midpoint rule of the radial overlap integrals to ~1e-3
-        wf = sfbgpu.ConfigurationSpaceModes(a.rmin, a.rmax, 400, a.nside)
-        one = sfbgpu.calc_wmix(np.ones((wf.nr, wf.npix)), wf, a)
-        assert np.max(np.abs(one - np.eye(one.shape[0]))) < 5e-3
+        # A constant window: nside 16 so that the window's band limit 2 lmax = 30 stays below
+        # 2 nside (at nside 8 the ring quadrature of L > 2 nside leaves a 3% diagonal error,
+        # in the oracle too); 400 shells put the midpoint rule of the overlaps near 1e-5.
+        a16 = sfbgpu.AnlmModes(0.02, 500.0, 1000.0, nside=16)
+        wf = sfbgpu.ConfigurationSpaceModes(a16.rmin, a16.rmax, 400, a16.nside)
+        one = sfbgpu.calc_wmix(np.ones((wf.nr, wf.npix)), wf, a16)
+        dev = float(np.max(np.abs(one - np.eye(one.shape[0]))))
+        record("calc_wmix_constant_window_identity", dev, nside=16, shells=400)
+        assert dev < 1e-4
