@@ -13,14 +13,17 @@
 // Error-free splitting (block-floating-point slicing, Ozaki, Ogita, Oishi,
 // Rump, Numer. Algorithms 59, 2012): every operand value is written as four
 // BF16 slices on a scale common to its whole K range - per lambda row (plan
-// tables), per column of F or A (a max pass over the CTA's K range).  The
-// products of slice level v = s_a + s_b (v = 0..3; ten products) are integer
-// multiples of one unit per accumulator entry and each level has its own FP32
-// accumulator in TMEM; the level sums stay below 2^24 units for K <= 1024
-// (rings) and K <= 512 (rows), so they are exact whatever the tensor cores'
-// accumulation order or rounding.  The epilogue adds the four levels with one
-// significant rounding.  Levels >= 4 (below 2^-27 of the leading products)
-// are dropped.
+// tables), per column of F or A (a max pass over the CTA's K range); the
+// leading slice of lambda and of F has 8 bits, that of A 7.  The products of
+// slice level v = s_a + s_b (v = 0..3; ten products) are integer multiples of
+// one unit per accumulator entry and each level has its own FP32 accumulator
+// in TMEM; the leading level sums stay within 2^24 units for K <= 1024 (ring
+// pairs) and K <= 512 (rows), so they are exact whatever the tensor cores'
+// accumulation order or rounding.  The analysis also adds the three level-4
+// products (near 2^-28 of the leading ones) into the level-3 accumulator,
+// whose own rounding is far below that; the synthesis, which only forms the
+// refinement's small corrections, drops them.  The epilogue adds the four
+// levels with one significant rounding.
 //
 // The F (analysis) and A (synthesis) tiles are sliced by the CTA's threads
 // into four K-major BF16 planes in shared memory; the lambda planes come
@@ -135,14 +138,16 @@ __device__ __forceinline__ void lvl_teardown(uint32_t tmem) {
 }
 
 // The ten level products of one K chunk (one K step of 16) as six MMAs
-// (tc_common.cuh): level v goes to TMEM columns [LS v, LS v + LS), LS = the
-// MMA's N (lambda rows or rings of this CTA).
+// (tc_common.cuh), with LV4 the three level-4 products as three more: level v
+// goes to TMEM columns [LS v, LS v + LS), LS = the MMA's N (lambda rows or
+// rings of this CTA), level 4 with level 3.
+template <bool LV4>
 __device__ __forceinline__ void lvl_mma(uint32_t tmem, uint32_t a0, uint32_t b0, uint32_t planeB, int LS,
                                         bool first_chunk) {
     const uint32_t sbo = (KC / 8) * 128;
     const uint32_t id1 = idesc_bf16(MTILE, LS), id2 = idesc_bf16(MTILE, 2 * LS);
 #pragma unroll
-    for (int q = 0; q < NMERGED; ++q) {
+    for (int q = 0; q < (LV4 ? NMERGED4 : NMERGED); ++q) {
         const uint64_t ad = smem_desc(a0 + mg_a(q) * PLANE_A, 128, sbo);
         const uint64_t bd = smem_desc(b0 + mg_b(q) * planeB, 128, sbo);
         const uint32_t acc = (first_chunk && mg_first(q)) ? 0u : 1u;
@@ -165,8 +170,9 @@ __device__ __forceinline__ void lvl_sum(float L0, float L1, float L2, float L3, 
 __device__ __forceinline__ uint32_t ph_of(int kc) { return (uint32_t)((kc / NSTAGE) & 1); }
 
 // MMA warp (lane 0 issues): for every chunk wait for its A slices and lambda
-// planes, issue the ten products, release the stage; finally commit `done`.
-// Returns the number of chunks issued.
+// planes, issue the ten (LV4: thirteen) products, release the stage; finally
+// commit `done`.  Returns the number of chunks issued.
+template <bool LV4>
 __device__ __forceinline__ int lvl_mma_loop(const LvlSmem &cs, uint32_t tmem, int nch, uint32_t planeB, int LS) {
     int issued = 0;
     for (int kc = 0; kc < nch; ++kc) {
@@ -178,7 +184,7 @@ __device__ __forceinline__ int lvl_mma_loop(const LvlSmem &cs, uint32_t tmem, in
         }
         fence_after();
         const uint32_t sa = smem_u32(cs.stage(s));
-        lvl_mma(tmem, sa, sa + 4 * PLANE_A, planeB, LS, kc == 0);
+        lvl_mma<LV4>(tmem, sa, sa + 4 * PLANE_A, planeB, LS, kc == 0);
         mma_commit(&cs.empty[s]);
         ++issued;
     }
@@ -200,7 +206,9 @@ __device__ __forceinline__ bool lvl_stage_free(const LvlSmem &cs, int kc) {
 }
 
 // Per (block z, column c): E with max_r |F[parity][m][r][c]| < 2^E, raised by
-// ceil(log2 nrn) - 9 for more than 512 rings (level sums below 2^24 units).
+// ceil(log2 nrn) - 10 for more than 1024 ring pairs, so that the exact level
+// sums (8-bit leading slices of F and lambda, at most 2^14 units a product)
+// stay within 2^24 units.
 // (nzr: F is zero outside the ring pairs [nzr[0], nzr[1]], which are the only ones read)
 __global__ void __launch_bounds__(256) k_colmax(const float2 *__restrict__ F, int64_t ncol, int lmax, int nrn,
                                                 int *__restrict__ Ecol, const int *__restrict__ nzr) {
@@ -223,7 +231,7 @@ __global__ void __launch_bounds__(256) k_colmax(const float2 *__restrict__ F, in
     }
     for (; r < r1; ++r) m0 = fmaxf(m0, fabsf(Fz[(int64_t)r * ncol].x));
     const int lg = 32 - __clz(nrn > 1 ? nrn - 1 : 1);
-    Ecol[(int64_t)z * ncol + c] = max(-90, min(scale_exp(fmaxf(fmaxf(m0, m1), fmaxf(m2, m3))) + max(0, lg - 9), 100));
+    Ecol[(int64_t)z * ncol + c] = max(-90, min(scale_exp(fmaxf(fmaxf(m0, m1), fmaxf(m2, m3))) + max(0, lg - 10), 100));
 }
 
 // Analysis: grid (column tiles, row tiles of NMAX, blocks z); warps 0-7
@@ -267,13 +275,13 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_analysis_tc(const __nv_bfloat16 
     const uint32_t planeB = (uint32_t)NPc * KC * 2;
     LvlSmem cs = lvl_smem(smem);
     float C[4];
-    slice_consts(cok ? Ecol[(int64_t)z * ncol + col0 + c] : 0, C);
+    slice_consts8(cok ? Ecol[(int64_t)z * ncol + col0 + c] : 0, C);
     const uint32_t tmem = lvl_setup(cs);
     const int LS = NPc;                         // MMA N and TMEM level stride
 
     if (!prod) {
         if ((tid & 31) == 0) {
-            const int issued = lvl_mma_loop(cs, tmem, nchunks, planeB, LS);
+            const int issued = lvl_mma_loop<true>(cs, tmem, nchunks, planeB, LS);
             if (issued != nchunks) atomicExch(cs.bad, 1);
         }
     } else {
@@ -456,7 +464,7 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_synthesis_tc(const __nv_bfloat16
 
     if (!prod) {
         if (lane == 0) {
-            const int issued = lvl_mma_loop(cs, tmem, nK, planeB, LS);
+            const int issued = lvl_mma_loop<false>(cs, tmem, nK, planeB, LS);
             if (issued != nK) atomicExch(cs.bad, 1);
         }
     } else {

@@ -120,6 +120,13 @@ __device__ __forceinline__ void slice_consts(int E, float (&C)[4]) {
     for (int k = 0; k < 4; ++k) C[k] = 1.5f * pow2f(E + 17 - 7 * k);
 }
 
+// The same with an 8-bit leading slice: s_k a multiple of 2^(E - 7 - 7k),
+// |s_0| <= 128 (BF16 holds the integers up to 256 exactly), |s_k| <= 64 after.
+__device__ __forceinline__ void slice_consts8(int E, float (&C)[4]) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) C[k] = 1.5f * pow2f(E + 16 - 7 * k);
+}
+
 __device__ __forceinline__ uint32_t bf16x2(float lo, float hi) {
     uint32_t r;
     asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
@@ -173,11 +180,20 @@ __device__ __forceinline__ int scale_exp(float mx) {
 // q2 A1 x [B0|B1] -> 1, 2;  q3 A1 x B2 -> 3;  q4 A2 x [B0|B1] -> 2, 3;
 // q5 A3 x B0 -> 3.  q0 and q1 write every level first (no accumulate on the
 // first K step).
+//
+// With the level-4 products (NMERGED4): q6 A1 x B3, q7 A2 x B2, q8 A3 x B1,
+// each of N into the level-3 accumulator.  Level 3 carries 2^-21 of the
+// leading level, so its FP32 rounding (it is no longer an integer sum below
+// 2^24 units) stays near 2^-45 of the result.  The three products (each near
+// 2^-28 of the leading ones) are then no longer truncated; what remains is
+// each operand's own four-slice representation and the level-5 products
+// (2^-35).
 constexpr int NMERGED = 6;
-__device__ __forceinline__ int mg_a(int q) { return q < 2 ? 0 : q < 4 ? 1 : q < 5 ? 2 : 3; }
-__device__ __forceinline__ int mg_b(int q) { return (q == 1 || q == 3) ? 2 : 0; }
+constexpr int NMERGED4 = 9;
+__device__ __forceinline__ int mg_a(int q) { return q < 2 ? 0 : q < 4 ? 1 : q < 5 ? 2 : q < 6 ? 3 : q - 5; }
+__device__ __forceinline__ int mg_b(int q) { return (q == 1 || q == 3) ? 2 : q < 6 ? 0 : 9 - q; }
 __device__ __forceinline__ int mg_lvl(int q) { return q == 0 ? 0 : q == 2 ? 1 : (q == 1 || q == 4) ? 2 : 3; }
-__device__ __forceinline__ bool mg_two(int q) { return q != 3 && q != 5; }
+__device__ __forceinline__ bool mg_two(int q) { return q != 3 && q < 5; }
 __device__ __forceinline__ bool mg_first(int q) { return q < 2; }
 
 }  // namespace tc
