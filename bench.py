@@ -528,6 +528,9 @@ def main():
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu captures: same geometry, 2 radial pieces x degree 15 (34 maps), "
                          "1e6 galaxies, no e2e / CPU baseline")
+    ap.add_argument("--full-basis", action="store_true",
+                    help="with --profile-case: the bench's own radial basis (328 maps) with the profile case's "
+                         "galaxy count, for per-kernel DRAM traffic captures")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -536,7 +539,7 @@ def main():
         args.ngal = args.ngal or 1_000_000
         args.no_cpu_baseline = True
         args.no_c1 = True
-        plan_extra = {"pieces": 2, "degree": 15}
+        plan_extra = {} if args.full_basis else {"pieces": 2, "degree": 15}
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -13,17 +13,17 @@
 // Error-free splitting (block-floating-point slicing, Ozaki, Ogita, Oishi,
 // Rump, Numer. Algorithms 59, 2012): every operand value is written as four
 // BF16 slices on a scale common to its whole K range - per lambda row (plan
-// tables), per column of F or A (a max pass over the CTA's K range); the
-// leading slice of lambda and of F has 8 bits, that of A 7.  The products of
-// slice level v = s_a + s_b (v = 0..3; ten products) are integer multiples of
-// one unit per accumulator entry and each level has its own FP32 accumulator
-// in TMEM; the leading level sums stay within 2^24 units for K <= 1024 (ring
-// pairs) and K <= 512 (rows), so they are exact whatever the tensor cores'
-// accumulation order or rounding.  The analysis also adds the three level-4
-// products (near 2^-28 of the leading ones) into the level-3 accumulator,
-// whose own rounding is far below that; the synthesis, which only forms the
-// refinement's small corrections, drops them.  The epilogue adds the four
-// levels with one significant rounding.
+// tables), per column of F or A (a max pass over the CTA's K range) - with
+// 8-bit slice steps, so each operand is represented to 2^-31 (A: 7-bit
+// leading slice) or 2^-32 (lambda, F: 8-bit leading slice) of its scale.  The
+// products of slice level v = s_a + s_b (v = 0..3; ten products) are integer
+// multiples of one unit per accumulator entry and each level has its own FP32
+// accumulator in TMEM; the level-0 sums stay within 2^24 units for K <= 1024
+// (ring pairs) and K <= 512 (rows), so they are exact whatever the tensor
+// cores' accumulation order or rounding, and the level-v sums (v >= 1) carry
+// 2^(-8 v) of the leading one, so a rounding there stays below 2^-32 of it.
+// Levels >= 4 (below 2^-32 of the leading products) are dropped.  The
+// epilogue adds the four levels with one significant rounding.
 //
 // The F (analysis) and A (synthesis) tiles are sliced by the CTA's threads
 // into four K-major BF16 planes in shared memory; the lambda planes come
@@ -138,16 +138,14 @@ __device__ __forceinline__ void lvl_teardown(uint32_t tmem) {
 }
 
 // The ten level products of one K chunk (one K step of 16) as six MMAs
-// (tc_common.cuh), with LV4 the three level-4 products as three more: level v
-// goes to TMEM columns [LS v, LS v + LS), LS = the MMA's N (lambda rows or
-// rings of this CTA), level 4 with level 3.
-template <bool LV4>
+// (tc_common.cuh): level v goes to TMEM columns [LS v, LS v + LS), LS = the
+// MMA's N (lambda rows or rings of this CTA).
 __device__ __forceinline__ void lvl_mma(uint32_t tmem, uint32_t a0, uint32_t b0, uint32_t planeB, int LS,
                                         bool first_chunk) {
     const uint32_t sbo = (KC / 8) * 128;
     const uint32_t id1 = idesc_bf16(MTILE, LS), id2 = idesc_bf16(MTILE, 2 * LS);
 #pragma unroll
-    for (int q = 0; q < (LV4 ? NMERGED4 : NMERGED); ++q) {
+    for (int q = 0; q < NMERGED; ++q) {
         const uint64_t ad = smem_desc(a0 + mg_a(q) * PLANE_A, 128, sbo);
         const uint64_t bd = smem_desc(b0 + mg_b(q) * planeB, 128, sbo);
         const uint32_t acc = (first_chunk && mg_first(q)) ? 0u : 1u;
@@ -170,9 +168,8 @@ __device__ __forceinline__ void lvl_sum(float L0, float L1, float L2, float L3, 
 __device__ __forceinline__ uint32_t ph_of(int kc) { return (uint32_t)((kc / NSTAGE) & 1); }
 
 // MMA warp (lane 0 issues): for every chunk wait for its A slices and lambda
-// planes, issue the ten (LV4: thirteen) products, release the stage; finally
-// commit `done`.  Returns the number of chunks issued.
-template <bool LV4>
+// planes, issue the ten products, release the stage; finally commit `done`.
+// Returns the number of chunks issued.
 __device__ __forceinline__ int lvl_mma_loop(const LvlSmem &cs, uint32_t tmem, int nch, uint32_t planeB, int LS) {
     int issued = 0;
     for (int kc = 0; kc < nch; ++kc) {
@@ -184,7 +181,7 @@ __device__ __forceinline__ int lvl_mma_loop(const LvlSmem &cs, uint32_t tmem, in
         }
         fence_after();
         const uint32_t sa = smem_u32(cs.stage(s));
-        lvl_mma<LV4>(tmem, sa, sa + 4 * PLANE_A, planeB, LS, kc == 0);
+        lvl_mma(tmem, sa, sa + 4 * PLANE_A, planeB, LS, kc == 0);
         mma_commit(&cs.empty[s]);
         ++issued;
     }
@@ -243,7 +240,8 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_analysis_tc(const __nv_bfloat16 
                                                             int64_t ncol, const int *__restrict__ Ecol,
                                                             double *__restrict__ A, float2 *__restrict__ Adf,
                                                             int accumulate, int *__restrict__ Eout,
-                                                            const int *__restrict__ nzr, int *err) {
+                                                            const int *__restrict__ nzr,
+                                                            const int2 *__restrict__ live, int *err) {
     extern __shared__ __align__(1024) unsigned char smem[];
     const int z = blockIdx.z;
     const int m = z >> 1, par = z & 1;
@@ -257,18 +255,28 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_analysis_tc(const __nv_bfloat16 
     const int c = tid & (MTILE - 1), kh = (tid >> 7) & 1;
     const bool prod = tid < NPROD;
     const bool cok = prod && col0 + c < ncol;
-    // nzr: the ring pairs outside [nzr[0], nzr[1]] carry zero spectra, and the chunks holding only
-    // such rings are left out (at least one chunk stays, so the accumulators are written)
-    int kc0 = 0;
+    // Chunk range [lo, hi]: nzr - the ring pairs outside [nzr[0], nzr[1]] carry zero spectra; live -
+    // the chunks of this row tile whose lambda slices are not all zero.  Products with the other
+    // chunks are exactly zero.  An empty range adds nothing (accumulate: the CTA returns) or gives
+    // zero coefficients (no MMA; the epilogue writes zeros).
+    int lo = 0, hi = nchunks - 1;
     if (nzr) {
-        const int lo = nzr[0], hi = nzr[1];
-        if (hi >= lo) {
-            kc0 = lo / KC;
-            nchunks = min(nchunks, hi / KC + 1) - kc0;
+        const int a = nzr[0], b = nzr[1];
+        if (b >= a) {
+            lo = max(lo, a / KC);
+            hi = min(hi, b / KC);
         } else {
-            nchunks = 1;
+            hi = lo - 1;
         }
     }
+    if (live) {
+        const int2 lv = live[(int64_t)z * gridDim.y + blockIdx.y];
+        lo = max(lo, lv.x);
+        hi = min(hi, lv.y);
+    }
+    if (hi < lo && accumulate) return;
+    const int kc0 = hi < lo ? 0 : lo;
+    nchunks = hi < lo ? 0 : hi - lo + 1;
     const float2 *Fz = F + ((int64_t)(par * (lmax + 1) + m) * nrn + (int64_t)kc0 * KC) * ncol + col0 + c;
     const __nv_bfloat16 *Lz = lamtc + lamtc_off[z] + (int64_t)kc0 * 4 * pad16(rows_of(m, par, lmax)) * KC;
     rlim -= kc0 * KC;
@@ -281,7 +289,7 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_analysis_tc(const __nv_bfloat16 
 
     if (!prod) {
         if ((tid & 31) == 0) {
-            const int issued = lvl_mma_loop<true>(cs, tmem, nchunks, planeB, LS);
+            const int issued = lvl_mma_loop(cs, tmem, nchunks, planeB, LS);
             if (issued != nchunks) atomicExch(cs.bad, 1);
         }
     } else {
@@ -351,6 +359,10 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_analysis_tc(const __nv_bfloat16 
             tmem_ld8(tmem + lane_base + (uint32_t)(LS + i0), v1);
             tmem_ld8(tmem + lane_base + (uint32_t)(2 * LS + i0), v2);
             tmem_ld8(tmem + lane_base + (uint32_t)(3 * LS + i0), v3);
+            if (nchunks == 0) {           // no MMA wrote the accumulators: the sums are zero
+#pragma unroll
+                for (int i = 0; i < 8; ++i) v0[i] = v1[i] = v2[i] = v3[i] = 0.f;
+            }
             if (cc < ncol) {
                 auto off = [&](int i) {
                     const int l = m + par + 2 * (row0 + i0 + i);
@@ -409,7 +421,8 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_synthesis_tc(const __nv_bfloat16
                                                              float *__restrict__ G, const double *__restrict__ Acur,
                                                              const float2 *__restrict__ A0, double *__restrict__ Anew,
                                                              float2 *__restrict__ Adfnew, const int *__restrict__ Ein,
-                                                             int *__restrict__ Eout, int *err) {
+                                                             int *__restrict__ Eout, const int2 *__restrict__ live,
+                                                             int *err) {
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ float red[2][MTILE];
     const int z = blockIdx.z;
@@ -422,7 +435,15 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_synthesis_tc(const __nv_bfloat16
     const bool upd = Adfnew != nullptr;
     if (upd && r0 >= nrows) return;          // no output row of this block in the tile
     float *Gz = upd ? nullptr : G + ((int64_t)(par * (lmax + 1) + m) * nrn) * ncol;
-    if (nrows == 0) {      // no l for this (m, parity): the block is zero
+    // live: the row chunks [lv.x, lv.y] of this ring tile whose lambda slices are not all zero (the
+    // products with the others are exactly zero); none - the tile's G is zero
+    int k0 = 0, nK = (nrows + KC - 1) / KC;
+    if (live && nrows > 0) {
+        const int2 lv = live[(int64_t)z * ((nrn + NT - 1) / NT) + nt];      // the table's ring tiles
+        k0 = lv.x;
+        nK = lv.y >= lv.x ? lv.y - lv.x + 1 : 0;
+    }
+    if (nrows == 0 || nK == 0) {      // no l for this (m, parity), or no live chunk: the tile is zero
         for (int rr = warp; rr < NT; rr += NTH / 32) {
             const int r = r0 + rr;
             if (r >= nrn) break;
@@ -430,12 +451,11 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_synthesis_tc(const __nv_bfloat16
         }
         return;
     }
-    const int nK = (nrows + KC - 1) / KC;
     const int c = tid & (MTILE - 1), kh = (tid >> 7) & 1;
     const bool prod = tid < NPROD;
     const bool cok = prod && col0 + c < ncol;
     const uint32_t planeB = (uint32_t)NT * KC * 2;
-    const __nv_bfloat16 *Lz = lamts + lamts_off[z] + (int64_t)nt * nK * 4 * NT * KC;
+    const __nv_bfloat16 *Lz = lamts + lamts_off[z] + ((int64_t)nt * ((nrows + KC - 1) / KC) + k0) * 4 * NT * KC;
     LvlSmem cs = lvl_smem(smem);
     auto aval = [&](int li) -> float2 {
         if (!cok || li >= nrows) return make_float2(0.f, 0.f);
@@ -464,14 +484,14 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_synthesis_tc(const __nv_bfloat16
 
     if (!prod) {
         if (lane == 0) {
-            const int issued = lvl_mma_loop<false>(cs, tmem, nK, planeB, LS);
+            const int issued = lvl_mma_loop(cs, tmem, nK, planeB, LS);
             if (issued != nK) atomicExch(cs.bad, 1);
         }
     } else {
         float2 pre[2][8];
         auto loadA = [&](int kc, float2 (&buf)[8]) {
 #pragma unroll
-            for (int j = 0; j < 8; ++j) buf[j] = aval(kc * KC + 8 * kh + j);
+            for (int j = 0; j < 8; ++j) buf[j] = aval((k0 + kc) * KC + 8 * kh + j);
         };
         auto chunk = [&](int kc, float2 (&cur)[8]) -> bool {
             const int s = kc % NSTAGE;
@@ -596,8 +616,8 @@ __device__ __forceinline__ void slices4(double v, int E, __nv_bfloat16 (&o)[4]) 
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         const double a = rint(y);
-        y = (y - a) * 128.0;
-        o[k] = __double2bfloat16(ldexp(a, E - 7 - 7 * k));      // at most 8 significant bits: exact
+        y = (y - a) * 256.0;
+        o[k] = __double2bfloat16(ldexp(a, E - 7 - 8 * k));      // at most 8 significant bits: exact
     }
 }
 
@@ -731,7 +751,7 @@ void launch_leg_analysis_tc(const Plan &p, const float2 *F, int64_t ncol, double
     tc::k_leg_analysis_tc<<<grid, tc::NTH, tc::LEG_SMEM, st>>>((const __nv_bfloat16 *)p.d_lamtc, p.d_lamtc_off,
                                                               p.lmax, (int)p.nrn, (rlim + tc::KC - 1) / tc::KC, rlim,
                                                               F, ncol, Ecol, A, Adf, accumulate ? 1 : 0, Eout,
-                                                              nzr, p.d_err);
+                                                              nzr, p.d_lamtc_live, p.d_err);
     note_launch();
 }
 
@@ -763,6 +783,87 @@ int64_t tc_synth_table_offsets(const Plan &p, std::vector<int64_t> &off, int64_t
     return o;
 }
 
+namespace tc {
+// Live chunk ranges of the sliced tables.  A chunk whose slices are all zero
+// contributes exactly zero to every product, so the contractions leave it
+// out: per (block z, row tile of NMAX rows) the analysis table's ring chunks,
+// per (block z, ring tile) the synthesis table's row chunks.  Ranges [x, y]
+// (x > y: no live chunk), preset to {INT_MAX, -1}.
+__global__ void k_fill_range(int2 *r, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        r[i] = make_int2(0x7fffffff, -1);
+}
+
+// grid (z, ring chunk kc); element e of a plane lies at row (core >> 1) * 8 + ((e & 63) >> 3) with
+// core = e >> 6 (core-matrix layout, KC = 16 columns per row group)
+__global__ void k_live_analysis(const uint16_t *__restrict__ tab, const int64_t *__restrict__ off, int lmax,
+                                int nch, int ntile, int2 *__restrict__ live) {
+    __shared__ int any[64];
+    const int z = blockIdx.x, kc = blockIdx.y;
+    const int m = z >> 1, par = z & 1;
+    const int nrows = rows_of(m, par, lmax);
+    if (nrows == 0 || kc >= nch) return;
+    const int NP = pad16(nrows);
+    const uint16_t *base = tab + off[z] + (int64_t)kc * 4 * NP * KC;
+    if (threadIdx.x < 64) any[threadIdx.x] = 0;
+    __syncthreads();
+    for (int e = threadIdx.x; e < 4 * NP * KC; e += blockDim.x) {
+        if (base[e] & 0x7fff) {
+            const int pe = e % (NP * KC);
+            const int li = ((pe >> 6) >> 1) * 8 + ((pe & 63) >> 3);
+            any[min(li / NMAX, 63)] = 1;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < ntile && any[threadIdx.x]) {
+        atomicMin(&live[(int64_t)z * ntile + threadIdx.x].x, kc);
+        atomicMax(&live[(int64_t)z * ntile + threadIdx.x].y, kc);
+    }
+}
+
+// grid (z, ring tile nt x row chunk kc)
+__global__ void k_live_synthesis(const uint16_t *__restrict__ tab, const int64_t *__restrict__ off, int lmax,
+                                 int NT, int ntiles, int nkmax, int2 *__restrict__ live) {
+    const int z = blockIdx.x, nt = blockIdx.y / nkmax, kc = blockIdx.y % nkmax;
+    const int m = z >> 1, par = z & 1;
+    const int nrows = rows_of(m, par, lmax);
+    const int nK = (nrows + KC - 1) / KC;
+    if (nrows == 0 || kc >= nK) return;
+    const uint16_t *base = tab + off[z] + ((int64_t)nt * nK + kc) * 4 * NT * KC;
+    int any = 0;
+    for (int e = threadIdx.x; e < 4 * NT * KC; e += blockDim.x) any |= base[e] & 0x7fff;
+    if (__syncthreads_or(any) && threadIdx.x == 0) {
+        atomicMin(&live[(int64_t)z * ntiles + nt].x, kc);
+        atomicMax(&live[(int64_t)z * ntiles + nt].y, kc);
+    }
+}
+}  // namespace tc
+
+int build_live_ranges(Plan &p, cudaStream_t st) {
+    const int nz = 2 * (p.lmax + 1);
+    const int ntile_a = (tc_np_max(p) + tc::NMAX - 1) / tc::NMAX;
+    const int NT = tc_synth_nt(p);
+    const int ntiles_s = (int)((p.nrn + NT - 1) / NT);
+    const int nkmax = (int)((p.lmax / 2 + 1 + tc::KC - 1) / tc::KC);
+    const int64_t na = (int64_t)nz * ntile_a, ns = (int64_t)nz * ntiles_s;
+    if (cudaMalloc(&p.d_lamtc_live, (size_t)(na + ns) * sizeof(int2)) != cudaSuccess) {
+        cudaGetLastError();
+        p.d_lamtc_live = nullptr;
+        return fail(SFB_ENOMEM, "device allocation failed (live chunk ranges)");
+    }
+    p.device_bytes += (na + ns) * (int64_t)sizeof(int2);
+    p.d_lamts_live = p.d_lamtc_live + na;
+    tc::k_fill_range<<<(unsigned)((na + ns + 255) / 256), 256, 0, st>>>(p.d_lamtc_live, na + ns);
+    note_launch();
+    tc::k_live_analysis<<<dim3((unsigned)nz, (unsigned)tc_chunks(p)), 256, 0, st>>>(
+        (const uint16_t *)p.d_lamtc, p.d_lamtc_off, p.lmax, tc_chunks(p), ntile_a, p.d_lamtc_live);
+    note_launch();
+    tc::k_live_synthesis<<<dim3((unsigned)nz, (unsigned)(ntiles_s * nkmax)), 256, 0, st>>>(
+        (const uint16_t *)p.d_lamts, p.d_lamts_off, p.lmax, NT, ntiles_s, nkmax, p.d_lamts_live);
+    note_launch();
+    return cudaGetLastError() == cudaSuccess ? SFB_OK : fail(SFB_ECUDA, "live chunk ranges failed");
+}
+
 void launch_build_lamts(const Plan &p, const int *Es, cudaStream_t st) {
     dim3 grid(64, (unsigned)(2 * (p.lmax + 1)));
     tc::k_build_lamts<<<grid, 256, 0, st>>>(p.d_lam, p.d_lam_off, p.lmax, (int)p.nrn, tc_synth_nt(p), Es,
@@ -780,7 +881,7 @@ void launch_leg_synthesis_tc(const Plan &p, const float2 *Adf, int64_t ncol, flo
               (unsigned)(2 * (p.lmax + 1)));
     tc::k_leg_synthesis_tc<<<grid, tc::NTH, tc::LEG_SMEM, st>>>((const __nv_bfloat16 *)p.d_lamts, p.d_lamts_off,
                                                                p.lmax, (int)p.nrn, NT, Adf, ncol, G, nullptr, nullptr,
-                                                               nullptr, nullptr, Ein, nullptr, p.d_err);
+                                                               nullptr, nullptr, Ein, nullptr, p.d_lamts_live, p.d_err);
     note_launch();
 }
 
@@ -808,7 +909,7 @@ void launch_gram_update(const Plan &p, const double *A, const float2 *Adf, const
               (unsigned)(2 * (p.lmax + 1)));
     tc::k_leg_synthesis_tc<<<grid, tc::NTH, tc::LEG_SMEM, st>>>((const __nv_bfloat16 *)p.d_gramts, p.d_gramts_off,
                                                                p.lmax, p.gram_rows, NT, Adf, ncol, nullptr, A, A0,
-                                                               Anew, Adfnew, Ein, Eout, p.d_err);
+                                                               Anew, Adfnew, Ein, Eout, nullptr, p.d_err);
     note_launch();
 }
 

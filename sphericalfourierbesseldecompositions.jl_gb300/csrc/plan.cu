@@ -413,8 +413,9 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, b
             {
                 Stage s(h, stage(SFB_STAGE_LEG_SYNTHESIS), st);
                 if (p.ral > 0) launch_leg_synthesis_tc(p, Db[cur], ncol, (float *)gbuf.ptr, st, p.ral, Eb[cur]);
-                launch_gram_update(p, Ab[cur], Db[cur], a0, ncol, Ab[nxt], Db[nxt], st, Eb[cur],
-                                   p.ral > 0 ? nullptr : Eb[nxt]);
+                // the update records the column exponents of its output; the aliased analysis raises
+                // them where it adds (its CTAs without live chunks leave the update's values)
+                launch_gram_update(p, Ab[cur], Db[cur], a0, ncol, Ab[nxt], Db[nxt], st, Eb[cur], Eb[nxt]);
             }
             if (p.ral > 0) {
                 {
@@ -953,6 +954,7 @@ int sfb_plan_create(const sfb_plan_desc *d, sfb_plan **out) {
             if ((st = upload(p, &p.d_lamts_off, soff.data(), soff.size())) != SFB_OK) break;
             if ((st = upload<uint16_t>(p, (uint16_t **)&p.d_lamts, nullptr, (size_t)ssz)) != SFB_OK) break;
             launch_build_lamts(p, Es, h->stream);
+            if ((st = build_live_ranges(p, h->stream)) != SFB_OK) break;
         }
         {
             // rings that alias (nph <= 2 lmax) form a prefix: the polar rings grow to the equatorial length
@@ -1006,7 +1008,7 @@ void sfb_plan_destroy(sfb_plan *h) {
     cudaSetDevice(p.device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     void *ptrs[] = {p.d_rings, p.d_twtab, p.d_twoff, p.d_phase, p.d_wphase, p.d_twtab32, p.d_wphase32, p.d_dtw,
-                    p.d_dtw_off, p.d_dtimg, p.d_dtimg_off, p.d_gramts, p.d_gramts_off, p.d_gram64, p.d_gram_off, p.d_cls_rings, p.d_cls_off, p.d_lam, p.d_lam32, p.d_lamtc, p.d_lamtc_off, p.d_lamts, p.d_lamts_off, p.d_lam_off, p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp,
+                    p.d_dtw_off, p.d_dtimg, p.d_dtimg_off, p.d_gramts, p.d_gramts_off, p.d_gram64, p.d_gram_off, p.d_cls_rings, p.d_cls_off, p.d_lam, p.d_lam32, p.d_lamtc, p.d_lamtc_off, p.d_lamts, p.d_lamts_off, p.d_lamtc_live, p.d_lam_off, p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp,
                     p.d_pair_l, p.d_pair_n, p.d_out_pair, p.d_out_lm, p.d_coef, p.d_coefT, p.d_proj_tiles, p.d_err,
                     p.maps.ptr, p.fbuf.ptr, p.gbuf.ptr, p.rbuf.ptr, p.alm.ptr, p.scratch.ptr, p.scratch2.ptr, p.dep.ptr, p.maps32.ptr,
                     p.ref.ptr, p.rf.ptr, p.rg.ptr, p.rr.ptr, p.ralm.ptr, p.almdf2.ptr, p.adf0.ptr, p.ecoef.ptr, p.erow.ptr, p.almdf.ptr, p.nzr64.ptr, h->d_pair_index, h->d_noff};

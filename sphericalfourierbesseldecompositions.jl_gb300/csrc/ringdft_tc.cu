@@ -15,17 +15,17 @@
 // Oishi and Rump, "Error-free transformations of matrix multiplication by
 // using fast routines of matrix multiplication", Numer. Algorithms 59, 2012):
 // every value of a map row is written on the row's common scale 2^E (max|x| <
-// 2^E) as x = sum_s a_s 2^(E - 7 - 7 s), s = 0..3, with integers |a_0| <= 128,
-// |a_s| <= 64; every table value on the table's common scale 2^EB (|T| <= 1 <
-// 2^EB = 2) as T = sum_s b_s 2^(EB - 7 - 7 s), |b_0| <= 128, |b_s| <= 64.
-// Each slice is a BF16 value with at most 8 significant bits.  The products
-// of level v = s_a + s_b (v = 0..3) are integers of one unit U 2^(-7 v) per
-// row and go to their own FP32 TMEM accumulator; the level-0 and level-1
-// sums stay within 2^24 units for rings of up to 1024 pixels, so they are
-// exact whatever order or rounding the tensor cores use (levels 2 and 3 are
-// 2^-14 and 2^-21 of the leading one: their rounding does not show).  The
-// three level-4 products (near 2^-28 of the leading ones) go into the level-3
-// accumulator; levels v >= 5 (2^-35) are dropped.  The epilogue adds the levels and the north/south rows
+// 2^E) as x = sum_s a_s 2^(E - 7 - 8 s), s = 0..3, with integers |a_s| <= 128;
+// every table value on the table's common scale 2^EB (|T| <= 1 < 2^EB = 2) as
+// T = sum_s b_s 2^(EB - 7 - 8 s), |b_0| <= 64, |b_s| <= 128.  Each slice is a
+// BF16 value with at most 8 significant bits, and each operand is represented
+// to 2^-32 of its scale.  The products of level v = s_a + s_b (v = 0..3; ten
+// products) are integers of one unit U 2^(-8 v) per row and go to their own
+// FP32 TMEM accumulator; the level-0 sum stays below 2^23 units for rings of
+// up to 1024 pixels, so it is exact whatever order or rounding the tensor
+// cores use (the level-v sums, v >= 1, carry 2^(-8 v) of the leading one, so
+// a rounding there is below 2^-32 of it).  Levels v >= 4 (below 2^-32 of the
+// leading products) are dropped.  The epilogue adds the levels and the north/south rows
 // with one significant FP32 rounding (TwoSum on the leading level).  The
 // table is unweighted so that cos 0 = 1 is exact in one slice: for m = 0
 // every pixel shares one table value, and a value far below its ring's
@@ -104,7 +104,7 @@ __device__ __forceinline__ void st_shared_v4(unsigned char *p, const uint32_t (&
 
 // Per (hemisphere, ring, map): E with max |x| < 2^E over the ring, raised by
 // ceil(log2 n) - 10 for rings longer than 1024 pixels so that the leading
-// products still sum within 2^24 units; ZERO_ROW_E for a row of zeros (a ring
+// products still sum below 2^23 units; ZERO_ROW_E for a row of zeros (a ring
 // outside the survey), whose tiles the DFT skips.  A row holding a
 // non-finite value keeps an ordinary exponent, so the value reaches the
 // spectra and the transform's finiteness check.  erow layout [2][nrn][nmaps];
@@ -287,12 +287,11 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float2 *__restric
                 fence_after();
                 const uint32_t base = smem_u32(smem + st * STAGE);
                 const uint32_t sbo = (KC / 8) * 128;
-                // the thirteen level products as nine MMAs (tc_common.cuh); level v at TMEM columns
-                // 128 v, level 4 with level 3
+                // the ten level products as six MMAs (tc_common.cuh); level v at TMEM columns 128 v
 #pragma unroll
                 for (int ks = 0; ks < KC / 16; ++ks) {
 #pragma unroll
-                    for (int q = 0; q < NMERGED4; ++q) {
+                    for (int q = 0; q < NMERGED; ++q) {
                         const bool first = kc == 0 && ks == 0 && mg_first(q);
                         mma_bf16(tmem + (uint32_t)(NCOL * mg_lvl(q)),
                                  smem_desc(base + mg_a(q) * PLANE + ks * 256, 128, sbo),
@@ -591,8 +590,8 @@ uint2 dft_slices(double v, int EB) {
     uint16_t s[4];
     for (int k = 0; k < 4; ++k) {
         const double a = std::nearbyint(y);
-        y = (y - a) * 128.0;
-        s[k] = bf16_of_exact((float)std::ldexp(a, EB - 7 - 7 * k));
+        y = (y - a) * 256.0;
+        s[k] = bf16_of_exact((float)std::ldexp(a, EB - 7 - 8 * k));
     }
     return make_uint2((uint32_t)s[0] | ((uint32_t)s[1] << 16), (uint32_t)s[2] | ((uint32_t)s[3] << 16));
 }

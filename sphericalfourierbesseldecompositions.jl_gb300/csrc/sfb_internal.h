@@ -121,6 +121,8 @@ struct Plan {
     int64_t *d_lamtc_off = nullptr; // [2*(lmax+1)+1] block offsets (bf16 elements)
     void *d_lamts = nullptr;        // split-BF16 table in tensor-core operand layout (synthesis)
     int64_t *d_lamts_off = nullptr;
+    int2 *d_lamtc_live = nullptr;   // live chunk ranges of the analysis table [z][row tile] (one allocation
+    int2 *d_lamts_live = nullptr;   // with the synthesis table's [z][ring tile]); see build_live_ranges
     int64_t *d_lam_off = nullptr;   // [2*(lmax+1)] offset of block (m, parity)
     int64_t lam_elems = 0;
     int64_t *d_spl_off = nullptr;
@@ -262,6 +264,7 @@ void launch_leg_analysis_tc(const Plan &p, const float2 *F, int64_t ncol, double
                             int *Eout = nullptr, const int *nzr = nullptr);
 int64_t tc_synth_table_offsets(const Plan &p, std::vector<int64_t> &off, int64_t nrn = -1);
 void launch_build_lamts(const Plan &p, const int *Es, cudaStream_t st);
+int build_live_ranges(Plan &p, cudaStream_t st);
 // rlim: ring tiles covering the first rlim rings only (-1: all)
 // Ein (optional): the column exponents of Adf per block z, as the analysis wrote them
 void launch_leg_synthesis_tc(const Plan &p, const float2 *Adf, int64_t ncol, float *G, cudaStream_t st,

@@ -108,23 +108,25 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
 }
 
 // ---- error-free slicing (block floating point, Ozaki et al.) -----------------
-// A value with |x| < 2^E is written as four slices s_k, each a multiple of
-// 2^(E - 6 - 7k) with at most 7 significant bits: s_k = RN(r_k) on that grid,
-// r_0 = x, r_{k+1} = r_k - s_k, formed as (r + C_k) - C_k with
-// C_k = 1.5 * 2^(E + 17 - 7k).  Every step is exact in FP32.
+// A value with |x| < 2^E is written as four slices s_k, s_k = RN(r_k) on the
+// grid 2^(E - 6 - 8k), r_0 = x, r_{k+1} = r_k - s_k, formed as (r + C_k) - C_k
+// with C_k = 1.5 * 2^(E + 17 - 8k).  Every step is exact in FP32.  |s_0| <= 64
+// grid units and, since |r_k| is at most half a unit of the grid before,
+// |s_k| <= 128 units for k >= 1: at most 8 significant bits, which BF16 holds
+// exactly (it holds the integers up to 256).
 
 __device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + e) << 23); }   // -126 <= e <= 127
 
 __device__ __forceinline__ void slice_consts(int E, float (&C)[4]) {
 #pragma unroll
-    for (int k = 0; k < 4; ++k) C[k] = 1.5f * pow2f(E + 17 - 7 * k);
+    for (int k = 0; k < 4; ++k) C[k] = 1.5f * pow2f(E + 17 - 8 * k);
 }
 
-// The same with an 8-bit leading slice: s_k a multiple of 2^(E - 7 - 7k),
-// |s_0| <= 128 (BF16 holds the integers up to 256 exactly), |s_k| <= 64 after.
+// The same with an 8-bit leading slice: grid 2^(E - 7 - 8k), |s_k| <= 128
+// units for every k.
 __device__ __forceinline__ void slice_consts8(int E, float (&C)[4]) {
 #pragma unroll
-    for (int k = 0; k < 4; ++k) C[k] = 1.5f * pow2f(E + 16 - 7 * k);
+    for (int k = 0; k < 4; ++k) C[k] = 1.5f * pow2f(E + 16 - 8 * k);
 }
 
 __device__ __forceinline__ uint32_t bf16x2(float lo, float hi) {
@@ -147,7 +149,7 @@ __device__ __forceinline__ void slice_pair(float x0, float x1, const float (&C)[
 }
 
 // Double-float source (x = hi + lo, |lo| <= ulp(hi)/2): the first slice comes
-// from hi, the remainder (hi - s_0) + lo rounds below the last slice unit.
+// from hi; the remainder (hi - s_0) + lo rounds at the last slice's unit.
 __device__ __forceinline__ void slice_pair_df(float h0, float l0, float h1, float l1, const float (&C)[4],
                                               uint32_t (&w)[4]) {
     const float a0 = __fsub_rn(__fadd_rn(h0, C[0]), C[0]);
@@ -179,21 +181,13 @@ __device__ __forceinline__ int scale_exp(float mx) {
 // N):  q0 A0 x [B0|B1] -> levels 0, 1;  q1 A0 x [B2|B3] -> 2, 3;
 // q2 A1 x [B0|B1] -> 1, 2;  q3 A1 x B2 -> 3;  q4 A2 x [B0|B1] -> 2, 3;
 // q5 A3 x B0 -> 3.  q0 and q1 write every level first (no accumulate on the
-// first K step).
-//
-// With the level-4 products (NMERGED4): q6 A1 x B3, q7 A2 x B2, q8 A3 x B1,
-// each of N into the level-3 accumulator.  Level 3 carries 2^-21 of the
-// leading level, so its FP32 rounding (it is no longer an integer sum below
-// 2^24 units) stays near 2^-45 of the result.  The three products (each near
-// 2^-28 of the leading ones) are then no longer truncated; what remains is
-// each operand's own four-slice representation and the level-5 products
-// (2^-35).
+// first K step).  With 8-bit slice steps the dropped level-4 products are
+// below 2^-32 of the leading ones.
 constexpr int NMERGED = 6;
-constexpr int NMERGED4 = 9;
-__device__ __forceinline__ int mg_a(int q) { return q < 2 ? 0 : q < 4 ? 1 : q < 5 ? 2 : q < 6 ? 3 : q - 5; }
-__device__ __forceinline__ int mg_b(int q) { return (q == 1 || q == 3) ? 2 : q < 6 ? 0 : 9 - q; }
+__device__ __forceinline__ int mg_a(int q) { return q < 2 ? 0 : q < 4 ? 1 : q < 5 ? 2 : 3; }
+__device__ __forceinline__ int mg_b(int q) { return (q == 1 || q == 3) ? 2 : 0; }
 __device__ __forceinline__ int mg_lvl(int q) { return q == 0 ? 0 : q == 2 ? 1 : (q == 1 || q == 4) ? 2 : 3; }
-__device__ __forceinline__ bool mg_two(int q) { return q != 3 && q < 5; }
+__device__ __forceinline__ bool mg_two(int q) { return q != 3 && q != 5; }
 __device__ __forceinline__ bool mg_first(int q) { return q < 2; }
 
 }  // namespace tc
