@@ -208,7 +208,8 @@ __device__ __forceinline__ bool lvl_stage_free(const LvlSmem &cs, int kc) {
 // stay within 2^24 units.
 // (nzr: F is zero outside the ring pairs [nzr[0], nzr[1]], which are the only ones read)
 __global__ void __launch_bounds__(256) k_colmax(const float2 *__restrict__ F, int64_t ncol, int lmax, int nrn,
-                                                int *__restrict__ Ecol, const int *__restrict__ nzr) {
+                                                int *__restrict__ Ecol, const int *__restrict__ nzr,
+                                                const int2 *__restrict__ live, int ntile) {
     const int z = blockIdx.y;
     const int m = z >> 1, par = z & 1;
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -219,6 +220,16 @@ __global__ void __launch_bounds__(256) k_colmax(const float2 *__restrict__ F, in
     if (nzr) {
         r = nzr[0];
         r1 = min(nrn, nzr[1] + 1);
+    }
+    if (live) {          // only the rings of the analysis's live chunks are read (and written)
+        int lo = 0x7fffffff, hi = -1;
+        for (int t = 0; t < ntile; ++t) {
+            const int2 lv = live[(int64_t)z * ntile + t];
+            lo = min(lo, lv.x);
+            hi = max(hi, lv.y);
+        }
+        r = max(r, lo * KC);
+        r1 = min(r1, (hi + 1) * KC);
     }
     for (; r + 3 < r1; r += 4) {
         m0 = fmaxf(m0, fabsf(Fz[(int64_t)r * ncol].x));
@@ -742,7 +753,8 @@ void launch_leg_analysis_tc(const Plan &p, const float2 *F, int64_t ncol, double
     if (rlim < 0 || rlim > p.nrn) rlim = (int)p.nrn;
     if (!scales_ready) {
         dim3 grid((unsigned)((ncol + 255) / 256), (unsigned)(2 * (p.lmax + 1)));
-        tc::k_colmax<<<grid, 256, 0, st>>>(F, ncol, p.lmax, (int)p.nrn, Ecol, nzr);
+        tc::k_colmax<<<grid, 256, 0, st>>>(F, ncol, p.lmax, (int)p.nrn, Ecol, nzr, p.d_lamtc_live,
+                                           (tc_np_max(p) + tc::NMAX - 1) / tc::NMAX);
         note_launch();
     }
     set_smem(tc::k_leg_analysis_tc, tc::LEG_SMEM);
@@ -837,6 +849,27 @@ __global__ void k_live_synthesis(const uint16_t *__restrict__ tab, const int64_t
         atomicMax(&live[(int64_t)z * ntiles + nt].y, kc);
     }
 }
+
+// Ring DFT spectra that no analysis chunk reads: ring pair r and column block u
+// (m in [64 u, 64 u + 63]) are dead when, for every block z of those m and
+// every row tile, the chunk of r lies outside the tile's live range.
+__global__ void k_dft_dead(const int2 *__restrict__ live, int lmax, int nrn, int ntile, int ntn,
+                           unsigned char *__restrict__ dead) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x, u = blockIdx.y;
+    if (r >= nrn) return;
+    const int kc = r / KC;
+    bool d = true;
+    for (int m = 64 * u; m <= min(lmax, 64 * u + 63) && d; ++m)
+        for (int par = 0; par < 2 && d; ++par) {
+            const int z = 2 * m + par;
+            if (rows_of(m, par, lmax) == 0) continue;
+            for (int t = 0; t < ntile; ++t) {
+                const int2 lv = live[(int64_t)z * ntile + t];
+                if (kc >= lv.x && kc <= lv.y) d = false;
+            }
+        }
+    dead[(int64_t)r * ntn + u] = d ? 1 : 0;
+}
 }  // namespace tc
 
 int build_live_ranges(Plan &p, cudaStream_t st) {
@@ -860,6 +893,16 @@ int build_live_ranges(Plan &p, cudaStream_t st) {
     note_launch();
     tc::k_live_synthesis<<<dim3((unsigned)nz, (unsigned)(ntiles_s * nkmax)), 256, 0, st>>>(
         (const uint16_t *)p.d_lamts, p.d_lamts_off, p.lmax, NT, ntiles_s, nkmax, p.d_lamts_live);
+    note_launch();
+    const int ntn = (p.lmax + 1 + 63) / 64;
+    if (cudaMalloc(&p.d_dft_dead, (size_t)p.nrn * ntn) != cudaSuccess) {
+        cudaGetLastError();
+        p.d_dft_dead = nullptr;
+        return fail(SFB_ENOMEM, "device allocation failed (ring DFT dead flags)");
+    }
+    p.device_bytes += p.nrn * ntn;
+    tc::k_dft_dead<<<dim3((unsigned)((p.nrn + 127) / 128), (unsigned)ntn), 128, 0, st>>>(
+        p.d_lamtc_live, p.lmax, (int)p.nrn, ntile_a, ntn, p.d_dft_dead);
     note_launch();
     return cudaGetLastError() == cudaSuccess ? SFB_OK : fail(SFB_ECUDA, "live chunk ranges failed");
 }

@@ -358,8 +358,11 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, b
         SFB_TRY(grow(p, p.almdf, (size_t)p.lmsize * ncol));
         nzr = reinterpret_cast<int *>(p.erow.ptr) + 2 * std::max<int64_t>(p.nrn * nm, (p.lmax + 1) * ncol);
         Stage s(h, stage(SFB_STAGE_RING_FFT), st);
+        // the Gram refinement and niter = 0 read the spectra only in the first analysis pass (over the
+        // span with data and the live chunks); the full refinement passes fold them over every ring
+        const bool skip_unread = (nm > 4 && p.d_gramts && p.niter > 0) || p.niter == 0;
         launch_ring_analysis_tc(p, reinterpret_cast<const float2 *>(maps), nm, reinterpret_cast<float2 *>(fbuf.ptr),
-                                reinterpret_cast<int *>(p.erow.ptr), nzr, st, ring_live, nlive);
+                                reinterpret_cast<int *>(p.erow.ptr), nzr, st, ring_live, nlive, skip_unread);
     } else {
         // many columns: the FFT records the span of ring pairs with data, over which the
         // first analysis pass sums (the spectra are zero elsewhere)
@@ -1008,7 +1011,7 @@ void sfb_plan_destroy(sfb_plan *h) {
     cudaSetDevice(p.device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     void *ptrs[] = {p.d_rings, p.d_twtab, p.d_twoff, p.d_phase, p.d_wphase, p.d_twtab32, p.d_wphase32, p.d_dtw,
-                    p.d_dtw_off, p.d_dtimg, p.d_dtimg_off, p.d_gramts, p.d_gramts_off, p.d_gram64, p.d_gram_off, p.d_cls_rings, p.d_cls_off, p.d_lam, p.d_lam32, p.d_lamtc, p.d_lamtc_off, p.d_lamts, p.d_lamts_off, p.d_lamtc_live, p.d_lam_off, p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp,
+                    p.d_dtw_off, p.d_dtimg, p.d_dtimg_off, p.d_gramts, p.d_gramts_off, p.d_gram64, p.d_gram_off, p.d_cls_rings, p.d_cls_off, p.d_lam, p.d_lam32, p.d_lamtc, p.d_lamtc_off, p.d_lamts, p.d_lamts_off, p.d_lamtc_live, p.d_dft_dead, p.d_lam_off, p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp,
                     p.d_pair_l, p.d_pair_n, p.d_out_pair, p.d_out_lm, p.d_coef, p.d_coefT, p.d_proj_tiles, p.d_err,
                     p.maps.ptr, p.fbuf.ptr, p.gbuf.ptr, p.rbuf.ptr, p.alm.ptr, p.scratch.ptr, p.scratch2.ptr, p.dep.ptr, p.maps32.ptr,
                     p.ref.ptr, p.rf.ptr, p.rg.ptr, p.rr.ptr, p.ralm.ptr, p.almdf2.ptr, p.adf0.ptr, p.ecoef.ptr, p.erow.ptr, p.almdf.ptr, p.nzr64.ptr, h->d_pair_index, h->d_noff};

@@ -165,7 +165,8 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float2 *__restric
                                                          const int64_t *__restrict__ dtw_off,
                                                          const unsigned char *__restrict__ img,
                                                          const int64_t *__restrict__ img_off, float2 *__restrict__ F,
-                                                         int64_t ldF, float2 wdf, int *err) {
+                                                         int64_t ldF, float2 wdf, const unsigned char *dead,
+                                                         int ntn, const int *span, int *err) {
     extern __shared__ __align__(1024) unsigned char smem[];
     // grid (column blocks u, row tiles, classes): the column blocks of one row tile are launched
     // together and read its map rows through L2 once
@@ -177,6 +178,16 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float2 *__restric
     if (pair0 >= npairs) return;
     const int u = blockIdx.x;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // dead: the spectra of ring r and column block u that no analysis chunk reads (lambda is zero in
+    // every slice there for all m of the block); a tile pair whose rings are all dead is not computed
+    if (dead) {
+        bool need = false;
+        if (tid < 2 * NPAIR) {
+            const int64_t qq = (int64_t)(ty & ~1) * NPAIR + tid;
+            if (qq < npairs) need = !dead[(int64_t)cls_rings[rb + (int)(qq / nmaps)] * ntn + u];
+        }
+        if (!__syncthreads_or(need)) return;
+    }
     // north-only tiles: where the south rows of this tile and of its partner tile ty ^ 1 are all zero
     // (southern rings outside the survey), the even tile takes the north rows of both, 128 pairs, with
     // F+ = F- = F_N, and the odd one has nothing left to do
@@ -239,6 +250,9 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float2 *__restric
             const int64_t qo = pair0 + pr;
             if (mm > lmax || qo >= npairs) continue;
             const int oring = cls_rings[rb + (int)(qo / nmaps)];
+            // unread spectra (outside the span of ring pairs with data, or dead) are not written
+            if (span && (oring < span[0] || oring > span[1])) continue;
+            if (dead && dead[(int64_t)oring * ntn + u]) continue;
             *reinterpret_cast<float4 *>(F + ((int64_t)(sg * L1 + mm) * nrn + oring) * ldF + 2 * (qo % nmaps)) =
                 make_float4(0.f, 0.f, 0.f, 0.f);
         }
@@ -578,7 +592,7 @@ void launch_build_dft_image(const Plan &p, int max_nch, cudaStream_t st) {
 }
 
 // Host-side slicing of one table value v (|v| < 2^EB) into four BF16 slices
-// b_s 2^(EB - 7 - 7 s), packed as uint2 {s0 | s1 << 16, s2 | s3 << 16}.
+// b_s 2^(EB - 7 - 8 s), packed as uint2 {s0 | s1 << 16, s2 | s3 << 16}.
 static uint16_t bf16_of_exact(float f) {
     uint32_t u;
     std::memcpy(&u, &f, 4);
@@ -597,7 +611,7 @@ uint2 dft_slices(double v, int EB) {
 }
 
 void launch_ring_analysis_tc(const Plan &p, const float2 *maps, int64_t nmaps, float2 *F, int *erow, int *nzr,
-                             cudaStream_t st, const int *ring_live, int64_t nlive) {
+                             cudaStream_t st, const int *ring_live, int64_t nlive, bool skip_unread) {
     {
         // nzr[0] = 0x7f7f7f7f (above any ring index), nzr[1] = -1
         cudaMemsetAsync(nzr, 0x7f, sizeof(int), st);
@@ -612,16 +626,20 @@ void launch_ring_analysis_tc(const Plan &p, const float2 *maps, int64_t nmaps, f
     const unsigned ntn = (unsigned)((p.lmax + 1 + 63) / 64);
     const double wq = 4.0 * M_PI / (double)p.npix;
     const float2 wdf = make_float2((float)wq, (float)(wq - (double)(float)wq));
+    // skip_unread: the spectra are read only by the first analysis pass, over the span of ring pairs
+    // with data and the live chunks, so the others need not be computed or written
+    const unsigned char *dead = skip_unread ? p.d_dft_dead : nullptr;
+    const int *span = skip_unread ? nzr : nullptr;
     // imaged classes read B from the image, the others gather it from the ring table
     auto launch = [&](dim3 grid, int c0, bool img) {
         if (img)
             dft::k_ring_dft_tc<true><<<grid, dft::NTHR, dft::SMEM, st>>>(
                 maps, p.npix, nmaps, p.d_rings, (int)p.nrn, p.lmax, p.d_cls_rings, p.d_cls_off + c0, erow, p.d_dtw,
-                p.d_dtw_off, p.d_dtimg, p.d_dtimg_off + c0, F, 2 * nmaps, wdf, p.d_err);
+                p.d_dtw_off, p.d_dtimg, p.d_dtimg_off + c0, F, 2 * nmaps, wdf, dead, (int)ntn, span, p.d_err);
         else
             dft::k_ring_dft_tc<false><<<grid, dft::NTHR, dft::SMEM, st>>>(
                 maps, p.npix, nmaps, p.d_rings, (int)p.nrn, p.lmax, p.d_cls_rings, p.d_cls_off + c0, erow, p.d_dtw,
-                p.d_dtw_off, nullptr, nullptr, F, 2 * nmaps, wdf, p.d_err);
+                p.d_dtw_off, nullptr, nullptr, F, 2 * nmaps, wdf, dead, (int)ntn, span, p.d_err);
         note_launch();
     };
     const unsigned mtiles = (unsigned)((nmaps + dft::NPAIR - 1) / dft::NPAIR);

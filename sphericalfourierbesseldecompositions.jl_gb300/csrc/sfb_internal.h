@@ -123,6 +123,7 @@ struct Plan {
     int64_t *d_lamts_off = nullptr;
     int2 *d_lamtc_live = nullptr;   // live chunk ranges of the analysis table [z][row tile] (one allocation
     int2 *d_lamts_live = nullptr;   // with the synthesis table's [z][ring tile]); see build_live_ranges
+    unsigned char *d_dft_dead = nullptr;   // [ring pair][64-m block]: spectra no analysis chunk reads
     int64_t *d_lam_off = nullptr;   // [2*(lmax+1)] offset of block (m, parity)
     int64_t lam_elems = 0;
     int64_t *d_spl_off = nullptr;
@@ -246,7 +247,8 @@ void launch_to_df(const double *in, int64_t n, float2 *out, cudaStream_t st);
 // nzr[0..1] receives the first and last ring pair holding a non-zero map row.
 // ring_live (optional): rings whose entry is 0 hold zeros in maps [0, nlive) and are not read.
 void launch_ring_analysis_tc(const Plan &p, const float2 *maps, int64_t nmaps, float2 *F, int *erow, int *nzr,
-                             cudaStream_t st, const int *ring_live = nullptr, int64_t nlive = 0);
+                             cudaStream_t st, const int *ring_live = nullptr, int64_t nlive = 0,
+                             bool skip_unread = false);
 uint2 dft_slices(double v, int EB);
 int64_t dft_image_offsets(const Plan &p, const std::vector<int32_t> &crings, const std::vector<int32_t> &coff,
                           bool with_polar, std::vector<int64_t> &off, int &max_nch);
