@@ -73,21 +73,24 @@ void launch_ang2pix(int64_t nside, const double *theta, const double *phi, int64
 // out[c][r] = in[r][c]; in is rows x cols row-major.
 __global__ void k_transpose(const double *in, int64_t rows, int64_t cols, double *out) {
     __shared__ double tile[32][33];
-    const int64_t c0 = (int64_t)blockIdx.x * 32, r0 = (int64_t)blockIdx.y * 32;
-    for (int j = threadIdx.y; j < 32; j += 8) {
-        const int64_t r = r0 + j, c = c0 + threadIdx.x;
-        if (r < rows && c < cols) tile[j][threadIdx.x] = in[r * cols + c];
-    }
-    __syncthreads();
-    for (int j = threadIdx.y; j < 32; j += 8) {
-        const int64_t c = c0 + j, r = r0 + threadIdx.x;
-        if (r < rows && c < cols) out[c * rows + r] = tile[threadIdx.x][j];
+    const int64_t c0 = (int64_t)blockIdx.x * 32;
+    for (int64_t r0 = (int64_t)blockIdx.y * 32; r0 < rows; r0 += (int64_t)gridDim.y * 32) {   // grid y <= 65535
+        for (int j = threadIdx.y; j < 32; j += 8) {
+            const int64_t r = r0 + j, c = c0 + threadIdx.x;
+            if (r < rows && c < cols) tile[j][threadIdx.x] = in[r * cols + c];
+        }
+        __syncthreads();
+        for (int j = threadIdx.y; j < 32; j += 8) {
+            const int64_t c = c0 + j, r = r0 + threadIdx.x;
+            if (r < rows && c < cols) out[c * rows + r] = tile[threadIdx.x][j];
+        }
+        __syncthreads();
     }
 }
 
 void launch_transpose(const double *in, int64_t rows, int64_t cols, double *out, cudaStream_t st) {
     if (rows <= 0 || cols <= 0) return;
-    dim3 grid((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32));
+    dim3 grid((unsigned)((cols + 31) / 32), (unsigned)std::min<int64_t>((rows + 31) / 32, 65535));
     k_transpose<<<grid, dim3(32, 8), 0, st>>>(in, rows, cols, out);
     note_launch();
 }
@@ -101,15 +104,19 @@ __device__ __forceinline__ TO convert_elem(TI v, TO *) { return (TO)v; }
 template <typename TI, typename TO>
 __global__ void k_transpose_ld(const TI *in, int64_t ldi, int64_t rows, int64_t cols, TO *out, int64_t ldo) {
     __shared__ TI tile[32][33];
-    const int64_t c0 = (int64_t)blockIdx.x * 32, r0 = (int64_t)blockIdx.y * 32;
-    for (int j = threadIdx.y; j < 32; j += 8) {
-        const int64_t r = r0 + j, c = c0 + threadIdx.x;
-        if (r < rows && c < cols) tile[j][threadIdx.x] = in[r * ldi + c];
-    }
-    __syncthreads();
-    for (int j = threadIdx.y; j < 32; j += 8) {
-        const int64_t c = c0 + j, r = r0 + threadIdx.x;
-        if (r < rows && c < cols) out[c * ldo + r] = convert_elem(tile[threadIdx.x][j], (TO *)nullptr);
+    const int64_t c0 = (int64_t)blockIdx.x * 32;
+    // row tiles over grid y, which is capped at 65535 (rows are pixels: 98304 tiles at nside 512)
+    for (int64_t r0 = (int64_t)blockIdx.y * 32; r0 < rows; r0 += (int64_t)gridDim.y * 32) {
+        for (int j = threadIdx.y; j < 32; j += 8) {
+            const int64_t r = r0 + j, c = c0 + threadIdx.x;
+            if (r < rows && c < cols) tile[j][threadIdx.x] = in[r * ldi + c];
+        }
+        __syncthreads();
+        for (int j = threadIdx.y; j < 32; j += 8) {
+            const int64_t c = c0 + j, r = r0 + threadIdx.x;
+            if (r < rows && c < cols) out[c * ldo + r] = convert_elem(tile[threadIdx.x][j], (TO *)nullptr);
+        }
+        __syncthreads();
     }
 }
 
@@ -117,7 +124,7 @@ template <typename TI, typename TO>
 static void transpose_ld(const TI *in, int64_t ldi, int64_t rows, int64_t cols, TO *out, int64_t ldo,
                          cudaStream_t st) {
     if (rows <= 0 || cols <= 0) return;
-    dim3 grid((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32));
+    dim3 grid((unsigned)((cols + 31) / 32), (unsigned)std::min<int64_t>((rows + 31) / 32, 65535));
     k_transpose_ld<TI, TO><<<grid, dim3(32, 8), 0, st>>>(in, ldi, rows, cols, out, ldo);
     note_launch();
 }

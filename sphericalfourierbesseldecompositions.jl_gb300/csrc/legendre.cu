@@ -523,8 +523,8 @@ __global__ void __launch_bounds__(128) k_fold_cols_df(const RingGeom *__restrict
             return max(-90, min(E + extra, 100));
         };
         const int64_t z = 2 * (int64_t)mp + par;
-        atomicMax(Ecol + z * ld + 2 * c, ex(mxr));
-        atomicMax(Ecol + z * ld + 2 * c + 1, ex(mxi));
+        if (mxr > 0.f) atomicMax(Ecol + z * ld + 2 * c, ex(mxr));      // all-zero ring chunks leave the preset
+        if (mxi > 0.f) atomicMax(Ecol + z * ld + 2 * c + 1, ex(mxi));
     }
 }
 
@@ -588,8 +588,8 @@ __global__ void __launch_bounds__(128) k_fold_cols(const RingGeom *__restrict__ 
             return max(-90, min(E + extra, 100));
         };
         const int64_t z = 2 * (int64_t)mp + par;
-        atomicMax(Ecol + z * ld + 2 * c, ex(mxr));
-        atomicMax(Ecol + z * ld + 2 * c + 1, ex(mxi));
+        if (mxr > 0.f) atomicMax(Ecol + z * ld + 2 * c, ex(mxr));      // all-zero ring chunks leave the preset
+        if (mxi > 0.f) atomicMax(Ecol + z * ld + 2 * c + 1, ex(mxi));
     }
 }
 
@@ -721,8 +721,10 @@ __global__ void __launch_bounds__(256) k_fold_alias(const RingGeom *__restrict__
         if (c >= ncplx) continue;
         const int64_t z = 2 * (int64_t)mp + par;
         const float2 m2 = MXREG ? mxr[MXREG ? q : 0] : mx[i];
-        atomicMax(Ecol + z * ld + 2 * c, ex(m2.x));
-        atomicMax(Ecol + z * ld + 2 * c + 1, ex(m2.y));
+        // a ring group whose residuals are all zero (lambda below the slices at polar rings) leaves the
+        // preset: its ex(0) would otherwise override the smaller exponents of the groups with data
+        if (m2.x > 0.f) atomicMax(Ecol + z * ld + 2 * c, ex(m2.x));
+        if (m2.y > 0.f) atomicMax(Ecol + z * ld + 2 * c + 1, ex(m2.y));
     }
 }
 

@@ -294,7 +294,12 @@ __global__ void __launch_bounds__(NTH, 2) k_leg_analysis_tc(const __nv_bfloat16 
     const uint32_t planeB = (uint32_t)NPc * KC * 2;
     LvlSmem cs = lvl_smem(smem);
     float C[4];
-    slice_consts8(cok ? Ecol[(int64_t)z * ncol + col0 + c] : 0, C);
+    {
+        // a column with no non-zero value anywhere keeps the preset (below any exponent): any scale
+        // slices its zeros exactly
+        const int ev = cok ? Ecol[(int64_t)z * ncol + col0 + c] : 0;
+        slice_consts8(ev < -1000 ? 0 : ev, C);
+    }
     const uint32_t tmem = lvl_setup(cs);
     const int LS = NPc;                         // MMA N and TMEM level stride
 
@@ -621,7 +626,7 @@ __global__ void k_lam_rowexp(const double *__restrict__ lam, const int64_t *lam_
     }
 }
 
-// four BF16 slices of v on the scale 2^E: b_k 2^(E - 7 - 7k), |b_0| <= 128, |b_k| <= 64
+// four BF16 slices of v on the scale 2^E: b_k 2^(E - 7 - 8k), |b_k| <= 128
 __device__ __forceinline__ void slices4(double v, int E, __nv_bfloat16 (&o)[4]) {
     double y = ldexp(v, 7 - E);
 #pragma unroll

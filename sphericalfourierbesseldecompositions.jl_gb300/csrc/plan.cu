@@ -957,7 +957,10 @@ int sfb_plan_create(const sfb_plan_desc *d, sfb_plan **out) {
             if ((st = upload(p, &p.d_lamts_off, soff.data(), soff.size())) != SFB_OK) break;
             if ((st = upload<uint16_t>(p, (uint16_t **)&p.d_lamts, nullptr, (size_t)ssz)) != SFB_OK) break;
             launch_build_lamts(p, Es, h->stream);
-            if ((st = build_live_ranges(p, h->stream)) != SFB_OK) break;
+            // SFBGPU_LIVE_CHUNKS=0: no live chunk ranges, so the contractions and the ring DFT run
+            // over every chunk and spectrum (the skipped products are exactly zero either way)
+            const char *lc = std::getenv("SFBGPU_LIVE_CHUNKS");
+            if (!(lc && lc[0] == '0') && (st = build_live_ranges(p, h->stream)) != SFB_OK) break;
         }
         {
             // rings that alias (nph <= 2 lmax) form a prefix: the polar rings grow to the equatorial length

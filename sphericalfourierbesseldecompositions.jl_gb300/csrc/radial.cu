@@ -289,17 +289,18 @@ void launch_extract_spline_chunk(const Plan &p, const double *A, int64_t ldA, in
 __global__ void k_gtab(const int64_t *spl_off, const double *sx, const double *sy, const double *sypp,
                        int64_t npairs, int64_t nr, double rmin, double dr, int with_r2dr, double *gtab) {
     const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t pr = blockIdx.y;
-    if (s >= nr || pr >= npairs) return;
+    if (s >= nr) return;
     const double r = rmin + dr / 2 + s * dr;
-    const int64_t o = spl_off[pr], N = spl_off[pr + 1] - o;
-    double g = spline_eval_dev(sx + o, sy + o, sypp + o, N, r);
-    if (with_r2dr) g *= r * r * dr;
-    gtab[pr * nr + s] = g;
+    for (int64_t pr = blockIdx.y; pr < npairs; pr += gridDim.y) {      // grid y is capped at 65535
+        const int64_t o = spl_off[pr], N = spl_off[pr + 1] - o;
+        double g = spline_eval_dev(sx + o, sy + o, sypp + o, N, r);
+        if (with_r2dr) g *= r * r * dr;
+        gtab[pr * nr + s] = g;
+    }
 }
 
 void launch_gtab(const Plan &p, int64_t nr, double rmin, double dr, int with_r2dr, double *gtab, cudaStream_t st) {
-    dim3 grid((unsigned)((nr + 127) / 128), (unsigned)p.npairs);
+    dim3 grid((unsigned)((nr + 127) / 128), (unsigned)std::min<int64_t>(p.npairs, 65535));
     k_gtab<<<grid, 128, 0, st>>>(p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp, p.npairs, nr, rmin, dr, with_r2dr,
                                  gtab);
                                  note_launch();
@@ -333,29 +334,31 @@ void launch_project_shells_g(const Plan &p, const double *gtab, int64_t nr, cons
 __global__ void k_shell_alm(const int32_t *pair_index, const int64_t *noff, int nmax, int lmax, const double *gtab,
                             int64_t nr, const double *anlm, double *A, int64_t ldA) {
     const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t lm = blockIdx.y;
     if (s >= nr) return;
-    // recover (l, m) from lm = l(l+1)/2 + m
-    int l = (int)((sqrt(8.0 * (double)lm + 1.0) - 1.0) / 2.0);
-    while ((int64_t)(l + 1) * (l + 2) / 2 <= lm) ++l;
-    while ((int64_t)l * (l + 1) / 2 > lm) --l;
-    const int m = (int)(lm - (int64_t)l * (l + 1) / 2);
-    double re = 0.0, im = 0.0;
-    for (int n = 1; n <= nmax; ++n) {
-        const int pr = pair_index[(int64_t)(n - 1) * (lmax + 1) + l];
-        if (pr < 0) continue;
-        const int64_t idx = noff[n - 1] + (int64_t)l * (l + 1) / 2 + m;
-        const double g = gtab[(int64_t)pr * nr + s];
-        re = fma(g, anlm[2 * idx], re);
-        im = fma(g, anlm[2 * idx + 1], im);
+    const int64_t lmsize = (int64_t)(lmax + 1) * (lmax + 2) / 2;
+    for (int64_t lm = blockIdx.y; lm < lmsize; lm += gridDim.y) {        // grid y is capped at 65535
+        // recover (l, m) from lm = l(l+1)/2 + m
+        int l = (int)((sqrt(8.0 * (double)lm + 1.0) - 1.0) / 2.0);
+        while ((int64_t)(l + 1) * (l + 2) / 2 <= lm) ++l;
+        while ((int64_t)l * (l + 1) / 2 > lm) --l;
+        const int m = (int)(lm - (int64_t)l * (l + 1) / 2);
+        double re = 0.0, im = 0.0;
+        for (int n = 1; n <= nmax; ++n) {
+            const int pr = pair_index[(int64_t)(n - 1) * (lmax + 1) + l];
+            if (pr < 0) continue;
+            const int64_t idx = noff[n - 1] + (int64_t)l * (l + 1) / 2 + m;
+            const double g = gtab[(int64_t)pr * nr + s];
+            re = fma(g, anlm[2 * idx], re);
+            im = fma(g, anlm[2 * idx + 1], im);
+        }
+        A[lm * ldA + 2 * s] = re;
+        A[lm * ldA + 2 * s + 1] = (m == 0) ? 0.0 : im;
     }
-    A[lm * ldA + 2 * s] = re;
-    A[lm * ldA + 2 * s + 1] = (m == 0) ? 0.0 : im;
 }
 
 void launch_shell_alm_g(const Plan &p, const int32_t *pair_index, const int64_t *noff, const double *gtab, int64_t nr,
                         const double *anlm, double *A, int64_t ldA, cudaStream_t st) {
-    dim3 grid((unsigned)((nr + 127) / 128), (unsigned)p.lmsize);
+    dim3 grid((unsigned)((nr + 127) / 128), (unsigned)std::min<int64_t>(p.lmsize, 65535));
     k_shell_alm<<<grid, 128, 0, st>>>(pair_index, noff, p.nmax, p.lmax, gtab, nr, anlm, A, ldA);
     note_launch();
 }
@@ -380,17 +383,18 @@ void launch_win_sep_g(const Plan &p, const double *gtab, int64_t nr, const doubl
 __global__ void k_win_dense(const int32_t *pair_n, const int32_t *pair_l, int64_t npairs, const double *gtab, int64_t nr,
                             const double *win, int64_t npix, int lmax, double *out) {
     const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t pr = blockIdx.y;
-    if (p >= npix || pr >= npairs) return;
+    if (p >= npix) return;
     const double *wc = win + p * nr;
-    const double *g = gtab + pr * nr;
-    double acc = 0.0;
-    for (int64_t s = 0; s < nr; ++s) acc += wc[s] * g[s];
-    out[p + npix * ((int64_t)pair_l[pr] + (int64_t)(lmax + 1) * (pair_n[pr] - 1))] = acc;
+    for (int64_t pr = blockIdx.y; pr < npairs; pr += gridDim.y) {      // grid y is capped at 65535
+        const double *g = gtab + pr * nr;
+        double acc = 0.0;
+        for (int64_t s = 0; s < nr; ++s) acc += wc[s] * g[s];
+        out[p + npix * ((int64_t)pair_l[pr] + (int64_t)(lmax + 1) * (pair_n[pr] - 1))] = acc;
+    }
 }
 
 void launch_win_dense_g(const Plan &p, const double *gtab, int64_t nr, const double *win, double *out, cudaStream_t st) {
-    dim3 grid((unsigned)((p.npix + 127) / 128), (unsigned)p.npairs);
+    dim3 grid((unsigned)((p.npix + 127) / 128), (unsigned)std::min<int64_t>(p.npairs, 65535));
     k_win_dense<<<grid, 128, 0, st>>>(p.d_pair_n, p.d_pair_l, p.npairs, gtab, nr, win, p.npix, p.lmax, out);
     note_launch();
 }

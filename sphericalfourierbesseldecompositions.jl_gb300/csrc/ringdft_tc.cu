@@ -400,11 +400,11 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float2 *__restric
             for (int q = 0; q < PD; ++q)
                 if (q < nch) load_chunk(q, pre[q]);
         }
-        for (int kc = 0; kc < nch; kc += PD) {
-            if (!do_chunk(kc, pre[0])) break;
-            if constexpr (PD > 1) {
-                if (kc + 1 < nch && !do_chunk(kc + 1, pre[1])) break;
-            }
+        bool go = true;
+        for (int kc = 0; kc < nch && go; kc += PD) {
+#pragma unroll
+            for (int q = 0; q < PD; ++q)
+                if (go && kc + q < nch) go = do_chunk(kc + q, pre[q]);
         }
     }
     // all MMAs complete before TMEM is read or released
