@@ -356,21 +356,23 @@ def stage_work(stage, precision, nm, ngal, nbasis, niter=3, lmax=238, sky=None):
     product, 2 (complex) x 2 flop per (block z, output row, input row, map)
     (counted under leg_synthesis).
     ring_fft: maps read + ring spectra written, nm npix b + nm n_ring (lmax+1)
-    2 b bytes (b = 4 mixed, 8 FP64); the mixed path computes it as a
-    tensor-core DFT, whose 4 flop per (pixel, m, map) is reported beside.
+    2 b bytes (b = 8: FP64, or the mixed path's double-float pairs); the
+    mixed path computes it as a tensor-core DFT, whose 4 flop per (pixel, m,
+    map) is reported beside.
     sky = sky_rings(...): in the mixed path the DFT flops count the pixels of
     the ring pairs with galaxies and the first analysis pass the rings of
     their span (the rows elsewhere are zero and skipped).
-    fold: G read + R written per pass (mixed: the aliased rings only; FP64:
-    F, G read + R written over all rings).  deposit: 40 B per galaxy (record
-    read + binning update) + the basis maps written (mixed: on the rings
-    holding galaxies, sky[2] pixels)."""
+    fold: G read + R written per pass (mixed: the aliased rings only, G FP32
+    and R double-float; FP64: F, G read + R written over all rings).
+    deposit: 40 B per galaxy (record read + binning update) + the basis maps
+    written, 8 B per value (mixed: double-float pairs on the rings holding
+    galaxies, sky[2] pixels)."""
     lmsize = (lmax + 1) * (lmax + 2) // 2
     nrn = 2 * NSIDE
     n_ring = 4 * NSIDE - 1
     npix = 12 * NSIDE ** 2
     ncol = 2 * nm
-    t = 4 if precision == "mixed" else 8
+    t = 8                                            # maps, spectra, residuals: FP64 or double-float
     fsz = 2 * (lmax + 1) * nrn * ncol * t
     ral, gram = gram_geometry(lmax, niter)
     gram = gram and precision == "mixed" and nm > 4
@@ -390,7 +392,7 @@ def stage_work(stage, precision, nm, ngal, nbasis, niter=3, lmax=238, sky=None):
         return ("byte", float(t) * nm * npix + float(nm) * n_ring * (lmax + 1) * 2 * t)
     if stage == "fold":
         if gram:
-            return ("byte", niter * 2.0 * 2 * (lmax + 1) * ral * ncol * t)
+            return ("byte", niter * 2.0 * (lmax + 1) * ral * ncol * (4 + 8))   # G (FP32) read, R (pairs) written
         return ("byte", niter * 3.0 * fsz)
     if stage == "deposit":
         mpix = sky[2] if (sky and precision == "mixed") else npix
@@ -753,9 +755,10 @@ def main():
             traffic, parts = stage_traffic(k, {"maps": nm, "galaxies": N})
             table[k]["traffic"] = traffic
             if traffic is not None:
-                table[k]["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum per call on the "
-                                              "profile case (nside 256, 35 maps, 1e6 galaxies), one kernel per "
-                                              "capture, scaled to this run: " + ", ".join(parts))
+                table[k]["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum per call, one kernel "
+                                              "per capture, on the profile cases (transforms: the bench basis with "
+                                              "1e6 galaxies; deposit: 35 maps with 1e7 galaxies), scaled to this run "
+                                              "by maps or galaxies: " + ", ".join(parts))
     dom = max(table, key=lambda k: stages[k]["ms_per_step"])
     roof = dict(table[dom])
     roof["kernel_stage"] = dom

@@ -70,8 +70,9 @@ def test_stage_work_counts_the_rings_with_data():
     sky = (npix // 2, 640, npix // 4)
     full = dict((st, b.stage_work(st, "mixed", nm, ngal, nbasis)) for st in ("deposit", "leg_analysis"))
     part = dict((st, b.stage_work(st, "mixed", nm, ngal, nbasis, sky=sky)) for st in ("deposit", "leg_analysis"))
-    assert part["deposit"][1] == pytest.approx(40.0 * ngal + 4.0 * nbasis * npix / 4)
-    assert full["deposit"][1] == pytest.approx(40.0 * ngal + 4.0 * nbasis * npix)
+    # maps are written as double-float pairs, 8 B per value
+    assert part["deposit"][1] == pytest.approx(40.0 * ngal + 8.0 * nbasis * npix / 4)
+    assert full["deposit"][1] == pytest.approx(40.0 * ngal + 8.0 * nbasis * npix)
     assert part["leg_analysis"][1] < full["leg_analysis"][1]
     # the FP64 path computes every ring: the sky does not change its counts
     assert b.stage_work("deposit", "fp64", nm, ngal, nbasis, sky=sky) == b.stage_work("deposit", "fp64", nm, ngal,
