@@ -797,6 +797,9 @@ int sfb_plan_create(const sfb_plan_desc *d, sfb_plan **out) {
             cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking) != cudaSuccess ||
             cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&p.dft_side, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&p.dft_fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&p.dft_join, cudaEventDisableTiming) != cudaSuccess ||
             [&] {
                 for (auto &e : h->ev_copy)
                     if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return true;
@@ -1027,6 +1030,9 @@ void sfb_plan_destroy(sfb_plan *h) {
     if (h->side) cudaStreamDestroy(h->side);
     if (h->ev_fork) cudaEventDestroy(h->ev_fork);
     if (h->ev_join) cudaEventDestroy(h->ev_join);
+    if (p.dft_side) cudaStreamDestroy(p.dft_side);
+    if (p.dft_fork) cudaEventDestroy(p.dft_fork);
+    if (p.dft_join) cudaEventDestroy(p.dft_join);
     for (auto e : h->ev_copy)
         if (e) cudaEventDestroy(e);
     delete h;

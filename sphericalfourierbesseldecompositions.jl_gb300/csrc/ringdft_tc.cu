@@ -166,11 +166,12 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float2 *__restric
                                                          const unsigned char *__restrict__ img,
                                                          const int64_t *__restrict__ img_off, float2 *__restrict__ F,
                                                          int64_t ldF, float2 wdf, const unsigned char *dead,
-                                                         int ntn, const int *span, int *err) {
+                                                         int ntn, const int *span, int rev, int *err) {
     extern __shared__ __align__(1024) unsigned char smem[];
     // grid (column blocks u, row tiles, classes): the column blocks of one row tile are launched
-    // together and read its map rows through L2 once
-    const int cls = blockIdx.z;
+    // together and read its map rows through L2 once; rev: classes in reverse order (the polar
+    // rings, longest first, so that the launch does not end on its longest CTAs)
+    const int cls = rev ? (int)(gridDim.z - 1 - blockIdx.z) : (int)blockIdx.z;
     const int rb = cls_off[cls];
     const int64_t npairs = (int64_t)(cls_off[cls + 1] - rb) * nmaps;
     const int ty = blockIdx.y;
@@ -631,22 +632,33 @@ void launch_ring_analysis_tc(const Plan &p, const float2 *maps, int64_t nmaps, f
     const unsigned char *dead = skip_unread ? p.d_dft_dead : nullptr;
     const int *span = skip_unread ? nzr : nullptr;
     // imaged classes read B from the image, the others gather it from the ring table
-    auto launch = [&](dim3 grid, int c0, bool img) {
+    auto launch = [&](dim3 grid, int c0, bool img, int rev, cudaStream_t s) {
         if (img)
-            dft::k_ring_dft_tc<true><<<grid, dft::NTHR, dft::SMEM, st>>>(
+            dft::k_ring_dft_tc<true><<<grid, dft::NTHR, dft::SMEM, s>>>(
                 maps, p.npix, nmaps, p.d_rings, (int)p.nrn, p.lmax, p.d_cls_rings, p.d_cls_off + c0, erow, p.d_dtw,
-                p.d_dtw_off, p.d_dtimg, p.d_dtimg_off + c0, F, 2 * nmaps, wdf, dead, (int)ntn, span, p.d_err);
+                p.d_dtw_off, p.d_dtimg, p.d_dtimg_off + c0, F, 2 * nmaps, wdf, dead, (int)ntn, span, rev, p.d_err);
         else
-            dft::k_ring_dft_tc<false><<<grid, dft::NTHR, dft::SMEM, st>>>(
+            dft::k_ring_dft_tc<false><<<grid, dft::NTHR, dft::SMEM, s>>>(
                 maps, p.npix, nmaps, p.d_rings, (int)p.nrn, p.lmax, p.d_cls_rings, p.d_cls_off + c0, erow, p.d_dtw,
-                p.d_dtw_off, nullptr, nullptr, F, 2 * nmaps, wdf, dead, (int)ntn, span, p.d_err);
+                p.d_dtw_off, nullptr, nullptr, F, 2 * nmaps, wdf, dead, (int)ntn, span, rev, p.d_err);
         note_launch();
     };
     const unsigned mtiles = (unsigned)((nmaps + dft::NPAIR - 1) / dft::NPAIR);
-    // polar rings: one class per ring, imaged when the whole polar set fits the image
-    if (p.n_polar > 0) launch(dim3(ntn, mtiles, (unsigned)p.n_polar), 0, p.dtimg_polar);
     const int64_t eq_tiles = ((int64_t)p.eq_max_rings * nmaps + dft::NPAIR - 1) / dft::NPAIR;
-    launch(dim3(ntn, (unsigned)eq_tiles, (unsigned)p.n_eq_cls), p.n_polar, p.d_dtimg != nullptr);
+    // the equatorial classes (equal CTAs, a partly filled last wave) run on the second stream beside
+    // the polar rings (longest first), so the tail of each launch overlaps the other
+    const bool two = p.dft_side && p.n_polar > 0;
+    if (two) {
+        cudaEventRecord(p.dft_fork, st);
+        cudaStreamWaitEvent(p.dft_side, p.dft_fork, 0);
+    }
+    launch(dim3(ntn, (unsigned)eq_tiles, (unsigned)p.n_eq_cls), p.n_polar, p.d_dtimg != nullptr, 0,
+           two ? p.dft_side : st);
+    if (p.n_polar > 0) launch(dim3(ntn, mtiles, (unsigned)p.n_polar), 0, p.dtimg_polar, 1, st);
+    if (two) {
+        cudaEventRecord(p.dft_join, p.dft_side);
+        cudaStreamWaitEvent(st, p.dft_join, 0);
+    }
 }
 
 }  // namespace sfb

@@ -124,6 +124,9 @@ struct Plan {
     int2 *d_lamtc_live = nullptr;   // live chunk ranges of the analysis table [z][row tile] (one allocation
     int2 *d_lamts_live = nullptr;   // with the synthesis table's [z][ring tile]); see build_live_ranges
     unsigned char *d_dft_dead = nullptr;   // [ring pair][64-m block]: spectra no analysis chunk reads
+    // second stream for the ring DFT's equatorial launch, forked from and joined to the call's stream
+    cudaStream_t dft_side = nullptr;
+    cudaEvent_t dft_fork = nullptr, dft_join = nullptr;
     int64_t *d_lam_off = nullptr;   // [2*(lmax+1)] offset of block (m, parity)
     int64_t lam_elems = 0;
     int64_t *d_spl_off = nullptr;
