@@ -361,8 +361,9 @@ int sht_analysis(sfb_plan *h, const double *maps, int64_t nm, cudaStream_t st, b
         // the Gram refinement and niter = 0 read the spectra only in the first analysis pass (over the
         // span with data and the live chunks); the full refinement passes fold them over every ring
         const bool skip_unread = (nm > 4 && p.d_gramts && p.niter > 0) || p.niter == 0;
-        launch_ring_analysis_tc(p, reinterpret_cast<const float2 *>(maps), nm, reinterpret_cast<float2 *>(fbuf.ptr),
-                                reinterpret_cast<int *>(p.erow.ptr), nzr, st, ring_live, nlive, skip_unread);
+        SFB_TRY(launch_ring_analysis_tc(p, reinterpret_cast<const float2 *>(maps), nm,
+                                        reinterpret_cast<float2 *>(fbuf.ptr), reinterpret_cast<int *>(p.erow.ptr), nzr,
+                                        st, ring_live, nlive, skip_unread));
     } else {
         // many columns: the FFT records the span of ring pairs with data, over which the
         // first analysis pass sums (the spectra are zero elsewhere)
@@ -896,6 +897,11 @@ int sfb_plan_create(const sfb_plan_desc *d, sfb_plan **out) {
             if ((st = upload(p, &p.d_dtw_off, doff.data(), doff.size())) != SFB_OK) break;
             if ((st = upload(p, &p.d_cls_rings, crings.data(), crings.size())) != SFB_OK) break;
             if ((st = upload(p, &p.d_cls_off, coff.data(), coff.size())) != SFB_OK) break;
+            p.h_cls_rings = crings;
+            p.h_cls_off = coff;
+            if ((st = upload<int64_t>(p, &p.d_aimg_off, nullptr, coff.size())) != SFB_OK) break;
+            // SFBGPU_DFT_AIMG=0: the DFT's producers slice the map rows themselves (no A image)
+            if (const char *e = std::getenv("SFBGPU_DFT_AIMG")) p.dft_aimg = e[0] != '0';
             // B operand image: the polar classes too while the whole image stays under
             // SFBGPU_DFT_IMAGE_MAX_BYTES (default 2 GiB; the equatorial classes are always imaged)
             {
@@ -1017,7 +1023,7 @@ void sfb_plan_destroy(sfb_plan *h) {
     cudaSetDevice(p.device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     void *ptrs[] = {p.d_rings, p.d_twtab, p.d_twoff, p.d_phase, p.d_wphase, p.d_twtab32, p.d_wphase32, p.d_dtw,
-                    p.d_dtw_off, p.d_dtimg, p.d_dtimg_off, p.d_gramts, p.d_gramts_off, p.d_gram64, p.d_gram_off, p.d_cls_rings, p.d_cls_off, p.d_lam, p.d_lam32, p.d_lamtc, p.d_lamtc_off, p.d_lamts, p.d_lamts_off, p.d_lamtc_live, p.d_dft_dead, p.d_lam_off, p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp,
+                    p.d_dtw_off, p.d_dtimg, p.d_dtimg_off, p.d_gramts, p.d_gramts_off, p.d_gram64, p.d_gram_off, p.d_cls_rings, p.d_cls_off, p.d_aimg_off, p.aimg.ptr, p.d_lam, p.d_lam32, p.d_lamtc, p.d_lamtc_off, p.d_lamts, p.d_lamts_off, p.d_lamtc_live, p.d_dft_dead, p.d_lam_off, p.d_spl_off, p.d_spl_x, p.d_spl_y, p.d_spl_ypp,
                     p.d_pair_l, p.d_pair_n, p.d_out_pair, p.d_out_lm, p.d_coef, p.d_coefT, p.d_proj_tiles, p.d_err,
                     p.maps.ptr, p.fbuf.ptr, p.gbuf.ptr, p.rbuf.ptr, p.alm.ptr, p.scratch.ptr, p.scratch2.ptr, p.dep.ptr, p.maps32.ptr,
                     p.ref.ptr, p.rf.ptr, p.rg.ptr, p.rr.ptr, p.ralm.ptr, p.almdf2.ptr, p.adf0.ptr, p.ecoef.ptr, p.erow.ptr, p.almdf.ptr, p.nzr64.ptr, h->d_pair_index, h->d_noff};

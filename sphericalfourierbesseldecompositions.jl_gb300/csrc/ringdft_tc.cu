@@ -152,11 +152,91 @@ __global__ void __launch_bounds__(128) k_ring_rowexp(const float2 *__restrict__ 
     }
 }
 
+// A-operand image: the four sliced planes of every live tile and 32-pixel
+// chunk, in the shared-memory core-matrix layout the DFT's MMAs read (4 PLANE
+// bytes per (class, tile, chunk), at chunk aoff[class] + tile nch + chunk), so
+// that the DFT fetches its A operand by bulk copy like its B operand.  The
+// rows, exponents and north-only rule are those of k_ring_dft_tc; tiles with
+// no live row (the DFT writes their spectra without reading A) are skipped.
+// Grid (tiles, classes, groups of SLICE_CPG chunks), one thread per (row,
+// 16-pixel half) as the DFT's imaged producers.
+constexpr int SLICE_CPG = 4;
+__global__ void __launch_bounds__(NPROD) k_dft_slice_a(const float2 *__restrict__ maps, int64_t npix, int64_t nmaps,
+                                                        const RingGeom *__restrict__ rings, int nrn,
+                                                        const int32_t *__restrict__ cls_rings,
+                                                        const int32_t *__restrict__ cls_off,
+                                                        const int *__restrict__ erow, const int64_t *__restrict__ aoff,
+                                                        unsigned char *__restrict__ aimg) {
+    const int cls = blockIdx.y;
+    const int rb = cls_off[cls];
+    const int64_t npairs = (int64_t)(cls_off[cls + 1] - rb) * nmaps;
+    const int ty = blockIdx.x;
+    const int64_t pair0 = (int64_t)ty * NPAIR;
+    if (pair0 >= npairs || (int)blockIdx.z * SLICE_CPG * KC >= rings[cls_rings[rb]].nph) return;
+    const int tid = threadIdx.x;
+    bool snz = false;
+    if (tid < 2 * NPAIR) {
+        const int64_t qq = (int64_t)(ty & ~1) * NPAIR + tid;
+        if (qq < npairs) {
+            const int rg = cls_rings[rb + (int)(qq / nmaps)];
+            if (rings[rg].start_s != rings[rg].start_n)
+                snz = erow[((int64_t)nrn + rg) * nmaps + qq % nmaps] != ZERO_ROW_E;
+        }
+    }
+    const bool nonly = !__syncthreads_or(snz);
+    if (nonly && (ty & 1)) return;
+    const int ti = tid & (NROW - 1), ahalf = (tid >> 7) & 1;
+    const int hemi = nonly ? 0 : ti >> 6;
+    const int64_t q = pair0 + (nonly ? ti : (ti & (NPAIR - 1)));
+    const bool rok = q < npairs;
+    int ring = cls_rings[rb];
+    int64_t b = 0;
+    if (rok) {
+        ring = cls_rings[rb + (int)(q / nmaps)];
+        b = q % nmaps;
+    }
+    const RingGeom g = rings[ring];
+    const int E = rok ? erow[((int64_t)hemi * nrn + ring) * nmaps + b] : ZERO_ROW_E;
+    const bool live = rok && (hemi == 0 || g.start_s != g.start_n) && E != ZERO_ROW_E;
+    if (!__syncthreads_or(live)) return;
+    const int n = rings[cls_rings[rb]].nph;
+    const int nch = (n + KC - 1) / KC;
+    const int kc0 = blockIdx.z * SLICE_CPG, kc1 = min(nch, kc0 + SLICE_CPG);
+    const float2 *x = maps + b * npix + (hemi ? g.start_s : g.start_n);
+    float C[4];
+    slice_consts8(E == ZERO_ROW_E ? 0 : E, C);
+    unsigned char *dst = aimg + (size_t)(aoff[cls] + (int64_t)ty * nch) * (4 * PLANE);
+    for (int kc = kc0; kc < kc1; ++kc) {
+        float4 v[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int j = kc * KC + 16 * ahalf + 2 * i;
+            v[i] = (live && j < n) ? *reinterpret_cast<const float4 *>(x + j) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int gq = 0; gq < 2; ++gq) {
+            const float4 *c4 = v + 4 * gq;
+            const float vh[8] = {c4[0].x, c4[0].z, c4[1].x, c4[1].z, c4[2].x, c4[2].z, c4[3].x, c4[3].z};
+            const float vl[8] = {c4[0].y, c4[0].w, c4[1].y, c4[1].w, c4[2].y, c4[2].w, c4[3].y, c4[3].w};
+            uint32_t w[4][4];
+            slice8_df(vh, vl, C, w);
+            const uint32_t off = core_off(ti, 16 * ahalf + 8 * gq);
+#pragma unroll
+            for (int sl = 0; sl < 4; ++sl)
+                *reinterpret_cast<uint4 *>(dst + (size_t)kc * (4 * PLANE) + sl * PLANE + off) =
+                    make_uint4(w[sl][0], w[sl][1], w[sl][2], w[sl][3]);
+        }
+    }
+}
+
 // IMG: the B operand of every chunk comes from the precomputed image (one
 // 32 KB bulk copy per stage, issued by thread 0) and all eight producer warps
 // slice the map rows, two threads per row; otherwise warps 4-7 gather B from
 // the ring's sliced table.
-template <bool IMG>
+// AIMG: the A operand comes from the A-operand image by bulk copy (thread 0; with IMG both planes of a
+// stage in one transaction, and the producers only release the stages and run the epilogue; without
+// IMG warps 4-7 gather the B planes from the ring's table meanwhile).
+template <bool IMG, bool AIMG>
 __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float2 *__restrict__ maps, int64_t npix, int64_t nmaps,
                                                          const RingGeom *__restrict__ rings, int nrn, int lmax,
                                                          const int32_t *__restrict__ cls_rings,
@@ -166,7 +246,9 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float2 *__restric
                                                          const unsigned char *__restrict__ img,
                                                          const int64_t *__restrict__ img_off, float2 *__restrict__ F,
                                                          int64_t ldF, float2 wdf, const unsigned char *dead,
-                                                         int ntn, const int *span, int rev, int *err) {
+                                                         int ntn, const int *span, int rev,
+                                                         const int64_t *__restrict__ aoff,
+                                                         const unsigned char *__restrict__ aimg, int *err) {
     extern __shared__ __align__(1024) unsigned char smem[];
     // grid (column blocks u, row tiles, classes): the column blocks of one row tile are launched
     // together and read its map rows through L2 once; rev: classes in reverse order (the polar
@@ -205,7 +287,8 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float2 *__restric
     if (nonly && (ty & 1)) return;
     const int npr = nonly ? 2 * NPAIR : NPAIR;      // (ring, map) pairs of this tile
     const bool prod = tid < NPROD;
-    const bool abuild = IMG ? prod : tid < NROW;   // IMG: all producers build A; else warps 0-3 A, 4-7 B
+    // IMG: all producers build A; else warps 0-3 A, 4-7 B; AIMG: the A planes arrive by bulk copy
+    const bool abuild = AIMG ? false : IMG ? prod : tid < NROW;
     const int ti = tid & (NROW - 1);
     const int ahalf = IMG ? (tid >> 7) & 1 : 0;    // IMG: which 16 pixels of the chunk this thread slices
     // barriers: full[s] (8 producer warps + the image copy), empty[s] (MMA commit), done (all MMAs)
@@ -224,6 +307,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float2 *__restric
     const uint2 *T = dtw + dtw_off[ring0];
     const int nch = (n + KC - 1) / KC;
     const unsigned char *bimg = IMG ? img + (size_t)(img_off[cls] + (int64_t)u * nch) * (4 * PLANE) : nullptr;
+    const unsigned char *atile = AIMG ? aimg + (size_t)(aoff[cls] + (int64_t)ty * nch) * (4 * PLANE) : nullptr;
 
     // A row ti: pair ti % 64, hemisphere ti / 64 (north-only tiles: pair ti, north)
     const int hemi = nonly ? 0 : ti >> 6;
@@ -238,13 +322,14 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float2 *__restric
     const RingGeom g = rings[ring];
     const int E = rok ? erow[((int64_t)hemi * nrn + ring) * nmaps + b] : ZERO_ROW_E;
     // zero rows are not read (on rings without galaxies they are not even written)
-    const bool live = abuild && rok && (hemi == 0 || g.start_s != g.start_n) && E != ZERO_ROW_E;
+    const bool rowlive = rok && (hemi == 0 || g.start_s != g.start_n) && E != ZERO_ROW_E;
+    const bool live = abuild && rowlive;
     const float2 *x = maps + b * npix + (hemi ? g.start_s : g.start_n);
     float C[4];
     slice_consts8(E == ZERO_ROW_E ? 0 : E, C);
     const int L1 = lmax + 1;
     // a tile of zero rows (rings outside the survey) has zero spectra: written without MMAs
-    if (!__syncthreads_or(live)) {
+    if (!__syncthreads_or(AIMG ? (rowlive && prod) : live)) {
         for (int i = tid; i < 2 * 64 * npr; i += NTHR) {
             const int pr = i % npr, mo = (i / npr) & 63, sg = i / (64 * npr);
             const int mm = 64 * u + mo;
@@ -274,7 +359,7 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float2 *__restric
     }
     if (tid == 0) {
         for (int i = 0; i < NSTAGE; ++i) {
-            mbar_init(&full[i], NPROD / 32 + (IMG ? 1 : 0));
+            mbar_init(&full[i], NPROD / 32 + ((IMG || AIMG) ? 1 : 0));
             mbar_init(&empty[i], 1);
         }
         mbar_init(done, 1);
@@ -345,7 +430,13 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float2 *__restric
             }
             unsigned char *sbase = smem + st * STAGE;         // A planes 0..3, B planes 4..7
             const int j0 = kc * KC;
-            if (IMG && tid == 0) {
+            if (AIMG && tid == 0) {
+                // A planes of this chunk (and with IMG the B planes): one bulk copy from each image
+                mbar_expect_tx(&full[st], (IMG ? 8 : 4) * PLANE);
+                bulk_g2s(sbase, atile + (size_t)kc * (4 * PLANE), 4 * PLANE, &full[st]);
+                if (IMG) bulk_g2s(sbase + 4 * PLANE, bimg + (size_t)kc * (4 * PLANE), 4 * PLANE, &full[st]);
+                ncopied = kc + 1;
+            } else if (IMG && tid == 0) {
                 // B planes of this chunk: one bulk copy from the image
                 mbar_expect_tx(&full[st], 4 * PLANE);
                 bulk_g2s(sbase + 4 * PLANE, bimg + (size_t)kc * (4 * PLANE), 4 * PLANE, &full[st]);
@@ -365,8 +456,8 @@ __global__ void __launch_bounds__(NTHR, 1) k_ring_dft_tc(const float2 *__restric
                     for (int s = 0; s < 4; ++s) st_shared_v4(sbase + s * PLANE + off, w[s]);
                 }
                 if (kc + PD < nch) load_chunk(kc + PD, cur);
-            } else if constexpr (!IMG) {
-                // B row: table slices at k = m (2 j + t) + part n/2 (mod 2n)
+            } else if (!IMG && tid >= NROW) {
+                // B row (warps 4-7): table slices at k = m (2 j + t) + part n/2 (mod 2n)
 #pragma unroll
                 for (int gq = 0; gq < 4; ++gq) {
                     uint32_t w[4][4];
@@ -611,8 +702,8 @@ uint2 dft_slices(double v, int EB) {
     return make_uint2((uint32_t)s[0] | ((uint32_t)s[1] << 16), (uint32_t)s[2] | ((uint32_t)s[3] << 16));
 }
 
-void launch_ring_analysis_tc(const Plan &p, const float2 *maps, int64_t nmaps, float2 *F, int *erow, int *nzr,
-                             cudaStream_t st, const int *ring_live, int64_t nlive, bool skip_unread) {
+int launch_ring_analysis_tc(Plan &p, const float2 *maps, int64_t nmaps, float2 *F, int *erow, int *nzr,
+                            cudaStream_t st, const int *ring_live, int64_t nlive, bool skip_unread) {
     {
         // nzr[0] = 0x7f7f7f7f (above any ring index), nzr[1] = -1
         cudaMemsetAsync(nzr, 0x7f, sizeof(int), st);
@@ -622,8 +713,10 @@ void launch_ring_analysis_tc(const Plan &p, const float2 *maps, int64_t nmaps, f
                                                  nlive, (int)(4 * p.nside - 1));
         note_launch();
     }
-    set_smem(dft::k_ring_dft_tc<true>, dft::SMEM);
-    set_smem(dft::k_ring_dft_tc<false>, dft::SMEM);
+    set_smem(dft::k_ring_dft_tc<true, true>, dft::SMEM);
+    set_smem(dft::k_ring_dft_tc<false, true>, dft::SMEM);
+    set_smem(dft::k_ring_dft_tc<true, false>, dft::SMEM);
+    set_smem(dft::k_ring_dft_tc<false, false>, dft::SMEM);
     const unsigned ntn = (unsigned)((p.lmax + 1 + 63) / 64);
     const double wq = 4.0 * M_PI / (double)p.npix;
     const float2 wdf = make_float2((float)wq, (float)(wq - (double)(float)wq));
@@ -632,19 +725,71 @@ void launch_ring_analysis_tc(const Plan &p, const float2 *maps, int64_t nmaps, f
     const unsigned char *dead = skip_unread ? p.d_dft_dead : nullptr;
     const int *span = skip_unread ? nzr : nullptr;
     // imaged classes read B from the image, the others gather it from the ring table
-    auto launch = [&](dim3 grid, int c0, bool img, int rev, cudaStream_t s) {
-        if (img)
-            dft::k_ring_dft_tc<true><<<grid, dft::NTHR, dft::SMEM, s>>>(
-                maps, p.npix, nmaps, p.d_rings, (int)p.nrn, p.lmax, p.d_cls_rings, p.d_cls_off + c0, erow, p.d_dtw,
-                p.d_dtw_off, p.d_dtimg, p.d_dtimg_off + c0, F, 2 * nmaps, wdf, dead, (int)ntn, span, rev, p.d_err);
-        else
-            dft::k_ring_dft_tc<false><<<grid, dft::NTHR, dft::SMEM, s>>>(
-                maps, p.npix, nmaps, p.d_rings, (int)p.nrn, p.lmax, p.d_cls_rings, p.d_cls_off + c0, erow, p.d_dtw,
-                p.d_dtw_off, nullptr, nullptr, F, 2 * nmaps, wdf, dead, (int)ntn, span, rev, p.d_err);
-        note_launch();
-    };
     const unsigned mtiles = (unsigned)((nmaps + dft::NPAIR - 1) / dft::NPAIR);
     const int64_t eq_tiles = ((int64_t)p.eq_max_rings * nmaps + dft::NPAIR - 1) / dft::NPAIR;
+    // A-operand image for the imaged launches: per-class chunk offsets for this map count, the
+    // buffer, and the slicing pass (after the row exponents, on the call's stream)
+    // the polar rings gather their twiddles from the ring tables (L1-resident) while A arrives by bulk
+    // copy; their twiddle image is read only when the A image is off
+    const bool aimg_polar = p.dft_aimg && p.n_polar > 0;
+    const bool aimg_eq = p.dft_aimg && p.d_dtimg != nullptr && p.n_eq_cls > 0;
+    if (aimg_polar || aimg_eq) {
+        const int ncls = (int)p.h_cls_off.size() - 1;
+        if (p.aimg_nmaps != nmaps) {
+            p.h_aimg_off.assign(ncls + 1, 0);
+            int64_t o = 0;
+            for (int c = 0; c < ncls; ++c) {
+                p.h_aimg_off[c] = o;
+                const int64_t rings_c = p.h_cls_off[c + 1] - p.h_cls_off[c];
+                const int64_t tiles = (rings_c * nmaps + dft::NPAIR - 1) / dft::NPAIR;
+                const int64_t nph = p.h_rings[p.h_cls_rings[p.h_cls_off[c]]].nph;
+                o += tiles * ((nph + dft::KC - 1) / dft::KC);
+            }
+            p.h_aimg_off[ncls] = o;
+            SFB_CUDA_TRY(cudaMemcpyAsync(p.d_aimg_off, p.h_aimg_off.data(), (size_t)(ncls + 1) * sizeof(int64_t),
+                                         cudaMemcpyHostToDevice, st));
+            p.aimg_nmaps = nmaps;
+        }
+        SFB_TRY(grow(p, p.aimg, (size_t)(p.h_aimg_off[ncls] * (4 * dft::PLANE) / sizeof(double))));
+        unsigned char *aimg = reinterpret_cast<unsigned char *>(p.aimg.ptr);
+        // chunk groups: the longest ring (4 nside pixels) in groups of SLICE_CPG chunks
+        const unsigned ngrp = (unsigned)((4 * p.nside + dft::KC * dft::SLICE_CPG - 1) / (dft::KC * dft::SLICE_CPG));
+        if (aimg_polar) {
+            dft::k_dft_slice_a<<<dim3(mtiles, (unsigned)p.n_polar, ngrp), dft::NPROD, 0, st>>>(
+                maps, p.npix, nmaps, p.d_rings, (int)p.nrn, p.d_cls_rings, p.d_cls_off, erow, p.d_aimg_off, aimg);
+            note_launch();
+        }
+        if (aimg_eq) {
+            dft::k_dft_slice_a<<<dim3((unsigned)eq_tiles, (unsigned)p.n_eq_cls, ngrp), dft::NPROD, 0, st>>>(
+                maps, p.npix, nmaps, p.d_rings, (int)p.nrn, p.d_cls_rings, p.d_cls_off + p.n_polar, erow,
+                p.d_aimg_off + p.n_polar, aimg);
+            note_launch();
+        }
+    }
+    unsigned char *aimg = reinterpret_cast<unsigned char *>(p.aimg.ptr);
+    auto launch = [&](dim3 grid, int c0, bool img, bool ai, int rev, cudaStream_t s) {
+        if (!img && ai)
+            dft::k_ring_dft_tc<false, true><<<grid, dft::NTHR, dft::SMEM, s>>>(
+                maps, p.npix, nmaps, p.d_rings, (int)p.nrn, p.lmax, p.d_cls_rings, p.d_cls_off + c0, erow, p.d_dtw,
+                p.d_dtw_off, nullptr, nullptr, F, 2 * nmaps, wdf, dead, (int)ntn, span, rev, p.d_aimg_off + c0, aimg,
+                p.d_err);
+        else if (img && ai)
+            dft::k_ring_dft_tc<true, true><<<grid, dft::NTHR, dft::SMEM, s>>>(
+                maps, p.npix, nmaps, p.d_rings, (int)p.nrn, p.lmax, p.d_cls_rings, p.d_cls_off + c0, erow, p.d_dtw,
+                p.d_dtw_off, p.d_dtimg, p.d_dtimg_off + c0, F, 2 * nmaps, wdf, dead, (int)ntn, span, rev,
+                p.d_aimg_off + c0, aimg, p.d_err);
+        else if (img)
+            dft::k_ring_dft_tc<true, false><<<grid, dft::NTHR, dft::SMEM, s>>>(
+                maps, p.npix, nmaps, p.d_rings, (int)p.nrn, p.lmax, p.d_cls_rings, p.d_cls_off + c0, erow, p.d_dtw,
+                p.d_dtw_off, p.d_dtimg, p.d_dtimg_off + c0, F, 2 * nmaps, wdf, dead, (int)ntn, span, rev, nullptr,
+                nullptr, p.d_err);
+        else
+            dft::k_ring_dft_tc<false, false><<<grid, dft::NTHR, dft::SMEM, s>>>(
+                maps, p.npix, nmaps, p.d_rings, (int)p.nrn, p.lmax, p.d_cls_rings, p.d_cls_off + c0, erow, p.d_dtw,
+                p.d_dtw_off, nullptr, nullptr, F, 2 * nmaps, wdf, dead, (int)ntn, span, rev, nullptr, nullptr,
+                p.d_err);
+        note_launch();
+    };
     // the equatorial classes (equal CTAs, a partly filled last wave) run on the second stream beside
     // the polar rings (longest first), so the tail of each launch overlaps the other
     const bool two = p.dft_side && p.n_polar > 0;
@@ -652,13 +797,15 @@ void launch_ring_analysis_tc(const Plan &p, const float2 *maps, int64_t nmaps, f
         cudaEventRecord(p.dft_fork, st);
         cudaStreamWaitEvent(p.dft_side, p.dft_fork, 0);
     }
-    launch(dim3(ntn, (unsigned)eq_tiles, (unsigned)p.n_eq_cls), p.n_polar, p.d_dtimg != nullptr, 0,
+    launch(dim3(ntn, (unsigned)eq_tiles, (unsigned)p.n_eq_cls), p.n_polar, p.d_dtimg != nullptr, aimg_eq, 0,
            two ? p.dft_side : st);
-    if (p.n_polar > 0) launch(dim3(ntn, mtiles, (unsigned)p.n_polar), 0, p.dtimg_polar, 1, st);
+    if (p.n_polar > 0)
+        launch(dim3(ntn, mtiles, (unsigned)p.n_polar), 0, p.dtimg_polar && !aimg_polar, aimg_polar, 1, st);
     if (two) {
         cudaEventRecord(p.dft_join, p.dft_side);
         cudaStreamWaitEvent(st, p.dft_join, 0);
     }
+    return SFB_OK;
 }
 
 }  // namespace sfb

@@ -124,6 +124,14 @@ struct Plan {
     int2 *d_lamtc_live = nullptr;   // live chunk ranges of the analysis table [z][row tile] (one allocation
     int2 *d_lamts_live = nullptr;   // with the synthesis table's [z][ring tile]); see build_live_ranges
     unsigned char *d_dft_dead = nullptr;   // [ring pair][64-m block]: spectra no analysis chunk reads
+    // ring DFT: host copies of the classes, and the A-operand image (the sliced planes of the map rows
+    // of every live tile, bulk-copied by the DFT) with its per-class chunk offsets for aimg_nmaps maps
+    std::vector<int32_t> h_cls_rings, h_cls_off;
+    bool dft_aimg = true;
+    DevBuf<double> aimg;
+    int64_t *d_aimg_off = nullptr;
+    std::vector<int64_t> h_aimg_off;
+    int64_t aimg_nmaps = -1;
     // second stream for the ring DFT's equatorial launch, forked from and joined to the call's stream
     cudaStream_t dft_side = nullptr;
     cudaEvent_t dft_fork = nullptr, dft_join = nullptr;
@@ -249,9 +257,9 @@ void launch_to_df(const double *in, int64_t n, float2 *out, cudaStream_t st);
 // Mixed-precision ring analysis on the tensor cores (double-float maps -> double-float F).
 // nzr[0..1] receives the first and last ring pair holding a non-zero map row.
 // ring_live (optional): rings whose entry is 0 hold zeros in maps [0, nlive) and are not read.
-void launch_ring_analysis_tc(const Plan &p, const float2 *maps, int64_t nmaps, float2 *F, int *erow, int *nzr,
-                             cudaStream_t st, const int *ring_live = nullptr, int64_t nlive = 0,
-                             bool skip_unread = false);
+int launch_ring_analysis_tc(Plan &p, const float2 *maps, int64_t nmaps, float2 *F, int *erow, int *nzr,
+                            cudaStream_t st, const int *ring_live = nullptr, int64_t nlive = 0,
+                            bool skip_unread = false);
 uint2 dft_slices(double v, int EB);
 int64_t dft_image_offsets(const Plan &p, const std::vector<int32_t> &crings, const std::vector<int32_t> &coff,
                           bool with_polar, std::vector<int64_t> &off, int &max_nch);
