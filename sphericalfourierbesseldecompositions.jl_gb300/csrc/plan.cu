@@ -902,6 +902,9 @@ int sfb_plan_create(const sfb_plan_desc *d, sfb_plan **out) {
             if ((st = upload<int64_t>(p, &p.d_aimg_off, nullptr, coff.size())) != SFB_OK) break;
             // SFBGPU_DFT_AIMG=0: the DFT's producers slice the map rows themselves (no A image)
             if (const char *e = std::getenv("SFBGPU_DFT_AIMG")) p.dft_aimg = e[0] != '0';
+            // SFBGPU_DFT_POLAR_GATHER=1: with the A image, the polar classes gather their twiddles from
+            // the ring tables instead of the twiddle image (half the DRAM reads, measured slower)
+            if (const char *e = std::getenv("SFBGPU_DFT_POLAR_GATHER")) p.dft_polar_gather = e[0] != '0';
             // B operand image: the polar classes too while the whole image stays under
             // SFBGPU_DFT_IMAGE_MAX_BYTES (default 2 GiB; the equatorial classes are always imaged)
             {

@@ -729,9 +729,10 @@ int launch_ring_analysis_tc(Plan &p, const float2 *maps, int64_t nmaps, float2 *
     const int64_t eq_tiles = ((int64_t)p.eq_max_rings * nmaps + dft::NPAIR - 1) / dft::NPAIR;
     // A-operand image for the imaged launches: per-class chunk offsets for this map count, the
     // buffer, and the slicing pass (after the row exponents, on the call's stream)
-    // the polar rings gather their twiddles from the ring tables (L1-resident) while A arrives by bulk
-    // copy; their twiddle image is read only when the A image is off
-    const bool aimg_polar = p.dft_aimg && p.n_polar > 0;
+    // with the A image the polar rings take B from the twiddle image as well (SFBGPU_DFT_POLAR_GATHER:
+    // from the L1-resident ring tables, gathered by warps 4-7)
+    const bool aimg_polar = p.dft_aimg && p.n_polar > 0 && (p.dft_polar_gather || p.dtimg_polar);
+    const bool polar_img = p.dtimg_polar && !(aimg_polar && p.dft_polar_gather);
     const bool aimg_eq = p.dft_aimg && p.d_dtimg != nullptr && p.n_eq_cls > 0;
     if (aimg_polar || aimg_eq) {
         const int ncls = (int)p.h_cls_off.size() - 1;
@@ -800,7 +801,7 @@ int launch_ring_analysis_tc(Plan &p, const float2 *maps, int64_t nmaps, float2 *
     launch(dim3(ntn, (unsigned)eq_tiles, (unsigned)p.n_eq_cls), p.n_polar, p.d_dtimg != nullptr, aimg_eq, 0,
            two ? p.dft_side : st);
     if (p.n_polar > 0)
-        launch(dim3(ntn, mtiles, (unsigned)p.n_polar), 0, p.dtimg_polar && !aimg_polar, aimg_polar, 1, st);
+        launch(dim3(ntn, mtiles, (unsigned)p.n_polar), 0, polar_img, aimg_polar, 1, st);
     if (two) {
         cudaEventRecord(p.dft_join, p.dft_side);
         cudaStreamWaitEvent(st, p.dft_join, 0);
