@@ -105,22 +105,27 @@ def test_mixed_vs_fp64_partial_sky(zlim):
     assert e2 < MIXED_TOL and emax < MIXED_TOL
 
 
-def test_dft_twiddle_image_matches_gather(monkeypatch):
-    """The ring DFT takes its twiddle operand from the precomputed image, or,
-    for polar rings past the image budget, gathers it from the ring tables:
-    both feed the tensor cores the same slices, so the a_nlm agree to the
-    run-to-run rounding of the deposit."""
+@pytest.mark.parametrize("env,val,name", [("SFBGPU_DFT_IMAGE_MAX_BYTES", "0", "polar_twiddles_gathered"),
+                                          ("SFBGPU_DFT_AIMG", "0", "rows_sliced_in_producers"),
+                                          ("SFBGPU_DFT_POLAR_GATHER", "1", "polar_gather_with_a_image")])
+def test_dft_operand_feeds_agree(monkeypatch, env, val, name):
+    """The ring DFT takes its twiddle operand from the precomputed image and
+    its map rows from the A image written by the slicing pass; the variants
+    gather the polar twiddles from the ring tables (past the image budget, or
+    by choice beside the A image) or slice the map rows in the DFT's producer
+    warps.  All feed the tensor cores the same slices, so the a_nlm agree to
+    the run-to-run rounding of the deposit."""
     cfg = (0.05, 500.0, 1000.0, 32, 200_000, 8)
     a, rtp, w, win, nbar = _setup(*cfg)
     img = sfbgpu.cat2amln(rtp, a, nbar, win, w, precision="mixed")
-    monkeypatch.setenv("SFBGPU_DFT_IMAGE_MAX_BYTES", "0")
+    monkeypatch.setenv(env, val)
     b = sfbgpu.AnlmModes(*cfg[:3], nside=cfg[3])
-    gat = sfbgpu.cat2amln(rtp, b, nbar, win, w, precision="mixed")
+    alt = sfbgpu.cat2amln(rtp, b, nbar, win, w, precision="mixed")
     f64 = sfbgpu.cat2amln(rtp, a, nbar, win, w, precision="fp64")
-    e_ig = _errors(gat, img)[0]
-    record("dft_image_vs_gather", e_ig)
-    assert e_ig < 1e-9
-    assert _errors(gat, f64)[0] < MIXED_TOL and _errors(img, f64)[0] < MIXED_TOL
+    e_ia = _errors(alt, img)[0]
+    record(f"dft_default_vs_{name}", e_ia)
+    assert e_ia < 1e-9
+    assert _errors(alt, f64)[0] < MIXED_TOL and _errors(img, f64)[0] < MIXED_TOL
 
 
 def test_gram_refinement_matches_full_passes(monkeypatch):
