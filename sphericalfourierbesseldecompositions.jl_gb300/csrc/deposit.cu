@@ -621,6 +621,169 @@ __global__ void __launch_bounds__(128) k_deposit_moments_bal(const int32_t *__re
     for (int k = 0; k <= deg; ++k) base[(int64_t)k * npix] = out[k * 128 + t];
 }
 
+// Shared-memory accumulators for the balanced moments (the default): thread t
+// keeps the double-float sums of the bin it walks in column t of acc_s (one
+// float2 per degree) instead of 25 register pairs, so a thread needs 48
+// registers instead of 117 and twice the warps are resident to cover the
+// dependent loads (offsets -> records) and the recurrence's latency.  The accesses are explicit
+// shared-memory instructions (volatile asm), so the compiler cannot move the
+// sums back into registers.  The arithmetic is that of k_deposit_moments_bal
+// operation for operation, so both kernels write the same bits.
+__device__ __forceinline__ float2 lds2(uint32_t a) {
+    float2 v;
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a));
+    return v;
+}
+
+__device__ __forceinline__ void sts2(uint32_t a, float2 v) {
+    asm volatile("st.shared.v2.f32 [%0], {%1, %2};" ::"r"(a), "f"(v.x), "f"(v.y));
+}
+
+// column stride of acc_s between degrees: 128 float2
+constexpr uint32_t ACC_DEG_BYTES = 128 * 8;
+
+template <int K, int MAXDEG>
+__device__ __forceinline__ void leg_chain_sm(dfl x, dfl q0, dfl q1, uint32_t col, int deg) {
+    if constexpr (K < MAXDEG) {
+        if (K >= deg) return;
+        const uint32_t a = col + (K + 1) * ACC_DEG_BYTES;
+        const float2 s = lds2(a);
+        const dfl q2 = leg_step<K>(x, q1, q0);
+        const dfl r = dfs_add({s.x, s.y}, q2);
+        sts2(a, make_float2(r.hi, r.lo));
+        leg_chain_sm<K + 1, MAXDEG>(x, q1, q2, col, deg);
+    }
+}
+
+template <int MAXDEG>
+__device__ __forceinline__ void bin_moments_sm(const float4 *__restrict__ sorted, int64_t g0, int64_t g1, int deg,
+                                               uint32_t col) {
+#pragma unroll
+    for (int k = 0; k <= MAXDEG; ++k)
+        if (k <= deg) sts2(col + k * ACC_DEG_BYTES, make_float2(0.f, 0.f));
+    float4 nxt = g0 < g1 ? sorted[g0] : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int64_t g = g0; g < g1; ++g) {
+        const float4 v = nxt;
+        if (g + 1 < g1) nxt = sorted[g + 1];
+        const dfl x = {v.x, v.y};
+        const dfl q0 = {v.z, v.w}, q1 = dfs_mul(q0, x);
+        float2 s = lds2(col);
+        dfl r = dfs_add({s.x, s.y}, q0);
+        sts2(col, make_float2(r.hi, r.lo));
+        if (MAXDEG >= 1 && deg >= 1) {
+            s = lds2(col + ACC_DEG_BYTES);
+            r = dfs_add({s.x, s.y}, q1);
+            sts2(col + ACC_DEG_BYTES, make_float2(r.hi, r.lo));
+        }
+        leg_chain_sm<1, MAXDEG>(x, q0, q1, col, deg);
+    }
+}
+
+template <int MAXDEG>
+__global__ void __launch_bounds__(128, 8) k_deposit_moments_sm(const int32_t *__restrict__ offset,
+                                                               const float4 *__restrict__ sorted, int64_t npix,
+                                                               int pieces, int deg, int64_t nbasis,
+                                                               const float2 *__restrict__ cdf,
+                                                               const float2 *__restrict__ mudf,
+                                                               float2 *__restrict__ maps, int64_t nside,
+                                                               const int *__restrict__ ring_live) {
+    __shared__ int hist[64];
+    __shared__ int perm[128];
+    __shared__ __align__(16) float2 acc_s[(MAXDEG + 1) * 128];
+    const int t = threadIdx.x;
+    const int64_t nkeys = (int64_t)(pieces + 2) * npix;
+    const int64_t B0 = (int64_t)blockIdx.x * 128;
+    const int slot0 = (int)(B0 / npix);
+    const int64_t bnd = (int64_t)(slot0 + 1) * npix;
+    const int64_t bt = B0 + t;
+    const int cnt = bt < nkeys ? offset[bt + 1] - offset[bt] : 0;
+    bool busy = cnt != 0;
+    if (cdf && bt < nkeys) {
+        const int sl = bt < bnd ? slot0 : slot0 + 1;
+        busy = busy || cdf[bt - (int64_t)sl * npix].x != 0.f;
+    }
+    if (!__syncthreads_or(busy)) {
+        if (bt >= nkeys) return;
+        const int sl = bt < bnd ? slot0 : slot0 + 1;
+        const int64_t px = bt - (int64_t)sl * npix;
+        if (ring_live && !ring_live[ring_of_pixel(nside, px)]) return;
+        if (sl >= pieces) {
+            maps[(nbasis - 2 + (sl - pieces)) * npix + px] = make_float2(0.f, 0.f);
+            return;
+        }
+        float2 *z = maps + (int64_t)sl * (deg + 1) * npix + px;
+        for (int k = 0; k <= deg; ++k) z[(int64_t)k * npix] = make_float2(0.f, 0.f);
+        return;
+    }
+    if (t < 64) hist[t] = 0;
+    __syncthreads();
+    const int key = 63 - min(cnt, 63);                 // longest bins first
+    atomicAdd(&hist[key], 1);
+    __syncthreads();
+    if (t < 32) {
+        const int h0 = hist[2 * t], h1 = hist[2 * t + 1];
+        int sc = h0 + h1;
+        for (int off = 1; off < 32; off <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, sc, off);
+            if (t >= off) sc += v;
+        }
+        const int base = sc - (h0 + h1);
+        hist[2 * t] = base;
+        hist[2 * t + 1] = base + h0;
+    }
+    __syncthreads();
+    const int walker = atomicAdd(&hist[key], 1);       // the thread that walks this thread's bin
+    perm[walker] = t;
+    __syncthreads();
+    const uint32_t acc0 = (uint32_t)__cvta_generic_to_shared(acc_s);
+    {
+        const int64_t b = B0 + perm[t];
+        if (b < nkeys) {
+            const int slot = b < bnd ? slot0 : slot0 + 1;
+            const int64_t g0 = offset[b], g1 = offset[b + 1];
+            const uint32_t col = acc0 + t * 8;
+            if (slot >= pieces) {
+                dfl sw = {0.f, 0.f};
+                for (int64_t g = g0; g < g1; ++g) {
+                    const float4 v = sorted[g];
+                    sw = df_add(sw, {v.z, v.w});
+                }
+                sts2(col, make_float2(sw.hi, sw.lo));
+            } else {
+                bin_moments_sm<MAXDEG>(sorted, g0, g1, deg, col);
+            }
+        }
+    }
+    __syncthreads();
+    if (bt >= nkeys) return;
+    // thread t writes its own bin (consecutive threads on consecutive pixels) from the walker's column
+    const int slot = bt < bnd ? slot0 : slot0 + 1;
+    const int64_t pix = bt - (int64_t)slot * npix;
+    const uint32_t src = acc0 + walker * 8;
+    const float2 c = cdf ? cdf[pix] : make_float2(0.f, 0.f);
+    const dfl rv = {c.x, c.y};
+    auto fluct = [&](dfl a, int64_t bi) -> float2 {
+        if (cdf) {
+            const float2 m = mudf[bi];
+            a = dfs_add(a, df_neg(dfs_mul({m.x, m.y}, rv)));
+        }
+        a = df_renorm(a);
+        return make_float2(a.hi, a.lo);
+    };
+    if (slot >= pieces) {
+        const float2 s = lds2(src);
+        const int64_t b = nbasis - 2 + (slot - pieces);
+        maps[b * npix + pix] = fluct({s.x, s.y}, b);
+        return;
+    }
+    const int64_t bb = (int64_t)slot * (deg + 1);
+    float2 *base = maps + bb * npix + pix;
+    for (int k = 0; k <= deg; ++k) {
+        const float2 s = lds2(src + k * ACC_DEG_BYTES);
+        base[(int64_t)k * npix] = fluct(df_renorm({s.x, s.y}), bb + k);
+    }
+}
+
 constexpr int STATS_STRIDE = 32;
 
 // Sampled projections onto ref over the bins of every STATS_STRIDE-th group of
@@ -729,8 +892,12 @@ static void launch_moments(const Plan &p, const int32_t *counts, const void *sor
     bool done = false;
     if constexpr (MAXDEG <= 31) {
         if (p.precision == SFB_MIXED && p.npix >= 128) {
-            k_deposit_moments_bal<MAXDEG><<<blocks, 128, 0, st>>>(counts, s4, p.npix, p.pieces, p.degree, p.nbasis,
-                                                                  cdf, mudf, mf, p.nside, ring_live);
+            if (p.moments_smem)
+                k_deposit_moments_sm<MAXDEG><<<blocks, 128, 0, st>>>(counts, s4, p.npix, p.pieces, p.degree,
+                                                                     p.nbasis, cdf, mudf, mf, p.nside, ring_live);
+            else
+                k_deposit_moments_bal<MAXDEG><<<blocks, 128, 0, st>>>(counts, s4, p.npix, p.pieces, p.degree,
+                                                                      p.nbasis, cdf, mudf, mf, p.nside, ring_live);
             done = true;
         }
     }

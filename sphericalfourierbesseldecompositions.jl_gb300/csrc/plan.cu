@@ -729,6 +729,8 @@ int sfb_plan_create(const sfb_plan_desc *d, sfb_plan **out) {
     p.niter = d->niter;
     p.precision = d->precision;
     p.radial_mode = d->radial_mode;
+    // SFBGPU_MOMENTS_SMEM=0: the mixed deposit's moments sum in registers (same bits, fewer resident warps)
+    if (const char *e = std::getenv("SFBGPU_MOMENTS_SMEM")) p.moments_smem = e[0] != '0';
     p.lmsize = lmsize_of(p.lmax);
     // pairs and output tables
     std::vector<int32_t> pair_n, pair_l, out_pair, out_lm, pair_index((size_t)p.nmax * (p.lmax + 1), -1);

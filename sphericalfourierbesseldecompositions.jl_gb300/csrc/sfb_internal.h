@@ -128,7 +128,8 @@ struct Plan {
     // of every live tile, bulk-copied by the DFT) with its per-class chunk offsets for aimg_nmaps maps
     std::vector<int32_t> h_cls_rings, h_cls_off;
     bool dft_aimg = true;
-    bool dft_polar_gather = false;  // polar classes gather their twiddles (else the twiddle image)
+    bool dft_polar_gather = false;
+    bool moments_smem = true;       // mixed deposit moments with shared-memory accumulators  // polar classes gather their twiddles (else the twiddle image)
     DevBuf<double> aimg;
     int64_t *d_aimg_off = nullptr;
     std::vector<int64_t> h_aimg_off;

@@ -107,14 +107,16 @@ def test_mixed_vs_fp64_partial_sky(zlim):
 
 @pytest.mark.parametrize("env,val,name", [("SFBGPU_DFT_IMAGE_MAX_BYTES", "0", "polar_twiddles_gathered"),
                                           ("SFBGPU_DFT_AIMG", "0", "rows_sliced_in_producers"),
-                                          ("SFBGPU_DFT_POLAR_GATHER", "1", "polar_gather_with_a_image")])
-def test_dft_operand_feeds_agree(monkeypatch, env, val, name):
+                                          ("SFBGPU_DFT_POLAR_GATHER", "1", "polar_gather_with_a_image"),
+                                          ("SFBGPU_MOMENTS_SMEM", "0", "moments_in_registers")])
+def test_kernel_variants_agree(monkeypatch, env, val, name):
     """The ring DFT takes its twiddle operand from the precomputed image and
     its map rows from the A image written by the slicing pass; the variants
     gather the polar twiddles from the ring tables (past the image budget, or
     by choice beside the A image) or slice the map rows in the DFT's producer
-    warps.  All feed the tensor cores the same slices, so the a_nlm agree to
-    the run-to-run rounding of the deposit."""
+    warps, and the deposit's moments sum in registers or in shared memory.
+    All do the same arithmetic, so the a_nlm agree to the run-to-run rounding
+    of the deposit (the order of the galaxies within a bin)."""
     cfg = (0.05, 500.0, 1000.0, 32, 200_000, 8)
     a, rtp, w, win, nbar = _setup(*cfg)
     img = sfbgpu.cat2amln(rtp, a, nbar, win, w, precision="mixed")
