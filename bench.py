@@ -88,6 +88,37 @@ def make_catalogue(seed=2):
     return np.ascontiguousarray(np.stack([r, th, ph], axis=1)), w    # (N, 3) = Julia 3xN memory
 
 
+def mock_sizes(nmocks, seed=7, lo=1_000_000, hi=20_000_000):
+    """Uneven mock sizes, uniform integers in [lo, hi] (the batched-mocks configuration)."""
+    return np.random.default_rng(seed).integers(lo, hi + 1, nmocks)
+
+
+def fill_mocks(sizes, gal, w, seed=8):
+    """Independent seeded mocks of the bench window written into gal (sum(sizes), 3) and w: r by the
+    inverse CDF of r^2 exp(-(r - RMEAN)^2 / 2 RSIG^2) on [RMIN, RMAX] (tabulated at 2^16 equally spaced
+    probabilities, linear between them), cos(theta) uniform in the cap, phi uniform, w ~ U[0.5, 1.5].
+    Returns the offsets (nmocks + 1)."""
+    rg = np.linspace(RMIN, RMAX, 1 << 18)
+    pdf = rg * rg * np.exp(-(rg - RMEAN) ** 2 / (2 * RSIG ** 2))
+    cdf = np.concatenate([[0.0], np.cumsum(0.5 * (pdf[1:] + pdf[:-1]) * np.diff(rg))])
+    cdf /= cdf[-1]
+    nq = 1 << 16
+    rq = np.interp(np.linspace(0.0, 1.0, nq + 1), cdf, rg)          # r at probabilities j / nq
+    off = np.zeros(len(sizes) + 1, np.int64)
+    off[1:] = np.cumsum(sizes)
+    z0 = np.cos(np.radians(CAP_DEG))
+    for k, n in enumerate(sizes):
+        rng = np.random.default_rng([seed, k])
+        a, b = off[k], off[k + 1]
+        q = rng.random(n) * nq
+        j = np.minimum(q.astype(np.int64), nq - 1)
+        gal[a:b, 0] = rq[j] + (q - j) * (rq[j + 1] - rq[j])
+        gal[a:b, 1] = np.arccos(rng.uniform(z0, 1.0, n))
+        gal[a:b, 2] = rng.uniform(0.0, 2 * np.pi, n)
+        w[a:b] = rng.uniform(0.5, 1.5, n)
+    return off
+
+
 # the reference's CPU-runnable configuration: full sky, r ~ r^2, unit weights
 C1 = dict(kmax=0.05, rmin=500.0, rmax=1000.0, nside=32, nr=250, ngal=200_000)
 C1_WORKLOAD = "cat2amln kmax=0.05 rmin=500 rmax=1000 nside=32 nr=250 N=2e5 full sky r~r^2 w=1 (C1)"
@@ -514,6 +545,65 @@ def aggregate_replicas(ms, ngal, world, device=None):
     return ms, ngal, ngal / (ms * 1e-3)
 
 
+def batched_mocks_bench(args, sfbgpu, capi, torch, plan, mask, wln, veff, nlmsize):
+    """Batched mocks: M independent seeded catalogues of the bench window, sizes uniform in [1e6, 2e7],
+    concatenated in pinned host memory and transformed by one sfb_cat2amln_batched call (host buffers,
+    the catalogue copies and result copies inside the timed call).  Prints one JSON line: galaxies/s over
+    the timed calls, the per-mock time, and the largest relative difference between a mock's row and the
+    single-catalogue call on the same mock (first and last mock)."""
+    sizes = mock_sizes(args.batched_mocks)
+    ntot = int(sizes.sum())
+    h_gal = torch.empty((ntot, 3), dtype=torch.float64).pin_memory()
+    h_w = torch.empty(ntot, dtype=torch.float64).pin_memory()
+    t0 = time.perf_counter()
+    off = fill_mocks(sizes, h_gal.numpy(), h_w.numpy())
+    t_gen = time.perf_counter() - t0
+    nbars = np.ascontiguousarray(sizes / veff, dtype=np.float64)
+    h_mask = torch.from_numpy(mask).pin_memory()
+    h_wln = torch.from_numpy(np.ascontiguousarray(wln.T)).pin_memory()
+    out = torch.empty((len(sizes), 2 * nlmsize), dtype=torch.float64).pin_memory()
+    hwin = capi.Window()
+    hwin.kind = capi.SFB_WINDOW_SEPARABLE
+    hwin.mask = capi.C.cast(h_mask.data_ptr(), capi._dp)
+    hwin.w_ln = capi.C.cast(h_wln.data_ptr(), capi._dp)
+
+    def call():
+        capi.check(capi.lib.sfb_cat2amln_batched(plan.handle, capi.C.c_void_p(h_gal.data_ptr()),
+                                                 capi.C.c_void_p(h_w.data_ptr()), capi.C.c_void_p(off.ctypes.data),
+                                                 len(sizes), capi.C.c_void_p(nbars.ctypes.data),
+                                                 capi.C.byref(hwin), capi.C.c_void_p(out.data_ptr())))
+
+    call()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(args.batched_repeats):
+        t0 = time.perf_counter()
+        call()
+        ts.append(time.perf_counter() - t0)
+    t = float(np.median(ts))
+    res = out.numpy()
+    diffs = []
+    for k in (0, len(sizes) - 1):
+        a, b = int(off[k]), int(off[k + 1])
+        single = np.empty(2 * nlmsize)
+        capi.check(capi.lib.sfb_cat2amln(plan.handle, capi.C.c_void_p(h_gal[a:b].data_ptr()),
+                                         capi.C.c_void_p(h_w[a:b].data_ptr()), b - a, float(nbars[k]),
+                                         capi.C.byref(hwin), capi.C.c_void_p(single.ctypes.data)))
+        diffs.append(float(np.max(np.abs(res[k] - single)) / np.max(np.abs(single))))
+    line = {"metric": "batched cat2amln galaxies/s (mixed)", "value": ntot / t, "unit": "galaxies/s",
+            "higher_is_better": True, "mocks": int(len(sizes)), "galaxies": ntot,
+            "sizes": {"min": int(sizes.min()), "max": int(sizes.max()), "mean": float(sizes.mean())},
+            "s_per_batch": t, "ms_per_mock": t / len(sizes) * 1e3, "repeats": args.batched_repeats,
+            "timing": "host wall clock of one sfb_cat2amln_batched call (median of the repeats after one "
+                      "warm-up): pinned host catalogues, their copies and the a_nlm copies inside",
+            "h2d_bytes_per_batch": int(32 * ntot), "d2h_bytes_per_batch": int(16 * nlmsize * len(sizes)),
+            "rows_vs_single_calls_max_rel_diff": max(diffs), "generation_s": t_gen,
+            "config": {"workload": f"{len(sizes)} independent seeded mocks of the bench window (cap 60 x "
+                                   "gauss(1500,400), w~U[0.5,1.5]), sizes uniform in [1e6, 2e7], kmax=0.1 "
+                                   "nside=256, mixed precision", "data": "synthetic"}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -530,6 +620,10 @@ def main():
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu captures: same geometry, 2 radial pieces x degree 15 (34 maps), "
                          "1e6 galaxies, no e2e / CPU baseline")
+    ap.add_argument("--batched-mocks", type=int, default=0,
+                    help="time sfb_cat2amln_batched on this many seeded mocks of the bench window with sizes "
+                         "uniform in [1e6, 2e7] (pinned host buffers), instead of the single-catalogue bench")
+    ap.add_argument("--batched-repeats", type=int, default=4, help="timed batched calls (after one warm-up)")
     ap.add_argument("--full-basis", action="store_true",
                     help="with --profile-case: the bench's own radial basis (328 maps) with the profile case's "
                          "galaxy count, for per-kernel DRAM traffic captures")
@@ -615,6 +709,10 @@ def main():
     win.mask = capi.C.cast(d_mask.data_ptr(), capi._dp)
     win.w_ln = capi.C.cast(d_wln.data_ptr(), capi._dp)
     stream = torch.cuda.current_stream(dev)
+    if args.batched_mocks:
+        if rank == 0:
+            batched_mocks_bench(args, sfbgpu, capi, torch, plan, mask, wln, veff, nlmsize)
+        return
 
     def step():
         capi.check(capi.lib.sfb_cat2amln_device(plan.handle, capi.C.c_void_p(d_gal.data_ptr()),
