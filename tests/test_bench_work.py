@@ -77,3 +77,29 @@ def test_stage_work_counts_the_rings_with_data():
     # the FP64 path computes every ring: the sky does not change its counts
     assert b.stage_work("deposit", "fp64", nm, ngal, nbasis, sky=sky) == b.stage_work("deposit", "fp64", nm, ngal,
                                                                                        nbasis)
+
+
+def test_batched_mock_generator():
+    """The batched-mocks bench: uneven sizes in [1e6, 2e7], offsets over the concatenation, every
+    mock inside the window's support (cap and radial range), independent seeds per mock, and the
+    inverse-CDF radial draw matching the rejection sampler of the single-catalogue bench."""
+    b = _bench()
+    sizes = b.mock_sizes(64)
+    assert sizes.min() >= 1_000_000 and sizes.max() <= 20_000_000 and len(np.unique(sizes)) > 60
+    small = np.array([20_000, 0, 50_000, 7])
+    gal = np.full((small.sum(), 3), np.nan)
+    w = np.full(small.sum(), np.nan)
+    off = b.fill_mocks(small, gal, w)
+    assert list(off) == [0, 20_000, 20_000, 70_000, 70_007]
+    assert np.all(np.isfinite(gal)) and np.all(np.isfinite(w))
+    assert gal[:, 0].min() >= b.RMIN and gal[:, 0].max() <= b.RMAX
+    assert gal[:, 1].max() <= np.radians(b.CAP_DEG) + 1e-12 and gal[:, 1].min() >= 0.0
+    assert np.all((gal[:, 2] >= 0) & (gal[:, 2] < 2 * np.pi)) and np.all((w >= 0.5) & (w < 1.5))
+    assert not np.allclose(gal[:7, 0], gal[20_000:20_007, 0])
+    # radial distribution against the rejection sampler (histogram within Poisson noise)
+    b.NGAL_MEAN = 200_000
+    ref, _ = b.make_catalogue(seed=5)
+    edges = np.linspace(b.RMIN, b.RMAX, 9)
+    h1 = np.histogram(gal[20_000:70_000, 0], edges)[0] / 50_000
+    h2 = np.histogram(ref[:, 0], edges)[0] / ref.shape[0]
+    assert np.all(np.abs(h1 - h2) < 5 * np.sqrt(h2 / 50_000) + 1e-3)
