@@ -734,6 +734,11 @@ int launch_ring_analysis_tc(Plan &p, const float2 *maps, int64_t nmaps, float2 *
     const bool aimg_polar = p.dft_aimg && p.n_polar > 0 && (p.dft_polar_gather || p.dtimg_polar);
     const bool polar_img = p.dtimg_polar && !(aimg_polar && p.dft_polar_gather);
     const bool aimg_eq = p.dft_aimg && p.d_dtimg != nullptr && p.n_eq_cls > 0;
+    // the equatorial classes (equal CTAs, a partly filled last wave) run on the second stream beside
+    // the polar rings (longest first), each class group's slicing pass directly before its DFT, so
+    // the slicing of one group overlaps the DFT of the other and the tail of each launch the other
+    const bool two = p.dft_side && p.n_polar > 0;
+    cudaStream_t st_eq = two ? p.dft_side : st;
     if (aimg_polar || aimg_eq) {
         const int ncls = (int)p.h_cls_off.size() - 1;
         if (p.aimg_nmaps != nmaps) {
@@ -752,6 +757,13 @@ int launch_ring_analysis_tc(Plan &p, const float2 *maps, int64_t nmaps, float2 *
             p.aimg_nmaps = nmaps;
         }
         SFB_TRY(grow(p, p.aimg, (size_t)(p.h_aimg_off[ncls] * (4 * dft::PLANE) / sizeof(double))));
+    }
+    if (two) {
+        // after the row exponents, the offsets upload and the image's allocation on the call's stream
+        cudaEventRecord(p.dft_fork, st);
+        cudaStreamWaitEvent(p.dft_side, p.dft_fork, 0);
+    }
+    if (aimg_polar || aimg_eq) {
         unsigned char *aimg = reinterpret_cast<unsigned char *>(p.aimg.ptr);
         // chunk groups: the longest ring (4 nside pixels) in groups of SLICE_CPG chunks
         const unsigned ngrp = (unsigned)((4 * p.nside + dft::KC * dft::SLICE_CPG - 1) / (dft::KC * dft::SLICE_CPG));
@@ -761,7 +773,7 @@ int launch_ring_analysis_tc(Plan &p, const float2 *maps, int64_t nmaps, float2 *
             note_launch();
         }
         if (aimg_eq) {
-            dft::k_dft_slice_a<<<dim3((unsigned)eq_tiles, (unsigned)p.n_eq_cls, ngrp), dft::NPROD, 0, st>>>(
+            dft::k_dft_slice_a<<<dim3((unsigned)eq_tiles, (unsigned)p.n_eq_cls, ngrp), dft::NPROD, 0, st_eq>>>(
                 maps, p.npix, nmaps, p.d_rings, (int)p.nrn, p.d_cls_rings, p.d_cls_off + p.n_polar, erow,
                 p.d_aimg_off + p.n_polar, aimg);
             note_launch();
@@ -791,15 +803,8 @@ int launch_ring_analysis_tc(Plan &p, const float2 *maps, int64_t nmaps, float2 *
                 p.d_err);
         note_launch();
     };
-    // the equatorial classes (equal CTAs, a partly filled last wave) run on the second stream beside
-    // the polar rings (longest first), so the tail of each launch overlaps the other
-    const bool two = p.dft_side && p.n_polar > 0;
-    if (two) {
-        cudaEventRecord(p.dft_fork, st);
-        cudaStreamWaitEvent(p.dft_side, p.dft_fork, 0);
-    }
     launch(dim3(ntn, (unsigned)eq_tiles, (unsigned)p.n_eq_cls), p.n_polar, p.d_dtimg != nullptr, aimg_eq, 0,
-           two ? p.dft_side : st);
+           st_eq);
     if (p.n_polar > 0)
         launch(dim3(ntn, mtiles, (unsigned)p.n_polar), 0, polar_img, aimg_polar, 1, st);
     if (two) {
