@@ -3,7 +3,9 @@
 #
 # Drop-in replacements for SFB.cat2amln / SFB.cat2nlm, SFB.field2anlm,
 # SFB.anlm2field and SFB.win_rhat_ln (reference src/cat2anlm.jl:257-422,
-# src/windows.jl:244-270) with the same argument meaning.  The device plan is
+# src/windows.jl:244-270) with the same argument meaning, and for the window
+# helpers SFB.apply_window, SFB.win_lnn, SFB.calc_wmix, SFB.amln2clnn and
+# SFB.winweights2galweights.  The device plan is
 # built once per AnlmModes (its k_nl, spline tables and ordering) and freed by
 # a finalizer.  Errors map to the exceptions the reference raises.
 #
@@ -228,6 +230,43 @@ function amln2clnn(anlm, cmodes; kw...)
                                         Ptr{Float64}),
                                        p.handle, a, C_NULL, nbatch, lnn, nlnn, out))
     return nbatch == 1 ? vec(out) : out
+end
+
+"""
+    win_lnn(win, wmodes, cmodes)    (src/windows.jl:382-392)
+
+W_l(n, n') = Σ_s r_s² Δr g_nl(r_s) g_n'l(r_s) W_00(r_s) / √(4π) for every column
+(l, n, n') of `cmodes.lnn`, with W_00 the shell a_00 of the window at 2 lmax (the
+reference's `calc_Wr_lm(win, 2 lmax, nside)`).  `win` is the nr × npix window at
+the plan's nside (a `SeparableArray` is materialised with `Matrix`).
+"""
+function win_lnn(win, wmodes, cmodes; kw...)
+    p = getplan(cmodes.amodesA; kw...)
+    W = Matrix{Float64}(win)
+    lnn = Matrix{Int64}(cmodes.lnn)
+    nlnn = size(lnn, 2)
+    out = Vector{Float64}(undef, nlnn)
+    GC.@preserve W lnn out check(ccall((:sfb_win_lnn, libsfb), Cint,
+                                       (Ptr{Cvoid}, Ptr{Float64}, Int64, Float64, Float64, Ptr{Int64}, Int64,
+                                        Ptr{Float64}),
+                                       p.handle, W, wmodes.nr, wmodes.rmin, wmodes.rmax, lnn, nlnn, out))
+    return out
+end
+
+"""
+    calc_wmix(win, wmodes, amodes; neg_m=false)    (src/windows.jl:299-366)
+
+The window mixing matrix W[(n l m), (n' l' m')] in `getidx` order on both axes,
+an nlmsize × nlmsize `Matrix{ComplexF64}` (lmax ≤ 128).  `win` as in `win_lnn`.
+"""
+function calc_wmix(win, wmodes, amodes; neg_m=false, kw...)
+    p = getplan(amodes; kw...)
+    W = Matrix{Float64}(win)
+    out = Matrix{ComplexF64}(undef, p.nlmsize, p.nlmsize)
+    GC.@preserve W out check(ccall((:sfb_calc_wmix, libsfb), Cint,
+                                   (Ptr{Cvoid}, Ptr{Float64}, Int64, Float64, Float64, Int32, Ptr{ComplexF64}),
+                                   p.handle, W, wmodes.nr, wmodes.rmin, wmodes.rmax, Int32(neg_m), out))
+    return out
 end
 
 """

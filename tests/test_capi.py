@@ -96,3 +96,65 @@ def test_last_error_truncates():
     buf = C.create_string_buffer(8)
     assert capi.lib.sfb_last_error(buf, 8) == capi.SFB_OK
     assert len(buf.value) <= 7
+
+
+def _julia_ccalls():
+    """(symbol, return type, argument types) of every ccall in the Julia binding."""
+    src = open(os.path.join(ROOT, "sphericalfourierbesseldecompositions.jl_gb300", "julia", "SFBGPU.jl")).read()
+    out = []
+    for m in re.finditer(r"ccall\(\(:(\w+),\s*libsfb\),\s*(\w+),\s*\(", src):
+        i, depth, args, cur = m.end(), 1, [], ""
+        while depth:
+            ch = src[i]
+            if ch in "({":
+                depth += 1
+            elif ch in ")}":
+                depth -= 1
+            if depth == 1 and ch == ",":
+                args.append(cur.strip())
+                cur = ""
+            elif depth:
+                cur += ch
+            i += 1
+        if cur.strip():
+            args.append(cur.strip())
+        out.append((m.group(1), m.group(2), args))
+    return out
+
+
+def _header_params():
+    """Parameter lists of the header's functions, each parameter classified as 'ptr' or its C type."""
+    hdr = open(os.path.join(ROOT, "include", "sfb_gpu.h")).read()
+    hdr = re.sub(r"/\*.*?\*/", "", hdr, flags=re.S)
+    hdr = re.sub(r"//[^\n]*", "", hdr)
+    decls = {}
+    for m in re.finditer(r"\b(int|void|int64_t)\s+(sfb_\w+)\s*\(([^)]*)\)\s*;", hdr):
+        params = [p.strip() for p in m.group(3).split(",") if p.strip() and p.strip() != "void"]
+        kinds = []
+        for p in params:
+            if "*" in p:
+                kinds.append("ptr")
+            else:
+                kinds.append(" ".join(p.replace("const ", "").split()[:-1]))
+        decls[m.group(2)] = (m.group(1), kinds)
+    return decls
+
+
+JULIA_TO_C = {"Int64": "int64_t", "Float64": "double", "Int32": "int32_t", "Cint": "int", "UInt64": "uint64_t",
+              "Csize_t": "size_t"}
+
+
+def test_julia_binding_matches_header():
+    """Every ccall of the Julia binding names a function the header declares, with as many arguments, each
+    of the matching kind (pointers as Ptr/Ref, integers and doubles by width), and the same return type."""
+    decls = _header_params()
+    calls = _julia_ccalls()
+    assert len(calls) >= 14
+    for name, ret, args in calls:
+        assert name in decls, name
+        cret, kinds = decls[name]
+        assert {"Cint": "int", "Cvoid": "void", "Int64": "int64_t"}[ret] == cret, name
+        assert len(args) == len(kinds), (name, args, kinds)
+        for a, k in zip(args, kinds):
+            jk = "ptr" if a.startswith(("Ptr{", "Ref{")) else JULIA_TO_C[a]
+            assert jk == k, (name, a, k)
