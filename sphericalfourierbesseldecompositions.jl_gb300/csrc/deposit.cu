@@ -625,10 +625,11 @@ __global__ void __launch_bounds__(128) k_deposit_moments_bal(const int32_t *__re
 // keeps the double-float sums of the bin it walks in column t of acc_s (one
 // float2 per degree) instead of 25 register pairs, so a thread needs 48
 // registers instead of 117 and twice the warps are resident to cover the
-// dependent loads (offsets -> records) and the recurrence's latency.  The accesses are explicit
-// shared-memory instructions (volatile asm), so the compiler cannot move the
-// sums back into registers.  The arithmetic is that of k_deposit_moments_bal
-// operation for operation, so both kernels write the same bits.
+// dependent loads (offsets -> records) and the recurrence's latency.  The
+// accesses are explicit shared-memory instructions (volatile asm), so the
+// compiler cannot move the sums back into registers.  The arithmetic is that
+// of k_deposit_moments_bal operation for operation: for the same order of the
+// galaxies within each bin both kernels write the same bits.
 __device__ __forceinline__ float2 lds2(uint32_t a) {
     float2 v;
     asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a));
