@@ -103,3 +103,69 @@ def test_batched_mock_generator():
     h1 = np.histogram(gal[20_000:70_000, 0], edges)[0] / 50_000
     h2 = np.histogram(ref[:, 0], edges)[0] / ref.shape[0]
     assert np.all(np.abs(h1 - h2) < 5 * np.sqrt(h2 / 50_000) + 1e-3)
+
+
+class _FakeTensor:
+    """Host stand-in for the pinned torch tensors of the batched extra (no device here)."""
+
+    def __init__(self, a):
+        self.a = a
+
+    def pin_memory(self):
+        return self
+
+    def numpy(self):
+        return self.a
+
+    def data_ptr(self):
+        return self.a.ctypes.data
+
+    def __getitem__(self, sl):
+        return _FakeTensor(self.a[sl])
+
+
+def test_batched_extra_plumbing():
+    """batched_mocks_bench on the host with a stand-in library: every mock reaches the batched call with
+    its offsets and n-bar, the per-mock rows come back in order, and the single-call comparison reads
+    the same galaxies (pointer arithmetic of the row slices)."""
+    import ctypes as C
+    b = _bench()
+    from sfbgpu import _capi as capi
+    nlm = 5
+
+    def as_arr(ptr, n):
+        return np.ctypeslib.as_array(C.cast(ptr.value, C.POINTER(C.c_double)), (n,))
+
+    def signature(gal, w, nbar):
+        # a row that depends on every galaxy of the mock: sums of r, w and r*w, scaled by 1/nbar
+        s = np.array([gal[:, 0].sum(), w.sum(), (gal[:, 0] * w).sum(), len(w), 1.0 / nbar])
+        return np.stack([s, -s], axis=1).ravel()
+
+    class Lib:
+        def sfb_cat2amln_batched(self, h, gp, wp, op, nm, nbp, win, outp):
+            off = np.ctypeslib.as_array(C.cast(op.value, C.POINTER(C.c_int64)), (nm + 1,))
+            nb = as_arr(nbp, nm)
+            gal = as_arr(gp, 3 * off[-1]).reshape(-1, 3)
+            w = as_arr(wp, off[-1])
+            out = as_arr(outp, nm * 2 * nlm).reshape(nm, 2 * nlm)
+            for k in range(nm):
+                out[k] = signature(gal[off[k]:off[k + 1]], w[off[k]:off[k + 1]], nb[k])
+            return 0
+
+        def sfb_cat2amln(self, h, gp, wp, n, nbar, win, outp):
+            out = np.ctypeslib.as_array(C.cast(outp.value, C.POINTER(C.c_double)), (2 * nlm,))
+            out[:] = signature(as_arr(gp, 3 * n).reshape(-1, 3), as_arr(wp, n), nbar)
+            return 0
+
+    fake_capi = types.SimpleNamespace(lib=Lib(), check=capi.check, Window=capi.Window, C=C, _dp=capi._dp,
+                                      SFB_WINDOW_SEPARABLE=capi.SFB_WINDOW_SEPARABLE)
+    fake_torch = types.SimpleNamespace(
+        float64=np.float64, cuda=types.SimpleNamespace(synchronize=lambda: None),
+        empty=lambda shape, dtype=None: _FakeTensor(np.empty(shape, np.float64)),
+        from_numpy=lambda a: _FakeTensor(a))
+    b.mock_sizes = lambda n, seed=7: np.array([3000, 1000, 2500])[:n]
+    plan = types.SimpleNamespace(handle=None)
+    rec = b.batched_mocks_bench(3, 2, fake_capi, fake_torch, plan, np.ones(12), np.ones((2, 3)), 10.0, nlm)
+    assert rec["mocks"] == 3 and rec["galaxies"] == 6500 and rec["repeats"] == 2
+    assert rec["rows_vs_single_calls_max_rel_diff"] == 0.0
+    assert rec["h2d_bytes_per_batch"] == 32 * 6500 and rec["d2h_bytes_per_batch"] == 16 * nlm * 3
