@@ -1467,7 +1467,8 @@ static int sfb_field2anlm_impl(sfb_plan *h, const void *f, int32_t dtype, int64_
             SFB_CUDA_TRY(cudaMemcpy2DAsync(d_f, nsc * es, static_cast<const char *>(f) + s0 * es, nr * es, nsc * es,
                                            p.npix, cudaMemcpyHostToDevice, st));
         const int64_t ld = resident ? nr : nsc, off = resident ? s0 : 0;
-        // maps[s][p] = f[s0+s + nr p]: FP32 maps straight from an FP32 field in mixed precision, else FP64
+        // maps[s][p] = f[s0+s + nr p]: double-float maps (lo = 0) straight from an FP32 field in mixed
+        // precision, else FP64
         bool maps64 = true;
         if (dtype == SFB_F32) {
             const float *src = reinterpret_cast<const float *>(d_f) + off;

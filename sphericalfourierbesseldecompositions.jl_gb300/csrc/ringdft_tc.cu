@@ -1,4 +1,5 @@
-// Ring Fourier analysis of FP32 maps on the tensor cores (mixed precision).
+// Ring Fourier analysis of double-float maps on the tensor cores (mixed
+// precision).
 //
 // For m <= lmax the ring transform is a matrix product: with rows q = (ring,
 // map) of one ring class (all rings of equal length n and phase type) and
@@ -35,11 +36,13 @@
 //
 // Tiles: M = 128 rows = 64 (ring, map) pairs x {north, south} (TMEM lanes
 // 0-63 north, 64-127 south), N = 128 accumulator columns (64 m values x
-// {cos, -sin}), K in chunks of 32 pixels.  The CTA builds the sliced A
-// planes and the B planes (gathered from the ring's sliced table) in shared
-// memory, double-buffered, with the next chunk's map values prefetched into
-// registers while the tensor cores work.  TMEM holds the four level
-// accumulators (4 x 128 columns).  Every mbarrier wait is bounded; on timeout
+// {cos, -sin}), K in chunks of 32 pixels, three shared-memory stages.  By
+// default both operands arrive by cp.async.bulk in the core-matrix layout
+// the MMAs read: A from the image k_dft_slice_a writes each call (the sliced
+// map rows), B from the twiddle image built with the plan.  The variants
+// slice A in the producer warps (the map values of the next chunk prefetched
+// into registers) or gather B from the ring's sliced table.  TMEM holds the
+// four level accumulators (4 x 128 columns).  Every mbarrier wait is bounded; on timeout
 // the CTA records ERR_TC_TIMEOUT, waits for its MMAs (bounded again),
 // releases TMEM and returns.
 //
