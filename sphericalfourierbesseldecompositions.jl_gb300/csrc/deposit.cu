@@ -10,9 +10,10 @@
 //   2. scan:    exclusive prefix sum of the (pieces + 2) * npix counters;
 //   3. scatter: (x, w) to its sorted position;
 //   4. moments: one thread per (slot, pixel) sums w P_k(x) over its galaxies
-//               in registers and writes every basis map element exactly once
-//               (coalesced over consecutive pixels; empty bins write zeros,
-//               so the maps need no clearing).
+//               (mixed precision: in its own shared-memory column) and every
+//               basis map element is written exactly once (coalesced over
+//               consecutive pixels; empty bins write zeros, so the maps need
+//               no clearing).
 // Summation order inside a bin follows the int-atomic ranks, so repeated
 // calls agree to rounding, not bit for bit.
 //
