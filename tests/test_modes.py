@@ -18,6 +18,44 @@ def test_knl_rmin0_golden():
     assert np.allclose(a.knl, GOLD["knl_rmin0_rmax1000"], rtol=1e-9, atol=0)
 
 
+def _boundary_det(l, k, rmin, rmax):
+    """Potential-boundary condition as a 2 x 2 determinant of spherical Bessel functions (scipy's
+    spherical_jn / spherical_yn, not the Bessel-J/Y form the root search uses): g' - l g / r = 0 at
+    rmin and g' + (l + 1) g / r = 0 at rmax for g = c j_l(kr) + d y_l(kr), i.e.
+    j_{l-1}(k rmax) y_{l+1}(k rmin) - j_{l+1}(k rmin) y_{l-1}(k rmax) = 0 (j_{-1} = cos x / x,
+    y_{-1} = sin x / x)."""
+    from scipy.special import spherical_jn, spherical_yn
+    xa, xb = k * rmin, k * rmax
+    with np.errstate(all="ignore"):
+        jm = np.cos(xb) / xb if l == 0 else spherical_jn(l - 1, xb)
+        ym = np.sin(xb) / xb if l == 0 else spherical_yn(l - 1, xb)
+        return jm * spherical_yn(l + 1, xa) - spherical_jn(l + 1, xa) * ym
+
+
+@pytest.mark.parametrize("kmax,rmin,rmax,lstep,npts", [(0.05, 500.0, 1000.0, 1, 100001),
+                                                      (0.1, 500.0, 2500.0, 19, 40001)])
+def test_knl_are_all_boundary_roots_below_kmax(kmax, rmin, rmax, lstep, npts):
+    """The modes the scan-and-secant search selects are exactly the roots of the boundary determinant
+    in (0, kmax], found independently (sign changes on a fine k grid, then Brent): same count for
+    every l checked (no root missed or added) and the same values to 1e-9 (C1 geometry: every l;
+    the bench geometry: every 19th l)."""
+    from scipy.optimize import brentq
+    a = sfbgpu.AnlmModes(kmax, rmin, rmax, cache=False)
+    k = np.linspace(1e-4, kmax, npts)
+    for l in range(0, a.lmax + 1, lstep):
+        d = _boundary_det(l, k, rmin, rmax)
+        ok = np.isfinite(d)
+        kk, sg = k[ok], np.sign(d[ok])
+        idx = np.nonzero(sg[:-1] * sg[1:] < 0)[0]
+        roots = np.array([brentq(lambda q: _boundary_det(l, q, rmin, rmax), kk[i], kk[i + 1], xtol=1e-15,
+                                 rtol=1e-14) for i in idx])
+        got = a.knl[:, l]
+        got = got[np.isfinite(got)]
+        assert len(got) == len(roots) == int(a.nmax_l[l]), (l, len(got), len(roots))
+        if len(roots):
+            assert np.max(np.abs(got - roots) / roots) < 1e-9, l
+
+
 def test_modes_structure_and_index_bijection():
     """reference test/test_modes.jl:13-37."""
     m = sfbgpu.AnlmModes(0.01, 100.0, 10000.0, cache=False)
